@@ -1,0 +1,336 @@
+"""Benchmark: CLV pattern-node updates/s of the pruning likelihood on GB300.
+
+Workload (one "step"): one full post-order lnL of a 128-taxon Yule tree
+(branch lengths Exp(mean 0.05)) over 100,000 sites simulated under
+GTR+Gamma4 (alpha 0.5, Dirichlet-drawn parameters), compressed to unique
+patterns; every internal CL is recomputed (127 node updates x P patterns).
+The headline form is the FP32-scaled plan walker; the plain FP64 path is
+measured beside it on the same plan.
+
+  value      updates/s of the FP32 form, device-timed with CUDA events over
+             K back-to-back runs (inputs resident in HBM; each run writes
+             ~0.6 GB of CLs, more than L2, so no extra flush is needed)
+  e2e        the same metric through the public API (Lik.lnL with a full
+             re-plan each step: host planning, program upload from pinned
+             memory, kernels, result read-back)
+  roofline   plan-walker kernel: algorithmic bytes per launch / event time,
+             against MEASURED_PEAKS.json hbm_gbs
+  cpu_baseline  the FP64 oracle CxLikExecute on the host cores (reference
+             build when present, else this repository's port)
+
+``--impl reference`` times the reference's CPU implementation on the same
+workload instead and prints its own line.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {"workload": "gtr_gamma4_128taxa_100ksites_full_lnL",
+            "ntaxa": 128, "nsites": 100000, "mean_brlen": 0.05,
+            "alpha": 0.5, "ncat": 4, "seed": 20261203}
+METRIC = "CLV pattern-node updates/s (FP32-scaled form, full post-order lnL)"
+UNIT = "updates/s"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class Dist:
+    """Barrier and max-reduce across replica ranks (gloo; one GPU each)."""
+
+    def __init__(self):
+        self.ws, self.rank = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.ws == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.out = None
+
+    def start(self):
+        try:
+            self.out = open(os.path.join(ROOT, "_clocks.tmp"), "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader",
+                 "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        path = os.path.join(ROOT, "_clocks.tmp")
+        rows = [r.split(",") for r in open(path).read().splitlines() if r.strip()]
+        os.unlink(path)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1].split()[0]))
+                smax.append(float(r[2].split()[0]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if "Active" in v and "Not" not in v:
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_case():
+    from crux_gb300 import synth
+    w = WORKLOAD
+    return synth.Case(w["ntaxa"], w["nsites"], w["mean_brlen"], w["seed"],
+                      alpha=w["alpha"], ncat=w["ncat"])
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_run(lib, case, aln, steps, threads):
+    """Time full-plan FP64 evaluations of the oracle; returns updates/s."""
+    from crux_gb300 import synth
+    lik = case.lik(lib=lib, alignment=aln)
+    lik.lnL()
+    t = 0.0
+    ups = 0
+    for _ in range(steps):
+        lik.lik.invalidate = True
+        lik._prep(None)
+        t0 = time.perf_counter()
+        lib.CxLikExecute(ctypes.byref(lik.lik))
+        t += time.perf_counter() - t0
+        ups += synth.nnodes_updates(lik)
+    return ups / t, t, ups
+
+
+def load_cpu_oracle():
+    from oracle import oracle
+    lib = oracle.load_ref()
+    threads = os.cpu_count() or 1
+    if lib is not None:
+        oracle.ref_threaded(lib)
+        threads = oracle.ref_ncpus(lib)
+        return lib, "reference", threads
+    lib = oracle.load_port()
+    lib.port_set_threads(threads)
+    return lib, "port", threads
+
+
+def run_reference(args, dist):
+    """--impl reference: the reference's CPU path on the host cores."""
+    if dist.rank != 0:
+        dist.close()
+        return
+    lib, kind, threads = load_cpu_oracle()
+    case = make_case()
+    aln = case.alignment()
+    cpu_run(lib, case, aln, max(args.warmup, 1), threads)
+    rate, secs, ups = cpu_run(lib, case, aln, args.steps, threads)
+    line = {"metric": METRIC.replace("FP32-scaled form", "FP64 CPU reference"),
+            "impl": "reference", "value": rate, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": dict(WORKLOAD, patterns=aln.nchars, l2_flush="inputs>L2"),
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads,
+                             "kind": kind,
+                             "sample": "%d full-tree FP64 lnL evaluations" %
+                                       args.steps},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def run_ours(args, dist):
+    from crux_gb300 import _native, synth
+    from crux_gb300.plan import Plan
+    gpu = _native.load()
+    case = make_case()
+
+    res = {}
+    for prec in ("fp32", "fp64"):
+        lik = case.lik(lib=gpu, precision=prec)
+        lnl_first = lik.lnL()
+        lik.lik.invalidate = True
+        lik._prep(None)
+        plan = Plan(lik, prec)
+        info = plan.info()
+        plan.time(max(args.warmup, 3))
+        dist.barrier()
+        clocks = Clocks()
+        if prec == "fp32":
+            clocks.start()
+        t = plan.time(args.steps)
+        ck = clocks.stop() if prec == "fp32" else None
+        ms = dist.max(t["ms_per_run"])
+        res[prec] = {"lik": lik, "plan": plan, "info": info, "t": t,
+                     "ms": ms, "clocks": ck, "lnL": t["lnL"],
+                     "lnL_first": lnl_first}
+
+    # End to end through the public API: full re-plan + lnL each step.
+    lik = res["fp32"]["lik"]
+    for _ in range(max(args.warmup, 3)):
+        lik.lik.invalidate = True
+        lik.lnL()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        lik.lik.invalidate = True
+        lik.lnL()
+    e2e_s = dist.max((time.perf_counter() - t0) / args.steps)
+    h2d, d2h = ctypes.c_size_t(), ctypes.c_size_t()
+    gpu.cxgLikLastIo(ctypes.byref(h2d), ctypes.byref(d2h))
+    nops = res["fp32"]["info"]["nops"]
+    npat = int(res["fp32"]["lik"].lik.mschars)
+    written = nops * npat * (4 * WORKLOAD["ncat"] * 4 + 4)
+
+    info = res["fp32"]["info"]
+    ws = dist.ws
+    value = info["updates"] * ws / (res["fp32"]["ms"] / 1e3)
+    e2e = info["updates"] * ws / e2e_s
+    kern_ms = res["fp32"]["t"]["kernel_ms"]
+    peaks = measured_peaks()
+    hbm = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = info["alg_bytes"] / (kern_ms / 1e3) / 1e9
+    traffic = profile_traffic("plan_kernel_fp32_128taxa_100ksites.md")
+
+    # Oracle check of both forms (FP64 oracle on the same plan).
+    cpu = None
+    check = {}
+    if dist.rank == 0 and not args.no_cpu:
+        lib, kind, threads = load_cpu_oracle()
+        aln = case.alignment()
+        rate, secs, ups = cpu_run(lib, case, aln, args.cpu_steps, threads)
+        want = case.lik(lib=lib, alignment=case.alignment()).lnL()
+        check = {p: abs(res[p]["lnL"] - want) / abs(want) for p in res}
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": "%d full-tree FP64 lnL evaluations (%.1f s)" %
+                         (args.cpu_steps, secs)}
+
+    if dist.rank == 0:
+        fp64 = res["fp64"]
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": res["fp32"]["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Yule tree, GTR+G4 simulation)",
+            "config": dict(WORKLOAD, patterns=int(fp64["lik"].lik.mschars),
+                           node_updates_per_step=nops,
+                           parallelism="replicas" if ws > 1 else "single",
+                           l2_flush="inputs>L2 (each step writes %.2f GB of CLs)"
+                                    % (written / 1e9)),
+            "e2e": {"value": e2e, "unit": UNIT,
+                    "h2d_bytes_per_step": int(h2d.value),
+                    "d2h_bytes_per_step": int(d2h.value)},
+            "gpu_launches": args.steps * info["kernels_per_run"],
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": traffic,
+                         "peak_source": "measured" if peaks else "fallback"},
+            "cpu_baseline": cpu,
+            "clocks": res["fp32"]["clocks"],
+            "fp64_plain": {
+                "value": info["updates"] * ws / (fp64["ms"] / 1e3),
+                "ms_per_step": fp64["ms"],
+                "kernel_ms": fp64["t"]["kernel_ms"],
+                "alg_bytes": fp64["info"]["alg_bytes"]},
+            "fp32_over_fp64": fp64["ms"] / res["fp32"]["ms"],
+            "kernel_ms": kern_ms,
+            "rel_err_vs_fp64_oracle": check,
+        }
+        print(json.dumps(line), flush=True)
+    for p in res.values():
+        p["plan"].close()
+    dist.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true",
+                    help="skip the CPU baseline and the oracle check")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    args = ap.parse_args()
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+    else:
+        run_ours(args, dist)
+
+
+if __name__ == "__main__":
+    main()

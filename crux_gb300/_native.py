@@ -1,0 +1,77 @@
+"""Loader for the GB300 library (crux_gb300/_lib/libcxlik_gpu.so).
+
+There is no CPU fallback: if the library is missing or no GPU is present the
+load raises, so a likelihood is never computed silently elsewhere.
+"""
+import ctypes
+import os
+
+from . import _abi
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib",
+                        "libcxlik_gpu.so")
+_lib = None
+
+
+class NativeUnavailable(RuntimeError):
+    pass
+
+
+def declare(lib):
+    """Declare every entry point of include/cxlik_gpu.h on `lib`."""
+    _abi.declare_core(lib)
+    P = ctypes.POINTER
+    c_int, c_uint, c_double = ctypes.c_int, ctypes.c_uint, ctypes.c_double
+    lib.cxgLastError.argtypes = []
+    lib.cxgLastError.restype = ctypes.c_char_p
+    lib.cxgInfo.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    lib.cxgInfo.restype = c_int
+    lib.cxgLikClSetLeafMasks.argtypes = [P(_abi.CxtLikCL), P(ctypes.c_uint8),
+                                         c_uint]
+    lib.cxgLikClSetLeafMasks.restype = c_int
+    lib.cxgLikClForget.argtypes = [P(c_double)]
+    lib.cxgLikClForget.restype = c_int
+    lib.cxgLikReset.argtypes = []
+    lib.cxgLikReset.restype = c_int
+    lib.cxgLikExecuteLnL.argtypes = [P(_abi.CxtLik), c_int, P(c_double),
+                                     P(c_double)]
+    lib.cxgLikExecuteLnL.restype = c_int
+    lib.cxgLikLastIo.argtypes = [P(ctypes.c_size_t), P(ctypes.c_size_t)]
+    lib.cxgLikLastIo.restype = c_int
+    lib.cxgLikDeviceBytes.argtypes = [P(ctypes.c_size_t)]
+    lib.cxgLikDeviceBytes.restype = c_int
+    vp = ctypes.c_void_p
+    lib.cxgPlanCreate.argtypes = [P(_abi.CxtLik), c_int, P(vp)]
+    lib.cxgPlanCreate.restype = c_int
+    lib.cxgPlanRun.argtypes = [vp, P(c_double), P(c_double)]
+    lib.cxgPlanRun.restype = c_int
+    lib.cxgPlanTime.argtypes = [vp, c_int, P(c_double), P(c_double),
+                                P(c_double)]
+    lib.cxgPlanTime.restype = c_int
+    lib.cxgPlanInfo.argtypes = [vp, P(c_double), P(c_double), P(c_uint),
+                                P(c_uint)]
+    lib.cxgPlanInfo.restype = c_int
+    lib.cxgPlanDestroy.argtypes = [vp]
+    lib.cxgPlanDestroy.restype = c_int
+    from . import _native_ext
+    _native_ext.declare_ext(lib)
+    return lib
+
+
+def load(path=LIB_PATH):
+    """Load and declare the library; raise NativeUnavailable if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise NativeUnavailable(
+            "%s is missing: build it with `python -m crux_gb300.build`" % path)
+    lib = ctypes.CDLL(path, mode=ctypes.RTLD_GLOBAL)
+    declare(lib)
+    _lib = lib
+    return lib
+
+
+def last_error(lib=None):
+    lib = lib or load()
+    return lib.cxgLastError().decode(errors="replace")

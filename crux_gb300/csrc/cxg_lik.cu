@@ -1,0 +1,767 @@
+// Host side of the drop-in boundary: CL registry, plan translation and the
+// extern "C" entry points of include/cxlik_gpu.h.
+//
+// The reference keeps each CL in host memory (Lik.pyx:60-107) and
+// CxLikExecute reads/writes it there.  Here every host CxtLikCL is an
+// identity: the registry maps its cLMat pointer to device buffers, internal
+// CLs are computed and kept on the device, and leaf CLs are uploaded once as
+// uint8 state masks.  A call translates lik->steps into a list of node
+// updates (a Compute step followed by its Merge steps up to ntrail == 0,
+// CxLik.c:314-596), uploads it in one copy, and launches two kernels: the
+// P-matrix builder and the plan walker.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "cxg_internal.h"
+
+namespace cxg {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string &msg) { g_err = msg; }
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t err, const char *what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(err);
+    return CXG_ECUDA;
+}
+
+#define CXG_CUDA(call)                                       \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
+    } while (0)
+
+enum { CL_INTERNAL = 0, CL_LEAF = 1 };
+
+struct DevCL {
+    int kind = CL_INTERNAL;
+    int precision = -1;   // precision of the data last written (internal)
+    unsigned npat = 0, ppad = 0, kcap = 0;
+    void *data = nullptr;
+    void *scaler = nullptr;
+    bool computed = false;
+};
+
+// Grow-only device buffer.
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t n) {
+        if (n <= cap) return 0;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = n < 4096 ? 4096 : n + n / 2;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(scratch)");
+        cap = want;
+        return 0;
+    }
+};
+
+// Grow-only pinned host buffer.
+struct HostBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t n) {
+        if (n <= cap) return 0;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = n < 4096 ? 4096 : n + n / 2;
+        cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaHostAlloc(staging)");
+        cap = want;
+        return 0;
+    }
+};
+
+struct FreqCache {
+    const unsigned *host = nullptr;
+    unsigned n = 0;
+    DevBuf dev;
+};
+
+struct State {
+    std::mutex mu;
+    bool ready = false;
+    cudaStream_t stream = nullptr;
+    std::unordered_map<uintptr_t, DevCL> cls;
+    size_t cl_bytes = 0;
+    size_t last_h2d = 0, last_d2h = 0;  // bytes copied by the last execute
+    DevBuf misc;         // CxLikQDecomp in/out
+    HostBuf stage, out;  // program staging, CxLikQDecomp staging
+    FreqCache freqs;
+};
+
+static State &state() {
+    static State *s = new State();  // never destroyed: outlives callers
+    return *s;
+}
+
+static int ensure_ready(State &S) {
+    if (S.ready) return 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    CXG_CUDA(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
+    S.ready = true;
+    return 0;
+}
+
+static void free_cl(State &S, DevCL &c) {
+    if (c.data) cudaFree(c.data);
+    if (c.scaler) cudaFree(c.scaler);
+    size_t elt = (c.kind == CL_LEAF) ? 1 : (c.precision == CXG_FP32 ? 4 : 8);
+    if (c.kind == CL_LEAF)
+        S.cl_bytes -= c.ppad;
+    else
+        S.cl_bytes -= (size_t)c.kcap * 4 * c.ppad * elt + (size_t)c.ppad * 8;
+    c.data = c.scaler = nullptr;
+}
+
+// Internal CL buffer for a parent written at `prec` with `kact` comps.
+static int parent_buffer(State &S, const CxtLikCL *cl, unsigned npat,
+                         unsigned kact, int prec, DevCL **out) {
+    if (cl == nullptr || cl->cLMat == nullptr)
+        return fail(CXG_EINVAL, "step parent CL has no cLMat");
+    uintptr_t key = (uintptr_t)cl->cLMat;
+    auto it = S.cls.find(key);
+    const unsigned ppad = pad_patterns(npat);
+    if (it != S.cls.end()) {
+        DevCL &c = it->second;
+        if (c.kind == CL_INTERNAL && c.precision == prec && c.npat == npat &&
+            c.kcap >= kact) {
+            *out = &c;
+            return 0;
+        }
+        free_cl(S, c);
+        S.cls.erase(it);
+    }
+    DevCL c;
+    c.kind = CL_INTERNAL;
+    c.precision = prec;
+    c.npat = npat;
+    c.ppad = ppad;
+    c.kcap = kact;
+    const size_t elt = prec == CXG_FP32 ? 4 : 8;
+    CXG_CUDA(cudaMalloc(&c.data, (size_t)kact * 4 * ppad * elt));
+    cudaError_t e = cudaMalloc(&c.scaler, (size_t)ppad * 8);
+    if (e != cudaSuccess) {
+        cudaFree(c.data);
+        return cuda_fail(e, "cudaMalloc(scaler)");
+    }
+    S.cl_bytes += (size_t)kact * 4 * ppad * elt + (size_t)ppad * 8;
+    auto ins = S.cls.emplace(key, c);
+    *out = &ins.first->second;
+    return 0;
+}
+
+// Upload leaf masks.  zero_any: a 0 mask (gap) means "any state", as
+// Lik.pyx:1469-1470 encodes it; otherwise a 0 mask stays a zero row.
+static int upload_leaf(State &S, const double *key, const uint8_t *masks,
+                       unsigned n, bool zero_any) {
+    auto it = S.cls.find((uintptr_t)key);
+    if (it != S.cls.end()) {
+        free_cl(S, it->second);
+        S.cls.erase(it);
+    }
+    DevCL c;
+    c.kind = CL_LEAF;
+    c.npat = n;
+    c.ppad = pad_patterns(n);
+    c.computed = true;
+    std::vector<uint8_t> h(c.ppad, 15);  // pad patterns: all states allowed
+    for (unsigned i = 0; i < n; ++i)
+        h[i] = (masks[i] & 15) ? (masks[i] & 15) : (zero_any ? 15 : 0);
+    CXG_CUDA(cudaMalloc(&c.data, c.ppad));
+    CXG_CUDA(cudaMemcpy(c.data, h.data(), c.ppad, cudaMemcpyHostToDevice));
+    S.cl_bytes += c.ppad;
+    S.cls.emplace((uintptr_t)key, c);
+    return 0;
+}
+
+// Leaf child used by a plan: registered masks, or (drop-in path) the host
+// rows of 4 doubles written by Lik.pyx:1466-1475.
+static int leaf_child(State &S, const CxtLik *lik, const CxtLikCL *cl,
+                      DevCL **out) {
+    if (cl == nullptr || cl->cLMat == nullptr)
+        return fail(CXG_EINVAL, "leaf child CL has no cLMat");
+    uintptr_t key = (uintptr_t)cl->cLMat;
+    auto it = S.cls.find(key);
+    if (it == S.cls.end() || it->second.kind != CL_LEAF ||
+        it->second.npat != lik->mschars) {
+        std::vector<uint8_t> m(lik->mschars);
+        for (unsigned c = 0; c < lik->mschars; ++c) {
+            unsigned v = 0;
+            for (unsigned j = 0; j < 4; ++j) {
+                double x = cl->cLMat[c * 4 + j];
+                if (x == 1.0)
+                    v |= 1u << j;
+                else if (x != 0.0)
+                    return fail(CXG_EINVAL,
+                                "leaf CL rows must hold 0/1 state indicators");
+            }
+            m[c] = (uint8_t)v;
+        }
+        // A row of zeros keeps mask 0, whose message is all zeros, as the
+        // reference computes it.
+        int rc = upload_leaf(S, cl->cLMat, m.data(), lik->mschars, false);
+        if (rc) return rc;
+        it = S.cls.find(key);
+    }
+    *out = &it->second;
+    return 0;
+}
+
+// Internal child: computed by an earlier run at this precision, or by an
+// earlier op of the plan being translated (`written`).
+static int internal_child(State &S, const CxtLik *lik, const CxtLikCL *cl,
+                          unsigned kact, int prec,
+                          const std::vector<DevCL *> &written, DevCL **out) {
+    if (cl == nullptr || cl->cLMat == nullptr)
+        return fail(CXG_EINVAL, "internal child CL has no cLMat");
+    auto it = S.cls.find((uintptr_t)cl->cLMat);
+    bool earlier = false;
+    if (it != S.cls.end())
+        for (DevCL *w : written) earlier |= (w == &it->second);
+    if (it == S.cls.end() || it->second.kind != CL_INTERNAL ||
+        !(it->second.computed || earlier) || it->second.precision != prec ||
+        it->second.npat != lik->mschars || it->second.kcap < kact)
+        return fail(CXG_EINVAL,
+                    "plan reads a child CL that has not been computed on the "
+                    "device at this precision");
+    *out = &it->second;
+    return 0;
+}
+
+// A translated plan: the device program of one lik->steps list at one
+// precision, runnable any number of times.  CL buffers it references must
+// outlive it.
+struct Plan {
+    int prec = CXG_FP64;
+    unsigned npat = 0, ppad = 0, kact = 0, nops = 0, nchild = 0;
+    DevBuf prog, pmat, ltab, partial, misc;
+    HostBuf out;
+    DevCL *root = nullptr;
+    std::vector<DevCL *> parents;
+    PmatArgs pa;
+    PlanArgs a;
+    double alg_bytes = 0.0;   // algorithmic bytes of one plan-walker launch
+    double updates = 0.0;     // pattern-node updates of one run
+};
+
+static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
+    int rc;
+    if (lik == nullptr) return fail(CXG_EINVAL, "lik is NULL");
+    if (lik->dim != 4)
+        return fail(CXG_EINVAL, "only 4-state (DNA) likelihoods run on the GPU");
+    if (prec != CXG_FP64 && prec != CXG_FP32)
+        return fail(CXG_EINVAL, "unknown precision");
+    const unsigned npat = lik->mschars;
+    if (npat == 0) return fail(CXG_EINVAL, "mschars is 0");
+    const unsigned ppad = pad_patterns(npat);
+
+    // Active components and the models they use.
+    std::vector<unsigned> act;
+    for (unsigned mc = 0; mc < lik->compsLen; ++mc)
+        if (lik->comps[mc].weightScaled != 0.0) act.push_back(mc);
+    const unsigned kact = (unsigned)act.size();
+    if (kact == 0) return fail(CXG_EINVAL, "no component has non-zero weight");
+    if (kact > kMaxComps)
+        return fail(CXG_EINVAL, "more than 8 active mixture components");
+    std::vector<const CxtLikModel *> models;
+    std::vector<int32_t> model_of(kact);
+    for (unsigned k = 0; k < kact; ++k) {
+        const CxtLikModel *m = lik->comps[act[k]].model;
+        int idx = -1;
+        for (size_t i = 0; i < models.size(); ++i)
+            if (models[i] == m) idx = (int)i;
+        if (idx < 0) {
+            idx = (int)models.size();
+            models.push_back(m);
+        }
+        model_of[k] = idx;
+    }
+
+    // Group steps into node updates.
+    std::vector<DevOp> ops;
+    std::vector<DevChild> kids;
+    std::vector<double> elen;
+    std::vector<uint32_t> lflag;
+    P.parents.clear();
+    const CxtLikCL *cur_parent = nullptr;
+    unsigned expect_trail = 0;
+    const double s_el = prec == CXG_FP32 ? 4.0 : 8.0;
+    const double e_el = prec == CXG_FP32 ? 4.0 : 8.0;
+    double bytes = 0.0;
+    for (unsigned s = 0; s < lik->stepsLen; ++s) {
+        const CxtLikStep &st = lik->steps[s];
+        if ((unsigned)st.variant > 3) return fail(CXG_EINVAL, "bad step variant");
+        const bool compute = (st.variant == CxeLikStepComputeL ||
+                              st.variant == CxeLikStepComputeI);
+        const bool leaf = (st.variant == CxeLikStepComputeL ||
+                           st.variant == CxeLikStepMergeL);
+        if (compute) {
+            if (cur_parent != nullptr)
+                return fail(CXG_EINVAL, "Compute step before ntrail reached 0");
+            DevCL *pc = nullptr;
+            rc = parent_buffer(S, st.parentCL, npat, kact, prec, &pc);
+            if (rc) return rc;
+            DevOp op;
+            op.data = pc->data;
+            op.scaler = pc->scaler;
+            op.child0 = (uint32_t)kids.size();
+            op.nchild = 0;
+            ops.push_back(op);
+            P.parents.push_back(pc);
+            cur_parent = st.parentCL;
+            bytes += 4.0 * kact * s_el + e_el;  // parent written
+        } else {
+            if (cur_parent == nullptr || st.parentCL != cur_parent ||
+                st.ntrail + 1 != expect_trail)
+                return fail(CXG_EINVAL, "Merge step does not continue its node");
+        }
+        DevCL *cc = nullptr;
+        rc = leaf ? leaf_child(S, lik, st.childCL, &cc)
+                  : internal_child(S, lik, st.childCL, kact, prec, P.parents,
+                                   &cc);
+        if (rc) return rc;
+        if (cc->data == P.parents.back()->data)
+            return fail(CXG_EINVAL, "step reads its own parent");
+        DevChild ch;
+        ch.data = cc->data;
+        ch.scaler = leaf ? nullptr : cc->scaler;
+        ch.leaf = leaf ? 1u : 0u;
+        ch.pm = (uint32_t)kids.size();
+        kids.push_back(ch);
+        elen.push_back(st.edgeLen);
+        lflag.push_back(ch.leaf);
+        bytes += leaf ? 1.0 : 4.0 * kact * s_el + e_el;  // child read
+        if (ops.back().nchild + 1 > kMaxChildren)
+            return fail(CXG_EINVAL, "node degree above 17");
+        ops.back().nchild++;
+        expect_trail = st.ntrail;
+        if (st.ntrail == 0) cur_parent = nullptr;
+    }
+    if (cur_parent != nullptr) return fail(CXG_EINVAL, "plan ends mid-node");
+
+    // Root CL.
+    if (lik->rootCLC == nullptr || lik->rootCLC->cLMat == nullptr)
+        return fail(CXG_EINVAL, "rootCLC has no cLMat");
+    {
+        auto it = S.cls.find((uintptr_t)lik->rootCLC->cLMat);
+        if (it == S.cls.end() || it->second.kind != CL_INTERNAL ||
+            it->second.precision != prec || it->second.kcap < kact)
+            return fail(CXG_EINVAL, "root CL has not been computed");
+        P.root = &it->second;
+        bool in_plan = false;
+        for (DevCL *p : P.parents) in_plan |= (p == P.root);
+        if (!in_plan && !P.root->computed)
+            return fail(CXG_EINVAL, "root CL has not been computed");
+    }
+    bytes += 4.0 * kact * s_el + e_el + 4.0 + 8.0;  // root read, freq, site
+
+    // Pattern weights, cached by host pointer.
+    const unsigned *fh = lik->charFreqs + lik->cbase;
+    if (S.freqs.host != fh || S.freqs.n != npat) {
+        rc = S.freqs.dev.ensure((size_t)npat * 4);
+        if (rc) return rc;
+        CXG_CUDA(cudaMemcpy(S.freqs.dev.p, fh, (size_t)npat * 4,
+                            cudaMemcpyHostToDevice));
+        S.freqs.host = fh;
+        S.freqs.n = npat;
+    }
+
+    // Pack the program: ops | kids | elen | lflag | cmult | rmult | model |
+    // cube | eig | pn, one pinned copy.
+    const unsigned nchild = (unsigned)kids.size();
+    const unsigned nmod = (unsigned)models.size();
+    auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+    size_t o_ops = 0;
+    size_t o_kids = al(o_ops + ops.size() * sizeof(DevOp));
+    size_t o_elen = al(o_kids + kids.size() * sizeof(DevChild));
+    size_t o_lflag = al(o_elen + elen.size() * 8);
+    size_t o_cm = al(o_lflag + lflag.size() * 4);
+    size_t o_rm = al(o_cm + kact * 8);
+    size_t o_mod = al(o_rm + kact * 8);
+    size_t o_cube = al(o_mod + kact * 4);
+    size_t o_eig = al(o_cube + nmod * 64 * 8);
+    size_t o_pn = al(o_eig + nmod * 4 * 8);
+    size_t total = al(o_pn + kact * 4 * 8);
+    rc = S.stage.ensure(total);
+    if (rc) return rc;
+    rc = P.prog.ensure(total);
+    if (rc) return rc;
+    char *h = static_cast<char *>(S.stage.p);
+    if (!ops.empty()) memcpy(h + o_ops, ops.data(), ops.size() * sizeof(DevOp));
+    if (!kids.empty())
+        memcpy(h + o_kids, kids.data(), kids.size() * sizeof(DevChild));
+    if (!elen.empty()) memcpy(h + o_elen, elen.data(), elen.size() * 8);
+    if (!lflag.empty()) memcpy(h + o_lflag, lflag.data(), lflag.size() * 4);
+    for (unsigned k = 0; k < kact; ++k) {
+        const CxtLikComp &cp = lik->comps[act[k]];
+        ((double *)(h + o_cm))[k] = cp.cmult;
+        ((double *)(h + o_rm))[k] = cp.model->rmult;
+        ((int32_t *)(h + o_mod))[k] = model_of[k];
+        for (unsigned i = 0; i < 4; ++i)
+            ((double *)(h + o_pn))[k * 4 + i] =
+                cp.model->piDiagNorm[i] * cp.weightScaled;
+    }
+    for (unsigned m = 0; m < nmod; ++m) {
+        memcpy(h + o_cube + m * 64 * 8, models[m]->qEigVecCube, 64 * 8);
+        memcpy(h + o_eig + m * 4 * 8, models[m]->qEigVals, 4 * 8);
+    }
+    char *d = static_cast<char *>(P.prog.p);
+    CXG_CUDA(cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, S.stream));
+    S.last_h2d = total;
+    // The staging buffer is reused by the next translation: finish the copy.
+    CXG_CUDA(cudaStreamSynchronize(S.stream));
+
+    rc = P.pmat.ensure((size_t)(nchild ? nchild : 1) * kact * 16 * 12);
+    if (rc) return rc;
+    rc = P.ltab.ensure((size_t)(nchild ? nchild : 1) * 16 * kact * 4 * 12);
+    if (rc) return rc;
+    PmatArgs &pa = P.pa;
+    pa.nchild = nchild;
+    pa.kact = kact;
+    pa.edge_len = (const double *)(d + o_elen);
+    pa.leafflag = (const uint32_t *)(d + o_lflag);
+    pa.cmult = (const double *)(d + o_cm);
+    pa.rmult = (const double *)(d + o_rm);
+    pa.model = (const int32_t *)(d + o_mod);
+    pa.cube = (const double *)(d + o_cube);
+    pa.eig = (const double *)(d + o_eig);
+    pa.wnorm = lik->wNorm;
+    pa.pm64 = (double *)P.pmat.p;
+    pa.pm32 = (float *)((char *)P.pmat.p + (size_t)nchild * kact * 16 * 8);
+    pa.ltab64 = (double *)P.ltab.p;
+    pa.ltab32 = (float *)((char *)P.ltab.p + (size_t)nchild * 16 * kact * 4 * 8);
+
+    const unsigned nb = plan_blocks(ppad);
+    rc = P.partial.ensure((size_t)nb * 16);
+    if (rc) return rc;
+    // misc: ticket (4) | ninf (4) | pad (8) | total (16) | site (ppad*8)
+    rc = P.misc.ensure(32 + (size_t)ppad * 8);
+    if (rc) return rc;
+    rc = P.out.ensure(32);
+    if (rc) return rc;
+    char *mp = static_cast<char *>(P.misc.p);
+    PlanArgs &a = P.a;
+    a.ops = (const DevOp *)(d + o_ops);
+    a.children = (const DevChild *)(d + o_kids);
+    a.nops = (uint32_t)ops.size();
+    a.kact = kact;
+    a.npat = npat;
+    a.ppad = ppad;
+    a.pm = prec == CXG_FP32 ? (const void *)pa.pm32 : (const void *)pa.pm64;
+    a.ltab = prec == CXG_FP32 ? (const void *)pa.ltab32 : (const void *)pa.ltab64;
+    a.pn = (const double *)(d + o_pn);
+    a.root = P.root->data;
+    a.rootsc = P.root->scaler;
+    a.freqs = (const uint32_t *)S.freqs.dev.p;
+    a.site = nullptr;
+    a.partial = (double *)P.partial.p;
+    a.ticket = (unsigned *)mp;
+    a.ninf = (uint32_t *)(mp + 4);
+    a.total = (double *)(mp + 16);
+    P.prec = prec;
+    P.npat = npat;
+    P.ppad = ppad;
+    P.kact = kact;
+    P.nops = (unsigned)ops.size();
+    P.nchild = nchild;
+    P.alg_bytes = bytes * npat;
+    P.updates = (double)ops.size() * npat;
+    return 0;
+}
+
+// Enqueue one run (P matrices, plan walk, result copy) on the stream;
+// optional events bracket the plan-walker launch.
+static int enqueue(State &S, Plan &P, bool want_site,
+                   cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr) {
+    char *mp = static_cast<char *>(P.misc.p);
+    P.a.site = want_site ? (double *)(mp + 32) : nullptr;
+    CXG_CUDA(cudaMemsetAsync(mp, 0, 32, S.stream));
+    CXG_CUDA(launch_pmat(P.pa, S.stream));
+    if (e0) CXG_CUDA(cudaEventRecord(e0, S.stream));
+    CXG_CUDA(launch_plan(P.prec, P.a, S.stream));
+    if (e1) CXG_CUDA(cudaEventRecord(e1, S.stream));
+    CXG_CUDA(cudaMemcpyAsync(P.out.p, mp, 32, cudaMemcpyDeviceToHost, S.stream));
+    return 0;
+}
+
+static int finish(State &S, Plan &P, double *lnL, double *site) {
+    if (site)
+        CXG_CUDA(cudaMemcpyAsync(site, static_cast<char *>(P.misc.p) + 32,
+                                 (size_t)P.npat * 8, cudaMemcpyDeviceToHost,
+                                 S.stream));
+    CXG_CUDA(cudaStreamSynchronize(S.stream));
+    for (DevCL *p : P.parents) p->computed = true;
+    const char *o = static_cast<const char *>(P.out.p);
+    uint32_t ninf;
+    double tot[2];
+    memcpy(&ninf, o + 4, 4);
+    memcpy(tot, o + 16, 16);
+    if (lnL) *lnL = ninf ? -INFINITY : tot[0] + tot[1];
+    return 0;
+}
+
+static Plan &scratch_plan() {
+    static Plan *p = new Plan();
+    return *p;
+}
+
+// Translate and run lik's plan.  `site` (host, mschars doubles) optional.
+static int execute(CxtLik *lik, int prec, double *lnL, double *site) {
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    int rc = ensure_ready(S);
+    if (rc) return rc;
+    Plan &P = scratch_plan();
+    rc = translate(S, lik, prec, P);
+    if (rc) return rc;
+    rc = enqueue(S, P, site != nullptr);
+    if (rc) return rc;
+    S.last_d2h = 32 + (site ? (size_t)P.npat * 8 : 0);
+    return finish(S, P, lnL, site);
+}
+
+}  // namespace cxg
+
+using namespace cxg;
+
+extern "C" {
+
+const char *cxgLastError(void) { return g_err.c_str(); }
+
+int cxgInfo(char *buf, size_t len) {
+    int dev = -1, rt = 0;
+    cudaRuntimeGetVersion(&rt);
+    cudaError_t e = cudaGetDevice(&dev);
+    snprintf(buf, len, "cxlik_gpu 1 sm_103a cudart %d device %d%s", rt, dev,
+             e == cudaSuccess ? "" : " (no device)");
+    return 0;
+}
+
+int cxgLikClSetLeafMasks(const CxtLikCL *cl, const uint8_t *masks,
+                         unsigned n) {
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    int rc = ensure_ready(S);
+    if (rc) return rc;
+    if (cl == nullptr || cl->cLMat == nullptr || masks == nullptr || n == 0)
+        return fail(CXG_EINVAL, "cxgLikClSetLeafMasks: bad argument");
+    return upload_leaf(S, cl->cLMat, masks, n, true);
+}
+
+int cxgLikClForget(const double *cLMat) {
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    auto it = S.cls.find((uintptr_t)cLMat);
+    if (it != S.cls.end()) {
+        free_cl(S, it->second);
+        S.cls.erase(it);
+    }
+    return 0;
+}
+
+int cxgLikReset(void) {
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    for (auto &kv : S.cls) free_cl(S, kv.second);
+    S.cls.clear();
+    S.freqs.host = nullptr;
+    S.freqs.n = 0;
+    return 0;
+}
+
+int cxgLikLastIo(size_t *h2d, size_t *d2h) {
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    if (h2d) *h2d = S.last_h2d;
+    if (d2h) *d2h = S.last_d2h;
+    return 0;
+}
+
+int cxgLikDeviceBytes(size_t *bytes) {
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    if (bytes) *bytes = S.cl_bytes;
+    return 0;
+}
+
+int cxgLikExecuteLnL(CxtLik *lik, int precision, double *lnL,
+                     double *siteLnL) {
+    return execute(lik, precision, lnL, siteLnL);
+}
+
+struct cxgPlan {
+    Plan p;
+};
+
+int cxgPlanCreate(CxtLik *lik, int precision, cxgPlan **out) {
+    if (out == nullptr) return fail(CXG_EINVAL, "cxgPlanCreate: out is NULL");
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    int rc = ensure_ready(S);
+    if (rc) return rc;
+    cxgPlan *h = new cxgPlan();
+    rc = translate(S, lik, precision, h->p);
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return 0;
+}
+
+int cxgPlanRun(cxgPlan *h, double *lnL, double *siteLnL) {
+    if (h == nullptr) return fail(CXG_EINVAL, "cxgPlanRun: NULL plan");
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    int rc = enqueue(S, h->p, siteLnL != nullptr);
+    if (rc) return rc;
+    return finish(S, h->p, lnL, siteLnL);
+}
+
+int cxgPlanTime(cxgPlan *h, int iters, double *ms_per_run,
+                double *plan_kernel_ms, double *lnL) {
+    if (h == nullptr || iters < 1) return fail(CXG_EINVAL, "cxgPlanTime: bad args");
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    Plan &P = h->p;
+    std::vector<cudaEvent_t> ev(2 * (size_t)iters + 2, nullptr);
+    for (auto &e : ev) CXG_CUDA(cudaEventCreate(&e));
+    int rc = 0;
+    cudaError_t ce = cudaEventRecord(ev[0], S.stream);
+    for (int i = 0; i < iters && rc == 0 && ce == cudaSuccess; ++i)
+        rc = enqueue(S, P, false, ev[2 + 2 * i], ev[3 + 2 * i]);
+    if (rc == 0 && ce == cudaSuccess) ce = cudaEventRecord(ev[1], S.stream);
+    if (rc == 0 && ce == cudaSuccess) ce = cudaEventSynchronize(ev[1]);
+    double kern = 0.0;
+    float tot = 0.0f;
+    if (rc == 0 && ce == cudaSuccess) {
+        ce = cudaEventElapsedTime(&tot, ev[0], ev[1]);
+        for (int i = 0; i < iters && ce == cudaSuccess; ++i) {
+            float k = 0.0f;
+            ce = cudaEventElapsedTime(&k, ev[2 + 2 * i], ev[3 + 2 * i]);
+            kern += k;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return cuda_fail(ce, "cxgPlanTime events");
+    if (ms_per_run) *ms_per_run = tot / iters;
+    if (plan_kernel_ms) *plan_kernel_ms = kern / iters;
+    return finish(S, P, lnL, nullptr);
+}
+
+int cxgPlanInfo(const cxgPlan *h, double *updates, double *alg_bytes,
+                unsigned *nops, unsigned *kernels_per_run) {
+    if (h == nullptr) return fail(CXG_EINVAL, "cxgPlanInfo: NULL plan");
+    if (updates) *updates = h->p.updates;
+    if (alg_bytes) *alg_bytes = h->p.alg_bytes;
+    if (nops) *nops = h->p.nops;
+    if (kernels_per_run) *kernels_per_run = 2;
+    return 0;
+}
+
+int cxgPlanDestroy(cxgPlan *h) {
+    if (h == nullptr) return 0;
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    cudaStreamSynchronize(S.stream);
+    Plan &P = h->p;
+    if (P.prog.p) cudaFree(P.prog.p);
+    if (P.pmat.p) cudaFree(P.pmat.p);
+    if (P.ltab.p) cudaFree(P.ltab.p);
+    if (P.partial.p) cudaFree(P.partial.p);
+    if (P.misc.p) cudaFree(P.misc.p);
+    if (P.out.p) cudaFreeHost(P.out.p);
+    delete h;
+    return 0;
+}
+
+void CxLikExecute(CxtLik *lik) {
+    // CxLik.c:914-968: nothing to do for an empty plan.
+    if (lik == nullptr || lik->stepsLen == 0) return;
+    double tot = 0.0;
+    if (execute(lik, CXG_FP64, &tot, lik->siteLnL + lik->cbase) != 0) {
+        // No error channel in the reference signature: poison the outputs
+        // so a caller cannot mistake them for a likelihood.
+        for (unsigned s = 0; s < lik->nstripes; ++s) lik->stripeLnL[s] = NAN;
+        return;
+    }
+    // Per-stripe sums in pattern order, as each reference worker does.
+    for (unsigned s = 0; s < lik->nstripes; ++s) {
+        double acc = 0.0;
+        const unsigned c0 = s * lik->stripeWidth;
+        for (unsigned c = c0; c < c0 + lik->stripeWidth && c < lik->mschars; ++c)
+            acc += lik->siteLnL[lik->cbase + c];
+        lik->stripeLnL[s] = acc;
+    }
+}
+
+bool CxLikQDecomp(int n, double *RTri, double *PiDiag, double *PiDiagNorm,
+                  double *qNorm, double *qEigVecCube, double *qEigVals) {
+    if (n != 4) {
+        set_error("CxLikQDecomp: only 4-state models are decomposed on the GPU");
+        return true;
+    }
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    if (ensure_ready(S)) return true;
+    if (S.out.ensure(74 * 8 + 10 * 8)) return true;
+    if (S.misc.ensure(32 + 128 * 8 + 84 * 8)) return true;
+    double *h = static_cast<double *>(S.out.p);
+    for (int i = 0; i < 6; ++i) h[i] = RTri[i];
+    for (int i = 0; i < 4; ++i) h[6 + i] = PiDiag[i];
+    double *din = (double *)((char *)S.misc.p + 32);
+    double *dout = din + 10;
+    if (cudaMemcpyAsync(din, h, 10 * 8, cudaMemcpyHostToDevice, S.stream) !=
+            cudaSuccess ||
+        launch_qdecomp(din, din + 6, dout, S.stream) != cudaSuccess ||
+        cudaMemcpyAsync(h, dout, 74 * 8, cudaMemcpyDeviceToHost, S.stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(S.stream) != cudaSuccess) {
+        set_error("CxLikQDecomp: CUDA failure");
+        return true;
+    }
+    if (h[73] != 0.0) {
+        set_error("CxLikQDecomp: eigensystem failed");
+        return true;
+    }
+    for (int i = 0; i < 4; ++i) PiDiagNorm[i] = h[i];
+    *qNorm = h[4];
+    for (int i = 0; i < 64; ++i) qEigVecCube[i] = h[5 + i];
+    for (int i = 0; i < 4; ++i) qEigVals[i] = h[69 + i];
+    return false;
+}
+
+void CxLikPt(int n, double *P, double *qEigVecCube, double *qEigVals,
+             double v) {
+    double ex[32];
+    if (n < 1 || n > 32) return;
+    for (int k = 0; k < n; ++k) ex[k] = exp(qEigVals[k] * v);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            double p = 0.0;
+            for (int k = 0; k < n; ++k) p += qEigVecCube[i * n * n + j * n + k] * ex[k];
+            P[i * n + j] = p < 0.0 ? 0.0 : p;
+        }
+}
+
+}  // extern "C"

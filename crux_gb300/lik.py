@@ -1,0 +1,781 @@
+"""The ``Lik`` likelihood object: model state, execution planning, lnL.
+
+Python-3 restatement of pkg/Crux/Tree/Lik.pyx (the reference is Python-2
+Cython).  ``Lik`` owns a ``CxtLik`` (include/cxlik_gpu.h, the ABI of
+lib/Crux/Tree/CxLik.h) and per-ring conditional-likelihood (CL) caches, plans
+the post-order step list with the reference's cache-validity rule, and hands
+the plan to a C library exporting ``CxLikExecute``.  By default that library
+is the GB300 one (crux_gb300/_lib/libcxlik_gpu.so); the ``lib=`` argument
+accepts any library with the same three entry points, which is how the tests
+run the same plans through the CPU oracles.
+
+Method map to the reference:
+  constructor / stripes    Lik.pyx:200-250     model alloc/init/decomp 388-475
+  dup / clone              Lik.pyx:587-660, 835-883
+  model API                Lik.pyx:885-1393    (weights, rates, freqs, alpha,
+                                                +I, mixtures)
+  _planAppend/_planRecurse/_plan  Lik.pyx:1395-1601
+  prep (weightScaled, wNorm)      Lik.pyx:1603-1665
+  lnL / siteLnLs / flush          Lik.pyx:1687-1787
+"""
+import ctypes
+import math
+import os
+import weakref
+
+import numpy as np
+
+from . import _abi
+from .alignment import Dna
+from .cxmath import gamma_rates
+
+CACHE_LINE = 64
+MQ_MULT = 8  # CxmLikMqMult (CxLik.h:277)
+
+
+class Config:
+    """Striping policy inputs (pkg/Crux/Config.py; Cx.c:7, 63-66)."""
+    threaded = True
+    ncpus = os.cpu_count() or 1
+
+
+def _tokens(nbytes=16):
+    return np.empty(max(nbytes // 8, 2), dtype=np.float64)
+
+
+class CL:
+    """CL cache of one ring, two polarities (Lik.pyx:32-108).
+
+    With a device library the host buffers are 16-byte identity tokens (the
+    device holds the data); with a host library they are real arrays.
+    """
+    __slots__ = ("c", "bufs", "lib", "device", "forget", "leaf", "valid",
+                 "parent", "nSibs", "edgeLen", "__weakref__")
+
+    def __init__(self, lib, device):
+        self.c = (_abi.CxtLikCL(), _abi.CxtLikCL())
+        self.bufs = [None, None]
+        self.lib = lib
+        self.device = device
+        # A GPU library caches device copies keyed by the host pointer:
+        # tell it when a host buffer goes away (also in drop-in mode).
+        self.forget = hasattr(lib, "cxgLikClForget")
+        self.leaf = False
+        # Python mirrors of the CxtLikCL cache-key fields, per polarity.
+        self.valid = [False, False]
+        self.parent = [None, None]
+        self.nSibs = [0, 0]
+        self.edgeLen = [0.0, 0.0]
+
+    def prepare(self, polarity, nchars, dim, ncomp):
+        if self.bufs[polarity] is None:
+            if self.device:
+                mat, lsc = _tokens(), _tokens()
+            else:
+                mat = np.zeros(nchars * dim * ncomp, dtype=np.float64)
+                lsc = np.zeros(nchars, dtype=np.float64)
+            self.bufs[polarity] = (mat, lsc)
+            self.c[polarity].cLMat = _abi.dptr(mat)
+            self.c[polarity].lnScale = _abi.dptr(lsc)
+
+    def resize(self, polarity, nchars, dim, ncomp):
+        self.flush_buffers(polarity)
+        self.prepare(polarity, nchars, dim, ncomp)
+
+    def flush_buffers(self, polarity):
+        b = self.bufs[polarity]
+        if b is not None:
+            if self.forget:
+                self.lib.cxgLikClForget(_abi.dptr(b[0]))
+            self.bufs[polarity] = None
+            self.c[polarity].cLMat = None
+            self.c[polarity].lnScale = None
+
+    def flush(self, polarity):
+        self.flush_buffers(polarity)
+        self.c[polarity].valid = False
+        self.c[polarity].parent = None
+        self.valid[polarity] = False
+        self.parent[polarity] = None
+
+    def set_valid(self, polarity, v):
+        self.valid[polarity] = v
+        self.c[polarity].valid = v
+
+    def release(self):
+        for p in (0, 1):
+            self.flush_buffers(p)
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class _Model:
+    """Host copy of one CxtLikModel with its arrays (Lik.pyx:388-466)."""
+
+    def __init__(self, dim, rlen):
+        self.s = _abi.CxtLikModel()
+        self.rclass = np.zeros(rlen, dtype=np.uint32)
+        self.rTri = np.ones(rlen, dtype=np.float64)
+        self.piDiag = np.full(dim, 1.0 / dim, dtype=np.float64)
+        self.piDiagNorm = np.zeros(dim, dtype=np.float64)
+        self.cube = np.zeros(dim * dim * dim, dtype=np.float64)
+        self.eig = np.zeros(dim, dtype=np.float64)
+        s = self.s
+        s.rclass = _abi.uptr(self.rclass)
+        s.rTri = _abi.dptr(self.rTri)
+        s.piDiag = _abi.dptr(self.piDiag)
+        s.piDiagNorm = _abi.dptr(self.piDiagNorm)
+        s.qEigVecCube = _abi.dptr(self.cube)
+        s.qEigVals = _abi.dptr(self.eig)
+
+
+def default_library():
+    from . import _native
+    return _native.load()
+
+
+class Lik:
+    """Tree likelihood over an alignment and a mixture of models."""
+
+    def __init__(self, tree=None, alignment=None, nmodels=1, ncat=1,
+                 catMedian=False, invar=False, lib=None, precision="fp64",
+                 dropin=False):
+        """`lib`: library exporting the CxLik entry points (default: the
+        GB300 one).  `precision`: "fp64" (plain) or "fp32" (scaled form).
+        `dropin`: drive the library exactly as Lik.pyx does -- host CL
+        buffers with leaf rows of 4 doubles, CxLikExecute, and the stripe
+        sum -- instead of the device-resident cxg* path."""
+        self.lib = lib if lib is not None else default_library()
+        self.dropin = dropin
+        self.device = hasattr(self.lib, "cxgLikClForget") and not dropin
+        self.precision = precision
+        self.lik = None
+        self.mate = None
+        self._models = []
+        if alignment is not None:
+            self._init0(tree)
+            nchars = alignment.nchars
+            npad = self._computeNpad(nchars, self._computeStripeWidth(nchars))
+            char_ = alignment.charType.get()
+            if npad != 0:
+                alignment.pad(char_.val2code(char_.any), npad)
+                nchars += npad
+            self._init1(tree, nchars, char_.nstates, 0)
+            self._init2(alignment, char_)
+            for _ in range(nmodels):
+                self.addModel(1.0, ncat, catMedian, invar)
+
+    # -- construction (Lik.pyx:221-324) ------------------------------------
+    @staticmethod
+    def _computeStripeWidth(nchars):
+        if Config.threaded:
+            quantum = CACHE_LINE // (4 * 8)
+            width = quantum
+            nstripes = -(-nchars // width)
+            while nstripes > Config.ncpus * MQ_MULT:
+                width += quantum
+                nstripes = -(-nchars // width)
+            return width
+        return nchars
+
+    @staticmethod
+    def _computeNpad(nchars, width):
+        return (width - nchars % width) if nchars % width else 0
+
+    def _init0(self, tree):
+        if tree.rooted:
+            raise ValueError("Tree must be unrooted")
+        tree.clearAux()
+
+    def _init1(self, tree, nchars, dim, polarity):
+        self.mate = None
+        self.tree = tree
+        L = self.lik = _abi.CxtLik()
+        L.polarity = polarity
+        L.dim = dim
+        L.rlen = dim * (dim - 1) // 2
+        L.cbase = 0
+        L.nchars = nchars
+        L.mschars = nchars
+        L.stripeWidth = self._computeStripeWidth(nchars)
+        L.nstripes = L.mschars // L.stripeWidth
+        assert L.nstripes * L.stripeWidth == L.mschars
+        L.invalidate = False
+        L.resize = False
+        L.reweight = False
+        L.wNorm = 0.0
+        self._models = []
+        self._comps = []          # per component: [model, cweight, cmult]
+        self._compsArr = None
+        self._modelsArr = None
+        self.siteLnLBuf = np.zeros(nchars, dtype=np.float64)
+        self.stripeLnLBuf = np.zeros(L.nstripes, dtype=np.float64)
+        L.siteLnL = _abi.dptr(self.siteLnLBuf)
+        L.stripeLnL = _abi.dptr(self.stripeLnLBuf)
+
+    def _init2(self, alignment, char_):
+        self.char_ = char_
+        self.alignment = alignment
+        L = self.lik
+        L.npad = alignment.npad
+        self._freqs = np.ascontiguousarray(alignment.freqs, dtype=np.uint32)
+        L.charFreqs = _abi.uptr(self._freqs)
+        stepsMax = 2 * alignment.ntaxa - 2
+        self._steps = (_abi.CxtLikStep * max(stepsMax, 1))()
+        L.steps = ctypes.cast(self._steps, ctypes.POINTER(_abi.CxtLikStep))
+        L.stepsLen = 0
+        L.stepsMax = stepsMax
+        self.rootCL = CL(self.lib, self.device)
+        L.rootCLC = ctypes.pointer(self.rootCL.c[L.polarity])
+
+    # -- component array maintenance ----------------------------------------
+    def _sync_comps(self):
+        """Rebuild the C comps/models arrays from the Python-side lists."""
+        n = len(self._comps)
+        arr = (_abi.CxtLikComp * max(n, 1))()
+        for i, c in enumerate(self._comps):
+            arr[i].model = ctypes.pointer(c["model"].s)
+            arr[i].weightScaled = c["weightScaled"]
+            arr[i].cweight = c["cweight"]
+            arr[i].cmult = c["cmult"]
+        self._compsArr = arr
+        self.lik.comps = ctypes.cast(arr, ctypes.POINTER(_abi.CxtLikComp))
+        self.lik.compsLen = n
+        self.lik.compsMax = max(n, 1)
+        m = len(self._models)
+        marr = (ctypes.POINTER(_abi.CxtLikModel) * max(m, 1))()
+        for i, mod in enumerate(self._models):
+            marr[i] = ctypes.pointer(mod.s)
+            mod.s.comp0 = mod.comp0
+            mod.s.clen = mod.clen
+        self._modelsArr = marr
+        self.lik.models = ctypes.cast(
+            marr, ctypes.POINTER(ctypes.POINTER(_abi.CxtLikModel)))
+        self.lik.modelsLen = m
+        self.lik.modelsMax = max(m, 1)
+
+    # -- models (Lik.pyx:388-509, 885-1393) ----------------------------------
+    def _model(self, i):
+        assert i < len(self._models)
+        return self._models[i]
+
+    def addModel(self, weight, ncat=1, catMedian=False, invar=False):
+        assert ncat > 0
+        L = self.lik
+        mod = _Model(L.dim, L.rlen)
+        ncomp = ncat + (1 if invar else 0)
+        mod.comp0 = len(self._comps)
+        mod.clen = ncomp
+        s = mod.s
+        s.decomp = True
+        s.weight = weight
+        s.rmult = 1.0
+        s.alpha = math.inf
+        s.catMedian = catMedian
+        s.invar = invar
+        for i in range(ncomp):
+            self._comps.append({"model": mod, "cweight": 1.0 if i == 0 else 0.0,
+                                "cmult": 1.0 if i == 0 else 0.0,
+                                "weightScaled": 0.0})
+        self._models.append(mod)
+        self._sync_comps()
+        L.resize = True
+        return len(self._models) - 1
+
+    def delModel(self, model):
+        assert model < len(self._models)
+        if len(self._models) == 0:
+            raise ValueError("No models remain")
+        mod = self._models[model]
+        del self._comps[mod.comp0:mod.comp0 + mod.clen]
+        for later in self._models[model + 1:]:
+            later.comp0 -= mod.clen
+        del self._models[model]
+        self._sync_comps()
+        self.lik.resize = True
+
+    def nmodels(self):
+        return len(self._models)
+
+    def getWNorm(self):
+        return self.lik.wNorm
+
+    def getWeight(self, model):
+        return self._model(model).s.weight
+
+    def setWeight(self, model, weight):
+        assert weight >= 0.0
+        self._model(model).s.weight = weight
+        self.lik.reweight = True
+
+    def getRmult(self, model):
+        return self._model(model).s.rmult
+
+    def setRmult(self, model, rmult):
+        assert rmult >= 0.0
+        self._model(model).s.rmult = rmult
+        self.lik.reweight = True
+
+    def getRclass(self, model):
+        return [int(x) for x in self._model(model).rclass]
+
+    def setRclass(self, model, rclass, rates=None):
+        mod = self._model(model)
+        rmax = 0
+        for r in rclass:
+            if r == rmax + 1:
+                rmax += 1
+            elif r > rmax + 1:
+                raise ValueError("Invalid rclass specification")
+        mod.rclass[:] = rclass
+        if rates is None:
+            mod.rTri[:] = 1.0
+        else:
+            if len(rates) != rmax + 1:
+                raise ValueError("Incorrect rates list length")
+            for i in range(self.lik.rlen):
+                if not isinstance(rates[rclass[i]], float):
+                    raise ValueError("Incorrect type for rate %d" % i)
+            for i in range(self.lik.rlen):
+                mod.rTri[i] = rates[rclass[i]]
+        mod.s.decomp = True
+
+    def getNrates(self, model):
+        return int(self._model(model).rclass.max()) + 1
+
+    def getRate(self, model, i):
+        mod = self._model(model)
+        for j in range(self.lik.rlen):
+            if mod.rclass[j] == i:
+                return float(mod.rTri[j])
+        raise ValueError("Invalid rate class index")
+
+    def setRate(self, model, i, rate):
+        mod = self._model(model)
+        assert rate >= 0.0
+        found = False
+        decomp = False
+        for j in range(self.lik.rlen):
+            if mod.rclass[j] == i:
+                if mod.rTri[j] != rate:
+                    decomp = True
+                mod.rTri[j] = rate
+                found = True
+        if not found:
+            raise ValueError("Invalid rate class index")
+        if decomp:
+            mod.s.decomp = True
+
+    def getFreq(self, model, i):
+        return float(self._model(model).piDiag[i])
+
+    def setFreq(self, model, i, freq):
+        mod = self._model(model)
+        assert freq > 0.0
+        if mod.piDiag[i] != freq:
+            mod.piDiag[i] = freq
+            mod.s.decomp = True
+
+    def getAlpha(self, model):
+        return self._model(model).s.alpha
+
+    def _ncat(self, mod):
+        return mod.clen - (1 if mod.s.invar else 0)
+
+    def setAlpha(self, model, alpha):
+        mod = self._model(model)
+        ncat = self._ncat(mod)
+        assert ncat > 1
+        if mod.s.alpha == alpha:
+            return
+        mod.s.alpha = alpha
+        comps = self._comps[mod.comp0:mod.comp0 + ncat]
+        if alpha != math.inf:
+            rates = gamma_rates(alpha, ncat, bool(mod.s.catMedian))
+            for c, r in zip(comps, rates):
+                c["cmult"] = r
+            cw = sum(c["cweight"] for c in comps) / ncat
+            for c in comps:
+                c["cweight"] = cw
+        else:
+            cw = sum(c["cweight"] for c in comps)
+            comps[0]["cweight"] = cw
+            comps[0]["cmult"] = 1.0
+            for c in comps[1:]:
+                c["cweight"] = 0.0
+                c["cmult"] = 0.0
+        self._sync_comps()
+        self.lik.invalidate = True
+
+    def getNcat(self, model):
+        return self._ncat(self._model(model))
+
+    def getCatMedian(self, model):
+        return bool(self._model(model).s.catMedian)
+
+    def getInvar(self, model):
+        return bool(self._model(model).s.invar)
+
+    def getWVar(self, model):
+        mod = self._model(model)
+        if mod.s.alpha == math.inf:
+            return self._comps[mod.comp0]["cweight"]
+        return sum(c["cweight"] for c in
+                   self._comps[mod.comp0:mod.comp0 + self._ncat(mod)])
+
+    def setWVar(self, model, wVar):
+        mod = self._model(model)
+        assert wVar >= 0.0
+        if mod.s.alpha == math.inf:
+            self._comps[mod.comp0]["cweight"] = wVar
+        else:
+            n = self._ncat(mod)
+            for c in self._comps[mod.comp0:mod.comp0 + n]:
+                c["cweight"] = wVar / n
+        self._sync_comps()
+        self.lik.reweight = True
+
+    def getWInvar(self, model):
+        mod = self._model(model)
+        if not mod.s.invar:
+            return 0.0
+        return self._comps[mod.comp0 + mod.clen - 1]["cweight"]
+
+    def setWInvar(self, model, wInvar):
+        mod = self._model(model)
+        if not mod.s.invar and wInvar != 0.0:
+            raise ValueError("Model does not support invariable sites.")
+        assert wInvar >= 0.0
+        self._comps[mod.comp0 + mod.clen - 1]["cweight"] = wInvar
+        self._sync_comps()
+        self.lik.reweight = True
+
+    # -- copies (Lik.pyx:587-660, 835-883) ------------------------------------
+    def _dup(self, other):
+        assert len(other._models) == 0
+        for fr in self._models:
+            ncat = fr.clen - (1 if fr.s.invar else 0)
+            m = other.addModel(fr.s.weight, ncat, bool(fr.s.catMedian),
+                               bool(fr.s.invar))
+            to = other._models[m]
+            to.s.rmult = fr.s.rmult
+            to.rclass[:] = fr.rclass
+            to.rTri[:] = fr.rTri
+            to.piDiag[:] = fr.piDiag
+            to.piDiagNorm[:] = fr.piDiagNorm
+            to.s.alpha = fr.s.alpha
+            to.s.catMedian = fr.s.catMedian
+        for i, c in enumerate(self._comps):
+            other._comps[i]["cweight"] = c["cweight"]
+            other._comps[i]["cmult"] = c["cmult"]
+        other._sync_comps()
+
+    def dup(self):
+        """Independent Lik on a duplicated tree; no cached CLs."""
+        ret = Lik(lib=self.lib, precision=self.precision, dropin=self.dropin)
+        tree = self.tree.dup()
+        ret._init0(tree)
+        ret._init1(tree, self.lik.nchars, self.lik.dim, 0)
+        ret._init2(self.alignment, self.char_)
+        self._dup(ret)
+        return ret
+
+    def clone(self):
+        """Mate Lik with the other CL polarity, sharing the tree."""
+        if self.mate is not None:
+            ret = self.mate
+            ret.lik.invalidate = True
+            resize = len(ret._comps) != len(self._comps)
+            for i in range(len(ret._models) - 1, -1, -1):
+                ret.delModel(i)
+        else:
+            assert self.lik.polarity == 0
+            resize = False
+            ret = Lik(lib=self.lib, precision=self.precision,
+                      dropin=self.dropin)
+            ret._init1(self.tree, self.lik.nchars, self.lik.dim, 1)
+            ret._init2(self.alignment, self.char_)
+            ret.mate = weakref.proxy(self)
+            self.mate = ret
+        self._dup(ret)
+        ret.lik.resize = resize
+        ret.lik.reweight = True
+        return ret
+
+    # -- planning (Lik.pyx:1395-1601) ----------------------------------------
+    def _planAppend(self, variant, ntrail, parentCL, childCL, edgeLen):
+        L = self.lik
+        assert ntrail != 0 or variant in (_abi.MergeL, _abi.MergeI)
+        st = self._steps[L.stepsLen]
+        L.stepsLen += 1
+        st.variant = variant
+        st.ntrail = ntrail
+        pol = L.polarity
+        st.parentCL = ctypes.pointer(parentCL.c[pol])
+        if childCL.bufs[1] is None:
+            assert childCL.bufs[0] is not None
+            st.childCL = ctypes.pointer(childCL.c[0])
+        else:
+            st.childCL = ctypes.pointer(childCL.c[pol])
+        if edgeLen < 0.0:
+            raise ValueError("Negative branch length")
+        st.edgeLen = edgeLen
+        self._plan_refs.append((parentCL, childCL))
+
+    def _leafInit(self, ring):
+        L = self.lik
+        taxon = ring.node.taxon
+        if taxon is None:
+            raise ValueError("Leaf node missing taxon")
+        cl = CL(self.lib, self.device)
+        cl.leaf = True
+        cl.prepare(0, L.mschars, L.dim, 1)
+        ind = self.alignment.taxaMap.indGet(taxon)
+        if ind == -1:
+            raise ValueError("Taxon %r missing from alignment's taxa map"
+                             % taxon)
+        row = self.alignment.getRow(ind)[L.cbase:L.cbase + L.mschars]
+        vals = self.char_.val_table[row]
+        if (vals < 0).any():
+            bad = row[vals < 0][0]
+            raise ValueError("State not defined: %r" % chr(bad))
+        vals = np.where(vals == 0, self.char_.any, vals)
+        if self.device:
+            masks = np.ascontiguousarray(vals, dtype=np.uint8)
+            rc = self.lib.cxgLikClSetLeafMasks(
+                ctypes.pointer(cl.c[0]),
+                masks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                L.mschars)
+            if rc != 0:
+                raise RuntimeError("cxgLikClSetLeafMasks: %s"
+                                   % self.lib.cxgLastError().decode())
+        else:
+            mat = cl.bufs[0][0].reshape(L.mschars, L.dim)
+            for j in range(L.dim):
+                mat[:, j] = ((vals >> j) & 1).astype(np.float64)
+            cl.bufs[0][1][:] = 0.0
+        ring.aux = cl
+        return cl
+
+    def _planRecurse(self, ring, parent, nSibs, edgeLen):
+        L = self.lik
+        pol = L.polarity
+        cL = ring.aux
+        degree = ring.node.getDegree()
+        if degree == 1:
+            if cL is None:
+                cL = self._leafInit(ring)
+        else:
+            if cL is None:
+                cL = CL(self.lib, self.device)
+                cL.prepare(pol, L.mschars, L.dim, L.compsLen)
+                ring.aux = cL
+            elif L.resize:
+                cL.resize(pol, L.mschars, L.dim, L.compsLen)
+            else:
+                cL.prepare(pol, L.mschars, L.dim, L.compsLen)
+
+        for r in ring.siblings():
+            if L.invalidate:
+                f = r.aux
+                if f is not None:
+                    f.flush(pol)
+            self._planRecurse(r.other, cL, degree, r.edge.length)
+
+        if L.invalidate or cL.parent[pol] is not parent \
+                or cL.nSibs[pol] != nSibs or cL.edgeLen[pol] != edgeLen:
+            parent.set_valid(pol, False)
+            cL.parent[pol] = parent
+            cL.nSibs[pol] = nSibs
+            cL.edgeLen[pol] = edgeLen
+            cLC = cL.c[pol]
+            cLC.parent = ctypes.pointer(parent.c[pol])
+            cLC.nSibs = nSibs
+            cLC.edgeLen = edgeLen
+
+        if degree != 1:
+            if L.invalidate or not cL.valid[pol]:
+                r = ring.next
+                for j in range(1, degree):
+                    if r.other.node.getDegree() > 1:
+                        variant = _abi.ComputeI if j == 1 else _abi.MergeI
+                    else:
+                        variant = _abi.ComputeL if j == 1 else _abi.MergeL
+                    self._planAppend(variant, degree - j - 1, cL, r.other.aux,
+                                     r.edge.length)
+                    r = r.next
+                cL.set_valid(pol, True)
+                parent.set_valid(pol, False)
+
+    def _plan(self, root):
+        L = self.lik
+        pol = L.polarity
+        if L.resize:
+            self.rootCL.resize(pol, L.mschars, L.dim, L.compsLen)
+        else:
+            self.rootCL.prepare(pol, L.mschars, L.dim, L.compsLen)
+        L.rootCLC = ctypes.pointer(self.rootCL.c[pol])
+        if root is None:
+            root = self.tree.base
+        degree = root.getDegree()
+        ring = root.ring
+        if degree == 1:
+            self._planRecurse(ring.other, self.rootCL, 2, ring.edge.length)
+            self._planRecurse(ring, self.rootCL, 2, 0.0)
+            if L.invalidate or not self.rootCL.valid[pol]:
+                variant = (_abi.ComputeI if ring.other.node.getDegree() > 1
+                           else _abi.ComputeL)
+                self._planAppend(variant, 1, self.rootCL, ring.other.aux,
+                                 ring.edge.length)
+                self._planAppend(_abi.MergeL, 0, self.rootCL, ring.aux, 0.0)
+                self.rootCL.set_valid(pol, True)
+        else:
+            for r in ring:
+                if L.invalidate:
+                    f = r.aux
+                    if f is not None:
+                        f.flush(pol)
+                self._planRecurse(r.other, self.rootCL, degree, r.edge.length)
+            if L.invalidate or not self.rootCL.valid[pol]:
+                variant = (_abi.ComputeI if ring.other.node.getDegree() > 1
+                           else _abi.ComputeL)
+                ntrail = degree - 1
+                self._planAppend(variant, ntrail, self.rootCL, ring.other.aux,
+                                 ring.edge.length)
+                for r in ring.siblings():
+                    variant = (_abi.MergeI if r.other.node.getDegree() > 1
+                               else _abi.MergeL)
+                    ntrail -= 1
+                    self._planAppend(variant, ntrail, self.rootCL,
+                                     r.other.aux, r.edge.length)
+                self.rootCL.set_valid(pol, True)
+        L.resize = False
+        L.invalidate = False
+
+    # -- preparation (Lik.pyx:1603-1685) -------------------------------------
+    def prep(self):
+        L = self.lik
+        if len(self._models) == 0:
+            raise ValueError("Empty model mixture")
+        if L.resize:
+            L.reweight = True
+        if L.reweight:
+            wsum = sum(m.s.weight for m in self._models)
+            if wsum == 0.0:
+                raise ValueError("At least one model must have non-zero "
+                                 "weight")
+            for m in self._models:
+                comps = self._comps[m.comp0:m.comp0 + m.clen]
+                wsumc = sum(c["cweight"] for c in comps)
+                assert wsumc > 0.0
+                for c in comps:
+                    c["weightScaled"] = (m.s.weight / wsum) * \
+                        (c["cweight"] / wsumc)
+            L.invalidate = True
+            L.reweight = False
+        for m in self._models:
+            if m.s.decomp:
+                self._decompModel(m)
+        qmean = 0.0
+        for c in self._comps:
+            if c["weightScaled"] != 0.0 and c["cmult"] != 0.0:
+                m = c["model"]
+                qmean += c["weightScaled"] * (m.s.rmult / m.s.qNorm)
+        wnorm = 1.0 / qmean if qmean != 0.0 else math.inf
+        if wnorm != L.wNorm:
+            L.invalidate = True
+            L.wNorm = wnorm
+        self._sync_comps()
+
+    def _decompModel(self, m):
+        qnorm = ctypes.c_double()
+        if self.lib.CxLikQDecomp(self.lik.dim, _abi.dptr(m.rTri),
+                                 _abi.dptr(m.piDiag), _abi.dptr(m.piDiagNorm),
+                                 ctypes.byref(qnorm), _abi.dptr(m.cube),
+                                 _abi.dptr(m.eig)):
+            raise ValueError("Error decomposing Q")
+        m.s.qNorm = qnorm.value
+        m.s.decomp = False
+
+    def _prep(self, root):
+        self.prep()
+        L = self.lik
+        stepsMax = 2 * self.alignment.ntaxa - 2
+        if L.stepsMax < stepsMax:
+            self._steps = (_abi.CxtLikStep * stepsMax)()
+            L.steps = ctypes.cast(self._steps,
+                                  ctypes.POINTER(_abi.CxtLikStep))
+            L.stepsMax = stepsMax
+        L.stepsLen = 0
+        self._plan_refs = []
+        self._plan(root)
+
+    # -- evaluation (Lik.pyx:1687-1763) ---------------------------------------
+    def _precision_code(self):
+        return 1 if self.precision == "fp32" else 0
+
+    def lnL(self, root=None):
+        """Log-likelihood, rooted at `root` (default: the tree's base)."""
+        self._prep(root)
+        if self.device:
+            out = ctypes.c_double()
+            rc = self.lib.cxgLikExecuteLnL(ctypes.byref(self.lik),
+                                           self._precision_code(),
+                                           ctypes.byref(out), None)
+            if rc != 0:
+                raise RuntimeError("cxgLikExecuteLnL: %s"
+                                   % self.lib.cxgLastError().decode())
+            return out.value
+        self.lib.CxLikExecute(ctypes.byref(self.lik))
+        ret = 0.0
+        for i in range(self.lik.nstripes):
+            ret += self.stripeLnLBuf[i]
+        return ret
+
+    def siteLnLs(self, root=None):
+        """Per-site lnL (pad sites excluded)."""
+        self._prep(root)
+        if self.device:
+            out = ctypes.c_double()
+            rc = self.lib.cxgLikExecuteLnL(ctypes.byref(self.lik),
+                                           self._precision_code(),
+                                           ctypes.byref(out),
+                                           _abi.dptr(self.siteLnLBuf))
+            if rc != 0:
+                raise RuntimeError("cxgLikExecuteLnL: %s"
+                                   % self.lib.cxgLastError().decode())
+        else:
+            self.lib.CxLikExecute(ctypes.byref(self.lik))
+        n = self.lik.nchars - self.lik.npad
+        return [float(x) for x in self.siteLnLBuf[:n]]
+
+    def execute_dropin(self, root=None):
+        """Plan, then run the library's drop-in CxLikExecute; return the
+        stripe sum the way Lik.lnL does (Lik.pyx:1697-1712)."""
+        self._prep(root)
+        self.lib.CxLikExecute(ctypes.byref(self.lik))
+        ret = 0.0
+        for i in range(self.lik.nstripes):
+            ret += self.stripeLnLBuf[i]
+        return ret
+
+    def flush(self):
+        """Drop all cached CLs of this polarity (Lik.pyx:1765-1787)."""
+        pol = self.lik.polarity
+        for e in self.tree.edges:
+            for ring in (e.ring, e.ring.other):
+                if ring.node.getDegree() > 1 and ring.aux is not None:
+                    ring.aux.flush(pol)
+
+    @property
+    def nsteps(self):
+        return self.lik.stepsLen
+
+    def steps(self):
+        """The current plan as (variant, ntrail, edgeLen) tuples."""
+        return [(self._steps[i].variant, self._steps[i].ntrail,
+                 self._steps[i].edgeLen) for i in range(self.lik.stepsLen)]

@@ -1,0 +1,226 @@
+/*
+ * cxlik_gpu.h -- C ABI of the GB300 pruning-likelihood library
+ * (crux_gb300/_lib/libcxlik_gpu.so).
+ *
+ * Part 1 is the drop-in boundary: the structures and the three entry points
+ * that Crux's Lik object (pkg/Crux/Tree/Lik.pyx) fills and calls.  Their
+ * layout and meaning are those of lib/Crux/Tree/CxLik.h; a caller built
+ * against that header links against this library unchanged.
+ *
+ * Part 2 holds the additional cxg* entry points: device-resident leaf data,
+ * cache release, an lnL-only execute, the FP32-scaled form, the batched
+ * persistent kernel, on-device MC3 and the serving loop.  They have no
+ * counterpart in the reference; each says what it adds.
+ *
+ * Error convention: CxLikQDecomp returns true on error (as the reference);
+ * every cxg* function returns 0 on success and a negative CXG_E* code on
+ * error; cxgLastError() gives a message for the most recent failure,
+ * including failures inside the void CxLikExecute.
+ */
+#ifndef CXLIK_GPU_H
+#define CXLIK_GPU_H
+
+#include <stdbool.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Part 1: drop-in structures (lib/Crux/Tree/CxLik.h:6-273).                 */
+/* ------------------------------------------------------------------------ */
+
+typedef struct CxsLikCL CxtLikCL;
+typedef struct CxsLikModel CxtLikModel;
+
+/* Conditional-likelihood (CL) cache of one directed half-edge
+ * (CxLik.h:9-60).  cLMat holds mschars rows of dim*ncomp doubles for an
+ * internal node, or mschars rows of dim doubles (0/1 state indicators) for a
+ * leaf.  This library treats the host cLMat/lnScale pointers as identities
+ * of device-resident buffers: internal CLs live only on the device and the
+ * host buffers are neither read nor written; leaf rows are read once, on
+ * first use, unless cxgLikClSetLeafMasks registered them. */
+struct CxsLikCL {
+    double *cLMat;
+    double *lnScale;
+    bool valid;
+    CxtLikCL *parent;
+    unsigned nSibs;
+    double edgeLen;
+};
+
+/* Mixture component (CxLik.h:64-81). */
+typedef struct {
+    CxtLikModel *model;
+    double weightScaled;
+    double cweight;
+    double cmult;
+} CxtLikComp;
+
+/* Mixture model (CxLik.h:90-139). */
+struct CxsLikModel {
+    bool decomp;
+    double weight;
+    double qNorm;
+    double rmult;
+    unsigned *rclass;
+    double *rTri;
+    double *piDiag;
+    double *piDiagNorm;
+    double *qEigVecCube;
+    double *qEigVals;
+    double alpha;
+    bool catMedian;
+    bool invar;
+    unsigned comp0;
+    unsigned clen;
+};
+
+/* Step variants (CxLik.h:150-155). */
+typedef enum {
+    CxeLikStepComputeL = 0,
+    CxeLikStepComputeI = 1,
+    CxeLikStepMergeL = 2,
+    CxeLikStepMergeI = 3
+} CxeLikStep;
+
+/* One planned step (CxLik.h:168-174). */
+typedef struct {
+    CxeLikStep variant;
+    unsigned ntrail;
+    CxtLikCL *parentCL;
+    CxtLikCL *childCL;
+    double edgeLen;
+} CxtLikStep;
+
+/* The likelihood object (CxLik.h:176-273, built without CxmMpi). */
+typedef struct {
+    unsigned polarity;
+    unsigned dim;
+    unsigned rlen;
+    unsigned cbase;
+    unsigned nchars;
+    unsigned mschars;
+    unsigned npad;
+    unsigned *charFreqs;
+    unsigned stripeWidth;
+    unsigned nstripes;
+    bool invalidate;
+    bool resize;
+    bool reweight;
+    double wNorm;
+    CxtLikModel **models;
+    unsigned modelsLen;
+    unsigned modelsMax;
+    CxtLikComp *comps;
+    unsigned compsLen;
+    unsigned compsMax;
+    CxtLikCL *rootCLC;
+    double *siteLnL;
+    double *stripeLnL;
+    CxtLikStep *steps;
+    unsigned stepsLen;
+    unsigned stepsMax;
+} CxtLik;
+
+/* Replaces CxLikQDecomp (CxLik.h:279-281; definition CxLik.c:177-250, whose
+ * argument order -- qNorm before the cube -- is the one callers use,
+ * Lik.pyx:472-474).  Normalises PiDiag into PiDiagNorm, builds
+ * Q = R*Pi with zero row sums, sets qNorm = 1/(2*sum_{i<j} R_ij pi_i pi_j),
+ * and writes qEigVecCube[i][j][k] = V[i][k]*Vinv[k][j] and the n real
+ * eigenvalues.  The decomposition runs in FP64 on the GPU (symmetrised
+ * Jacobi; Q of a reversible model is similar to a symmetric matrix).
+ * Returns true on error (n != 4, non-positive frequency, no GPU). */
+bool CxLikQDecomp(int n, double *RTri, double *PiDiag, double *PiDiagNorm,
+                  double *qNorm, double *qEigVecCube, double *qEigVals);
+
+/* Replaces CxLikPt (CxLik.h:282-283; CxLik.c:258-292):
+ * P[i*n+j] = max(0, sum_k cube[i][j][k]*exp(eigVals[k]*v)).  Host FP64. */
+void CxLikPt(int n, double *P, double *qEigVecCube, double *qEigVals,
+             double v);
+
+/* Replaces CxLikExecute (CxLik.h:284-285; CxLik.c:914-968).  Runs the
+ * lik->steps plan on the GPU in FP64 with the reference's per-pattern
+ * scaler, then writes siteLnL[cbase .. cbase+mschars) and
+ * stripeLnL[0 .. nstripes).  Failures leave a message in cxgLastError(). */
+void CxLikExecute(CxtLik *lik);
+
+/* ------------------------------------------------------------------------ */
+/* Part 2: additions (no counterpart in the reference).                      */
+/* ------------------------------------------------------------------------ */
+
+enum {
+    CXG_OK = 0,
+    CXG_EINVAL = -1,   /* bad argument or unsupported shape */
+    CXG_ENOMEM = -2,   /* device or host allocation failed */
+    CXG_ECUDA = -3,    /* CUDA runtime error */
+    CXG_ETIMEOUT = -4, /* a bounded device wait gave up */
+    CXG_EBUSY = -5     /* admission refused (serving loop) */
+};
+
+/* Precision of a plan execution. */
+enum {
+    CXG_FP64 = 0,      /* plain: FP64 CLVs, the reference's scaler */
+    CXG_FP32 = 1       /* FP32 CLVs, per-pattern power-of-two exponents */
+};
+
+/* Message describing the most recent failure on the calling thread. */
+const char *cxgLastError(void);
+
+/* Library version and build facts: writes "cxlik_gpu <ver> sm_103a ..." */
+int cxgInfo(char *buf, size_t len);
+
+/* Register leaf CL `cl` (identified by cl->cLMat) with n per-pattern state
+ * masks (bit j set = state j allowed; 0 is treated as "any", as
+ * Lik.pyx:1469-1470).  Replaces the host upload of mschars*4 doubles. */
+int cxgLikClSetLeafMasks(const CxtLikCL *cl, const uint8_t *masks,
+                         unsigned n);
+
+/* Release the device buffers behind a host CL identity.  Call when the
+ * host cLMat is freed (CL.flush / CL.__dealloc__ in Lik.pyx:47-53, 98-107),
+ * so that a later allocation at the same address is not mistaken for it. */
+int cxgLikClForget(const double *cLMat);
+
+/* Release every device buffer and cached plan. */
+int cxgLikReset(void);
+
+/* Execute lik's plan at the given precision; write the compensated FP64
+ * sum of site lnLs to *lnL (one 8-byte device-to-host copy).  If siteLnL is
+ * non-NULL also fill it (mschars doubles, pad patterns included). */
+int cxgLikExecuteLnL(CxtLik *lik, int precision, double *lnL,
+                     double *siteLnL);
+
+/* Bytes copied host->device and device->host by the most recent
+ * cxgLikExecuteLnL / CxLikExecute (program upload; result read-back). */
+int cxgLikLastIo(size_t *h2d, size_t *d2h);
+
+/* Device memory currently held for CL buffers, in bytes. */
+int cxgLikDeviceBytes(size_t *bytes);
+
+/* A translated plan: lik->steps turned into a device program once and run
+ * any number of times (e.g. to time it, or to re-evaluate after changing
+ * nothing but branch lengths in the same CxtLikStep array -- call
+ * cxgPlanCreate again after any change).  The CL buffers the plan
+ * references must stay registered while it exists. */
+typedef struct cxgPlan cxgPlan;
+int cxgPlanCreate(CxtLik *lik, int precision, cxgPlan **plan);
+/* Run once and wait; lnL as cxgLikExecuteLnL. */
+int cxgPlanRun(cxgPlan *plan, double *lnL, double *siteLnL);
+/* Run `iters` times back to back on the device (no host sync between runs);
+ * report the mean wall time per run and the mean plan-walker kernel time,
+ * both from CUDA events on the library's stream, and the last lnL. */
+int cxgPlanTime(cxgPlan *plan, int iters, double *ms_per_run,
+                double *plan_kernel_ms, double *lnL);
+/* Pattern-node updates per run, algorithmic bytes of one plan-walker
+ * launch, node updates (ops) and kernels launched per run. */
+int cxgPlanInfo(const cxgPlan *plan, double *updates, double *alg_bytes,
+                unsigned *nops, unsigned *kernels_per_run);
+int cxgPlanDestroy(cxgPlan *plan);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CXLIK_GPU_H */
