@@ -53,6 +53,12 @@ def declare(lib):
     lib.cxgPlanInfo.restype = c_int
     lib.cxgPlanDestroy.argtypes = [vp]
     lib.cxgPlanDestroy.restype = c_int
+    lib.cxgPlanShape.argtypes = [vp, P(c_uint), P(c_uint), P(c_uint)]
+    lib.cxgPlanShape.restype = c_int
+    lib.cxgTune.argtypes = [c_uint, ctypes.c_size_t]
+    lib.cxgTune.restype = c_int
+    lib.cxgTuneGet.argtypes = [P(c_uint), P(ctypes.c_size_t)]
+    lib.cxgTuneGet.restype = c_int
     from . import _native_ext
     _native_ext.declare_ext(lib)
     return lib

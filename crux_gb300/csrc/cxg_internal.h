@@ -13,8 +13,16 @@ namespace cxg {
 // Patterns are padded to a multiple of this on the device, so that every
 // plane of a CL buffer starts on a 512-byte boundary.
 constexpr unsigned kPatternQuantum = 128;
-// Threads per CTA of the plan walkers.
+// Largest CTA of the plan walkers (one thread per pattern of the tile).
 constexpr unsigned kBlock = 128;
+// Default patterns per tile.
+constexpr unsigned kTile = 64;
+// Most shared-memory stack slots per tile.
+constexpr unsigned kMaxSlots = 16;
+// Op records in flight per CTA (bulk-copy ring depth).
+constexpr unsigned kRing = 4;
+// Iteration bound of every spin on an mbarrier.
+constexpr unsigned kSpinLimit = 1u << 26;
 // Largest number of active mixture components held in registers.
 constexpr unsigned kMaxComps = 8;
 // Largest node degree handled in one op (children per parent).
@@ -24,35 +32,60 @@ inline unsigned pad_patterns(unsigned p) {
     return (p + kPatternQuantum - 1) / kPatternQuantum * kPatternQuantum;
 }
 
-// One child of an op.  `data` is a CL buffer ([K][4][ppad] of the op's
-// precision) or, for a leaf, uint8 masks [ppad]; `scaler` is the child's
-// per-pattern log scale (FP64) or power-of-two exponent (FP32), null for a
-// leaf.  `pm` indexes the child's block of P matrices / leaf tables.
-struct DevChild {
+// Where a child's CL comes from during a plan walk.
+enum : uint32_t {
+    SRC_GLOBAL = 0,  // internal CL in HBM, computed by an earlier run
+    SRC_LEAF = 1,    // leaf masks, staged in shared memory per tile
+    SRC_SLOT = 2     // internal CL produced earlier in this run, still held
+                     // in the tile's shared-memory stack slot `idx`
+};
+
+// Op records.  The host packs every node update of a plan into one
+// fixed-stride record (rstride bytes, a multiple of 16), so that a CTA can
+// stream the records into shared memory with bulk copies ahead of use:
+//
+//   RecHead | RecChild[nchild] | T P[nchild][kact][16]
+//
+// The P matrices are filled in place by the P-matrix kernel of each run.
+struct RecHead {
+    void *data;        // parent CL in HBM, [K][U][ppad] 16-byte units
+    void *scaler;      // parent scaler [ppad]
+    uint32_t nchild;
+    int32_t slot;      // stack slot keeping the result for a later op, or -1
+    uint32_t pad_[2];
+};
+
+// One child of an op.  `data`/`scaler` address the HBM copy (SRC_GLOBAL);
+// `idx` is the staged-leaf index (SRC_LEAF) or the stack slot (SRC_SLOT).
+struct RecChild {
     const void *data;
     const void *scaler;
-    uint32_t leaf;
-    uint32_t pm;
+    uint32_t src;
+    uint32_t idx;
+    uint32_t tab;      // FP64 plans: leaf-message table of this child
+    uint32_t pad_;
 };
 
-// One node update: the parent CL and the range of its children.
-struct DevOp {
-    void *data;
-    void *scaler;
-    uint32_t child0;
-    uint32_t nchild;
-};
+static_assert(sizeof(RecHead) == 32, "record header is 32 bytes");
+static_assert(sizeof(RecChild) == 32, "record child is 32 bytes");
 
-// Per-call constants of a plan execution.
+// Per-call constants of a plan execution.  CL buffers in HBM are
+// [K][U][ppad] 16-byte units (U = 1 for FP32: states 0-3; U = 2 for FP64:
+// states 0-1, 2-3), so that one thread per pattern moves whole units and a
+// warp writes 512 contiguous bytes per store.
 struct PlanArgs {
-    const DevOp *ops;
-    const DevChild *children;
+    const unsigned char *rec;      // [nops][rstride] op records
+    const uint8_t *const *leaves;  // [nleaf] mask arrays staged per tile
+    uint32_t rstride;
+    uint32_t ring;        // records in flight per CTA
     uint32_t nops;
+    uint32_t nleaf;
+    uint32_t nslot;       // shared-memory stack slots per tile
+    uint32_t tile;        // patterns per CTA (== blockDim.x)
     uint32_t kact;        // active components (weightScaled != 0)
     uint32_t npat;        // patterns (mschars)
     uint32_t ppad;        // padded pattern stride
-    const void *pm;       // [nchild][kact][16] P matrices (double or float)
-    const void *ltab;     // [nchild][16 masks][kact][4] leaf messages
+    uint32_t root_last;   // the last op writes the root CL
     const double *pn;     // [kact][4] pi_i * weightScaled (root weights)
     const void *root;     // root CL buffer
     const void *rootsc;   // root scaler
@@ -62,24 +95,32 @@ struct PlanArgs {
     uint32_t *ninf;       // count of -inf sites
     unsigned *ticket;     // last-block counter
     double *total;        // [2] final (sum, compensation)
+    uint32_t *err;        // nonzero: a bounded wait gave up
+    const double *ltab;   // FP64 plans: [ntab][16 masks][kact][4]
 };
 
-// Inputs of the P-matrix kernel: one row per (child, active comp).
+size_t plan_smem_bytes(int precision, unsigned kact, unsigned tile,
+                       unsigned nslot, unsigned nleaf, unsigned ring,
+                       unsigned rstride);
+
+// Inputs of the P-matrix kernel: one thread per (child, active comp); the
+// P matrix (FP64 arithmetic, stored as the plan's precision) goes into the
+// child's op record at byte offset dst[child] + k * 16 * sizeof(T).
 struct PmatArgs {
     uint32_t nchild;
     uint32_t kact;
+    int precision;
     const double *edge_len;    // [nchild]
-    const uint32_t *leafflag;  // [nchild]
     const double *cmult;       // [kact]
     const double *rmult;       // [kact]
     const int32_t *model;      // [kact] model index of each active comp
     const double *cube;        // [nmodels][64]
     const double *eig;         // [nmodels][4]
+    const uint64_t *dst;       // [nchild] byte offsets into rec
+    const int32_t *tab;        // [nchild] leaf table index (FP64) or -1
     double wnorm;
-    double *pm64;              // [nchild][kact][16]
-    float *pm32;
-    double *ltab64;            // [nchild][16][kact][4]
-    float *ltab32;
+    unsigned char *rec;
+    double *ltab;              // FP64 plans: leaf-message tables
 };
 
 // Thread-local error message.
@@ -92,6 +133,6 @@ cudaError_t launch_pmat(const PmatArgs &a, cudaStream_t s);
 cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s);
 cudaError_t launch_qdecomp(const double *rtri, const double *pi, double *out,
                            cudaStream_t s);
-unsigned plan_blocks(unsigned ppad);
+unsigned plan_blocks(unsigned ppad, unsigned tile);
 
 }  // namespace cxg

@@ -1,21 +1,26 @@
 // Device kernels of the pruning likelihood on sm_103a.
 //
 // Layout in HBM: a CL buffer of K active components over ppad patterns is
-// state-planar, [K][4][ppad], so that the threads of a warp, one pattern
-// each, read and write 32 consecutive elements of a plane per instruction.
-// Leaves are one uint8 state mask per pattern.  Scalers are one FP64 log
-// scale (plain form) or one int32 power-of-two exponent (FP32 form) per
-// pattern.
+// [K][U][ppad] 16-byte units (FP32: U = 1, a float4 of the four states;
+// FP64: U = 2, two double2), so that the threads of a warp, one pattern
+// each, move 512 contiguous bytes per instruction.  Leaves are one uint8
+// state mask per pattern.  Scalers are one FP64 log scale (plain form) or
+// one int32 power-of-two exponent (FP32 form) per pattern.
 //
 // Kernels:
 //   pmat_kernel     P(t) = V diag(exp(lambda r t)) V^-1 per (child edge,
 //                   component), FP64, clipped at 0 (CxLik.c:258-292), plus
 //                   the 16-entry message table of every leaf child.
-//   plan_kernel<T>  walks the whole node-update list for one pattern per
-//                   thread (patterns are independent through the entire
-//                   post-order, CxLik.c:314-596, so no grid-wide sync is
-//                   needed), then aggregates the root (CxLik.c:598-632) and
-//                   reduces the weighted site lnLs with a compensated sum.
+//   walk_kernel<T>  one CTA per tile of patterns, one thread per pattern,
+//                   walks the whole node-update list (patterns are
+//                   independent through the entire post-order,
+//                   CxLik.c:314-596, so no grid-wide sync is needed).  CLs
+//                   produced and consumed within the walk stay in a
+//                   shared-memory stack (slots assigned by the host), so HBM
+//                   sees the write-through of every parent, the staged leaf
+//                   masks and CLs cached by earlier runs.  Then it
+//                   aggregates the root (CxLik.c:598-632) and reduces the
+//                   weighted site lnLs with a compensated sum.
 //   qdecomp_kernel  FP64 eigensystem of a reversible 4x4 Q by Jacobi
 //                   rotations of the symmetrised matrix (CxLik.c:59-250).
 #include <math.h>
@@ -25,7 +30,7 @@
 namespace cxg {
 
 // ---------------------------------------------------------------------------
-// P matrices and leaf message tables.
+// P matrices, written into the op records.
 // ---------------------------------------------------------------------------
 __global__ void pmat_kernel(PmatArgs a) {
     const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -52,29 +57,31 @@ __global__ void pmat_kernel(PmatArgs a) {
             P[i * 4 + j] = s < 0.0 ? 0.0 : s;
         }
     }
-    double *o64 = a.pm64 + ((size_t)c * a.kact + k) * 16;
-    float *o32 = a.pm32 + ((size_t)c * a.kact + k) * 16;
-#pragma unroll
-    for (int q = 0; q < 16; ++q) {
-        o64[q] = P[q];
-        o32[q] = (float)P[q];
-    }
-    if (a.leafflag[c]) {
-        // Message of a leaf with state mask m: sum over allowed states j of
-        // P[i][j], in j order -- exactly the reference's P * (0/1 vector).
+    const int tb = a.tab[c];
+    if (tb >= 0) {
+        // Message of a leaf with state mask m: the sum over allowed states j
+        // of P[i][j], in j order -- exactly P times the reference's 0/1 row.
         for (int mask = 0; mask < 16; ++mask) {
-            double *t64 = a.ltab64 + (((size_t)c * 16 + mask) * a.kact + k) * 4;
-            float *t32 = a.ltab32 + (((size_t)c * 16 + mask) * a.kact + k) * 4;
+            double *t = a.ltab + (((size_t)tb * 16 + mask) * a.kact + k) * 4;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                double s = 0.0;
+                double acc = 0.0;
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
-                    if (mask & (1 << j)) s = __dadd_rn(s, P[i * 4 + j]);
-                t64[i] = s;
-                t32[i] = (float)s;
+                    if (mask & (1 << j)) acc = __dadd_rn(acc, P[i * 4 + j]);
+                t[i] = acc;
             }
         }
+    }
+    unsigned char *dst = a.rec + a.dst[c];
+    if (a.precision == CXG_FP32) {
+        float *o = reinterpret_cast<float *>(dst) + (size_t)k * 16;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) o[q] = (float)P[q];
+    } else {
+        double *o = reinterpret_cast<double *>(dst) + (size_t)k * 16;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) o[q] = P[q];
     }
 }
 
@@ -116,6 +123,7 @@ __device__ void reduce_sites(const PlanArgs &a, double v, bool neg_inf) {
     __shared__ Comp warp_part[kBlock / 32];
     __shared__ unsigned ninf_block;
     __shared__ bool last;
+    const unsigned nwarp = blockDim.x / 32;
     if (threadIdx.x == 0) ninf_block = 0;
     __syncthreads();
     if (neg_inf) atomicAdd(&ninf_block, 1u);
@@ -125,7 +133,7 @@ __device__ void reduce_sites(const PlanArgs &a, double v, bool neg_inf) {
     __syncthreads();
     if (threadIdx.x == 0) {
         Comp b = warp_part[0];
-        for (unsigned w = 1; w < kBlock / 32; ++w) b = comp_add(b, warp_part[w]);
+        for (unsigned w = 1; w < nwarp; ++w) b = comp_add(b, warp_part[w]);
         a.partial[2 * blockIdx.x] = b.s;
         a.partial[2 * blockIdx.x + 1] = b.c;
         if (ninf_block) atomicAdd(a.ninf, ninf_block);
@@ -137,16 +145,17 @@ __device__ void reduce_sites(const PlanArgs &a, double v, bool neg_inf) {
     if (!last) return;
     __threadfence();
     Comp acc{0.0, 0.0};
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += kBlock) {
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
         const volatile double *pp = a.partial;
         acc = comp_add(acc, Comp{pp[2 * b], pp[2 * b + 1]});
     }
     acc = warp_comp(acc);
+    __syncthreads();
     if (lane == 0) warp_part[warp] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {
         Comp b = warp_part[0];
-        for (unsigned w = 1; w < kBlock / 32; ++w) b = comp_add(b, warp_part[w]);
+        for (unsigned w = 1; w < nwarp; ++w) b = comp_add(b, warp_part[w]);
         a.total[0] = b.s;
         a.total[1] = b.c;
         *a.ticket = 0;  // ready for the next launch
@@ -154,7 +163,7 @@ __device__ void reduce_sites(const PlanArgs &a, double v, bool neg_inf) {
 }
 
 // ---------------------------------------------------------------------------
-// Plan walkers.  T = double: plain form, the reference's scaler (max over
+// Plan walker.  T = double: plain form, the reference's scaler (max over
 // child messages, CxLik.c:390-403 and 577-588).  T = float: FP32 form, scale
 // by the power of two that puts the largest parent entry in [0.5, 1); the
 // exponent is an exact integer.
@@ -164,60 +173,257 @@ struct Prec;
 
 template <>
 struct Prec<double> {
-    typedef double S;  // scaler type
+    typedef double S;   // scaler type
+    typedef double2 V;  // 16-byte unit
+    static constexpr int U = 2;
 };
 
 template <>
 struct Prec<float> {
     typedef int S;
+    typedef float4 V;
+    static constexpr int U = 1;
 };
+
+__device__ __forceinline__ void unpack(const float4 v, float *x) {
+    x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+__device__ __forceinline__ float4 pack4(const float *x) {
+    return make_float4(x[0], x[1], x[2], x[3]);
+}
+__device__ __forceinline__ void unpack(const double2 v, double *x) {
+    x[0] = v.x; x[1] = v.y;
+}
+__device__ __forceinline__ double2 pack2(const double *x) {
+    return make_double2(x[0], x[1]);
+}
+
+// Four states of component k of a CL held as U units at `base` with unit
+// stride `stride` (HBM: ppad; shared memory: tile).
+template <typename T>
+__device__ __forceinline__ void load4(const typename Prec<T>::V *base,
+                                      size_t stride, T *x);
+template <>
+__device__ __forceinline__ void load4<float>(const float4 *base, size_t,
+                                             float *x) {
+    unpack(*base, x);
+}
+template <>
+__device__ __forceinline__ void load4<double>(const double2 *base,
+                                              size_t stride, double *x) {
+    unpack(base[0], x);
+    unpack(base[stride], x + 2);
+}
+template <typename T>
+__device__ __forceinline__ void store4(typename Prec<T>::V *base,
+                                       size_t stride, const T *x);
+template <>
+__device__ __forceinline__ void store4<float>(float4 *base, size_t,
+                                              const float *x) {
+    *base = pack4(x);
+}
+template <>
+__device__ __forceinline__ void store4<double>(double2 *base, size_t stride,
+                                               const double *x) {
+    base[0] = pack2(x);
+    base[stride] = pack2(x + 2);
+}
+// Read-only 16-byte load through the non-coherent path.
+__device__ __forceinline__ float4 ldro(const float4 *p) { return __ldg(p); }
+__device__ __forceinline__ double2 ldro(const double2 *p) { return __ldg(p); }
 
 __device__ __forceinline__ float pow2f(int n) {  // n in [-126, 127]
     return __int_as_float((n + 127) << 23);
 }
 
-template <typename T, int KT>
-__global__ void __launch_bounds__(kBlock) plan_kernel(PlanArgs a) {
-    typedef typename Prec<T>::S S;
-    const unsigned p = blockIdx.x * kBlock + threadIdx.x;
-    const size_t ppad = a.ppad;
-    const T *pm = static_cast<const T *>(a.pm);
-    const T *lt = static_cast<const T *>(a.ltab);
+// Shared memory of one CTA: record ring [ring][rstride], mbarriers,
+// stack slots [nslot][K][U][tile] units, slot scalers [nslot][tile], staged
+// leaf masks [nleaf][tile].
+struct SmemLayout {
+    size_t ring, bars, slots, slot_sc, masks, total;
+};
 
+static __host__ __device__ SmemLayout smem_layout(int precision, unsigned kact,
+                                                  unsigned tile, unsigned nslot,
+                                                  unsigned nleaf, unsigned ring,
+                                                  unsigned rstride) {
+    const size_t U = precision == CXG_FP32 ? 1 : 2;
+    const size_t sc = precision == CXG_FP32 ? 4 : 8;
+    SmemLayout L;
+    L.ring = 0;
+    L.bars = (size_t)ring * rstride;
+    L.slots = L.bars + ((ring * 8 + 15) & ~15u);
+    L.slot_sc = L.slots + (size_t)nslot * kact * U * tile * 16;
+    L.masks = L.slot_sc + (((size_t)nslot * tile * sc + 15) & ~(size_t)15);
+    L.total = L.masks + (size_t)nleaf * tile;
+    return L;
+}
+
+size_t plan_smem_bytes(int precision, unsigned kact, unsigned tile,
+                       unsigned nslot, unsigned nleaf, unsigned ring,
+                       unsigned rstride) {
+    return smem_layout(precision, kact, tile, nslot, nleaf, ring, rstride).total;
+}
+
+// --- mbarrier and bulk-copy primitives (PTX) --------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                     smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
+                                         uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Spin on a phase with an iteration bound; false if it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kSpinLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+template <typename T, int KT>
+__global__ void __launch_bounds__(kBlock) walk_kernel(PlanArgs a) {
+    typedef typename Prec<T>::S S;
+    typedef typename Prec<T>::V V;
+    constexpr int U = Prec<T>::U;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_ok;
+    const unsigned tile = blockDim.x;
+    const unsigned tid = threadIdx.x;
+    const unsigned p = blockIdx.x * tile + tid;
+    const size_t ppad = a.ppad;
+    const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT,
+                                       tile, a.nslot, a.nleaf, a.ring, a.rstride);
+    unsigned char *ring = smem + Lay.ring;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + Lay.bars);
+    V *slots = reinterpret_cast<V *>(smem + Lay.slots);
+    S *slot_sc = reinterpret_cast<S *>(smem + Lay.slot_sc);
+    uint8_t *masks = smem + Lay.masks;
+    const unsigned R = a.ring;
+
+    // Start streaming the first R op records.
+    if (tid == 0) {
+        for (unsigned r = 0; r < R; ++r) mbar_init(&bars[r], 1);
+        fence_mbar_init();
+        for (unsigned o = 0; o < R && o < a.nops; ++o) {
+            mbar_expect_tx(&bars[o], a.rstride);
+            bulk_g2s(ring + (size_t)o * a.rstride, a.rec + (size_t)o * a.rstride,
+                     a.rstride, &bars[o]);
+        }
+    }
+    // Stage this tile's leaf masks with 16-byte loads.
+    const unsigned chunks = tile / 16;
+    for (unsigned i = tid; i < a.nleaf * chunks; i += tile) {
+        const unsigned l = i / chunks, c = i % chunks;
+        const uint4 *src =
+            reinterpret_cast<const uint4 *>(a.leaves[l] + (size_t)blockIdx.x * tile) + c;
+        reinterpret_cast<uint4 *>(masks + (size_t)l * tile)[c] = __ldg(src);
+    }
+    __syncthreads();
+
+    T acc[KT * 4];
+    S lns = S(0);
     for (unsigned o = 0; o < a.nops; ++o) {
-        const DevOp op = a.ops[o];
-        T acc[KT * 4];
-        T sc = T(0);       // plain form: max over child messages
-        S lns = S(0);      // log scale (double) or exponent (int)
-        for (unsigned ci = 0; ci < op.nchild; ++ci) {
-            const DevChild ch = a.children[op.child0 + ci];
+        const unsigned stage = o % R;
+        if (tid == 0) s_ok = mbar_wait_bounded(&bars[stage], (o / R) & 1u);
+        __syncthreads();
+        if (!s_ok) {
+            if (tid == 0) atomicOr(a.err, 1u);
+            return;  // all threads leave together; the host reports CXG_ETIMEOUT
+        }
+        const unsigned char *rec = ring + (size_t)stage * a.rstride;
+        const RecHead *hd = reinterpret_cast<const RecHead *>(rec);
+        const RecChild *kids = reinterpret_cast<const RecChild *>(rec + sizeof(RecHead));
+        const unsigned nchild = hd->nchild;
+        const T *pmats = reinterpret_cast<const T *>(rec + sizeof(RecHead) +
+                                                     nchild * sizeof(RecChild));
+        T sc = T(0);  // plain form: max over child messages
+        lns = S(0);
+        for (unsigned ci = 0; ci < nchild; ++ci) {
+            const RecChild ch = kids[ci];
+            const V *P = reinterpret_cast<const V *>(pmats + (size_t)ci * KT * 16);
             T msg[KT * 4];
-            if (ch.leaf) {
-                const unsigned m = static_cast<const uint8_t *>(ch.data)[p];
-                const T *t = lt + ((size_t)ch.pm * 16 + m) * (KT * 4);
+            const bool leaf = (ch.src == SRC_LEAF);
+            const bool in_slot = (ch.src == SRC_SLOT);
+            const unsigned m = leaf ? masks[(size_t)ch.idx * tile + tid] : 0u;
+            const V *xs = in_slot ? slots + (size_t)ch.idx * KT * U * tile + tid
+                                  : static_cast<const V *>(ch.data) + p;
+            const size_t stride = in_slot ? tile : ppad;
 #pragma unroll
-                for (int q = 0; q < KT * 4; ++q) msg[q] = t[q];
-            } else {
-                const T *x = static_cast<const T *>(ch.data);
-                const T *P = pm + (size_t)ch.pm * (KT * 16);
+            if (sizeof(T) == 8 && leaf) {
+                // FP64 leaves: table lookup (no FP64 arithmetic).
+                const double2 *t = reinterpret_cast<const double2 *>(
+                    a.ltab + ((size_t)ch.tab * 16 + m) * (KT * 4));
 #pragma unroll
-                for (int k = 0; k < KT; ++k) {
-                    const T x0 = x[(k * 4 + 0) * ppad + p];
-                    const T x1 = x[(k * 4 + 1) * ppad + p];
-                    const T x2 = x[(k * 4 + 2) * ppad + p];
-                    const T x3 = x[(k * 4 + 3) * ppad + p];
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const T *r = P + k * 16 + i * 4;
-                        T v = r[0] * x0;
-                        v = fma(r[1], x1, v);
-                        v = fma(r[2], x2, v);
-                        v = fma(r[3], x3, v);
-                        msg[k * 4 + i] = v;
-                    }
+                for (int q = 0; q < KT * 2; ++q) {
+                    const double2 v = __ldg(t + q);
+                    msg[2 * q] = (T)v.x;
+                    msg[2 * q + 1] = (T)v.y;
                 }
-                const S l = static_cast<const S *>(ch.scaler)[p];
-                lns = (ci == 0) ? l : lns + l;
+            } else
+#pragma unroll
+            for (int k = 0; k < KT; ++k) {
+                T x[4];
+                if (leaf) {
+                    // Leaf rows are 0/1 state indicators (Lik.pyx:1466-1475):
+                    // P * indicator is exact, as in the reference.
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) x[j] = (T)((m >> j) & 1u);
+                } else {
+                    load4<T>(xs + (size_t)k * U * stride, stride, x);
+                }
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    T r[4];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        T tmp[4 / U];
+                        unpack(P[(k * 16 + i * 4) / (4 / U) + u], tmp);
+#pragma unroll
+                        for (int q = 0; q < 4 / U; ++q) r[u * (4 / U) + q] = tmp[q];
+                    }
+                    T v = r[0] * x[0];
+                    v = fma(r[1], x[1], v);
+                    v = fma(r[2], x[2], v);
+                    v = fma(r[3], x[3], v);
+                    msg[k * 4 + i] = v;
+                }
+            }
+            if (!leaf) {
+                const S l = in_slot ? slot_sc[(size_t)ch.idx * tile + tid]
+                                    : static_cast<const S *>(ch.scaler)[p];
+                lns = lns + l;
             }
             if (ci == 0) {
 #pragma unroll
@@ -230,6 +436,17 @@ __global__ void __launch_bounds__(kBlock) plan_kernel(PlanArgs a) {
 #pragma unroll
                 for (int q = 0; q < KT * 4; ++q) sc = fmax(sc, msg[q]);
             }
+        }
+        void *ydata = hd->data;
+        void *yscaler = hd->scaler;
+        const int yslot = hd->slot;
+        // Every thread has read the record: hand its stage to the next copy.
+        __syncthreads();
+        if (tid == 0 && o + R < a.nops) {
+            fence_proxy_async();
+            mbar_expect_tx(&bars[stage], a.rstride);
+            bulk_g2s(ring + (size_t)stage * a.rstride,
+                     a.rec + (size_t)(o + R) * a.rstride, a.rstride, &bars[stage]);
         }
         if (sizeof(T) == 8) {
             // Reference rescale: divide by the scaler unless it is 1, add
@@ -250,9 +467,9 @@ __global__ void __launch_bounds__(kBlock) plan_kernel(PlanArgs a) {
                 frexpf((float)mx, &e);
                 const int n = -e;
                 if (n >= -126 && n <= 127) {
-                    const float s = pow2f(n);
+                    const float s1 = pow2f(n);
 #pragma unroll
-                    for (int q = 0; q < KT * 4; ++q) acc[q] *= (T)s;
+                    for (int q = 0; q < KT * 4; ++q) acc[q] *= (T)s1;
                 } else {
                     const int n1 = n / 2, n2 = n - n1;
                     const float s1 = pow2f(n1), s2 = pow2f(n2);
@@ -262,26 +479,33 @@ __global__ void __launch_bounds__(kBlock) plan_kernel(PlanArgs a) {
                 lns = lns + (S)e;
             }
         }
-        T *y = static_cast<T *>(op.data);
+        V *y = static_cast<V *>(ydata) + p;
 #pragma unroll
-        for (int q = 0; q < KT * 4; ++q) y[q * ppad + p] = acc[q];
-        static_cast<S *>(op.scaler)[p] = lns;
+        for (int k = 0; k < KT; ++k) store4<T>(y + (size_t)k * U * ppad, ppad, acc + k * 4);
+        static_cast<S *>(yscaler)[p] = lns;
+        if (yslot >= 0) {
+            V *ys = slots + (size_t)yslot * KT * U * tile + tid;
+#pragma unroll
+            for (int k = 0; k < KT; ++k) store4<T>(ys + (size_t)k * U * tile, tile, acc + k * 4);
+            slot_sc[(size_t)yslot * tile + tid] = lns;
+        }
     }
 
     // Root aggregation (CxLik.c:598-632): L = sum_k sum_i pn[k][i] root.
-    const T *root = static_cast<const T *>(a.root);
+    if (!a.root_last) {
+        const V *r = static_cast<const V *>(a.root) + p;
+#pragma unroll
+        for (int k = 0; k < KT; ++k) load4<T>(r + (size_t)k * U * ppad, ppad, acc + k * 4);
+        lns = static_cast<const S *>(a.rootsc)[p];
+    }
     double L = 0.0;
 #pragma unroll
-    for (int k = 0; k < KT; ++k)
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-            L = fma(a.pn[k * 4 + i], (double)root[(k * 4 + i) * ppad + p], L);
-    const S rs = static_cast<const S *>(a.rootsc)[p];
+    for (int q = 0; q < KT * 4; ++q) L = fma(__ldg(a.pn + q), (double)acc[q], L);
     double v = 0.0;
     bool ninf = false;
     if (p < a.npat) {
-        const double lsc = (sizeof(T) == 8) ? (double)rs
-                                           : (double)rs * 0.69314718055994530942;
+        const double lsc = (sizeof(T) == 8) ? (double)lns
+                                           : (double)lns * 0.69314718055994530942;
         v = (log(L) + lsc) * (double)a.freqs[p];
         if (isnan(v)) v = -INFINITY;
         if (a.site) a.site[p] = v;
@@ -293,14 +517,28 @@ __global__ void __launch_bounds__(kBlock) plan_kernel(PlanArgs a) {
     reduce_sites(a, v, ninf);
 }
 
-unsigned plan_blocks(unsigned ppad) { return ppad / kBlock; }
+unsigned plan_blocks(unsigned ppad, unsigned tile) { return ppad / tile; }
 
 template <typename T>
-static cudaError_t launch_plan_t(const PlanArgs &a, cudaStream_t s) {
-    const unsigned nb = plan_blocks(a.ppad);
+static cudaError_t launch_plan_t(int precision, const PlanArgs &a,
+                                 cudaStream_t s) {
+    const unsigned nb = plan_blocks(a.ppad, a.tile);
+    const size_t sm = plan_smem_bytes(precision, a.kact, a.tile, a.nslot, a.nleaf,
+                                      a.ring, a.rstride);
     switch (a.kact) {
-#define CXG_K(K) \
-    case K: plan_kernel<T, K><<<nb, kBlock, 0, s>>>(a); break;
+#define CXG_K(K)                                                              \
+    case K: {                                                                 \
+        static size_t optin = 0;                                              \
+        if (sm > 48 * 1024 && sm > optin) {                                   \
+            cudaError_t e = cudaFuncSetAttribute(                             \
+                walk_kernel<T, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                (int)sm);                                                     \
+            if (e != cudaSuccess) return e;                                   \
+            optin = sm;                                                       \
+        }                                                                     \
+        walk_kernel<T, K><<<nb, a.tile, sm, s>>>(a);                          \
+        break;                                                                \
+    }
         CXG_K(1) CXG_K(2) CXG_K(3) CXG_K(4) CXG_K(5) CXG_K(6) CXG_K(7) CXG_K(8)
 #undef CXG_K
         default:
@@ -310,8 +548,11 @@ static cudaError_t launch_plan_t(const PlanArgs &a, cudaStream_t s) {
 }
 
 cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s) {
-    return precision == CXG_FP32 ? launch_plan_t<float>(a, s)
-                                 : launch_plan_t<double>(a, s);
+    if (a.tile == 0 || a.tile > kBlock || a.tile % 32 || a.ppad % a.tile ||
+        a.ring == 0 || a.rstride % 16 || a.rstride == 0)
+        return cudaErrorInvalidValue;
+    return precision == CXG_FP32 ? launch_plan_t<float>(precision, a, s)
+                                 : launch_plan_t<double>(precision, a, s);
 }
 
 // ---------------------------------------------------------------------------

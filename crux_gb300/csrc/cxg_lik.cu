@@ -253,7 +253,7 @@ static int internal_child(State &S, const CxtLik *lik, const CxtLikCL *cl,
 struct Plan {
     int prec = CXG_FP64;
     unsigned npat = 0, ppad = 0, kact = 0, nops = 0, nchild = 0;
-    DevBuf prog, pmat, ltab, partial, misc;
+    DevBuf prog, partial, misc, ltab;
     HostBuf out;
     DevCL *root = nullptr;
     std::vector<DevCL *> parents;
@@ -261,7 +261,13 @@ struct Plan {
     PlanArgs a;
     double alg_bytes = 0.0;   // algorithmic bytes of one plan-walker launch
     double updates = 0.0;     // pattern-node updates of one run
+    unsigned tile = kTile, nslot = 0, nleaf = 0;
 };
+
+// Launch shape of the plan walker: patterns per CTA and the shared-memory
+// budget of the CL stack (set by cxgTune).
+static unsigned g_tile = kTile;
+static size_t g_smem_budget = 24 * 1024;
 
 static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
     int rc;
@@ -297,10 +303,21 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
     }
 
     // Group steps into node updates.
-    std::vector<DevOp> ops;
-    std::vector<DevChild> kids;
+    struct HostOp {
+        void *data, *scaler;
+        uint32_t child0, nchild;
+        int slot;
+    };
+    struct HostChild {
+        const void *data, *scaler;
+        uint32_t src, idx;
+        int32_t tab;
+    };
+    std::vector<HostOp> ops;
+    std::vector<HostChild> kids;
     std::vector<double> elen;
-    std::vector<uint32_t> lflag;
+    std::vector<DevCL *> kid_cl;
+    int32_t ntab = 0;
     P.parents.clear();
     const CxtLikCL *cur_parent = nullptr;
     unsigned expect_trail = 0;
@@ -320,11 +337,12 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
             DevCL *pc = nullptr;
             rc = parent_buffer(S, st.parentCL, npat, kact, prec, &pc);
             if (rc) return rc;
-            DevOp op;
+            HostOp op;
             op.data = pc->data;
             op.scaler = pc->scaler;
             op.child0 = (uint32_t)kids.size();
             op.nchild = 0;
+            op.slot = -1;
             ops.push_back(op);
             P.parents.push_back(pc);
             cur_parent = st.parentCL;
@@ -341,16 +359,17 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
         if (rc) return rc;
         if (cc->data == P.parents.back()->data)
             return fail(CXG_EINVAL, "step reads its own parent");
-        DevChild ch;
+        HostChild ch;
         ch.data = cc->data;
         ch.scaler = leaf ? nullptr : cc->scaler;
-        ch.leaf = leaf ? 1u : 0u;
-        ch.pm = (uint32_t)kids.size();
+        ch.src = leaf ? SRC_LEAF : SRC_GLOBAL;
+        ch.idx = 0;
+        ch.tab = (leaf && prec == CXG_FP64) ? ntab++ : -1;
         kids.push_back(ch);
+        kid_cl.push_back(cc);
         elen.push_back(st.edgeLen);
-        lflag.push_back(ch.leaf);
         bytes += leaf ? 1.0 : 4.0 * kact * s_el + e_el;  // child read
-        if (ops.back().nchild + 1 > kMaxChildren)
+        if (ops.back().nchild + 1u > kMaxChildren)
             return fail(CXG_EINVAL, "node degree above 17");
         ops.back().nchild++;
         expect_trail = st.ntrail;
@@ -374,6 +393,82 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
     }
     bytes += 4.0 * kact * s_el + e_el + 4.0 + 8.0;  // root read, freq, site
 
+    // Staged leaves: each distinct leaf child once per tile.
+    std::vector<const uint8_t *> leaf_ptrs;
+    {
+        std::unordered_map<DevCL *, uint32_t> leaf_idx;
+        for (size_t c = 0; c < kids.size(); ++c) {
+            if (kids[c].src != SRC_LEAF) continue;
+            auto it = leaf_idx.find(kid_cl[c]);
+            if (it == leaf_idx.end()) {
+                it = leaf_idx.emplace(kid_cl[c], (uint32_t)leaf_ptrs.size()).first;
+                leaf_ptrs.push_back(static_cast<const uint8_t *>(kid_cl[c]->data));
+            }
+            kids[c].idx = it->second;
+        }
+    }
+    const unsigned tile = g_tile;
+    const unsigned nleaf = (unsigned)leaf_ptrs.size();
+
+    // Shared-memory stack: a parent keeps a slot until its one consumer (a
+    // later op of this run) reads it; with no free slot the oldest holder
+    // loses its slot and its consumer reads the HBM copy instead.
+    // Record stride: the largest op's header, children and P matrices.
+    const size_t elt = prec == CXG_FP32 ? 4 : 8;
+    size_t rstride = 16;
+    for (const HostOp &op : ops) {
+        size_t b = sizeof(RecHead) + op.nchild * (sizeof(RecChild) + kact * 16 * elt);
+        b = (b + 15) & ~(size_t)15;
+        if (b > rstride) rstride = b;
+    }
+    const unsigned ring = kRing;
+    const size_t base_bytes = plan_smem_bytes(prec, kact, tile, 0, 0, ring,
+                                              (unsigned)rstride);
+    const size_t slot_bytes =
+        plan_smem_bytes(prec, kact, tile, 1, 0, ring, (unsigned)rstride) - base_bytes;
+    const size_t leaf_bytes =
+        plan_smem_bytes(prec, kact, tile, 0, nleaf, ring, (unsigned)rstride);
+    unsigned cap = 0;
+    if (g_smem_budget > leaf_bytes)
+        cap = (unsigned)((g_smem_budget - leaf_bytes) / slot_bytes);
+    if (cap > kMaxSlots) cap = kMaxSlots;
+    unsigned used = 0;
+    {
+        std::vector<int> owner(cap, -1);                 // op holding slot
+        std::unordered_map<DevCL *, int> made;           // parent -> op
+        for (size_t o = 0; o < ops.size(); ++o) {
+            for (uint32_t c = ops[o].child0; c < ops[o].child0 + ops[o].nchild; ++c) {
+                if (kids[c].src == SRC_LEAF) continue;
+                auto it = made.find(kid_cl[c]);
+                if (it == made.end()) continue;          // from an earlier run
+                const int prod = it->second;
+                const int sl = ops[prod].slot;
+                if (sl >= 0 && owner[sl] == prod) {
+                    kids[c].src = SRC_SLOT;
+                    kids[c].idx = (uint32_t)sl;
+                    owner[sl] = -1;
+                }
+                made.erase(it);
+            }
+            if (o + 1 == ops.size() || cap == 0) continue;  // root: no slot
+            int sl = -1;
+            for (unsigned k = 0; k < cap && sl < 0; ++k)
+                if (owner[k] < 0) sl = (int)k;
+            if (sl < 0) {
+                int oldest = -1;
+                for (unsigned k = 0; k < cap; ++k)
+                    if (oldest < 0 || owner[k] < owner[oldest]) oldest = (int)k;
+                sl = oldest;
+            }
+            owner[sl] = (int)o;
+            ops[o].slot = sl;
+            made[P.parents[o]] = (int)o;
+            if ((unsigned)sl + 1 > used) used = (unsigned)sl + 1;
+        }
+    }
+    const unsigned nslot = used;
+    const bool root_last = !ops.empty() && P.parents.back() == P.root;
+
     // Pattern weights, cached by host pointer.
     const unsigned *fh = lik->charFreqs + lik->cbase;
     if (S.freqs.host != fh || S.freqs.n != npat) {
@@ -385,32 +480,58 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
         S.freqs.n = npat;
     }
 
-    // Pack the program: ops | kids | elen | lflag | cmult | rmult | model |
-    // cube | eig | pn, one pinned copy.
+    // Pack the program into pinned staging, one copy:
+    //   records [nops][rstride] | elen | cmult | rmult | model | cube | eig |
+    //   dst | pn | leaves
     const unsigned nchild = (unsigned)kids.size();
     const unsigned nmod = (unsigned)models.size();
     auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
-    size_t o_ops = 0;
-    size_t o_kids = al(o_ops + ops.size() * sizeof(DevOp));
-    size_t o_elen = al(o_kids + kids.size() * sizeof(DevChild));
-    size_t o_lflag = al(o_elen + elen.size() * 8);
-    size_t o_cm = al(o_lflag + lflag.size() * 4);
+    const size_t nrec = ops.empty() ? 1 : ops.size();
+    size_t o_rec = 0;
+    size_t o_elen = al(o_rec + nrec * rstride);
+    size_t o_cm = al(o_elen + elen.size() * 8);
     size_t o_rm = al(o_cm + kact * 8);
     size_t o_mod = al(o_rm + kact * 8);
     size_t o_cube = al(o_mod + kact * 4);
     size_t o_eig = al(o_cube + nmod * 64 * 8);
-    size_t o_pn = al(o_eig + nmod * 4 * 8);
-    size_t total = al(o_pn + kact * 4 * 8);
+    size_t o_dst = al(o_eig + nmod * 4 * 8);
+    size_t o_tab = al(o_dst + (size_t)nchild * 8);
+    size_t o_pn = al(o_tab + (size_t)nchild * 4);
+    size_t o_leaf = al(o_pn + kact * 4 * 8);
+    size_t total = al(o_leaf + (nleaf ? nleaf : 1) * sizeof(void *));
     rc = S.stage.ensure(total);
     if (rc) return rc;
     rc = P.prog.ensure(total);
     if (rc) return rc;
     char *h = static_cast<char *>(S.stage.p);
-    if (!ops.empty()) memcpy(h + o_ops, ops.data(), ops.size() * sizeof(DevOp));
-    if (!kids.empty())
-        memcpy(h + o_kids, kids.data(), kids.size() * sizeof(DevChild));
+    memset(h, 0, o_elen);
+    uint64_t *dsts = (uint64_t *)(h + o_dst);
+    for (size_t o = 0; o < ops.size(); ++o) {
+        char *r = h + o_rec + o * rstride;
+        RecHead hd;
+        memset(&hd, 0, sizeof(hd));
+        hd.data = ops[o].data;
+        hd.scaler = ops[o].scaler;
+        hd.nchild = ops[o].nchild;
+        hd.slot = ops[o].slot;
+        memcpy(r, &hd, sizeof(hd));
+        for (uint32_t ci = 0; ci < ops[o].nchild; ++ci) {
+            const HostChild &k = kids[ops[o].child0 + ci];
+            RecChild rc_;
+            memset(&rc_, 0, sizeof(rc_));
+            rc_.data = k.data;
+            rc_.scaler = k.scaler;
+            rc_.src = k.src;
+            rc_.idx = k.idx;
+            rc_.tab = k.tab < 0 ? 0u : (uint32_t)k.tab;
+            memcpy(r + sizeof(RecHead) + ci * sizeof(RecChild), &rc_, sizeof(rc_));
+            dsts[ops[o].child0 + ci] = o_rec + o * rstride + sizeof(RecHead) +
+                                       ops[o].nchild * sizeof(RecChild) +
+                                       ci * kact * 16 * elt;
+        }
+    }
     if (!elen.empty()) memcpy(h + o_elen, elen.data(), elen.size() * 8);
-    if (!lflag.empty()) memcpy(h + o_lflag, lflag.data(), lflag.size() * 4);
+    for (unsigned c = 0; c < nchild; ++c) ((int32_t *)(h + o_tab))[c] = kids[c].tab;
     for (unsigned k = 0; k < kact; ++k) {
         const CxtLikComp &cp = lik->comps[act[k]];
         ((double *)(h + o_cm))[k] = cp.cmult;
@@ -424,50 +545,53 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
         memcpy(h + o_cube + m * 64 * 8, models[m]->qEigVecCube, 64 * 8);
         memcpy(h + o_eig + m * 4 * 8, models[m]->qEigVals, 4 * 8);
     }
+    if (nleaf) memcpy(h + o_leaf, leaf_ptrs.data(), nleaf * sizeof(void *));
     char *d = static_cast<char *>(P.prog.p);
     CXG_CUDA(cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, S.stream));
     S.last_h2d = total;
     // The staging buffer is reused by the next translation: finish the copy.
     CXG_CUDA(cudaStreamSynchronize(S.stream));
 
-    rc = P.pmat.ensure((size_t)(nchild ? nchild : 1) * kact * 16 * 12);
-    if (rc) return rc;
-    rc = P.ltab.ensure((size_t)(nchild ? nchild : 1) * 16 * kact * 4 * 12);
-    if (rc) return rc;
     PmatArgs &pa = P.pa;
     pa.nchild = nchild;
     pa.kact = kact;
+    pa.precision = prec;
     pa.edge_len = (const double *)(d + o_elen);
-    pa.leafflag = (const uint32_t *)(d + o_lflag);
     pa.cmult = (const double *)(d + o_cm);
     pa.rmult = (const double *)(d + o_rm);
     pa.model = (const int32_t *)(d + o_mod);
     pa.cube = (const double *)(d + o_cube);
     pa.eig = (const double *)(d + o_eig);
+    pa.dst = (const uint64_t *)(d + o_dst);
+    pa.tab = (const int32_t *)(d + o_tab);
     pa.wnorm = lik->wNorm;
-    pa.pm64 = (double *)P.pmat.p;
-    pa.pm32 = (float *)((char *)P.pmat.p + (size_t)nchild * kact * 16 * 8);
-    pa.ltab64 = (double *)P.ltab.p;
-    pa.ltab32 = (float *)((char *)P.ltab.p + (size_t)nchild * 16 * kact * 4 * 8);
+    pa.rec = (unsigned char *)(d + o_rec);
+    rc = P.ltab.ensure((size_t)(ntab ? ntab : 1) * 16 * kact * 4 * 8);
+    if (rc) return rc;
+    pa.ltab = (double *)P.ltab.p;
 
-    const unsigned nb = plan_blocks(ppad);
+    const unsigned nb = plan_blocks(ppad, tile);
     rc = P.partial.ensure((size_t)nb * 16);
     if (rc) return rc;
-    // misc: ticket (4) | ninf (4) | pad (8) | total (16) | site (ppad*8)
+    // misc: ticket (4) | ninf (4) | err (4) | pad (4) | total (16) | site
     rc = P.misc.ensure(32 + (size_t)ppad * 8);
     if (rc) return rc;
     rc = P.out.ensure(32);
     if (rc) return rc;
     char *mp = static_cast<char *>(P.misc.p);
     PlanArgs &a = P.a;
-    a.ops = (const DevOp *)(d + o_ops);
-    a.children = (const DevChild *)(d + o_kids);
+    a.rec = (const unsigned char *)(d + o_rec);
+    a.rstride = (uint32_t)rstride;
+    a.ring = ring;
+    a.leaves = (const uint8_t *const *)(d + o_leaf);
+    a.nleaf = nleaf;
+    a.nslot = nslot;
+    a.tile = tile;
+    a.root_last = root_last ? 1u : 0u;
     a.nops = (uint32_t)ops.size();
     a.kact = kact;
     a.npat = npat;
     a.ppad = ppad;
-    a.pm = prec == CXG_FP32 ? (const void *)pa.pm32 : (const void *)pa.pm64;
-    a.ltab = prec == CXG_FP32 ? (const void *)pa.ltab32 : (const void *)pa.ltab64;
     a.pn = (const double *)(d + o_pn);
     a.root = P.root->data;
     a.rootsc = P.root->scaler;
@@ -476,7 +600,9 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
     a.partial = (double *)P.partial.p;
     a.ticket = (unsigned *)mp;
     a.ninf = (uint32_t *)(mp + 4);
+    a.err = (uint32_t *)(mp + 8);
     a.total = (double *)(mp + 16);
+    a.ltab = (const double *)P.ltab.p;
     P.prec = prec;
     P.npat = npat;
     P.ppad = ppad;
@@ -485,6 +611,9 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
     P.nchild = nchild;
     P.alg_bytes = bytes * npat;
     P.updates = (double)ops.size() * npat;
+    P.tile = tile;
+    P.nslot = nslot;
+    P.nleaf = nleaf;
     return 0;
 }
 
@@ -511,10 +640,14 @@ static int finish(State &S, Plan &P, double *lnL, double *site) {
     CXG_CUDA(cudaStreamSynchronize(S.stream));
     for (DevCL *p : P.parents) p->computed = true;
     const char *o = static_cast<const char *>(P.out.p);
-    uint32_t ninf;
+    uint32_t ninf, err;
     double tot[2];
     memcpy(&ninf, o + 4, 4);
+    memcpy(&err, o + 8, 4);
     memcpy(tot, o + 16, 16);
+    if (err)
+        return fail(CXG_ETIMEOUT,
+                    "plan walker: an op-record copy did not complete in time");
     if (lnL) *lnL = ninf ? -INFINITY : tot[0] + tot[1];
     return 0;
 }
@@ -585,6 +718,24 @@ int cxgLikReset(void) {
     S.cls.clear();
     S.freqs.host = nullptr;
     S.freqs.n = 0;
+    return 0;
+}
+
+int cxgTune(unsigned tile, size_t smem_budget) {
+    if (tile != 32 && tile != 64 && tile != 128)
+        return fail(CXG_EINVAL, "cxgTune: tile must be 32, 64 or 128");
+    if (smem_budget > 200 * 1024)
+        return fail(CXG_EINVAL, "cxgTune: shared-memory budget above 200 KiB");
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    g_tile = tile;
+    g_smem_budget = smem_budget;
+    return 0;
+}
+
+int cxgTuneGet(unsigned *tile, size_t *smem_budget) {
+    if (tile) *tile = g_tile;
+    if (smem_budget) *smem_budget = g_smem_budget;
     return 0;
 }
 
@@ -669,6 +820,15 @@ int cxgPlanTime(cxgPlan *h, int iters, double *ms_per_run,
     return finish(S, P, lnL, nullptr);
 }
 
+int cxgPlanShape(const cxgPlan *h, unsigned *tile, unsigned *nslot,
+                 unsigned *nleaf) {
+    if (h == nullptr) return fail(CXG_EINVAL, "cxgPlanShape: NULL plan");
+    if (tile) *tile = h->p.tile;
+    if (nslot) *nslot = h->p.nslot;
+    if (nleaf) *nleaf = h->p.nleaf;
+    return 0;
+}
+
 int cxgPlanInfo(const cxgPlan *h, double *updates, double *alg_bytes,
                 unsigned *nops, unsigned *kernels_per_run) {
     if (h == nullptr) return fail(CXG_EINVAL, "cxgPlanInfo: NULL plan");
@@ -686,7 +846,6 @@ int cxgPlanDestroy(cxgPlan *h) {
     cudaStreamSynchronize(S.stream);
     Plan &P = h->p;
     if (P.prog.p) cudaFree(P.prog.p);
-    if (P.pmat.p) cudaFree(P.pmat.p);
     if (P.ltab.p) cudaFree(P.ltab.p);
     if (P.partial.p) cudaFree(P.partial.p);
     if (P.misc.p) cudaFree(P.misc.p);

@@ -47,6 +47,13 @@ class Plan:
         return {"updates": up.value, "alg_bytes": by.value,
                 "nops": nops.value, "kernels_per_run": nk.value}
 
+    def shape(self):
+        t, n, l = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
+        self._check(self.lib.cxgPlanShape(self.h, ctypes.byref(t),
+                                          ctypes.byref(n), ctypes.byref(l)),
+                    "cxgPlanShape")
+        return {"tile": t.value, "nslot": n.value, "nleaf": l.value}
+
     def close(self):
         if self.h:
             self.lib.cxgPlanDestroy(self.h)

@@ -218,6 +218,16 @@ int cxgPlanTime(cxgPlan *plan, int iters, double *ms_per_run,
 int cxgPlanInfo(const cxgPlan *plan, double *updates, double *alg_bytes,
                 unsigned *nops, unsigned *kernels_per_run);
 int cxgPlanDestroy(cxgPlan *plan);
+/* Launch shape chosen for a plan: patterns per CTA, shared-memory stack
+ * slots, staged leaves. */
+int cxgPlanShape(const cxgPlan *plan, unsigned *tile, unsigned *nslot,
+                 unsigned *nleaf);
+
+/* Launch shape of the plan walker for plans translated from now on:
+ * patterns per CTA (32, 64 or 128) and the shared-memory budget of its CL
+ * stack (bytes, <= 200 KiB).  Chosen by the autotuner (crux_gb300.tune). */
+int cxgTune(unsigned tile, size_t smem_budget);
+int cxgTuneGet(unsigned *tile, size_t *smem_budget);
 
 #ifdef __cplusplus
 }

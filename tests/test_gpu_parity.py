@@ -230,6 +230,7 @@ def test_plan_handle_runs_and_times(gpu, port):
 
 def test_device_memory_released(gpu):
     import gc
+    gc.collect()
     before = ctypes.c_size_t()
     gpu.cxgLikDeviceBytes(ctypes.byref(before))
     case = synth.Case(20, 1500, 0.1, 51)
@@ -243,3 +244,24 @@ def test_device_memory_released(gpu):
     after = ctypes.c_size_t()
     gpu.cxgLikDeviceBytes(ctypes.byref(after))
     assert after.value == before.value
+
+
+import golden_cases as G  # noqa: E402
+
+
+@pytest.mark.parametrize("path", G.fixtures())
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_golden_fixtures(gpu, path, precision):
+    """Full lnL, site lnLs and dirty-path lnLs against the reference's own
+    outputs stored in tests/golden."""
+    fx = G.load(path)
+    lik = G.build_lik(fx, gpu, precision)
+    assert rel(lik.lnL(), fx["lnL"]) <= TOL[precision]
+    sites = np.array(lik.siteLnLs())
+    want = np.array(fx["siteLnL"])
+    assert np.all(np.abs(sites - want) <=
+                  TOL[precision] * np.maximum(1.0, np.abs(want)) * 10)
+    edges = lik.tree.edges
+    for i, f, w in fx["dirty"]:
+        edges[i].length *= f
+        assert rel(lik.lnL(), w) <= TOL[precision]
