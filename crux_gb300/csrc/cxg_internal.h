@@ -116,7 +116,7 @@ struct PmatArgs {
     const int32_t *model;      // [kact] model index of each active comp
     const double *cube;        // [nmodels][64]
     const double *eig;         // [nmodels][4]
-    const uint64_t *dst;       // [nchild] byte offsets into rec
+    const uint64_t *dst;       // [nchild] byte offsets from rec
     const int32_t *tab;        // [nchild] leaf table index (FP64) or -1
     double wnorm;
     unsigned char *rec;

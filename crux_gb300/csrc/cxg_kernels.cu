@@ -380,7 +380,6 @@ __global__ void __launch_bounds__(kBlock) walk_kernel(PlanArgs a) {
             const V *xs = in_slot ? slots + (size_t)ch.idx * KT * U * tile + tid
                                   : static_cast<const V *>(ch.data) + p;
             const size_t stride = in_slot ? tile : ppad;
-#pragma unroll
             if (sizeof(T) == 8 && leaf) {
                 // FP64 leaves: table lookup (no FP64 arithmetic).
                 const double2 *t = reinterpret_cast<const double2 *>(
@@ -391,7 +390,7 @@ __global__ void __launch_bounds__(kBlock) walk_kernel(PlanArgs a) {
                     msg[2 * q] = (T)v.x;
                     msg[2 * q + 1] = (T)v.y;
                 }
-            } else
+            } else {
 #pragma unroll
             for (int k = 0; k < KT; ++k) {
                 T x[4];
@@ -419,6 +418,7 @@ __global__ void __launch_bounds__(kBlock) walk_kernel(PlanArgs a) {
                     v = fma(r[3], x[3], v);
                     msg[k * 4 + i] = v;
                 }
+            }
             }
             if (!leaf) {
                 const S l = in_slot ? slot_sc[(size_t)ch.idx * tile + tid]

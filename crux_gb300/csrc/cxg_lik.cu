@@ -525,9 +525,13 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
             rc_.idx = k.idx;
             rc_.tab = k.tab < 0 ? 0u : (uint32_t)k.tab;
             memcpy(r + sizeof(RecHead) + ci * sizeof(RecChild), &rc_, sizeof(rc_));
-            dsts[ops[o].child0 + ci] = o_rec + o * rstride + sizeof(RecHead) +
-                                       ops[o].nchild * sizeof(RecChild) +
-                                       ci * kact * 16 * elt;
+            // Byte offset from the start of the records (pa.rec).
+            const size_t off = o * rstride + sizeof(RecHead) +
+                               ops[o].nchild * sizeof(RecChild) +
+                               ci * kact * 16 * elt;
+            if (off + kact * 16 * elt > (o + 1) * rstride)
+                return fail(CXG_EINVAL, "internal: P matrix outside its record");
+            dsts[ops[o].child0 + ci] = off;
         }
     }
     if (!elen.empty()) memcpy(h + o_elen, elen.data(), elen.size() * 8);
