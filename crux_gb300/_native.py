@@ -59,6 +59,10 @@ def declare(lib):
     lib.cxgTune.restype = c_int
     lib.cxgTuneGet.argtypes = [P(c_uint), P(ctypes.c_size_t)]
     lib.cxgTuneGet.restype = c_int
+    lib.cxgLikExecuteNoAlloc.argtypes = [P(_abi.CxtLik), c_int,
+                                         P(ctypes.c_uint32), P(c_double),
+                                         vp, P(c_double)]
+    lib.cxgLikExecuteNoAlloc.restype = c_int
     from . import _native_ext
     _native_ext.declare_ext(lib)
     return lib

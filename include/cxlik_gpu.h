@@ -229,6 +229,31 @@ int cxgPlanShape(const cxgPlan *plan, unsigned *tile, unsigned *nslot,
 int cxgTune(unsigned tile, size_t smem_budget);
 int cxgTuneGet(unsigned *tile, size_t *smem_budget);
 
+/* No counterpart in the reference.  Evaluate lik's plan without allocating
+ * anything, for callers that cannot call cudaMalloc.  Such a caller may
+ * own the device heap through its own pool or allocator, may be on a
+ * latency-critical path where cudaMalloc/cudaFree could synchronise the
+ * device, or may be about to capture the work into a CUDA graph.  Every
+ * memory the computation touches is the caller's:
+ *   - each CxtLikCL in lik->steps and lik->rootCLC holds DEVICE pointers:
+ *     internal CL: cLMat -> kact*4*ceil128(mschars) elements of the
+ *     precision (double or float) laid out [kact][U][ppad] in 16-byte
+ *     units, lnScale -> ppad scalers (double for CXG_FP64, int32 for
+ *     CXG_FP32; size the buffer for 8 bytes per pattern); leaf CL: cLMat
+ *     -> ppad uint8 state masks (pad patterns set to 15), lnScale unused;
+ *   - dFreqs: mschars uint32 pattern weights on the device;
+ *   - dSiteLnL: optional device output of mschars site lnLs (NULL: none);
+ *   - stream: the caller's cudaStream_t (NULL: the default stream).
+ * Scratch is a fixed 4 MiB device array in the library (every GPU that
+ * loads the library holds it until exit); limits: <= 1024 node updates,
+ * <= 2048 children, <= 2^20 patterns, <= 8 active components.  The first
+ * call on a device looks up that array's address: make it before any
+ * stream capture.  Calls share the array; calls that overlap on the GPU
+ * race.  Returns after the lnL has been copied back. */
+int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
+                         const uint32_t *dFreqs, double *dSiteLnL,
+                         void *stream, double *lnL);
+
 #ifdef __cplusplus
 }
 #endif
