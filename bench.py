@@ -327,6 +327,99 @@ def run_ours(args, dist):
     dist.close()
 
 
+BATCH = {"workload": "batch256_logu_taxa16-512_sites500-50000_gtr_gamma4",
+         "jobs": 256, "taxa": [16, 512], "sites": [500, 50000],
+         "mean_brlen": 0.1, "alpha": 0.5, "seed": 20261204}
+
+
+def make_batch_cases(n=None):
+    """The batched workload: jobs with log-uniform taxon and site counts,
+    each simulated under GTR+G4 with its own Dirichlet draws."""
+    import numpy as np
+    from crux_gb300 import synth
+    rng = np.random.default_rng(BATCH["seed"])
+    out = []
+    for j in range(n or BATCH["jobs"]):
+        nt = synth.log_uniform_int(rng, *BATCH["taxa"])
+        ns = synth.log_uniform_int(rng, *BATCH["sites"])
+        out.append(synth.Case(nt, ns, BATCH["mean_brlen"],
+                              int(rng.integers(1 << 30)), alpha=BATCH["alpha"]))
+    return out
+
+
+def run_batch(args, dist):
+    """Batched persistent kernel (FP32 form, one graph launch for all jobs)
+    against the same jobs issued one launch per node update in the plain
+    FP64 form."""
+    from crux_gb300 import _native
+    from crux_gb300.batch import Batch
+    gpu = _native.load()
+    t0 = time.perf_counter()
+    cases = make_batch_cases(args.jobs)
+    setup_s = time.perf_counter() - t0
+    res = {}
+    liks = {}
+    for prec, per_node in (("fp32", False), ("fp64", True), ("fp64", False)):
+        key = prec + ("_per_node" if per_node else "_batched")
+        if prec not in liks:
+            liks[prec] = [c.lik(lib=gpu, precision=prec) for c in cases]
+            for lk in liks[prec]:
+                lk.prepare_plan()
+        b = Batch(liks[prec], prec, per_node=per_node)
+        info = b.info()
+        lnls = b.run()
+        b.time(max(args.warmup, 3) if not per_node else 1)
+        clocks = Clocks()
+        if key == "fp32_batched":
+            clocks.start()
+        t = b.time(args.steps if not per_node else max(1, args.steps // 10))
+        ck = clocks.stop() if key == "fp32_batched" else None
+        b.close()
+        res[key] = {"info": info, "t": t, "lnL": lnls, "clocks": ck}
+    check = {}
+    if not args.no_cpu:
+        from oracle import oracle
+        port = oracle.load_port()
+        port.port_set_threads(os.cpu_count() or 1)
+        for j in range(0, len(cases), max(1, len(cases) // 8)):
+            want = cases[j].lik(lib=port).lnL()
+            for k, r in res.items():
+                e = abs(r["lnL"][j] - want) / abs(want)
+                check[k] = max(check.get(k, 0.0), e)
+    fb = res["fp32_batched"]
+    upd = fb["info"]["updates"]
+    peaks = measured_peaks()
+    hbm = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = fb["info"]["alg_bytes"] / (fb["t"]["walk_ms"] / 1e3) / 1e9
+    line = {
+        "metric": "CLV pattern-node updates/s (batched FP32-scaled form)",
+        "value": upd / (fb["t"]["ms_per_run"] / 1e3), "unit": UNIT,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": fb["t"]["ms_per_run"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": dict(BATCH, jobs=len(cases), updates_per_run=upd,
+                       items=fb["info"]["items"], grid=fb["info"]["grid"],
+                       setup_s=round(setup_s, 1)),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None},
+        "gpu_launches": args.steps * fb["info"]["launches_per_run"],
+        "clocks": fb["clocks"],
+        "fp64_per_node": {
+            "value": upd / (res["fp64_per_node"]["t"]["ms_per_run"] / 1e3),
+            "ms_per_run": res["fp64_per_node"]["t"]["ms_per_run"],
+            "launches_per_run": res["fp64_per_node"]["info"]["launches_per_run"]},
+        "fp64_batched": {
+            "value": upd / (res["fp64_batched"]["t"]["ms_per_run"] / 1e3),
+            "ms_per_run": res["fp64_batched"]["t"]["ms_per_run"]},
+        "speedup_vs_fp64_per_node":
+            res["fp64_per_node"]["t"]["ms_per_run"] / fb["t"]["ms_per_run"],
+        "rel_err_vs_fp64_oracle_max": check,
+    }
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -340,10 +433,16 @@ def main():
                     help="full-tree evaluations per step")
     ap.add_argument("--profile", action="store_true",
                     help="FP32 plan only, no e2e/CPU legs (for ncu)")
+    ap.add_argument("--workload", default="tree128",
+                    choices=["tree128", "batch256"])
+    ap.add_argument("--jobs", type=int, default=None,
+                    help="batch256: number of jobs (default 256)")
     args = ap.parse_args()
     dist = Dist()
     if args.impl == "reference":
         run_reference(args, dist)
+    elif args.workload == "batch256":
+        run_batch(args, dist)
     else:
         run_ours(args, dist)
 

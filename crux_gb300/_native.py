@@ -63,6 +63,18 @@ def declare(lib):
                                          P(ctypes.c_uint32), P(c_double),
                                          vp, P(c_double)]
     lib.cxgLikExecuteNoAlloc.restype = c_int
+    lib.cxgBatchCreate.argtypes = [P(P(_abi.CxtLik)), c_uint, c_int, c_uint,
+                                   P(vp)]
+    lib.cxgBatchCreate.restype = c_int
+    lib.cxgBatchRun.argtypes = [vp, P(c_double)]
+    lib.cxgBatchRun.restype = c_int
+    lib.cxgBatchTime.argtypes = [vp, c_int, P(c_double), P(c_double)]
+    lib.cxgBatchTime.restype = c_int
+    lib.cxgBatchInfo.argtypes = [vp, P(c_double), P(c_double), P(c_uint),
+                                 P(c_uint), P(ctypes.c_ulonglong)]
+    lib.cxgBatchInfo.restype = c_int
+    lib.cxgBatchDestroy.argtypes = [vp]
+    lib.cxgBatchDestroy.restype = c_int
     from . import _native_ext
     _native_ext.declare_ext(lib)
     return lib

@@ -97,11 +97,37 @@ struct PlanArgs {
     double *total;        // [2] final (sum, compensation)
     uint32_t *err;        // nonzero: a bounded wait gave up
     const double *ltab;   // FP64 plans: [ntab][16 masks][kact][4]
+    uint32_t ntiles;      // tiles of this job (ppad / tile)
+    uint32_t no_root;     // 1: stop after the ops (per-node launches)
+};
+
+// One (job, tile) work item of a batched launch.
+struct WalkItem {
+    uint32_t job;
+    uint32_t tile;
+};
+
+// A batched launch: a persistent grid claims items from `counter` (items
+// sorted longest first by the host); shared memory is laid out for the
+// largest job (nslot, nleaf, rstride maxima); all jobs share kact, tile and
+// the ring depth.
+struct BatchArgs {
+    const PlanArgs *jobs;
+    const WalkItem *items;
+    uint32_t nitems;
+    unsigned *counter;
+    uint32_t tile, ring, kact;
+    uint32_t max_nslot, max_nleaf, max_rstride;
 };
 
 size_t plan_smem_bytes(int precision, unsigned kact, unsigned tile,
                        unsigned nslot, unsigned nleaf, unsigned ring,
                        unsigned rstride);
+cudaError_t launch_batch(int precision, const BatchArgs &b, unsigned grid,
+                         cudaStream_t s);
+// Resident CTAs per SM of the batched walker for this shape.
+int batch_ctas_per_sm(int precision, unsigned kact, unsigned tile,
+                      size_t smem);
 
 // Inputs of the P-matrix kernel: one thread per (child, active comp); the
 // P matrix (FP64 arithmetic, stored as the plan's precision) goes into the
@@ -130,6 +156,8 @@ int cuda_fail(cudaError_t err, const char *what);
 
 // Kernel launchers (cxg_kernels.cu).
 cudaError_t launch_pmat(const PmatArgs &a, cudaStream_t s);
+cudaError_t launch_pmat_batch(const PmatArgs *jobs, const uint32_t *prefix,
+                              uint32_t njobs, uint32_t total, cudaStream_t s);
 cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s);
 cudaError_t launch_qdecomp(const double *rtri, const double *pi, double *out,
                            cudaStream_t s);

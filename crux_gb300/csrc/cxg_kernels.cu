@@ -32,9 +32,7 @@ namespace cxg {
 // ---------------------------------------------------------------------------
 // P matrices, written into the op records.
 // ---------------------------------------------------------------------------
-__global__ void pmat_kernel(PmatArgs a) {
-    const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= a.nchild * a.kact) return;
+__device__ __forceinline__ void pmat_one(const PmatArgs &a, unsigned idx) {
     const unsigned c = idx / a.kact, k = idx % a.kact;
     const int m = a.model[k];
     // Same association as the reference: ((edgeLen*cmult)*rmult)*wNorm.
@@ -85,6 +83,34 @@ __global__ void pmat_kernel(PmatArgs a) {
     }
 }
 
+__global__ void pmat_kernel(PmatArgs a) {
+    const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.nchild * a.kact) return;
+    pmat_one(a, idx);
+}
+
+// P matrices of many jobs in one launch: thread t belongs to the job whose
+// prefix range [prefix[j], prefix[j+1]) holds it.
+__global__ void pmat_batch_kernel(const PmatArgs *jobs, const uint32_t *prefix,
+                                  uint32_t njobs, uint32_t total) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    unsigned lo = 0, hi = njobs;  // find j with prefix[j] <= t < prefix[j+1]
+    while (hi - lo > 1) {
+        const unsigned mid = (lo + hi) / 2;
+        if (prefix[mid] <= t) lo = mid; else hi = mid;
+    }
+    pmat_one(jobs[lo], t - prefix[lo]);
+}
+
+cudaError_t launch_pmat_batch(const PmatArgs *jobs, const uint32_t *prefix,
+                              uint32_t njobs, uint32_t total, cudaStream_t s) {
+    if (total == 0) return cudaSuccess;
+    pmat_batch_kernel<<<(total + 127) / 128, 128, 0, s>>>(jobs, prefix, njobs,
+                                                          total);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pmat(const PmatArgs &a, cudaStream_t s) {
     const unsigned n = a.nchild * a.kact;
     if (n == 0) return cudaSuccess;
@@ -117,9 +143,11 @@ __device__ __forceinline__ Comp warp_comp(Comp v) {
     return v;
 }
 
-// Block sum of `v` (finite values; -inf sites are counted separately), then
-// the last block to finish folds all block partials into a.total.
-__device__ void reduce_sites(const PlanArgs &a, double v, bool neg_inf) {
+// Tile sum of `v` (finite values; -inf sites are counted separately) into
+// a.partial[tile]; the last tile of the job to finish folds all of the job's
+// partials into a.total.
+__device__ void reduce_sites(const PlanArgs &a, unsigned tile_idx, double v,
+                             bool neg_inf) {
     __shared__ Comp warp_part[kBlock / 32];
     __shared__ unsigned ninf_block;
     __shared__ bool last;
@@ -134,32 +162,34 @@ __device__ void reduce_sites(const PlanArgs &a, double v, bool neg_inf) {
     if (threadIdx.x == 0) {
         Comp b = warp_part[0];
         for (unsigned w = 1; w < nwarp; ++w) b = comp_add(b, warp_part[w]);
-        a.partial[2 * blockIdx.x] = b.s;
-        a.partial[2 * blockIdx.x + 1] = b.c;
+        a.partial[2 * tile_idx] = b.s;
+        a.partial[2 * tile_idx + 1] = b.c;
         if (ninf_block) atomicAdd(a.ninf, ninf_block);
         __threadfence();
         const unsigned t = atomicAdd(a.ticket, 1u);
-        last = (t == gridDim.x - 1);
+        last = (t == a.ntiles - 1);
     }
     __syncthreads();
-    if (!last) return;
-    __threadfence();
-    Comp acc{0.0, 0.0};
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-        const volatile double *pp = a.partial;
-        acc = comp_add(acc, Comp{pp[2 * b], pp[2 * b + 1]});
+    if (last) {
+        __threadfence();
+        Comp acc{0.0, 0.0};
+        for (unsigned b = threadIdx.x; b < a.ntiles; b += blockDim.x) {
+            const volatile double *pp = a.partial;
+            acc = comp_add(acc, Comp{pp[2 * b], pp[2 * b + 1]});
+        }
+        acc = warp_comp(acc);
+        __syncthreads();
+        if (lane == 0) warp_part[warp] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            Comp b = warp_part[0];
+            for (unsigned w = 1; w < nwarp; ++w) b = comp_add(b, warp_part[w]);
+            a.total[0] = b.s;
+            a.total[1] = b.c;
+            *a.ticket = 0;  // ready for the next launch
+        }
     }
-    acc = warp_comp(acc);
-    __syncthreads();
-    if (lane == 0) warp_part[warp] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        Comp b = warp_part[0];
-        for (unsigned w = 1; w < nwarp; ++w) b = comp_add(b, warp_part[w]);
-        a.total[0] = b.s;
-        a.total[1] = b.c;
-        *a.ticket = 0;  // ready for the next launch
-    }
+    __syncthreads();  // warp_part / last are reused by the next item
 }
 
 // ---------------------------------------------------------------------------
@@ -236,11 +266,12 @@ __device__ __forceinline__ float pow2f(int n) {  // n in [-126, 127]
     return __int_as_float((n + 127) << 23);
 }
 
-// Shared memory of one CTA: record ring [ring][rstride], mbarriers,
+// Shared memory of one CTA: mbarriers [ring], record ring [ring][rstride],
 // stack slots [nslot][K][U][tile] units, slot scalers [nslot][tile], staged
-// leaf masks [nleaf][tile].
+// leaf masks [nleaf][tile].  A batched launch lays it out for its largest
+// job; every job uses a prefix of each region.
 struct SmemLayout {
-    size_t ring, bars, slots, slot_sc, masks, total;
+    size_t bars, ring, slots, slot_sc, masks, total;
 };
 
 static __host__ __device__ SmemLayout smem_layout(int precision, unsigned kact,
@@ -250,9 +281,9 @@ static __host__ __device__ SmemLayout smem_layout(int precision, unsigned kact,
     const size_t U = precision == CXG_FP32 ? 1 : 2;
     const size_t sc = precision == CXG_FP32 ? 4 : 8;
     SmemLayout L;
-    L.ring = 0;
-    L.bars = (size_t)ring * rstride;
-    L.slots = L.bars + ((ring * 8 + 15) & ~15u);
+    L.bars = 0;
+    L.ring = ((size_t)ring * 8 + 127) & ~(size_t)127;
+    L.slots = L.ring + (size_t)ring * rstride;
     L.slot_sc = L.slots + (size_t)nslot * kact * U * tile * 16;
     L.masks = L.slot_sc + (((size_t)nslot * tile * sc + 15) & ~(size_t)15);
     L.total = L.masks + (size_t)nleaf * tile;
@@ -312,30 +343,33 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     return false;
 }
 
+// Walk every op of job `a` for tile `tile_idx` (one thread per pattern),
+// aggregate the root and reduce.  `phase` (thread 0 only) holds, per ring
+// stage, the parity of the next completion to wait for; it persists across
+// the items a CTA processes.  Returns false if a bounded wait gave up.
 template <typename T, int KT>
-__global__ void __launch_bounds__(kBlock) walk_kernel(PlanArgs a) {
+__device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
+                          const SmemLayout &Lay, unsigned ring_depth,
+                          uint32_t &phase) {
     typedef typename Prec<T>::S S;
     typedef typename Prec<T>::V V;
     constexpr int U = Prec<T>::U;
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_ok;
     const unsigned tile = blockDim.x;
     const unsigned tid = threadIdx.x;
-    const unsigned p = blockIdx.x * tile + tid;
+    const unsigned p = tile_idx * tile + tid;
     const size_t ppad = a.ppad;
-    const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT,
-                                       tile, a.nslot, a.nleaf, a.ring, a.rstride);
-    unsigned char *ring = smem + Lay.ring;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + Lay.bars);
+    unsigned char *ring = smem + Lay.ring;
     V *slots = reinterpret_cast<V *>(smem + Lay.slots);
     S *slot_sc = reinterpret_cast<S *>(smem + Lay.slot_sc);
     uint8_t *masks = smem + Lay.masks;
-    const unsigned R = a.ring;
+    const unsigned R = ring_depth;
 
-    // Start streaming the first R op records.
+    // Start streaming the job's first R op records.
     if (tid == 0) {
-        for (unsigned r = 0; r < R; ++r) mbar_init(&bars[r], 1);
-        fence_mbar_init();
+        fence_proxy_async();
         for (unsigned o = 0; o < R && o < a.nops; ++o) {
             mbar_expect_tx(&bars[o], a.rstride);
             bulk_g2s(ring + (size_t)o * a.rstride, a.rec + (size_t)o * a.rstride,
@@ -347,7 +381,7 @@ __global__ void __launch_bounds__(kBlock) walk_kernel(PlanArgs a) {
     for (unsigned i = tid; i < a.nleaf * chunks; i += tile) {
         const unsigned l = i / chunks, c = i % chunks;
         const uint4 *src =
-            reinterpret_cast<const uint4 *>(a.leaves[l] + (size_t)blockIdx.x * tile) + c;
+            reinterpret_cast<const uint4 *>(a.leaves[l] + (size_t)tile_idx * tile) + c;
         reinterpret_cast<uint4 *>(masks + (size_t)l * tile)[c] = __ldg(src);
     }
     __syncthreads();
@@ -356,11 +390,15 @@ __global__ void __launch_bounds__(kBlock) walk_kernel(PlanArgs a) {
     S lns = S(0);
     for (unsigned o = 0; o < a.nops; ++o) {
         const unsigned stage = o % R;
-        if (tid == 0) s_ok = mbar_wait_bounded(&bars[stage], (o / R) & 1u);
+        if (tid == 0) {
+            const uint32_t par = (phase >> stage) & 1u;
+            s_ok = mbar_wait_bounded(&bars[stage], par);
+            phase ^= 1u << stage;
+        }
         __syncthreads();
         if (!s_ok) {
             if (tid == 0) atomicOr(a.err, 1u);
-            return;  // all threads leave together; the host reports CXG_ETIMEOUT
+            return false;  // all threads leave together
         }
         const unsigned char *rec = ring + (size_t)stage * a.rstride;
         const RecHead *hd = reinterpret_cast<const RecHead *>(rec);
@@ -491,6 +529,10 @@ __global__ void __launch_bounds__(kBlock) walk_kernel(PlanArgs a) {
         }
     }
 
+    if (a.no_root) {
+        __syncthreads();
+        return true;
+    }
     // Root aggregation (CxLik.c:598-632): L = sum_k sum_i pn[k][i] root.
     if (!a.root_last) {
         const V *r = static_cast<const V *>(a.root) + p;
@@ -514,10 +556,64 @@ __global__ void __launch_bounds__(kBlock) walk_kernel(PlanArgs a) {
             v = 0.0;
         }
     }
-    reduce_sites(a, v, ninf);
+    reduce_sites(a, tile_idx, v, ninf);
+    return true;
+}
+
+__device__ __forceinline__ void init_ring(const SmemLayout &Lay, unsigned R) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    if (threadIdx.x == 0) {
+        uint64_t *bars = reinterpret_cast<uint64_t *>(smem + Lay.bars);
+        for (unsigned r = 0; r < R; ++r) mbar_init(&bars[r], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+}
+
+// One plan: one CTA per tile.
+template <typename T, int KT>
+__global__ void __launch_bounds__(kBlock) walk_kernel(PlanArgs a) {
+    const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT,
+                                       blockDim.x, a.nslot, a.nleaf, a.ring,
+                                       a.rstride);
+    init_ring(Lay, a.ring);
+    uint32_t phase = 0;
+    walk_tile<T, KT>(a, blockIdx.x, Lay, a.ring, phase);
+}
+
+// Many jobs: a persistent grid claims (job, tile) items in the host's order
+// (longest first).
+template <typename T, int KT>
+__global__ void __launch_bounds__(kBlock) walk_batch_kernel(BatchArgs b) {
+    __shared__ unsigned s_item;
+    const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT,
+                                       blockDim.x, b.max_nslot, b.max_nleaf,
+                                       b.ring, b.max_rstride);
+    init_ring(Lay, b.ring);
+    uint32_t phase = 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);
+        __syncthreads();
+        const unsigned item = s_item;
+        __syncthreads();
+        if (item >= b.nitems) break;
+        const WalkItem it = b.items[item];
+        if (!walk_tile<T, KT>(b.jobs[it.job], it.tile, Lay, b.ring, phase)) break;
+    }
 }
 
 unsigned plan_blocks(unsigned ppad, unsigned tile) { return ppad / tile; }
+
+template <typename Kern>
+static cudaError_t ensure_smem(Kern k, size_t sm, size_t &optin) {
+    if (sm > 48 * 1024 && sm > optin) {
+        cudaError_t e = cudaFuncSetAttribute(
+            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        optin = sm;
+    }
+    return cudaSuccess;
+}
 
 template <typename T>
 static cudaError_t launch_plan_t(int precision, const PlanArgs &a,
@@ -526,18 +622,13 @@ static cudaError_t launch_plan_t(int precision, const PlanArgs &a,
     const size_t sm = plan_smem_bytes(precision, a.kact, a.tile, a.nslot, a.nleaf,
                                       a.ring, a.rstride);
     switch (a.kact) {
-#define CXG_K(K)                                                              \
-    case K: {                                                                 \
-        static size_t optin = 0;                                              \
-        if (sm > 48 * 1024 && sm > optin) {                                   \
-            cudaError_t e = cudaFuncSetAttribute(                             \
-                walk_kernel<T, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                (int)sm);                                                     \
-            if (e != cudaSuccess) return e;                                   \
-            optin = sm;                                                       \
-        }                                                                     \
-        walk_kernel<T, K><<<nb, a.tile, sm, s>>>(a);                          \
-        break;                                                                \
+#define CXG_K(K)                                                           \
+    case K: {                                                              \
+        static size_t optin = 0;                                           \
+        cudaError_t e = ensure_smem(walk_kernel<T, K>, sm, optin);         \
+        if (e != cudaSuccess) return e;                                    \
+        walk_kernel<T, K><<<nb, a.tile, sm, s>>>(a);                       \
+        break;                                                             \
     }
         CXG_K(1) CXG_K(2) CXG_K(3) CXG_K(4) CXG_K(5) CXG_K(6) CXG_K(7) CXG_K(8)
 #undef CXG_K
@@ -549,10 +640,69 @@ static cudaError_t launch_plan_t(int precision, const PlanArgs &a,
 
 cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s) {
     if (a.tile == 0 || a.tile > kBlock || a.tile % 32 || a.ppad % a.tile ||
-        a.ring == 0 || a.rstride % 16 || a.rstride == 0)
+        a.ring == 0 || a.ring > 8 || a.rstride % 16 || a.rstride == 0 ||
+        a.ntiles != a.ppad / a.tile)
         return cudaErrorInvalidValue;
     return precision == CXG_FP32 ? launch_plan_t<float>(precision, a, s)
                                  : launch_plan_t<double>(precision, a, s);
+}
+
+template <typename T>
+static cudaError_t launch_batch_t(int precision, const BatchArgs &b,
+                                  unsigned grid, cudaStream_t s) {
+    const size_t sm = plan_smem_bytes(precision, b.kact, b.tile, b.max_nslot,
+                                      b.max_nleaf, b.ring, b.max_rstride);
+    switch (b.kact) {
+#define CXG_K(K)                                                           \
+    case K: {                                                              \
+        static size_t optin = 0;                                           \
+        cudaError_t e = ensure_smem(walk_batch_kernel<T, K>, sm, optin);   \
+        if (e != cudaSuccess) return e;                                    \
+        walk_batch_kernel<T, K><<<grid, b.tile, sm, s>>>(b);               \
+        break;                                                             \
+    }
+        CXG_K(1) CXG_K(2) CXG_K(3) CXG_K(4) CXG_K(5) CXG_K(6) CXG_K(7) CXG_K(8)
+#undef CXG_K
+        default:
+            return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch(int precision, const BatchArgs &b, unsigned grid,
+                         cudaStream_t s) {
+    if (b.tile == 0 || b.tile > kBlock || b.tile % 32 || b.ring == 0 ||
+        b.ring > 8 || b.max_rstride % 16 || b.max_rstride == 0 || grid == 0)
+        return cudaErrorInvalidValue;
+    return precision == CXG_FP32 ? launch_batch_t<float>(precision, b, grid, s)
+                                 : launch_batch_t<double>(precision, b, grid, s);
+}
+
+template <typename T>
+static int batch_occ_t(unsigned kact, unsigned tile, size_t smem) {
+    int n = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (kact) {
+#define CXG_K(K)                                                                \
+    case K: {                                                                   \
+        static size_t optin = 0;                                                \
+        e = ensure_smem(walk_batch_kernel<T, K>, smem, optin);                  \
+        if (e == cudaSuccess)                                                   \
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(                  \
+                &n, walk_batch_kernel<T, K>, (int)tile, smem);                  \
+        break;                                                                  \
+    }
+        CXG_K(1) CXG_K(2) CXG_K(3) CXG_K(4) CXG_K(5) CXG_K(6) CXG_K(7) CXG_K(8)
+#undef CXG_K
+        default:
+            break;
+    }
+    return e == cudaSuccess ? n : 0;
+}
+
+int batch_ctas_per_sm(int precision, unsigned kact, unsigned tile, size_t smem) {
+    return precision == CXG_FP32 ? batch_occ_t<float>(kact, tile, smem)
+                                 : batch_occ_t<double>(kact, tile, smem);
 }
 
 // ---------------------------------------------------------------------------

@@ -14,6 +14,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <string>
 #include <unordered_map>
@@ -88,11 +89,24 @@ struct HostBuf {
     }
 };
 
-struct FreqCache {
-    const unsigned *host = nullptr;
-    unsigned n = 0;
+// Pattern weights on the device, one buffer per (host pointer, length),
+// re-uploaded when the host content's hash changes.  Buffers are never
+// shared between keys, so plans of different Liks never see each other's
+// weights.
+struct FreqEntry {
     DevBuf dev;
+    uint64_t hash = 0;
 };
+
+static uint64_t hash_u32(const unsigned *p, unsigned n) {
+    uint64_t h = 0x9e3779b97f4a7c15ull ^ n;
+    for (unsigned i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 0x100000001b3ull;
+        h ^= h >> 29;
+    }
+    return h;
+}
 
 struct State {
     std::mutex mu;
@@ -103,7 +117,7 @@ struct State {
     size_t last_h2d = 0, last_d2h = 0;  // bytes copied by the last execute
     DevBuf misc;         // CxLikQDecomp in/out
     HostBuf stage, out;  // program staging, CxLikQDecomp staging
-    FreqCache freqs;
+    std::unordered_map<std::string, FreqEntry> freqs;
 };
 
 static State &state() {
@@ -269,7 +283,8 @@ struct Plan {
 static unsigned g_tile = kTile;
 static size_t g_smem_budget = 24 * 1024;
 
-static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
+static int translate(State &S, CxtLik *lik, int prec, Plan &P,
+                     bool use_slots = true) {
     int rc;
     if (lik == nullptr) return fail(CXG_EINVAL, "lik is NULL");
     if (lik->dim != 4)
@@ -432,6 +447,7 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
     if (g_smem_budget > leaf_bytes)
         cap = (unsigned)((g_smem_budget - leaf_bytes) / slot_bytes);
     if (cap > kMaxSlots) cap = kMaxSlots;
+    if (!use_slots) cap = 0;
     unsigned used = 0;
     {
         std::vector<int> owner(cap, -1);                 // op holding slot
@@ -469,15 +485,22 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
     const unsigned nslot = used;
     const bool root_last = !ops.empty() && P.parents.back() == P.root;
 
-    // Pattern weights, cached by host pointer.
+    // Pattern weights, one device copy per (host pointer, length).
     const unsigned *fh = lik->charFreqs + lik->cbase;
-    if (S.freqs.host != fh || S.freqs.n != npat) {
-        rc = S.freqs.dev.ensure((size_t)npat * 4);
-        if (rc) return rc;
-        CXG_CUDA(cudaMemcpy(S.freqs.dev.p, fh, (size_t)npat * 4,
-                            cudaMemcpyHostToDevice));
-        S.freqs.host = fh;
-        S.freqs.n = npat;
+    const void *dfreqs = nullptr;
+    {
+        char key[64];
+        snprintf(key, sizeof(key), "%p:%u", (const void *)fh, npat);
+        FreqEntry &fe = S.freqs[key];
+        const uint64_t hv = hash_u32(fh, npat);
+        if (fe.dev.p == nullptr || fe.hash != hv) {
+            rc = fe.dev.ensure((size_t)npat * 4);
+            if (rc) return rc;
+            CXG_CUDA(cudaMemcpy(fe.dev.p, fh, (size_t)npat * 4,
+                                cudaMemcpyHostToDevice));
+            fe.hash = hv;
+        }
+        dfreqs = fe.dev.p;
     }
 
     // Pack the program into pinned staging, one copy:
@@ -599,7 +622,7 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
     a.pn = (const double *)(d + o_pn);
     a.root = P.root->data;
     a.rootsc = P.root->scaler;
-    a.freqs = (const uint32_t *)S.freqs.dev.p;
+    a.freqs = (const uint32_t *)dfreqs;
     a.site = nullptr;
     a.partial = (double *)P.partial.p;
     a.ticket = (unsigned *)mp;
@@ -607,6 +630,8 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P) {
     a.err = (uint32_t *)(mp + 8);
     a.total = (double *)(mp + 16);
     a.ltab = (const double *)P.ltab.p;
+    a.ntiles = nb;
+    a.no_root = 0;
     P.prec = prec;
     P.npat = npat;
     P.ppad = ppad;
@@ -654,6 +679,19 @@ static int finish(State &S, Plan &P, double *lnL, double *site) {
                     "plan walker: an op-record copy did not complete in time");
     if (lnL) *lnL = ninf ? -INFINITY : tot[0] + tot[1];
     return 0;
+}
+
+static void free_plan(Plan &P) {
+    if (P.prog.p) cudaFree(P.prog.p);
+    if (P.ltab.p) cudaFree(P.ltab.p);
+    if (P.partial.p) cudaFree(P.partial.p);
+    if (P.misc.p) cudaFree(P.misc.p);
+    if (P.out.p) cudaFreeHost(P.out.p);
+    P.prog = DevBuf();
+    P.ltab = DevBuf();
+    P.partial = DevBuf();
+    P.misc = DevBuf();
+    P.out = HostBuf();
 }
 
 static Plan &scratch_plan() {
@@ -720,8 +758,9 @@ int cxgLikReset(void) {
     std::lock_guard<std::mutex> g(S.mu);
     for (auto &kv : S.cls) free_cl(S, kv.second);
     S.cls.clear();
-    S.freqs.host = nullptr;
-    S.freqs.n = 0;
+    for (auto &kv : S.freqs)
+        if (kv.second.dev.p) cudaFree(kv.second.dev.p);
+    S.freqs.clear();
     return 0;
 }
 
@@ -848,13 +887,87 @@ int cxgPlanDestroy(cxgPlan *h) {
     State &S = state();
     std::lock_guard<std::mutex> g(S.mu);
     cudaStreamSynchronize(S.stream);
-    Plan &P = h->p;
-    if (P.prog.p) cudaFree(P.prog.p);
-    if (P.ltab.p) cudaFree(P.ltab.p);
-    if (P.partial.p) cudaFree(P.partial.p);
-    if (P.misc.p) cudaFree(P.misc.p);
-    if (P.out.p) cudaFreeHost(P.out.p);
+    free_plan(h->p);
     delete h;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Batches: many translated plans run by one persistent launch.
+// ---------------------------------------------------------------------------
+struct cxgBatch {
+    int prec = CXG_FP64;
+    bool per_node = false;
+    std::vector<Plan *> plans;
+    DevBuf jobs, items, pmats, prefix, results;
+    HostBuf out;
+    BatchArgs args;
+    unsigned grid = 0, nitems = 0;
+    uint32_t pmat_total = 0;
+    double updates = 0.0, alg_bytes = 0.0;
+    unsigned long long launches = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+static void free_batch(cxgBatch *b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (Plan *p : b->plans) {
+        free_plan(*p);
+        delete p;
+    }
+    for (DevBuf *d : {&b->jobs, &b->items, &b->pmats, &b->prefix, &b->results})
+        if (d->p) cudaFree(d->p);
+    if (b->out.p) cudaFreeHost(b->out.p);
+    delete b;
+}
+
+// Enqueue one run of the batch.  e0/e1 (optional) bracket the walker.
+static int batch_enqueue(State &S, cxgBatch *b, cudaEvent_t e0 = nullptr,
+                         cudaEvent_t e1 = nullptr) {
+    const size_t n = b->plans.size();
+    CXG_CUDA(cudaMemsetAsync(b->results.p, 0, n * 32 + 16, S.stream));
+    CXG_CUDA(launch_pmat_batch(static_cast<const PmatArgs *>(b->pmats.p),
+                               static_cast<const uint32_t *>(b->prefix.p),
+                               (uint32_t)n, b->pmat_total, S.stream));
+    if (e0) CXG_CUDA(cudaEventRecord(e0, S.stream));
+    if (!b->per_node) {
+        CXG_CUDA(launch_batch(b->prec, b->args, b->grid, S.stream));
+    } else {
+        // The plain comparison: one launch per node update.
+        for (Plan *P : b->plans) {
+            for (unsigned o = 0; o < P->nops; ++o) {
+                PlanArgs a = P->a;
+                a.rec = P->a.rec + (size_t)o * P->a.rstride;
+                a.nops = 1;
+                a.no_root = (o + 1 < P->nops) ? 1u : 0u;
+                a.root_last = (o + 1 < P->nops) ? 0u : P->a.root_last;
+                CXG_CUDA(launch_plan(b->prec, a, S.stream));
+            }
+        }
+    }
+    if (e1) CXG_CUDA(cudaEventRecord(e1, S.stream));
+    CXG_CUDA(cudaMemcpyAsync(b->out.p, b->results.p, n * 32,
+                             cudaMemcpyDeviceToHost, S.stream));
+    return 0;
+}
+
+static int batch_finish(State &S, cxgBatch *b, double *lnLs) {
+    CXG_CUDA(cudaStreamSynchronize(S.stream));
+    const char *o = static_cast<const char *>(b->out.p);
+    for (size_t j = 0; j < b->plans.size(); ++j) {
+        uint32_t ninf, err;
+        double tot[2];
+        memcpy(&ninf, o + j * 32 + 4, 4);
+        memcpy(&err, o + j * 32 + 8, 4);
+        memcpy(tot, o + j * 32 + 16, 16);
+        if (err)
+            return fail(CXG_ETIMEOUT,
+                        "batched walker: an op-record copy did not complete");
+        if (lnLs) lnLs[j] = ninf ? -INFINITY : tot[0] + tot[1];
+        for (DevCL *p : b->plans[j]->parents) p->computed = true;
+    }
     return 0;
 }
 
@@ -876,6 +989,214 @@ void CxLikExecute(CxtLik *lik) {
             acc += lik->siteLnL[lik->cbase + c];
         lik->stripeLnL[s] = acc;
     }
+}
+
+int cxgBatchCreate(CxtLik *const *liks, unsigned n, int precision,
+                   unsigned flags, cxgBatch **out) {
+    if (out == nullptr || liks == nullptr || n == 0)
+        return fail(CXG_EINVAL, "cxgBatchCreate: bad arguments");
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    int rc = ensure_ready(S);
+    if (rc) return rc;
+    cxgBatch *b = new cxgBatch();
+    b->prec = precision;
+    b->per_node = (flags & CXG_BATCH_PER_NODE) != 0;
+    unsigned kact = 0, max_nslot = 0, max_nleaf = 0, max_rstride = 16;
+    for (unsigned j = 0; j < n; ++j) {
+        Plan *P = new Plan();
+        b->plans.push_back(P);
+        rc = translate(S, liks[j], precision, *P, !b->per_node);
+        if (rc) {
+            free_batch(b);
+            return rc;
+        }
+        if (j == 0) kact = P->kact;
+        if (P->kact != kact) {
+            free_batch(b);
+            return fail(CXG_EINVAL,
+                        "cxgBatchCreate: jobs must share the number of active "
+                        "components (group them by K)");
+        }
+        if (P->nslot > max_nslot) max_nslot = P->nslot;
+        if (P->nleaf > max_nleaf) max_nleaf = P->nleaf;
+        if (P->a.rstride > max_rstride) max_rstride = P->a.rstride;
+        b->updates += P->updates;
+        b->alg_bytes += P->alg_bytes;
+        b->launches += P->nops;
+    }
+    // Per-job results live side by side: [ticket ninf err pad total] x n,
+    // then the work counter.
+    if ((rc = b->results.ensure((size_t)n * 32 + 16)) ||
+        (rc = b->out.ensure((size_t)n * 32)) ||
+        (rc = b->jobs.ensure((size_t)n * sizeof(PlanArgs))) ||
+        (rc = b->pmats.ensure((size_t)n * sizeof(PmatArgs))) ||
+        (rc = b->prefix.ensure((size_t)(n + 1) * 4))) {
+        free_batch(b);
+        return rc;
+    }
+    std::vector<PlanArgs> jobs(n);
+    std::vector<PmatArgs> pm(n);
+    std::vector<uint32_t> prefix(n + 1, 0);
+    std::vector<WalkItem> items;
+    char *res = static_cast<char *>(b->results.p);
+    for (unsigned j = 0; j < n; ++j) {
+        PlanArgs a = b->plans[j]->a;
+        a.ticket = (unsigned *)(res + (size_t)j * 32);
+        a.ninf = (uint32_t *)(res + (size_t)j * 32 + 4);
+        a.err = (uint32_t *)(res + (size_t)j * 32 + 8);
+        a.total = (double *)(res + (size_t)j * 32 + 16);
+        a.site = nullptr;
+        b->plans[j]->a = a;
+        jobs[j] = a;
+        pm[j] = b->plans[j]->pa;
+        prefix[j + 1] = prefix[j] + pm[j].nchild * pm[j].kact;
+        for (unsigned t = 0; t < a.ntiles; ++t) items.push_back(WalkItem{j, t});
+    }
+    // Longest jobs first, so the persistent grid ends together.
+    std::stable_sort(items.begin(), items.end(),
+                     [&](const WalkItem &x, const WalkItem &y) {
+                         return jobs[x.job].nops > jobs[y.job].nops;
+                     });
+    b->nitems = (unsigned)items.size();
+    b->pmat_total = prefix[n];
+    if ((rc = b->items.ensure(items.size() * sizeof(WalkItem)))) {
+        free_batch(b);
+        return rc;
+    }
+    cudaError_t e;
+    if ((e = cudaMemcpy(b->jobs.p, jobs.data(), n * sizeof(PlanArgs),
+                        cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(b->pmats.p, pm.data(), n * sizeof(PmatArgs),
+                        cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(b->prefix.p, prefix.data(), (n + 1) * 4,
+                        cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(b->items.p, items.data(), items.size() * sizeof(WalkItem),
+                        cudaMemcpyHostToDevice)) != cudaSuccess) {
+        free_batch(b);
+        return cuda_fail(e, "cxgBatchCreate upload");
+    }
+    BatchArgs &ba = b->args;
+    ba.jobs = static_cast<const PlanArgs *>(b->jobs.p);
+    ba.items = static_cast<const WalkItem *>(b->items.p);
+    ba.nitems = b->nitems;
+    ba.counter = (unsigned *)(res + (size_t)n * 32);
+    ba.tile = b->plans[0]->tile;
+    ba.ring = kRing;
+    ba.kact = kact;
+    ba.max_nslot = max_nslot;
+    ba.max_nleaf = max_nleaf;
+    ba.max_rstride = max_rstride;
+    if (!b->per_node) {
+        const size_t smem = plan_smem_bytes(precision, kact, ba.tile, max_nslot,
+                                            max_nleaf, kRing, max_rstride);
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        const int per = batch_ctas_per_sm(precision, kact, ba.tile, smem);
+        if (per <= 0 || nsm <= 0) {
+            free_batch(b);
+            return fail(CXG_EINVAL, "cxgBatchCreate: walker does not fit an SM");
+        }
+        b->grid = (unsigned)(per * nsm);
+        b->launches = 1;
+        // Capture one run as a CUDA graph.
+        if ((e = cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal)) !=
+            cudaSuccess) {
+            free_batch(b);
+            return cuda_fail(e, "cudaStreamBeginCapture");
+        }
+        rc = batch_enqueue(S, b);
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(S.stream, &graph);
+        if (rc || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            free_batch(b);
+            return rc ? rc : cuda_fail(e, "cudaStreamEndCapture");
+        }
+        b->graph = graph;
+        if ((e = cudaGraphInstantiate(&b->exec, graph, 0)) != cudaSuccess) {
+            free_batch(b);
+            return cuda_fail(e, "cudaGraphInstantiate");
+        }
+    } else {
+        b->launches += 0;
+    }
+    *out = b;
+    return 0;
+}
+
+int cxgBatchRun(cxgBatch *b, double *lnLs) {
+    if (b == nullptr) return fail(CXG_EINVAL, "cxgBatchRun: NULL batch");
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    if (b->exec)
+        CXG_CUDA(cudaGraphLaunch(b->exec, S.stream));
+    else {
+        int rc = batch_enqueue(S, b);
+        if (rc) return rc;
+    }
+    return batch_finish(S, b, lnLs);
+}
+
+int cxgBatchTime(cxgBatch *b, int iters, double *ms_per_run,
+                 double *walk_ms) {
+    if (b == nullptr || iters < 1) return fail(CXG_EINVAL, "cxgBatchTime: bad args");
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    std::vector<cudaEvent_t> ev(2 * (size_t)iters + 2, nullptr);
+    for (auto &x : ev) CXG_CUDA(cudaEventCreate(&x));
+    int rc = 0;
+    cudaError_t ce = cudaEventRecord(ev[0], S.stream);
+    // Wall time per run through the graph (or the per-node launches).
+    for (int i = 0; i < iters && rc == 0 && ce == cudaSuccess; ++i) {
+        if (b->exec)
+            ce = cudaGraphLaunch(b->exec, S.stream);
+        else
+            rc = batch_enqueue(S, b);
+    }
+    if (rc == 0 && ce == cudaSuccess) ce = cudaEventRecord(ev[1], S.stream);
+    // Walker-only time, with events around the walker launch(es).
+    for (int i = 0; i < iters && rc == 0 && ce == cudaSuccess; ++i)
+        rc = batch_enqueue(S, b, ev[2 + 2 * i], ev[3 + 2 * i]);
+    if (rc == 0 && ce == cudaSuccess) ce = cudaStreamSynchronize(S.stream);
+    float tot = 0.0f;
+    double walk = 0.0;
+    if (rc == 0 && ce == cudaSuccess) {
+        ce = cudaEventElapsedTime(&tot, ev[0], ev[1]);
+        for (int i = 0; i < iters && ce == cudaSuccess; ++i) {
+            float k = 0.0f;
+            ce = cudaEventElapsedTime(&k, ev[2 + 2 * i], ev[3 + 2 * i]);
+            walk += k;
+        }
+    }
+    for (auto &x : ev) cudaEventDestroy(x);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return cuda_fail(ce, "cxgBatchTime events");
+    if (ms_per_run) *ms_per_run = tot / iters;
+    if (walk_ms) *walk_ms = walk / iters;
+    return batch_finish(S, b, nullptr);
+}
+
+int cxgBatchInfo(const cxgBatch *b, double *updates, double *alg_bytes,
+                 unsigned *nitems, unsigned *grid,
+                 unsigned long long *launches_per_run) {
+    if (b == nullptr) return fail(CXG_EINVAL, "cxgBatchInfo: NULL batch");
+    if (updates) *updates = b->updates;
+    if (alg_bytes) *alg_bytes = b->alg_bytes;
+    if (nitems) *nitems = b->nitems;
+    if (grid) *grid = b->grid;
+    if (launches_per_run) *launches_per_run = b->launches + 1;  // + P kernel
+    return 0;
+}
+
+int cxgBatchDestroy(cxgBatch *b) {
+    if (b == nullptr) return 0;
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    cudaStreamSynchronize(S.stream);
+    free_batch(b);
+    return 0;
 }
 
 bool CxLikQDecomp(int n, double *RTri, double *PiDiag, double *PiDiagNorm,

@@ -380,6 +380,8 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
     a.err = reinterpret_cast<uint32_t *>(dev + o_misc + 8);
     a.total = reinterpret_cast<double *>(dev + o_misc + 16);
     a.ltab = reinterpret_cast<const double *>(dev + o_ltab);
+    a.ntiles = nb;
+    a.no_root = 0;
     e = launch_plan(prec, a, st);
     if (e != cudaSuccess) return cuda_fail(e, "walk_kernel");
     e = cudaMemcpyAsync(g_na_result, dev + o_misc, 32, cudaMemcpyDeviceToHost, st);

@@ -763,6 +763,14 @@ class Lik:
             ret += self.stripeLnLBuf[i]
         return ret
 
+    def prepare_plan(self, root=None, full=True):
+        """Plan without executing (for plans and batches run elsewhere);
+        `full` re-plans every CL, as after a model change."""
+        if full:
+            self.lik.invalidate = True
+        self._prep(root)
+        return self.lik.stepsLen
+
     def flush(self):
         """Drop all cached CLs of this polarity (Lik.pyx:1765-1787)."""
         pol = self.lik.polarity

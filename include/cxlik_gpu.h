@@ -223,6 +223,26 @@ int cxgPlanDestroy(cxgPlan *plan);
 int cxgPlanShape(const cxgPlan *plan, unsigned *tile, unsigned *nslot,
                  unsigned *nleaf);
 
+/* A batch: the plans of many likelihoods (trees, alignments, models; all
+ * with the same number of active components) run by one persistent launch
+ * that walks (job, pattern-tile) items, longest jobs first; one run (P
+ * matrices, walker, result copy) is captured once as a CUDA graph and
+ * replayed.  CXG_BATCH_PER_NODE instead issues one walker launch per node
+ * update without the shared-memory stack -- the unfused comparison. */
+typedef struct cxgBatch cxgBatch;
+enum { CXG_BATCH_PER_NODE = 1 };
+int cxgBatchCreate(CxtLik *const *liks, unsigned n, int precision,
+                   unsigned flags, cxgBatch **batch);
+int cxgBatchRun(cxgBatch *batch, double *lnLs);
+/* Mean time per run over `iters` runs (graph launches back to back) and
+ * the mean event-timed walker time. */
+int cxgBatchTime(cxgBatch *batch, int iters, double *ms_per_run,
+                 double *walk_ms);
+int cxgBatchInfo(const cxgBatch *batch, double *updates, double *alg_bytes,
+                 unsigned *nitems, unsigned *grid,
+                 unsigned long long *launches_per_run);
+int cxgBatchDestroy(cxgBatch *batch);
+
 /* Launch shape of the plan walker for plans translated from now on:
  * patterns per CTA (32, 64 or 128) and the shared-memory budget of its CL
  * stack (bytes, <= 200 KiB).  Chosen by the autotuner (crux_gb300.tune). */
