@@ -14,7 +14,7 @@ ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libcxlik_gpu.so")
-SOURCES = ["cxg_kernels.cu", "cxg_lik.cu", "cxg_noalloc.cu"]
+SOURCES = ["cxg_kernels.cu", "cxg_lik.cu", "cxg_noalloc.cu", "cxg_mc3.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O3", "-I" + os.path.join(ROOT, "include"),
@@ -32,7 +32,7 @@ def _stale(obj, src):
     if not os.path.exists(obj):
         return True
     deps = [src] + [os.path.join(SRC, f) for f in os.listdir(SRC)
-                    if f.endswith(".h")] + [os.path.join(ROOT, "include",
+                    if f.endswith((".h", ".cuh"))] + [os.path.join(ROOT, "include",
                                                           "cxlik_gpu.h")]
     t = os.path.getmtime(obj)
     return any(os.path.getmtime(d) > t for d in deps)

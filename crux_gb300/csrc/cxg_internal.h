@@ -154,6 +154,18 @@ void set_error(const std::string &msg);
 int fail(int code, const std::string &msg);
 int cuda_fail(cudaError_t err, const char *what);
 
+#define CXG_CUDA(call)                                         \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cxg::cuda_fail(e_, #call); \
+    } while (0)
+
+#define CXG_CHECK_LAUNCH(what)                                 \
+    do {                                                       \
+        cudaError_t e_ = cudaGetLastError();                   \
+        if (e_ != cudaSuccess) return cxg::cuda_fail(e_, what);  \
+    } while (0)
+
 // Kernel launchers (cxg_kernels.cu).
 cudaError_t launch_pmat(const PmatArgs &a, cudaStream_t s);
 cudaError_t launch_pmat_batch(const PmatArgs *jobs, const uint32_t *prefix,

@@ -26,63 +26,13 @@
 #include <math.h>
 
 #include "cxg_internal.h"
+#include "cxg_device.cuh"
 
 namespace cxg {
 
 // ---------------------------------------------------------------------------
 // P matrices, written into the op records.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void pmat_one(const PmatArgs &a, unsigned idx) {
-    const unsigned c = idx / a.kact, k = idx % a.kact;
-    const int m = a.model[k];
-    // Same association as the reference: ((edgeLen*cmult)*rmult)*wNorm.
-    const double t = __dmul_rn(__dmul_rn(__dmul_rn(a.edge_len[c], a.cmult[k]),
-                                         a.rmult[k]), a.wnorm);
-    const double *cube = a.cube + (size_t)m * 64;
-    const double *ev = a.eig + (size_t)m * 4;
-    double ex[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) ex[q] = exp(__dmul_rn(ev[q], t));
-    double P[16];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            double s = 0.0;
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                s = __dadd_rn(s, __dmul_rn(cube[i * 16 + j * 4 + q], ex[q]));
-            P[i * 4 + j] = s < 0.0 ? 0.0 : s;
-        }
-    }
-    const int tb = a.tab[c];
-    if (tb >= 0) {
-        // Message of a leaf with state mask m: the sum over allowed states j
-        // of P[i][j], in j order -- exactly P times the reference's 0/1 row.
-        for (int mask = 0; mask < 16; ++mask) {
-            double *t = a.ltab + (((size_t)tb * 16 + mask) * a.kact + k) * 4;
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                double acc = 0.0;
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    if (mask & (1 << j)) acc = __dadd_rn(acc, P[i * 4 + j]);
-                t[i] = acc;
-            }
-        }
-    }
-    unsigned char *dst = a.rec + a.dst[c];
-    if (a.precision == CXG_FP32) {
-        float *o = reinterpret_cast<float *>(dst) + (size_t)k * 16;
-#pragma unroll
-        for (int q = 0; q < 16; ++q) o[q] = (float)P[q];
-    } else {
-        double *o = reinterpret_cast<double *>(dst) + (size_t)k * 16;
-#pragma unroll
-        for (int q = 0; q < 16; ++q) o[q] = P[q];
-    }
-}
-
 __global__ void pmat_kernel(PmatArgs a) {
     const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= a.nchild * a.kact) return;
@@ -703,94 +653,6 @@ static int batch_occ_t(unsigned kact, unsigned tile, size_t smem) {
 int batch_ctas_per_sm(int precision, unsigned kact, unsigned tile, size_t smem) {
     return precision == CXG_FP32 ? batch_occ_t<float>(kact, tile, smem)
                                  : batch_occ_t<double>(kact, tile, smem);
-}
-
-// ---------------------------------------------------------------------------
-// FP64 eigensystem of Q = R Pi (reversible, 4 states).
-// out: [0..3] piNorm, [4] qNorm, [5..68] cube, [69..72] eigenvalues,
-// [73] status (0 ok, 1 bad input, 2 no convergence).
-// ---------------------------------------------------------------------------
-__device__ void qdecomp4(const double *rtri, const double *pi, double *out) {
-    double pn[4], sq[4], q[16], s[16], u[16];
-    double psum = 0.0;
-    for (int i = 0; i < 4; ++i) psum += pi[i];
-    bool ok = true;
-    for (int i = 0; i < 4; ++i) {
-        pn[i] = pi[i] / psum;
-        ok = ok && (pn[i] > 0.0);
-    }
-    if (!ok) {
-        out[73] = 1.0;
-        return;
-    }
-    // Upper-triangle order of rtri: (0,1) (0,2) (0,3) (1,2) (1,3) (2,3).
-    const int tri[4][4] = {{-1, 0, 1, 2}, {0, -1, 3, 4}, {1, 3, -1, 5},
-                           {2, 4, 5, -1}};
-    double qscale = 0.0;
-    for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j) {
-            if (i == j) continue;
-            q[i * 4 + j] = rtri[tri[i][j]] * pn[j];
-            if (j < i) qscale += q[i * 4 + j] * pn[i] * 2.0;
-        }
-    for (int i = 0; i < 4; ++i) {
-        double d = 0.0;
-        for (int j = 0; j < 4; ++j)
-            if (j != i) d -= q[i * 4 + j];
-        q[i * 4 + i] = d;
-    }
-    for (int i = 0; i < 4; ++i) sq[i] = sqrt(pn[i]);
-    for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j)
-            s[i * 4 + j] = (i == j) ? q[i * 4 + i] : rtri[tri[i][j]] * sq[i] * sq[j];
-    for (int i = 0; i < 16; ++i) u[i] = (i % 5 == 0) ? 1.0 : 0.0;
-    int conv = 0;
-    for (int sweep = 0; sweep < 64 && !conv; ++sweep) {
-        double off = 0.0, dg = 0.0;
-        for (int i = 0; i < 4; ++i) {
-            dg += s[i * 4 + i] * s[i * 4 + i];
-            for (int j = i + 1; j < 4; ++j) off += s[i * 4 + j] * s[i * 4 + j];
-        }
-        if (off == 0.0 || off <= 1e-40 * dg) {
-            conv = 1;
-            break;
-        }
-        for (int pp = 0; pp < 3; ++pp)
-            for (int qq = pp + 1; qq < 4; ++qq) {
-                const double apq = s[pp * 4 + qq];
-                if (apq == 0.0) continue;
-                const double app = s[pp * 4 + pp], aqq = s[qq * 4 + qq];
-                const double th = (aqq - app) / (2.0 * apq);
-                const double t = (th >= 0.0 ? 1.0 : -1.0) /
-                                 (fabs(th) + sqrt(th * th + 1.0));
-                const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
-                for (int k = 0; k < 4; ++k) {
-                    const double akp = s[k * 4 + pp], akq = s[k * 4 + qq];
-                    s[k * 4 + pp] = c * akp - sn * akq;
-                    s[k * 4 + qq] = sn * akp + c * akq;
-                }
-                for (int k = 0; k < 4; ++k) {
-                    const double apk = s[pp * 4 + k], aqk = s[qq * 4 + k];
-                    s[pp * 4 + k] = c * apk - sn * aqk;
-                    s[qq * 4 + k] = sn * apk + c * aqk;
-                }
-                s[pp * 4 + qq] = s[qq * 4 + pp] = 0.0;
-                for (int k = 0; k < 4; ++k) {
-                    const double ukp = u[k * 4 + pp], ukq = u[k * 4 + qq];
-                    u[k * 4 + pp] = c * ukp - sn * ukq;
-                    u[k * 4 + qq] = sn * ukp + c * ukq;
-                }
-            }
-    }
-    for (int i = 0; i < 4; ++i) out[i] = pn[i];
-    out[4] = 1.0 / qscale;
-    for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j)
-            for (int k = 0; k < 4; ++k)
-                out[5 + i * 16 + j * 4 + k] =
-                    (u[i * 4 + k] / sq[i]) * (u[j * 4 + k] * sq[j]);
-    for (int k = 0; k < 4; ++k) out[69 + k] = s[k * 4 + k];
-    out[73] = conv ? 0.0 : 2.0;
 }
 
 __global__ void qdecomp_kernel(const double *rtri, const double *pi,

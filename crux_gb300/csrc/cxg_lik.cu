@@ -38,11 +38,6 @@ int cuda_fail(cudaError_t err, const char *what) {
     return CXG_ECUDA;
 }
 
-#define CXG_CUDA(call)                                       \
-    do {                                                     \
-        cudaError_t e_ = (call);                             \
-        if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
-    } while (0)
 
 enum { CL_INTERNAL = 0, CL_LEAF = 1 };
 

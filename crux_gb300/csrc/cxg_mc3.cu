@@ -1,0 +1,886 @@
+// On-device Metropolis-coupled MCMC (MC3) over the pruning likelihood.
+//
+// The reference runs each chain on the host: a proposal mutates the tree or
+// the model, Lik.lnL recomputes the dirty path, and a Metropolis test in
+// FP64 accepts or rejects it; chains swap heats every swapStride steps
+// (pkg/Crux/Mc3/Chain.pyx:438-476 brlenPropose, :320-377
+// rateShapeInvPropose, :1816-1911 advance0/advance1; heats
+// 1/(1 + ind * heatDelta), :51).  Here all chains live in HBM and one
+// generation is four kernels, captured together into a CUDA graph:
+//
+//   mc3_propose  one thread per chain: draw the move (Philox), apply it to
+//                the chain's tree or to the spare model slot, list the dirty
+//                internal nodes bottom-up, and write their op records.
+//                Dirty CLs go to each node's spare CL buffer, so a rejected
+//                move costs no restore.
+//   mc3_pmat     P matrices of every child edge of every chain's ops.
+//   walk_batch   the batched plan walker over (chain, pattern tile) items.
+//   mc3_accept   FP64 Metropolis per chain, then the heat swap; accepted
+//                moves flip the spare buffers in; rejected moves are undone.
+//
+// Moves (weights set by the caller): branch-length multiplier (as the
+// reference: m = exp(lambda (u - 1/2)), Exp(brlenPrior) prior, Hastings
+// ln m); NNI across a random internal edge (symmetric); GTR
+// exchangeabilities from a Dirichlet centred on the current values (flat
+// Dirichlet prior, Hastings from the two Dirichlet densities); the inverse
+// Gamma shape multiplier of the reference (rateShapeInvPropose, Exp(1)
+// prior on 1/alpha).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <mutex>
+#include <vector>
+
+#include "cxg_devmath.cuh"
+#include "cxg_device.cuh"
+#include "cxg_internal.h"
+
+namespace cxg {
+
+enum { MV_BRLEN = 0, MV_NNI = 1, MV_RATES = 2, MV_ALPHA = 3, MV_INIT = 4 };
+constexpr int kMoves = 4;
+
+struct Mc3Model {
+    double rates[6], freqs[4], alpha;
+    double pinorm[4], qnorm, cube[64], eig[4];
+    double cmult[kMaxComps], rmult[kMaxComps];
+    int32_t midx[kMaxComps];
+    double wnorm;
+    double pn[kMaxComps * 4];
+    int32_t ok;
+};
+
+struct Mc3Prop {
+    int32_t type, node, a, c;
+    double oldlen, lnPrior, lnHast;
+    int32_t model_changed, ndirty;
+};
+
+struct Mc3Dev {
+    uint32_t nchains, ntaxa, nnodes, root, kact, npat, ppad, prec;
+    uint32_t rstride, M, maxkids, ntiles;
+    int32_t *parent;      // [c][nnodes]
+    int32_t *child;       // [c][nnodes][3]
+    double *len;          // [c][nnodes]
+    uint8_t *cur;         // [c][nnodes]
+    uint8_t *dirtyflag;   // [c][nnodes]
+    int32_t *dirty;       // [c][M] dirty internal nodes, bottom-up
+    int32_t *stack;       // [c][nnodes] DFS scratch
+    void **cl_data;       // [c][M][2]
+    void **cl_sc;         // [c][M][2]
+    const uint8_t *const *leafmask;  // [ntaxa]
+    Mc3Model *model;      // [c][2]
+    uint8_t *curmodel;    // [c]
+    double *lnL, *heat;   // [c]
+    uint64_t seed;
+    uint64_t *gen;        // generation counter
+    Mc3Prop *prop;        // [c]
+    PlanArgs *jobs;       // [c]
+    unsigned char *rec;   // [c][M][rstride]
+    const uint8_t **leaves;  // [c][ntaxa]
+    double *kid_len;      // [c][maxkids]
+    uint64_t *kid_dst;    // [c][maxkids]
+    int32_t *kid_tab;     // [c][maxkids]
+    uint32_t *nkids;      // [c]
+    double *ltab;         // [c][maxkids][16][kact][4] (FP64 chains)
+    char *results;        // [c][32]
+    unsigned *counter;
+    double wcdf[kMoves];
+    double brlen_lambda, brlen_prior, rate_conc, alpha_lambda, alpha_prior;
+    uint32_t swap_stride;
+    uint32_t *acc, *rej;  // [c][kMoves]
+    uint32_t *nswap;      // [c]
+    double *trace;        // [trace_cap] cold-chain lnL after each generation
+    uint64_t trace_cap;
+    uint32_t *status;     // nonzero: a model could not be decomposed
+};
+
+// Model derived quantities: Q eigensystem (FP64 Jacobi on the device),
+// Gamma category rates, wNorm and the root weights (Lik.pyx:1603-1665).
+__device__ bool mc3_model_finish(Mc3Model &m, unsigned ncat) {
+    double tmp[74];
+    qdecomp4(m.rates, m.freqs, tmp);
+    if (tmp[73] != 0.0) return false;
+    for (int i = 0; i < 4; ++i) m.pinorm[i] = tmp[i];
+    m.qnorm = tmp[4];
+    for (int i = 0; i < 64; ++i) m.cube[i] = tmp[5 + i];
+    for (int i = 0; i < 4; ++i) m.eig[i] = tmp[69 + i];
+    if (ncat > 1) {
+        if (!d_gamma_rates(m.alpha, (int)ncat, m.cmult)) return false;
+    } else {
+        m.cmult[0] = 1.0;
+    }
+    double qmean = 0.0;
+    const double w = 1.0 / ncat;
+    for (unsigned k = 0; k < ncat; ++k) {
+        m.rmult[k] = 1.0;
+        m.midx[k] = 0;
+        if (m.cmult[k] != 0.0) qmean += w * (1.0 / m.qnorm);
+    }
+    m.wnorm = 1.0 / qmean;
+    for (unsigned k = 0; k < ncat; ++k)
+        for (int i = 0; i < 4; ++i) m.pn[k * 4 + i] = m.pinorm[i] * w;
+    m.ok = 1;
+    return true;
+}
+
+__global__ void mc3_init_kernel(Mc3Dev d) {
+    const unsigned c = blockIdx.x;
+    if (threadIdx.x != 0 || c >= d.nchains) return;
+    Mc3Model &m = d.model[c * 2 + d.curmodel[c]];
+    if (!mc3_model_finish(m, d.kact)) atomicOr(d.status, 1u);
+}
+
+// log density of Dirichlet(alpha) at x (both length n).
+__device__ double ln_dirichlet(const double *alpha, const double *x, int n) {
+    double s = 0.0, r = 0.0;
+    for (int i = 0; i < n; ++i) {
+        s += alpha[i];
+        r += (alpha[i] - 1.0) * log(x[i]) - lgamma(alpha[i]);
+    }
+    return r + lgamma(s);
+}
+
+__global__ void mc3_propose_kernel(Mc3Dev d) {
+    const unsigned c = blockIdx.x;
+    if (threadIdx.x != 0 || c >= d.nchains) return;
+    const uint64_t g = *d.gen;
+    const unsigned N = d.ntaxa, NN = d.nnodes, M = d.M;
+    int32_t *parent = d.parent + (size_t)c * NN;
+    int32_t *child = d.child + (size_t)c * NN * 3;
+    double *len = d.len + (size_t)c * NN;
+    uint8_t *cur = d.cur + (size_t)c * NN;
+    uint8_t *dflag = d.dirtyflag + (size_t)c * NN;
+    int32_t *dirty = d.dirty + (size_t)c * M;
+    int32_t *stack = d.stack + (size_t)c * NN;
+    Mc3Prop &pr = d.prop[c];
+    Philox rng;
+    philox_init(rng, d.seed, c, g);
+    if (c == 0) *d.counter = 0;
+    char *res = d.results + (size_t)c * 32;
+    *(uint32_t *)(res + 4) = 0;  // ninf
+    *(uint32_t *)(res + 8) = 0;  // err
+
+    const Mc3Model &m0 = d.model[c * 2 + d.curmodel[c]];
+    Mc3Model &m1 = d.model[c * 2 + (1 - d.curmodel[c])];
+    pr.model_changed = 0;
+    pr.lnPrior = 0.0;
+    pr.lnHast = 0.0;
+    bool full = false;
+    int lowest = -1;  // lowest dirty node of a path move
+    if (g == 0) {
+        pr.type = MV_INIT;
+        full = true;
+    } else {
+        const double u = philox_u01(rng);
+        int t = 0;
+        while (t < kMoves - 1 && u >= d.wcdf[t]) ++t;
+        if (t == MV_NNI && N < 4) t = MV_BRLEN;
+        if (t == MV_ALPHA && d.kact < 2) t = MV_BRLEN;
+        pr.type = t;
+        if (t == MV_BRLEN) {
+            // Uniform edge = uniform non-root node (Chain.pyx:442-447).
+            unsigned k = philox_below(rng, NN - 1);
+            const unsigned e = (k >= d.root) ? k + 1 : k;
+            const double lnM = d.brlen_lambda * (philox_u01(rng) - 0.5);
+            const double v0 = len[e], v1 = v0 * exp(lnM);
+            len[e] = v1;
+            pr.node = (int)e;
+            pr.oldlen = v0;
+            pr.lnPrior = -d.brlen_prior * (v1 - v0);
+            pr.lnHast = lnM;
+            lowest = parent[e];
+        } else if (t == MV_NNI) {
+            // Internal non-root node v, edge (v, p): swap a child a of v
+            // with a sibling c of v (another child of p).
+            unsigned k = philox_below(rng, M - 1);  // internal ids N..NN-1 minus root
+            unsigned v = N + k;
+            if (v >= d.root) ++v;
+            const int p = parent[v];
+            const int ai = (int)philox_below(rng, 2);
+            const int a = child[v * 3 + ai];
+            int sib[2], ns = 0;
+            for (int j = 0; j < 3; ++j) {
+                const int x = child[p * 3 + j];
+                if (x >= 0 && x != (int)v) sib[ns++] = x;
+            }
+            const int cc = sib[ns > 1 ? philox_below(rng, ns) : 0];
+            for (int j = 0; j < 3; ++j) {
+                if (child[v * 3 + j] == a) child[v * 3 + j] = cc;
+                if (child[p * 3 + j] == cc) child[p * 3 + j] = a;
+            }
+            parent[a] = p;
+            parent[cc] = (int)v;
+            pr.node = (int)v;
+            pr.a = a;
+            pr.c = cc;
+            lowest = (int)v;
+        } else if (t == MV_RATES) {
+            // Exchangeabilities ~ Dirichlet(conc * r / sum r).
+            double r0[6], r1[6], a0[6], a1[6], s0 = 0.0, s1 = 0.0;
+            for (int i = 0; i < 6; ++i) s0 += m0.rates[i];
+            for (int i = 0; i < 6; ++i) {
+                r0[i] = m0.rates[i] / s0;
+                a0[i] = d.rate_conc * r0[i];
+                r1[i] = philox_gamma(rng, a0[i]);
+                if (r1[i] < 1e-300) r1[i] = 1e-300;
+                s1 += r1[i];
+            }
+            for (int i = 0; i < 6; ++i) {
+                r1[i] /= s1;
+                a1[i] = d.rate_conc * r1[i];
+            }
+            m1 = m0;
+            for (int i = 0; i < 6; ++i) m1.rates[i] = r1[i] * 6.0;
+            pr.lnHast = ln_dirichlet(a1, r0, 6) - ln_dirichlet(a0, r1, 6);
+            pr.model_changed = 1;
+            full = true;
+        } else {
+            // Inverse Gamma shape multiplier (Chain.pyx:320-377).
+            const double lnM = d.alpha_lambda * (philox_u01(rng) - 0.5);
+            const double a0i = 1.0 / m0.alpha, a1i = a0i * exp(lnM);
+            m1 = m0;
+            m1.alpha = 1.0 / a1i;
+            pr.lnPrior = -d.alpha_prior * (a1i - a0i);
+            pr.lnHast = lnM;
+            pr.model_changed = 1;
+            full = true;
+        }
+        if (pr.model_changed && !mc3_model_finish(m1, d.kact)) {
+            // A model that cannot be decomposed is rejected outright.
+            pr.lnPrior = -INFINITY;
+            m1.ok = 0;
+        }
+    }
+
+    // Dirty internal nodes, children before parents.
+    int nd = 0;
+    if (full) {
+        // Iterative post-order from the root.
+        int sp = 0, top = 0;
+        stack[sp++] = (int)d.root;
+        while (sp > 0) {
+            const int v = stack[--sp];
+            dirty[top++] = v;  // pre-order (parents first), reversed below
+            for (int j = 0; j < 3; ++j) {
+                const int x = child[v * 3 + j];
+                if (x >= (int)N) stack[sp++] = x;
+            }
+        }
+        // Reversed pre-order is a valid post-order (children first).
+        for (int i = 0, j = top - 1; i < j; ++i, --j) {
+            const int t = dirty[i];
+            dirty[i] = dirty[j];
+            dirty[j] = t;
+        }
+        nd = top;
+    } else {
+        for (int v = lowest; v >= 0; v = parent[v]) dirty[nd++] = v;
+    }
+    pr.ndirty = nd;
+    for (int i = 0; i < nd; ++i) dflag[dirty[i]] = 1;
+
+    // Op records: parent -> its spare buffer; children -> spare buffer if
+    // dirty (computed earlier in this walk), else current.
+    const Mc3Model &mm = pr.model_changed ? m1 : m0;
+    const size_t elt = d.prec == CXG_FP32 ? 4 : 8;
+    unsigned char *rec = d.rec + (size_t)c * M * d.rstride;
+    const uint8_t **leaves = d.leaves + (size_t)c * N;
+    double *klen = d.kid_len + (size_t)c * d.maxkids;
+    uint64_t *kdst = d.kid_dst + (size_t)c * d.maxkids;
+    int32_t *ktab = d.kid_tab + (size_t)c * d.maxkids;
+    unsigned nkid = 0, nleaf = 0;
+    for (int o = 0; o < nd; ++o) {
+        const int v = dirty[o];
+        const int mi = v - (int)N;
+        unsigned char *r = rec + (size_t)o * d.rstride;
+        RecHead hd;
+        hd.data = d.cl_data[((size_t)c * M + mi) * 2 + (1 - cur[v])];
+        hd.scaler = d.cl_sc[((size_t)c * M + mi) * 2 + (1 - cur[v])];
+        unsigned nch = 0;
+        for (int j = 0; j < 3; ++j)
+            if (child[v * 3 + j] >= 0) ++nch;
+        hd.nchild = nch;
+        hd.slot = -1;
+        hd.pad_[0] = hd.pad_[1] = 0;
+        memcpy(r, &hd, sizeof(hd));
+        unsigned ci = 0;
+        for (int j = 0; j < 3; ++j) {
+            const int u = child[v * 3 + j];
+            if (u < 0) continue;
+            RecChild ch;
+            memset(&ch, 0, sizeof(ch));
+            if (u < (int)N) {
+                unsigned li = 0;
+                while (li < nleaf && leaves[li] != d.leafmask[u]) ++li;
+                if (li == nleaf) leaves[nleaf++] = d.leafmask[u];
+                ch.src = SRC_LEAF;
+                ch.idx = li;
+                ch.tab = nkid;
+                ktab[nkid] = d.prec == CXG_FP64 ? (int32_t)nkid : -1;
+            } else {
+                const int ui = u - (int)N;
+                const int b = dflag[u] ? 1 - cur[u] : cur[u];
+                ch.data = d.cl_data[((size_t)c * M + ui) * 2 + b];
+                ch.scaler = d.cl_sc[((size_t)c * M + ui) * 2 + b];
+                ch.src = SRC_GLOBAL;
+                ktab[nkid] = -1;
+            }
+            memcpy(r + sizeof(RecHead) + ci * sizeof(RecChild), &ch, sizeof(ch));
+            klen[nkid] = len[u];
+            kdst[nkid] = (size_t)o * d.rstride + sizeof(RecHead) +
+                         nch * sizeof(RecChild) + ci * d.kact * 16 * elt;
+            ++nkid;
+            ++ci;
+        }
+    }
+    d.nkids[c] = nkid;
+    PlanArgs &job = d.jobs[c];
+    job.nops = (uint32_t)nd;
+    job.nleaf = nleaf;
+    job.pn = mm.pn;
+}
+
+// P matrices of every chain's child edges: thread per (chain, kid, comp).
+__global__ void mc3_pmat_kernel(Mc3Dev d) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned per = d.maxkids * d.kact;
+    const unsigned c = t / per, r = t % per;
+    if (c >= d.nchains || r >= d.nkids[c] * d.kact) return;
+    const Mc3Prop &pr = d.prop[c];
+    const Mc3Model &mm = d.model[c * 2 + (pr.model_changed ? 1 - d.curmodel[c]
+                                                            : d.curmodel[c])];
+    PmatArgs a;
+    a.nchild = d.nkids[c];
+    a.kact = d.kact;
+    a.precision = (int)d.prec;
+    a.edge_len = d.kid_len + (size_t)c * d.maxkids;
+    a.cmult = mm.cmult;
+    a.rmult = mm.rmult;
+    a.model = mm.midx;
+    a.cube = mm.cube;
+    a.eig = mm.eig;
+    a.dst = d.kid_dst + (size_t)c * d.maxkids;
+    a.tab = d.kid_tab + (size_t)c * d.maxkids;
+    a.wnorm = mm.wnorm;
+    a.rec = d.rec + (size_t)c * d.M * d.rstride;
+    a.ltab = d.ltab + (size_t)c * d.maxkids * 16 * d.kact * 4;
+    pmat_one(a, r);
+}
+
+__global__ void mc3_accept_kernel(Mc3Dev d) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const uint64_t g = *d.gen;
+    const unsigned N = d.ntaxa, NN = d.nnodes;
+    for (unsigned c = 0; c < d.nchains; ++c) {
+        Mc3Prop &pr = d.prop[c];
+        const char *res = d.results + (size_t)c * 32;
+        const uint32_t ninf = *(const uint32_t *)(res + 4);
+        const double lnL1 = ninf ? -INFINITY
+                                 : ((const double *)(res + 16))[0] +
+                                       ((const double *)(res + 16))[1];
+        bool accept;
+        if (pr.type == MV_INIT) {
+            accept = true;
+        } else {
+            Philox rng;
+            philox_init(rng, d.seed, 0x40000000u + c, g);
+            const double u = philox_u01(rng);
+            // p = [(likelihood ratio)(prior ratio)]^heat * (Hastings ratio)
+            const double p =
+                exp(((lnL1 - d.lnL[c]) + pr.lnPrior) * d.heat[c] + pr.lnHast);
+            accept = (p >= u) && isfinite(lnL1);
+        }
+        uint8_t *cur = d.cur + (size_t)c * NN;
+        uint8_t *dflag = d.dirtyflag + (size_t)c * NN;
+        const int32_t *dirty = d.dirty + (size_t)c * d.M;
+        for (int i = 0; i < pr.ndirty; ++i) {
+            if (accept) cur[dirty[i]] ^= 1;
+            dflag[dirty[i]] = 0;
+        }
+        if (accept) {
+            d.lnL[c] = lnL1;
+            if (pr.model_changed) d.curmodel[c] ^= 1;
+            if (pr.type < kMoves) d.acc[c * kMoves + pr.type]++;
+        } else {
+            int32_t *parent = d.parent + (size_t)c * NN;
+            int32_t *child = d.child + (size_t)c * NN * 3;
+            if (pr.type == MV_BRLEN) {
+                d.len[(size_t)c * NN + pr.node] = pr.oldlen;
+            } else if (pr.type == MV_NNI) {
+                const int v = pr.node, a = pr.a, cc = pr.c;
+                const int p = parent[a];
+                for (int j = 0; j < 3; ++j) {
+                    if (child[v * 3 + j] == cc) child[v * 3 + j] = a;
+                    if (child[p * 3 + j] == a) child[p * 3 + j] = cc;
+                }
+                parent[a] = v;
+                parent[cc] = p;
+            }
+            if (pr.type < kMoves) d.rej[c * kMoves + pr.type]++;
+        }
+        (void)N;
+    }
+    // Heat swap between a random pair (Chain.pyx:1874-1911).
+    if (d.nchains > 1 && g > 0 && g % d.swap_stride == 0) {
+        Philox rng;
+        philox_init(rng, d.seed, 0x7fffffffu, g);
+        const unsigned a = philox_below(rng, d.nchains);
+        unsigned b = philox_below(rng, d.nchains - 1);
+        if (b >= a) ++b;
+        const double u = philox_u01(rng);
+        const double p = exp((d.lnL[b] - d.lnL[a]) * d.heat[a] +
+                             (d.lnL[a] - d.lnL[b]) * d.heat[b]);
+        if (p >= u) {
+            const double t = d.heat[a];
+            d.heat[a] = d.heat[b];
+            d.heat[b] = t;
+            d.nswap[a]++;
+            d.nswap[b]++;
+        }
+    }
+    if (g < d.trace_cap) {
+        double cold = d.lnL[0];
+        for (unsigned c = 0; c < d.nchains; ++c)
+            if (d.heat[c] == 1.0) cold = d.lnL[c];
+        d.trace[g] = cold;
+    }
+    *d.gen = g + 1;
+}
+
+}  // namespace cxg
+
+using namespace cxg;
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+struct cxgMc3 {
+    Mc3Dev d;
+    cxgMc3Config cfg;
+    cudaStream_t stream = nullptr;
+    std::vector<void *> allocs;
+    BatchArgs ba;
+    unsigned grid = 0, pmat_grid = 0;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    unsigned graph_gens = 0;
+    double last_walk_ms = 0.0;
+};
+
+static std::mutex g_mc3_mu;
+
+static int mc3_alloc(cxgMc3 *h, void **p, size_t n) {
+    cudaError_t e = cudaMalloc(p, n ? n : 16);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(mc3)");
+    h->allocs.push_back(*p);
+    e = cudaMemset(*p, 0, n ? n : 16);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(mc3)");
+    return 0;
+}
+
+template <typename T>
+static int mc3_upload(cxgMc3 *h, T **dst, const T *src, size_t count) {
+    int rc = mc3_alloc(h, (void **)dst, count * sizeof(T));
+    if (rc) return rc;
+    if (src) {
+        cudaError_t e = cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(mc3)");
+    }
+    return 0;
+}
+
+static void mc3_free(cxgMc3 *h) {
+    if (h->exec) cudaGraphExecDestroy(h->exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    for (void *p : h->allocs) cudaFree(p);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+static int mc3_enqueue_gen(cxgMc3 *h) {
+    const Mc3Dev &d = h->d;
+    mc3_propose_kernel<<<d.nchains, 32, 0, h->stream>>>(d);
+    CXG_CHECK_LAUNCH("mc3_propose_kernel");
+    mc3_pmat_kernel<<<h->pmat_grid, 128, 0, h->stream>>>(d);
+    CXG_CHECK_LAUNCH("mc3_pmat_kernel");
+    cudaError_t e = launch_batch((int)d.prec, h->ba, h->grid, h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "walk_batch_kernel");
+    mc3_accept_kernel<<<1, 32, 0, h->stream>>>(d);
+    CXG_CHECK_LAUNCH("mc3_accept_kernel");
+    return 0;
+}
+
+extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
+    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    if (cfg == nullptr || out == nullptr) return fail(CXG_EINVAL, "cxgMc3Create: NULL");
+    const unsigned N = cfg->ntaxa;
+    if (N < 3 || N > 4096) return fail(CXG_EINVAL, "cxgMc3Create: 3..4096 taxa");
+    if (cfg->ncat < 1 || cfg->ncat > kMaxComps)
+        return fail(CXG_EINVAL, "cxgMc3Create: 1..8 rate categories");
+    if (cfg->nchains < 1 || cfg->nchains > 1024)
+        return fail(CXG_EINVAL, "cxgMc3Create: 1..1024 chains");
+    if (cfg->precision != CXG_FP32 && cfg->precision != CXG_FP64)
+        return fail(CXG_EINVAL, "unknown precision");
+    if (cfg->npat == 0) return fail(CXG_EINVAL, "cxgMc3Create: no patterns");
+    const unsigned NN = 2 * N - 2, M = N - 2;
+    if (cfg->root < N || cfg->root >= NN)
+        return fail(CXG_EINVAL, "cxgMc3Create: root must be an internal node");
+    // Children from the parent array; check a binary rooted tree.
+    std::vector<int32_t> child(NN * 3, -1);
+    std::vector<int> nch(NN, 0);
+    for (unsigned v = 0; v < NN; ++v) {
+        const int p = cfg->parent[v];
+        if (v == cfg->root) {
+            if (p != -1) return fail(CXG_EINVAL, "root has a parent");
+            continue;
+        }
+        if (p < (int)N || p >= (int)NN)
+            return fail(CXG_EINVAL, "parent of a node must be an internal node");
+        if (nch[p] >= 3) return fail(CXG_EINVAL, "node with more than 3 children");
+        child[p * 3 + nch[p]++] = (int)v;
+    }
+    for (unsigned v = N; v < NN; ++v)
+        if (nch[v] != (v == cfg->root ? 3 : 2))
+            return fail(CXG_EINVAL, "tree is not binary (root degree 3)");
+    cxgMc3 *h = new cxgMc3();
+    h->cfg = *cfg;
+    Mc3Dev &d = h->d;
+    memset(&d, 0, sizeof(d));
+    const unsigned C = cfg->nchains, K = cfg->ncat;
+    d.nchains = C;
+    d.ntaxa = N;
+    d.nnodes = NN;
+    d.root = cfg->root;
+    d.kact = K;
+    d.npat = cfg->npat;
+    d.ppad = pad_patterns(cfg->npat);
+    d.prec = (uint32_t)cfg->precision;
+    d.M = M;
+    d.maxkids = NN;  // children over all internal nodes: NN - 1
+    const size_t elt = cfg->precision == CXG_FP32 ? 4 : 8;
+    d.rstride = (uint32_t)((sizeof(RecHead) + 3 * (sizeof(RecChild) + K * 16 * elt) + 15) &
+                           ~(size_t)15);
+    unsigned tile = 0;
+    size_t budget = 0;
+    cxgTuneGet(&tile, &budget);
+    d.ntiles = d.ppad / tile;
+    d.seed = cfg->seed;
+    d.swap_stride = cfg->swap_stride ? cfg->swap_stride : 1;
+    double wsum = 0.0;
+    for (int i = 0; i < kMoves; ++i) wsum += cfg->move_weight[i];
+    if (!(wsum > 0.0)) {
+        mc3_free(h);
+        return fail(CXG_EINVAL, "cxgMc3Create: all move weights are zero");
+    }
+    double acc = 0.0;
+    for (int i = 0; i < kMoves; ++i) {
+        acc += cfg->move_weight[i] / wsum;
+        d.wcdf[i] = (i == kMoves - 1) ? 2.0 : acc;
+    }
+    d.brlen_lambda = cfg->brlen_lambda;
+    d.brlen_prior = cfg->brlen_prior;
+    d.rate_conc = cfg->rate_conc;
+    d.alpha_lambda = cfg->alpha_lambda;
+    d.alpha_prior = cfg->alpha_prior;
+    d.trace_cap = cfg->trace_cap;
+    int rc = 0;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        mc3_free(h);
+        return cuda_fail(e, "cudaStreamCreate(mc3)");
+    }
+    // Topology, lengths, buffers.
+    std::vector<int32_t> par_all((size_t)C * NN), ch_all((size_t)C * NN * 3);
+    std::vector<double> len_all((size_t)C * NN);
+    for (unsigned c = 0; c < C; ++c) {
+        memcpy(&par_all[(size_t)c * NN], cfg->parent, NN * 4);
+        memcpy(&ch_all[(size_t)c * NN * 3], child.data(), NN * 3 * 4);
+        memcpy(&len_all[(size_t)c * NN], cfg->len, NN * 8);
+    }
+    std::vector<double> heat(C), lnl(C, 0.0);
+    for (unsigned c = 0; c < C; ++c) heat[c] = 1.0 / (1.0 + c * cfg->heat_delta);
+    std::vector<Mc3Model> models((size_t)C * 2);
+    for (auto &m : models) {
+        memset(&m, 0, sizeof(m));
+        for (int i = 0; i < 6; ++i) m.rates[i] = cfg->rates[i];
+        for (int i = 0; i < 4; ++i) m.freqs[i] = cfg->freqs[i];
+        m.alpha = cfg->alpha;
+    }
+    // Leaf masks (0 = any state, as Lik.pyx:1469-1470), pattern weights.
+    std::vector<uint8_t> masks((size_t)N * d.ppad, 15);
+    for (unsigned t = 0; t < N; ++t)
+        for (unsigned p = 0; p < cfg->npat; ++p) {
+            const uint8_t v = cfg->masks[(size_t)t * cfg->npat + p] & 15;
+            masks[(size_t)t * d.ppad + p] = v ? v : 15;
+        }
+    uint8_t *dmask = nullptr;
+    uint32_t *dfreq = nullptr;
+    const uint8_t **leafptr_host = new const uint8_t *[N];
+    std::vector<void *> cl((size_t)C * M * 2), sc((size_t)C * M * 2);
+    const size_t cl_bytes = (size_t)K * 4 * d.ppad * elt, sc_bytes = (size_t)d.ppad * 8;
+    if ((rc = mc3_upload(h, &d.parent, par_all.data(), par_all.size())) ||
+        (rc = mc3_upload(h, &d.child, ch_all.data(), ch_all.size())) ||
+        (rc = mc3_upload(h, &d.len, len_all.data(), len_all.size())) ||
+        (rc = mc3_upload<uint8_t>(h, &d.cur, nullptr, (size_t)C * NN)) ||
+        (rc = mc3_upload<uint8_t>(h, &d.dirtyflag, nullptr, (size_t)C * NN)) ||
+        (rc = mc3_upload<int32_t>(h, &d.dirty, nullptr, (size_t)C * M)) ||
+        (rc = mc3_upload<int32_t>(h, &d.stack, nullptr, (size_t)C * NN)) ||
+        (rc = mc3_upload(h, &d.model, models.data(), models.size())) ||
+        (rc = mc3_upload<uint8_t>(h, &d.curmodel, nullptr, C)) ||
+        (rc = mc3_upload(h, &d.lnL, lnl.data(), C)) ||
+        (rc = mc3_upload(h, &d.heat, heat.data(), C)) ||
+        (rc = mc3_upload<uint64_t>(h, &d.gen, nullptr, 1)) ||
+        (rc = mc3_upload<Mc3Prop>(h, &d.prop, nullptr, C)) ||
+        (rc = mc3_upload<PlanArgs>(h, &d.jobs, nullptr, C)) ||
+        (rc = mc3_upload<unsigned char>(h, &d.rec, nullptr, (size_t)C * M * d.rstride)) ||
+        (rc = mc3_upload<const uint8_t *>(h, (const uint8_t ***)&d.leaves, nullptr,
+                                          (size_t)C * N)) ||
+        (rc = mc3_upload<double>(h, &d.kid_len, nullptr, (size_t)C * d.maxkids)) ||
+        (rc = mc3_upload<uint64_t>(h, &d.kid_dst, nullptr, (size_t)C * d.maxkids)) ||
+        (rc = mc3_upload<int32_t>(h, &d.kid_tab, nullptr, (size_t)C * d.maxkids)) ||
+        (rc = mc3_upload<uint32_t>(h, &d.nkids, nullptr, C)) ||
+        (rc = mc3_upload<double>(h, &d.ltab, nullptr,
+                                 cfg->precision == CXG_FP64
+                                     ? (size_t)C * d.maxkids * 16 * K * 4
+                                     : 2)) ||
+        (rc = mc3_upload<char>(h, &d.results, nullptr, (size_t)C * 32 + 16)) ||
+        (rc = mc3_upload<uint32_t>(h, &d.acc, nullptr, (size_t)C * kMoves)) ||
+        (rc = mc3_upload<uint32_t>(h, &d.rej, nullptr, (size_t)C * kMoves)) ||
+        (rc = mc3_upload<uint32_t>(h, &d.nswap, nullptr, C)) ||
+        (rc = mc3_upload<double>(h, &d.trace, nullptr, cfg->trace_cap ? cfg->trace_cap : 1)) ||
+        (rc = mc3_upload<uint32_t>(h, &d.status, nullptr, 1)) ||
+        (rc = mc3_upload(h, &dmask, masks.data(), masks.size())) ||
+        (rc = mc3_upload(h, &dfreq, cfg->freqs_pattern, cfg->npat))) {
+        delete[] leafptr_host;
+        mc3_free(h);
+        return rc;
+    }
+    for (unsigned t = 0; t < N; ++t) leafptr_host[t] = dmask + (size_t)t * d.ppad;
+    rc = mc3_upload(h, (const uint8_t ***)&d.leafmask, leafptr_host, N);
+    delete[] leafptr_host;
+    if (rc) {
+        mc3_free(h);
+        return rc;
+    }
+    d.counter = (unsigned *)(d.results + (size_t)C * 32);
+    {
+        void *slab_cl = nullptr, *slab_sc = nullptr;
+        if ((rc = mc3_alloc(h, &slab_cl, cl.size() * cl_bytes)) ||
+            (rc = mc3_alloc(h, &slab_sc, sc.size() * sc_bytes))) {
+            mc3_free(h);
+            return rc;
+        }
+        for (size_t i = 0; i < cl.size(); ++i) {
+            cl[i] = static_cast<char *>(slab_cl) + i * cl_bytes;
+            sc[i] = static_cast<char *>(slab_sc) + i * sc_bytes;
+        }
+    }
+    if ((rc = mc3_upload(h, &d.cl_data, cl.data(), cl.size())) ||
+        (rc = mc3_upload(h, &d.cl_sc, sc.data(), sc.size()))) {
+        mc3_free(h);
+        return rc;
+    }
+    // Walk jobs: one per chain.
+    double *partial = nullptr;
+    if ((rc = mc3_upload<double>(h, &partial, nullptr, (size_t)C * d.ntiles * 2))) {
+        mc3_free(h);
+        return rc;
+    }
+    std::vector<PlanArgs> jobs(C);
+    std::vector<WalkItem> items;
+    for (unsigned c = 0; c < C; ++c) {
+        PlanArgs a;
+        memset(&a, 0, sizeof(a));
+        a.rec = d.rec + (size_t)c * M * d.rstride;
+        a.leaves = d.leaves + (size_t)c * N;
+        a.rstride = d.rstride;
+        a.ring = kRing;
+        a.nops = 0;
+        a.nleaf = 0;
+        a.nslot = 0;
+        a.tile = tile;
+        a.kact = K;
+        a.npat = d.npat;
+        a.ppad = d.ppad;
+        a.root_last = 1;
+        a.freqs = dfreq;
+        a.partial = partial + (size_t)c * d.ntiles * 2;
+        a.ticket = (unsigned *)(d.results + (size_t)c * 32);
+        a.ninf = (uint32_t *)(d.results + (size_t)c * 32 + 4);
+        a.err = (uint32_t *)(d.results + (size_t)c * 32 + 8);
+        a.total = (double *)(d.results + (size_t)c * 32 + 16);
+        a.ltab = d.ltab + (cfg->precision == CXG_FP64 ? (size_t)c * d.maxkids * 16 * K * 4 : 0);
+        a.ntiles = d.ntiles;
+        a.no_root = 0;
+        jobs[c] = a;
+    }
+    for (unsigned t = 0; t < d.ntiles; ++t)
+        for (unsigned c = 0; c < C; ++c) items.push_back(WalkItem{c, t});
+    WalkItem *ditems = nullptr;
+    e = cudaMemcpy(d.jobs, jobs.data(), C * sizeof(PlanArgs), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess || (rc = mc3_upload(h, &ditems, items.data(), items.size()))) {
+        mc3_free(h);
+        return rc ? rc : cuda_fail(e, "cudaMemcpy(jobs)");
+    }
+    BatchArgs &ba = h->ba;
+    ba.jobs = d.jobs;
+    ba.items = ditems;
+    ba.nitems = (uint32_t)items.size();
+    ba.counter = d.counter;
+    ba.tile = tile;
+    ba.ring = kRing;
+    ba.kact = K;
+    ba.max_nslot = 0;
+    ba.max_nleaf = N;
+    ba.max_rstride = d.rstride;
+    const size_t smem = plan_smem_bytes(cfg->precision, K, tile, 0, N, kRing, d.rstride);
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int per = batch_ctas_per_sm(cfg->precision, K, tile, smem);
+    if (per <= 0) {
+        mc3_free(h);
+        return fail(CXG_EINVAL, "cxgMc3Create: walker does not fit an SM");
+    }
+    h->grid = (unsigned)(per * nsm);
+    h->pmat_grid = (C * d.maxkids * K + 127) / 128;
+    // Derived model quantities, then generation 0 (full evaluation).
+    mc3_init_kernel<<<C, 32, 0, h->stream>>>(d);
+    if ((e = cudaGetLastError()) != cudaSuccess) {
+        mc3_free(h);
+        return cuda_fail(e, "mc3_init_kernel");
+    }
+    if ((rc = mc3_enqueue_gen(h))) {
+        mc3_free(h);
+        return rc;
+    }
+    uint32_t st = 0;
+    if ((e = cudaMemcpyAsync(&st, d.status, 4, cudaMemcpyDeviceToHost, h->stream)) !=
+            cudaSuccess ||
+        (e = cudaStreamSynchronize(h->stream)) != cudaSuccess) {
+        mc3_free(h);
+        return cuda_fail(e, "cxgMc3Create init");
+    }
+    if (st) {
+        mc3_free(h);
+        return fail(CXG_EINVAL, "cxgMc3Create: initial model cannot be decomposed");
+    }
+    // Capture a block of generations as one graph.
+    h->graph_gens = cfg->graph_gens ? cfg->graph_gens : 16;
+    e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        mc3_free(h);
+        return cuda_fail(e, "cudaStreamBeginCapture(mc3)");
+    }
+    for (unsigned i = 0; i < h->graph_gens && rc == 0; ++i) rc = mc3_enqueue_gen(h);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(h->stream, &graph);
+    if (rc || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        mc3_free(h);
+        return rc ? rc : cuda_fail(e, "cudaStreamEndCapture(mc3)");
+    }
+    h->graph = graph;
+    if ((e = cudaGraphInstantiate(&h->exec, graph, 0)) != cudaSuccess) {
+        mc3_free(h);
+        return cuda_fail(e, "cudaGraphInstantiate(mc3)");
+    }
+    *out = h;
+    return 0;
+}
+
+extern "C" int cxgMc3Run(cxgMc3 *h, unsigned long long ngen, double *seconds) {
+    if (h == nullptr) return fail(CXG_EINVAL, "cxgMc3Run: NULL");
+    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    cudaEvent_t t0, t1;
+    CXG_CUDA(cudaEventCreate(&t0));
+    CXG_CUDA(cudaEventCreate(&t1));
+    CXG_CUDA(cudaEventRecord(t0, h->stream));
+    unsigned long long left = ngen;
+    while (left >= h->graph_gens) {
+        CXG_CUDA(cudaGraphLaunch(h->exec, h->stream));
+        left -= h->graph_gens;
+    }
+    for (; left > 0; --left) {
+        int rc = mc3_enqueue_gen(h);
+        if (rc) return rc;
+    }
+    CXG_CUDA(cudaEventRecord(t1, h->stream));
+    CXG_CUDA(cudaEventSynchronize(t1));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, t0, t1);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (seconds) *seconds = ms / 1e3;
+    uint32_t st = 0;
+    CXG_CUDA(cudaMemcpy(&st, h->d.status, 4, cudaMemcpyDeviceToHost));
+    (void)st;  // undecomposable proposed models are rejected, not errors
+    // Any bounded wait that gave up?
+    std::vector<char> res((size_t)h->d.nchains * 32);
+    CXG_CUDA(cudaMemcpy(res.data(), h->d.results, res.size(), cudaMemcpyDeviceToHost));
+    for (unsigned c = 0; c < h->d.nchains; ++c)
+        if (*(const uint32_t *)(res.data() + (size_t)c * 32 + 8))
+            return fail(CXG_ETIMEOUT, "MC3 walker: a record copy timed out");
+    return 0;
+}
+
+extern "C" int cxgMc3Chain(cxgMc3 *h, unsigned chain, double *lnL, double *heat,
+                           int32_t *parent, double *len, double *rates,
+                           double *freqs, double *alpha) {
+    if (h == nullptr || chain >= h->d.nchains) return fail(CXG_EINVAL, "cxgMc3Chain: bad chain");
+    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    const Mc3Dev &d = h->d;
+    CXG_CUDA(cudaStreamSynchronize(h->stream));
+    if (lnL) CXG_CUDA(cudaMemcpy(lnL, d.lnL + chain, 8, cudaMemcpyDeviceToHost));
+    if (heat) CXG_CUDA(cudaMemcpy(heat, d.heat + chain, 8, cudaMemcpyDeviceToHost));
+    if (parent)
+        CXG_CUDA(cudaMemcpy(parent, d.parent + (size_t)chain * d.nnodes, d.nnodes * 4,
+                            cudaMemcpyDeviceToHost));
+    if (len)
+        CXG_CUDA(cudaMemcpy(len, d.len + (size_t)chain * d.nnodes, d.nnodes * 8,
+                            cudaMemcpyDeviceToHost));
+    uint8_t cm = 0;
+    CXG_CUDA(cudaMemcpy(&cm, d.curmodel + chain, 1, cudaMemcpyDeviceToHost));
+    Mc3Model m;
+    CXG_CUDA(cudaMemcpy(&m, d.model + chain * 2 + cm, sizeof(m), cudaMemcpyDeviceToHost));
+    if (rates) memcpy(rates, m.rates, 48);
+    if (freqs) memcpy(freqs, m.freqs, 32);
+    if (alpha) *alpha = m.alpha;
+    return 0;
+}
+
+extern "C" int cxgMc3Stats(cxgMc3 *h, unsigned *accepts, unsigned *rejects,
+                           unsigned *swaps, unsigned long long *gen) {
+    if (h == nullptr) return fail(CXG_EINVAL, "cxgMc3Stats: NULL");
+    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    const Mc3Dev &d = h->d;
+    CXG_CUDA(cudaStreamSynchronize(h->stream));
+    if (accepts)
+        CXG_CUDA(cudaMemcpy(accepts, d.acc, (size_t)d.nchains * kMoves * 4,
+                            cudaMemcpyDeviceToHost));
+    if (rejects)
+        CXG_CUDA(cudaMemcpy(rejects, d.rej, (size_t)d.nchains * kMoves * 4,
+                            cudaMemcpyDeviceToHost));
+    if (swaps) CXG_CUDA(cudaMemcpy(swaps, d.nswap, d.nchains * 4, cudaMemcpyDeviceToHost));
+    if (gen) CXG_CUDA(cudaMemcpy(gen, d.gen, 8, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+extern "C" int cxgMc3Trace(cxgMc3 *h, double *out, unsigned long long n) {
+    if (h == nullptr) return fail(CXG_EINVAL, "cxgMc3Trace: NULL");
+    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    if (n > h->d.trace_cap) n = h->d.trace_cap;
+    CXG_CUDA(cudaStreamSynchronize(h->stream));
+    CXG_CUDA(cudaMemcpy(out, h->d.trace, n * 8, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+extern "C" int cxgMc3Destroy(cxgMc3 *h) {
+    if (h == nullptr) return 0;
+    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    cudaStreamSynchronize(h->stream);
+    mc3_free(h);
+    return 0;
+}

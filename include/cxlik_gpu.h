@@ -243,6 +243,52 @@ int cxgBatchInfo(const cxgBatch *batch, double *updates, double *alg_bytes,
                  unsigned long long *launches_per_run);
 int cxgBatchDestroy(cxgBatch *batch);
 
+/* On-device MC3 (no counterpart entry point in the reference; the
+ * reference runs its chains on the host, pkg/Crux/Mc3/Chain.pyx).  All
+ * chains share one alignment; each keeps its tree, model, lnL, heat and CLs
+ * in HBM.  Nodes 0..ntaxa-1 are the leaves (in mask order), the tree is
+ * binary and rooted at internal node `root` (degree 3). */
+typedef struct {
+    unsigned ntaxa;
+    unsigned npat;
+    const uint8_t *masks;          /* [ntaxa][npat] state masks, 0 = any */
+    const uint32_t *freqs_pattern; /* [npat] pattern weights */
+    const int32_t *parent;         /* [2*ntaxa-2], -1 at the root */
+    const double *len;             /* [2*ntaxa-2] length of edge to parent */
+    unsigned root;
+    double rates[6];    /* exchangeabilities AC AG AT CG CT GT */
+    double freqs[4];    /* base frequencies */
+    double alpha;       /* Gamma shape (ignored when ncat == 1) */
+    unsigned ncat;      /* Gamma categories, 1..8 */
+    unsigned nchains;
+    double heat_delta;  /* chain i runs at heat 1/(1 + i*heat_delta) */
+    unsigned swap_stride;
+    unsigned long long seed;
+    double move_weight[4];  /* branch length, NNI, rates, alpha */
+    double brlen_lambda, brlen_prior;
+    double rate_conc;       /* Dirichlet concentration of rate moves */
+    double alpha_lambda, alpha_prior;
+    int precision;          /* CXG_FP32 or CXG_FP64 */
+    unsigned graph_gens;    /* generations per captured graph (0: 16) */
+    unsigned long long trace_cap;  /* cold-chain lnL trace length */
+} cxgMc3Config;
+typedef struct cxgMc3 cxgMc3;
+/* Build the chains and run generation 0 (a full evaluation). */
+int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **mc3);
+/* Advance every chain `ngen` generations (one move each, then a heat-swap
+ * attempt every swap_stride); *seconds = device time. */
+int cxgMc3Run(cxgMc3 *mc3, unsigned long long ngen, double *seconds);
+/* Current state of one chain (tree in the same node numbering). */
+int cxgMc3Chain(cxgMc3 *mc3, unsigned chain, double *lnL, double *heat,
+                int32_t *parent, double *len, double *rates, double *freqs,
+                double *alpha);
+/* Accept/reject counts [chain][move], swaps [chain], generation count. */
+int cxgMc3Stats(cxgMc3 *mc3, unsigned *accepts, unsigned *rejects,
+                unsigned *swaps, unsigned long long *gen);
+/* Cold-chain lnL after each generation 0..n-1. */
+int cxgMc3Trace(cxgMc3 *mc3, double *out, unsigned long long n);
+int cxgMc3Destroy(cxgMc3 *mc3);
+
 /* Launch shape of the plan walker for plans translated from now on:
  * patterns per CTA (32, 64 or 128) and the shared-memory budget of its CL
  * stack (bytes, <= 200 KiB).  Chosen by the autotuner (crux_gb300.tune). */

@@ -1,0 +1,80 @@
+"""On-device MC3: after generations of branch-length, NNI, rate and alpha
+moves, every chain's device lnL equals the FP64 oracle's lnL of that
+chain's tree and model (1e-11 relative for the plain FP64 chains, 1e-6 for
+FP32 chains); moves are accepted and heats are swapped."""
+import numpy as np
+import pytest
+
+from crux_gb300 import synth
+from crux_gb300.mc3 import Mc3
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-11, "fp32": 1e-6}
+MOVES = {"brlen": 2.0, "nni": 2.0, "rates": 0.5, "alpha": 0.5}
+
+
+def build(precision, nchains=4, seed=9, moves=MOVES, ntaxa=16, nsites=1000):
+    case = synth.Case(ntaxa, nsites, 0.1, 5)
+    aln = case.alignment()
+    t = case.tree(aln.taxaMap)
+    return Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=0.5,
+               ncat=4, nchains=nchains, heat_delta=0.2, seed=seed,
+               moves=moves, precision=precision, graph_gens=8)
+
+
+def check_chains(m, port, tol):
+    for i in range(m.nchains):
+        lik, st = m.chain_lik(i, port)
+        want = lik.lnL()
+        assert abs(st["lnL"] - want) <= tol * abs(want), (i, st["lnL"], want)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_mc3_chains_match_oracle(gpu, port, precision):
+    m = build(precision)
+    check_chains(m, port, TOL[precision])       # generation 0
+    m.run(157)                                  # graphs of 8 + remainder
+    check_chains(m, port, TOL[precision])
+    st = m.stats()
+    assert st["generation"] == 158
+    acc = st["accepts"].sum(axis=0)
+    rej = st["rejects"].sum(axis=0)
+    assert (acc + rej)[:2].min() > 0
+    assert acc[0] > 0 and acc[1] > 0            # brlen and NNI accepted
+    assert st["swaps"].sum() > 0
+    heats = sorted(m.chain_state(i)["heat"] for i in range(m.nchains))
+    assert np.allclose(heats, sorted(1.0 / (1.0 + 0.2 * i) for i in range(4)))
+    tr = m.trace(158)
+    assert np.isfinite(tr).all()
+    m.close()
+
+
+def test_mc3_same_seed_fp32_follows_fp64(gpu):
+    """Same seed: the FP32 chains draw the same moves as the FP64 chains, so
+    the cold-chain traces agree until an acceptance decision falls within
+    the FP32 error of its threshold."""
+    a, b = build("fp64", seed=21), build("fp32", seed=21)
+    a.run(40)
+    b.run(40)
+    ta, tb = a.trace(41), b.trace(41)
+    rel = np.abs(ta - tb) / np.abs(ta)
+    assert rel[0] <= 1e-6
+    assert (rel[:20] <= 1e-6).all()
+    a.close()
+    b.close()
+
+
+def test_mc3_brlen_only_single_category(gpu, port):
+    case = synth.Case(10, 500, 0.1, 11, alpha=None)
+    aln = case.alignment()
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=None,
+            nchains=2, heat_delta=0.1, seed=4, moves={"brlen": 1.0},
+            precision="fp64", graph_gens=4)
+    m.run(50)
+    for i in range(2):
+        lik, st = m.chain_lik(i, port)
+        want = lik.lnL()
+        assert abs(st["lnL"] - want) <= 1e-11 * abs(want)
+    m.close()
