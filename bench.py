@@ -420,6 +420,89 @@ def run_batch(args, dist):
     dist.close()
 
 
+MC3 = {"mc3": {"workload": "mc3_128taxa_100ksites_gtr_gamma4_8chains",
+               "ntaxa": 128, "nsites": 100000, "mean_brlen": 0.05,
+               "nchains": 8, "heat_delta": 0.1, "seed": 20261205,
+               "moves": {"brlen": 2.0, "nni": 2.0, "rates": 1.0,
+                         "alpha": 1.0}, "gens": 2000, "check_every": 1000},
+       "mc3small": {"workload": "mc3_16taxa_1000sites_gtr_gamma4_4chains",
+                    "ntaxa": 16, "nsites": 1000, "mean_brlen": 0.1,
+                    "nchains": 4, "heat_delta": 0.2, "seed": 20261206,
+                    "moves": {"brlen": 1.0, "nni": 1.0}, "gens": 1000,
+                    "check_every": 250}}
+
+
+def run_mc3(args, dist):
+    """On-device MC3: generations/s of the FP32-scaled chains and of the
+    plain FP64 chains from the same seed, with the cold chain's lnL checked
+    against the FP64 oracle every `check_every` generations."""
+    from crux_gb300 import _native, synth
+    from crux_gb300.mc3 import Mc3
+    w = MC3[args.workload]
+    gens = args.gens or w["gens"]
+    gpu = _native.load()
+    case = synth.Case(w["ntaxa"], w["nsites"], w["mean_brlen"], w["seed"])
+    aln = case.alignment()
+    port = None
+    if not args.no_cpu:
+        from oracle import oracle
+        port = oracle.load_port()
+        port.port_set_threads(os.cpu_count() or 1)
+    out = {}
+    for prec in ("fp32", "fp64"):
+        m = Mc3(case.tree(aln.taxaMap), aln, case.params["rates"],
+                case.params["freqs"], alpha=0.5, ncat=4,
+                nchains=w["nchains"], heat_delta=w["heat_delta"],
+                seed=w["seed"], moves=w["moves"], precision=prec,
+                graph_gens=16)
+        m.run(max(args.warmup, 3) * 16)
+        secs = 0.0
+        drift = []
+        done = 0
+        clocks = Clocks()
+        if prec == "fp32":
+            clocks.start()
+        while done < gens:
+            step = min(w["check_every"], gens - done)
+            secs += m.run(step)
+            done += step
+            if port is not None and prec == "fp32":
+                cold = max(range(m.nchains),
+                           key=lambda i: m.chain_state(i)["heat"])
+                lik, st = m.chain_lik(cold, port)
+                want = lik.lnL()
+                drift.append(abs(st["lnL"] - want) / abs(want))
+        ck = clocks.stop() if prec == "fp32" else None
+        st = m.stats()
+        out[prec] = {"gens_per_s": gens / secs, "secs": secs,
+                     "accept_rate": (st["accepts"].sum() /
+                                     max(1, st["accepts"].sum() +
+                                         st["rejects"].sum())),
+                     "swaps": int(st["swaps"].sum()) // 2,
+                     "drift": drift, "clocks": ck,
+                     "trace_head": [float(x) for x in m.trace(8)]}
+        m.close()
+    f32, f64 = out["fp32"], out["fp64"]
+    line = {
+        "metric": "MC3 generations/s (FP32-scaled chains, on device)",
+        "value": f32["gens_per_s"], "unit": "generations/s", "n_gpus": 1,
+        "steps": gens, "warmup": max(args.warmup, 3) * 16,
+        "ms_per_step": 1e3 * f32["secs"] / gens, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": dict(w, gens=gens, patterns=aln.nchars),
+        "fp64_plain_gens_per_s": f64["gens_per_s"],
+        "fp32_over_fp64": f32["gens_per_s"] / f64["gens_per_s"],
+        "accept_rate": f32["accept_rate"], "swaps": f32["swaps"],
+        "drift_vs_fp64_oracle": f32["drift"],
+        "trace_head_fp32": f32["trace_head"],
+        "trace_head_fp64": f64["trace_head"],
+        "clocks": f32["clocks"],
+    }
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -434,7 +517,9 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="FP32 plan only, no e2e/CPU legs (for ncu)")
     ap.add_argument("--workload", default="tree128",
-                    choices=["tree128", "batch256"])
+                    choices=["tree128", "batch256", "mc3", "mc3small"])
+    ap.add_argument("--gens", type=int, default=None,
+                    help="mc3 workloads: generations to time")
     ap.add_argument("--jobs", type=int, default=None,
                     help="batch256: number of jobs (default 256)")
     args = ap.parse_args()
@@ -443,6 +528,8 @@ def main():
         run_reference(args, dist)
     elif args.workload == "batch256":
         run_batch(args, dist)
+    elif args.workload in MC3:
+        run_mc3(args, dist)
     else:
         run_ours(args, dist)
 
