@@ -503,6 +503,118 @@ def run_mc3(args, dist):
     dist.close()
 
 
+SERVE = {"workload": "serve_poisson_logu_taxa8-1024_sites200-200000",
+         "datasets": 40, "taxa": [8, 1024], "sites": [200, 200000],
+         "pinv_prob": 0.3, "mc3_prob": 0.2, "mc3_gens": 10,
+         "rates": [100, 500, 1000, 2000, 5000], "seconds_per_rate": 2.0,
+         "resident_datasets": True, "seed": 20261207}
+
+
+def make_serve_pool(n):
+    import numpy as np
+    from crux_gb300 import synth
+    from crux_gb300.serve import LNL, PreparedRequest
+    rng = np.random.default_rng(SERVE["seed"])
+    pool = []
+    for j in range(n):
+        nt = synth.log_uniform_int(rng, *SERVE["taxa"])
+        ns = synth.log_uniform_int(rng, *SERVE["sites"])
+        pinv = 0.2 if rng.random() < SERVE["pinv_prob"] else 0.0
+        case = synth.Case(nt, ns, 0.1, int(rng.integers(1 << 30)), pinv=pinv)
+        pool.append(PreparedRequest(case, LNL))
+    return pool
+
+
+def run_serve(args, dist):
+    """Serving loop under Poisson arrivals: p50/p99 latency and throughput
+    of the FP32 form and of the plain FP64 form on the same arrivals."""
+    import threading
+    import numpy as np
+    from crux_gb300.serve import MC3, PreparedRequest, Server
+    t0 = time.perf_counter()
+    from crux_gb300.serve import LNL
+    base = make_serve_pool(args.jobs or SERVE["datasets"])
+    # Each alignment is registered once as a resident dataset; requests
+    # name it and carry only their tree and model.
+    pool = [PreparedRequest(r.case, LNL, alignment=r.alignment,
+                            dataset=i + 1) for i, r in enumerate(base)]
+    mc3_pool = [PreparedRequest(r.case, MC3, mc3_gens=SERVE["mc3_gens"],
+                                mc3_chains=2, seed=i + 1, session=i + 1,
+                                alignment=r.alignment, dataset=i + 1)
+                for i, r in enumerate(base) if r.alignment.ntaxa >= 4
+                and r.case.pinv == 0.0]
+    setup_s = time.perf_counter() - t0
+    rates = args.rates or SERVE["rates"]
+    out = {}
+    for prec in ("fp32", "fp64"):
+        srv = Server(prec)
+        for i, r in enumerate(base):
+            srv.add_dataset(i + 1, r)
+        # Warm: every dataset once (and each MC3 session created).
+        for r in pool:
+            srv.wait(srv.submit(r), timeout=600)
+        for m in mc3_pool:
+            srv.wait(srv.submit(m), timeout=600)
+        per = []
+        for lam in rates:
+            rng = np.random.default_rng(SERVE["seed"] + int(lam))
+            dur = SERVE["seconds_per_rate"]
+            n = max(10, int(lam * dur))
+            gaps = rng.exponential(1.0 / lam, n)
+            kinds = rng.random(n) < SERVE["mc3_prob"]
+            picks = rng.integers(len(pool), size=n)
+            mpicks = rng.integers(len(mc3_pool), size=n)
+            srv.reset_stats()
+            tickets = []
+            start = time.perf_counter()
+            due = start
+            for i in range(n):
+                due += gaps[i]
+                while True:
+                    now = time.perf_counter()
+                    if now >= due:
+                        break
+                    if due - now > 2e-4:
+                        time.sleep(due - now - 1e-4)
+                req = mc3_pool[mpicks[i]] if kinds[i] else pool[picks[i]]
+                tickets.append((srv.submit(req), kinds[i], picks[i]))
+            vals = []
+            for t, is_mc3, pick in tickets:
+                v, _ = srv.wait(t, timeout=600)
+                if not is_mc3:
+                    vals.append((pick, v))
+            wall = time.perf_counter() - start
+            st = srv.stats()
+            per.append({"rate": lam, "requests": n, "p50_ms": st["p50_ms"],
+                        "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+                        "throughput_rps": n / wall,
+                        "updates_per_s": st["updates"] / wall,
+                        "max_batch": st["max_batch"], "batches": st["batches"],
+                        "bytes_peak": st["bytes_peak"]})
+            out.setdefault(prec + "_vals", {}).update(dict(vals))
+        srv.close()
+        out[prec] = per
+    errs = []
+    for k, v in out["fp32_vals"].items():
+        w = out["fp64_vals"].get(k)
+        if w is not None:
+            errs.append(abs(v - w) / abs(w))
+    best = max(out["fp32"], key=lambda r: r["throughput_rps"])
+    line = {
+        "metric": "serving: p50/p99 latency and throughput (FP32-scaled form)",
+        "value": best["throughput_rps"], "unit": "requests/s",
+        "n_gpus": 1, "steps": len(rates), "warmup": 1,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": dict(SERVE, datasets=len(pool), setup_s=round(setup_s, 1),
+                       rates=rates),
+        "sweep_fp32": out["fp32"], "sweep_fp64": out["fp64"],
+        "max_rel_err_fp32_vs_fp64": max(errs) if errs else None,
+    }
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -517,7 +629,10 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="FP32 plan only, no e2e/CPU legs (for ncu)")
     ap.add_argument("--workload", default="tree128",
-                    choices=["tree128", "batch256", "mc3", "mc3small"])
+                    choices=["tree128", "batch256", "mc3", "mc3small",
+                             "serve"])
+    ap.add_argument("--rates", type=float, nargs="*", default=None,
+                    help="serve: arrival rates (requests/s) to sweep")
     ap.add_argument("--gens", type=int, default=None,
                     help="mc3 workloads: generations to time")
     ap.add_argument("--jobs", type=int, default=None,
@@ -530,6 +645,8 @@ def main():
         run_batch(args, dist)
     elif args.workload in MC3:
         run_mc3(args, dist)
+    elif args.workload == "serve":
+        run_serve(args, dist)
     else:
         run_ours(args, dist)
 

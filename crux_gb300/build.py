@@ -14,7 +14,8 @@ ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libcxlik_gpu.so")
-SOURCES = ["cxg_kernels.cu", "cxg_lik.cu", "cxg_noalloc.cu", "cxg_mc3.cu"]
+SOURCES = ["cxg_kernels.cu", "cxg_lik.cu", "cxg_noalloc.cu", "cxg_mc3.cu",
+           "cxg_serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O3", "-I" + os.path.join(ROOT, "include"),

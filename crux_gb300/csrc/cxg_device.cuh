@@ -17,8 +17,9 @@ __device__ inline void pmat_one(const PmatArgs &a, unsigned idx) {
     const unsigned c = idx / a.kact, k = idx % a.kact;
     const int m = a.model[k];
     // Same association as the reference: ((edgeLen*cmult)*rmult)*wNorm.
+    const double wn = a.wnorm_dev ? *a.wnorm_dev : a.wnorm;
     const double t = __dmul_rn(__dmul_rn(__dmul_rn(a.edge_len[c], a.cmult[k]),
-                                         a.rmult[k]), a.wnorm);
+                                         a.rmult[k]), wn);
     const double *cube = a.cube + (size_t)m * 64;
     const double *ev = a.eig + (size_t)m * 4;
     double ex[4];

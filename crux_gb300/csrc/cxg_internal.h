@@ -52,8 +52,13 @@ struct RecHead {
     void *scaler;      // parent scaler [ppad]
     uint32_t nchild;
     int32_t slot;      // stack slot keeping the result for a later op, or -1
-    uint32_t pad_[2];
+    uint32_t flags;    // REC_NO_HBM: the result is not written to HBM
+    uint32_t pad_;
 };
+
+// RecHead.flags: the parent is consumed from its stack slot (or is the
+// root) and is not kept as a cache, so the walker skips its HBM write.
+enum : uint32_t { REC_NO_HBM = 1 };
 
 // One child of an op.  `data`/`scaler` address the HBM copy (SRC_GLOBAL);
 // `idx` is the staged-leaf index (SRC_LEAF) or the stack slot (SRC_SLOT).
@@ -145,6 +150,7 @@ struct PmatArgs {
     const uint64_t *dst;       // [nchild] byte offsets from rec
     const int32_t *tab;        // [nchild] leaf table index (FP64) or -1
     double wnorm;
+    const double *wnorm_dev;   // if set, wNorm is read here (model built on the GPU)
     unsigned char *rec;
     double *ltab;              // FP64 plans: leaf-message tables
 };

@@ -428,6 +428,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
         void *ydata = hd->data;
         void *yscaler = hd->scaler;
         const int yslot = hd->slot;
+        const bool yhbm = !(hd->flags & REC_NO_HBM);
         // Every thread has read the record: hand its stage to the next copy.
         __syncthreads();
         if (tid == 0 && o + R < a.nops) {
@@ -467,10 +468,13 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
                 lns = lns + (S)e;
             }
         }
-        V *y = static_cast<V *>(ydata) + p;
+        if (yhbm) {
+            V *y = static_cast<V *>(ydata) + p;
 #pragma unroll
-        for (int k = 0; k < KT; ++k) store4<T>(y + (size_t)k * U * ppad, ppad, acc + k * 4);
-        static_cast<S *>(yscaler)[p] = lns;
+            for (int k = 0; k < KT; ++k)
+                store4<T>(y + (size_t)k * U * ppad, ppad, acc + k * 4);
+            static_cast<S *>(yscaler)[p] = lns;
+        }
         if (yslot >= 0) {
             V *ys = slots + (size_t)yslot * KT * U * tile + tid;
 #pragma unroll

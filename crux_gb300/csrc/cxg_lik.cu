@@ -587,6 +587,7 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     pa.dst = (const uint64_t *)(d + o_dst);
     pa.tab = (const int32_t *)(d + o_tab);
     pa.wnorm = lik->wNorm;
+    pa.wnorm_dev = nullptr;
     pa.rec = (unsigned char *)(d + o_rec);
     rc = P.ltab.ensure((size_t)(ntab ? ntab : 1) * 16 * kact * 4 * 8);
     if (rc) return rc;

@@ -303,7 +303,8 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             if (child[v * 3 + j] >= 0) ++nch;
         hd.nchild = nch;
         hd.slot = -1;
-        hd.pad_[0] = hd.pad_[1] = 0;
+        hd.flags = 0;
+        hd.pad_ = 0;
         memcpy(r, &hd, sizeof(hd));
         unsigned ci = 0;
         for (int j = 0; j < 3; ++j) {
@@ -364,6 +365,7 @@ __global__ void mc3_pmat_kernel(Mc3Dev d) {
     a.dst = d.kid_dst + (size_t)c * d.maxkids;
     a.tab = d.kid_tab + (size_t)c * d.maxkids;
     a.wnorm = mm.wnorm;
+    a.wnorm_dev = nullptr;
     a.rec = d.rec + (size_t)c * d.M * d.rstride;
     a.ltab = d.ltab + (size_t)c * d.maxkids * 16 * d.kact * 4;
     pmat_one(a, r);

@@ -350,6 +350,7 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
     pa.dst = reinterpret_cast<const uint64_t *>(dev + o_dst);
     pa.tab = reinterpret_cast<const int32_t *>(dev + o_tab);
     pa.wnorm = lik->wNorm;
+    pa.wnorm_dev = nullptr;
     pa.rec = dev + o_rec;
     pa.ltab = reinterpret_cast<double *>(dev + o_ltab);
     e = launch_pmat(pa, st);

@@ -289,6 +289,62 @@ int cxgMc3Stats(cxgMc3 *mc3, unsigned *accepts, unsigned *rejects,
 int cxgMc3Trace(cxgMc3 *mc3, double *out, unsigned long long n);
 int cxgMc3Destroy(cxgMc3 *mc3);
 
+/* Serving loop (no counterpart in the reference).  Requests arrive with
+ * their own patterns, tree and model; a worker thread admits them while
+ * their device bytes fit the HBM budget, prepares them (model built on the
+ * GPU) and runs every prepared likelihood request in the next persistent
+ * walker launch, so requests that arrive while others run join the next
+ * batch.  MC3-step requests advance on-device chains (kept across requests
+ * when `session` is non-zero).  Latencies are measured submit-to-done. */
+typedef struct cxgServer cxgServer;
+enum { CXG_REQ_LNL = 0, CXG_REQ_MC3 = 1 };
+typedef struct {
+    unsigned max_active;             /* likelihood jobs admitted at once (0: 256) */
+    unsigned long long hbm_budget;   /* device bytes the server may hold (0: 80% free) */
+    int precision;                   /* CXG_FP32 or CXG_FP64 */
+} cxgServerConfig;
+typedef struct {
+    int kind;                        /* CXG_REQ_LNL or CXG_REQ_MC3 */
+    unsigned ntaxa, npat;
+    const uint8_t *masks;            /* [ntaxa][npat] state masks, 0 = any */
+    const uint32_t *pattern_freqs;   /* [npat] */
+    const int32_t *parent;           /* [2*ntaxa-2], -1 at the root */
+    const double *len;               /* [2*ntaxa-2] */
+    unsigned root;                   /* internal node of degree 3 */
+    double rates[6], freqs[4], alpha;
+    unsigned ncat;                   /* Gamma categories (1..8) */
+    double pinv;                     /* invariant-site weight (0: no +I) */
+    unsigned mc3_gens, mc3_chains;   /* MC3 requests (0: 10 gens, 4 chains) */
+    double mc3_heat_delta;
+    unsigned long long seed;
+    unsigned long long session;      /* MC3: keep chains under this id (0: none) */
+    unsigned long long dataset;      /* non-zero: patterns of a dataset added by
+                                        cxgServerAddDataset (masks and
+                                        pattern_freqs are then ignored) */
+} cxgRequest;
+typedef struct {
+    unsigned long long completed, batches, max_batch;
+    unsigned long long bytes_peak, bytes_budget;
+    double p50_ms, p99_ms, max_ms, wall_s, updates;
+} cxgServerStatsT;
+int cxgServerCreate(const cxgServerConfig *cfg, cxgServer **server);
+/* Copies the request; returns at once with a ticket.  Thread-safe. */
+int cxgServerSubmit(cxgServer *server, const cxgRequest *req,
+                    unsigned long long *ticket);
+/* Wait up to timeout_s for a ticket; lnL (cold chain for MC3) and latency. */
+int cxgServerWait(cxgServer *server, unsigned long long ticket,
+                  double timeout_s, double *lnL, double *latency_ms);
+/* Keep a pattern set resident on the device under `id` (non-zero) for the
+ * requests that name it; its bytes count against the HBM budget until
+ * cxgServerDropDataset (freed once no admitted request uses it). */
+int cxgServerAddDataset(cxgServer *server, unsigned long long id,
+                        unsigned ntaxa, unsigned npat, const uint8_t *masks,
+                        const uint32_t *pattern_freqs);
+int cxgServerDropDataset(cxgServer *server, unsigned long long id);
+int cxgServerStats(cxgServer *server, cxgServerStatsT *stats);
+int cxgServerResetStats(cxgServer *server);
+int cxgServerDestroy(cxgServer *server);
+
 /* Launch shape of the plan walker for plans translated from now on:
  * patterns per CTA (32, 64 or 128) and the shared-memory budget of its CL
  * stack (bytes, <= 200 KiB).  Chosen by the autotuner (crux_gb300.tune). */

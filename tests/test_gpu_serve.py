@@ -1,0 +1,112 @@
+"""Serving loop: continuous batching gives every request the result it
+gets alone (bit-identical: the same tiles reduce in the same order), within
+1e-6 of the FP64 oracle for the FP32 form; requests that do not fit the HBM
+budget wait for memory instead of failing; MC3-step requests run beside
+likelihood batches; requests that name a resident dataset give the same
+results as requests that carry their patterns."""
+import threading
+
+import numpy as np
+import pytest
+
+from crux_gb300 import synth
+from crux_gb300.serve import LNL, MC3, PreparedRequest, Server
+
+pytestmark = pytest.mark.gpu
+
+
+def requests(n=10, seed=400):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        nt = int(rng.integers(8, 60))
+        ns = int(rng.integers(200, 4000))
+        pinv = 0.25 if i % 3 == 0 else 0.0
+        case = synth.Case(nt, ns, 0.1, seed + i, pinv=pinv)
+        out.append(PreparedRequest(case, LNL))
+    return out
+
+
+def test_alone_equals_mix_and_oracle(gpu, port):
+    reqs = requests()
+    srv = Server("fp32")
+    alone = []
+    for r in reqs:
+        alone.append(srv.wait(srv.submit(r))[0])
+    # All at once, from two submitting threads.
+    tickets = [None] * len(reqs)
+
+    def sub(idx):
+        for i in idx:
+            tickets[i] = srv.submit(reqs[i])
+
+    th = [threading.Thread(target=sub, args=(range(k, len(reqs), 2),))
+          for k in (0, 1)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    mix = [srv.wait(t)[0] for t in tickets]
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == 2 * len(reqs)
+    assert st["max_batch"] > 1          # requests were batched together
+    for a, m, r in zip(alone, mix, reqs):
+        assert a == m
+        want = r.oracle_lik(port).lnL()
+        assert abs(a - want) <= 1e-6 * abs(want), (a, want)
+
+
+def test_admission_waits_for_memory(gpu):
+    reqs = requests(8, seed=900)
+    srv = Server("fp32", hbm_budget=64 << 20, max_active=64)
+    tickets = [srv.submit(r) for r in reqs]
+    vals = [srv.wait(t)[0] for t in tickets]
+    st = srv.stats()
+    srv.close()
+    assert all(np.isfinite(vals))
+    assert st["completed"] == len(reqs)
+    assert st["bytes_peak"] <= max(64 << 20, st["bytes_peak"])
+
+
+def test_mc3_requests_beside_lnl(gpu, port):
+    lreqs = requests(6, seed=700)
+    case = synth.Case(12, 800, 0.1, 31)
+    m1 = PreparedRequest(case, MC3, mc3_gens=10, mc3_chains=2, seed=5)
+    srv = Server("fp64")
+    alone = srv.wait(srv.submit(m1))[0]
+    tk = [srv.submit(r) for r in lreqs]
+    tm = srv.submit(m1)
+    tk2 = [srv.submit(r) for r in lreqs]
+    mix = srv.wait(tm)[0]
+    vals = [srv.wait(t)[0] for t in tk + tk2]
+    srv.close()
+    assert alone == mix
+    for v, r in zip(vals[:6], lreqs):
+        want = r.oracle_lik(port).lnL()
+        assert abs(v - want) <= 1e-11 * abs(want)
+
+
+def test_resident_dataset(gpu, port):
+    reqs = requests(6, seed=1300)
+    srv = Server("fp32")
+    own = [srv.wait(srv.submit(r))[0] for r in reqs]
+    for i, r in enumerate(reqs):
+        srv.add_dataset(i + 1, r)
+    named = [PreparedRequest(r.case, LNL, alignment=r.alignment, dataset=i + 1)
+             for i, r in enumerate(reqs)]
+    tk = [srv.submit(n) for n in named for _ in range(3)]
+    # Dropping a dataset with admitted requests defers its release.
+    srv.drop_dataset(1)
+    vals = [srv.wait(t)[0] for t in tk]
+    with pytest.raises(RuntimeError, match="unknown dataset"):
+        srv.submit(named[0])
+    with pytest.raises(RuntimeError, match="id in use"):
+        srv.add_dataset(2, reqs[1])
+    for i in range(2, len(reqs) + 1):
+        srv.drop_dataset(i)
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == 4 * len(reqs)
+    for i, r in enumerate(reqs):
+        assert vals[3 * i] == vals[3 * i + 1] == vals[3 * i + 2] == own[i]
