@@ -157,6 +157,32 @@ def profile_traffic(name):
     return None
 
 
+def autotune(lib, prec, args, lik=None, liks=None):
+    """Pick the walker's launch shape (tile, threads per pattern, stack
+    budget) by timing the candidates on this workload; ``--shape`` fixes it
+    instead.  Returns the shape with how it was chosen."""
+    from crux_gb300 import tune
+    if args.shape:
+        tune.set_shape(lib, *args.shape)
+        t, g, b = args.shape
+        return {"tile": t, "tpp": g, "budget": b, "source": "--shape"}
+    if liks is not None:
+        r = tune.tune_batch(liks, prec, iters=3,
+                            shapes=tune.candidates(
+                                prec, tune.active_components(liks[0]),
+                                budgets=(12 << 10, 24 << 10, 48 << 10)))
+    else:
+        r = tune.tune_plan(lik, prec, iters=10)
+    best = dict(r["best"])
+    top = sorted(r["table"], key=lambda x: x["ms"])
+    per_tpp = {}
+    for x in top:
+        per_tpp.setdefault(str(x["tpp"]), [x["tile"], x["budget"], x["ms"]])
+    best.update(source="autotuned", candidates=len(r["table"]),
+                worst_ms=top[-1]["ms"], best_per_tpp=per_tpp)
+    return best
+
+
 def cpu_run(lib, case, aln, steps, threads):
     """Time full-plan FP64 evaluations of the oracle; returns updates/s."""
     from crux_gb300 import synth
@@ -219,12 +245,14 @@ def run_ours(args, dist):
     gpu = _native.load()
     case = make_case()
 
+    from crux_gb300 import tune
     res = {}
     for prec in (("fp32",) if args.profile else ("fp32", "fp64")):
         lik = case.lik(lib=gpu, precision=prec)
         lnl_first = lik.lnL()
         lik.lik.invalidate = True
         lik._prep(None)
+        shape = autotune(gpu, prec, args, lik=lik)
         plan = Plan(lik, prec)
         info = plan.info()
         plan.time(max(args.warmup, 3))
@@ -237,7 +265,8 @@ def run_ours(args, dist):
         ms = dist.max(t["ms_per_run"])
         res[prec] = {"lik": lik, "plan": plan, "info": info, "t": t,
                      "ms": ms, "clocks": ck, "lnL": t["lnL"],
-                     "lnL_first": lnl_first}
+                     "lnL_first": lnl_first, "shape": shape,
+                     "plan_shape": plan.shape()}
 
     if args.profile:
         for p in res.values():
@@ -246,7 +275,10 @@ def run_ours(args, dist):
                           "ms_per_run": res["fp32"]["ms"]}))
         return
 
-    # End to end through the public API: full re-plan + lnL each run.
+    # End to end through the public API: full re-plan + lnL each run, with
+    # the FP32 form's tuned shape.
+    sh = res["fp32"]["shape"]
+    tune.set_shape(gpu, sh["tile"], sh["tpp"], sh["budget"])
     lik = res["fp32"]["lik"]
     for _ in range(max(args.warmup, 3)):
         lik.lik.invalidate = True
@@ -272,7 +304,7 @@ def run_ours(args, dist):
     peaks = measured_peaks()
     hbm = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = info["alg_bytes"] / (kern_ms / 1e3) / 1e9
-    traffic = profile_traffic("plan_kernel_fp32_128taxa_100ksites.md")
+    traffic = profile_traffic("walk_kernel_fp32_128taxa_100ksites.md")
 
     # Oracle check of both forms (FP64 oracle on the same plan).
     cpu = None
@@ -300,6 +332,8 @@ def run_ours(args, dist):
                            node_updates_per_eval=nops,
                            evals_per_step=args.batch,
                            parallelism="replicas" if ws > 1 else "single",
+                           walker_shape=res["fp32"]["shape"],
+                           walker_shape_fp64=fp64["shape"],
                            l2_flush="inputs>L2 (each step writes %.2f GB of CLs)"
                                     % (written / 1e9)),
             "e2e": {"value": e2e, "unit": UNIT,
@@ -365,6 +399,8 @@ def run_batch(args, dist):
             liks[prec] = [c.lik(lib=gpu, precision=prec) for c in cases]
             for lk in liks[prec]:
                 lk.prepare_plan()
+        shape = autotune(gpu, prec, args, liks=liks[prec]) if not per_node \
+            else None
         b = Batch(liks[prec], prec, per_node=per_node)
         info = b.info()
         lnls = b.run()
@@ -375,7 +411,8 @@ def run_batch(args, dist):
         t = b.time(args.steps if not per_node else max(1, args.steps // 10))
         ck = clocks.stop() if key == "fp32_batched" else None
         b.close()
-        res[key] = {"info": info, "t": t, "lnL": lnls, "clocks": ck}
+        res[key] = {"info": info, "t": t, "lnL": lnls, "clocks": ck,
+                    "shape": shape}
     check = {}
     if not args.no_cpu:
         from oracle import oracle
@@ -400,7 +437,8 @@ def run_batch(args, dist):
         "data": "synthetic (seeded)",
         "config": dict(BATCH, jobs=len(cases), updates_per_run=upd,
                        items=fb["info"]["items"], grid=fb["info"]["grid"],
-                       setup_s=round(setup_s, 1)),
+                       setup_s=round(setup_s, 1), walker_shape=fb["shape"],
+                       walker_shape_fp64=res["fp64_batched"]["shape"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "traffic": None},
         "gpu_launches": args.steps * fb["info"]["launches_per_run"],
@@ -450,6 +488,10 @@ def run_mc3(args, dist):
         port.port_set_threads(os.cpu_count() or 1)
     out = {}
     for prec in ("fp32", "fp64"):
+        lk = case.lik(lib=gpu, precision=prec, alignment=aln)
+        lk.prepare_plan()
+        shape = autotune(gpu, prec, args, lik=lk)
+        del lk
         m = Mc3(case.tree(aln.taxaMap), aln, case.params["rates"],
                 case.params["freqs"], alpha=0.5, ncat=4,
                 nchains=w["nchains"], heat_delta=w["heat_delta"],
@@ -479,7 +521,7 @@ def run_mc3(args, dist):
                                      max(1, st["accepts"].sum() +
                                          st["rejects"].sum())),
                      "swaps": int(st["swaps"].sum()) // 2,
-                     "drift": drift, "clocks": ck,
+                     "drift": drift, "clocks": ck, "shape": shape,
                      "trace_head": [float(x) for x in m.trace(8)]}
         m.close()
     f32, f64 = out["fp32"], out["fp64"]
@@ -490,7 +532,8 @@ def run_mc3(args, dist):
         "ms_per_step": 1e3 * f32["secs"] / gens, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": dict(w, gens=gens, patterns=aln.nchars),
+        "config": dict(w, gens=gens, patterns=aln.nchars,
+                       walker_shape=f32["shape"], walker_shape_fp64=f64["shape"]),
         "fp64_plain_gens_per_s": f64["gens_per_s"],
         "fp32_over_fp64": f32["gens_per_s"] / f64["gens_per_s"],
         "accept_rate": f32["accept_rate"], "swaps": f32["swaps"],
@@ -546,7 +589,15 @@ def run_serve(args, dist):
     setup_s = time.perf_counter() - t0
     rates = args.rates or SERVE["rates"]
     out = {}
+    from crux_gb300 import _native
+    gpu = _native.load()
+    # Tune the walker on the median-sized dataset of the pool.
+    med = sorted(base, key=lambda r: r.req.ntaxa * r.req.npat)[len(base) // 2]
     for prec in ("fp32", "fp64"):
+        lk = med.case.lik(lib=gpu, precision=prec, alignment=med.alignment)
+        lk.prepare_plan()
+        out[prec + "_shape"] = autotune(gpu, prec, args, lik=lk)
+        del lk
         srv = Server(prec)
         for i, r in enumerate(base):
             srv.add_dataset(i + 1, r)
@@ -607,7 +658,8 @@ def run_serve(args, dist):
         "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": dict(SERVE, datasets=len(pool), setup_s=round(setup_s, 1),
-                       rates=rates),
+                       rates=rates, walker_shape=out["fp32_shape"],
+                       walker_shape_fp64=out["fp64_shape"]),
         "sweep_fp32": out["fp32"], "sweep_fp64": out["fp64"],
         "max_rel_err_fp32_vs_fp64": max(errs) if errs else None,
     }
@@ -621,6 +673,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--shape", type=lambda v: tuple(int(x) for x in v.split(",")),
+                    default=None,
+                    help="walker shape tile,threads_per_pattern,stack_bytes "
+                         "instead of autotuning")
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU baseline and the oracle check")
     ap.add_argument("--cpu-steps", type=int, default=3)

@@ -13,8 +13,10 @@ namespace cxg {
 // Patterns are padded to a multiple of this on the device, so that every
 // plane of a CL buffer starts on a 512-byte boundary.
 constexpr unsigned kPatternQuantum = 128;
-// Largest CTA of the plan walkers (one thread per pattern of the tile).
+// Most patterns per tile.
 constexpr unsigned kBlock = 128;
+// Largest CTA of the plan walkers: tile patterns x threads per pattern.
+constexpr unsigned kMaxThreads = 256;
 // Default patterns per tile.
 constexpr unsigned kTile = 64;
 // Most shared-memory stack slots per tile.
@@ -86,7 +88,7 @@ struct PlanArgs {
     uint32_t nops;
     uint32_t nleaf;
     uint32_t nslot;       // shared-memory stack slots per tile
-    uint32_t tile;        // patterns per CTA (== blockDim.x)
+    uint32_t tile;        // patterns per CTA (blockDim.x / tpp)
     uint32_t kact;        // active components (weightScaled != 0)
     uint32_t npat;        // patterns (mschars)
     uint32_t ppad;        // padded pattern stride
@@ -104,7 +106,27 @@ struct PlanArgs {
     const double *ltab;   // FP64 plans: [ntab][16 masks][kact][4]
     uint32_t ntiles;      // tiles of this job (ppad / tile)
     uint32_t no_root;     // 1: stop after the ops (per-node launches)
+    uint32_t tpp;         // threads per pattern (each holds kact / tpp
+                          // components); 0 is read as 1
 };
+
+// Threads per pattern a walker is built for with `kact` components: 1 for
+// every shape; 2 and 4 for the FP32 form when they divide kact.
+inline bool walker_shape_ok(int precision, unsigned kact, unsigned tpp) {
+    if (tpp == 1) return kact >= 1 && kact <= kMaxComps;
+    if (precision != CXG_FP32 || (tpp != 2 && tpp != 4)) return false;
+    return kact % tpp == 0 && kact / tpp <= (tpp == 2 ? 4u : 2u);
+}
+
+// Threads per pattern for a new plan: the tuned value where the walker is
+// built for it (walker_shape_ok, tile x tpp <= kMaxThreads), else 1.
+inline unsigned tuned_tpp(int precision, unsigned kact, unsigned tile) {
+    unsigned t = 0, tpp = 1;
+    size_t b = 0;
+    cxgTuneGet(&t, &tpp, &b);
+    if (!walker_shape_ok(precision, kact, tpp) || tile * tpp > kMaxThreads) tpp = 1;
+    return tpp;
+}
 
 // One (job, tile) work item of a batched launch.
 struct WalkItem {
@@ -123,6 +145,7 @@ struct BatchArgs {
     unsigned *counter;
     uint32_t tile, ring, kact;
     uint32_t max_nslot, max_nleaf, max_rstride;
+    uint32_t tpp;         // threads per pattern (all jobs); 0 is read as 1
 };
 
 size_t plan_smem_bytes(int precision, unsigned kact, unsigned tile,
@@ -132,7 +155,7 @@ cudaError_t launch_batch(int precision, const BatchArgs &b, unsigned grid,
                          cudaStream_t s);
 // Resident CTAs per SM of the batched walker for this shape.
 int batch_ctas_per_sm(int precision, unsigned kact, unsigned tile,
-                      size_t smem);
+                      unsigned tpp, size_t smem);
 
 // Inputs of the P-matrix kernel: one thread per (child, active comp); the
 // P matrix (FP64 arithmetic, stored as the plan's precision) goes into the

@@ -98,7 +98,7 @@ __device__ __forceinline__ Comp warp_comp(Comp v) {
 // partials into a.total.
 __device__ void reduce_sites(const PlanArgs &a, unsigned tile_idx, double v,
                              bool neg_inf) {
-    __shared__ Comp warp_part[kBlock / 32];
+    __shared__ Comp warp_part[kMaxThreads / 32];
     __shared__ unsigned ninf_block;
     __shared__ bool last;
     const unsigned nwarp = blockDim.x / 32;
@@ -293,22 +293,39 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     return false;
 }
 
-// Walk every op of job `a` for tile `tile_idx` (one thread per pattern),
-// aggregate the root and reduce.  `phase` (thread 0 only) holds, per ring
-// stage, the parity of the next completion to wait for; it persists across
-// the items a CTA processes.  Returns false if a bounded wait gave up.
-template <typename T, int KT>
+// Max over the G consecutive lanes that share a pattern.
+template <int G, typename X>
+__device__ __forceinline__ X group_max(X x) {
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+    return x;
+}
+
+// Walk every op of job `a` for tile `tile_idx`, aggregate the root and
+// reduce.  G consecutive threads share a pattern, each holding KT of its
+// KT*G components; with G = 1 one thread owns a pattern.  Every G gives the
+// same bits: scalers are maxima over the group, and the root sum and the
+// tile reduction run in the G = 1 order.  `phase` (thread 0 only) holds,
+// per ring stage, the parity of the next completion to wait for; it
+// persists across the items a CTA processes.  Returns false if a bounded
+// wait gave up.
+template <typename T, int KT, int G>
 __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
                           const SmemLayout &Lay, unsigned ring_depth,
                           uint32_t &phase) {
     typedef typename Prec<T>::S S;
     typedef typename Prec<T>::V V;
     constexpr int U = Prec<T>::U;
+    constexpr int KA = KT * G;  // active components of the job
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_ok;
-    const unsigned tile = blockDim.x;
+    const unsigned nthr = blockDim.x;
+    const unsigned tile = nthr / G;
     const unsigned tid = threadIdx.x;
-    const unsigned p = tile_idx * tile + tid;
+    const unsigned pl = tid / G;   // pattern within the tile
+    const unsigned g = tid % G;    // component group of this thread
+    const unsigned k0 = g * KT;    // its first component
+    const unsigned p = tile_idx * tile + pl;
     const size_t ppad = a.ppad;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + Lay.bars);
     unsigned char *ring = smem + Lay.ring;
@@ -328,7 +345,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
     }
     // Stage this tile's leaf masks with 16-byte loads.
     const unsigned chunks = tile / 16;
-    for (unsigned i = tid; i < a.nleaf * chunks; i += tile) {
+    for (unsigned i = tid; i < a.nleaf * chunks; i += nthr) {
         const unsigned l = i / chunks, c = i % chunks;
         const uint4 *src =
             reinterpret_cast<const uint4 *>(a.leaves[l] + (size_t)tile_idx * tile) + c;
@@ -360,18 +377,18 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
         lns = S(0);
         for (unsigned ci = 0; ci < nchild; ++ci) {
             const RecChild ch = kids[ci];
-            const V *P = reinterpret_cast<const V *>(pmats + (size_t)ci * KT * 16);
+            const V *P = reinterpret_cast<const V *>(pmats + ((size_t)ci * KA + k0) * 16);
             T msg[KT * 4];
             const bool leaf = (ch.src == SRC_LEAF);
             const bool in_slot = (ch.src == SRC_SLOT);
-            const unsigned m = leaf ? masks[(size_t)ch.idx * tile + tid] : 0u;
-            const V *xs = in_slot ? slots + (size_t)ch.idx * KT * U * tile + tid
-                                  : static_cast<const V *>(ch.data) + p;
+            const unsigned m = leaf ? masks[(size_t)ch.idx * tile + pl] : 0u;
+            const V *xs = in_slot ? slots + ((size_t)ch.idx * KA + k0) * U * tile + pl
+                                  : static_cast<const V *>(ch.data) + (size_t)k0 * U * ppad + p;
             const size_t stride = in_slot ? tile : ppad;
             if (sizeof(T) == 8 && leaf) {
                 // FP64 leaves: table lookup (no FP64 arithmetic).
                 const double2 *t = reinterpret_cast<const double2 *>(
-                    a.ltab + ((size_t)ch.tab * 16 + m) * (KT * 4));
+                    a.ltab + (((size_t)ch.tab * 16 + m) * KA + k0) * 4);
 #pragma unroll
                 for (int q = 0; q < KT * 2; ++q) {
                     const double2 v = __ldg(t + q);
@@ -409,7 +426,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             }
             }
             if (!leaf) {
-                const S l = in_slot ? slot_sc[(size_t)ch.idx * tile + tid]
+                const S l = in_slot ? slot_sc[(size_t)ch.idx * tile + pl]
                                     : static_cast<const S *>(ch.scaler)[p];
                 lns = lns + l;
             }
@@ -438,6 +455,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
                      a.rec + (size_t)(o + R) * a.rstride, a.rstride, &bars[stage]);
         }
         if (sizeof(T) == 8) {
+            sc = group_max<G>(sc);
             // Reference rescale: divide by the scaler unless it is 1, add
             // its log (a zero scaler gives NaN rows and a -inf site, as in
             // the reference).
@@ -451,6 +469,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             T mx = T(0);
 #pragma unroll
             for (int q = 0; q < KT * 4; ++q) mx = fmax(mx, acc[q]);
+            mx = group_max<G>(mx);
             if (mx > T(0) && mx <= (T)3.0e38) {
                 int e;
                 frexpf((float)mx, &e);
@@ -469,17 +488,17 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             }
         }
         if (yhbm) {
-            V *y = static_cast<V *>(ydata) + p;
+            V *y = static_cast<V *>(ydata) + (size_t)k0 * U * ppad + p;
 #pragma unroll
             for (int k = 0; k < KT; ++k)
                 store4<T>(y + (size_t)k * U * ppad, ppad, acc + k * 4);
-            static_cast<S *>(yscaler)[p] = lns;
+            if (g == 0) static_cast<S *>(yscaler)[p] = lns;
         }
         if (yslot >= 0) {
-            V *ys = slots + (size_t)yslot * KT * U * tile + tid;
+            V *ys = slots + ((size_t)yslot * KA + k0) * U * tile + pl;
 #pragma unroll
             for (int k = 0; k < KT; ++k) store4<T>(ys + (size_t)k * U * tile, tile, acc + k * 4);
-            slot_sc[(size_t)yslot * tile + tid] = lns;
+            if (g == 0) slot_sc[(size_t)yslot * tile + pl] = lns;
         }
     }
 
@@ -489,17 +508,26 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
     }
     // Root aggregation (CxLik.c:598-632): L = sum_k sum_i pn[k][i] root.
     if (!a.root_last) {
-        const V *r = static_cast<const V *>(a.root) + p;
+        const V *r = static_cast<const V *>(a.root) + (size_t)k0 * U * ppad + p;
 #pragma unroll
         for (int k = 0; k < KT; ++k) load4<T>(r + (size_t)k * U * ppad, ppad, acc + k * 4);
         lns = static_cast<const S *>(a.rootsc)[p];
     }
+    // L = sum over components and states in one sequential order; every
+    // lane of the group gathers the others' entries and sums them all.
     double L = 0.0;
+    const unsigned lead = (tid & 31u) - g;
 #pragma unroll
-    for (int q = 0; q < KT * 4; ++q) L = fma(__ldg(a.pn + q), (double)acc[q], L);
+    for (int gg = 0; gg < G; ++gg) {
+#pragma unroll
+        for (int q = 0; q < KT * 4; ++q) {
+            const T x = G > 1 ? __shfl_sync(0xffffffffu, acc[q], lead + gg) : acc[q];
+            L = fma(__ldg(a.pn + gg * KT * 4 + q), (double)x, L);
+        }
+    }
     double v = 0.0;
     bool ninf = false;
-    if (p < a.npat) {
+    if (g == 0 && p < a.npat) {
         const double lsc = (sizeof(T) == 8) ? (double)lns
                                            : (double)lns * 0.69314718055994530942;
         v = (log(L) + lsc) * (double)a.freqs[p];
@@ -509,6 +537,19 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             ninf = (v < 0.0);
             v = 0.0;
         }
+    }
+    if (G > 1) {
+        // Pattern pl's value moves to thread pl, so the tile reduces in the
+        // one-thread-per-pattern order (the extra threads add exact zeros).
+        __shared__ double s_v[kBlock];
+        __shared__ unsigned char s_inf[kBlock];
+        if (g == 0) {
+            s_v[pl] = v;
+            s_inf[pl] = ninf;
+        }
+        __syncthreads();
+        v = tid < tile ? s_v[tid] : 0.0;
+        ninf = tid < tile ? s_inf[tid] != 0 : false;
     }
     reduce_sites(a, tile_idx, v, ninf);
     return true;
@@ -525,23 +566,23 @@ __device__ __forceinline__ void init_ring(const SmemLayout &Lay, unsigned R) {
 }
 
 // One plan: one CTA per tile.
-template <typename T, int KT>
-__global__ void __launch_bounds__(kBlock) walk_kernel(PlanArgs a) {
-    const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT,
-                                       blockDim.x, a.nslot, a.nleaf, a.ring,
+template <typename T, int KT, int G>
+__global__ void __launch_bounds__(kMaxThreads) walk_kernel(PlanArgs a) {
+    const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT * G,
+                                       blockDim.x / G, a.nslot, a.nleaf, a.ring,
                                        a.rstride);
     init_ring(Lay, a.ring);
     uint32_t phase = 0;
-    walk_tile<T, KT>(a, blockIdx.x, Lay, a.ring, phase);
+    walk_tile<T, KT, G>(a, blockIdx.x, Lay, a.ring, phase);
 }
 
 // Many jobs: a persistent grid claims (job, tile) items in the host's order
 // (longest first).
-template <typename T, int KT>
-__global__ void __launch_bounds__(kBlock) walk_batch_kernel(BatchArgs b) {
+template <typename T, int KT, int G>
+__global__ void __launch_bounds__(kMaxThreads) walk_batch_kernel(BatchArgs b) {
     __shared__ unsigned s_item;
-    const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT,
-                                       blockDim.x, b.max_nslot, b.max_nleaf,
+    const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT * G,
+                                       blockDim.x / G, b.max_nslot, b.max_nleaf,
                                        b.ring, b.max_rstride);
     init_ring(Lay, b.ring);
     uint32_t phase = 0;
@@ -552,7 +593,7 @@ __global__ void __launch_bounds__(kBlock) walk_batch_kernel(BatchArgs b) {
         __syncthreads();
         if (item >= b.nitems) break;
         const WalkItem it = b.items[item];
-        if (!walk_tile<T, KT>(b.jobs[it.job], it.tile, Lay, b.ring, phase)) break;
+        if (!walk_tile<T, KT, G>(b.jobs[it.job], it.tile, Lay, b.ring, phase)) break;
     }
 }
 
@@ -569,31 +610,60 @@ static cudaError_t ensure_smem(Kern k, size_t sm, size_t &optin) {
     return cudaSuccess;
 }
 
+// Instantiated walker shapes (per-thread components KT, threads per
+// pattern G): every kact with G = 1; the FP32 form also splits a pattern's
+// components over 2 or 4 threads (walker_shape_ok).
+#define CXG_SHAPES_G1(X) X(1, 1) X(2, 1) X(3, 1) X(4, 1) X(5, 1) X(6, 1) X(7, 1) X(8, 1)
+#define CXG_SHAPES_GN(X) X(1, 2) X(2, 2) X(3, 2) X(4, 2) X(1, 4) X(2, 4)
+
+template <typename T, int KT, int G>
+static cudaError_t walk_fn(size_t sm, void (**fn)(PlanArgs)) {
+    static size_t optin = 0;
+    *fn = walk_kernel<T, KT, G>;
+    return ensure_smem(walk_kernel<T, KT, G>, sm, optin);
+}
+template <typename T, int KT, int G>
+static cudaError_t batch_fn(size_t sm, void (**fn)(BatchArgs)) {
+    static size_t optin = 0;
+    *fn = walk_batch_kernel<T, KT, G>;
+    return ensure_smem(walk_batch_kernel<T, KT, G>, sm, optin);
+}
+
+// The walker for (kact, G), with its dynamic shared memory limit raised to
+// `sm` bytes.
+template <typename T, typename Fn>
+static cudaError_t pick_walker(unsigned kact, unsigned G, size_t sm, Fn *fn, bool batch) {
+#define CXG_X(KT, GG)                                                              \
+    if (kact == (KT) * (GG) && G == (GG)) {                                        \
+        if (batch) return batch_fn<T, KT, GG>(sm, reinterpret_cast<void (**)(BatchArgs)>(fn)); \
+        return walk_fn<T, KT, GG>(sm, reinterpret_cast<void (**)(PlanArgs)>(fn)); \
+    }
+    CXG_SHAPES_G1(CXG_X)
+    if constexpr (sizeof(T) == 4) {
+        CXG_SHAPES_GN(CXG_X)
+    }
+#undef CXG_X
+    return cudaErrorInvalidValue;
+}
+
 template <typename T>
 static cudaError_t launch_plan_t(int precision, const PlanArgs &a,
                                  cudaStream_t s) {
+    const unsigned G = a.tpp ? a.tpp : 1;
     const unsigned nb = plan_blocks(a.ppad, a.tile);
     const size_t sm = plan_smem_bytes(precision, a.kact, a.tile, a.nslot, a.nleaf,
                                       a.ring, a.rstride);
-    switch (a.kact) {
-#define CXG_K(K)                                                           \
-    case K: {                                                              \
-        static size_t optin = 0;                                           \
-        cudaError_t e = ensure_smem(walk_kernel<T, K>, sm, optin);         \
-        if (e != cudaSuccess) return e;                                    \
-        walk_kernel<T, K><<<nb, a.tile, sm, s>>>(a);                       \
-        break;                                                             \
-    }
-        CXG_K(1) CXG_K(2) CXG_K(3) CXG_K(4) CXG_K(5) CXG_K(6) CXG_K(7) CXG_K(8)
-#undef CXG_K
-        default:
-            return cudaErrorInvalidValue;
-    }
+    void (*fn)(PlanArgs) = nullptr;
+    cudaError_t e = pick_walker<T>(a.kact, G, sm, &fn, false);
+    if (e != cudaSuccess) return e;
+    fn<<<nb, a.tile * G, sm, s>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s) {
+    const unsigned G = a.tpp ? a.tpp : 1;
     if (a.tile == 0 || a.tile > kBlock || a.tile % 32 || a.ppad % a.tile ||
+        a.tile * G > kMaxThreads || !walker_shape_ok(precision, a.kact, G) ||
         a.ring == 0 || a.ring > 8 || a.rstride % 16 || a.rstride == 0 ||
         a.ntiles != a.ppad / a.tile)
         return cudaErrorInvalidValue;
@@ -604,28 +674,21 @@ cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s) {
 template <typename T>
 static cudaError_t launch_batch_t(int precision, const BatchArgs &b,
                                   unsigned grid, cudaStream_t s) {
+    const unsigned G = b.tpp ? b.tpp : 1;
     const size_t sm = plan_smem_bytes(precision, b.kact, b.tile, b.max_nslot,
                                       b.max_nleaf, b.ring, b.max_rstride);
-    switch (b.kact) {
-#define CXG_K(K)                                                           \
-    case K: {                                                              \
-        static size_t optin = 0;                                           \
-        cudaError_t e = ensure_smem(walk_batch_kernel<T, K>, sm, optin);   \
-        if (e != cudaSuccess) return e;                                    \
-        walk_batch_kernel<T, K><<<grid, b.tile, sm, s>>>(b);               \
-        break;                                                             \
-    }
-        CXG_K(1) CXG_K(2) CXG_K(3) CXG_K(4) CXG_K(5) CXG_K(6) CXG_K(7) CXG_K(8)
-#undef CXG_K
-        default:
-            return cudaErrorInvalidValue;
-    }
+    void (*fn)(BatchArgs) = nullptr;
+    cudaError_t e = pick_walker<T>(b.kact, G, sm, &fn, true);
+    if (e != cudaSuccess) return e;
+    fn<<<grid, b.tile * G, sm, s>>>(b);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batch(int precision, const BatchArgs &b, unsigned grid,
                          cudaStream_t s) {
-    if (b.tile == 0 || b.tile > kBlock || b.tile % 32 || b.ring == 0 ||
+    const unsigned G = b.tpp ? b.tpp : 1;
+    if (b.tile == 0 || b.tile > kBlock || b.tile % 32 || b.tile * G > kMaxThreads ||
+        !walker_shape_ok(precision, b.kact, G) || b.ring == 0 ||
         b.ring > 8 || b.max_rstride % 16 || b.max_rstride == 0 || grid == 0)
         return cudaErrorInvalidValue;
     return precision == CXG_FP32 ? launch_batch_t<float>(precision, b, grid, s)
@@ -633,30 +696,21 @@ cudaError_t launch_batch(int precision, const BatchArgs &b, unsigned grid,
 }
 
 template <typename T>
-static int batch_occ_t(unsigned kact, unsigned tile, size_t smem) {
+static int batch_occ_t(unsigned kact, unsigned tile, unsigned G, size_t smem) {
+    void (*fn)(BatchArgs) = nullptr;
+    cudaError_t e = pick_walker<T>(kact, G, smem, &fn, true);
     int n = 0;
-    cudaError_t e = cudaErrorInvalidValue;
-    switch (kact) {
-#define CXG_K(K)                                                                \
-    case K: {                                                                   \
-        static size_t optin = 0;                                                \
-        e = ensure_smem(walk_batch_kernel<T, K>, smem, optin);                  \
-        if (e == cudaSuccess)                                                   \
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(                  \
-                &n, walk_batch_kernel<T, K>, (int)tile, smem);                  \
-        break;                                                                  \
-    }
-        CXG_K(1) CXG_K(2) CXG_K(3) CXG_K(4) CXG_K(5) CXG_K(6) CXG_K(7) CXG_K(8)
-#undef CXG_K
-        default:
-            break;
-    }
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, (int)(tile * G), smem);
     return e == cudaSuccess ? n : 0;
 }
 
-int batch_ctas_per_sm(int precision, unsigned kact, unsigned tile, size_t smem) {
-    return precision == CXG_FP32 ? batch_occ_t<float>(kact, tile, smem)
-                                 : batch_occ_t<double>(kact, tile, smem);
+int batch_ctas_per_sm(int precision, unsigned kact, unsigned tile, unsigned tpp,
+                      size_t smem) {
+    const unsigned G = tpp ? tpp : 1;
+    if (!walker_shape_ok(precision, kact, G) || tile * G > kMaxThreads) return 0;
+    return precision == CXG_FP32 ? batch_occ_t<float>(kact, tile, G, smem)
+                                 : batch_occ_t<double>(kact, tile, G, smem);
 }
 
 __global__ void qdecomp_kernel(const double *rtri, const double *pi,

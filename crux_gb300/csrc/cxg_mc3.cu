@@ -564,9 +564,10 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     const size_t elt = cfg->precision == CXG_FP32 ? 4 : 8;
     d.rstride = (uint32_t)((sizeof(RecHead) + 3 * (sizeof(RecChild) + K * 16 * elt) + 15) &
                            ~(size_t)15);
-    unsigned tile = 0;
+    unsigned tile = 0, tpp_q = 1;
     size_t budget = 0;
-    cxgTuneGet(&tile, &budget);
+    cxgTuneGet(&tile, &tpp_q, &budget);
+    const unsigned tpp = tuned_tpp(cfg->precision, K, tile);
     d.ntiles = d.ppad / tile;
     d.seed = cfg->seed;
     d.swap_stride = cfg->swap_stride ? cfg->swap_stride : 1;
@@ -703,6 +704,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
         a.nleaf = 0;
         a.nslot = 0;
         a.tile = tile;
+        a.tpp = tpp;
         a.kact = K;
         a.npat = d.npat;
         a.ppad = d.ppad;
@@ -732,6 +734,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     ba.nitems = (uint32_t)items.size();
     ba.counter = d.counter;
     ba.tile = tile;
+    ba.tpp = tpp;
     ba.ring = kRing;
     ba.kact = K;
     ba.max_nslot = 0;
@@ -741,7 +744,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int per = batch_ctas_per_sm(cfg->precision, K, tile, smem);
+    const int per = batch_ctas_per_sm(cfg->precision, K, tile, tpp, smem);
     if (per <= 0) {
         mc3_free(h);
         return fail(CXG_EINVAL, "cxgMc3Create: walker does not fit an SM");

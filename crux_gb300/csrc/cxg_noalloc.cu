@@ -198,7 +198,13 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
             return fail(CXG_EINVAL, "cxgLikExecuteNoAlloc: leaf tables above 1.5 MiB");
     }
     const size_t o_part = al16(o_ltab + (ltab_bytes ? ltab_bytes : 16));
-    const unsigned tile = kTile;
+    unsigned tile = kTile;
+    size_t budget = 0;
+    {
+        unsigned tpp_q = 1;
+        cxgTuneGet(&tile, &tpp_q, &budget);
+    }
+    const unsigned tpp = tuned_tpp(prec, kact, tile);
     const unsigned nb = plan_blocks(ppad, tile);
     if (o_part + (size_t)nb * 16 > kNaScratchBytes)
         return fail(CXG_EINVAL, "cxgLikExecuteNoAlloc: scratch too small");
@@ -231,13 +237,8 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
     const size_t leaf_b = plan_smem_bytes(prec, kact, tile, 0, leaf_count_est,
                                           kRing, (unsigned)rstride);
     unsigned cap = 0;
-    {
-        unsigned tile_q = 0;
-        size_t budget = 0;
-        cxgTuneGet(&tile_q, &budget);
-        if (budget > leaf_b) cap = (unsigned)((budget - leaf_b) / slot_b);
-        if (cap > kMaxSlots) cap = kMaxSlots;
-    }
+    if (budget > leaf_b) cap = (unsigned)((budget - leaf_b) / slot_b);
+    if (cap > kMaxSlots) cap = kMaxSlots;
     uint64_t *dsts = reinterpret_cast<uint64_t *>(h + o_dst);
     int32_t *tabs = reinterpret_cast<int32_t *>(h + o_tab);
     double *elens = reinterpret_cast<double *>(h + o_elen);
@@ -366,6 +367,7 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
     a.nleaf = nleaf;
     a.nslot = used;
     a.tile = tile;
+    a.tpp = tpp;
     a.kact = kact;
     a.npat = npat;
     a.ppad = ppad;

@@ -103,6 +103,7 @@ struct HostKid {
 struct HostPlan {
     bool ready = false;
     unsigned K = 0, ppad = 0, ntiles = 0, nops = 0, nk = 0, nslot = 0, nhbm = 0;
+    unsigned tile = kTile, tpp = 1;
     size_t rstride = 0, job_bytes = 0, data_bytes = 0;
     std::vector<int> order, slot, hbm;
     std::vector<std::vector<HostKid>> kids;
@@ -221,7 +222,11 @@ void plan_request(SrvRequest &rq, int prec) {
     const unsigned N = r.ntaxa, NN = 2 * N - 2;
     P.K = r.ncat + (r.pinv > 0.0 ? 1 : 0);
     P.ppad = pad_patterns(r.npat);
-    P.ntiles = P.ppad / kTile;
+    unsigned tq = 0;
+    size_t budget = 0;
+    cxgTuneGet(&P.tile, &tq, &budget);
+    P.tpp = tuned_tpp(prec, P.K, P.tile);
+    P.ntiles = P.ppad / P.tile;
     const size_t elt = prec == CXG_FP32 ? 4 : 8;
     const unsigned K = P.K;
     P.rstride = (sizeof(RecHead) + 3 * (sizeof(RecChild) + K * 16 * elt) + 15) & ~(size_t)15;
@@ -244,13 +249,10 @@ void plan_request(SrvRequest &rq, int prec) {
         std::reverse(P.order.begin(), P.order.end());  // children first
     }
     const unsigned nops = (unsigned)P.order.size();
-    unsigned tq = 0;
-    size_t budget = 0;
-    cxgTuneGet(&tq, &budget);
-    const size_t base_b = plan_smem_bytes(prec, K, kTile, 0, 0, kRing, (unsigned)P.rstride);
+    const size_t base_b = plan_smem_bytes(prec, K, P.tile, 0, 0, kRing, (unsigned)P.rstride);
     const size_t slot_b =
-        plan_smem_bytes(prec, K, kTile, 1, 0, kRing, (unsigned)P.rstride) - base_b;
-    const size_t leaf_b = plan_smem_bytes(prec, K, kTile, 0, N, kRing, (unsigned)P.rstride);
+        plan_smem_bytes(prec, K, P.tile, 1, 0, kRing, (unsigned)P.rstride) - base_b;
+    const size_t leaf_b = plan_smem_bytes(prec, K, P.tile, 0, N, kRing, (unsigned)P.rstride);
     unsigned cap = budget > leaf_b ? (unsigned)((budget - leaf_b) / slot_b) : 0;
     if (cap > kMaxSlots) cap = kMaxSlots;
     std::vector<int> owner(cap, -1), op_of(NN, -1);
@@ -516,7 +518,8 @@ int prepare_job(cxgServer *S, SrvJob &J) {
     a.nops = P.nops;
     a.nleaf = N;
     a.nslot = P.nslot;
-    a.tile = kTile;
+    a.tile = P.tile;
+    a.tpp = P.tpp;
     a.kact = K;
     a.npat = r.npat;
     a.ppad = J.ppad;
@@ -548,7 +551,7 @@ int prepare_job(cxgServer *S, SrvJob &J) {
     return 0;
 }
 
-// Launch one batch of prepared jobs (all with the same kact).
+// Launch one batch of prepared jobs (all of one walker shape).
 int launch_batch_of(cxgServer *S, SrvBatch &B, cudaStream_t st) {
     const size_t n = B.jobs.size();
     std::vector<PlanArgs> jobs(n);
@@ -604,19 +607,20 @@ int launch_batch_of(cxgServer *S, SrvBatch &B, cudaStream_t st) {
     ba.items = (const WalkItem *)(B.mem + o_items);
     ba.nitems = (uint32_t)items.size();
     ba.counter = (unsigned *)(res + n * 32);
-    ba.tile = kTile;
+    ba.tile = B.jobs[0]->a.tile;
+    ba.tpp = B.jobs[0]->a.tpp;
     ba.ring = kRing;
     ba.kact = B.jobs[0]->kact;
     ba.max_nslot = max_nslot;
     ba.max_nleaf = max_nleaf;
     ba.max_rstride = max_rstride;
     const int prec = S->cfg.precision;
-    const size_t smem = plan_smem_bytes(prec, ba.kact, kTile, max_nslot, max_nleaf,
+    const size_t smem = plan_smem_bytes(prec, ba.kact, ba.tile, max_nslot, max_nleaf,
                                         kRing, max_rstride);
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int per = batch_ctas_per_sm(prec, ba.kact, kTile, smem);
+    const int per = batch_ctas_per_sm(prec, ba.kact, ba.tile, ba.tpp, smem);
     if (per <= 0) return fail(CXG_EINVAL, "server: walker does not fit an SM");
     cudaError_t e = launch_batch(prec, ba, (unsigned)(per * nsm), st);
     if (e != cudaSuccess) return cuda_fail(e, "walk_batch_kernel (server)");
@@ -706,8 +710,11 @@ void lnl_loop(cxgServer *S) {
         // 3. Launch a batch per component count while a stream is free.
         if (!ready.empty() && inflight.size() < 2) {
             // A failed launch must give its slot back.
+            // One launch per walker shape: components, tile, threads per
+            // pattern.
             std::map<unsigned, std::vector<SrvJob *>> byk;
-            for (SrvJob *J : ready) byk[J->kact].push_back(J);
+            for (SrvJob *J : ready)
+                byk[J->kact | J->a.tile << 8 | J->a.tpp << 16].push_back(J);
             ready.clear();
             for (auto &kv : byk) {
                 SrvBatch B;

@@ -1,0 +1,111 @@
+"""Autotuner of the plan walker's launch shape.
+
+The walker's shape is three numbers, set process-wide by ``cxgTune``
+(include/cxlik_gpu.h) and read when a plan, batch, MC3 run or server
+request is translated:
+
+* ``tile``: patterns per CTA (32, 64 or 128);
+* ``tpp``: threads per pattern (1, 2 or 4). The FP32 form splits a
+  pattern's components over that many consecutive threads when the count
+  divides them;
+* ``budget``: shared-memory bytes for the CL stack of a tile. This caps the
+  number of stack slots; results that find no slot go through HBM.
+
+Every shape gives bit-identical results, so the choice is speed alone.
+``tune_plan`` and ``tune_batch`` time each candidate on the caller's own
+workload with CUDA events (the walker launch, after warm-up), set the
+fastest with ``cxgTune`` and return the whole table.
+"""
+import ctypes
+import itertools
+
+TILES = (32, 64, 128)
+TPPS = (1, 2, 4)
+BUDGETS = (0, 12 << 10, 24 << 10, 48 << 10, 96 << 10)
+MAX_THREADS = 256
+
+
+def get(lib):
+    """The current shape as (tile, tpp, budget)."""
+    t, g, b = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_size_t()
+    lib.cxgTuneGet(ctypes.byref(t), ctypes.byref(g), ctypes.byref(b))
+    return t.value, g.value, b.value
+
+
+def set_shape(lib, tile, tpp, budget):
+    if lib.cxgTune(tile, tpp, budget) != 0:
+        raise ValueError("cxgTune: %s" % lib.cxgLastError().decode())
+
+
+def shape_ok(precision, kact, tile, tpp):
+    """Whether the library has a walker for this shape (the C rule of
+    walker_shape_ok, crux_gb300/csrc/cxg_internal.h)."""
+    if tile * tpp > MAX_THREADS:
+        return False
+    if tpp == 1:
+        return 1 <= kact <= 8
+    if precision != "fp32" or kact % tpp:
+        return False
+    return kact // tpp <= (4 if tpp == 2 else 2)
+
+
+def candidates(precision, kact, tiles=TILES, tpps=TPPS, budgets=BUDGETS):
+    return [(t, g, b) for t, g, b in itertools.product(tiles, tpps, budgets)
+            if shape_ok(precision, kact, t, g)]
+
+
+def active_components(lik):
+    """Mixture components with non-zero weight (the walker's kact)."""
+    L = lik.lik
+    return sum(1 for c in range(L.compsLen) if L.comps[c].weightScaled != 0.0)
+
+
+def _sweep(lib, shapes, measure):
+    saved = get(lib)
+    table = []
+    try:
+        for shape in shapes:
+            set_shape(lib, *shape)
+            ms = measure()
+            table.append({"tile": shape[0], "tpp": shape[1],
+                          "budget": shape[2], "ms": ms})
+    finally:
+        set_shape(lib, *saved)
+    best = min(table, key=lambda r: r["ms"])
+    set_shape(lib, best["tile"], best["tpp"], best["budget"])
+    return {"best": best, "table": table}
+
+
+def tune_plan(lik, precision="fp32", iters=20, shapes=None):
+    """Tune on one Lik's current full plan (``lik._prep`` done); the time is
+    the walker kernel's mean over `iters` back-to-back runs."""
+    from .plan import Plan
+    shapes = shapes or candidates(precision, active_components(lik))
+
+    def measure():
+        plan = Plan(lik, precision)
+        try:
+            plan.time(3)
+            return plan.time(iters)["kernel_ms"]
+        finally:
+            plan.close()
+
+    return _sweep(lik.lib, shapes, measure)
+
+
+def tune_batch(liks, precision="fp32", iters=5, shapes=None):
+    """Tune on a batch of planned Liks (one persistent launch); the time is
+    the walker's mean over `iters` graph replays."""
+    from .batch import Batch
+    lk = liks[0]
+    shapes = shapes or candidates(precision, active_components(lk))
+
+    def measure():
+        b = Batch(liks, precision)
+        try:
+            b.time(2)
+            return b.time(iters)["walk_ms"]
+        finally:
+            b.close()
+
+    return _sweep(lk.lib, shapes, measure)

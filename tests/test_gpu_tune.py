@@ -1,0 +1,101 @@
+"""Walker shapes and the autotuner: every (tile, threads per pattern,
+stack budget) gives bit-identical lnLs and site lnLs, in single plans and
+in batches, within the oracle tolerance of each form; the tuner times its
+candidates and sets the fastest."""
+import numpy as np
+import pytest
+
+from crux_gb300 import synth, tune
+from crux_gb300.batch import Batch
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp32": 1e-6, "fp64": 1e-11}
+
+
+@pytest.fixture
+def restore(gpu):
+    saved = tune.get(gpu)
+    yield
+    tune.set_shape(gpu, *saved)
+
+
+@pytest.mark.parametrize("pinv", [0.0, 0.2])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_every_shape_same_bits(gpu, port, restore, precision, pinv):
+    case = synth.Case(40, 3000, 0.1, 77, pinv=pinv, gap_frac=0.01)
+    want = case.lik(lib=port).lnL()
+    lik = case.lik(lib=gpu, precision=precision)
+    kact = tune.active_components(lik)
+    shapes = tune.candidates(precision, kact, budgets=(0, 24 << 10, 96 << 10))
+    assert any(g > 1 for _, g, _ in shapes) == (precision == "fp32" and
+                                                kact % 2 == 0)
+    first = None
+    for shape in shapes:
+        tune.set_shape(gpu, *shape)
+        lik.lik.invalidate = True
+        v = lik.lnL()
+        lik.lik.invalidate = True
+        s = lik.siteLnLs()
+        if first is None:
+            first = (v, s)
+            assert abs(v - want) <= TOL[precision] * abs(want), (v, want)
+        else:
+            assert v == first[0], shape
+            assert s == first[1], shape
+
+
+def test_batch_every_shape_same_bits(gpu, restore):
+    rng = np.random.default_rng(5)
+    cases = [synth.Case(int(rng.integers(8, 70)), int(rng.integers(300, 5000)),
+                        0.1, 300 + i) for i in range(6)]
+    liks = [c.lik(lib=gpu, precision="fp32") for c in cases]
+    first = None
+    for shape in tune.candidates("fp32", 4, budgets=(0, 24 << 10)):
+        tune.set_shape(gpu, *shape)
+        for lk in liks:
+            lk.prepare_plan()
+        b = Batch(liks, "fp32")
+        out = b.run()
+        b.close()
+        if first is None:
+            first = out
+        else:
+            assert np.array_equal(out, first), shape
+
+
+def test_tune_plan_sets_fastest(gpu, restore):
+    case = synth.Case(32, 20000, 0.1, 91)
+    lik = case.lik(lib=gpu, precision="fp32")
+    lik.prepare_plan()
+    shapes = [(64, 1, 24 << 10), (64, 4, 24 << 10), (128, 2, 12 << 10)]
+    res = tune.tune_plan(lik, "fp32", iters=5, shapes=shapes)
+    assert len(res["table"]) == 3
+    best = res["best"]
+    assert best["ms"] == min(r["ms"] for r in res["table"])
+    assert tune.get(gpu) == (best["tile"], best["tpp"], best["budget"])
+
+
+def test_mc3_and_server_follow_the_shape(gpu, restore):
+    """MC3 chains and server requests translated under different shapes
+    give the same bits."""
+    from crux_gb300.mc3 import Mc3
+    from crux_gb300.serve import LNL, PreparedRequest, Server
+    case = synth.Case(16, 1500, 0.1, 12)
+    aln = case.alignment()
+    req = PreparedRequest(case, LNL)
+    traces, served = [], []
+    for shape in [(64, 1, 24 << 10), (64, 4, 24 << 10), (32, 2, 0)]:
+        tune.set_shape(gpu, *shape)
+        m = Mc3(case.tree(aln.taxaMap), aln, case.params["rates"],
+                case.params["freqs"], alpha=0.5, ncat=4, nchains=2, seed=3,
+                moves={"brlen": 1.0, "nni": 1.0, "rates": 0.5, "alpha": 0.5},
+                precision="fp32", graph_gens=4)
+        m.run(24)
+        traces.append(m.trace(25))
+        m.close()
+        srv = Server("fp32")
+        served.append(srv.wait(srv.submit(req))[0])
+        srv.close()
+    assert all(np.array_equal(traces[0], t) for t in traces[1:])
+    assert served[0] == served[1] == served[2]

@@ -85,3 +85,16 @@ def test_ref_port_agree(ref, port):
         for u, v in zip(x, y):
             for p, q in zip(u, v):
                 assert math.isclose(p, q, rel_tol=1e-12)
+
+
+def test_tune_candidates_follow_walker_shapes():
+    """The autotuner offers only shapes the library has a walker for."""
+    from crux_gb300 import tune
+    c4 = tune.candidates("fp32", 4)
+    assert (64, 4, 24 << 10) in c4 and (128, 2, 0) in c4
+    assert all(t * g <= 256 for t, g, _ in c4)
+    assert (128, 4, 0) not in c4
+    assert all(g == 1 for _, g, _ in tune.candidates("fp32", 5))
+    assert all(g == 1 for _, g, _ in tune.candidates("fp64", 4))
+    assert {g for _, g, _ in tune.candidates("fp32", 6)} == {1, 2}
+    assert {g for _, g, _ in tune.candidates("fp32", 8)} == {1, 2, 4}
