@@ -546,6 +546,110 @@ def run_mc3(args, dist):
     dist.close()
 
 
+DIRTY = {"workload": "dirty64_gtr_gamma4_inv_64taxa_10ksites",
+         "ntaxa": 64, "nsites": 10000, "mean_brlen": 0.05, "alpha": 0.5,
+         "ncat": 4, "pinv": 0.2, "gap_frac": 0.005, "recomputes": 10000,
+         "rescale": [0.5, 2.0], "seed": 20261208}
+
+
+def run_dirty(args, dist):
+    """A full lnL, then dirty-path lnLs after random single-branch rescales
+    (x U(0.5, 2)), each through the public Lik.lnL call (planning included).
+    The FP32 form and the plain FP64 form replay the same rescales; so does
+    the FP64 oracle on the host cores, which checks every lnL and is timed
+    as the CPU baseline."""
+    import numpy as np
+    from crux_gb300 import _native, synth
+    from crux_gb300._abi import STEP_DTYPE, ComputeI, ComputeL
+    from crux_gb300.plan import Plan
+    w = DIRTY
+    n = args.gens or w["recomputes"]
+    warm = max(args.warmup, 3)
+    gpu = _native.load()
+    case = synth.Case(w["ntaxa"], w["nsites"], w["mean_brlen"], w["seed"],
+                      alpha=w["alpha"], ncat=w["ncat"], pinv=w["pinv"],
+                      gap_frac=w["gap_frac"])
+    aln = case.alignment()
+    rng = np.random.default_rng(w["seed"])
+    nedge = 2 * w["ntaxa"] - 3
+    moves = [(int(rng.integers(nedge)), float(rng.uniform(*w["rescale"])))
+             for _ in range(warm + n)]
+
+    def replay(lik, count_updates=False):
+        edges = lik.tree.edges
+        vals, ups = [lik.lnL()], 0
+        t0 = None
+        for i, (e, f) in enumerate(moves):
+            if i == warm:
+                t0 = time.perf_counter()
+            edges[e].length *= f
+            vals.append(lik.lnL())
+            if count_updates and i >= warm:
+                st = np.frombuffer(lik._steps, dtype=STEP_DTYPE)[:lik.nsteps]
+                ups += int(np.isin(st["variant"], (ComputeL, ComputeI)).sum())
+        return vals, time.perf_counter() - t0, ups
+
+    out = {}
+    for prec in ("fp32", "fp64"):
+        lik = case.lik(lib=gpu, precision=prec, alignment=aln)
+        lik.prepare_plan()
+        shape = autotune(gpu, prec, args, lik=lik)
+        lik = case.lik(lib=gpu, precision=prec, alignment=aln)
+        clocks = Clocks()
+        if prec == "fp32":
+            clocks.start()
+        vals, secs, nodes = replay(lik, count_updates=True)
+        ck = clocks.stop() if prec == "fp32" else None
+        # Device time of one dirty path: the next rescale's plan, rerun.
+        lik.tree.edges[0].length *= 1.25
+        lik.prepare_plan(full=False)
+        plan = Plan(lik, prec)
+        plan.time(5)
+        dev = plan.time(50)
+        plan.close()
+        out[prec] = {"vals": vals, "secs": secs, "nodes": nodes,
+                     "shape": shape, "clocks": ck, "device": dev}
+    cpu, err = None, {}
+    if not args.no_cpu:
+        lib, kind, threads = load_cpu_oracle()
+        lo = case.lik(lib=lib, alignment=case.alignment())
+        want, secs, _ = replay(lo)
+        want = np.array(want)
+        for prec in ("fp32", "fp64"):
+            got = np.array(out[prec]["vals"])
+            err[prec] = float(np.max(np.abs(got - want) / np.abs(want)))
+        cpu = {"value": n / secs, "unit": "recomputes/s", "cores": threads,
+               "kind": kind,
+               "sample": "the same %d rescales and dirty-path lnLs, "
+                         "planning included (%.1f s)" % (n, secs)}
+    f32, f64 = out["fp32"], out["fp64"]
+    npat = aln.nchars
+    line = {
+        "metric": "dirty-path lnL recomputes/s through Lik.lnL "
+                  "(FP32-scaled form)",
+        "value": n / f32["secs"], "unit": "recomputes/s", "n_gpus": 1,
+        "steps": n, "warmup": warm, "ms_per_step": 1e3 * f32["secs"] / n,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded)",
+        "config": dict(w, recomputes=n, patterns=npat,
+                       walker_shape=f32["shape"],
+                       walker_shape_fp64=f64["shape"]),
+        "updates_per_s": f32["nodes"] * npat / f32["secs"],
+        "mean_nodes_per_recompute": f32["nodes"] / n,
+        "device_ms_per_dirty_path": f32["device"]["ms_per_run"],
+        "fp64_plain": {"value": n / f64["secs"],
+                       "updates_per_s": f64["nodes"] * npat / f64["secs"],
+                       "device_ms_per_dirty_path": f64["device"]["ms_per_run"]},
+        "fp32_over_fp64": f64["secs"] / f32["secs"],
+        "cpu_baseline": cpu,
+        "max_rel_err_vs_fp64_oracle": err,
+        "lnL_checked": len(f32["vals"]) if err else 0,
+        "clocks": f32["clocks"],
+    }
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
 SERVE = {"workload": "serve_poisson_logu_taxa8-1024_sites200-200000",
          "datasets": 40, "taxa": [8, 1024], "sites": [200, 200000],
          "pinv_prob": 0.3, "mc3_prob": 0.2, "mc3_gens": 10,
@@ -685,7 +789,7 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="FP32 plan only, no e2e/CPU legs (for ncu)")
     ap.add_argument("--workload", default="tree128",
-                    choices=["tree128", "batch256", "mc3", "mc3small",
+                    choices=["tree128", "batch256", "mc3", "mc3small", "dirty64",
                              "serve"])
     ap.add_argument("--rates", type=float, nargs="*", default=None,
                     help="serve: arrival rates (requests/s) to sweep")
@@ -703,6 +807,8 @@ def main():
         run_mc3(args, dist)
     elif args.workload == "serve":
         run_serve(args, dist)
+    elif args.workload == "dirty64":
+        run_dirty(args, dist)
     else:
         run_ours(args, dist)
 

@@ -8,6 +8,8 @@ import ctypes
 from ctypes import (POINTER, Structure, c_bool, c_double, c_int, c_uint,
                     c_void_p)
 
+import numpy as np
+
 
 class CxtLikCL(Structure):
     pass
@@ -66,6 +68,17 @@ class CxtLikStep(Structure):
         ("childCL", POINTER(CxtLikCL)),
         ("edgeLen", c_double),
     ]
+
+
+# numpy view of a CxtLikStep array (the planner writes a plan's steps in
+# one assignment).
+STEP_DTYPE = np.dtype({
+    "names": ["variant", "ntrail", "parentCL", "childCL", "edgeLen"],
+    "formats": ["<i4", "<u4", "<u8", "<u8", "<f8"],
+    "offsets": [CxtLikStep.variant.offset, CxtLikStep.ntrail.offset,
+                CxtLikStep.parentCL.offset, CxtLikStep.childCL.offset,
+                CxtLikStep.edgeLen.offset],
+    "itemsize": ctypes.sizeof(CxtLikStep)})
 
 
 class CxtLik(Structure):

@@ -49,11 +49,14 @@ class CL:
     With a device library the host buffers are 16-byte identity tokens (the
     device holds the data); with a host library they are real arrays.
     """
-    __slots__ = ("c", "bufs", "lib", "device", "forget", "leaf", "valid",
-                 "parent", "nSibs", "edgeLen", "__weakref__")
+    __slots__ = ("c", "ptr", "addr", "bufs", "lib", "device", "forget",
+                 "leaf", "valid", "parent", "nSibs", "edgeLen", "__weakref__")
 
     def __init__(self, lib, device):
         self.c = (_abi.CxtLikCL(), _abi.CxtLikCL())
+        # Pointers to the two structs, made once (plans store them).
+        self.ptr = (ctypes.pointer(self.c[0]), ctypes.pointer(self.c[1]))
+        self.addr = (ctypes.addressof(self.c[0]), ctypes.addressof(self.c[1]))
         self.bufs = [None, None]
         self.lib = lib
         self.device = device
@@ -508,23 +511,30 @@ class Lik:
 
     # -- planning (Lik.pyx:1395-1601) ----------------------------------------
     def _planAppend(self, variant, ntrail, parentCL, childCL, edgeLen):
-        L = self.lik
+        # Steps are collected here and written into the CxtLikStep array by
+        # _flushSteps at the end of _plan.
         assert ntrail != 0 or variant in (_abi.MergeL, _abi.MergeI)
-        st = self._steps[L.stepsLen]
-        L.stepsLen += 1
-        st.variant = variant
-        st.ntrail = ntrail
-        pol = L.polarity
-        st.parentCL = ctypes.pointer(parentCL.c[pol])
+        pol = self._pol
         if childCL.bufs[1] is None:
             assert childCL.bufs[0] is not None
-            st.childCL = ctypes.pointer(childCL.c[0])
+            child = childCL.addr[0]
         else:
-            st.childCL = ctypes.pointer(childCL.c[pol])
+            child = childCL.addr[pol]
         if edgeLen < 0.0:
             raise ValueError("Negative branch length")
-        st.edgeLen = edgeLen
+        self._pending.append((variant, ntrail, parentCL.addr[pol], child,
+                              edgeLen))
         self._plan_refs.append((parentCL, childCL))
+
+    def _flushSteps(self):
+        L = self.lik
+        n = len(self._pending)
+        if n:
+            view = np.frombuffer(self._steps, dtype=_abi.STEP_DTYPE)
+            view[L.stepsLen:L.stepsLen + n] = np.array(self._pending,
+                                                        dtype=_abi.STEP_DTYPE)
+            L.stepsLen += n
+        self._pending = []
 
     def _leafInit(self, ring):
         L = self.lik
@@ -562,8 +572,11 @@ class Lik:
         return cl
 
     def _planRecurse(self, ring, parent, nSibs, edgeLen):
-        L = self.lik
-        pol = L.polarity
+        # self._pol, self._inval, self._resize and self._dims are the
+        # polarity, invalidate and resize flags and the CL shape, read from
+        # the CxtLik once per plan by _plan (they do not change during it).
+        pol = self._pol
+        inval = self._inval
         cL = ring.aux
         degree = ring.node.getDegree()
         if degree == 1:
@@ -572,33 +585,36 @@ class Lik:
         else:
             if cL is None:
                 cL = CL(self.lib, self.device)
-                cL.prepare(pol, L.mschars, L.dim, L.compsLen)
+                cL.prepare(pol, *self._dims)
                 ring.aux = cL
-            elif L.resize:
-                cL.resize(pol, L.mschars, L.dim, L.compsLen)
-            else:
-                cL.prepare(pol, L.mschars, L.dim, L.compsLen)
+            elif self._resize:
+                cL.resize(pol, *self._dims)
+            elif cL.bufs[pol] is None:
+                cL.prepare(pol, *self._dims)
 
-        for r in ring.siblings():
-            if L.invalidate:
+        r = ring.next
+        while r is not ring:
+            nxt = r.next
+            if inval:
                 f = r.aux
                 if f is not None:
                     f.flush(pol)
             self._planRecurse(r.other, cL, degree, r.edge.length)
+            r = nxt
 
-        if L.invalidate or cL.parent[pol] is not parent \
+        if inval or cL.parent[pol] is not parent \
                 or cL.nSibs[pol] != nSibs or cL.edgeLen[pol] != edgeLen:
             parent.set_valid(pol, False)
             cL.parent[pol] = parent
             cL.nSibs[pol] = nSibs
             cL.edgeLen[pol] = edgeLen
             cLC = cL.c[pol]
-            cLC.parent = ctypes.pointer(parent.c[pol])
+            cLC.parent = parent.ptr[pol]
             cLC.nSibs = nSibs
             cLC.edgeLen = edgeLen
 
         if degree != 1:
-            if L.invalidate or not cL.valid[pol]:
+            if inval or not cL.valid[pol]:
                 r = ring.next
                 for j in range(1, degree):
                     if r.other.node.getDegree() > 1:
@@ -614,11 +630,16 @@ class Lik:
     def _plan(self, root):
         L = self.lik
         pol = L.polarity
+        self._pol = pol
+        self._pending = []
+        self._inval = bool(L.invalidate)
+        self._resize = bool(L.resize)
+        self._dims = (L.mschars, L.dim, L.compsLen)
         if L.resize:
             self.rootCL.resize(pol, L.mschars, L.dim, L.compsLen)
         else:
             self.rootCL.prepare(pol, L.mschars, L.dim, L.compsLen)
-        L.rootCLC = ctypes.pointer(self.rootCL.c[pol])
+        L.rootCLC = self.rootCL.ptr[pol]
         if root is None:
             root = self.tree.base
         degree = root.getDegree()
@@ -653,6 +674,7 @@ class Lik:
                     self._planAppend(variant, ntrail, self.rootCL,
                                      r.other.aux, r.edge.length)
                 self.rootCL.set_valid(pol, True)
+        self._flushSteps()
         L.resize = False
         L.invalidate = False
 

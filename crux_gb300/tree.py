@@ -90,11 +90,16 @@ class Node:
         return sum(1 for _ in self.ring)
 
     def getDegree(self):
-        return self.degree_calc()
+        # Cached: only Edge.attach and Edge.detach change a degree, and they
+        # clear the cache of both end nodes.
+        d = self._degree
+        if d is None:
+            d = self._degree = self.degree_calc()
+        return d
 
     @property
     def degree(self):
-        return self.degree_calc()
+        return self.getDegree()
 
     def getTaxon(self):
         return self.taxon
@@ -115,6 +120,7 @@ class Edge:
         assert nodeA is not nodeB
         for ring, node in ((self.ring, nodeA), (self.ring.other, nodeB)):
             ring.node = node
+            node._degree = None
             head = node.ring
             if head is not None:
                 tail = head.prev
@@ -129,6 +135,7 @@ class Edge:
     def detach(self):
         for ring in (self.ring, self.ring.other):
             node = ring.node
+            node._degree = None
             nxt = ring.next
             if nxt is ring:
                 node.ring = None
