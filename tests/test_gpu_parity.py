@@ -265,3 +265,23 @@ def test_golden_fixtures(gpu, path, precision):
     for i, f, w in fx["dirty"]:
         edges[i].length *= f
         assert rel(lik.lnL(), w) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_many_dirty_paths_gtr_gamma_inv(gpu, port, precision):
+    """300 dirty-path lnLs on the 64-taxon GTR+G4+I shape with 0.5 % gaps:
+    each rescale sets one branch to its generated length x U(0.5, 2), and
+    every lnL is checked against the oracle replaying the same rescales."""
+    case = synth.Case(64, 10000, 0.05, 20261208, pinv=0.2, gap_frac=0.005)
+    lg = case.lik(lib=gpu, precision=precision)
+    lo = case.lik(lib=port)
+    eg, eo = lg.tree.edges, lo.tree.edges
+    base = [e.length for e in eg]
+    rng = np.random.default_rng(8)
+    assert rel(lg.lnL(), lo.lnL()) <= TOL[precision]
+    for _ in range(300):
+        i = int(rng.integers(len(eg)))
+        f = float(rng.uniform(0.5, 2.0))
+        eg[i].length = eo[i].length = base[i] * f
+        a, b = lg.lnL(), lo.lnL()
+        assert rel(a, b) <= TOL[precision], (a, b)
