@@ -461,7 +461,7 @@ def run_batch(args, dist):
 MC3 = {"mc3": {"workload": "mc3_128taxa_100ksites_gtr_gamma4_8chains",
                "ntaxa": 128, "nsites": 100000, "mean_brlen": 0.05,
                "nchains": 8, "heat_delta": 0.1, "seed": 20261205,
-               "moves": {"brlen": 2.0, "nni": 2.0, "rates": 1.0,
+               "moves": {"brlen": 2.0, "nni": 1.0, "spr": 1.0, "rates": 1.0,
                          "alpha": 1.0}, "gens": 2000, "check_every": 1000},
        "mc3small": {"workload": "mc3_16taxa_1000sites_gtr_gamma4_4chains",
                     "ntaxa": 16, "nsites": 1000, "mean_brlen": 0.1,

@@ -21,10 +21,16 @@
 // Moves (weights set by the caller): branch-length multiplier (as the
 // reference: m = exp(lambda (u - 1/2)), Exp(brlenPrior) prior, Hastings
 // ln m); NNI across a random internal edge (symmetric); GTR
-// exchangeabilities from a Dirichlet centred on the current values (flat
-// Dirichlet prior, Hastings from the two Dirichlet densities); the inverse
-// Gamma shape multiplier of the reference (rateShapeInvPropose, Exp(1)
-// prior on 1/alpha).
+// exchangeabilities and base frequencies, each from a Dirichlet centred on
+// the current values (flat Dirichlet prior, Hastings from the two
+// Dirichlet densities); the inverse Gamma shape multiplier of the
+// reference (rateShapeInvPropose, Exp(1) prior on 1/alpha); SPR: prune a
+// subtree whose parent p is not the root (p's two edges merge), regraft p
+// on a uniform edge outside the subtree, split at a uniform point.  SPR
+// keeps the tree length (prior ratio 1 under iid exponential lengths); the
+// pruned tree and so the edge count are the same both ways, and the
+// Jacobian of (l_p, l_b, l_x, u) -> (l_b + l_p, u l_x, (1 - u) l_x,
+// l_p / (l_p + l_b)) gives the Hastings ratio l_x / (l_b + l_p).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
@@ -38,8 +44,11 @@
 
 namespace cxg {
 
-enum { MV_BRLEN = 0, MV_NNI = 1, MV_RATES = 2, MV_ALPHA = 3, MV_INIT = 4 };
-constexpr int kMoves = 4;
+enum {
+    MV_BRLEN = 0, MV_NNI = 1, MV_RATES = 2, MV_ALPHA = 3, MV_FREQS = 4, MV_SPR = 5,
+    MV_INIT = 6
+};
+constexpr int kMoves = 6;
 
 struct Mc3Model {
     double rates[6], freqs[4], alpha;
@@ -55,6 +64,11 @@ struct Mc3Prop {
     int32_t type, node, a, c;
     double oldlen, lnPrior, lnHast;
     int32_t model_changed, ndirty;
+    // SPR undo: subtree s, its parent p, p's old parent g and other child b,
+    // target x and its parent xp in the pruned tree; child slots of p in g,
+    // of b in p and of x in xp; the old lengths of b, p and x.
+    int32_t s, p, g, b, x, xp, jg, jb, jx;
+    double lb, lp, lx;
 };
 
 struct Mc3Dev {
@@ -88,6 +102,7 @@ struct Mc3Dev {
     unsigned *counter;
     double wcdf[kMoves];
     double brlen_lambda, brlen_prior, rate_conc, alpha_lambda, alpha_prior;
+    double freq_conc;
     uint32_t swap_stride;
     uint32_t *acc, *rej;  // [c][kMoves]
     uint32_t *nswap;      // [c]
@@ -176,7 +191,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         const double u = philox_u01(rng);
         int t = 0;
         while (t < kMoves - 1 && u >= d.wcdf[t]) ++t;
-        if (t == MV_NNI && N < 4) t = MV_BRLEN;
+        if ((t == MV_NNI || t == MV_SPR) && N < 4) t = MV_BRLEN;
         if (t == MV_ALPHA && d.kact < 2) t = MV_BRLEN;
         pr.type = t;
         if (t == MV_BRLEN) {
@@ -216,6 +231,114 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             pr.a = a;
             pr.c = cc;
             lowest = (int)v;
+        } else if (t == MV_SPR) {
+            // Subtree s: uniform over non-root nodes whose parent is not
+            // the root (the root keeps its three children).
+            const unsigned ns = NN - 1 - 3;
+            unsigned k = philox_below(rng, ns);
+            int s = -1;
+            for (unsigned v = 0; v < NN && s < 0; ++v) {
+                if (v == d.root || parent[v] == (int)d.root) continue;
+                if (k-- == 0) s = (int)v;
+            }
+            const int p = parent[s], g = parent[p];
+            int jb = -1, jg = -1;
+            for (int j = 0; j < 3; ++j) {
+                const int x = child[p * 3 + j];
+                if (x >= 0 && x != s) jb = j;
+                if (child[g * 3 + j] == p) jg = j;
+            }
+            const int b = child[p * 3 + jb];
+            // Mark the subtree of s (2 in the dirty flags, cleared below).
+            unsigned nsub = 0;
+            {
+                int sp = 0;
+                stack[sp++] = s;
+                while (sp > 0) {
+                    const int v = stack[--sp];
+                    dflag[v] = 2;
+                    ++nsub;
+                    for (int j = 0; j < 3; ++j) {
+                        const int x = child[v * 3 + j];
+                        if (x >= 0) stack[sp++] = x;
+                    }
+                }
+            }
+            // Prune: b takes p's place under g, the two edges merge.
+            pr.lb = len[b];
+            pr.lp = len[p];
+            child[g * 3 + jg] = b;
+            parent[b] = g;
+            len[b] = pr.lb + pr.lp;
+            // Target edge (x, parent[x]) of the pruned tree, outside the
+            // subtree: not the root, not p, not marked.
+            const unsigned ne = NN - 2 - nsub;
+            k = philox_below(rng, ne);
+            int x = -1;
+            for (unsigned v = 0; v < NN && x < 0; ++v) {
+                if (v == d.root || (int)v == p || dflag[v] == 2) continue;
+                if (k-- == 0) x = (int)v;
+            }
+            {
+                int sp = 0;
+                stack[sp++] = s;
+                while (sp > 0) {
+                    const int v = stack[--sp];
+                    dflag[v] = 0;
+                    for (int j = 0; j < 3; ++j) {
+                        const int y = child[v * 3 + j];
+                        if (y >= 0) stack[sp++] = y;
+                    }
+                }
+            }
+            const int xp = parent[x];
+            int jx = -1;
+            for (int j = 0; j < 3; ++j)
+                if (child[xp * 3 + j] == x) jx = j;
+            const double lx = len[x];
+            pr.lx = (x == b) ? pr.lb : lx;
+            // Regraft p on (x, xp) at a uniform point.
+            const double u = philox_u01(rng);
+            child[xp * 3 + jx] = p;
+            parent[p] = xp;
+            child[p * 3 + jb] = x;
+            parent[x] = p;
+            len[p] = u * lx;
+            len[x] = (1.0 - u) * lx;
+            pr.s = s;
+            pr.p = p;
+            pr.g = g;
+            pr.b = b;
+            pr.x = x;
+            pr.xp = xp;
+            pr.jg = jg;
+            pr.jb = jb;
+            pr.jx = jx;
+            pr.lnHast = (lx > 0.0) ? log(lx) - log(pr.lb + pr.lp) : 0.0;
+            pr.lnPrior = (lx > 0.0) ? 0.0 : -INFINITY;
+            // Dirty: both paths to the root (p's new place, g's old child).
+            for (int v = p; v >= 0; v = parent[v]) dflag[v] = 1;
+            for (int v = g; v >= 0; v = parent[v]) dflag[v] = 1;
+        } else if (t == MV_FREQS) {
+            // Base frequencies ~ Dirichlet(conc * pi).
+            double f0[4], f1[4], a0[4], a1[4], s0 = 0.0, s1 = 0.0;
+            for (int i = 0; i < 4; ++i) s0 += m0.freqs[i];
+            for (int i = 0; i < 4; ++i) {
+                f0[i] = m0.freqs[i] / s0;
+                a0[i] = d.freq_conc * f0[i];
+                f1[i] = philox_gamma(rng, a0[i]);
+                if (f1[i] < 1e-300) f1[i] = 1e-300;
+                s1 += f1[i];
+            }
+            for (int i = 0; i < 4; ++i) {
+                f1[i] /= s1;
+                a1[i] = d.freq_conc * f1[i];
+            }
+            m1 = m0;
+            for (int i = 0; i < 4; ++i) m1.freqs[i] = f1[i];
+            pr.lnHast = ln_dirichlet(a1, f0, 4) - ln_dirichlet(a0, f1, 4);
+            pr.model_changed = 1;
+            full = true;
         } else if (t == MV_RATES) {
             // Exchangeabilities ~ Dirichlet(conc * r / sum r).
             double r0[6], r1[6], a0[6], a1[6], s0 = 0.0, s1 = 0.0;
@@ -256,7 +379,24 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
 
     // Dirty internal nodes, children before parents.
     int nd = 0;
-    if (full) {
+    if (pr.type == MV_SPR) {
+        // The nodes flagged above, in reversed pre-order of the new tree.
+        int sp = 0;
+        stack[sp++] = (int)d.root;
+        while (sp > 0) {
+            const int v = stack[--sp];
+            if (dflag[v]) dirty[nd++] = v;
+            for (int j = 0; j < 3; ++j) {
+                const int x = child[v * 3 + j];
+                if (x >= (int)N) stack[sp++] = x;
+            }
+        }
+        for (int i = 0, j = nd - 1; i < j; ++i, --j) {
+            const int t = dirty[i];
+            dirty[i] = dirty[j];
+            dirty[j] = t;
+        }
+    } else if (full) {
         // Iterative post-order from the root.
         int sp = 0, top = 0;
         stack[sp++] = (int)d.root;
@@ -410,6 +550,19 @@ __global__ void mc3_accept_kernel(Mc3Dev d) {
             int32_t *child = d.child + (size_t)c * NN * 3;
             if (pr.type == MV_BRLEN) {
                 d.len[(size_t)c * NN + pr.node] = pr.oldlen;
+            } else if (pr.type == MV_SPR) {
+                // Take p out of (x, xp), put it back between g and b.
+                const int p = pr.p, x = pr.x, b = pr.b, g = pr.g, xp = pr.xp;
+                double *len = d.len + (size_t)c * NN;
+                child[xp * 3 + pr.jx] = x;
+                parent[x] = xp;
+                child[p * 3 + pr.jb] = b;
+                parent[b] = p;
+                child[g * 3 + pr.jg] = p;
+                parent[p] = g;
+                len[b] = pr.lb;
+                len[p] = pr.lp;
+                if (x != b) len[x] = pr.lx;
             } else if (pr.type == MV_NNI) {
                 const int v = pr.node, a = pr.a, cc = pr.c;
                 const int p = parent[a];
@@ -585,6 +738,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     d.brlen_lambda = cfg->brlen_lambda;
     d.brlen_prior = cfg->brlen_prior;
     d.rate_conc = cfg->rate_conc;
+    d.freq_conc = cfg->freq_conc > 0.0 ? cfg->freq_conc : 300.0;
     d.alpha_lambda = cfg->alpha_lambda;
     d.alpha_prior = cfg->alpha_prior;
     d.trace_cap = cfg->trace_cap;

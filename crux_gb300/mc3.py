@@ -20,7 +20,7 @@ from .alignment import Alignment, TaxaMap
 from .tree import Tree
 
 LAMBDA = 2.0 * math.log(1.6)
-MOVES = ("brlen", "nni", "rates", "alpha")
+MOVES = ("brlen", "nni", "rates", "alpha", "freqs", "spr")
 
 
 class Mc3Config(ctypes.Structure):
@@ -40,10 +40,11 @@ class Mc3Config(ctypes.Structure):
         ("heat_delta", ctypes.c_double),
         ("swap_stride", ctypes.c_uint),
         ("seed", ctypes.c_ulonglong),
-        ("move_weight", ctypes.c_double * 4),
+        ("move_weight", ctypes.c_double * 6),
         ("brlen_lambda", ctypes.c_double),
         ("brlen_prior", ctypes.c_double),
         ("rate_conc", ctypes.c_double),
+        ("freq_conc", ctypes.c_double),
         ("alpha_lambda", ctypes.c_double),
         ("alpha_prior", ctypes.c_double),
         ("precision", ctypes.c_int),
@@ -141,7 +142,8 @@ class Mc3:
     def __init__(self, tree, alignment, rates, freqs, alpha=None, ncat=4,
                  nchains=4, heat_delta=0.05, swap_stride=1, seed=1,
                  moves=None, precision="fp32", brlen_lambda=LAMBDA,
-                 brlen_prior=10.0, rate_conc=300.0, alpha_lambda=LAMBDA,
+                 brlen_prior=10.0, rate_conc=300.0, freq_conc=300.0,
+                 alpha_lambda=LAMBDA,
                  alpha_prior=1.0, graph_gens=16, trace_cap=1 << 20, lib=None):
         self.lib = lib or _native.load()
         declare(self.lib)
@@ -181,6 +183,7 @@ class Mc3:
         c.brlen_lambda = brlen_lambda
         c.brlen_prior = brlen_prior
         c.rate_conc = rate_conc
+        c.freq_conc = freq_conc
         c.alpha_lambda = alpha_lambda
         c.alpha_prior = alpha_prior
         c.precision = 1 if precision == "fp32" else 0
@@ -224,15 +227,15 @@ class Mc3:
                 "alpha": alpha.value}
 
     def stats(self):
-        n = self.nchains * 4
+        n = self.nchains * len(MOVES)
         acc = (ctypes.c_uint * n)()
         rej = (ctypes.c_uint * n)()
         sw = (ctypes.c_uint * self.nchains)()
         gen = ctypes.c_ulonglong()
         self._check(self.lib.cxgMc3Stats(self.h, acc, rej, sw,
                                          ctypes.byref(gen)), "cxgMc3Stats")
-        a = np.array(acc).reshape(self.nchains, 4)
-        r = np.array(rej).reshape(self.nchains, 4)
+        a = np.array(acc).reshape(self.nchains, len(MOVES))
+        r = np.array(rej).reshape(self.nchains, len(MOVES))
         return {"accepts": a, "rejects": r, "swaps": np.array(sw),
                 "generation": gen.value}
 

@@ -81,3 +81,32 @@ def test_load_without_gpu_reports_no_device():
     buf = ctypes.create_string_buffer(256)
     assert lib.cxgInfo(buf, 256) == 0
     assert buf.value.startswith(b"cxlik_gpu")
+
+
+def test_extension_struct_layouts_match_header():
+    """The ctypes mirrors of the MC3 and server structs (crux_gb300.mc3,
+    crux_gb300.serve) have the header's field offsets and sizes."""
+    from crux_gb300 import mc3, serve
+    pairs = [("cxgMc3Config", mc3.Mc3Config), ("cxgRequest", serve.Request),
+             ("cxgServerConfig", serve.ServerConfig),
+             ("cxgServerStatsT", serve.ServerStats)]
+    lines = []
+    want = []
+    for cname, py in pairs:
+        lines.append('printf("%%zu\\n", sizeof(%s));' % cname)
+        want.append(ctypes.sizeof(py))
+        for f in py._fields_:
+            lines.append('printf("%%zu\\n", offsetof(%s, %s));' % (cname, f[0]))
+            want.append(getattr(py, f[0]).offset)
+    src = ("#include <stddef.h>\n#include <stdio.h>\n#include \"cxlik_gpu.h\"\n"
+           "int main(void) {\n" + "\n".join(lines) + "\nreturn 0;\n}\n")
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "p.c")
+        open(c, "w").write(src)
+        exe = os.path.join(d, "p")
+        subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"),
+                        c, "-o", exe], check=True)
+        got = subprocess.run([exe], capture_output=True, text=True,
+                             check=True).stdout.split()
+    assert [int(x) for x in got] == want

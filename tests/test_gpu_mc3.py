@@ -11,7 +11,8 @@ from crux_gb300.mc3 import Mc3
 pytestmark = pytest.mark.gpu
 
 TOL = {"fp64": 1e-11, "fp32": 1e-6}
-MOVES = {"brlen": 2.0, "nni": 2.0, "rates": 0.5, "alpha": 0.5}
+MOVES = {"brlen": 2.0, "nni": 1.0, "spr": 1.0, "rates": 0.5, "alpha": 0.5,
+         "freqs": 0.5}
 
 
 def build(precision, nchains=4, seed=9, moves=MOVES, ntaxa=16, nsites=1000):
@@ -40,8 +41,9 @@ def test_mc3_chains_match_oracle(gpu, port, precision):
     assert st["generation"] == 158
     acc = st["accepts"].sum(axis=0)
     rej = st["rejects"].sum(axis=0)
-    assert (acc + rej)[:2].min() > 0
+    assert (acc + rej).min() > 0                # every move was drawn
     assert acc[0] > 0 and acc[1] > 0            # brlen and NNI accepted
+    assert acc[5] > 0                           # SPR accepted
     assert st["swaps"].sum() > 0
     heats = sorted(m.chain_state(i)["heat"] for i in range(m.nchains))
     assert np.allclose(heats, sorted(1.0 / (1.0 + 0.2 * i) for i in range(4)))
@@ -78,3 +80,31 @@ def test_mc3_brlen_only_single_category(gpu, port):
         want = lik.lnL()
         assert abs(st["lnL"] - want) <= 1e-11 * abs(want)
     m.close()
+
+
+def test_mc3_samples_the_prior_without_data(gpu):
+    """With all-gap columns the likelihood is 1, so the chain samples the
+    prior: iid Exp(10) branch lengths, whatever the topology moves do.  A
+    wrong Hastings ratio in the branch-length, NNI or SPR move biases the
+    tree length away from (2N - 3) x 0.1."""
+    from crux_gb300.alignment import Alignment, TaxaMap
+    case = synth.Case(8, 50, 0.1, 17)
+    aln0 = case.alignment()
+    rows = np.full((aln0.ntaxa, 4), ord("-"), dtype=np.uint8)
+    aln = Alignment(taxaMap=TaxaMap(aln0.taxaMap.taxa), rows=rows)
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=None,
+            nchains=1, seed=123, precision="fp64", graph_gens=32,
+            moves={"brlen": 1.0, "nni": 1.0, "spr": 1.0})
+    tl = []
+    m.run(2000)
+    for _ in range(1500):
+        m.run(64)
+        st = m.chain_state(0)
+        assert abs(st["lnL"]) < 1e-9
+        tl.append(st["len"].sum())
+    m.close()
+    nedge = 2 * 8 - 3
+    assert abs(np.mean(tl) - nedge * 0.1) < 0.08 * nedge * 0.1, np.mean(tl)
+    # Exp(10) lengths: the tree length has variance nedge / 100.
+    assert abs(np.var(tl) - nedge / 100.0) < 0.3 * nedge / 100.0, np.var(tl)
