@@ -393,7 +393,9 @@ def run_batch(args, dist):
     setup_s = time.perf_counter() - t0
     res = {}
     liks = {}
-    for prec, per_node in (("fp32", False), ("fp64", True), ("fp64", False)):
+    runs = (("fp32", False),) if args.profile else \
+        (("fp32", False), ("fp64", True), ("fp64", False))
+    for prec, per_node in runs:
         key = prec + ("_per_node" if per_node else "_batched")
         if prec not in liks:
             liks[prec] = [c.lik(lib=gpu, precision=prec) for c in cases]
@@ -413,6 +415,12 @@ def run_batch(args, dist):
         b.close()
         res[key] = {"info": info, "t": t, "lnL": lnls, "clocks": ck,
                     "shape": shape}
+    if args.profile:
+        print(json.dumps({"profile_run": True, "workload": BATCH["workload"],
+                          "jobs": len(cases),
+                          "ms_per_run": res["fp32_batched"]["t"]["ms_per_run"]}))
+        dist.close()
+        return
     check = {}
     if not args.no_cpu:
         from oracle import oracle
@@ -476,7 +484,9 @@ def run_mc3(args, dist):
     against the FP64 oracle every `check_every` generations."""
     from crux_gb300 import _native, synth
     from crux_gb300.mc3 import Mc3
-    w = MC3[args.workload]
+    w = dict(MC3[args.workload])
+    if args.chains:
+        w["nchains"] = args.chains
     gens = args.gens or w["gens"]
     gpu = _native.load()
     case = synth.Case(w["ntaxa"], w["nsites"], w["mean_brlen"], w["seed"])
@@ -487,7 +497,7 @@ def run_mc3(args, dist):
         port = oracle.load_port()
         port.port_set_threads(os.cpu_count() or 1)
     out = {}
-    for prec in ("fp32", "fp64"):
+    for prec in (("fp32",) if args.profile else ("fp32", "fp64")):
         lk = case.lik(lib=gpu, precision=prec, alignment=aln)
         lk.prepare_plan()
         shape = autotune(gpu, prec, args, lik=lk)
@@ -524,6 +534,12 @@ def run_mc3(args, dist):
                      "drift": drift, "clocks": ck, "shape": shape,
                      "trace_head": [float(x) for x in m.trace(8)]}
         m.close()
+    if args.profile:
+        print(json.dumps({"profile_run": True, "workload": w["workload"],
+                          "nchains": w["nchains"],
+                          "gens_per_s": out["fp32"]["gens_per_s"]}))
+        dist.close()
+        return
     f32, f64 = out["fp32"], out["fp64"]
     line = {
         "metric": "MC3 generations/s (FP32-scaled chains, on device)",
@@ -802,6 +818,8 @@ def main():
                     help="serve: arrival rates (requests/s) to sweep")
     ap.add_argument("--gens", type=int, default=None,
                     help="mc3 workloads: generations to time")
+    ap.add_argument("--chains", type=int, default=None,
+                    help="MC3 workloads: number of chains")
     ap.add_argument("--jobs", type=int, default=None,
                     help="batch256: number of jobs (default 256)")
     args = ap.parse_args()

@@ -72,10 +72,14 @@ __device__ inline void pmat_one(const PmatArgs &a, unsigned idx) {
 // [73] status (0 ok, 1 bad input, 2 no convergence).
 // ---------------------------------------------------------------------------
 __device__ inline void qdecomp4(const double *rtri, const double *pi, double *out) {
+    // Every fixed-size loop is unrolled so that the 4 x 4 matrices live in
+    // registers; the arithmetic and its order are those of the loops.
     double pn[4], sq[4], q[16], s[16], u[16];
     double psum = 0.0;
+#pragma unroll
     for (int i = 0; i < 4; ++i) psum += pi[i];
     bool ok = true;
+#pragma unroll
     for (int i = 0; i < 4; ++i) {
         pn[i] = pi[i] / psum;
         ok = ok && (pn[i] > 0.0);
@@ -87,69 +91,93 @@ __device__ inline void qdecomp4(const double *rtri, const double *pi, double *ou
     // Upper-triangle order of rtri: (0,1) (0,2) (0,3) (1,2) (1,3) (2,3).
     const int tri[4][4] = {{-1, 0, 1, 2}, {0, -1, 3, 4}, {1, 3, -1, 5},
                            {2, 4, 5, -1}};
+    double rt[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) rt[i] = rtri[i];
     double qscale = 0.0;
+#pragma unroll
     for (int i = 0; i < 4; ++i)
+#pragma unroll
         for (int j = 0; j < 4; ++j) {
             if (i == j) continue;
-            q[i * 4 + j] = rtri[tri[i][j]] * pn[j];
+            q[i * 4 + j] = rt[tri[i][j]] * pn[j];
             if (j < i) qscale += q[i * 4 + j] * pn[i] * 2.0;
         }
+#pragma unroll
     for (int i = 0; i < 4; ++i) {
         double d = 0.0;
+#pragma unroll
         for (int j = 0; j < 4; ++j)
             if (j != i) d -= q[i * 4 + j];
         q[i * 4 + i] = d;
     }
+#pragma unroll
     for (int i = 0; i < 4; ++i) sq[i] = sqrt(pn[i]);
+#pragma unroll
     for (int i = 0; i < 4; ++i)
+#pragma unroll
         for (int j = 0; j < 4; ++j)
-            s[i * 4 + j] = (i == j) ? q[i * 4 + i] : rtri[tri[i][j]] * sq[i] * sq[j];
+            s[i * 4 + j] = (i == j) ? q[i * 4 + i] : rt[tri[i][j]] * sq[i] * sq[j];
+#pragma unroll
     for (int i = 0; i < 16; ++i) u[i] = (i % 5 == 0) ? 1.0 : 0.0;
     int conv = 0;
     for (int sweep = 0; sweep < 64 && !conv; ++sweep) {
         double off = 0.0, dg = 0.0;
+#pragma unroll
         for (int i = 0; i < 4; ++i) {
             dg += s[i * 4 + i] * s[i * 4 + i];
+#pragma unroll
             for (int j = i + 1; j < 4; ++j) off += s[i * 4 + j] * s[i * 4 + j];
         }
         if (off == 0.0 || off <= 1e-40 * dg) {
             conv = 1;
             break;
         }
+#pragma unroll
         for (int pp = 0; pp < 3; ++pp)
+#pragma unroll
             for (int qq = pp + 1; qq < 4; ++qq) {
                 const double apq = s[pp * 4 + qq];
-                if (apq == 0.0) continue;
-                const double app = s[pp * 4 + pp], aqq = s[qq * 4 + qq];
-                const double th = (aqq - app) / (2.0 * apq);
-                const double t = (th >= 0.0 ? 1.0 : -1.0) /
-                                 (fabs(th) + sqrt(th * th + 1.0));
-                const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
-                for (int k = 0; k < 4; ++k) {
-                    const double akp = s[k * 4 + pp], akq = s[k * 4 + qq];
-                    s[k * 4 + pp] = c * akp - sn * akq;
-                    s[k * 4 + qq] = sn * akp + c * akq;
-                }
-                for (int k = 0; k < 4; ++k) {
-                    const double apk = s[pp * 4 + k], aqk = s[qq * 4 + k];
-                    s[pp * 4 + k] = c * apk - sn * aqk;
-                    s[qq * 4 + k] = sn * apk + c * aqk;
-                }
-                s[pp * 4 + qq] = s[qq * 4 + pp] = 0.0;
-                for (int k = 0; k < 4; ++k) {
-                    const double ukp = u[k * 4 + pp], ukq = u[k * 4 + qq];
-                    u[k * 4 + pp] = c * ukp - sn * ukq;
-                    u[k * 4 + qq] = sn * ukp + c * ukq;
+                if (apq != 0.0) {
+                    const double app = s[pp * 4 + pp], aqq = s[qq * 4 + qq];
+                    const double th = (aqq - app) / (2.0 * apq);
+                    const double t = (th >= 0.0 ? 1.0 : -1.0) /
+                                     (fabs(th) + sqrt(th * th + 1.0));
+                    const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const double akp = s[k * 4 + pp], akq = s[k * 4 + qq];
+                        s[k * 4 + pp] = c * akp - sn * akq;
+                        s[k * 4 + qq] = sn * akp + c * akq;
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const double apk = s[pp * 4 + k], aqk = s[qq * 4 + k];
+                        s[pp * 4 + k] = c * apk - sn * aqk;
+                        s[qq * 4 + k] = sn * apk + c * aqk;
+                    }
+                    s[pp * 4 + qq] = s[qq * 4 + pp] = 0.0;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const double ukp = u[k * 4 + pp], ukq = u[k * 4 + qq];
+                        u[k * 4 + pp] = c * ukp - sn * ukq;
+                        u[k * 4 + qq] = sn * ukp + c * ukq;
+                    }
                 }
             }
     }
+#pragma unroll
     for (int i = 0; i < 4; ++i) out[i] = pn[i];
     out[4] = 1.0 / qscale;
+#pragma unroll
     for (int i = 0; i < 4; ++i)
+#pragma unroll
         for (int j = 0; j < 4; ++j)
+#pragma unroll
             for (int k = 0; k < 4; ++k)
                 out[5 + i * 16 + j * 4 + k] =
                     (u[i * 4 + k] / sq[i]) * (u[j * 4 + k] * sq[j]);
+#pragma unroll
     for (int k = 0; k < 4; ++k) out[69 + k] = s[k * 4 + k];
     out[73] = conv ? 0.0 : 2.0;
 }

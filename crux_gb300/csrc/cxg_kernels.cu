@@ -601,7 +601,10 @@ unsigned plan_blocks(unsigned ppad, unsigned tile) { return ppad / tile; }
 
 template <typename Kern>
 static cudaError_t ensure_smem(Kern k, size_t sm, size_t &optin) {
-    if (sm > 48 * 1024 && sm > optin) {
+    // Raised on every new maximum, not only above 48 KiB: the default limit
+    // counts static and dynamic shared memory together, so a dynamic size
+    // just under 48 KiB plus the walker's static arrays would not launch.
+    if (sm > optin) {
         cudaError_t e = cudaFuncSetAttribute(
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;

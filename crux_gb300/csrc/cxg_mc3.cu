@@ -109,23 +109,12 @@ struct Mc3Dev {
     double *trace;        // [trace_cap] cold-chain lnL after each generation
     uint64_t trace_cap;
     uint32_t *status;     // nonzero: a model could not be decomposed
+    uint32_t nslot_cap;   // shared-memory stack slots of the walker
 };
 
-// Model derived quantities: Q eigensystem (FP64 Jacobi on the device),
-// Gamma category rates, wNorm and the root weights (Lik.pyx:1603-1665).
-__device__ bool mc3_model_finish(Mc3Model &m, unsigned ncat) {
-    double tmp[74];
-    qdecomp4(m.rates, m.freqs, tmp);
-    if (tmp[73] != 0.0) return false;
-    for (int i = 0; i < 4; ++i) m.pinorm[i] = tmp[i];
-    m.qnorm = tmp[4];
-    for (int i = 0; i < 64; ++i) m.cube[i] = tmp[5 + i];
-    for (int i = 0; i < 4; ++i) m.eig[i] = tmp[69 + i];
-    if (ncat > 1) {
-        if (!d_gamma_rates(m.alpha, (int)ncat, m.cmult)) return false;
-    } else {
-        m.cmult[0] = 1.0;
-    }
+// wNorm and the root weights of a model whose eigensystem and category
+// rates are set (Lik.pyx:1603-1665; every category has weight 1/ncat).
+__device__ void mc3_model_weights(Mc3Model &m, unsigned ncat) {
     double qmean = 0.0;
     const double w = 1.0 / ncat;
     for (unsigned k = 0; k < ncat; ++k) {
@@ -137,6 +126,74 @@ __device__ bool mc3_model_finish(Mc3Model &m, unsigned ncat) {
     for (unsigned k = 0; k < ncat; ++k)
         for (int i = 0; i < 4; ++i) m.pn[k * 4 + i] = m.pinorm[i] * w;
     m.ok = 1;
+}
+
+// Model derived quantities: Q eigensystem (FP64 Jacobi on the device),
+// Gamma category rates, wNorm and the root weights (Lik.pyx:1603-1665).
+// `what` names the parts whose inputs changed (FIN_EIG: rates or
+// frequencies, FIN_GAMMA: alpha); the others are kept.
+enum : unsigned { FIN_EIG = 1, FIN_GAMMA = 2, FIN_ALL = 3 };
+__device__ bool mc3_model_finish(Mc3Model &m, unsigned ncat, unsigned what = FIN_ALL) {
+    if (what & FIN_EIG) {
+        double tmp[74];
+        qdecomp4(m.rates, m.freqs, tmp);
+        if (tmp[73] != 0.0) return false;
+        for (int i = 0; i < 4; ++i) m.pinorm[i] = tmp[i];
+        m.qnorm = tmp[4];
+        for (int i = 0; i < 64; ++i) m.cube[i] = tmp[5 + i];
+        for (int i = 0; i < 4; ++i) m.eig[i] = tmp[69 + i];
+    }
+    if (what & FIN_GAMMA) {
+        if (ncat > 1) {
+            if (!d_gamma_rates(m.alpha, (int)ncat, m.cmult)) return false;
+        } else {
+            m.cmult[0] = 1.0;
+        }
+    }
+    mc3_model_weights(m, ncat);
+    return true;
+}
+
+// The same with one warp: lanes 0..ncat-2 compute the Gamma category cuts
+// while lane 31 forms the eigensystem; lane 0 finishes.  All 32 lanes of
+// the warp call it; the result (true: decomposed) is lane 0's.
+__device__ bool mc3_model_finish_warp(Mc3Model &m, unsigned ncat, unsigned what) {
+    __shared__ double s_cut[kMaxComps];
+    __shared__ int s_bad;
+    const unsigned lane = threadIdx.x & 31u;
+    if (lane == 0) s_bad = 0;
+    __syncwarp();
+    if ((what & FIN_GAMMA) && ncat > 1 && lane < ncat - 1) {
+        const double cut = d_gamma_cut(m.alpha, (int)ncat, (int)lane);
+        if (cut == -1.0)
+            s_bad = 1;
+        else
+            s_cut[lane] = cut;
+    }
+    if ((what & FIN_EIG) && lane == 31) {
+        double tmp[74];
+        qdecomp4(m.rates, m.freqs, tmp);
+        if (tmp[73] != 0.0) {
+            s_bad = 1;
+        } else {
+            for (int i = 0; i < 4; ++i) m.pinorm[i] = tmp[i];
+            m.qnorm = tmp[4];
+            for (int i = 0; i < 64; ++i) m.cube[i] = tmp[5 + i];
+            for (int i = 0; i < 4; ++i) m.eig[i] = tmp[69 + i];
+        }
+    }
+    __syncwarp();
+    if (lane != 0) return false;
+    if (s_bad) return false;
+    if (what & FIN_GAMMA) {
+        if (ncat > 1) {
+            for (unsigned i = 0; i + 1 < ncat; ++i) m.cmult[i] = s_cut[i];
+            d_gamma_rates_from_cuts((int)ncat, m.cmult);
+        } else {
+            m.cmult[0] = 1.0;
+        }
+    }
+    mc3_model_weights(m, ncat);
     return true;
 }
 
@@ -157,309 +214,419 @@ __device__ double ln_dirichlet(const double *alpha, const double *x, int n) {
     return r + lgamma(s);
 }
 
+// Shared memory of one chain's proposal: the tree (parent, child, len,
+// cur), dirty flags, DFS stack, dirty list, per-op prefixes of children
+// and leaf children, and the stack slot of each op and of each op's
+// children.
+__host__ __device__ inline size_t mc3_propose_smem(unsigned NN, unsigned M) {
+    return (size_t)NN * (8 + 4 + 12 + 4 + 1 + 1) + (size_t)M * 4 + (size_t)(M + 1) * 8 +
+           (size_t)M * 4 + 64;
+}
+
+// One block per chain.  The chain's tree is staged in shared memory; one
+// thread draws and applies the move and lists the dirty nodes there (the
+// serial part: pointer chasing at shared-memory latency), then the block
+// writes the op records and the tree back in parallel.
 __global__ void mc3_propose_kernel(Mc3Dev d) {
     const unsigned c = blockIdx.x;
-    if (threadIdx.x != 0 || c >= d.nchains) return;
+    if (c >= d.nchains) return;
     const uint64_t g = *d.gen;
     const unsigned N = d.ntaxa, NN = d.nnodes, M = d.M;
-    int32_t *parent = d.parent + (size_t)c * NN;
-    int32_t *child = d.child + (size_t)c * NN * 3;
-    double *len = d.len + (size_t)c * NN;
-    uint8_t *cur = d.cur + (size_t)c * NN;
-    uint8_t *dflag = d.dirtyflag + (size_t)c * NN;
-    int32_t *dirty = d.dirty + (size_t)c * M;
-    int32_t *stack = d.stack + (size_t)c * NN;
+    extern __shared__ __align__(16) unsigned char psm[];
+    double *len = reinterpret_cast<double *>(psm);
+    int32_t *parent = reinterpret_cast<int32_t *>(len + NN);
+    int32_t *child = parent + NN;
+    int32_t *stack = child + (size_t)NN * 3;
+    int32_t *dirty = stack + NN;
+    uint32_t *kid0 = reinterpret_cast<uint32_t *>(dirty + M);   // [M + 1]
+    uint32_t *leaf0 = kid0 + (M + 1);                           // [M + 1]
+    uint8_t *cur = reinterpret_cast<uint8_t *>(leaf0 + (M + 1));
+    uint8_t *dflag = cur + NN;
+    int8_t *op_slot = reinterpret_cast<int8_t *>(dflag + NN);   // [M]
+    int8_t *kid_slot = op_slot + M;                             // [M][3]
+    int32_t *g_parent = d.parent + (size_t)c * NN;
+    int32_t *g_child = d.child + (size_t)c * NN * 3;
+    double *g_len = d.len + (size_t)c * NN;
+    for (unsigned i = threadIdx.x; i < NN; i += blockDim.x) {
+        len[i] = g_len[i];
+        parent[i] = g_parent[i];
+        cur[i] = d.cur[(size_t)c * NN + i];
+        dflag[i] = 0;
+    }
+    for (unsigned i = threadIdx.x; i < NN * 3; i += blockDim.x) child[i] = g_child[i];
+    __syncthreads();
     Mc3Prop &pr = d.prop[c];
-    Philox rng;
-    philox_init(rng, d.seed, c, g);
-    if (c == 0) *d.counter = 0;
-    char *res = d.results + (size_t)c * 32;
-    *(uint32_t *)(res + 4) = 0;  // ninf
-    *(uint32_t *)(res + 8) = 0;  // err
+    __shared__ int s_nd, s_lowest;
+    __shared__ unsigned s_fin;
+    __shared__ bool s_full;
+    if (threadIdx.x == 0) {
+        s_fin = 0;
+        Philox rng;
+        philox_init(rng, d.seed, c, g);
+        if (c == 0) *d.counter = 0;
+        char *res = d.results + (size_t)c * 32;
+        *(uint32_t *)(res + 4) = 0;  // ninf
+        *(uint32_t *)(res + 8) = 0;  // err
 
-    const Mc3Model &m0 = d.model[c * 2 + d.curmodel[c]];
-    Mc3Model &m1 = d.model[c * 2 + (1 - d.curmodel[c])];
-    pr.model_changed = 0;
-    pr.lnPrior = 0.0;
-    pr.lnHast = 0.0;
-    bool full = false;
-    int lowest = -1;  // lowest dirty node of a path move
-    if (g == 0) {
-        pr.type = MV_INIT;
-        full = true;
-    } else {
-        const double u = philox_u01(rng);
-        int t = 0;
-        while (t < kMoves - 1 && u >= d.wcdf[t]) ++t;
-        if ((t == MV_NNI || t == MV_SPR) && N < 4) t = MV_BRLEN;
-        if (t == MV_ALPHA && d.kact < 2) t = MV_BRLEN;
-        pr.type = t;
-        if (t == MV_BRLEN) {
-            // Uniform edge = uniform non-root node (Chain.pyx:442-447).
-            unsigned k = philox_below(rng, NN - 1);
-            const unsigned e = (k >= d.root) ? k + 1 : k;
-            const double lnM = d.brlen_lambda * (philox_u01(rng) - 0.5);
-            const double v0 = len[e], v1 = v0 * exp(lnM);
-            len[e] = v1;
-            pr.node = (int)e;
-            pr.oldlen = v0;
-            pr.lnPrior = -d.brlen_prior * (v1 - v0);
-            pr.lnHast = lnM;
-            lowest = parent[e];
-        } else if (t == MV_NNI) {
-            // Internal non-root node v, edge (v, p): swap a child a of v
-            // with a sibling c of v (another child of p).
-            unsigned k = philox_below(rng, M - 1);  // internal ids N..NN-1 minus root
-            unsigned v = N + k;
-            if (v >= d.root) ++v;
-            const int p = parent[v];
-            const int ai = (int)philox_below(rng, 2);
-            const int a = child[v * 3 + ai];
-            int sib[2], ns = 0;
-            for (int j = 0; j < 3; ++j) {
-                const int x = child[p * 3 + j];
-                if (x >= 0 && x != (int)v) sib[ns++] = x;
-            }
-            const int cc = sib[ns > 1 ? philox_below(rng, ns) : 0];
-            for (int j = 0; j < 3; ++j) {
-                if (child[v * 3 + j] == a) child[v * 3 + j] = cc;
-                if (child[p * 3 + j] == cc) child[p * 3 + j] = a;
-            }
-            parent[a] = p;
-            parent[cc] = (int)v;
-            pr.node = (int)v;
-            pr.a = a;
-            pr.c = cc;
-            lowest = (int)v;
-        } else if (t == MV_SPR) {
-            // Subtree s: uniform over non-root nodes whose parent is not
-            // the root (the root keeps its three children).
-            const unsigned ns = NN - 1 - 3;
-            unsigned k = philox_below(rng, ns);
-            int s = -1;
-            for (unsigned v = 0; v < NN && s < 0; ++v) {
-                if (v == d.root || parent[v] == (int)d.root) continue;
-                if (k-- == 0) s = (int)v;
-            }
-            const int p = parent[s], g = parent[p];
-            int jb = -1, jg = -1;
-            for (int j = 0; j < 3; ++j) {
-                const int x = child[p * 3 + j];
-                if (x >= 0 && x != s) jb = j;
-                if (child[g * 3 + j] == p) jg = j;
-            }
-            const int b = child[p * 3 + jb];
-            // Mark the subtree of s (2 in the dirty flags, cleared below).
-            unsigned nsub = 0;
-            {
-                int sp = 0;
-                stack[sp++] = s;
-                while (sp > 0) {
-                    const int v = stack[--sp];
-                    dflag[v] = 2;
-                    ++nsub;
-                    for (int j = 0; j < 3; ++j) {
-                        const int x = child[v * 3 + j];
-                        if (x >= 0) stack[sp++] = x;
-                    }
-                }
-            }
-            // Prune: b takes p's place under g, the two edges merge.
-            pr.lb = len[b];
-            pr.lp = len[p];
-            child[g * 3 + jg] = b;
-            parent[b] = g;
-            len[b] = pr.lb + pr.lp;
-            // Target edge (x, parent[x]) of the pruned tree, outside the
-            // subtree: not the root, not p, not marked.
-            const unsigned ne = NN - 2 - nsub;
-            k = philox_below(rng, ne);
-            int x = -1;
-            for (unsigned v = 0; v < NN && x < 0; ++v) {
-                if (v == d.root || (int)v == p || dflag[v] == 2) continue;
-                if (k-- == 0) x = (int)v;
-            }
-            {
-                int sp = 0;
-                stack[sp++] = s;
-                while (sp > 0) {
-                    const int v = stack[--sp];
-                    dflag[v] = 0;
-                    for (int j = 0; j < 3; ++j) {
-                        const int y = child[v * 3 + j];
-                        if (y >= 0) stack[sp++] = y;
-                    }
-                }
-            }
-            const int xp = parent[x];
-            int jx = -1;
-            for (int j = 0; j < 3; ++j)
-                if (child[xp * 3 + j] == x) jx = j;
-            const double lx = len[x];
-            pr.lx = (x == b) ? pr.lb : lx;
-            // Regraft p on (x, xp) at a uniform point.
-            const double u = philox_u01(rng);
-            child[xp * 3 + jx] = p;
-            parent[p] = xp;
-            child[p * 3 + jb] = x;
-            parent[x] = p;
-            len[p] = u * lx;
-            len[x] = (1.0 - u) * lx;
-            pr.s = s;
-            pr.p = p;
-            pr.g = g;
-            pr.b = b;
-            pr.x = x;
-            pr.xp = xp;
-            pr.jg = jg;
-            pr.jb = jb;
-            pr.jx = jx;
-            pr.lnHast = (lx > 0.0) ? log(lx) - log(pr.lb + pr.lp) : 0.0;
-            pr.lnPrior = (lx > 0.0) ? 0.0 : -INFINITY;
-            // Dirty: both paths to the root (p's new place, g's old child).
-            for (int v = p; v >= 0; v = parent[v]) dflag[v] = 1;
-            for (int v = g; v >= 0; v = parent[v]) dflag[v] = 1;
-        } else if (t == MV_FREQS) {
-            // Base frequencies ~ Dirichlet(conc * pi).
-            double f0[4], f1[4], a0[4], a1[4], s0 = 0.0, s1 = 0.0;
-            for (int i = 0; i < 4; ++i) s0 += m0.freqs[i];
-            for (int i = 0; i < 4; ++i) {
-                f0[i] = m0.freqs[i] / s0;
-                a0[i] = d.freq_conc * f0[i];
-                f1[i] = philox_gamma(rng, a0[i]);
-                if (f1[i] < 1e-300) f1[i] = 1e-300;
-                s1 += f1[i];
-            }
-            for (int i = 0; i < 4; ++i) {
-                f1[i] /= s1;
-                a1[i] = d.freq_conc * f1[i];
-            }
-            m1 = m0;
-            for (int i = 0; i < 4; ++i) m1.freqs[i] = f1[i];
-            pr.lnHast = ln_dirichlet(a1, f0, 4) - ln_dirichlet(a0, f1, 4);
-            pr.model_changed = 1;
-            full = true;
-        } else if (t == MV_RATES) {
-            // Exchangeabilities ~ Dirichlet(conc * r / sum r).
-            double r0[6], r1[6], a0[6], a1[6], s0 = 0.0, s1 = 0.0;
-            for (int i = 0; i < 6; ++i) s0 += m0.rates[i];
-            for (int i = 0; i < 6; ++i) {
-                r0[i] = m0.rates[i] / s0;
-                a0[i] = d.rate_conc * r0[i];
-                r1[i] = philox_gamma(rng, a0[i]);
-                if (r1[i] < 1e-300) r1[i] = 1e-300;
-                s1 += r1[i];
-            }
-            for (int i = 0; i < 6; ++i) {
-                r1[i] /= s1;
-                a1[i] = d.rate_conc * r1[i];
-            }
-            m1 = m0;
-            for (int i = 0; i < 6; ++i) m1.rates[i] = r1[i] * 6.0;
-            pr.lnHast = ln_dirichlet(a1, r0, 6) - ln_dirichlet(a0, r1, 6);
-            pr.model_changed = 1;
+        const Mc3Model &m0 = d.model[c * 2 + d.curmodel[c]];
+        Mc3Model &m1 = d.model[c * 2 + (1 - d.curmodel[c])];
+        pr.model_changed = 0;
+        pr.lnPrior = 0.0;
+        pr.lnHast = 0.0;
+        bool full = false;
+        int lowest = -1;  // lowest dirty node of a path move
+        if (g == 0) {
+            pr.type = MV_INIT;
             full = true;
         } else {
-            // Inverse Gamma shape multiplier (Chain.pyx:320-377).
-            const double lnM = d.alpha_lambda * (philox_u01(rng) - 0.5);
-            const double a0i = 1.0 / m0.alpha, a1i = a0i * exp(lnM);
-            m1 = m0;
-            m1.alpha = 1.0 / a1i;
-            pr.lnPrior = -d.alpha_prior * (a1i - a0i);
-            pr.lnHast = lnM;
-            pr.model_changed = 1;
-            full = true;
+            const double u = philox_u01(rng);
+            int t = 0;
+            while (t < kMoves - 1 && u >= d.wcdf[t]) ++t;
+            if ((t == MV_NNI || t == MV_SPR) && N < 4) t = MV_BRLEN;
+            if (t == MV_ALPHA && d.kact < 2) t = MV_BRLEN;
+            pr.type = t;
+            if (t == MV_BRLEN) {
+                // Uniform edge = uniform non-root node (Chain.pyx:442-447).
+                unsigned k = philox_below(rng, NN - 1);
+                const unsigned e = (k >= d.root) ? k + 1 : k;
+                const double lnM = d.brlen_lambda * (philox_u01(rng) - 0.5);
+                const double v0 = len[e], v1 = v0 * exp(lnM);
+                len[e] = v1;
+                pr.node = (int)e;
+                pr.oldlen = v0;
+                pr.lnPrior = -d.brlen_prior * (v1 - v0);
+                pr.lnHast = lnM;
+                lowest = parent[e];
+            } else if (t == MV_NNI) {
+                // Internal non-root node v, edge (v, p): swap a child a of v
+                // with a sibling c of v (another child of p).
+                unsigned k = philox_below(rng, M - 1);  // internal ids N..NN-1 minus root
+                unsigned v = N + k;
+                if (v >= d.root) ++v;
+                const int p = parent[v];
+                const int ai = (int)philox_below(rng, 2);
+                const int a = child[v * 3 + ai];
+                int sib[2], ns = 0;
+                for (int j = 0; j < 3; ++j) {
+                    const int x = child[p * 3 + j];
+                    if (x >= 0 && x != (int)v) sib[ns++] = x;
+                }
+                const int cc = sib[ns > 1 ? philox_below(rng, ns) : 0];
+                for (int j = 0; j < 3; ++j) {
+                    if (child[v * 3 + j] == a) child[v * 3 + j] = cc;
+                    if (child[p * 3 + j] == cc) child[p * 3 + j] = a;
+                }
+                parent[a] = p;
+                parent[cc] = (int)v;
+                pr.node = (int)v;
+                pr.a = a;
+                pr.c = cc;
+                lowest = (int)v;
+            } else if (t == MV_SPR) {
+                // Subtree s: uniform over non-root nodes whose parent is not
+                // the root (the root keeps its three children).
+                const unsigned ns = NN - 1 - 3;
+                unsigned k = philox_below(rng, ns);
+                int s = -1;
+                for (unsigned v = 0; v < NN && s < 0; ++v) {
+                    if (v == d.root || parent[v] == (int)d.root) continue;
+                    if (k-- == 0) s = (int)v;
+                }
+                const int p = parent[s], g = parent[p];
+                int jb = -1, jg = -1;
+                for (int j = 0; j < 3; ++j) {
+                    const int x = child[p * 3 + j];
+                    if (x >= 0 && x != s) jb = j;
+                    if (child[g * 3 + j] == p) jg = j;
+                }
+                const int b = child[p * 3 + jb];
+                // Mark the subtree of s (2 in the dirty flags, cleared below).
+                unsigned nsub = 0;
+                {
+                    int sp = 0;
+                    stack[sp++] = s;
+                    while (sp > 0) {
+                        const int v = stack[--sp];
+                        dflag[v] = 2;
+                        ++nsub;
+                        for (int j = 0; j < 3; ++j) {
+                            const int x = child[v * 3 + j];
+                            if (x >= 0) stack[sp++] = x;
+                        }
+                    }
+                }
+                // Prune: b takes p's place under g, the two edges merge.
+                pr.lb = len[b];
+                pr.lp = len[p];
+                child[g * 3 + jg] = b;
+                parent[b] = g;
+                len[b] = pr.lb + pr.lp;
+                // Target edge (x, parent[x]) of the pruned tree, outside the
+                // subtree: not the root, not p, not marked.
+                const unsigned ne = NN - 2 - nsub;
+                k = philox_below(rng, ne);
+                int x = -1;
+                for (unsigned v = 0; v < NN && x < 0; ++v) {
+                    if (v == d.root || (int)v == p || dflag[v] == 2) continue;
+                    if (k-- == 0) x = (int)v;
+                }
+                {
+                    int sp = 0;
+                    stack[sp++] = s;
+                    while (sp > 0) {
+                        const int v = stack[--sp];
+                        dflag[v] = 0;
+                        for (int j = 0; j < 3; ++j) {
+                            const int y = child[v * 3 + j];
+                            if (y >= 0) stack[sp++] = y;
+                        }
+                    }
+                }
+                const int xp = parent[x];
+                int jx = -1;
+                for (int j = 0; j < 3; ++j)
+                    if (child[xp * 3 + j] == x) jx = j;
+                const double lx = len[x];
+                pr.lx = (x == b) ? pr.lb : lx;
+                // Regraft p on (x, xp) at a uniform point.
+                const double u = philox_u01(rng);
+                child[xp * 3 + jx] = p;
+                parent[p] = xp;
+                child[p * 3 + jb] = x;
+                parent[x] = p;
+                len[p] = u * lx;
+                len[x] = (1.0 - u) * lx;
+                pr.s = s;
+                pr.p = p;
+                pr.g = g;
+                pr.b = b;
+                pr.x = x;
+                pr.xp = xp;
+                pr.jg = jg;
+                pr.jb = jb;
+                pr.jx = jx;
+                pr.lnHast = (lx > 0.0) ? log(lx) - log(pr.lb + pr.lp) : 0.0;
+                pr.lnPrior = (lx > 0.0) ? 0.0 : -INFINITY;
+                // Dirty: both paths to the root (p's new place, g's old child).
+                for (int v = p; v >= 0; v = parent[v]) dflag[v] = 1;
+                for (int v = g; v >= 0; v = parent[v]) dflag[v] = 1;
+            } else if (t == MV_FREQS) {
+                // Base frequencies ~ Dirichlet(conc * pi).
+                double f0[4], f1[4], a0[4], a1[4], s0 = 0.0, s1 = 0.0;
+                for (int i = 0; i < 4; ++i) s0 += m0.freqs[i];
+                for (int i = 0; i < 4; ++i) {
+                    f0[i] = m0.freqs[i] / s0;
+                    a0[i] = d.freq_conc * f0[i];
+                    f1[i] = philox_gamma(rng, a0[i]);
+                    if (f1[i] < 1e-300) f1[i] = 1e-300;
+                    s1 += f1[i];
+                }
+                for (int i = 0; i < 4; ++i) {
+                    f1[i] /= s1;
+                    a1[i] = d.freq_conc * f1[i];
+                }
+                m1 = m0;
+                for (int i = 0; i < 4; ++i) m1.freqs[i] = f1[i];
+                pr.lnHast = ln_dirichlet(a1, f0, 4) - ln_dirichlet(a0, f1, 4);
+                pr.model_changed = 1;
+                s_fin = FIN_EIG;
+                full = true;
+            } else if (t == MV_RATES) {
+                // Exchangeabilities ~ Dirichlet(conc * r / sum r).
+                double r0[6], r1[6], a0[6], a1[6], s0 = 0.0, s1 = 0.0;
+                for (int i = 0; i < 6; ++i) s0 += m0.rates[i];
+                for (int i = 0; i < 6; ++i) {
+                    r0[i] = m0.rates[i] / s0;
+                    a0[i] = d.rate_conc * r0[i];
+                    r1[i] = philox_gamma(rng, a0[i]);
+                    if (r1[i] < 1e-300) r1[i] = 1e-300;
+                    s1 += r1[i];
+                }
+                for (int i = 0; i < 6; ++i) {
+                    r1[i] /= s1;
+                    a1[i] = d.rate_conc * r1[i];
+                }
+                m1 = m0;
+                for (int i = 0; i < 6; ++i) m1.rates[i] = r1[i] * 6.0;
+                pr.lnHast = ln_dirichlet(a1, r0, 6) - ln_dirichlet(a0, r1, 6);
+                pr.model_changed = 1;
+                s_fin = FIN_EIG;
+                full = true;
+            } else {
+                // Inverse Gamma shape multiplier (Chain.pyx:320-377).
+                const double lnM = d.alpha_lambda * (philox_u01(rng) - 0.5);
+                const double a0i = 1.0 / m0.alpha, a1i = a0i * exp(lnM);
+                m1 = m0;
+                m1.alpha = 1.0 / a1i;
+                pr.lnPrior = -d.alpha_prior * (a1i - a0i);
+                pr.lnHast = lnM;
+                pr.model_changed = 1;
+                s_fin = FIN_GAMMA;
+                full = true;
+            }
         }
-        if (pr.model_changed && !mc3_model_finish(m1, d.kact)) {
+        s_full = full;
+        s_lowest = lowest;
+    }
+    __syncthreads();
+    // The proposed model's derived quantities (a second warp) while thread
+    // 0 lists the dirty nodes and assigns stack slots.
+    if (threadIdx.x >= 32 && threadIdx.x < 64 && s_fin) {
+        Mc3Model &m1 = d.model[c * 2 + (1 - d.curmodel[c])];
+        const bool ok = mc3_model_finish_warp(m1, d.kact, s_fin);
+        if (threadIdx.x == 32 && !ok) {
             // A model that cannot be decomposed is rejected outright.
             pr.lnPrior = -INFINITY;
             m1.ok = 0;
         }
     }
+    if (threadIdx.x == 0) {
+        const bool full = s_full;
+        const int lowest = s_lowest;
+        // Dirty internal nodes, children before parents.
+        int nd = 0;
+        if (pr.type == MV_SPR) {
+            // The nodes flagged above, in reversed pre-order of the new tree.
+            int sp = 0;
+            stack[sp++] = (int)d.root;
+            while (sp > 0) {
+                const int v = stack[--sp];
+                if (dflag[v]) dirty[nd++] = v;
+                for (int j = 0; j < 3; ++j) {
+                    const int x = child[v * 3 + j];
+                    if (x >= (int)N) stack[sp++] = x;
+                }
+            }
+            for (int i = 0, j = nd - 1; i < j; ++i, --j) {
+                const int t = dirty[i];
+                dirty[i] = dirty[j];
+                dirty[j] = t;
+            }
+        } else if (full) {
+            // Iterative post-order from the root.
+            int sp = 0, top = 0;
+            stack[sp++] = (int)d.root;
+            while (sp > 0) {
+                const int v = stack[--sp];
+                dirty[top++] = v;  // pre-order (parents first), reversed below
+                for (int j = 0; j < 3; ++j) {
+                    const int x = child[v * 3 + j];
+                    if (x >= (int)N) stack[sp++] = x;
+                }
+            }
+            // Reversed pre-order is a valid post-order (children first).
+            for (int i = 0, j = top - 1; i < j; ++i, --j) {
+                const int t = dirty[i];
+                dirty[i] = dirty[j];
+                dirty[j] = t;
+            }
+            nd = top;
+        } else {
+            for (int v = lowest; v >= 0; v = parent[v]) dirty[nd++] = v;
+        }
+        pr.ndirty = nd;
+        for (int i = 0; i < nd; ++i) dflag[dirty[i]] = 1;
 
-    // Dirty internal nodes, children before parents.
-    int nd = 0;
-    if (pr.type == MV_SPR) {
-        // The nodes flagged above, in reversed pre-order of the new tree.
-        int sp = 0;
-        stack[sp++] = (int)d.root;
-        while (sp > 0) {
-            const int v = stack[--sp];
-            if (dflag[v]) dirty[nd++] = v;
+        // Children and leaf children before each op (record layout).
+        unsigned nk = 0, nl = 0;
+        for (int o = 0; o < nd; ++o) {
+            kid0[o] = nk;
+            leaf0[o] = nl;
+            const int v = dirty[o];
             for (int j = 0; j < 3; ++j) {
-                const int x = child[v * 3 + j];
-                if (x >= (int)N) stack[sp++] = x;
+                const int u = child[v * 3 + j];
+                if (u < 0) continue;
+                ++nk;
+                if (u < (int)N) ++nl;
             }
         }
-        for (int i = 0, j = nd - 1; i < j; ++i, --j) {
-            const int t = dirty[i];
-            dirty[i] = dirty[j];
-            dirty[j] = t;
-        }
-    } else if (full) {
-        // Iterative post-order from the root.
-        int sp = 0, top = 0;
-        stack[sp++] = (int)d.root;
-        while (sp > 0) {
-            const int v = stack[--sp];
-            dirty[top++] = v;  // pre-order (parents first), reversed below
+        kid0[nd] = nk;
+        leaf0[nd] = nl;
+        // Shared-memory stack slots, as the host planner assigns them: a
+        // result keeps a slot until its one consumer (a later op of this
+        // walk) reads it; with no free slot the oldest holder loses its
+        // slot and its consumer reads the HBM copy.  The DFS stack is free
+        // now and maps a dirty node to its op.
+        int32_t *op_of = stack;
+        int owner[kMaxSlots];
+        const int cap = (int)d.nslot_cap;
+        for (int q = 0; q < cap; ++q) owner[q] = -1;
+        for (int o = 0; o < nd; ++o) {
+            const int v = dirty[o];
+            int ci = 0;
             for (int j = 0; j < 3; ++j) {
-                const int x = child[v * 3 + j];
-                if (x >= (int)N) stack[sp++] = x;
+                const int u = child[v * 3 + j];
+                if (u < 0) continue;
+                int ks = -1;
+                if (u >= (int)N && dflag[u]) {
+                    const int prod = op_of[u];
+                    const int sl = op_slot[prod];
+                    if (sl >= 0 && owner[sl] == prod) {
+                        ks = sl;
+                        owner[sl] = -1;
+                    }
+                }
+                kid_slot[o * 3 + ci++] = (int8_t)ks;
             }
+            op_of[v] = o;
+            int sl = -1;
+            if (o + 1 < nd && cap > 0) {
+                for (int q = 0; q < cap && sl < 0; ++q)
+                    if (owner[q] < 0) sl = q;
+                if (sl < 0) {
+                    sl = 0;
+                    for (int q = 1; q < cap; ++q)
+                        if (owner[q] < owner[sl]) sl = q;
+                }
+                owner[sl] = o;
+            }
+            op_slot[o] = (int8_t)sl;
         }
-        // Reversed pre-order is a valid post-order (children first).
-        for (int i = 0, j = top - 1; i < j; ++i, --j) {
-            const int t = dirty[i];
-            dirty[i] = dirty[j];
-            dirty[j] = t;
-        }
-        nd = top;
-    } else {
-        for (int v = lowest; v >= 0; v = parent[v]) dirty[nd++] = v;
+        s_nd = nd;
     }
-    pr.ndirty = nd;
-    for (int i = 0; i < nd; ++i) dflag[dirty[i]] = 1;
-
-    // Op records: parent -> its spare buffer; children -> spare buffer if
-    // dirty (computed earlier in this walk), else current.
-    const Mc3Model &mm = pr.model_changed ? m1 : m0;
+    __syncthreads();
+    const int nd = s_nd;
+    // Op records, one op per thread: parent -> its spare buffer; children
+    // -> spare buffer if dirty (computed earlier in this walk), else
+    // current.  Leaf children take staged-leaf indices in op order (each
+    // leaf has one parent, so no leaf is staged twice).
+    const Mc3Model &mm = pr.model_changed ? d.model[c * 2 + (1 - d.curmodel[c])]
+                                          : d.model[c * 2 + d.curmodel[c]];
     const size_t elt = d.prec == CXG_FP32 ? 4 : 8;
     unsigned char *rec = d.rec + (size_t)c * M * d.rstride;
     const uint8_t **leaves = d.leaves + (size_t)c * N;
     double *klen = d.kid_len + (size_t)c * d.maxkids;
     uint64_t *kdst = d.kid_dst + (size_t)c * d.maxkids;
     int32_t *ktab = d.kid_tab + (size_t)c * d.maxkids;
-    unsigned nkid = 0, nleaf = 0;
-    for (int o = 0; o < nd; ++o) {
+    for (int o = threadIdx.x; o < nd; o += blockDim.x) {
         const int v = dirty[o];
         const int mi = v - (int)N;
         unsigned char *r = rec + (size_t)o * d.rstride;
         RecHead hd;
         hd.data = d.cl_data[((size_t)c * M + mi) * 2 + (1 - cur[v])];
         hd.scaler = d.cl_sc[((size_t)c * M + mi) * 2 + (1 - cur[v])];
-        unsigned nch = 0;
-        for (int j = 0; j < 3; ++j)
-            if (child[v * 3 + j] >= 0) ++nch;
+        const unsigned nch = kid0[o + 1] - kid0[o];
         hd.nchild = nch;
-        hd.slot = -1;
+        hd.slot = op_slot[o];
         hd.flags = 0;
         hd.pad_ = 0;
         memcpy(r, &hd, sizeof(hd));
-        unsigned ci = 0;
+        unsigned ci = 0, nkid = kid0[o], li = leaf0[o];
         for (int j = 0; j < 3; ++j) {
             const int u = child[v * 3 + j];
             if (u < 0) continue;
             RecChild ch;
             memset(&ch, 0, sizeof(ch));
             if (u < (int)N) {
-                unsigned li = 0;
-                while (li < nleaf && leaves[li] != d.leafmask[u]) ++li;
-                if (li == nleaf) leaves[nleaf++] = d.leafmask[u];
+                leaves[li] = d.leafmask[u];
                 ch.src = SRC_LEAF;
-                ch.idx = li;
+                ch.idx = li++;
                 ch.tab = nkid;
                 ktab[nkid] = d.prec == CXG_FP64 ? (int32_t)nkid : -1;
+            } else if (kid_slot[o * 3 + ci] >= 0) {
+                ch.src = SRC_SLOT;
+                ch.idx = (uint32_t)kid_slot[o * 3 + ci];
+                ktab[nkid] = -1;
             } else {
                 const int ui = u - (int)N;
                 const int b = dflag[u] ? 1 - cur[u] : cur[u];
@@ -476,11 +643,21 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             ++ci;
         }
     }
-    d.nkids[c] = nkid;
-    PlanArgs &job = d.jobs[c];
-    job.nops = (uint32_t)nd;
-    job.nleaf = nleaf;
-    job.pn = mm.pn;
+    // The tree (moved) and the dirty list back to HBM.
+    for (unsigned i = threadIdx.x; i < NN; i += blockDim.x) {
+        g_len[i] = len[i];
+        g_parent[i] = parent[i];
+    }
+    for (unsigned i = threadIdx.x; i < NN * 3; i += blockDim.x) g_child[i] = child[i];
+    for (int i = threadIdx.x; i < nd; i += blockDim.x)
+        d.dirty[(size_t)c * M + i] = dirty[i];
+    if (threadIdx.x == 0) {
+        d.nkids[c] = kid0[nd];
+        PlanArgs &job = d.jobs[c];
+        job.nops = (uint32_t)nd;
+        job.nleaf = leaf0[nd];
+        job.pn = mm.pn;
+    }
 }
 
 // P matrices of every chain's child edges: thread per (chain, kid, comp).
@@ -511,11 +688,12 @@ __global__ void mc3_pmat_kernel(Mc3Dev d) {
     pmat_one(a, r);
 }
 
+// One block; thread c decides chain c, then thread 0 tries the heat swap.
 __global__ void mc3_accept_kernel(Mc3Dev d) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0) return;
     const uint64_t g = *d.gen;
     const unsigned N = d.ntaxa, NN = d.nnodes;
-    for (unsigned c = 0; c < d.nchains; ++c) {
+    for (unsigned c = threadIdx.x; c < d.nchains; c += blockDim.x) {
         Mc3Prop &pr = d.prop[c];
         const char *res = d.results + (size_t)c * 32;
         const uint32_t ninf = *(const uint32_t *)(res + 4);
@@ -577,6 +755,8 @@ __global__ void mc3_accept_kernel(Mc3Dev d) {
         }
         (void)N;
     }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     // Heat swap between a random pair (Chain.pyx:1874-1911).
     if (d.nchains > 1 && g > 0 && g % d.swap_stride == 0) {
         Philox rng;
@@ -618,6 +798,7 @@ struct cxgMc3 {
     std::vector<void *> allocs;
     BatchArgs ba;
     unsigned grid = 0, pmat_grid = 0;
+    size_t propose_smem = 0;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
     unsigned graph_gens = 0;
@@ -656,13 +837,14 @@ static void mc3_free(cxgMc3 *h) {
 
 static int mc3_enqueue_gen(cxgMc3 *h) {
     const Mc3Dev &d = h->d;
-    mc3_propose_kernel<<<d.nchains, 32, 0, h->stream>>>(d);
+    mc3_propose_kernel<<<d.nchains, 128, h->propose_smem, h->stream>>>(d);
     CXG_CHECK_LAUNCH("mc3_propose_kernel");
     mc3_pmat_kernel<<<h->pmat_grid, 128, 0, h->stream>>>(d);
     CXG_CHECK_LAUNCH("mc3_pmat_kernel");
     cudaError_t e = launch_batch((int)d.prec, h->ba, h->grid, h->stream);
     if (e != cudaSuccess) return cuda_fail(e, "walk_batch_kernel");
-    mc3_accept_kernel<<<1, 32, 0, h->stream>>>(d);
+    mc3_accept_kernel<<<1, d.nchains < 1024 ? ((d.nchains + 31) / 32) * 32 : 1024, 0,
+                        h->stream>>>(d);
     CXG_CHECK_LAUNCH("mc3_accept_kernel");
     return 0;
 }
@@ -671,7 +853,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     std::lock_guard<std::mutex> lk(g_mc3_mu);
     if (cfg == nullptr || out == nullptr) return fail(CXG_EINVAL, "cxgMc3Create: NULL");
     const unsigned N = cfg->ntaxa;
-    if (N < 3 || N > 4096) return fail(CXG_EINVAL, "cxgMc3Create: 3..4096 taxa");
+    if (N < 3 || N > 3000) return fail(CXG_EINVAL, "cxgMc3Create: 3..3000 taxa");
     if (cfg->ncat < 1 || cfg->ncat > kMaxComps)
         return fail(CXG_EINVAL, "cxgMc3Create: 1..8 rate categories");
     if (cfg->nchains < 1 || cfg->nchains > 1024)
@@ -722,6 +904,18 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     cxgTuneGet(&tile, &tpp_q, &budget);
     const unsigned tpp = tuned_tpp(cfg->precision, K, tile);
     d.ntiles = d.ppad / tile;
+    {
+        // Stack slots within the tuned shared-memory budget, every leaf
+        // staged (the most a generation's walk stages).
+        const size_t base_b =
+            plan_smem_bytes(cfg->precision, K, tile, 0, 0, kRing, d.rstride);
+        const size_t slot_b =
+            plan_smem_bytes(cfg->precision, K, tile, 1, 0, kRing, d.rstride) - base_b;
+        const size_t leaf_b =
+            plan_smem_bytes(cfg->precision, K, tile, 0, N, kRing, d.rstride);
+        size_t cap = budget > leaf_b ? (budget - leaf_b) / slot_b : 0;
+        d.nslot_cap = (uint32_t)(cap > kMaxSlots ? kMaxSlots : cap);
+    }
     d.seed = cfg->seed;
     d.swap_stride = cfg->swap_stride ? cfg->swap_stride : 1;
     double wsum = 0.0;
@@ -856,7 +1050,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
         a.ring = kRing;
         a.nops = 0;
         a.nleaf = 0;
-        a.nslot = 0;
+        a.nslot = d.nslot_cap;
         a.tile = tile;
         a.tpp = tpp;
         a.kact = K;
@@ -891,10 +1085,11 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     ba.tpp = tpp;
     ba.ring = kRing;
     ba.kact = K;
-    ba.max_nslot = 0;
+    ba.max_nslot = d.nslot_cap;
     ba.max_nleaf = N;
     ba.max_rstride = d.rstride;
-    const size_t smem = plan_smem_bytes(cfg->precision, K, tile, 0, N, kRing, d.rstride);
+    const size_t smem = plan_smem_bytes(cfg->precision, K, tile, d.nslot_cap, N, kRing,
+                                        d.rstride);
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -905,6 +1100,16 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     }
     h->grid = (unsigned)(per * nsm);
     h->pmat_grid = (C * d.maxkids * K + 127) / 128;
+    h->propose_smem = mc3_propose_smem(NN, M);
+    {  // (the default limit counts the kernel's static shared memory too)
+        e = cudaFuncSetAttribute(mc3_propose_kernel,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)h->propose_smem);
+        if (e != cudaSuccess) {
+            mc3_free(h);
+            return cuda_fail(e, "cxgMc3Create: proposal shared memory");
+        }
+    }
     // Derived model quantities, then generation 0 (full evaluation).
     mc3_init_kernel<<<C, 32, 0, h->stream>>>(d);
     if ((e = cudaGetLastError()) != cudaSuccess) {

@@ -66,12 +66,19 @@ def _sweep(lib, shapes, measure):
     try:
         for shape in shapes:
             set_shape(lib, *shape)
-            ms = measure()
-            table.append({"tile": shape[0], "tpp": shape[1],
-                          "budget": shape[2], "ms": ms})
+            row = {"tile": shape[0], "tpp": shape[1], "budget": shape[2]}
+            try:
+                row["ms"] = measure()
+            except RuntimeError as e:
+                # A shape the device cannot launch is skipped, with why.
+                row["ms"] = float("inf")
+                row["error"] = str(e)
+            table.append(row)
     finally:
         set_shape(lib, *saved)
     best = min(table, key=lambda r: r["ms"])
+    if best["ms"] == float("inf"):
+        raise RuntimeError("no walker shape ran: %s" % table[0].get("error"))
     set_shape(lib, best["tile"], best["tpp"], best["budget"])
     return {"best": best, "table": table}
 

@@ -20,14 +20,18 @@ def restore(gpu):
     tune.set_shape(gpu, *saved)
 
 
-@pytest.mark.parametrize("pinv", [0.0, 0.2])
+@pytest.mark.parametrize("shape", [(40, 3000, 0.0), (40, 3000, 0.2),
+                                   (16, 1000, 0.0)])
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
-def test_every_shape_same_bits(gpu, port, restore, precision, pinv):
-    case = synth.Case(40, 3000, 0.1, 77, pinv=pinv, gap_frac=0.01)
+def test_every_shape_same_bits(gpu, port, restore, precision, shape):
+    """Every candidate shape, every stack budget (a budget near 48 KiB puts
+    static plus dynamic shared memory across the default launch limit)."""
+    ntaxa, nsites, pinv = shape
+    case = synth.Case(ntaxa, nsites, 0.1, 77, pinv=pinv, gap_frac=0.01)
     want = case.lik(lib=port).lnL()
     lik = case.lik(lib=gpu, precision=precision)
     kact = tune.active_components(lik)
-    shapes = tune.candidates(precision, kact, budgets=(0, 24 << 10, 96 << 10))
+    shapes = tune.candidates(precision, kact)
     assert any(g > 1 for _, g, _ in shapes) == (precision == "fp32" and
                                                 kact % 2 == 0)
     first = None
