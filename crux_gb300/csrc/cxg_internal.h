@@ -63,7 +63,9 @@ struct RecHead {
 enum : uint32_t { REC_NO_HBM = 1 };
 
 // One child of an op.  `data`/`scaler` address the HBM copy (SRC_GLOBAL);
-// `idx` is the staged-leaf index (SRC_LEAF) or the stack slot (SRC_SLOT).
+// for SRC_LEAF `data` is the leaf's mask array [ppad] (one uint8 state
+// mask per pattern) and `idx` its staged row when the job stages leaves;
+// for SRC_SLOT `idx` is the stack slot.
 struct RecChild {
     const void *data;
     const void *scaler;
@@ -82,11 +84,20 @@ static_assert(sizeof(RecChild) == 32, "record child is 32 bytes");
 // warp writes 512 contiguous bytes per store.
 struct PlanArgs {
     const unsigned char *rec;      // [nops][rstride] op records
-    const uint8_t *const *leaves;  // [nleaf] mask arrays staged per tile
+    // [nops][lmax] mask arrays of each op's leaf children, in the record's
+    // child order, null-terminated when fewer than lmax: they are copied
+    // with the op's record, so lmax rows of tile bytes follow it in the
+    // stage (a plan with no leaf children may use lmax 0).
+    const uint8_t *const *lrows;
+    uint32_t lmax;
+    // A job whose leaves fit the staging budget stages them instead: nleaf
+    // mask arrays, each loaded once per tile; leaf children then name their
+    // staged row by RecChild.idx (lmax is 0).  nleaf 0: leaves stream.
+    const uint8_t *const *leaves;
+    uint32_t nleaf;
     uint32_t rstride;
     uint32_t ring;        // records in flight per CTA
     uint32_t nops;
-    uint32_t nleaf;
     uint32_t nslot;       // shared-memory stack slots per tile
     uint32_t tile;        // patterns per CTA (blockDim.x / tpp)
     uint32_t kact;        // active components (weightScaled != 0)
@@ -136,7 +147,7 @@ struct WalkItem {
 
 // A batched launch: a persistent grid claims items from `counter` (items
 // sorted longest first by the host); shared memory is laid out for the
-// largest job (nslot, nleaf, rstride maxima); all jobs share kact, tile and
+// largest job (nslot, rstride and lmax maxima); all jobs share kact, tile and
 // the ring depth.
 struct BatchArgs {
     const PlanArgs *jobs;
@@ -144,18 +155,21 @@ struct BatchArgs {
     uint32_t nitems;
     unsigned *counter;
     uint32_t tile, ring, kact;
-    uint32_t max_nslot, max_nleaf, max_rstride;
+    uint32_t max_nslot, max_rstride, max_lmax, max_nleaf;
     uint32_t tpp;         // threads per pattern (all jobs); 0 is read as 1
 };
 
-size_t plan_smem_bytes(int precision, unsigned kact, unsigned tile,
-                       unsigned nslot, unsigned nleaf, unsigned ring,
-                       unsigned rstride);
+size_t plan_smem_bytes(int precision, unsigned kact, unsigned tile, unsigned nslot,
+                       unsigned ring, unsigned rstride, unsigned lmax,
+                       unsigned nleaf);
+// Largest staged leaf rows per CTA: jobs whose leaves take more stream
+// them with their records instead.
+constexpr size_t kLeafStageBytes = 16 * 1024;
 cudaError_t launch_batch(int precision, const BatchArgs &b, unsigned grid,
                          cudaStream_t s);
 // Resident CTAs per SM of the batched walker for this shape.
 int batch_ctas_per_sm(int precision, unsigned kact, unsigned tile,
-                      unsigned tpp, size_t smem);
+                      unsigned tpp, bool staged, size_t smem);
 
 // Inputs of the P-matrix kernel: one thread per (child, active comp); the
 // P matrix (FP64 arithmetic, stored as the plan's precision) goes into the

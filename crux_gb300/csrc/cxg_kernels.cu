@@ -216,34 +216,37 @@ __device__ __forceinline__ float pow2f(int n) {  // n in [-126, 127]
     return __int_as_float((n + 127) << 23);
 }
 
-// Shared memory of one CTA: mbarriers [ring], record ring [ring][rstride],
-// stack slots [nslot][K][U][tile] units, slot scalers [nslot][tile], staged
-// leaf masks [nleaf][tile].  A batched launch lays it out for its largest
-// job; every job uses a prefix of each region.
+// Shared memory of one CTA: mbarriers [ring]; the stage ring [ring] of
+// `stage` bytes, each an op record (rstride) followed, for a job that
+// streams its leaves, by this tile's mask rows of the op's leaf children
+// (lmax rows of tile bytes); stack slots [nslot][K][U][tile] units; slot
+// scalers [nslot][tile]; and, for a job that stages its leaves, every
+// leaf's mask row [nleaf][tile], loaded once per tile.  A batched launch
+// lays it out for its largest job; every job uses a prefix of each region.
 struct SmemLayout {
-    size_t bars, ring, slots, slot_sc, masks, total;
+    size_t bars, ring, stage, slots, slot_sc, masks, total;
 };
 
 static __host__ __device__ SmemLayout smem_layout(int precision, unsigned kact,
                                                   unsigned tile, unsigned nslot,
-                                                  unsigned nleaf, unsigned ring,
-                                                  unsigned rstride) {
+                                                  unsigned ring, unsigned rstride,
+                                                  unsigned lmax, unsigned nleaf) {
     const size_t U = precision == CXG_FP32 ? 1 : 2;
     const size_t sc = precision == CXG_FP32 ? 4 : 8;
     SmemLayout L;
     L.bars = 0;
     L.ring = ((size_t)ring * 8 + 127) & ~(size_t)127;
-    L.slots = L.ring + (size_t)ring * rstride;
+    L.stage = ((size_t)rstride + (size_t)lmax * tile + 15) & ~(size_t)15;
+    L.slots = L.ring + (size_t)ring * L.stage;
     L.slot_sc = L.slots + (size_t)nslot * kact * U * tile * 16;
     L.masks = L.slot_sc + (((size_t)nslot * tile * sc + 15) & ~(size_t)15);
     L.total = L.masks + (size_t)nleaf * tile;
     return L;
 }
 
-size_t plan_smem_bytes(int precision, unsigned kact, unsigned tile,
-                       unsigned nslot, unsigned nleaf, unsigned ring,
-                       unsigned rstride) {
-    return smem_layout(precision, kact, tile, nslot, nleaf, ring, rstride).total;
+size_t plan_smem_bytes(int precision, unsigned kact, unsigned tile, unsigned nslot,
+                       unsigned ring, unsigned rstride, unsigned lmax, unsigned nleaf) {
+    return smem_layout(precision, kact, tile, nslot, ring, rstride, lmax, nleaf).total;
 }
 
 // --- mbarrier and bulk-copy primitives (PTX) --------------------------------
@@ -286,6 +289,42 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// Leaf-row pointers of op q that thread 0 reads ahead (the first
+// kLeafPre; rows past them are read when the stage is issued).  Indexed
+// with constants only, so they stay in registers.
+constexpr int kLeafPre = 4;
+__device__ __forceinline__ void read_rows(const PlanArgs &a, unsigned q,
+                                          const uint8_t *(&pre)[kLeafPre]) {
+    const uint8_t *const *rows = a.lrows + (size_t)q * a.lmax;
+#pragma unroll
+    for (int j = 0; j < kLeafPre; ++j) pre[j] = (unsigned)j < a.lmax ? rows[j] : nullptr;
+}
+
+// Start op q's stage: its record and this tile's mask rows of its leaf
+// children (a.lrows[q][0..lmax), null-terminated, in the record's child
+// order), all completing on the stage's mbarrier.
+__device__ __forceinline__ void issue_stage(const PlanArgs &a, unsigned q,
+                                            unsigned char *st, uint64_t *bar,
+                                            unsigned tile_idx, unsigned tile,
+                                            const uint8_t *const (&pre)[kLeafPre]) {
+    const uint8_t *const *rows = a.lrows + (size_t)q * a.lmax;
+    unsigned n = 0;
+#pragma unroll
+    for (int j = 0; j < kLeafPre; ++j)
+        if (n == (unsigned)j && pre[j] != nullptr) n = j + 1;
+    if (n == kLeafPre)
+        while (n < a.lmax && rows[n] != nullptr) ++n;
+    fence_proxy_async();
+    mbar_expect_tx(bar, a.rstride + n * tile);
+    bulk_g2s(st, a.rec + (size_t)q * a.rstride, a.rstride, bar);
+    const size_t off = (size_t)tile_idx * tile;
+#pragma unroll
+    for (int j = 0; j < kLeafPre; ++j)
+        if ((unsigned)j < n) bulk_g2s(st + a.rstride + (size_t)j * tile, pre[j] + off, tile, bar);
+    for (unsigned j = kLeafPre; j < n; ++j)
+        bulk_g2s(st + a.rstride + (size_t)j * tile, rows[j] + off, tile, bar);
+}
+
 // Spin on a phase with an iteration bound; false if it gave up.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
     for (uint32_t it = 0; it < kSpinLimit; ++it)
@@ -309,7 +348,7 @@ __device__ __forceinline__ X group_max(X x) {
 // per ring stage, the parity of the next completion to wait for; it
 // persists across the items a CTA processes.  Returns false if a bounded
 // wait gave up.
-template <typename T, int KT, int G>
+template <typename T, int KT, int G, bool STAGED>
 __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
                           const SmemLayout &Lay, unsigned ring_depth,
                           uint32_t &phase) {
@@ -331,32 +370,50 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
     unsigned char *ring = smem + Lay.ring;
     V *slots = reinterpret_cast<V *>(smem + Lay.slots);
     S *slot_sc = reinterpret_cast<S *>(smem + Lay.slot_sc);
+    // STAGED: every leaf's row is staged once per tile and records travel
+    // alone (stage stride a.rstride).  Else each stage carries its op's
+    // leaf rows (stage stride Lay.stage).
+    const size_t sstride = STAGED ? (size_t)a.rstride : Lay.stage;
     uint8_t *masks = smem + Lay.masks;
     const unsigned R = ring_depth;
 
-    // Start streaming the job's first R op records.
-    if (tid == 0) {
-        fence_proxy_async();
-        for (unsigned o = 0; o < R && o < a.nops; ++o) {
-            mbar_expect_tx(&bars[o], a.rstride);
-            bulk_g2s(ring + (size_t)o * a.rstride, a.rec + (size_t)o * a.rstride,
-                     a.rstride, &bars[o]);
+    if (STAGED) {
+        // Start streaming the job's first R op records.
+        if (tid == 0) {
+            fence_proxy_async();
+            for (unsigned o = 0; o < R && o < a.nops; ++o) {
+                mbar_expect_tx(&bars[o], a.rstride);
+                bulk_g2s(ring + (size_t)o * a.rstride, a.rec + (size_t)o * a.rstride,
+                         a.rstride, &bars[o]);
+            }
         }
+        // Stage this tile's leaf masks with 16-byte loads.
+        const unsigned chunks = tile / 16;
+        for (unsigned i = tid; i < a.nleaf * chunks; i += nthr) {
+            const unsigned l = i / chunks, c = i % chunks;
+            const uint4 *src =
+                reinterpret_cast<const uint4 *>(a.leaves[l] + (size_t)tile_idx * tile) + c;
+            reinterpret_cast<uint4 *>(masks + (size_t)l * tile)[c] = __ldg(src);
+        }
+        __syncthreads();
+    } else {
+        // Start streaming the job's first R stages (records and leaf rows).
+        if (tid == 0)
+            for (unsigned o = 0; o < R && o < a.nops; ++o) {
+                const uint8_t *rows0[kLeafPre];
+                read_rows(a, o, rows0);
+                issue_stage(a, o, ring + (size_t)o * sstride, &bars[o], tile_idx, tile, rows0);
+            }
     }
-    // Stage this tile's leaf masks with 16-byte loads.
-    const unsigned chunks = tile / 16;
-    for (unsigned i = tid; i < a.nleaf * chunks; i += nthr) {
-        const unsigned l = i / chunks, c = i % chunks;
-        const uint4 *src =
-            reinterpret_cast<const uint4 *>(a.leaves[l] + (size_t)tile_idx * tile) + c;
-        reinterpret_cast<uint4 *>(masks + (size_t)l * tile)[c] = __ldg(src);
-    }
-    __syncthreads();
 
     T acc[KT * 4];
     S lns = S(0);
     for (unsigned o = 0; o < a.nops; ++o) {
         const unsigned stage = o % R;
+        // Streaming: thread 0 reads op o + R's leaf-row pointers now; it
+        // issues that stage after this op, when the loads have long arrived.
+        const uint8_t *pre[kLeafPre] = {nullptr, nullptr, nullptr, nullptr};
+        if (!STAGED && tid == 0 && o + R < a.nops) read_rows(a, o + R, pre);
         if (tid == 0) {
             const uint32_t par = (phase >> stage) & 1u;
             s_ok = mbar_wait_bounded(&bars[stage], par);
@@ -367,7 +424,9 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             if (tid == 0) atomicOr(a.err, 1u);
             return false;  // all threads leave together
         }
-        const unsigned char *rec = ring + (size_t)stage * a.rstride;
+        const unsigned char *rec = ring + (size_t)stage * sstride;
+        const uint8_t *lrow = rec + a.rstride;  // this op's leaf rows
+        unsigned nlk = 0;  // leaf children of this op seen so far
         const RecHead *hd = reinterpret_cast<const RecHead *>(rec);
         const RecChild *kids = reinterpret_cast<const RecChild *>(rec + sizeof(RecHead));
         const unsigned nchild = hd->nchild;
@@ -381,7 +440,12 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             T msg[KT * 4];
             const bool leaf = (ch.src == SRC_LEAF);
             const bool in_slot = (ch.src == SRC_SLOT);
-            const unsigned m = leaf ? masks[(size_t)ch.idx * tile + pl] : 0u;
+            unsigned m = 0u;
+            if (STAGED) {
+                if (leaf) m = masks[(size_t)ch.idx * tile + pl];
+            } else {
+                if (leaf) m = lrow[(size_t)(nlk++) * tile + pl];
+            }
             const V *xs = in_slot ? slots + ((size_t)ch.idx * KA + k0) * U * tile + pl
                                   : static_cast<const V *>(ch.data) + (size_t)k0 * U * ppad + p;
             const size_t stride = in_slot ? tile : ppad;
@@ -446,13 +510,18 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
         void *yscaler = hd->scaler;
         const int yslot = hd->slot;
         const bool yhbm = !(hd->flags & REC_NO_HBM);
-        // Every thread has read the record: hand its stage to the next copy.
+        // Every thread has read the stage: hand it to op o + R.
         __syncthreads();
         if (tid == 0 && o + R < a.nops) {
-            fence_proxy_async();
-            mbar_expect_tx(&bars[stage], a.rstride);
-            bulk_g2s(ring + (size_t)stage * a.rstride,
-                     a.rec + (size_t)(o + R) * a.rstride, a.rstride, &bars[stage]);
+            if (STAGED) {
+                fence_proxy_async();
+                mbar_expect_tx(&bars[stage], a.rstride);
+                bulk_g2s(ring + (size_t)stage * a.rstride,
+                         a.rec + (size_t)(o + R) * a.rstride, a.rstride, &bars[stage]);
+            } else {
+                issue_stage(a, o + R, ring + (size_t)stage * sstride, &bars[stage], tile_idx,
+                            tile, pre);
+            }
         }
         if (sizeof(T) == 8) {
             sc = group_max<G>(sc);
@@ -566,24 +635,25 @@ __device__ __forceinline__ void init_ring(const SmemLayout &Lay, unsigned R) {
 }
 
 // One plan: one CTA per tile.
-template <typename T, int KT, int G>
+template <typename T, int KT, int G, bool STAGED>
 __global__ void __launch_bounds__(kMaxThreads) walk_kernel(PlanArgs a) {
     const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT * G,
-                                       blockDim.x / G, a.nslot, a.nleaf, a.ring,
-                                       a.rstride);
+                                       blockDim.x / G, a.nslot, a.ring,
+                                       a.rstride, a.lmax, a.nleaf);
     init_ring(Lay, a.ring);
     uint32_t phase = 0;
-    walk_tile<T, KT, G>(a, blockIdx.x, Lay, a.ring, phase);
+    walk_tile<T, KT, G, STAGED>(a, blockIdx.x, Lay, a.ring, phase);
 }
 
 // Many jobs: a persistent grid claims (job, tile) items in the host's order
 // (longest first).
-template <typename T, int KT, int G>
+template <typename T, int KT, int G, bool STAGED>
 __global__ void __launch_bounds__(kMaxThreads) walk_batch_kernel(BatchArgs b) {
     __shared__ unsigned s_item;
     const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT * G,
-                                       blockDim.x / G, b.max_nslot, b.max_nleaf,
-                                       b.ring, b.max_rstride);
+                                       blockDim.x / G, b.max_nslot,
+                                       b.ring, b.max_rstride, b.max_lmax,
+                                       b.max_nleaf);
     init_ring(Lay, b.ring);
     uint32_t phase = 0;
     for (;;) {
@@ -593,7 +663,7 @@ __global__ void __launch_bounds__(kMaxThreads) walk_batch_kernel(BatchArgs b) {
         __syncthreads();
         if (item >= b.nitems) break;
         const WalkItem it = b.items[item];
-        if (!walk_tile<T, KT, G>(b.jobs[it.job], it.tile, Lay, b.ring, phase)) break;
+        if (!walk_tile<T, KT, G, STAGED>(b.jobs[it.job], it.tile, Lay, b.ring, phase)) break;
     }
 }
 
@@ -619,27 +689,35 @@ static cudaError_t ensure_smem(Kern k, size_t sm, size_t &optin) {
 #define CXG_SHAPES_G1(X) X(1, 1) X(2, 1) X(3, 1) X(4, 1) X(5, 1) X(6, 1) X(7, 1) X(8, 1)
 #define CXG_SHAPES_GN(X) X(1, 2) X(2, 2) X(3, 2) X(4, 2) X(1, 4) X(2, 4)
 
-template <typename T, int KT, int G>
+template <typename T, int KT, int G, bool ST>
 static cudaError_t walk_fn(size_t sm, void (**fn)(PlanArgs)) {
     static size_t optin = 0;
-    *fn = walk_kernel<T, KT, G>;
-    return ensure_smem(walk_kernel<T, KT, G>, sm, optin);
+    *fn = walk_kernel<T, KT, G, ST>;
+    return ensure_smem(walk_kernel<T, KT, G, ST>, sm, optin);
 }
-template <typename T, int KT, int G>
+template <typename T, int KT, int G, bool ST>
 static cudaError_t batch_fn(size_t sm, void (**fn)(BatchArgs)) {
     static size_t optin = 0;
-    *fn = walk_batch_kernel<T, KT, G>;
-    return ensure_smem(walk_batch_kernel<T, KT, G>, sm, optin);
+    *fn = walk_batch_kernel<T, KT, G, ST>;
+    return ensure_smem(walk_batch_kernel<T, KT, G, ST>, sm, optin);
 }
 
-// The walker for (kact, G), with its dynamic shared memory limit raised to
-// `sm` bytes.
+// The walker for (kact, G, staged leaves or streamed), with its dynamic
+// shared memory limit raised to `sm` bytes.
 template <typename T, typename Fn>
-static cudaError_t pick_walker(unsigned kact, unsigned G, size_t sm, Fn *fn, bool batch) {
+static cudaError_t pick_walker(unsigned kact, unsigned G, bool staged, size_t sm, Fn *fn,
+                               bool batch) {
 #define CXG_X(KT, GG)                                                              \
     if (kact == (KT) * (GG) && G == (GG)) {                                        \
-        if (batch) return batch_fn<T, KT, GG>(sm, reinterpret_cast<void (**)(BatchArgs)>(fn)); \
-        return walk_fn<T, KT, GG>(sm, reinterpret_cast<void (**)(PlanArgs)>(fn)); \
+        if (batch)                                                                 \
+            return staged ? batch_fn<T, KT, GG, true>(                             \
+                                sm, reinterpret_cast<void (**)(BatchArgs)>(fn))    \
+                          : batch_fn<T, KT, GG, false>(                            \
+                                sm, reinterpret_cast<void (**)(BatchArgs)>(fn));   \
+        return staged ? walk_fn<T, KT, GG, true>(                                  \
+                            sm, reinterpret_cast<void (**)(PlanArgs)>(fn))         \
+                      : walk_fn<T, KT, GG, false>(                                 \
+                            sm, reinterpret_cast<void (**)(PlanArgs)>(fn));        \
     }
     CXG_SHAPES_G1(CXG_X)
     if constexpr (sizeof(T) == 4) {
@@ -654,10 +732,10 @@ static cudaError_t launch_plan_t(int precision, const PlanArgs &a,
                                  cudaStream_t s) {
     const unsigned G = a.tpp ? a.tpp : 1;
     const unsigned nb = plan_blocks(a.ppad, a.tile);
-    const size_t sm = plan_smem_bytes(precision, a.kact, a.tile, a.nslot, a.nleaf,
-                                      a.ring, a.rstride);
+    const size_t sm = plan_smem_bytes(precision, a.kact, a.tile, a.nslot,
+                                      a.ring, a.rstride, a.lmax, a.nleaf);
     void (*fn)(PlanArgs) = nullptr;
-    cudaError_t e = pick_walker<T>(a.kact, G, sm, &fn, false);
+    cudaError_t e = pick_walker<T>(a.kact, G, a.lmax == 0, sm, &fn, false);
     if (e != cudaSuccess) return e;
     fn<<<nb, a.tile * G, sm, s>>>(a);
     return cudaGetLastError();
@@ -679,9 +757,10 @@ static cudaError_t launch_batch_t(int precision, const BatchArgs &b,
                                   unsigned grid, cudaStream_t s) {
     const unsigned G = b.tpp ? b.tpp : 1;
     const size_t sm = plan_smem_bytes(precision, b.kact, b.tile, b.max_nslot,
-                                      b.max_nleaf, b.ring, b.max_rstride);
+                                      b.ring, b.max_rstride, b.max_lmax,
+                                      b.max_nleaf);
     void (*fn)(BatchArgs) = nullptr;
-    cudaError_t e = pick_walker<T>(b.kact, G, sm, &fn, true);
+    cudaError_t e = pick_walker<T>(b.kact, G, b.max_lmax == 0, sm, &fn, true);
     if (e != cudaSuccess) return e;
     fn<<<grid, b.tile * G, sm, s>>>(b);
     return cudaGetLastError();
@@ -699,9 +778,9 @@ cudaError_t launch_batch(int precision, const BatchArgs &b, unsigned grid,
 }
 
 template <typename T>
-static int batch_occ_t(unsigned kact, unsigned tile, unsigned G, size_t smem) {
+static int batch_occ_t(unsigned kact, unsigned tile, unsigned G, bool staged, size_t smem) {
     void (*fn)(BatchArgs) = nullptr;
-    cudaError_t e = pick_walker<T>(kact, G, smem, &fn, true);
+    cudaError_t e = pick_walker<T>(kact, G, staged, smem, &fn, true);
     int n = 0;
     if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, (int)(tile * G), smem);
@@ -709,11 +788,11 @@ static int batch_occ_t(unsigned kact, unsigned tile, unsigned G, size_t smem) {
 }
 
 int batch_ctas_per_sm(int precision, unsigned kact, unsigned tile, unsigned tpp,
-                      size_t smem) {
+                      bool staged, size_t smem) {
     const unsigned G = tpp ? tpp : 1;
     if (!walker_shape_ok(precision, kact, G) || tile * G > kMaxThreads) return 0;
-    return precision == CXG_FP32 ? batch_occ_t<float>(kact, tile, G, smem)
-                                 : batch_occ_t<double>(kact, tile, G, smem);
+    return precision == CXG_FP32 ? batch_occ_t<float>(kact, tile, G, staged, smem)
+                                 : batch_occ_t<double>(kact, tile, G, staged, smem);
 }
 
 __global__ void qdecomp_kernel(const double *rtri, const double *pi,

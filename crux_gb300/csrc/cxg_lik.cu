@@ -404,8 +404,12 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     }
     bytes += 4.0 * kact * s_el + e_el + 4.0 + 8.0;  // root read, freq, site
 
-    // Staged leaves: each distinct leaf child once per tile.
+    // Leaves: staged once per tile (each distinct leaf one row, named by
+    // kids[c].idx) when they fit kLeafStageBytes, else each op's mask
+    // arrays (kids[c].data) travel with its record (lmax rows per stage).
+    const unsigned tile = g_tile;
     std::vector<const uint8_t *> leaf_ptrs;
+    unsigned lmax = 0;
     {
         std::unordered_map<DevCL *, uint32_t> leaf_idx;
         for (size_t c = 0; c < kids.size(); ++c) {
@@ -417,9 +421,17 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
             }
             kids[c].idx = it->second;
         }
+        for (const HostOp &op : ops) {
+            unsigned n = 0;
+            for (uint32_t c = op.child0; c < op.child0 + op.nchild; ++c)
+                n += kids[c].src == SRC_LEAF;
+            if (n > lmax) lmax = n;
+        }
     }
-    const unsigned tile = g_tile;
     const unsigned nleaf = (unsigned)leaf_ptrs.size();
+    const bool stage_leaves = (size_t)nleaf * tile <= kLeafStageBytes;
+    const unsigned s_lmax = stage_leaves ? 0 : lmax;
+    const unsigned s_nleaf = stage_leaves ? nleaf : 0;
 
     // Shared-memory stack: a parent keeps a slot until its one consumer (a
     // later op of this run) reads it; with no free slot the oldest holder
@@ -433,15 +445,14 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
         if (b > rstride) rstride = b;
     }
     const unsigned ring = kRing;
-    const size_t base_bytes = plan_smem_bytes(prec, kact, tile, 0, 0, ring,
-                                              (unsigned)rstride);
+    const size_t base_bytes = plan_smem_bytes(prec, kact, tile, 0, ring,
+                                              (unsigned)rstride, s_lmax, s_nleaf);
     const size_t slot_bytes =
-        plan_smem_bytes(prec, kact, tile, 1, 0, ring, (unsigned)rstride) - base_bytes;
-    const size_t leaf_bytes =
-        plan_smem_bytes(prec, kact, tile, 0, nleaf, ring, (unsigned)rstride);
+        plan_smem_bytes(prec, kact, tile, 1, ring, (unsigned)rstride, s_lmax, s_nleaf) -
+        base_bytes;
     unsigned cap = 0;
-    if (g_smem_budget > leaf_bytes)
-        cap = (unsigned)((g_smem_budget - leaf_bytes) / slot_bytes);
+    if (g_smem_budget > base_bytes)
+        cap = (unsigned)((g_smem_budget - base_bytes) / slot_bytes);
     if (cap > kMaxSlots) cap = kMaxSlots;
     if (!use_slots) cap = 0;
     unsigned used = 0;
@@ -501,7 +512,7 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
 
     // Pack the program into pinned staging, one copy:
     //   records [nops][rstride] | elen | cmult | rmult | model | cube | eig |
-    //   dst | pn | leaves
+    //   dst | pn
     const unsigned nchild = (unsigned)kids.size();
     const unsigned nmod = (unsigned)models.size();
     auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
@@ -516,8 +527,9 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     size_t o_dst = al(o_eig + nmod * 4 * 8);
     size_t o_tab = al(o_dst + (size_t)nchild * 8);
     size_t o_pn = al(o_tab + (size_t)nchild * 4);
-    size_t o_leaf = al(o_pn + kact * 4 * 8);
-    size_t total = al(o_leaf + (nleaf ? nleaf : 1) * sizeof(void *));
+    size_t o_lrow = al(o_pn + kact * 4 * 8);
+    size_t o_leaf = al(o_lrow + (nrec * (s_lmax ? s_lmax : 1)) * sizeof(void *));
+    size_t total = al(o_leaf + (s_nleaf ? s_nleaf : 1) * sizeof(void *));
     rc = S.stage.ensure(total);
     if (rc) return rc;
     rc = P.prog.ensure(total);
@@ -568,7 +580,18 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
         memcpy(h + o_cube + m * 64 * 8, models[m]->qEigVecCube, 64 * 8);
         memcpy(h + o_eig + m * 4 * 8, models[m]->qEigVals, 4 * 8);
     }
-    if (nleaf) memcpy(h + o_leaf, leaf_ptrs.data(), nleaf * sizeof(void *));
+    {
+        // Streamed: leaf rows of each op in child order, null-terminated.
+        // Staged: the leaf table.
+        const void **lr = reinterpret_cast<const void **>(h + o_lrow);
+        memset(lr, 0, nrec * (s_lmax ? s_lmax : 1) * sizeof(void *));
+        for (size_t o = 0; o < ops.size() && s_lmax; ++o) {
+            unsigned j = 0;
+            for (uint32_t c = ops[o].child0; c < ops[o].child0 + ops[o].nchild; ++c)
+                if (kids[c].src == SRC_LEAF) lr[o * s_lmax + j++] = kids[c].data;
+        }
+        if (s_nleaf) memcpy(h + o_leaf, leaf_ptrs.data(), s_nleaf * sizeof(void *));
+    }
     char *d = static_cast<char *>(P.prog.p);
     CXG_CUDA(cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, S.stream));
     S.last_h2d = total;
@@ -605,10 +628,12 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     char *mp = static_cast<char *>(P.misc.p);
     PlanArgs &a = P.a;
     a.rec = (const unsigned char *)(d + o_rec);
+    a.lrows = (const uint8_t *const *)(d + o_lrow);
+    a.lmax = s_lmax;
+    a.leaves = (const uint8_t *const *)(d + o_leaf);
+    a.nleaf = s_nleaf;
     a.rstride = (uint32_t)rstride;
     a.ring = ring;
-    a.leaves = (const uint8_t *const *)(d + o_leaf);
-    a.nleaf = nleaf;
     a.nslot = nslot;
     a.tile = tile;
     a.tpp = tuned_tpp(prec, kact, tile);
@@ -907,8 +932,10 @@ struct cxgBatch {
     std::vector<Plan *> plans;
     DevBuf jobs, items, pmats, prefix, results;
     HostBuf out;
-    BatchArgs args;
-    unsigned grid = 0, nitems = 0;
+    // Jobs that stage their leaves and jobs that stream them run as two
+    // persistent launches (each walker is built for one of the two).
+    BatchArgs args[2];
+    unsigned grid[2] = {0, 0}, nitems = 0;
     uint32_t pmat_total = 0;
     double updates = 0.0, alg_bytes = 0.0;
     unsigned long long launches = 0;
@@ -933,19 +960,22 @@ static void free_batch(cxgBatch *b) {
 static int batch_enqueue(State &S, cxgBatch *b, cudaEvent_t e0 = nullptr,
                          cudaEvent_t e1 = nullptr) {
     const size_t n = b->plans.size();
-    CXG_CUDA(cudaMemsetAsync(b->results.p, 0, n * 32 + 16, S.stream));
+    CXG_CUDA(cudaMemsetAsync(b->results.p, 0, n * 32 + 32, S.stream));
     CXG_CUDA(launch_pmat_batch(static_cast<const PmatArgs *>(b->pmats.p),
                                static_cast<const uint32_t *>(b->prefix.p),
                                (uint32_t)n, b->pmat_total, S.stream));
     if (e0) CXG_CUDA(cudaEventRecord(e0, S.stream));
     if (!b->per_node) {
-        CXG_CUDA(launch_batch(b->prec, b->args, b->grid, S.stream));
+        for (int gi = 0; gi < 2; ++gi)
+            if (b->args[gi].nitems)
+                CXG_CUDA(launch_batch(b->prec, b->args[gi], b->grid[gi], S.stream));
     } else {
         // The plain comparison: one launch per node update.
         for (Plan *P : b->plans) {
             for (unsigned o = 0; o < P->nops; ++o) {
                 PlanArgs a = P->a;
                 a.rec = P->a.rec + (size_t)o * P->a.rstride;
+                a.lrows = P->a.lrows + (size_t)o * P->a.lmax;
                 a.nops = 1;
                 a.no_root = (o + 1 < P->nops) ? 1u : 0u;
                 a.root_last = (o + 1 < P->nops) ? 0u : P->a.root_last;
@@ -1008,7 +1038,7 @@ int cxgBatchCreate(CxtLik *const *liks, unsigned n, int precision,
     cxgBatch *b = new cxgBatch();
     b->prec = precision;
     b->per_node = (flags & CXG_BATCH_PER_NODE) != 0;
-    unsigned kact = 0, max_nslot = 0, max_nleaf = 0, max_rstride = 16;
+    unsigned kact = 0;
     for (unsigned j = 0; j < n; ++j) {
         Plan *P = new Plan();
         b->plans.push_back(P);
@@ -1024,16 +1054,13 @@ int cxgBatchCreate(CxtLik *const *liks, unsigned n, int precision,
                         "cxgBatchCreate: jobs must share the number of active "
                         "components (group them by K)");
         }
-        if (P->nslot > max_nslot) max_nslot = P->nslot;
-        if (P->nleaf > max_nleaf) max_nleaf = P->nleaf;
-        if (P->a.rstride > max_rstride) max_rstride = P->a.rstride;
         b->updates += P->updates;
         b->alg_bytes += P->alg_bytes;
         b->launches += P->nops;
     }
     // Per-job results live side by side: [ticket ninf err pad total] x n,
-    // then the work counter.
-    if ((rc = b->results.ensure((size_t)n * 32 + 16)) ||
+    // then the work counters of the two launches (16 bytes apart).
+    if ((rc = b->results.ensure((size_t)n * 32 + 32)) ||
         (rc = b->out.ensure((size_t)n * 32)) ||
         (rc = b->jobs.ensure((size_t)n * sizeof(PlanArgs))) ||
         (rc = b->pmats.ensure((size_t)n * sizeof(PmatArgs))) ||
@@ -1059,9 +1086,12 @@ int cxgBatchCreate(CxtLik *const *liks, unsigned n, int precision,
         prefix[j + 1] = prefix[j] + pm[j].nchild * pm[j].kact;
         for (unsigned t = 0; t < a.ntiles; ++t) items.push_back(WalkItem{j, t});
     }
-    // Longest jobs first, so the persistent grid ends together.
+    // Staged-leaf jobs first, then streamed ones (the two launches); each
+    // group longest jobs first, so its persistent grid ends together.
     std::stable_sort(items.begin(), items.end(),
                      [&](const WalkItem &x, const WalkItem &y) {
+                         const bool sx = jobs[x.job].lmax != 0, sy = jobs[y.job].lmax != 0;
+                         if (sx != sy) return sy;
                          return jobs[x.job].nops > jobs[y.job].nops;
                      });
     b->nitems = (unsigned)items.size();
@@ -1082,31 +1112,50 @@ int cxgBatchCreate(CxtLik *const *liks, unsigned n, int precision,
         free_batch(b);
         return cuda_fail(e, "cxgBatchCreate upload");
     }
-    BatchArgs &ba = b->args;
-    ba.jobs = static_cast<const PlanArgs *>(b->jobs.p);
-    ba.items = static_cast<const WalkItem *>(b->items.p);
-    ba.nitems = b->nitems;
-    ba.counter = (unsigned *)(res + (size_t)n * 32);
-    ba.tile = b->plans[0]->tile;
-    ba.tpp = b->plans[0]->tpp;
-    ba.ring = kRing;
-    ba.kact = kact;
-    ba.max_nslot = max_nslot;
-    ba.max_nleaf = max_nleaf;
-    ba.max_rstride = max_rstride;
+    unsigned nstaged = 0;
+    while (nstaged < items.size() && jobs[items[nstaged].job].lmax == 0) ++nstaged;
+    for (int gi = 0; gi < 2; ++gi) {
+        BatchArgs &ba = b->args[gi];
+        memset(&ba, 0, sizeof(ba));
+        const unsigned i0 = gi == 0 ? 0 : nstaged;
+        const unsigned i1 = gi == 0 ? nstaged : (unsigned)items.size();
+        ba.jobs = static_cast<const PlanArgs *>(b->jobs.p);
+        ba.items = static_cast<const WalkItem *>(b->items.p) + i0;
+        ba.nitems = i1 - i0;
+        ba.counter = (unsigned *)(res + (size_t)n * 32 + 16 * gi);
+        ba.tile = b->plans[0]->tile;
+        ba.tpp = b->plans[0]->tpp;
+        ba.ring = kRing;
+        ba.kact = kact;
+        ba.max_rstride = 16;
+        for (unsigned i = i0; i < i1; ++i) {
+            const PlanArgs &a = jobs[items[i].job];
+            ba.max_nslot = std::max(ba.max_nslot, a.nslot);
+            ba.max_rstride = std::max(ba.max_rstride, a.rstride);
+            ba.max_lmax = std::max(ba.max_lmax, a.lmax);
+            ba.max_nleaf = std::max(ba.max_nleaf, a.nleaf);
+        }
+    }
     if (!b->per_node) {
-        const size_t smem = plan_smem_bytes(precision, kact, ba.tile, max_nslot,
-                                            max_nleaf, kRing, max_rstride);
         int dev = 0, nsm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        const int per = batch_ctas_per_sm(precision, kact, ba.tile, ba.tpp, smem);
-        if (per <= 0 || nsm <= 0) {
-            free_batch(b);
-            return fail(CXG_EINVAL, "cxgBatchCreate: walker does not fit an SM");
+        b->launches = 0;
+        for (int gi = 0; gi < 2; ++gi) {
+            const BatchArgs &ba = b->args[gi];
+            if (ba.nitems == 0) continue;
+            const size_t smem =
+                plan_smem_bytes(precision, kact, ba.tile, ba.max_nslot, kRing,
+                                ba.max_rstride, ba.max_lmax, ba.max_nleaf);
+            const int per =
+                batch_ctas_per_sm(precision, kact, ba.tile, ba.tpp, gi == 0, smem);
+            if (per <= 0 || nsm <= 0) {
+                free_batch(b);
+                return fail(CXG_EINVAL, "cxgBatchCreate: walker does not fit an SM");
+            }
+            b->grid[gi] = (unsigned)(per * nsm);
+            b->launches += 1;
         }
-        b->grid = (unsigned)(per * nsm);
-        b->launches = 1;
         // Capture one run as a CUDA graph.
         if ((e = cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal)) !=
             cudaSuccess) {
@@ -1192,7 +1241,7 @@ int cxgBatchInfo(const cxgBatch *b, double *updates, double *alg_bytes,
     if (updates) *updates = b->updates;
     if (alg_bytes) *alg_bytes = b->alg_bytes;
     if (nitems) *nitems = b->nitems;
-    if (grid) *grid = b->grid;
+    if (grid) *grid = b->grid[0] + b->grid[1];
     if (launches_per_run) *launches_per_run = b->launches + 1;  // + P kernel
     return 0;
 }

@@ -92,7 +92,7 @@ struct Mc3Dev {
     Mc3Prop *prop;        // [c]
     PlanArgs *jobs;       // [c]
     unsigned char *rec;   // [c][M][rstride]
-    const uint8_t **leaves;  // [c][ntaxa]
+    const uint8_t **lrows;  // [c][M][3] leaf-child mask arrays of each op
     double *kid_len;      // [c][maxkids]
     uint64_t *kid_dst;    // [c][maxkids]
     int32_t *kid_tab;     // [c][maxkids]
@@ -110,6 +110,7 @@ struct Mc3Dev {
     uint64_t trace_cap;
     uint32_t *status;     // nonzero: a model could not be decomposed
     uint32_t nslot_cap;   // shared-memory stack slots of the walker
+    uint32_t staged;      // leaves staged per tile (else streamed)
 };
 
 // wNorm and the root weights of a model whose eigensystem and category
@@ -215,11 +216,10 @@ __device__ double ln_dirichlet(const double *alpha, const double *x, int n) {
 }
 
 // Shared memory of one chain's proposal: the tree (parent, child, len,
-// cur), dirty flags, DFS stack, dirty list, per-op prefixes of children
-// and leaf children, and the stack slot of each op and of each op's
-// children.
+// cur), dirty flags, DFS stack, dirty list, the per-op prefix of
+// children, and the stack slot of each op and of each op's children.
 __host__ __device__ inline size_t mc3_propose_smem(unsigned NN, unsigned M) {
-    return (size_t)NN * (8 + 4 + 12 + 4 + 1 + 1) + (size_t)M * 4 + (size_t)(M + 1) * 8 +
+    return (size_t)NN * (8 + 4 + 12 + 4 + 1 + 1) + (size_t)M * 4 + (size_t)(M + 1) * 4 +
            (size_t)M * 4 + 64;
 }
 
@@ -239,8 +239,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
     int32_t *stack = child + (size_t)NN * 3;
     int32_t *dirty = stack + NN;
     uint32_t *kid0 = reinterpret_cast<uint32_t *>(dirty + M);   // [M + 1]
-    uint32_t *leaf0 = kid0 + (M + 1);                           // [M + 1]
-    uint8_t *cur = reinterpret_cast<uint8_t *>(leaf0 + (M + 1));
+    uint8_t *cur = reinterpret_cast<uint8_t *>(kid0 + (M + 1));
     uint8_t *dflag = cur + NN;
     int8_t *op_slot = reinterpret_cast<int8_t *>(dflag + NN);   // [M]
     int8_t *kid_slot = op_slot + M;                             // [M][3]
@@ -527,21 +526,15 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         pr.ndirty = nd;
         for (int i = 0; i < nd; ++i) dflag[dirty[i]] = 1;
 
-        // Children and leaf children before each op (record layout).
-        unsigned nk = 0, nl = 0;
+        // Children before each op (record layout).
+        unsigned nk = 0;
         for (int o = 0; o < nd; ++o) {
             kid0[o] = nk;
-            leaf0[o] = nl;
             const int v = dirty[o];
-            for (int j = 0; j < 3; ++j) {
-                const int u = child[v * 3 + j];
-                if (u < 0) continue;
-                ++nk;
-                if (u < (int)N) ++nl;
-            }
+            for (int j = 0; j < 3; ++j)
+                if (child[v * 3 + j] >= 0) ++nk;
         }
         kid0[nd] = nk;
-        leaf0[nd] = nl;
         // Shared-memory stack slots, as the host planner assigns them: a
         // result keeps a slot until its one consumer (a later op of this
         // walk) reads it; with no free slot the oldest holder loses its
@@ -588,13 +581,12 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
     const int nd = s_nd;
     // Op records, one op per thread: parent -> its spare buffer; children
     // -> spare buffer if dirty (computed earlier in this walk), else
-    // current.  Leaf children take staged-leaf indices in op order (each
-    // leaf has one parent, so no leaf is staged twice).
+    // current.  A leaf child points at the leaf's mask array.
     const Mc3Model &mm = pr.model_changed ? d.model[c * 2 + (1 - d.curmodel[c])]
                                           : d.model[c * 2 + d.curmodel[c]];
     const size_t elt = d.prec == CXG_FP32 ? 4 : 8;
     unsigned char *rec = d.rec + (size_t)c * M * d.rstride;
-    const uint8_t **leaves = d.leaves + (size_t)c * N;
+    const uint8_t **lrows = d.lrows + (size_t)c * M * 3;
     double *klen = d.kid_len + (size_t)c * d.maxkids;
     uint64_t *kdst = d.kid_dst + (size_t)c * d.maxkids;
     int32_t *ktab = d.kid_tab + (size_t)c * d.maxkids;
@@ -611,16 +603,18 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         hd.flags = 0;
         hd.pad_ = 0;
         memcpy(r, &hd, sizeof(hd));
-        unsigned ci = 0, nkid = kid0[o], li = leaf0[o];
+        unsigned ci = 0, nkid = kid0[o], nl = 0;
+        const uint8_t **lr = lrows + (size_t)o * 3;
         for (int j = 0; j < 3; ++j) {
             const int u = child[v * 3 + j];
             if (u < 0) continue;
             RecChild ch;
             memset(&ch, 0, sizeof(ch));
             if (u < (int)N) {
-                leaves[li] = d.leafmask[u];
+                ch.data = d.leafmask[u];
+                ch.idx = (uint32_t)u;  // staged row (leaf u is taxon u)
+                lr[nl++] = d.leafmask[u];
                 ch.src = SRC_LEAF;
-                ch.idx = li++;
                 ch.tab = nkid;
                 ktab[nkid] = d.prec == CXG_FP64 ? (int32_t)nkid : -1;
             } else if (kid_slot[o * 3 + ci] >= 0) {
@@ -642,6 +636,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             ++nkid;
             ++ci;
         }
+        for (unsigned j = nl; j < 3; ++j) lr[j] = nullptr;
     }
     // The tree (moved) and the dirty list back to HBM.
     for (unsigned i = threadIdx.x; i < NN; i += blockDim.x) {
@@ -655,7 +650,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         d.nkids[c] = kid0[nd];
         PlanArgs &job = d.jobs[c];
         job.nops = (uint32_t)nd;
-        job.nleaf = leaf0[nd];
         job.pn = mm.pn;
     }
 }
@@ -905,15 +899,15 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     const unsigned tpp = tuned_tpp(cfg->precision, K, tile);
     d.ntiles = d.ppad / tile;
     {
-        // Stack slots within the tuned shared-memory budget, every leaf
-        // staged (the most a generation's walk stages).
+        // Leaves staged per tile when they fit, else streamed with the op
+        // records; stack slots within the tuned shared-memory budget.
+        d.staged = (size_t)N * tile <= kLeafStageBytes;
+        const unsigned lm = d.staged ? 0 : 3, nl = d.staged ? N : 0;
         const size_t base_b =
-            plan_smem_bytes(cfg->precision, K, tile, 0, 0, kRing, d.rstride);
+            plan_smem_bytes(cfg->precision, K, tile, 0, kRing, d.rstride, lm, nl);
         const size_t slot_b =
-            plan_smem_bytes(cfg->precision, K, tile, 1, 0, kRing, d.rstride) - base_b;
-        const size_t leaf_b =
-            plan_smem_bytes(cfg->precision, K, tile, 0, N, kRing, d.rstride);
-        size_t cap = budget > leaf_b ? (budget - leaf_b) / slot_b : 0;
+            plan_smem_bytes(cfg->precision, K, tile, 1, kRing, d.rstride, lm, nl) - base_b;
+        size_t cap = budget > base_b ? (budget - base_b) / slot_b : 0;
         d.nslot_cap = (uint32_t)(cap > kMaxSlots ? kMaxSlots : cap);
     }
     d.seed = cfg->seed;
@@ -986,8 +980,8 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
         (rc = mc3_upload<Mc3Prop>(h, &d.prop, nullptr, C)) ||
         (rc = mc3_upload<PlanArgs>(h, &d.jobs, nullptr, C)) ||
         (rc = mc3_upload<unsigned char>(h, &d.rec, nullptr, (size_t)C * M * d.rstride)) ||
-        (rc = mc3_upload<const uint8_t *>(h, (const uint8_t ***)&d.leaves, nullptr,
-                                          (size_t)C * N)) ||
+        (rc = mc3_upload<const uint8_t *>(h, (const uint8_t ***)&d.lrows, nullptr,
+                                          (size_t)C * M * 3)) ||
         (rc = mc3_upload<double>(h, &d.kid_len, nullptr, (size_t)C * d.maxkids)) ||
         (rc = mc3_upload<uint64_t>(h, &d.kid_dst, nullptr, (size_t)C * d.maxkids)) ||
         (rc = mc3_upload<int32_t>(h, &d.kid_tab, nullptr, (size_t)C * d.maxkids)) ||
@@ -1045,11 +1039,13 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
         PlanArgs a;
         memset(&a, 0, sizeof(a));
         a.rec = d.rec + (size_t)c * M * d.rstride;
-        a.leaves = d.leaves + (size_t)c * N;
+        a.lrows = d.lrows + (size_t)c * M * 3;
+        a.lmax = d.staged ? 0 : 3;
+        a.leaves = d.staged ? d.leafmask : nullptr;
+        a.nleaf = d.staged ? N : 0;
         a.rstride = d.rstride;
         a.ring = kRing;
         a.nops = 0;
-        a.nleaf = 0;
         a.nslot = d.nslot_cap;
         a.tile = tile;
         a.tpp = tpp;
@@ -1086,14 +1082,15 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     ba.ring = kRing;
     ba.kact = K;
     ba.max_nslot = d.nslot_cap;
-    ba.max_nleaf = N;
     ba.max_rstride = d.rstride;
-    const size_t smem = plan_smem_bytes(cfg->precision, K, tile, d.nslot_cap, N, kRing,
-                                        d.rstride);
+    ba.max_lmax = d.staged ? 0 : 3;
+    ba.max_nleaf = d.staged ? N : 0;
+    const size_t smem = plan_smem_bytes(cfg->precision, K, tile, d.nslot_cap, kRing,
+                                        d.rstride, ba.max_lmax, ba.max_nleaf);
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int per = batch_ctas_per_sm(cfg->precision, K, tile, tpp, smem);
+    const int per = batch_ctas_per_sm(cfg->precision, K, tile, tpp, d.staged != 0, smem);
     if (per <= 0) {
         mc3_free(h);
         return fail(CXG_EINVAL, "cxgMc3Create: walker does not fit an SM");

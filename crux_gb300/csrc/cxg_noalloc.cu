@@ -172,7 +172,7 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
 
     // Scratch layout (same offsets on host and device):
     //   misc 256 | records | elen | cmult | rmult | model | cube | eig | dst |
-    //   tab | pn | leaves | ltab | partial
+    //   tab | pn | leaf rows | ltab | partial
     const size_t o_misc = 0;
     const size_t o_rec = 256;
     const size_t o_elen = al16(o_rec + (size_t)(nops ? nops : 1) * rstride);
@@ -184,8 +184,11 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
     const size_t o_dst = al16(o_eig + nmod * 4 * 8);
     const size_t o_tab = al16(o_dst + (size_t)nkids * 8);
     const size_t o_pn = al16(o_tab + (size_t)nkids * 4);
-    const size_t o_leaf = al16(o_pn + kact * 4 * 8);
-    const size_t o_ltab = al16(o_leaf + (size_t)(nkids ? nkids : 1) * sizeof(void *));
+    // Leaf rows: up to maxdeg leaf children per op (lmax), null-terminated.
+    const unsigned lmax = maxdeg;
+    const size_t o_lrow = al16(o_pn + kact * 4 * 8);
+    const size_t o_ltab =
+        al16(o_lrow + (size_t)(nops ? nops : 1) * (lmax ? lmax : 1) * sizeof(void *));
     size_t ltab_bytes = 0;
     if (prec == CXG_FP64) {
         unsigned nleafkids = 0;
@@ -208,36 +211,30 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
     const unsigned nb = plan_blocks(ppad, tile);
     if (o_part + (size_t)nb * 16 > kNaScratchBytes)
         return fail(CXG_EINVAL, "cxgLikExecuteNoAlloc: scratch too small");
-    const size_t upload = o_ltab;  // host-packed prefix (misc..leaves)
+    const size_t upload = o_ltab;  // host-packed prefix (misc..root weights)
 
     unsigned char *h = g_na_host;
     memset(h, 0, upload);  // ticket, ninf, err and records start at zero
 
-    // Pass 2: records, children, leaves.  Each op's parent is the CxtLikCL
-    // of its Compute step; every pointer is the caller's device memory.
+    // Pass 2: records and children.  Each op's parent is the CxtLikCL of
+    // its Compute step; every pointer is the caller's device memory (a leaf
+    // child's cLMat is its mask array, read directly by the walker).
     const CxtLikCL *op_parent[kNaMaxOps];
     int op_slot[kNaMaxOps];
-    const void *leaf_ptr[kNaMaxKids];
-    unsigned nleaf = 0;
     // Shared-memory stack slots (LIFO, oldest holder loses its slot), as in
     // the allocating path.
-    const size_t base_b = plan_smem_bytes(prec, kact, tile, 0, 0, kRing,
-                                          (unsigned)rstride);
+    // (Leaves always stream here: no leaf table in the fixed scratch.)
+    const size_t base_b =
+        plan_smem_bytes(prec, kact, tile, 0, kRing, (unsigned)rstride, lmax, 0);
     const size_t slot_b =
-        plan_smem_bytes(prec, kact, tile, 1, 0, kRing, (unsigned)rstride) - base_b;
+        plan_smem_bytes(prec, kact, tile, 1, kRing, (unsigned)rstride, lmax, 0) - base_b;
+    const void **lrows = reinterpret_cast<const void **>(h + o_lrow);
     int owner[kMaxSlots];
     for (unsigned k = 0; k < kMaxSlots; ++k) owner[k] = -1;
     unsigned used = 0;
     unsigned o = 0, kid = 0, ntab = 0;
-    unsigned leaf_count_est = 0;
-    for (unsigned s = 0; s < lik->stepsLen; ++s)
-        if (lik->steps[s].variant == CxeLikStepComputeL ||
-            lik->steps[s].variant == CxeLikStepMergeL)
-            ++leaf_count_est;
-    const size_t leaf_b = plan_smem_bytes(prec, kact, tile, 0, leaf_count_est,
-                                          kRing, (unsigned)rstride);
     unsigned cap = 0;
-    if (budget > leaf_b) cap = (unsigned)((budget - leaf_b) / slot_b);
+    if (budget > base_b) cap = (unsigned)((budget - base_b) / slot_b);
     if (cap > kMaxSlots) cap = kMaxSlots;
     uint64_t *dsts = reinterpret_cast<uint64_t *>(h + o_dst);
     int32_t *tabs = reinterpret_cast<int32_t *>(h + o_tab);
@@ -264,12 +261,14 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
             ch.data = stp.childCL->cLMat;
             ch.scaler = stp.childCL->lnScale;
             if (leaf) {
-                unsigned li = 0;
-                while (li < nleaf && leaf_ptr[li] != (const void *)stp.childCL->cLMat)
-                    ++li;
-                if (li == nleaf) leaf_ptr[nleaf++] = stp.childCL->cLMat;
+                // Mask rows are copied in tile-sized pieces: 16-byte aligned.
+                if ((uintptr_t)stp.childCL->cLMat % 16)
+                    return fail(CXG_EINVAL, "leaf mask array not 16-byte aligned");
+                const void **lr = lrows + (size_t)o * lmax;
+                unsigned j = 0;
+                while (lr[j] != nullptr) ++j;
+                lr[j] = stp.childCL->cLMat;
                 ch.src = SRC_LEAF;
-                ch.idx = li;
                 ch.tab = prec == CXG_FP64 ? ntab : 0;
                 tabs[kid] = prec == CXG_FP64 ? (int32_t)ntab++ : -1;
             } else {
@@ -331,7 +330,6 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
         memcpy(h + o_cube + m * 64 * 8, models[m]->qEigVecCube, 64 * 8);
         memcpy(h + o_eig + m * 4 * 8, models[m]->qEigVals, 4 * 8);
     }
-    memcpy(h + o_leaf, leaf_ptr, (size_t)nleaf * sizeof(void *));
     const bool root_last =
         nops > 0 && op_parent[nops - 1] == lik->rootCLC;
 
@@ -360,11 +358,11 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
     PlanArgs a;
     memset(&a, 0, sizeof(a));
     a.rec = dev + o_rec;
-    a.leaves = reinterpret_cast<const uint8_t *const *>(dev + o_leaf);
+    a.lrows = reinterpret_cast<const uint8_t *const *>(dev + o_lrow);
+    a.lmax = lmax;
     a.rstride = (uint32_t)rstride;
     a.ring = kRing;
     a.nops = nops;
-    a.nleaf = nleaf;
     a.nslot = used;
     a.tile = tile;
     a.tpp = tpp;

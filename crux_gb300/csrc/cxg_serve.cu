@@ -103,19 +103,21 @@ struct HostKid {
 struct HostPlan {
     bool ready = false;
     unsigned K = 0, ppad = 0, ntiles = 0, nops = 0, nk = 0, nslot = 0, nhbm = 0;
-    unsigned tile = kTile, tpp = 1;
+    unsigned tile = kTile, tpp = 1, lmax = 0;
+    bool staged = false;  // leaves staged per tile (else streamed)
     size_t rstride = 0, job_bytes = 0, data_bytes = 0;
     std::vector<int> order, slot, hbm;
     std::vector<std::vector<HostKid>> kids;
 };
 
-// Patterns on the device: leaf masks, pattern weights and the leaf table.
+// Patterns on the device: leaf masks, pattern weights and the table of the
+// leaves' mask arrays (for jobs that stage their leaves).
 // A registered dataset also keeps its host copy (MC3 requests build their
 // chains from it) and a count of the admitted requests that use it.
 struct SrvDataset {
     uint8_t *masks = nullptr;      // [ntaxa][ppad]
     uint32_t *weights = nullptr;   // [npat]
-    const uint8_t **leaves = nullptr;  // [ntaxa]
+    const uint8_t **leaves = nullptr;  // [ntaxa] mask array of each taxon
     char *mem = nullptr;
     size_t bytes = 0;
     unsigned ntaxa = 0, npat = 0;
@@ -249,11 +251,21 @@ void plan_request(SrvRequest &rq, int prec) {
         std::reverse(P.order.begin(), P.order.end());  // children first
     }
     const unsigned nops = (unsigned)P.order.size();
-    const size_t base_b = plan_smem_bytes(prec, K, P.tile, 0, 0, kRing, (unsigned)P.rstride);
+    // Leaf children per op (each op's mask rows travel with its record).
+    P.lmax = 0;
+    for (int v : P.order) {
+        unsigned n = 0;
+        for (int j = 0; j < 3; ++j) n += (child[v * 3 + j] >= 0 && child[v * 3 + j] < (int)N);
+        if (n > P.lmax) P.lmax = n;
+    }
+    P.staged = (size_t)N * P.tile <= kLeafStageBytes;
+    const unsigned s_lmax = P.staged ? 0 : P.lmax, s_nleaf = P.staged ? N : 0;
+    const size_t base_b =
+        plan_smem_bytes(prec, K, P.tile, 0, kRing, (unsigned)P.rstride, s_lmax, s_nleaf);
     const size_t slot_b =
-        plan_smem_bytes(prec, K, P.tile, 1, 0, kRing, (unsigned)P.rstride) - base_b;
-    const size_t leaf_b = plan_smem_bytes(prec, K, P.tile, 0, N, kRing, (unsigned)P.rstride);
-    unsigned cap = budget > leaf_b ? (unsigned)((budget - leaf_b) / slot_b) : 0;
+        plan_smem_bytes(prec, K, P.tile, 1, kRing, (unsigned)P.rstride, s_lmax, s_nleaf) -
+        base_b;
+    unsigned cap = budget > base_b ? (unsigned)((budget - base_b) / slot_b) : 0;
     if (cap > kMaxSlots) cap = kMaxSlots;
     std::vector<int> owner(cap, -1), op_of(NN, -1);
     std::vector<char> need_hbm(nops, 0);
@@ -315,6 +327,7 @@ void plan_request(SrvRequest &rq, int prec) {
     b += al256((size_t)P.nhbm * K * 4 * P.ppad * elt);   // spilled CLs
     b += al256((size_t)P.nhbm * P.ppad * 8);             // their scalers
     b += al256((size_t)nops * P.rstride);                // records
+    b += al256((size_t)nops * (P.lmax ? P.lmax : 1) * 8);  // leaf rows
     b += al256(kids * (8 + 8 + 4));                      // lens, dsts, tabs
     b += al256((size_t)P.ntiles * 16);                   // partial sums
     b += al256(sizeof(SrvModel));
@@ -344,11 +357,11 @@ int upload_dataset(unsigned N, unsigned npat, const uint8_t *masks,
             dst[q] = v ? v : 15;
         }
     }
-    std::vector<const uint8_t *> hl(N);
-    for (unsigned t = 0; t < N; ++t) hl[t] = ds.masks + (size_t)t * ppad;
     CXG_CUDA(cudaMemcpyAsync(ds.masks, hm.data(), hm.size(), cudaMemcpyHostToDevice, s));
     CXG_CUDA(cudaMemcpyAsync(ds.weights, pfreqs, (size_t)npat * 4,
                              cudaMemcpyHostToDevice, s));
+    std::vector<const uint8_t *> hl(N);
+    for (unsigned t = 0; t < N; ++t) hl[t] = ds.masks + (size_t)t * ppad;
     CXG_CUDA(cudaMemcpyAsync(ds.leaves, hl.data(), N * sizeof(void *),
                              cudaMemcpyHostToDevice, s));
     return 0;
@@ -440,6 +453,8 @@ int prepare_job(cxgServer *S, SrvJob &J) {
     char *cls = take((size_t)P.nhbm * K * 4 * ppad * elt);
     char *scs = take((size_t)P.nhbm * ppad * 8);
     unsigned char *rec = (unsigned char *)take((size_t)P.nops * rstride);
+    const uint8_t **lrows =
+        (const uint8_t **)take((size_t)P.nops * (P.lmax ? P.lmax : 1) * sizeof(void *));
     char *kidarr = take((size_t)P.nk * (8 + 8 + 4));
     double *partial = (double *)take((size_t)P.ntiles * 16);
     SrvModel *model = (SrvModel *)take(sizeof(SrvModel));
@@ -450,6 +465,7 @@ int prepare_job(cxgServer *S, SrvJob &J) {
     auto cl_of = [&](int h) { return cls + (size_t)h * K * 4 * ppad * elt; };
     auto sc_of = [&](int h) { return scs + (size_t)h * ppad * 8; };
     std::vector<unsigned char> hrec((size_t)P.nops * rstride, 0);
+    std::vector<const uint8_t *> hlr((size_t)P.nops * (P.lmax ? P.lmax : 1), nullptr);
     std::vector<double> hlen(P.nk);
     std::vector<uint64_t> hdst(P.nk);
     std::vector<int32_t> htab(P.nk, -1);
@@ -474,7 +490,12 @@ int prepare_job(cxgServer *S, SrvJob &J) {
             memset(&ch, 0, sizeof(ch));
             ch.src = (uint32_t)k.src;
             if (k.src == SRC_LEAF) {
-                ch.idx = (uint32_t)k.idx;
+                ch.data = J.ds->masks + (size_t)k.idx * ppad;  // taxon's masks
+                ch.idx = (uint32_t)k.idx;                       // its staged row
+                const uint8_t **lr = hlr.data() + (size_t)o * P.lmax;
+                unsigned j = 0;
+                while (lr[j] != nullptr) ++j;
+                lr[j] = static_cast<const uint8_t *>(ch.data);
                 ch.tab = nk;
                 htab[nk] = prec == CXG_FP64 ? (int32_t)nk : -1;
                 if (prec != CXG_FP64) ch.tab = 0;
@@ -502,6 +523,8 @@ int prepare_job(cxgServer *S, SrvJob &J) {
     // the host vectors may go out of scope afterwards.
     cudaStream_t s = S->s_prep;
     CXG_CUDA(cudaMemcpyAsync(rec, hrec.data(), hrec.size(), cudaMemcpyHostToDevice, s));
+    CXG_CUDA(cudaMemcpyAsync(lrows, hlr.data(), hlr.size() * sizeof(void *),
+                             cudaMemcpyHostToDevice, s));
     CXG_CUDA(cudaMemcpyAsync(klen, hlen.data(), nk * 8, cudaMemcpyHostToDevice, s));
     CXG_CUDA(cudaMemcpyAsync(kdst, hdst.data(), nk * 8, cudaMemcpyHostToDevice, s));
     CXG_CUDA(cudaMemcpyAsync(ktab, htab.data(), nk * 4, cudaMemcpyHostToDevice, s));
@@ -512,11 +535,13 @@ int prepare_job(cxgServer *S, SrvJob &J) {
     PlanArgs &a = J.a;
     memset(&a, 0, sizeof(a));
     a.rec = rec;
-    a.leaves = J.ds->leaves;
+    a.lrows = lrows;
+    a.lmax = P.staged ? 0 : P.lmax;
+    a.leaves = P.staged ? J.ds->leaves : nullptr;
+    a.nleaf = P.staged ? N : 0;
     a.rstride = (uint32_t)rstride;
     a.ring = kRing;
     a.nops = P.nops;
-    a.nleaf = N;
     a.nslot = P.nslot;
     a.tile = P.tile;
     a.tpp = P.tpp;
@@ -558,7 +583,7 @@ int launch_batch_of(cxgServer *S, SrvBatch &B, cudaStream_t st) {
     std::vector<PmatArgs> pm(n);
     std::vector<uint32_t> prefix(n + 1, 0);
     std::vector<WalkItem> items;
-    unsigned max_nslot = 0, max_nleaf = 0, max_rstride = 16;
+    unsigned max_nslot = 0, max_rstride = 16, max_lmax = 0, max_nleaf = 0;
     size_t nitems = 0;
     for (size_t j = 0; j < n; ++j) nitems += B.jobs[j]->ntiles;
     const size_t o_jobs = 0, o_items = al256(n * sizeof(PlanArgs));
@@ -586,8 +611,9 @@ int launch_batch_of(cxgServer *S, SrvBatch &B, cudaStream_t st) {
         prefix[j + 1] = prefix[j] + J->nchild * J->kact;
         for (unsigned t = 0; t < J->ntiles; ++t) items.push_back(WalkItem{(uint32_t)j, t});
         max_nslot = std::max(max_nslot, a.nslot);
-        max_nleaf = std::max(max_nleaf, a.nleaf);
         max_rstride = std::max(max_rstride, a.rstride);
+        max_lmax = std::max(max_lmax, a.lmax);
+        max_nleaf = std::max(max_nleaf, a.nleaf);
     }
     std::stable_sort(items.begin(), items.end(), [&](const WalkItem &x, const WalkItem &y) {
         return jobs[x.job].nops > jobs[y.job].nops;
@@ -612,15 +638,16 @@ int launch_batch_of(cxgServer *S, SrvBatch &B, cudaStream_t st) {
     ba.ring = kRing;
     ba.kact = B.jobs[0]->kact;
     ba.max_nslot = max_nslot;
-    ba.max_nleaf = max_nleaf;
     ba.max_rstride = max_rstride;
+    ba.max_lmax = max_lmax;
+    ba.max_nleaf = max_nleaf;
     const int prec = S->cfg.precision;
-    const size_t smem = plan_smem_bytes(prec, ba.kact, ba.tile, max_nslot, max_nleaf,
-                                        kRing, max_rstride);
+    const size_t smem = plan_smem_bytes(prec, ba.kact, ba.tile, max_nslot,
+                                        kRing, max_rstride, max_lmax, max_nleaf);
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int per = batch_ctas_per_sm(prec, ba.kact, ba.tile, ba.tpp, smem);
+    const int per = batch_ctas_per_sm(prec, ba.kact, ba.tile, ba.tpp, max_lmax == 0, smem);
     if (per <= 0) return fail(CXG_EINVAL, "server: walker does not fit an SM");
     cudaError_t e = launch_batch(prec, ba, (unsigned)(per * nsm), st);
     if (e != cudaSuccess) return cuda_fail(e, "walk_batch_kernel (server)");
@@ -711,10 +738,11 @@ void lnl_loop(cxgServer *S) {
         if (!ready.empty() && inflight.size() < 2) {
             // A failed launch must give its slot back.
             // One launch per walker shape: components, tile, threads per
-            // pattern.
+            // pattern, staged or streamed leaves.
             std::map<unsigned, std::vector<SrvJob *>> byk;
             for (SrvJob *J : ready)
-                byk[J->kact | J->a.tile << 8 | J->a.tpp << 16].push_back(J);
+                byk[J->kact | J->a.tile << 8 | J->a.tpp << 16 | (J->a.lmax ? 1u : 0u) << 24]
+                    .push_back(J);
             ready.clear();
             for (auto &kv : byk) {
                 SrvBatch B;

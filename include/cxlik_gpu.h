@@ -369,7 +369,8 @@ int cxgTuneGet(unsigned *tile, unsigned *threads_per_pattern,
  *     precision (double or float) laid out [kact][U][ppad] in 16-byte
  *     units, lnScale -> ppad scalers (double for CXG_FP64, int32 for
  *     CXG_FP32; size the buffer for 8 bytes per pattern); leaf CL: cLMat
- *     -> ppad uint8 state masks (pad patterns set to 15), lnScale unused;
+ *     -> ppad uint8 state masks (pad patterns set to 15; 16-byte aligned, as
+ *     cudaMalloc returns), lnScale unused;
  *   - dFreqs: mschars uint32 pattern weights on the device;
  *   - dSiteLnL: optional device output of mschars site lnLs (NULL: none);
  *   - stream: the caller's cudaStream_t (NULL: the default stream).
