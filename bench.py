@@ -673,6 +673,53 @@ def run_dirty(args, dist):
     dist.close()
 
 
+COMPACT = {"workload": "compact_simulated_gtr_gamma4",
+           "shapes": [[128, 100000], [1024, 200000]], "mean_brlen": 0.05,
+           "gap_frac": 0.005, "seed": 20261209}
+
+
+def run_compact(args, dist):
+    """Pattern compression (Alignment.compact) of simulated alignments:
+    sites/s of the GPU path (cxgCompact, host arrays in and out) against
+    the host restatement, with the outputs compared bit for bit."""
+    import numpy as np
+    from crux_gb300 import _native, synth
+    from crux_gb300 import compact as gc
+    from crux_gb300.alignment import Alignment, CTMatrix
+    gpu = _native.load()
+    out = []
+    for ntaxa, nsites in COMPACT["shapes"]:
+        case = synth.Case(ntaxa, nsites, COMPACT["mean_brlen"], COMPACT["seed"],
+                          gap_frac=COMPACT["gap_frac"])
+        raw = Alignment(CTMatrix(case.fasta))
+        for _ in range(max(args.warmup, 1)):
+            gc.compact(raw, gpu)
+        reps = max(1, args.steps // 4)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            rows, freqs, masks = gc.compact(raw, gpu)
+        g_s = (time.perf_counter() - t0) / reps
+        h = Alignment(CTMatrix(case.fasta))
+        t0 = time.perf_counter()
+        h.compact()
+        h_s = time.perf_counter() - t0
+        out.append({"ntaxa": ntaxa, "nsites": nsites, "patterns": int(len(freqs)),
+                    "gpu_s": g_s, "host_s": h_s,
+                    "gpu_sites_per_s": nsites / g_s, "host_sites_per_s": nsites / h_s,
+                    "bit_exact": bool(np.array_equal(rows, h.rows) and
+                                      np.array_equal(freqs, h.freqs))})
+    line = {
+        "metric": "pattern compression sites/s (GPU, host arrays in and out)",
+        "value": out[-1]["gpu_sites_per_s"], "unit": "sites/s", "n_gpus": 1,
+        "steps": max(1, args.steps // 4), "warmup": max(args.warmup, 1),
+        "ms_per_step": 1e3 * out[-1]["gpu_s"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (seeded)", "config": dict(COMPACT), "shapes": out,
+    }
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
 SERVE = {"workload": "serve_poisson_logu_taxa8-1024_sites200-200000",
          "datasets": 40, "taxa": [8, 1024], "sites": [200, 200000],
          "pinv_prob": 0.3, "mc3_prob": 0.2, "mc3_gens": 10,
@@ -812,7 +859,7 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="FP32 plan only, no e2e/CPU legs (for ncu)")
     ap.add_argument("--workload", default="tree128",
-                    choices=["tree128", "batch256", "mc3", "mc3small", "dirty64",
+                    choices=["tree128", "batch256", "mc3", "mc3small", "dirty64", "compact",
                              "serve"])
     ap.add_argument("--rates", type=float, nargs="*", default=None,
                     help="serve: arrival rates (requests/s) to sweep")
@@ -834,6 +881,8 @@ def main():
         run_serve(args, dist)
     elif args.workload == "dirty64":
         run_dirty(args, dist)
+    elif args.workload == "compact":
+        run_compact(args, dist)
     else:
         run_ours(args, dist)
 

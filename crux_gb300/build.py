@@ -15,7 +15,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libcxlik_gpu.so")
 SOURCES = ["cxg_kernels.cu", "cxg_lik.cu", "cxg_noalloc.cu", "cxg_mc3.cu",
-           "cxg_serve.cu"]
+           "cxg_serve.cu", "cxg_compact.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O3", "-I" + os.path.join(ROOT, "include"),

@@ -348,6 +348,20 @@ int cxgServerStats(cxgServer *server, cxgServerStatsT *stats);
 int cxgServerResetStats(cxgServer *server);
 int cxgServerDestroy(cxgServer *server);
 
+/* Pattern compression on the device (Alignment.compact,
+ * pkg/Crux/CTMatrix.pyx:949-1031, after canonize :856-887): the sorted
+ * unique columns of rows [ntaxa][nsites] (character codes) with summed
+ * frequencies (freqs NULL: 1 per site), bit-exact with the host algorithm:
+ * characters map through canon[256], columns order bytewise, identical
+ * columns merge.  Writes rows_out [ntaxa][npat] (canonical codes; may be
+ * NULL), freqs_out [npat], and when masks_out is given the leaf-tip
+ * encoding masks_out [ntaxa][npat] = val[code] & 15, 0 -> any_mask
+ * (Lik.pyx:1466-1475).  Output arrays need room for nsites patterns. */
+int cxgCompact(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
+               const uint32_t *freqs, const uint8_t *canon, const uint8_t *val,
+               uint8_t any_mask, uint8_t *rows_out, uint32_t *freqs_out,
+               uint8_t *masks_out, unsigned *npat);
+
 /* Launch shape of the plan walker for plans translated from now on:
  * patterns per CTA (32, 64 or 128), threads per pattern (1, 2 or 4: the
  * FP32 form splits a pattern's components over that many threads when the
