@@ -162,6 +162,18 @@ struct BatchArgs {
 size_t plan_smem_bytes(int precision, unsigned kact, unsigned tile, unsigned nslot,
                        unsigned ring, unsigned rstride, unsigned lmax,
                        unsigned nleaf);
+// Pattern compression on the device (cxg_compact.cu): scratch bytes, and
+// the compaction of rows [ntaxa][nsites] (device) into rows_out / masks
+// (row strides rstride / mstride; mask pad patterns up to mstride get
+// any_mask), freq_out and *npat_dev (device).  canon_host is the host copy
+// of the device table canon.  Waits for the stream once.
+size_t compact_work_bytes(unsigned ntaxa, unsigned nsites);
+int compact_device(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
+                   const uint32_t *freq_in, const uint8_t *canon_host, const uint8_t *canon,
+                   const uint8_t *val, uint8_t any_mask, uint8_t *rows_out, unsigned rstride,
+                   uint8_t *masks, unsigned mstride, uint32_t *freq_out, uint32_t *npat_dev,
+                   void *work, size_t work_bytes, cudaStream_t s);
+
 // Largest staged leaf rows per CTA: jobs whose leaves take more stream
 // them with their records instead.
 constexpr size_t kLeafStageBytes = 16 * 1024;

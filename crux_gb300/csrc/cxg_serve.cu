@@ -118,6 +118,7 @@ struct SrvDataset {
     uint8_t *masks = nullptr;      // [ntaxa][ppad]
     uint32_t *weights = nullptr;   // [npat]
     const uint8_t **leaves = nullptr;  // [ntaxa] mask array of each taxon
+    size_t stride = 0;  // mask row stride (>= the padded pattern count)
     char *mem = nullptr;
     size_t bytes = 0;
     unsigned ntaxa = 0, npat = 0;
@@ -344,6 +345,7 @@ int upload_dataset(unsigned N, unsigned npat, const uint8_t *masks,
     ds.bytes = dataset_bytes(N, npat);
     ds.ntaxa = N;
     ds.npat = npat;
+    ds.stride = ppad;
     CXG_CUDA(cudaMallocAsync((void **)&ds.mem, ds.bytes, s));
     ds.masks = (uint8_t *)ds.mem;
     ds.weights = (uint32_t *)(ds.mem + al256((size_t)N * ppad));
@@ -490,7 +492,7 @@ int prepare_job(cxgServer *S, SrvJob &J) {
             memset(&ch, 0, sizeof(ch));
             ch.src = (uint32_t)k.src;
             if (k.src == SRC_LEAF) {
-                ch.data = J.ds->masks + (size_t)k.idx * ppad;  // taxon's masks
+                ch.data = J.ds->masks + (size_t)k.idx * J.ds->stride;  // taxon's masks
                 ch.idx = (uint32_t)k.idx;                       // its staged row
                 const uint8_t **lr = hlr.data() + (size_t)o * P.lmax;
                 unsigned j = 0;
@@ -1033,6 +1035,93 @@ extern "C" int cxgServerAddDataset(cxgServer *S, unsigned long long id, unsigned
         if (ds->mem) cudaFree(ds->mem);
         return rc;
     }
+    std::lock_guard<std::mutex> g(S->mu);
+    S->bytes_in_use += ds->bytes;
+    S->bytes_peak = std::max(S->bytes_peak, S->bytes_in_use);
+    S->datasets[id] = ds.release();
+    return 0;
+}
+
+extern "C" int cxgServerAddDatasetRaw(cxgServer *S, unsigned long long id, unsigned ntaxa,
+                                      unsigned nsites, const uint8_t *rows,
+                                      const uint8_t *canon, const uint8_t *val,
+                                      uint8_t any_mask, unsigned *npat) {
+    if (S == nullptr || rows == nullptr || canon == nullptr || val == nullptr ||
+        npat == nullptr || id == 0)
+        return fail(CXG_EINVAL, "cxgServerAddDatasetRaw: NULL or zero id");
+    if (ntaxa < 3 || nsites == 0)
+        return fail(CXG_EINVAL, "cxgServerAddDatasetRaw: bad shape");
+    {
+        std::lock_guard<std::mutex> g(S->mu);
+        if (S->datasets.count(id)) return fail(CXG_EINVAL, "cxgServerAddDatasetRaw: id in use");
+    }
+    // The dataset keeps masks with row stride pad(nsites) >= pad(npat)
+    // (pad patterns are "any"), weights and the leaf table; the raw rows
+    // and the compaction scratch are freed afterwards.
+    const unsigned N = ntaxa;
+    const size_t stride = pad_patterns(nsites);
+    auto ds = std::make_unique<SrvDataset>();
+    ds->bytes = al256((size_t)N * stride) + al256((size_t)nsites * 4) +
+                al256((size_t)N * sizeof(void *));
+    ds->ntaxa = N;
+    ds->stride = stride;
+    cudaStream_t s = S->s_prep;
+    const size_t work = compact_work_bytes(N, nsites);
+    const size_t in_bytes = (size_t)N * nsites;
+    char *tmp = nullptr;
+    int rc = 0;
+    cudaError_t e = cudaMallocAsync((void **)&ds->mem, ds->bytes, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&tmp, al256(in_bytes) + 1024 + 256 + work, s);
+    if (e != cudaSuccess) {
+        if (ds->mem) cudaFreeAsync(ds->mem, s);
+        cudaStreamSynchronize(s);
+        return cuda_fail(e, "cxgServerAddDatasetRaw: device memory");
+    }
+    ds->masks = (uint8_t *)ds->mem;
+    ds->weights = (uint32_t *)(ds->mem + al256((size_t)N * stride));
+    ds->leaves = (const uint8_t **)(ds->mem + al256((size_t)N * stride) +
+                                    al256((size_t)nsites * 4));
+    uint8_t *d_rows = (uint8_t *)tmp;
+    uint8_t *d_tab = (uint8_t *)tmp + al256(in_bytes);       // canon | val
+    uint32_t *d_np = (uint32_t *)(d_tab + 512 + 256);
+    void *d_work = tmp + al256(in_bytes) + 1024 + 256;
+    uint8_t tabs[512];
+    memcpy(tabs, canon, 256);
+    memcpy(tabs + 256, val, 256);
+    std::vector<const uint8_t *> hl(N);
+    for (unsigned t = 0; t < N; ++t) hl[t] = ds->masks + (size_t)t * stride;
+    uint32_t np = 0;
+    if ((e = cudaMemcpyAsync(d_rows, rows, in_bytes, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(d_tab, tabs, 512, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(ds->leaves, hl.data(), N * sizeof(void *),
+                             cudaMemcpyHostToDevice, s)))
+        rc = cuda_fail(e, "cxgServerAddDatasetRaw: upload");
+    if (rc == 0)
+        rc = compact_device(d_rows, N, nsites, nullptr, canon, d_tab, d_tab + 256, any_mask,
+                            nullptr, 0, ds->masks, (unsigned)stride, ds->weights, d_np,
+                            d_work, work, s);
+    if (rc == 0 && ((e = cudaMemcpyAsync(&np, d_np, 4, cudaMemcpyDeviceToHost, s)) ||
+                    (e = cudaStreamSynchronize(s))))
+        rc = cuda_fail(e, "cxgServerAddDatasetRaw: pattern count");
+    if (rc == 0) {
+        // Host copies for MC3 sessions built on this dataset.
+        ds->npat = np;
+        ds->hmasks.resize((size_t)N * np);
+        ds->hfreqs.resize(np);
+        if ((e = cudaMemcpy2DAsync(ds->hmasks.data(), np, ds->masks, stride, np, N,
+                                   cudaMemcpyDeviceToHost, s)) ||
+            (e = cudaMemcpyAsync(ds->hfreqs.data(), ds->weights, (size_t)np * 4,
+                                 cudaMemcpyDeviceToHost, s)) ||
+            (e = cudaStreamSynchronize(s)))
+            rc = cuda_fail(e, "cxgServerAddDatasetRaw: host copy");
+    }
+    cudaFreeAsync(tmp, s);
+    if (rc) {
+        cudaFreeAsync(ds->mem, s);
+        cudaStreamSynchronize(s);
+        return rc;
+    }
+    *npat = np;
     std::lock_guard<std::mutex> g(S->mu);
     S->bytes_in_use += ds->bytes;
     S->bytes_peak = std::max(S->bytes_peak, S->bytes_in_use);

@@ -71,6 +71,10 @@ def declare(lib):
                                         ctypes.c_uint, P(ctypes.c_uint8),
                                         P(ctypes.c_uint32)]
     lib.cxgServerAddDataset.restype = ctypes.c_int
+    lib.cxgServerAddDatasetRaw.argtypes = [
+        vp, ctypes.c_ulonglong, ctypes.c_uint, ctypes.c_uint, P(ctypes.c_uint8),
+        P(ctypes.c_uint8), P(ctypes.c_uint8), ctypes.c_uint8, P(ctypes.c_uint)]
+    lib.cxgServerAddDatasetRaw.restype = ctypes.c_int
     lib.cxgServerDropDataset.argtypes = [vp, ctypes.c_ulonglong]
     lib.cxgServerDropDataset.restype = ctypes.c_int
     lib.cxgServerStats.argtypes = [vp, P(ServerStats)]
@@ -157,6 +161,26 @@ class Server:
         if rc != 0:
             raise RuntimeError("cxgServerAddDataset: %s"
                                % self.lib.cxgLastError().decode())
+
+    def add_dataset_raw(self, ident, alignment):
+        """Keep a raw (uncompacted) alignment's patterns on the device under
+        `ident`; the server compacts it there.  Returns the pattern count
+        (that of Alignment.compact, in the same order)."""
+        ch = alignment.charType.get()
+        rows = np.ascontiguousarray(alignment.rows, dtype=np.uint8)
+        canon = np.ascontiguousarray(ch.canon_table, dtype=np.uint8)
+        val = np.ascontiguousarray(np.where(ch.val_table < 0, 0, ch.val_table),
+                                   dtype=np.uint8)
+        u8 = ctypes.POINTER(ctypes.c_uint8)
+        npat = ctypes.c_uint()
+        rc = self.lib.cxgServerAddDatasetRaw(
+            self.h, ident, rows.shape[0], rows.shape[1],
+            rows.ctypes.data_as(u8), canon.ctypes.data_as(u8),
+            val.ctypes.data_as(u8), ch.any, ctypes.byref(npat))
+        if rc != 0:
+            raise RuntimeError("cxgServerAddDatasetRaw: %s"
+                               % self.lib.cxgLastError().decode())
+        return npat.value
 
     def drop_dataset(self, ident):
         rc = self.lib.cxgServerDropDataset(self.h, ident)

@@ -344,6 +344,14 @@ int cxgServerAddDataset(cxgServer *server, unsigned long long id,
                         unsigned ntaxa, unsigned npat, const uint8_t *masks,
                         const uint32_t *pattern_freqs);
 int cxgServerDropDataset(cxgServer *server, unsigned long long id);
+/* The same from a raw alignment rows [ntaxa][nsites] (character codes):
+ * the server compacts it on the device (as cxgCompact: canon, val and
+ * any_mask of the character type) and keeps the patterns resident without
+ * a host round trip; *npat receives the pattern count requests must use. */
+int cxgServerAddDatasetRaw(cxgServer *server, unsigned long long id,
+                           unsigned ntaxa, unsigned nsites, const uint8_t *rows,
+                           const uint8_t *canon, const uint8_t *val,
+                           uint8_t any_mask, unsigned *npat);
 int cxgServerStats(cxgServer *server, cxgServerStatsT *stats);
 int cxgServerResetStats(cxgServer *server);
 int cxgServerDestroy(cxgServer *server);

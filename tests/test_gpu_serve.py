@@ -110,3 +110,28 @@ def test_resident_dataset(gpu, port):
     assert st["completed"] == 4 * len(reqs)
     for i, r in enumerate(reqs):
         assert vals[3 * i] == vals[3 * i + 1] == vals[3 * i + 2] == own[i]
+
+
+def test_raw_dataset_compacted_on_device(gpu):
+    """A raw alignment registered with add_dataset_raw is compacted on the
+    device into the same patterns, in the same order, as the host's
+    Alignment.compact: requests on it equal requests on the host-compacted
+    dataset bit for bit, lnL and MC3 steps alike."""
+    from crux_gb300.alignment import Alignment, CTMatrix
+    case = synth.Case(30, 4000, 0.1, 77, gap_frac=0.01)
+    host = PreparedRequest(case, LNL)
+    srv = Server("fp32")
+    srv.add_dataset(1, host)
+    npat = srv.add_dataset_raw(2, Alignment(CTMatrix(case.fasta)))
+    assert npat == host.req.npat
+    a = PreparedRequest(case, LNL, alignment=host.alignment, dataset=1)
+    b = PreparedRequest(case, LNL, alignment=host.alignment, dataset=2)
+    va, vb = srv.wait(srv.submit(a))[0], srv.wait(srv.submit(b))[0]
+    ma = PreparedRequest(case, MC3, alignment=host.alignment, dataset=1,
+                         mc3_gens=5, mc3_chains=2, seed=3)
+    mb = PreparedRequest(case, MC3, alignment=host.alignment, dataset=2,
+                         mc3_gens=5, mc3_chains=2, seed=3)
+    la, lb = srv.wait(srv.submit(ma))[0], srv.wait(srv.submit(mb))[0]
+    srv.close()
+    assert va == vb
+    assert la == lb
