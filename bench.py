@@ -88,16 +88,21 @@ class Clocks:
     def __init__(self):
         self.proc = None
         self.out = None
+        self.path = None
 
     def start(self):
+        import tempfile
+        fd, self.path = tempfile.mkstemp(prefix="crux_gb300_clocks_", suffix=".csv")
+        self.out = os.fdopen(fd, "w")
         try:
-            self.out = open(os.path.join(ROOT, "_clocks.tmp"), "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader",
                  "-lms", "100"], stdout=self.out, stderr=subprocess.DEVNULL)
             time.sleep(0.3)
         except OSError:
             self.proc = None
+            self.out.close()
+            os.unlink(self.path)
 
     def stop(self):
         if self.proc is None:
@@ -108,9 +113,8 @@ class Clocks:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.out.close()
-        path = os.path.join(ROOT, "_clocks.tmp")
-        rows = [r.split(",") for r in open(path).read().splitlines() if r.strip()]
-        os.unlink(path)
+        rows = [r.split(",") for r in open(self.path).read().splitlines() if r.strip()]
+        os.unlink(self.path)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
                  "sw_power_cap"]
