@@ -11,8 +11,11 @@ namespace cxg {
 
 // P(t) = max(0, sum_k cube[i][j][k] exp(lambda_k t)) for child c and
 // component k of idx = c * kact + k (CxLik.c:258-292), FP64, stored into
-// the op record as the plan's precision; FP64 plans also get the 16-row
-// leaf message table of a leaf child.
+// the op record as the plan's precision.  A leaf child (tab >= 0) gets its
+// message table instead: row mask = sum over the allowed states j of
+// P[i][j], in j order (P times the reference's 0/1 row, CxLik.c:357-374
+// with Lik.pyx:1466-1475), in the FP64 table for FP64 plans and in the
+// record, rounded once to FP32, for FP32 plans.
 __device__ inline void pmat_one(const PmatArgs &a, unsigned idx) {
     const unsigned c = idx / a.kact, k = idx % a.kact;
     const int m = a.model[k];
@@ -38,6 +41,21 @@ __device__ inline void pmat_one(const PmatArgs &a, unsigned idx) {
         }
     }
     const int tb = a.tab[c];
+    unsigned char *dst = a.rec + a.dst[c];
+    if (tb >= 0 && a.precision == CXG_FP32) {
+        float *o = reinterpret_cast<float *>(dst);
+        for (int mask = 0; mask < 16; ++mask) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                double acc = 0.0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (mask & (1 << j)) acc = __dadd_rn(acc, P[i * 4 + j]);
+                o[((size_t)mask * a.kact + k) * 4 + i] = (float)acc;
+            }
+        }
+        return;
+    }
     if (tb >= 0) {
         // Message of a leaf with state mask m: the sum over allowed states j
         // of P[i][j], in j order -- exactly P times the reference's 0/1 row.
@@ -53,7 +71,6 @@ __device__ inline void pmat_one(const PmatArgs &a, unsigned idx) {
             }
         }
     }
-    unsigned char *dst = a.rec + a.dst[c];
     if (a.precision == CXG_FP32) {
         float *o = reinterpret_cast<float *>(dst) + (size_t)k * 16;
 #pragma unroll

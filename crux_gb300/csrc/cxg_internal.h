@@ -46,9 +46,12 @@ enum : uint32_t {
 // fixed-stride record (rstride bytes, a multiple of 16), so that a CTA can
 // stream the records into shared memory with bulk copies ahead of use:
 //
-//   RecHead | RecChild[nchild] | T P[nchild][kact][16]
+//   RecHead | RecChild[nchild] | one area per child, at RecChild.off
 //
-// The P matrices are filled in place by the P-matrix kernel of each run.
+// A child's area is filled in place by the P-matrix kernel of each run:
+// the P matrices T P[kact][16], or for a leaf child of an FP32 plan its
+// message table float[16 masks][kact][4] (the message P x indicator(mask)
+// of every state mask, summed in FP64 and rounded once).
 struct RecHead {
     void *data;        // parent CL in HBM, [K][U][ppad] 16-byte units
     void *scaler;      // parent scaler [ppad]
@@ -72,8 +75,15 @@ struct RecChild {
     uint32_t src;
     uint32_t idx;
     uint32_t tab;      // FP64 plans: leaf-message table of this child
-    uint32_t pad_;
+    uint32_t off;      // byte offset of the child's area in the record
 };
+
+// Bytes of a child's area in an op record.
+__host__ __device__ inline size_t child_area_bytes(int precision, unsigned kact,
+                                                   bool leaf) {
+    if (precision == CXG_FP32 && leaf) return (size_t)16 * kact * 4 * 4;
+    return (size_t)kact * 16 * (precision == CXG_FP32 ? 4 : 8);
+}
 
 static_assert(sizeof(RecHead) == 32, "record header is 32 bytes");
 static_assert(sizeof(RecChild) == 32, "record child is 32 bytes");
@@ -197,7 +207,8 @@ struct PmatArgs {
     const double *cube;        // [nmodels][64]
     const double *eig;         // [nmodels][4]
     const uint64_t *dst;       // [nchild] byte offsets from rec
-    const int32_t *tab;        // [nchild] leaf table index (FP64) or -1
+    const int32_t *tab;        // [nchild] leaf child: FP64 table index (FP32:
+                               // any value >= 0, the table goes in the record); -1
     double wnorm;
     const double *wnorm_dev;   // if set, wNorm is read here (model built on the GPU)
     unsigned char *rec;

@@ -430,13 +430,12 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
         const RecHead *hd = reinterpret_cast<const RecHead *>(rec);
         const RecChild *kids = reinterpret_cast<const RecChild *>(rec + sizeof(RecHead));
         const unsigned nchild = hd->nchild;
-        const T *pmats = reinterpret_cast<const T *>(rec + sizeof(RecHead) +
-                                                     nchild * sizeof(RecChild));
         T sc = T(0);  // plain form: max over child messages
         lns = S(0);
         for (unsigned ci = 0; ci < nchild; ++ci) {
             const RecChild ch = kids[ci];
-            const V *P = reinterpret_cast<const V *>(pmats + ((size_t)ci * KA + k0) * 16);
+            const T *area = reinterpret_cast<const T *>(rec + ch.off);
+            const V *P = reinterpret_cast<const V *>(area + (size_t)k0 * 16);
             T msg[KT * 4];
             const bool leaf = (ch.src == SRC_LEAF);
             const bool in_slot = (ch.src == SRC_SLOT);
@@ -449,7 +448,18 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             const V *xs = in_slot ? slots + ((size_t)ch.idx * KA + k0) * U * tile + pl
                                   : static_cast<const V *>(ch.data) + (size_t)k0 * U * ppad + p;
             const size_t stride = in_slot ? tile : ppad;
-            if (sizeof(T) == 8 && leaf) {
+            if (sizeof(T) == 4 && leaf) {
+                // FP32 leaves: the message of mask m from the record's table.
+                const float4 *t = reinterpret_cast<const float4 *>(area) + (size_t)m * KA + k0;
+#pragma unroll
+                for (int k = 0; k < KT; ++k) {
+                    const float4 v = t[k];
+                    msg[k * 4 + 0] = (T)v.x;
+                    msg[k * 4 + 1] = (T)v.y;
+                    msg[k * 4 + 2] = (T)v.z;
+                    msg[k * 4 + 3] = (T)v.w;
+                }
+            } else if (sizeof(T) == 8 && leaf) {
                 // FP64 leaves: table lookup (no FP64 arithmetic).
                 const double2 *t = reinterpret_cast<const double2 *>(
                     a.ltab + (((size_t)ch.tab * 16 + m) * KA + k0) * 4);

@@ -375,7 +375,9 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
         ch.scaler = leaf ? nullptr : cc->scaler;
         ch.src = leaf ? SRC_LEAF : SRC_GLOBAL;
         ch.idx = 0;
-        ch.tab = (leaf && prec == CXG_FP64) ? ntab++ : -1;
+        // Leaf children: an FP64 table index, or (FP32) >= 0 for the table
+        // in the record.
+        ch.tab = leaf ? (prec == CXG_FP64 ? ntab++ : 0) : -1;
         kids.push_back(ch);
         kid_cl.push_back(cc);
         elen.push_back(st.edgeLen);
@@ -436,11 +438,12 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     // Shared-memory stack: a parent keeps a slot until its one consumer (a
     // later op of this run) reads it; with no free slot the oldest holder
     // loses its slot and its consumer reads the HBM copy instead.
-    // Record stride: the largest op's header, children and P matrices.
-    const size_t elt = prec == CXG_FP32 ? 4 : 8;
+    // Record stride: the largest op's header, children and child areas.
     size_t rstride = 16;
     for (const HostOp &op : ops) {
-        size_t b = sizeof(RecHead) + op.nchild * (sizeof(RecChild) + kact * 16 * elt);
+        size_t b = sizeof(RecHead) + op.nchild * sizeof(RecChild);
+        for (uint32_t c = op.child0; c < op.child0 + op.nchild; ++c)
+            b += child_area_bytes(prec, kact, kids[c].src == SRC_LEAF);
         b = (b + 15) & ~(size_t)15;
         if (b > rstride) rstride = b;
     }
@@ -546,8 +549,12 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
         hd.nchild = ops[o].nchild;
         hd.slot = ops[o].slot;
         memcpy(r, &hd, sizeof(hd));
+        size_t area = sizeof(RecHead) + ops[o].nchild * sizeof(RecChild);
         for (uint32_t ci = 0; ci < ops[o].nchild; ++ci) {
             const HostChild &k = kids[ops[o].child0 + ci];
+            const size_t ab = child_area_bytes(prec, kact, k.src == SRC_LEAF);
+            if (area + ab > rstride)
+                return fail(CXG_EINVAL, "internal: child area outside its record");
             RecChild rc_;
             memset(&rc_, 0, sizeof(rc_));
             rc_.data = k.data;
@@ -555,14 +562,11 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
             rc_.src = k.src;
             rc_.idx = k.idx;
             rc_.tab = k.tab < 0 ? 0u : (uint32_t)k.tab;
+            rc_.off = (uint32_t)area;
             memcpy(r + sizeof(RecHead) + ci * sizeof(RecChild), &rc_, sizeof(rc_));
             // Byte offset from the start of the records (pa.rec).
-            const size_t off = o * rstride + sizeof(RecHead) +
-                               ops[o].nchild * sizeof(RecChild) +
-                               ci * kact * 16 * elt;
-            if (off + kact * 16 * elt > (o + 1) * rstride)
-                return fail(CXG_EINVAL, "internal: P matrix outside its record");
-            dsts[ops[o].child0 + ci] = off;
+            dsts[ops[o].child0 + ci] = o * rstride + area;
+            area += ab;
         }
     }
     if (!elen.empty()) memcpy(h + o_elen, elen.data(), elen.size() * 8);

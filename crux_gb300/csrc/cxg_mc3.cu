@@ -35,6 +35,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -584,7 +585,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
     // current.  A leaf child points at the leaf's mask array.
     const Mc3Model &mm = pr.model_changed ? d.model[c * 2 + (1 - d.curmodel[c])]
                                           : d.model[c * 2 + d.curmodel[c]];
-    const size_t elt = d.prec == CXG_FP32 ? 4 : 8;
     unsigned char *rec = d.rec + (size_t)c * M * d.rstride;
     const uint8_t **lrows = d.lrows + (size_t)c * M * 3;
     double *klen = d.kid_len + (size_t)c * d.maxkids;
@@ -604,6 +604,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         hd.pad_ = 0;
         memcpy(r, &hd, sizeof(hd));
         unsigned ci = 0, nkid = kid0[o], nl = 0;
+        size_t area = sizeof(RecHead) + nch * sizeof(RecChild);
         const uint8_t **lr = lrows + (size_t)o * 3;
         for (int j = 0; j < 3; ++j) {
             const int u = child[v * 3 + j];
@@ -616,7 +617,8 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 lr[nl++] = d.leafmask[u];
                 ch.src = SRC_LEAF;
                 ch.tab = nkid;
-                ktab[nkid] = d.prec == CXG_FP64 ? (int32_t)nkid : -1;
+                // FP64: table index; FP32: >= 0, the table goes in the record.
+                ktab[nkid] = (int32_t)nkid;
             } else if (kid_slot[o * 3 + ci] >= 0) {
                 ch.src = SRC_SLOT;
                 ch.idx = (uint32_t)kid_slot[o * 3 + ci];
@@ -629,10 +631,11 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 ch.src = SRC_GLOBAL;
                 ktab[nkid] = -1;
             }
+            ch.off = (uint32_t)area;
             memcpy(r + sizeof(RecHead) + ci * sizeof(RecChild), &ch, sizeof(ch));
             klen[nkid] = len[u];
-            kdst[nkid] = (size_t)o * d.rstride + sizeof(RecHead) +
-                         nch * sizeof(RecChild) + ci * d.kact * 16 * elt;
+            kdst[nkid] = (size_t)o * d.rstride + area;
+            area += child_area_bytes((int)d.prec, d.kact, u < (int)N);
             ++nkid;
             ++ci;
         }
@@ -891,7 +894,11 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     d.M = M;
     d.maxkids = NN;  // children over all internal nodes: NN - 1
     const size_t elt = cfg->precision == CXG_FP32 ? 4 : 8;
-    d.rstride = (uint32_t)((sizeof(RecHead) + 3 * (sizeof(RecChild) + K * 16 * elt) + 15) &
+    d.rstride = (uint32_t)((sizeof(RecHead) +
+                            3 * (sizeof(RecChild) +
+                                 std::max(child_area_bytes(cfg->precision, K, true),
+                                          child_area_bytes(cfg->precision, K, false))) +
+                            15) &
                            ~(size_t)15);
     unsigned tile = 0, tpp_q = 1;
     size_t budget = 0;

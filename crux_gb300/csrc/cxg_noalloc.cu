@@ -27,6 +27,8 @@
 // or on several streams, race on it; a mutex serialises calls from this
 // process up to the point where the result has been read back.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <math.h>
 #include <string.h>
 
@@ -93,7 +95,6 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
         return fail(CXG_EINVAL, "cxgLikExecuteNoAlloc: patterns must be 1..2^20");
     const unsigned ppad = pad_patterns(npat);
     const int prec = precision;
-    const size_t elt = prec == CXG_FP32 ? 4 : 8;
     unsigned char *dev = nullptr;
     int rc = na_setup(&dev);
     if (rc) return rc;
@@ -161,9 +162,13 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
         lik->rootCLC->lnScale == nullptr)
         return fail(CXG_EINVAL, "rootCLC without device buffers");
 
+    // Record stride: the largest op, every child taking the larger area
+    // (an FP32 leaf's message table or a P matrix).
     size_t rstride = 16;
     {
-        size_t b = sizeof(RecHead) + maxdeg * (sizeof(RecChild) + kact * 16 * elt);
+        const size_t area = std::max(child_area_bytes(prec, kact, true),
+                                     child_area_bytes(prec, kact, false));
+        size_t b = sizeof(RecHead) + maxdeg * (sizeof(RecChild) + area);
         b = al16(b);
         if (b > rstride) rstride = b;
     }
@@ -252,6 +257,7 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
         hd.scaler = par->lnScale;
         hd.nchild = n;
         hd.slot = -1;
+        size_t area = sizeof(RecHead) + n * sizeof(RecChild);
         for (unsigned ci = 0; ci < n; ++ci, ++kid) {
             const CxtLikStep &stp = lik->steps[s + ci];
             const bool leaf = stp.variant == CxeLikStepComputeL ||
@@ -270,7 +276,7 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
                 lr[j] = stp.childCL->cLMat;
                 ch.src = SRC_LEAF;
                 ch.tab = prec == CXG_FP64 ? ntab : 0;
-                tabs[kid] = prec == CXG_FP64 ? (int32_t)ntab++ : -1;
+                tabs[kid] = prec == CXG_FP64 ? (int32_t)ntab++ : 0;
             } else {
                 if (stp.childCL->lnScale == nullptr)
                     return fail(CXG_EINVAL, "internal child without scaler buffer");
@@ -288,12 +294,14 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
                     break;
                 }
             }
+            const size_t ab = child_area_bytes(prec, kact, leaf);
+            if (area + ab > rstride)
+                return fail(CXG_EINVAL, "internal: child area outside its record");
+            ch.off = (uint32_t)area;
             memcpy(r + sizeof(RecHead) + ci * sizeof(RecChild), &ch, sizeof(ch));
             // Byte offset from the start of the records (pa.rec).
-            dsts[kid] = (size_t)o * rstride + sizeof(RecHead) +
-                        n * sizeof(RecChild) + ci * kact * 16 * elt;
-            if (dsts[kid] + kact * 16 * elt > (size_t)(o + 1) * rstride)
-                return fail(CXG_EINVAL, "internal: P matrix outside its record");
+            dsts[kid] = (size_t)o * rstride + area;
+            area += ab;
             elens[kid] = stp.edgeLen;
         }
         op_parent[o] = par;

@@ -232,7 +232,12 @@ void plan_request(SrvRequest &rq, int prec) {
     P.ntiles = P.ppad / P.tile;
     const size_t elt = prec == CXG_FP32 ? 4 : 8;
     const unsigned K = P.K;
-    P.rstride = (sizeof(RecHead) + 3 * (sizeof(RecChild) + K * 16 * elt) + 15) & ~(size_t)15;
+    // Record stride: up to three children, each with the larger area (an
+    // FP32 leaf's message table or a P matrix).
+    P.rstride = (sizeof(RecHead) +
+                 3 * (sizeof(RecChild) + std::max(child_area_bytes(prec, K, true),
+                                                  child_area_bytes(prec, K, false))) +
+                 15) & ~(size_t)15;
     std::vector<int32_t> child(NN * 3, -1);
     std::vector<int> nch(NN, 0);
     for (unsigned v = 0; v < NN; ++v) {
@@ -374,7 +379,10 @@ size_t mc3_bytes(const cxgRequest &r, int prec, unsigned nc) {
     const size_t elt = prec == CXG_FP32 ? 4 : 8;
     const size_t ppad = pad_patterns(r.npat), N = r.ntaxa, M = N - 2;
     const size_t K = r.ncat;
-    const size_t rstride = sizeof(RecHead) + 3 * (sizeof(RecChild) + K * 16 * elt) + 16;
+    const size_t rstride =
+        sizeof(RecHead) + 3 * (sizeof(RecChild) + std::max(child_area_bytes(prec, K, true),
+                                                           child_area_bytes(prec, K, false))) +
+        16;
     return nc * (2 * M * (K * 4 * ppad * elt + ppad * 8) + M * rstride) +
            N * ppad + ((size_t)4 << 20);
 }
@@ -486,11 +494,13 @@ int prepare_job(cxgServer *S, SrvJob &J) {
             hd.flags = REC_NO_HBM;
         }
         memcpy(rr, &hd, sizeof(hd));
+        size_t area = sizeof(RecHead) + nch * sizeof(RecChild);
         for (unsigned ci = 0; ci < nch; ++ci) {
             const HostKid &k = P.kids[o][ci];
             RecChild ch;
             memset(&ch, 0, sizeof(ch));
             ch.src = (uint32_t)k.src;
+            ch.off = (uint32_t)area;
             if (k.src == SRC_LEAF) {
                 ch.data = J.ds->masks + (size_t)k.idx * J.ds->stride;  // taxon's masks
                 ch.idx = (uint32_t)k.idx;                       // its staged row
@@ -498,9 +508,8 @@ int prepare_job(cxgServer *S, SrvJob &J) {
                 unsigned j = 0;
                 while (lr[j] != nullptr) ++j;
                 lr[j] = static_cast<const uint8_t *>(ch.data);
-                ch.tab = nk;
-                htab[nk] = prec == CXG_FP64 ? (int32_t)nk : -1;
-                if (prec != CXG_FP64) ch.tab = 0;
+                ch.tab = prec == CXG_FP64 ? nk : 0;
+                htab[nk] = prec == CXG_FP64 ? (int32_t)nk : 0;
             } else if (k.src == SRC_SLOT) {
                 ch.idx = (uint32_t)k.idx;
             } else {
@@ -509,8 +518,8 @@ int prepare_job(cxgServer *S, SrvJob &J) {
             }
             memcpy(rr + sizeof(RecHead) + ci * sizeof(RecChild), &ch, sizeof(ch));
             hlen[nk] = J.rq->len[k.node];
-            hdst[nk] = (size_t)o * rstride + sizeof(RecHead) + nch * sizeof(RecChild) +
-                       ci * K * 16 * elt;
+            hdst[nk] = (size_t)o * rstride + area;
+            area += child_area_bytes(prec, K, k.src == SRC_LEAF);
             ++nk;
         }
     }
