@@ -162,14 +162,14 @@ def profile_traffic(name):
 
 
 def autotune(lib, prec, args, lik=None, liks=None):
-    """Pick the walker's launch shape (tile, threads per pattern, stack
-    budget) by timing the candidates on this workload; ``--shape`` fixes it
+    """Pick the walker's launch shape (tile, threads per pattern, patterns
+    per thread, stack budget) by timing the candidates on this workload; ``--shape`` fixes it
     instead.  Returns the shape with how it was chosen."""
     from crux_gb300 import tune
     if args.shape:
         tune.set_shape(lib, *args.shape)
-        t, g, b = args.shape
-        return {"tile": t, "tpp": g, "budget": b, "source": "--shape"}
+        t, g, p, b = args.shape
+        return {"tile": t, "tpp": g, "ppt": p, "budget": b, "source": "--shape"}
     if liks is not None:
         r = tune.tune_batch(liks, prec, iters=3,
                             shapes=tune.candidates(
@@ -181,7 +181,9 @@ def autotune(lib, prec, args, lik=None, liks=None):
     top = sorted(r["table"], key=lambda x: x["ms"])
     per_tpp = {}
     for x in top:
-        per_tpp.setdefault(str(x["tpp"]), [x["tile"], x["budget"], x["ms"]])
+        per_tpp.setdefault(str(x["tpp"]) if x["ppt"] == 1 else
+                           "%d/ppt%d" % (x["tpp"], x["ppt"]),
+                           [x["tile"], x["budget"], x["ms"]])
     best.update(source="autotuned", candidates=len(r["table"]),
                 worst_ms=top[-1]["ms"], best_per_tpp=per_tpp)
     return best
@@ -282,7 +284,7 @@ def run_ours(args, dist):
     # End to end through the public API: full re-plan + lnL each run, with
     # the FP32 form's tuned shape.
     sh = res["fp32"]["shape"]
-    tune.set_shape(gpu, sh["tile"], sh["tpp"], sh["budget"])
+    tune.set_shape(gpu, sh["tile"], sh["tpp"], sh["ppt"], sh["budget"])
     lik = res["fp32"]["lik"]
     for _ in range(max(args.warmup, 3)):
         lik.lik.invalidate = True
@@ -853,7 +855,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--shape", type=lambda v: tuple(int(x) for x in v.split(",")),
                     default=None,
-                    help="walker shape tile,threads_per_pattern,stack_bytes "
+                    help="walker shape tile,threads_per_pattern,"
+                         "patterns_per_thread,stack_bytes "
                          "instead of autotuning")
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU baseline and the oracle check")

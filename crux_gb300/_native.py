@@ -53,11 +53,13 @@ def declare(lib):
     lib.cxgPlanInfo.restype = c_int
     lib.cxgPlanDestroy.argtypes = [vp]
     lib.cxgPlanDestroy.restype = c_int
-    lib.cxgPlanShape.argtypes = [vp, P(c_uint), P(c_uint), P(c_uint), P(c_uint)]
+    lib.cxgPlanShape.argtypes = [vp, P(c_uint), P(c_uint), P(c_uint), P(c_uint),
+                                 P(c_uint)]
     lib.cxgPlanShape.restype = c_int
-    lib.cxgTune.argtypes = [c_uint, c_uint, ctypes.c_size_t]
+    lib.cxgTune.argtypes = [c_uint, c_uint, c_uint, ctypes.c_size_t]
     lib.cxgTune.restype = c_int
-    lib.cxgTuneGet.argtypes = [P(c_uint), P(c_uint), P(ctypes.c_size_t)]
+    lib.cxgTuneGet.argtypes = [P(c_uint), P(c_uint), P(c_uint),
+                               P(ctypes.c_size_t)]
     lib.cxgTuneGet.restype = c_int
     lib.cxgLikExecuteNoAlloc.argtypes = [P(_abi.CxtLik), c_int,
                                          P(ctypes.c_uint32), P(c_double),

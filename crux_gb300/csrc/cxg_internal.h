@@ -129,11 +129,18 @@ struct PlanArgs {
     uint32_t no_root;     // 1: stop after the ops (per-node launches)
     uint32_t tpp;         // threads per pattern (each holds kact / tpp
                           // components); 0 is read as 1
+    uint32_t ppt;         // patterns per thread (1 or 2); 0 is read as 1
 };
 
-// Threads per pattern a walker is built for with `kact` components: 1 for
-// every shape; 2 and 4 for the FP32 form when they divide kact.
-inline bool walker_shape_ok(int precision, unsigned kact, unsigned tpp) {
+// Threads per pattern and patterns per thread a walker is built for with
+// `kact` components: one of each for every shape; 2 or 4 threads per
+// pattern for the FP32 form when they divide kact; 2 patterns per thread
+// for the FP32 form with one thread per pattern and at most 5 components.
+inline bool walker_shape_ok(int precision, unsigned kact, unsigned tpp,
+                            unsigned ppt = 1) {
+    if (ppt == 2)
+        return precision == CXG_FP32 && tpp == 1 && kact >= 1 && kact <= 5;
+    if (ppt != 1) return false;
     if (tpp == 1) return kact >= 1 && kact <= kMaxComps;
     if (precision != CXG_FP32 || (tpp != 2 && tpp != 4)) return false;
     return kact % tpp == 0 && kact / tpp <= (tpp == 2 ? 4u : 2u);
@@ -142,11 +149,22 @@ inline bool walker_shape_ok(int precision, unsigned kact, unsigned tpp) {
 // Threads per pattern for a new plan: the tuned value where the walker is
 // built for it (walker_shape_ok, tile x tpp <= kMaxThreads), else 1.
 inline unsigned tuned_tpp(int precision, unsigned kact, unsigned tile) {
-    unsigned t = 0, tpp = 1;
+    unsigned t = 0, tpp = 1, ppt = 1;
     size_t b = 0;
-    cxgTuneGet(&t, &tpp, &b);
+    cxgTuneGet(&t, &tpp, &ppt, &b);
     if (!walker_shape_ok(precision, kact, tpp) || tile * tpp > kMaxThreads) tpp = 1;
     return tpp;
+}
+
+// Patterns per thread for a new plan with `tpp` threads per pattern: the
+// tuned value where the walker is built for it (and the tile keeps at
+// least one warp), else 1.
+inline unsigned tuned_ppt(int precision, unsigned kact, unsigned tile, unsigned tpp) {
+    unsigned t = 0, tq = 1, ppt = 1;
+    size_t b = 0;
+    cxgTuneGet(&t, &tq, &ppt, &b);
+    if (!walker_shape_ok(precision, kact, tpp, ppt) || tile / ppt < 32) ppt = 1;
+    return ppt;
 }
 
 // One (job, tile) work item of a batched launch.
@@ -167,6 +185,7 @@ struct BatchArgs {
     uint32_t tile, ring, kact;
     uint32_t max_nslot, max_rstride, max_lmax, max_nleaf;
     uint32_t tpp;         // threads per pattern (all jobs); 0 is read as 1
+    uint32_t ppt;         // patterns per thread (all jobs); 0 is read as 1
 };
 
 size_t plan_smem_bytes(int precision, unsigned kact, unsigned tile, unsigned nslot,
@@ -191,7 +210,7 @@ cudaError_t launch_batch(int precision, const BatchArgs &b, unsigned grid,
                          cudaStream_t s);
 // Resident CTAs per SM of the batched walker for this shape.
 int batch_ctas_per_sm(int precision, unsigned kact, unsigned tile,
-                      unsigned tpp, bool staged, size_t smem);
+                      unsigned tpp, unsigned ppt, bool staged, size_t smem);
 
 // Inputs of the P-matrix kernel: one thread per (child, active comp); the
 // P matrix (FP64 arithmetic, stored as the plan's precision) goes into the

@@ -93,25 +93,33 @@ __device__ __forceinline__ Comp warp_comp(Comp v) {
     return v;
 }
 
-// Tile sum of `v` (finite values; -inf sites are counted separately) into
-// a.partial[tile]; the last tile of the job to finish folds all of the job's
-// partials into a.total.
-__device__ void reduce_sites(const PlanArgs &a, unsigned tile_idx, double v,
-                             bool neg_inf) {
-    __shared__ Comp warp_part[kMaxThreads / 32];
+// Tile sum of site values (finite values; -inf sites are counted
+// separately) into a.partial[tile]; the last tile of the job to finish
+// folds all of the job's partials into a.total.  Thread t holds the values
+// of patterns t + h * blockDim (h < NV): every group of 32 consecutive
+// patterns reduces by the same shuffle tree and the groups add in pattern
+// order, and warp 0 alone folds the partials, so the sums do not depend
+// on the launch shape.
+template <int NV>
+__device__ void reduce_sites_n(const PlanArgs &a, unsigned tile_idx, const double *v,
+                               const bool *neg_inf) {
+    __shared__ Comp warp_part[2 * kMaxThreads / 32];
     __shared__ unsigned ninf_block;
     __shared__ bool last;
     const unsigned nwarp = blockDim.x / 32;
     if (threadIdx.x == 0) ninf_block = 0;
     __syncthreads();
-    if (neg_inf) atomicAdd(&ninf_block, 1u);
-    Comp c = warp_comp(Comp{v, 0.0});
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) warp_part[warp] = c;
+#pragma unroll
+    for (int h = 0; h < NV; ++h) {
+        if (neg_inf[h]) atomicAdd(&ninf_block, 1u);
+        const Comp c = warp_comp(Comp{v[h], 0.0});
+        if (lane == 0) warp_part[h * nwarp + warp] = c;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         Comp b = warp_part[0];
-        for (unsigned w = 1; w < nwarp; ++w) b = comp_add(b, warp_part[w]);
+        for (unsigned w = 1; w < NV * nwarp; ++w) b = comp_add(b, warp_part[w]);
         a.partial[2 * tile_idx] = b.s;
         a.partial[2 * tile_idx + 1] = b.c;
         if (ninf_block) atomicAdd(a.ninf, ninf_block);
@@ -120,26 +128,26 @@ __device__ void reduce_sites(const PlanArgs &a, unsigned tile_idx, double v,
         last = (t == a.ntiles - 1);
     }
     __syncthreads();
-    if (last) {
+    if (last && warp == 0) {
         __threadfence();
         Comp acc{0.0, 0.0};
-        for (unsigned b = threadIdx.x; b < a.ntiles; b += blockDim.x) {
+        for (unsigned b = lane; b < a.ntiles; b += 32) {
             const volatile double *pp = a.partial;
             acc = comp_add(acc, Comp{pp[2 * b], pp[2 * b + 1]});
         }
         acc = warp_comp(acc);
-        __syncthreads();
-        if (lane == 0) warp_part[warp] = acc;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            Comp b = warp_part[0];
-            for (unsigned w = 1; w < nwarp; ++w) b = comp_add(b, warp_part[w]);
-            a.total[0] = b.s;
-            a.total[1] = b.c;
+        if (lane == 0) {
+            a.total[0] = acc.s;
+            a.total[1] = acc.c;
             *a.ticket = 0;  // ready for the next launch
         }
     }
     __syncthreads();  // warp_part / last are reused by the next item
+}
+
+__device__ __forceinline__ void reduce_sites(const PlanArgs &a, unsigned tile_idx, double v,
+                                             bool neg_inf) {
+    reduce_sites_n<1>(a, tile_idx, &v, &neg_inf);
 }
 
 // ---------------------------------------------------------------------------
@@ -634,6 +642,230 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
     return true;
 }
 
+// The FP32 walker with two patterns per thread (one thread per pattern
+// pair, components not split): thread t owns patterns t and t + blockDim
+// of the tile, so loads stay coalesced, and every P row, record field and
+// loop step serves both.  The arithmetic of each pattern is that of
+// walk_tile<float, K, 1, STAGED>, and the tile reduction runs in its order,
+// so the bits are the same.
+template <int K, bool STAGED>
+__device__ bool walk_tile2(const PlanArgs &a, unsigned tile_idx, const SmemLayout &Lay,
+                           unsigned ring_depth, uint32_t &phase) {
+    typedef float T;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int s_ok;
+    const unsigned nthr = blockDim.x;
+    const unsigned tile = 2 * nthr;
+    const unsigned tid = threadIdx.x;
+    const unsigned pl[2] = {tid, tid + nthr};
+    const unsigned p[2] = {tile_idx * tile + tid, tile_idx * tile + tid + nthr};
+    const size_t ppad = a.ppad;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + Lay.bars);
+    unsigned char *ring = smem + Lay.ring;
+    float4 *slots = reinterpret_cast<float4 *>(smem + Lay.slots);
+    int *slot_sc = reinterpret_cast<int *>(smem + Lay.slot_sc);
+    const size_t sstride = STAGED ? (size_t)a.rstride : Lay.stage;
+    uint8_t *masks = smem + Lay.masks;
+    const unsigned R = ring_depth;
+
+    if (STAGED) {
+        if (tid == 0) {
+            fence_proxy_async();
+            for (unsigned o = 0; o < R && o < a.nops; ++o) {
+                mbar_expect_tx(&bars[o], a.rstride);
+                bulk_g2s(ring + (size_t)o * a.rstride, a.rec + (size_t)o * a.rstride,
+                         a.rstride, &bars[o]);
+            }
+        }
+        const unsigned chunks = tile / 16;
+        for (unsigned i = tid; i < a.nleaf * chunks; i += nthr) {
+            const unsigned l = i / chunks, c = i % chunks;
+            const uint4 *src =
+                reinterpret_cast<const uint4 *>(a.leaves[l] + (size_t)tile_idx * tile) + c;
+            reinterpret_cast<uint4 *>(masks + (size_t)l * tile)[c] = __ldg(src);
+        }
+        __syncthreads();
+    } else {
+        if (tid == 0)
+            for (unsigned o = 0; o < R && o < a.nops; ++o) {
+                const uint8_t *rows0[kLeafPre];
+                read_rows(a, o, rows0);
+                issue_stage(a, o, ring + (size_t)o * sstride, &bars[o], tile_idx, tile, rows0);
+            }
+    }
+
+    T acc[2][K * 4];
+    int lns[2] = {0, 0};
+    for (unsigned o = 0; o < a.nops; ++o) {
+        const unsigned stage = o % R;
+        const uint8_t *pre[kLeafPre] = {nullptr, nullptr, nullptr, nullptr};
+        if (!STAGED && tid == 0 && o + R < a.nops) read_rows(a, o + R, pre);
+        if (tid == 0) {
+            const uint32_t par = (phase >> stage) & 1u;
+            s_ok = mbar_wait_bounded(&bars[stage], par);
+            phase ^= 1u << stage;
+        }
+        __syncthreads();
+        if (!s_ok) {
+            if (tid == 0) atomicOr(a.err, 1u);
+            return false;  // all threads leave together
+        }
+        const unsigned char *rec = ring + (size_t)stage * sstride;
+        const uint8_t *lrow = rec + a.rstride;
+        unsigned nlk = 0;
+        const RecHead *hd = reinterpret_cast<const RecHead *>(rec);
+        const RecChild *kids = reinterpret_cast<const RecChild *>(rec + sizeof(RecHead));
+        const unsigned nchild = hd->nchild;
+        lns[0] = lns[1] = 0;
+        for (unsigned ci = 0; ci < nchild; ++ci) {
+            const RecChild ch = kids[ci];
+            const float *area = reinterpret_cast<const float *>(rec + ch.off);
+            T msg[2][K * 4];
+            if (ch.src == SRC_LEAF) {
+                unsigned m[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    m[h] = STAGED ? masks[(size_t)ch.idx * tile + pl[h]]
+                                  : lrow[(size_t)nlk * tile + pl[h]];
+                if (!STAGED) ++nlk;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const float4 *t = reinterpret_cast<const float4 *>(area) + (size_t)m[h] * K;
+#pragma unroll
+                    for (int k = 0; k < K; ++k) {
+                        const float4 v = t[k];
+                        msg[h][k * 4 + 0] = v.x;
+                        msg[h][k * 4 + 1] = v.y;
+                        msg[h][k * 4 + 2] = v.z;
+                        msg[h][k * 4 + 3] = v.w;
+                    }
+                }
+            } else {
+                const bool in_slot = (ch.src == SRC_SLOT);
+                const float4 *P = reinterpret_cast<const float4 *>(area);
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    float x[2][4];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const float4 v =
+                            in_slot ? slots[((size_t)ch.idx * K + k) * tile + pl[h]]
+                                    : static_cast<const float4 *>(ch.data)[(size_t)k * ppad + p[h]];
+                        unpack(v, x[h]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        float r[4];
+                        unpack(P[k * 4 + i], r);
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            float v = r[0] * x[h][0];
+                            v = fmaf(r[1], x[h][1], v);
+                            v = fmaf(r[2], x[h][2], v);
+                            v = fmaf(r[3], x[h][3], v);
+                            msg[h][k * 4 + i] = v;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    lns[h] += in_slot ? slot_sc[(size_t)ch.idx * tile + pl[h]]
+                                      : static_cast<const int *>(ch.scaler)[p[h]];
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (ci == 0) {
+#pragma unroll
+                    for (int q = 0; q < K * 4; ++q) acc[h][q] = msg[h][q];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < K * 4; ++q) acc[h][q] *= msg[h][q];
+                }
+            }
+        }
+        void *ydata = hd->data;
+        void *yscaler = hd->scaler;
+        const int yslot = hd->slot;
+        const bool yhbm = !(hd->flags & REC_NO_HBM);
+        __syncthreads();
+        if (tid == 0 && o + R < a.nops) {
+            if (STAGED) {
+                fence_proxy_async();
+                mbar_expect_tx(&bars[stage], a.rstride);
+                bulk_g2s(ring + (size_t)stage * a.rstride,
+                         a.rec + (size_t)(o + R) * a.rstride, a.rstride, &bars[stage]);
+            } else {
+                issue_stage(a, o + R, ring + (size_t)stage * sstride, &bars[stage], tile_idx,
+                            tile, pre);
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            T mx = T(0);
+#pragma unroll
+            for (int q = 0; q < K * 4; ++q) mx = fmax(mx, acc[h][q]);
+            if (mx > T(0) && mx <= (T)3.0e38) {
+                int e;
+                frexpf(mx, &e);
+                const int n = -e;
+                if (n >= -126 && n <= 127) {
+                    const float s1 = pow2f(n);
+#pragma unroll
+                    for (int q = 0; q < K * 4; ++q) acc[h][q] *= s1;
+                } else {
+                    const int n1 = n / 2, n2 = n - n1;
+                    const float s1 = pow2f(n1), s2 = pow2f(n2);
+#pragma unroll
+                    for (int q = 0; q < K * 4; ++q) acc[h][q] = (acc[h][q] * s1) * s2;
+                }
+                lns[h] += e;
+            }
+            if (yhbm) {
+                float4 *y = static_cast<float4 *>(ydata) + p[h];
+#pragma unroll
+                for (int k = 0; k < K; ++k) y[(size_t)k * ppad] = pack4(acc[h] + k * 4);
+                static_cast<int *>(yscaler)[p[h]] = lns[h];
+            }
+            if (yslot >= 0) {
+                float4 *ys = slots + (size_t)yslot * K * tile + pl[h];
+#pragma unroll
+                for (int k = 0; k < K; ++k) ys[(size_t)k * tile] = pack4(acc[h] + k * 4);
+                slot_sc[(size_t)yslot * tile + pl[h]] = lns[h];
+            }
+        }
+    }
+
+    if (a.no_root) {
+        __syncthreads();
+        return true;
+    }
+    double v[2] = {0.0, 0.0};
+    bool ninf[2] = {false, false};
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        if (!a.root_last) {
+            const float4 *r = static_cast<const float4 *>(a.root) + p[h];
+#pragma unroll
+            for (int k = 0; k < K; ++k) unpack(r[(size_t)k * ppad], acc[h] + k * 4);
+            lns[h] = static_cast<const int *>(a.rootsc)[p[h]];
+        }
+        double L = 0.0;
+#pragma unroll
+        for (int q = 0; q < K * 4; ++q) L = fma(__ldg(a.pn + q), (double)acc[h][q], L);
+        if (p[h] < a.npat) {
+            v[h] = (log(L) + (double)lns[h] * 0.69314718055994530942) * (double)a.freqs[p[h]];
+            if (isnan(v[h])) v[h] = -INFINITY;
+            if (a.site) a.site[p[h]] = v[h];
+            if (isinf(v[h])) {
+                ninf[h] = (v[h] < 0.0);
+                v[h] = 0.0;
+            }
+        }
+    }
+    reduce_sites_n<2>(a, tile_idx, v, ninf);
+    return true;
+}
+
 __device__ __forceinline__ void init_ring(const SmemLayout &Lay, unsigned R) {
     extern __shared__ __align__(128) unsigned char smem[];
     if (threadIdx.x == 0) {
@@ -677,6 +909,34 @@ __global__ void __launch_bounds__(kMaxThreads) walk_batch_kernel(BatchArgs b) {
     }
 }
 
+// Two patterns per thread (FP32, one thread per pattern pair).
+template <int K, bool STAGED>
+__global__ void __launch_bounds__(kBlock) walk_kernel2(PlanArgs a) {
+    const SmemLayout Lay = smem_layout(CXG_FP32, K, blockDim.x * 2, a.nslot, a.ring,
+                                       a.rstride, a.lmax, a.nleaf);
+    init_ring(Lay, a.ring);
+    uint32_t phase = 0;
+    walk_tile2<K, STAGED>(a, blockIdx.x, Lay, a.ring, phase);
+}
+
+template <int K, bool STAGED>
+__global__ void __launch_bounds__(kBlock) walk_batch_kernel2(BatchArgs b) {
+    __shared__ unsigned s_item;
+    const SmemLayout Lay = smem_layout(CXG_FP32, K, blockDim.x * 2, b.max_nslot, b.ring,
+                                       b.max_rstride, b.max_lmax, b.max_nleaf);
+    init_ring(Lay, b.ring);
+    uint32_t phase = 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);
+        __syncthreads();
+        const unsigned item = s_item;
+        __syncthreads();
+        if (item >= b.nitems) break;
+        const WalkItem it = b.items[item];
+        if (!walk_tile2<K, STAGED>(b.jobs[it.job], it.tile, Lay, b.ring, phase)) break;
+    }
+}
+
 unsigned plan_blocks(unsigned ppad, unsigned tile) { return ppad / tile; }
 
 template <typename Kern>
@@ -711,6 +971,35 @@ static cudaError_t batch_fn(size_t sm, void (**fn)(BatchArgs)) {
     *fn = walk_batch_kernel<T, KT, G, ST>;
     return ensure_smem(walk_batch_kernel<T, KT, G, ST>, sm, optin);
 }
+template <int K, bool ST>
+static cudaError_t walk2_fn(size_t sm, void (**fn)(PlanArgs)) {
+    static size_t optin = 0;
+    *fn = walk_kernel2<K, ST>;
+    return ensure_smem(walk_kernel2<K, ST>, sm, optin);
+}
+template <int K, bool ST>
+static cudaError_t batch2_fn(size_t sm, void (**fn)(BatchArgs)) {
+    static size_t optin = 0;
+    *fn = walk_batch_kernel2<K, ST>;
+    return ensure_smem(walk_batch_kernel2<K, ST>, sm, optin);
+}
+
+// The two-patterns-per-thread walker for kact (FP32), with its dynamic
+// shared memory limit raised to `sm` bytes.
+template <typename Fn>
+static cudaError_t pick_walker2(unsigned kact, bool staged, size_t sm, Fn *fn, bool batch) {
+#define CXG_X2(K)                                                                       \
+    if (kact == (K)) {                                                                  \
+        if (batch)                                                                      \
+            return staged ? batch2_fn<K, true>(sm, reinterpret_cast<void (**)(BatchArgs)>(fn)) \
+                          : batch2_fn<K, false>(sm, reinterpret_cast<void (**)(BatchArgs)>(fn)); \
+        return staged ? walk2_fn<K, true>(sm, reinterpret_cast<void (**)(PlanArgs)>(fn))       \
+                      : walk2_fn<K, false>(sm, reinterpret_cast<void (**)(PlanArgs)>(fn));     \
+    }
+    CXG_X2(1) CXG_X2(2) CXG_X2(3) CXG_X2(4) CXG_X2(5)
+#undef CXG_X2
+    return cudaErrorInvalidValue;
+}
 
 // The walker for (kact, G, staged leaves or streamed), with its dynamic
 // shared memory limit raised to `sm` bytes.
@@ -740,21 +1029,23 @@ static cudaError_t pick_walker(unsigned kact, unsigned G, bool staged, size_t sm
 template <typename T>
 static cudaError_t launch_plan_t(int precision, const PlanArgs &a,
                                  cudaStream_t s) {
-    const unsigned G = a.tpp ? a.tpp : 1;
+    const unsigned G = a.tpp ? a.tpp : 1, NP = a.ppt ? a.ppt : 1;
     const unsigned nb = plan_blocks(a.ppad, a.tile);
     const size_t sm = plan_smem_bytes(precision, a.kact, a.tile, a.nslot,
                                       a.ring, a.rstride, a.lmax, a.nleaf);
     void (*fn)(PlanArgs) = nullptr;
-    cudaError_t e = pick_walker<T>(a.kact, G, a.lmax == 0, sm, &fn, false);
+    cudaError_t e = NP == 2 ? pick_walker2(a.kact, a.lmax == 0, sm, &fn, false)
+                            : pick_walker<T>(a.kact, G, a.lmax == 0, sm, &fn, false);
     if (e != cudaSuccess) return e;
-    fn<<<nb, a.tile * G, sm, s>>>(a);
+    fn<<<nb, a.tile * G / NP, sm, s>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s) {
-    const unsigned G = a.tpp ? a.tpp : 1;
+    const unsigned G = a.tpp ? a.tpp : 1, NP = a.ppt ? a.ppt : 1;
     if (a.tile == 0 || a.tile > kBlock || a.tile % 32 || a.ppad % a.tile ||
-        a.tile * G > kMaxThreads || !walker_shape_ok(precision, a.kact, G) ||
+        a.tile * G > kMaxThreads || a.tile / NP < 32 ||
+        !walker_shape_ok(precision, a.kact, G, NP) ||
         a.ring == 0 || a.ring > 8 || a.rstride % 16 || a.rstride == 0 ||
         a.ntiles != a.ppad / a.tile)
         return cudaErrorInvalidValue;
@@ -765,22 +1056,23 @@ cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s) {
 template <typename T>
 static cudaError_t launch_batch_t(int precision, const BatchArgs &b,
                                   unsigned grid, cudaStream_t s) {
-    const unsigned G = b.tpp ? b.tpp : 1;
+    const unsigned G = b.tpp ? b.tpp : 1, NP = b.ppt ? b.ppt : 1;
     const size_t sm = plan_smem_bytes(precision, b.kact, b.tile, b.max_nslot,
                                       b.ring, b.max_rstride, b.max_lmax,
                                       b.max_nleaf);
     void (*fn)(BatchArgs) = nullptr;
-    cudaError_t e = pick_walker<T>(b.kact, G, b.max_lmax == 0, sm, &fn, true);
+    cudaError_t e = NP == 2 ? pick_walker2(b.kact, b.max_lmax == 0, sm, &fn, true)
+                            : pick_walker<T>(b.kact, G, b.max_lmax == 0, sm, &fn, true);
     if (e != cudaSuccess) return e;
-    fn<<<grid, b.tile * G, sm, s>>>(b);
+    fn<<<grid, b.tile * G / NP, sm, s>>>(b);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batch(int precision, const BatchArgs &b, unsigned grid,
                          cudaStream_t s) {
-    const unsigned G = b.tpp ? b.tpp : 1;
+    const unsigned G = b.tpp ? b.tpp : 1, NP = b.ppt ? b.ppt : 1;
     if (b.tile == 0 || b.tile > kBlock || b.tile % 32 || b.tile * G > kMaxThreads ||
-        !walker_shape_ok(precision, b.kact, G) || b.ring == 0 ||
+        b.tile / NP < 32 || !walker_shape_ok(precision, b.kact, G, NP) || b.ring == 0 ||
         b.ring > 8 || b.max_rstride % 16 || b.max_rstride == 0 || grid == 0)
         return cudaErrorInvalidValue;
     return precision == CXG_FP32 ? launch_batch_t<float>(precision, b, grid, s)
@@ -788,21 +1080,24 @@ cudaError_t launch_batch(int precision, const BatchArgs &b, unsigned grid,
 }
 
 template <typename T>
-static int batch_occ_t(unsigned kact, unsigned tile, unsigned G, bool staged, size_t smem) {
+static int batch_occ_t(unsigned kact, unsigned tile, unsigned G, unsigned NP, bool staged,
+                       size_t smem) {
     void (*fn)(BatchArgs) = nullptr;
-    cudaError_t e = pick_walker<T>(kact, G, staged, smem, &fn, true);
+    cudaError_t e = NP == 2 ? pick_walker2(kact, staged, smem, &fn, true)
+                            : pick_walker<T>(kact, G, staged, smem, &fn, true);
     int n = 0;
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, (int)(tile * G), smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, (int)(tile * G / NP), smem);
     return e == cudaSuccess ? n : 0;
 }
 
 int batch_ctas_per_sm(int precision, unsigned kact, unsigned tile, unsigned tpp,
-                      bool staged, size_t smem) {
-    const unsigned G = tpp ? tpp : 1;
-    if (!walker_shape_ok(precision, kact, G) || tile * G > kMaxThreads) return 0;
-    return precision == CXG_FP32 ? batch_occ_t<float>(kact, tile, G, staged, smem)
-                                 : batch_occ_t<double>(kact, tile, G, staged, smem);
+                      unsigned ppt, bool staged, size_t smem) {
+    const unsigned G = tpp ? tpp : 1, NP = ppt ? ppt : 1;
+    if (!walker_shape_ok(precision, kact, G, NP) || tile * G > kMaxThreads || tile / NP < 32)
+        return 0;
+    return precision == CXG_FP32 ? batch_occ_t<float>(kact, tile, G, NP, staged, smem)
+                                 : batch_occ_t<double>(kact, tile, G, NP, staged, smem);
 }
 
 __global__ void qdecomp_kernel(const double *rtri, const double *pi,

@@ -270,13 +270,14 @@ struct Plan {
     PlanArgs a;
     double alg_bytes = 0.0;   // algorithmic bytes of one plan-walker launch
     double updates = 0.0;     // pattern-node updates of one run
-    unsigned tile = kTile, tpp = 1, nslot = 0, nleaf = 0;
+    unsigned tile = kTile, tpp = 1, ppt = 1, nslot = 0, nleaf = 0;
 };
 
 // Launch shape of the plan walker: patterns per CTA, threads per pattern
 // and the shared-memory budget of the CL stack (set by cxgTune).
 static unsigned g_tile = kTile;
 static unsigned g_tpp = 1;
+static unsigned g_ppt = 1;
 static size_t g_smem_budget = 24 * 1024;
 
 static int translate(State &S, CxtLik *lik, int prec, Plan &P,
@@ -641,6 +642,7 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     a.nslot = nslot;
     a.tile = tile;
     a.tpp = tuned_tpp(prec, kact, tile);
+    a.ppt = tuned_ppt(prec, kact, tile, a.tpp);
     a.root_last = root_last ? 1u : 0u;
     a.nops = (uint32_t)ops.size();
     a.kact = kact;
@@ -669,6 +671,7 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     P.updates = (double)ops.size() * npat;
     P.tile = tile;
     P.tpp = a.tpp;
+    P.ppt = a.ppt;
     P.nslot = nslot;
     P.nleaf = nleaf;
     return 0;
@@ -792,26 +795,33 @@ int cxgLikReset(void) {
     return 0;
 }
 
-int cxgTune(unsigned tile, unsigned tpp, size_t smem_budget) {
+int cxgTune(unsigned tile, unsigned tpp, unsigned ppt, size_t smem_budget) {
     if (tile != 32 && tile != 64 && tile != 128)
         return fail(CXG_EINVAL, "cxgTune: tile must be 32, 64 or 128");
     if (tpp != 1 && tpp != 2 && tpp != 4)
         return fail(CXG_EINVAL, "cxgTune: threads per pattern must be 1, 2 or 4");
     if (tile * tpp > kMaxThreads)
         return fail(CXG_EINVAL, "cxgTune: tile x threads per pattern above 256");
+    if (ppt != 1 && ppt != 2)
+        return fail(CXG_EINVAL, "cxgTune: patterns per thread must be 1 or 2");
+    if (ppt == 2 && (tpp != 1 || tile < 64))
+        return fail(CXG_EINVAL,
+                    "cxgTune: two patterns per thread need one thread per pattern, tile >= 64");
     if (smem_budget > 200 * 1024)
         return fail(CXG_EINVAL, "cxgTune: shared-memory budget above 200 KiB");
     State &S = state();
     std::lock_guard<std::mutex> g(S.mu);
     g_tile = tile;
     g_tpp = tpp;
+    g_ppt = ppt;
     g_smem_budget = smem_budget;
     return 0;
 }
 
-int cxgTuneGet(unsigned *tile, unsigned *tpp, size_t *smem_budget) {
+int cxgTuneGet(unsigned *tile, unsigned *tpp, unsigned *ppt, size_t *smem_budget) {
     if (tile) *tile = g_tile;
     if (tpp) *tpp = g_tpp;
+    if (ppt) *ppt = g_ppt;
     if (smem_budget) *smem_budget = g_smem_budget;
     return 0;
 }
@@ -897,11 +907,12 @@ int cxgPlanTime(cxgPlan *h, int iters, double *ms_per_run,
     return finish(S, P, lnL, nullptr);
 }
 
-int cxgPlanShape(const cxgPlan *h, unsigned *tile, unsigned *tpp, unsigned *nslot,
-                 unsigned *nleaf) {
+int cxgPlanShape(const cxgPlan *h, unsigned *tile, unsigned *tpp, unsigned *ppt,
+                 unsigned *nslot, unsigned *nleaf) {
     if (h == nullptr) return fail(CXG_EINVAL, "cxgPlanShape: NULL plan");
     if (tile) *tile = h->p.tile;
     if (tpp) *tpp = h->p.tpp;
+    if (ppt) *ppt = h->p.ppt;
     if (nslot) *nslot = h->p.nslot;
     if (nleaf) *nleaf = h->p.nleaf;
     return 0;
@@ -1129,6 +1140,7 @@ int cxgBatchCreate(CxtLik *const *liks, unsigned n, int precision,
         ba.counter = (unsigned *)(res + (size_t)n * 32 + 16 * gi);
         ba.tile = b->plans[0]->tile;
         ba.tpp = b->plans[0]->tpp;
+        ba.ppt = b->plans[0]->ppt;
         ba.ring = kRing;
         ba.kact = kact;
         ba.max_rstride = 16;
@@ -1152,7 +1164,7 @@ int cxgBatchCreate(CxtLik *const *liks, unsigned n, int precision,
                 plan_smem_bytes(precision, kact, ba.tile, ba.max_nslot, kRing,
                                 ba.max_rstride, ba.max_lmax, ba.max_nleaf);
             const int per =
-                batch_ctas_per_sm(precision, kact, ba.tile, ba.tpp, gi == 0, smem);
+                batch_ctas_per_sm(precision, kact, ba.tile, ba.tpp, ba.ppt, gi == 0, smem);
             if (per <= 0 || nsm <= 0) {
                 free_batch(b);
                 return fail(CXG_EINVAL, "cxgBatchCreate: walker does not fit an SM");

@@ -902,8 +902,10 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
                            ~(size_t)15);
     unsigned tile = 0, tpp_q = 1;
     size_t budget = 0;
-    cxgTuneGet(&tile, &tpp_q, &budget);
+    unsigned ppt_q = 1;
+    cxgTuneGet(&tile, &tpp_q, &ppt_q, &budget);
     const unsigned tpp = tuned_tpp(cfg->precision, K, tile);
+    const unsigned ppt = tuned_ppt(cfg->precision, K, tile, tpp);
     d.ntiles = d.ppad / tile;
     {
         // Leaves staged per tile when they fit, else streamed with the op
@@ -1056,6 +1058,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
         a.nslot = d.nslot_cap;
         a.tile = tile;
         a.tpp = tpp;
+        a.ppt = ppt;
         a.kact = K;
         a.npat = d.npat;
         a.ppad = d.ppad;
@@ -1086,6 +1089,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     ba.counter = d.counter;
     ba.tile = tile;
     ba.tpp = tpp;
+    ba.ppt = ppt;
     ba.ring = kRing;
     ba.kact = K;
     ba.max_nslot = d.nslot_cap;
@@ -1097,7 +1101,8 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int per = batch_ctas_per_sm(cfg->precision, K, tile, tpp, d.staged != 0, smem);
+    const int per =
+        batch_ctas_per_sm(cfg->precision, K, tile, tpp, ppt, d.staged != 0, smem);
     if (per <= 0) {
         mc3_free(h);
         return fail(CXG_EINVAL, "cxgMc3Create: walker does not fit an SM");

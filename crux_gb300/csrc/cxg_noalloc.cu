@@ -210,7 +210,8 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
     size_t budget = 0;
     {
         unsigned tpp_q = 1;
-        cxgTuneGet(&tile, &tpp_q, &budget);
+        unsigned ppt_q = 1;
+        cxgTuneGet(&tile, &tpp_q, &ppt_q, &budget);
     }
     const unsigned tpp = tuned_tpp(prec, kact, tile);
     const unsigned nb = plan_blocks(ppad, tile);
@@ -374,6 +375,7 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
     a.nslot = used;
     a.tile = tile;
     a.tpp = tpp;
+    a.ppt = tuned_ppt(prec, kact, tile, tpp);
     a.kact = kact;
     a.npat = npat;
     a.ppad = ppad;

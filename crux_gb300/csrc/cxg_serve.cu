@@ -103,7 +103,7 @@ struct HostKid {
 struct HostPlan {
     bool ready = false;
     unsigned K = 0, ppad = 0, ntiles = 0, nops = 0, nk = 0, nslot = 0, nhbm = 0;
-    unsigned tile = kTile, tpp = 1, lmax = 0;
+    unsigned tile = kTile, tpp = 1, ppt = 1, lmax = 0;
     bool staged = false;  // leaves staged per tile (else streamed)
     size_t rstride = 0, job_bytes = 0, data_bytes = 0;
     std::vector<int> order, slot, hbm;
@@ -227,8 +227,10 @@ void plan_request(SrvRequest &rq, int prec) {
     P.ppad = pad_patterns(r.npat);
     unsigned tq = 0;
     size_t budget = 0;
-    cxgTuneGet(&P.tile, &tq, &budget);
+    unsigned pq = 1;
+    cxgTuneGet(&P.tile, &tq, &pq, &budget);
     P.tpp = tuned_tpp(prec, P.K, P.tile);
+    P.ppt = tuned_ppt(prec, P.K, P.tile, P.tpp);
     P.ntiles = P.ppad / P.tile;
     const size_t elt = prec == CXG_FP32 ? 4 : 8;
     const unsigned K = P.K;
@@ -556,6 +558,7 @@ int prepare_job(cxgServer *S, SrvJob &J) {
     a.nslot = P.nslot;
     a.tile = P.tile;
     a.tpp = P.tpp;
+    a.ppt = P.ppt;
     a.kact = K;
     a.npat = r.npat;
     a.ppad = J.ppad;
@@ -646,6 +649,7 @@ int launch_batch_of(cxgServer *S, SrvBatch &B, cudaStream_t st) {
     ba.counter = (unsigned *)(res + n * 32);
     ba.tile = B.jobs[0]->a.tile;
     ba.tpp = B.jobs[0]->a.tpp;
+    ba.ppt = B.jobs[0]->a.ppt;
     ba.ring = kRing;
     ba.kact = B.jobs[0]->kact;
     ba.max_nslot = max_nslot;
@@ -658,7 +662,8 @@ int launch_batch_of(cxgServer *S, SrvBatch &B, cudaStream_t st) {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int per = batch_ctas_per_sm(prec, ba.kact, ba.tile, ba.tpp, max_lmax == 0, smem);
+    const int per =
+        batch_ctas_per_sm(prec, ba.kact, ba.tile, ba.tpp, ba.ppt, max_lmax == 0, smem);
     if (per <= 0) return fail(CXG_EINVAL, "server: walker does not fit an SM");
     cudaError_t e = launch_batch(prec, ba, (unsigned)(per * nsm), st);
     if (e != cudaSuccess) return cuda_fail(e, "walk_batch_kernel (server)");
@@ -752,7 +757,8 @@ void lnl_loop(cxgServer *S) {
             // pattern, staged or streamed leaves.
             std::map<unsigned, std::vector<SrvJob *>> byk;
             for (SrvJob *J : ready)
-                byk[J->kact | J->a.tile << 8 | J->a.tpp << 16 | (J->a.lmax ? 1u : 0u) << 24]
+                byk[J->kact | J->a.tile << 8 | J->a.tpp << 16 | J->a.ppt << 20 |
+                    (J->a.lmax ? 1u : 0u) << 24]
                     .push_back(J);
             ready.clear();
             for (auto &kv : byk) {

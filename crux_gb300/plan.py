@@ -48,13 +48,15 @@ class Plan:
                 "nops": nops.value, "kernels_per_run": nk.value}
 
     def shape(self):
-        t, g = ctypes.c_uint(), ctypes.c_uint()
+        t, g, p = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
         n, l = ctypes.c_uint(), ctypes.c_uint()
         self._check(self.lib.cxgPlanShape(self.h, ctypes.byref(t),
-                                          ctypes.byref(g), ctypes.byref(n),
-                                          ctypes.byref(l)), "cxgPlanShape")
+                                          ctypes.byref(g), ctypes.byref(p),
+                                          ctypes.byref(n), ctypes.byref(l)),
+                    "cxgPlanShape")
         return {"tile": t.value, "threads_per_pattern": g.value,
-                "nslot": n.value, "nleaf": l.value}
+                "patterns_per_thread": p.value, "nslot": n.value,
+                "nleaf": l.value}
 
     def close(self):
         if self.h:

@@ -1,6 +1,6 @@
 """Autotuner of the plan walker's launch shape.
 
-The walker's shape is three numbers, set process-wide by ``cxgTune``
+The walker's shape is four numbers, set process-wide by ``cxgTune``
 (include/cxlik_gpu.h) and read when a plan, batch, MC3 run or server
 request is translated:
 
@@ -8,6 +8,9 @@ request is translated:
 * ``tpp``: threads per pattern (1, 2 or 4). The FP32 form splits a
   pattern's components over that many consecutive threads when the count
   divides them;
+* ``ppt``: patterns per thread (1 or 2). The FP32 form with one thread per
+  pattern and at most five components can give each thread two patterns,
+  half a tile apart, for twice the independent arithmetic per thread;
 * ``budget``: shared-memory bytes for the CL stack of a tile. This caps the
   number of stack slots; results that find no slot go through HBM.
 
@@ -21,26 +24,34 @@ import itertools
 
 TILES = (32, 64, 128)
 TPPS = (1, 2, 4)
+PPTS = (1, 2)
 BUDGETS = (0, 12 << 10, 24 << 10, 48 << 10, 96 << 10)
 MAX_THREADS = 256
 
 
 def get(lib):
-    """The current shape as (tile, tpp, budget)."""
-    t, g, b = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_size_t()
-    lib.cxgTuneGet(ctypes.byref(t), ctypes.byref(g), ctypes.byref(b))
-    return t.value, g.value, b.value
+    """The current shape as (tile, tpp, ppt, budget)."""
+    t, g, p = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
+    b = ctypes.c_size_t()
+    lib.cxgTuneGet(ctypes.byref(t), ctypes.byref(g), ctypes.byref(p),
+                   ctypes.byref(b))
+    return t.value, g.value, p.value, b.value
 
 
-def set_shape(lib, tile, tpp, budget):
-    if lib.cxgTune(tile, tpp, budget) != 0:
+def set_shape(lib, tile, tpp, ppt, budget):
+    if lib.cxgTune(tile, tpp, ppt, budget) != 0:
         raise ValueError("cxgTune: %s" % lib.cxgLastError().decode())
 
 
-def shape_ok(precision, kact, tile, tpp):
-    """Whether the library has a walker for this shape (the C rule of
-    walker_shape_ok, crux_gb300/csrc/cxg_internal.h)."""
-    if tile * tpp > MAX_THREADS:
+def shape_ok(precision, kact, tile, tpp, ppt=1):
+    """Whether the library has a walker for this shape (the C rules of
+    walker_shape_ok and tuned_ppt, crux_gb300/csrc/cxg_internal.h)."""
+    if tile * tpp > MAX_THREADS or kact < 1:
+        return False
+    if ppt == 2:
+        return (precision == "fp32" and tpp == 1 and 1 <= kact <= 5
+                and tile >= 64)
+    if ppt != 1:
         return False
     if tpp == 1:
         return 1 <= kact <= 8
@@ -49,9 +60,12 @@ def shape_ok(precision, kact, tile, tpp):
     return kact // tpp <= (4 if tpp == 2 else 2)
 
 
-def candidates(precision, kact, tiles=TILES, tpps=TPPS, budgets=BUDGETS):
-    return [(t, g, b) for t, g, b in itertools.product(tiles, tpps, budgets)
-            if shape_ok(precision, kact, t, g)]
+def candidates(precision, kact, tiles=TILES, tpps=TPPS, budgets=BUDGETS,
+               ppts=PPTS):
+    """(tile, tpp, ppt, budget) shapes the library has a walker for."""
+    return [(t, g, p, b) for t, g, p, b in itertools.product(tiles, tpps, ppts,
+                                                             budgets)
+            if shape_ok(precision, kact, t, g, p)]
 
 
 def active_components(lik):
@@ -66,7 +80,8 @@ def _sweep(lib, shapes, measure):
     try:
         for shape in shapes:
             set_shape(lib, *shape)
-            row = {"tile": shape[0], "tpp": shape[1], "budget": shape[2]}
+            row = {"tile": shape[0], "tpp": shape[1], "ppt": shape[2],
+                   "budget": shape[3]}
             try:
                 row["ms"] = measure()
             except RuntimeError as e:
@@ -79,7 +94,7 @@ def _sweep(lib, shapes, measure):
     best = min(table, key=lambda r: r["ms"])
     if best["ms"] == float("inf"):
         raise RuntimeError("no walker shape ran: %s" % table[0].get("error"))
-    set_shape(lib, best["tile"], best["tpp"], best["budget"])
+    set_shape(lib, best["tile"], best["tpp"], best["ppt"], best["budget"])
     return {"best": best, "table": table}
 
 

@@ -219,9 +219,9 @@ int cxgPlanInfo(const cxgPlan *plan, double *updates, double *alg_bytes,
                 unsigned *nops, unsigned *kernels_per_run);
 int cxgPlanDestroy(cxgPlan *plan);
 /* Launch shape chosen for a plan: patterns per CTA, threads per pattern,
- * shared-memory stack slots, staged leaves. */
+ * patterns per thread, shared-memory stack slots, distinct leaves. */
 int cxgPlanShape(const cxgPlan *plan, unsigned *tile, unsigned *threads_per_pattern,
-                 unsigned *nslot, unsigned *nleaf);
+                 unsigned *patterns_per_thread, unsigned *nslot, unsigned *nleaf);
 
 /* A batch: the plans of many likelihoods (trees, alignments, models; all
  * with the same number of active components) run by one persistent launch
@@ -373,12 +373,15 @@ int cxgCompact(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
 /* Launch shape of the plan walker for plans translated from now on:
  * patterns per CTA (32, 64 or 128), threads per pattern (1, 2 or 4: the
  * FP32 form splits a pattern's components over that many threads when the
- * count divides them; tile x threads <= 256) and the shared-memory budget
- * of its CL stack (bytes, <= 200 KiB).  Every shape gives the same bits.
- * Chosen by the autotuner (crux_gb300.tune). */
-int cxgTune(unsigned tile, unsigned threads_per_pattern, size_t smem_budget);
+ * count divides them; tile x threads <= 256), patterns per thread (1 or 2:
+ * the FP32 form with one thread per pattern and <= 5 components can give a
+ * thread two patterns; tile >= 64) and the shared-memory budget of its CL
+ * stack (bytes, <= 200 KiB).  Every shape gives the same bits.  Chosen by
+ * the autotuner (crux_gb300.tune). */
+int cxgTune(unsigned tile, unsigned threads_per_pattern,
+            unsigned patterns_per_thread, size_t smem_budget);
 int cxgTuneGet(unsigned *tile, unsigned *threads_per_pattern,
-               size_t *smem_budget);
+               unsigned *patterns_per_thread, size_t *smem_budget);
 
 /* No counterpart in the reference.  Evaluate lik's plan without allocating
  * anything, for callers that cannot call cudaMalloc.  Such a caller may

@@ -1,5 +1,5 @@
 """Walker shapes and the autotuner: every (tile, threads per pattern,
-stack budget) gives bit-identical lnLs and site lnLs, in single plans and
+patterns per thread, stack budget) gives bit-identical lnLs and site lnLs, in single plans and
 in batches, within the oracle tolerance of each form; the tuner times its
 candidates and sets the fastest."""
 import numpy as np
@@ -30,10 +30,14 @@ def test_every_shape_same_bits(gpu, port, restore, precision, shape):
     case = synth.Case(ntaxa, nsites, 0.1, 77, pinv=pinv, gap_frac=0.01)
     want = case.lik(lib=port).lnL()
     lik = case.lik(lib=gpu, precision=precision)
+    lik.lnL()  # the component weights are set by the first evaluation
     kact = tune.active_components(lik)
+    assert kact == (4 if pinv == 0.0 else 5)
     shapes = tune.candidates(precision, kact)
-    assert any(g > 1 for _, g, _ in shapes) == (precision == "fp32" and
-                                                kact % 2 == 0)
+    assert any(g > 1 for _, g, _, _ in shapes) == (precision == "fp32" and
+                                                   kact % 2 == 0)
+    assert any(p > 1 for _, _, p, _ in shapes) == (precision == "fp32" and
+                                                   kact <= 5)
     first = None
     for shape in shapes:
         tune.set_shape(gpu, *shape)
@@ -72,12 +76,14 @@ def test_tune_plan_sets_fastest(gpu, restore):
     case = synth.Case(32, 20000, 0.1, 91)
     lik = case.lik(lib=gpu, precision="fp32")
     lik.prepare_plan()
-    shapes = [(64, 1, 24 << 10), (64, 4, 24 << 10), (128, 2, 12 << 10)]
+    shapes = [(64, 1, 1, 24 << 10), (64, 4, 1, 24 << 10),
+              (128, 2, 1, 12 << 10), (128, 1, 2, 24 << 10)]
     res = tune.tune_plan(lik, "fp32", iters=5, shapes=shapes)
-    assert len(res["table"]) == 3
+    assert len(res["table"]) == 4
     best = res["best"]
     assert best["ms"] == min(r["ms"] for r in res["table"])
-    assert tune.get(gpu) == (best["tile"], best["tpp"], best["budget"])
+    assert tune.get(gpu) == (best["tile"], best["tpp"], best["ppt"],
+                             best["budget"])
 
 
 def test_mc3_and_server_follow_the_shape(gpu, restore):
@@ -89,7 +95,9 @@ def test_mc3_and_server_follow_the_shape(gpu, restore):
     aln = case.alignment()
     req = PreparedRequest(case, LNL)
     traces, served = [], []
-    for shape in [(64, 1, 24 << 10), (64, 4, 24 << 10), (32, 2, 0)]:
+    shapes = [(64, 1, 1, 24 << 10), (64, 4, 1, 24 << 10), (32, 2, 1, 0),
+              (128, 1, 2, 24 << 10)]
+    for shape in shapes:
         tune.set_shape(gpu, *shape)
         m = Mc3(case.tree(aln.taxaMap), aln, case.params["rates"],
                 case.params["freqs"], alpha=0.5, ncat=4, nchains=2, seed=3,
@@ -102,4 +110,4 @@ def test_mc3_and_server_follow_the_shape(gpu, restore):
         served.append(srv.wait(srv.submit(req))[0])
         srv.close()
     assert all(np.array_equal(traces[0], t) for t in traces[1:])
-    assert served[0] == served[1] == served[2]
+    assert all(s == served[0] for s in served[1:])
