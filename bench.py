@@ -189,21 +189,25 @@ def autotune(lib, prec, args, lik=None, liks=None):
     return best
 
 
-def cpu_run(lib, case, aln, steps, threads):
-    """Time full-plan FP64 evaluations of the oracle; returns updates/s."""
+def cpu_run(lib, case, aln, steps, threads, min_s=0.0):
+    """Time full-plan FP64 evaluations of the oracle: at least `steps`, and
+    more until `min_s` seconds of CxLikExecute have run.  Returns
+    (updates/s, seconds, updates, evaluations)."""
     from crux_gb300 import synth
     lik = case.lik(lib=lib, alignment=aln)
     lik.lnL()
     t = 0.0
     ups = 0
-    for _ in range(steps):
+    n = 0
+    while n < steps or t < min_s:
+        n += 1
         lik.lik.invalidate = True
         lik._prep(None)
         t0 = time.perf_counter()
         lib.CxLikExecute(ctypes.byref(lik.lik))
         t += time.perf_counter() - t0
         ups += synth.nnodes_updates(lik)
-    return ups / t, t, ups
+    return ups / t, t, ups, n
 
 
 def load_cpu_oracle():
@@ -228,7 +232,7 @@ def run_reference(args, dist):
     case = make_case()
     aln = case.alignment()
     cpu_run(lib, case, aln, max(args.warmup, 1), threads)
-    rate, secs, ups = cpu_run(lib, case, aln, args.steps, threads)
+    rate, secs, ups, _ = cpu_run(lib, case, aln, args.steps, threads)
     line = {"metric": METRIC, "impl": "reference", "value": rate, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
@@ -318,12 +322,13 @@ def run_ours(args, dist):
     if dist.rank == 0 and not args.no_cpu:
         lib, kind, threads = load_cpu_oracle()
         aln = case.alignment()
-        rate, secs, ups = cpu_run(lib, case, aln, args.cpu_steps, threads)
+        rate, secs, ups, nev = cpu_run(lib, case, aln, args.cpu_steps,
+                                       threads, min_s=args.cpu_seconds)
         want = case.lik(lib=lib, alignment=case.alignment()).lnL()
         check = {p: abs(res[p]["lnL"] - want) / abs(want) for p in res}
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": "%d full-tree FP64 lnL evaluations (%.1f s)" %
-                         (args.cpu_steps, secs)}
+                         (nev, secs)}
 
     if dist.rank == 0:
         fp64 = res["fp64"]
@@ -861,6 +866,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU baseline and the oracle check")
     ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="least CPU-baseline time for the default workload")
     ap.add_argument("--batch", type=int, default=256,
                     help="full-tree evaluations per step")
     ap.add_argument("--profile", action="store_true",
