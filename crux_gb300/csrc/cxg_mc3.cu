@@ -31,6 +31,12 @@
 // pruned tree and so the edge count are the same both ways, and the
 // Jacobian of (l_p, l_b, l_x, u) -> (l_b + l_p, u l_x, (1 - u) l_x,
 // l_p / (l_p + l_b)) gives the Hastings ratio l_x / (l_b + l_p).
+// Extending TBR (etbrPropose, Chain.pyx:478-819): each end of a uniform
+// edge eA moves its node along a random path, extended with probability
+// etbr_pext per step, into the path's last edge; the lengths of eA and of
+// the first edge of each path get multipliers.  A chain's tree has two
+// buffers: an eTBR move writes the re-rooted result into the spare one,
+// which an accepted move makes current.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
@@ -47,9 +53,9 @@ namespace cxg {
 
 enum {
     MV_BRLEN = 0, MV_NNI = 1, MV_RATES = 2, MV_ALPHA = 3, MV_FREQS = 4, MV_SPR = 5,
-    MV_INIT = 6
+    MV_ETBR = 6, MV_INIT = 7
 };
-constexpr int kMoves = 6;
+constexpr int kMoves = 7;
 
 struct Mc3Model {
     double rates[6], freqs[4], alpha;
@@ -75,9 +81,12 @@ struct Mc3Prop {
 struct Mc3Dev {
     uint32_t nchains, ntaxa, nnodes, root, kact, npat, ppad, prec;
     uint32_t rstride, M, maxkids, ntiles;
-    int32_t *parent;      // [c][nnodes]
-    int32_t *child;       // [c][nnodes][3]
-    double *len;          // [c][nnodes]
+    // Two tree buffers per chain, b = curtree[c] current: buffer b of
+    // chain c starts at (b * nchains + c) * nnodes entries.
+    int32_t *parent;      // [2][c][nnodes]
+    int32_t *child;       // [2][c][nnodes][3]
+    double *len;          // [2][c][nnodes]
+    uint8_t *curtree;     // [c]
     uint8_t *cur;         // [c][nnodes]
     uint8_t *dirtyflag;   // [c][nnodes]
     int32_t *dirty;       // [c][M] dirty internal nodes, bottom-up
@@ -103,7 +112,7 @@ struct Mc3Dev {
     unsigned *counter;
     double wcdf[kMoves];
     double brlen_lambda, brlen_prior, rate_conc, alpha_lambda, alpha_prior;
-    double freq_conc;
+    double freq_conc, etbr_pext;
     uint32_t swap_stride;
     uint32_t *acc, *rej;  // [c][kMoves]
     uint32_t *nswap;      // [c]
@@ -216,6 +225,86 @@ __device__ double ln_dirichlet(const double *alpha, const double *x, int n) {
     return r + lgamma(s);
 }
 
+// One end of an eTBR move (Chain.pyx:517-597 for the X end, the same for
+// Y) on a binary tree held as incidence lists: inc[v][0..2] are the edges
+// at node v (-1: none) and ex[e] is the XOR of edge e's two end nodes, so
+// the node across e from v is ex[e] ^ v.  From node n0 of edge eA: pick
+// one of n0's other edges (eX), walk to its far node, and while that node
+// is internal, extend with probability pext along a uniform edge other
+// than the one just walked.  When the walk went past eX's far node n1,
+// the rearrangement moves n0's sibling edge s to n1, eX to the
+// second-to-last node r1 of the walk, and the last edge eR to n0, so n0
+// (with eA) sits inside eR.  Lengths travel with their edges.
+//
+// ln q(back)/q(forth): the walk that undoes the move runs from n0 along eX
+// back to n1 and ends across s, so it stops at s's far node as this walk
+// stops at its last node, r0: each stop costs (1 - pext) at an internal
+// node and nothing at a leaf.  (The reference conditions that term on the
+// other end of eA, Chain.pyx:723-736; the ratio here is the one under
+// which a chain on an empty alignment samples topologies uniformly, which
+// tests check.)
+struct EtbrEnd {
+    int eX;      // first edge of the walk, -1 when n0 is a leaf
+    double lnq;  // ln of the proposal ratio of this end's walk
+};
+
+__device__ inline int etbr_deg(const int32_t *inc, int v) {
+    return (inc[v * 3] >= 0) + (inc[v * 3 + 1] >= 0) + (inc[v * 3 + 2] >= 0);
+}
+
+__device__ inline int etbr_pick(const int32_t *inc, int v, int ein, Philox &rng) {
+    int cand[3], n = 0;
+    for (int j = 0; j < 3; ++j) {
+        const int e = inc[v * 3 + j];
+        if (e >= 0 && e != ein) cand[n++] = e;
+    }
+    return cand[n > 1 ? philox_below(rng, (uint32_t)n) : 0];
+}
+
+__device__ inline void etbr_swap_edge(int32_t *inc, int v, int eold, int enew) {
+    for (int j = 0; j < 3; ++j)
+        if (inc[v * 3 + j] == eold) {
+            inc[v * 3 + j] = enew;
+            return;
+        }
+}
+
+__device__ EtbrEnd etbr_end(int n0, int eA, int32_t *inc, int32_t *ex, Philox &rng,
+                            double pext) {
+    EtbrEnd r{-1, 0.0};
+    if (etbr_deg(inc, n0) <= 1) return r;
+    const int eX = etbr_pick(inc, n0, eA, rng);
+    r.eX = eX;
+    const int n1 = ex[eX] ^ n0;
+    int e_last = eX, r1 = n0, r0 = n1;
+    while (etbr_deg(inc, r0) > 1) {
+        if (pext < philox_u01(rng)) break;
+        const int e = etbr_pick(inc, r0, e_last, rng);
+        r1 = r0;
+        r0 = ex[e] ^ r0;
+        e_last = e;
+    }
+    if (r0 == n1) return r;  // the walk did not leave eX: nothing moves
+    int s = -1;
+    for (int j = 0; j < 3; ++j) {
+        const int e = inc[n0 * 3 + j];
+        if (e >= 0 && e != eA && e != eX) s = e;
+    }
+    const int cs = ex[s] ^ n0;
+    const int eR = e_last;
+    // s: n0 -> n1; eX: n1 -> r1; eR: r1 -> n0 (in this order, each node
+    // keeps three edges; r1 may be n1).
+    etbr_swap_edge(inc, n1, eX, s);
+    ex[s] ^= n0 ^ n1;
+    etbr_swap_edge(inc, n0, s, eR);
+    etbr_swap_edge(inc, r1, eR, eX);
+    ex[eX] ^= n1 ^ r1;
+    ex[eR] ^= r1 ^ n0;
+    const double l1m = log1p(-pext);
+    r.lnq = (etbr_deg(inc, cs) > 1 ? l1m : 0.0) - (etbr_deg(inc, r0) > 1 ? l1m : 0.0);
+    return r;
+}
+
 // Shared memory of one chain's proposal: the tree (parent, child, len,
 // cur), dirty flags, DFS stack, dirty list, the per-op prefix of
 // children, and the stack slot of each op and of each op's children.
@@ -244,9 +333,13 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
     uint8_t *dflag = cur + NN;
     int8_t *op_slot = reinterpret_cast<int8_t *>(dflag + NN);   // [M]
     int8_t *kid_slot = op_slot + M;                             // [M][3]
-    int32_t *g_parent = d.parent + (size_t)c * NN;
-    int32_t *g_child = d.child + (size_t)c * NN * 3;
-    double *g_len = d.len + (size_t)c * NN;
+    const unsigned tb = d.curtree[c];
+    const size_t t_cur = (size_t)tb * d.nchains + c, t_alt = (size_t)(1 - tb) * d.nchains + c;
+    int32_t *g_parent = d.parent + t_cur * NN;
+    int32_t *g_child = d.child + t_cur * NN * 3;
+    double *g_len = d.len + t_cur * NN;
+    int32_t *a_child = d.child + t_alt * NN * 3;
+    double *a_len = d.len + t_alt * NN;
     for (unsigned i = threadIdx.x; i < NN; i += blockDim.x) {
         len[i] = g_len[i];
         parent[i] = g_parent[i];
@@ -258,9 +351,10 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
     Mc3Prop &pr = d.prop[c];
     __shared__ int s_nd, s_lowest;
     __shared__ unsigned s_fin;
-    __shared__ bool s_full;
+    __shared__ bool s_full, s_etbr;
     if (threadIdx.x == 0) {
         s_fin = 0;
+        s_etbr = false;
         Philox rng;
         philox_init(rng, d.seed, c, g);
         if (c == 0) *d.counter = 0;
@@ -410,6 +504,79 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 // Dirty: both paths to the root (p's new place, g's old child).
                 for (int v = p; v >= 0; v = parent[v]) dflag[v] = 1;
                 for (int v = g; v >= 0; v = parent[v]) dflag[v] = 1;
+            } else if (t == MV_ETBR) {
+                // Edges are named by the node below them in the current
+                // rooting; len[] holds their lengths.  child[] becomes the
+                // incidence lists and stack[] the end-node XORs.
+                int32_t *inc = child, *ex = stack;
+                for (unsigned v = 0; v < NN; ++v) {
+                    if (v == d.root) continue;
+                    int j = 0;
+                    while (inc[v * 3 + j] >= 0) ++j;
+                    inc[v * 3 + j] = (int)v;
+                    ex[v] = (int)v ^ parent[v];
+                }
+                unsigned k = philox_below(rng, NN - 1);
+                const int eA = (int)((k >= d.root) ? k + 1 : k);
+                const int nX0 = eA, nY0 = ex[eA] ^ eA;
+                const EtbrEnd X = etbr_end(nX0, eA, inc, ex, rng, d.etbr_pext);
+                const EtbrEnd Y = etbr_end(nY0, eA, inc, ex, rng, d.etbr_pext);
+                double lnH = X.lnq + Y.lnq, lnP = 0.0;
+                const int em[3] = {eA, X.eX, Y.eX};
+                for (int q = 0; q < 3; ++q) {
+                    if (em[q] < 0) continue;
+                    const double lnM = d.brlen_lambda * (philox_u01(rng) - 0.5);
+                    const double v0 = len[em[q]], v1 = v0 * exp(lnM);
+                    len[em[q]] = v1;
+                    lnH += lnM;
+                    lnP += -d.brlen_prior * (v1 - v0);
+                }
+                pr.lnPrior = lnP;
+                pr.lnHast = lnH;
+                // Root the result at the same node again, by an Euler
+                // walk: parent[] gets the new parents, the spare buffer the
+                // new child slots (-1 where the slot held the parent edge)
+                // and lengths; dflag[v] is v's next incidence slot.
+                parent[d.root] = -1;
+                a_len[d.root] = len[d.root];
+                int v = (int)d.root;
+                // The walk takes 3 NN slot steps and NN - 1 steps back up;
+                // the bound only guards against a malformed tree.
+                unsigned steps = 0;
+                const unsigned max_steps = 4 * NN + 4;
+                for (; steps < max_steps; ++steps) {
+                    if (dflag[v] < 3) {
+                        const int j = dflag[v]++;
+                        const int e = inc[v * 3 + j];
+                        const int u = e >= 0 ? (ex[e] ^ v) : -1;
+                        if (u < 0 || u == parent[v]) {
+                            a_child[v * 3 + j] = -1;
+                            continue;
+                        }
+                        a_child[v * 3 + j] = u;
+                        parent[u] = v;
+                        a_len[u] = len[e];
+                        v = u;
+                    } else {
+                        if (v == (int)d.root) break;
+                        v = parent[v];
+                    }
+                }
+                if (steps < max_steps) {
+                    s_etbr = true;
+                } else {
+                    // Not reachable for a binary tree: report it, put the
+                    // current tree back and reject the move.
+                    atomicOr(d.status, 2u);
+                    for (unsigned i = 0; i < NN; ++i) {
+                        len[i] = g_len[i];
+                        parent[i] = g_parent[i];
+                        dflag[i] = 0;
+                    }
+                    for (unsigned i = 0; i < NN * 3; ++i) child[i] = g_child[i];
+                    pr.lnPrior = -INFINITY;
+                    lowest = (int)d.root;
+                }
             } else if (t == MV_FREQS) {
                 // Base frequencies ~ Dirichlet(conc * pi).
                 double f0[4], f1[4], a0[4], a1[4], s0 = 0.0, s1 = 0.0;
@@ -469,6 +636,38 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         s_lowest = lowest;
     }
     __syncthreads();
+    if (s_etbr) {
+        // The re-rooted tree into shared memory.  A node whose children
+        // are the same set as before keeps their old order; it is dirty if
+        // the set or a child's edge length changed.
+        for (unsigned v = threadIdx.x; v < NN; v += blockDim.x) {
+            len[v] = a_len[v];
+            int nw[3] = {-1, -1, -1}, n = 0;
+            for (int j = 0; j < 3; ++j) {
+                const int x = a_child[v * 3 + j];
+                if (x >= 0) nw[n++] = x;
+            }
+            int same = 1, nold = 0;
+            for (int j = 0; j < 3; ++j) {
+                const int x = g_child[v * 3 + j];
+                if (x < 0) continue;
+                ++nold;
+                same &= (x == nw[0] || x == nw[1] || x == nw[2]);
+            }
+            same &= (nold == n);
+            for (int j = 0; j < 3; ++j) child[v * 3 + j] = same ? g_child[v * 3 + j] : nw[j];
+            dflag[v] = (v >= N && !same) ? 1 : 0;
+        }
+        __syncthreads();
+        for (unsigned v = N + threadIdx.x; v < NN; v += blockDim.x) {
+            if (dflag[v]) continue;
+            for (int j = 0; j < 3; ++j) {
+                const int u = child[v * 3 + j];
+                if (u >= 0 && len[u] != g_len[u]) dflag[v] = 1;
+            }
+        }
+        __syncthreads();
+    }
     // The proposed model's derived quantities (a second warp) while thread
     // 0 lists the dirty nodes and assigns stack slots.
     if (threadIdx.x >= 32 && threadIdx.x < 64 && s_fin) {
@@ -485,7 +684,15 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         const int lowest = s_lowest;
         // Dirty internal nodes, children before parents.
         int nd = 0;
-        if (pr.type == MV_SPR) {
+        if (s_etbr) {
+            // Every ancestor of a changed node, and the root, is dirty too.
+            dflag[d.root] = 1;
+            for (unsigned v = N; v < NN; ++v) {
+                if (dflag[v] != 1) continue;
+                for (int u = parent[v]; u >= 0 && dflag[u] != 1; u = parent[u]) dflag[u] = 1;
+            }
+        }
+        if (pr.type == MV_SPR || s_etbr) {
             // The nodes flagged above, in reversed pre-order of the new tree.
             int sp = 0;
             stack[sp++] = (int)d.root;
@@ -641,12 +848,19 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         }
         for (unsigned j = nl; j < 3; ++j) lr[j] = nullptr;
     }
-    // The tree (moved) and the dirty list back to HBM.
-    for (unsigned i = threadIdx.x; i < NN; i += blockDim.x) {
-        g_len[i] = len[i];
-        g_parent[i] = parent[i];
+    // The tree (moved) and the dirty list back to HBM; an eTBR result goes
+    // to the spare tree buffer, which the accept kernel makes current.
+    {
+        const size_t to = s_etbr ? t_alt : t_cur;
+        int32_t *o_parent = d.parent + to * NN;
+        int32_t *o_child = d.child + to * NN * 3;
+        double *o_len = d.len + to * NN;
+        for (unsigned i = threadIdx.x; i < NN; i += blockDim.x) {
+            o_len[i] = len[i];
+            o_parent[i] = parent[i];
+        }
+        for (unsigned i = threadIdx.x; i < NN * 3; i += blockDim.x) o_child[i] = child[i];
     }
-    for (unsigned i = threadIdx.x; i < NN * 3; i += blockDim.x) g_child[i] = child[i];
     for (int i = threadIdx.x; i < nd; i += blockDim.x)
         d.dirty[(size_t)c * M + i] = dirty[i];
     if (threadIdx.x == 0) {
@@ -707,7 +921,7 @@ __global__ void mc3_accept_kernel(Mc3Dev d) {
             // p = [(likelihood ratio)(prior ratio)]^heat * (Hastings ratio)
             const double p =
                 exp(((lnL1 - d.lnL[c]) + pr.lnPrior) * d.heat[c] + pr.lnHast);
-            accept = (p >= u) && isfinite(lnL1);
+            accept = (p >= u) && (p > 0.0) && isfinite(lnL1);
         }
         uint8_t *cur = d.cur + (size_t)c * NN;
         uint8_t *dflag = d.dirtyflag + (size_t)c * NN;
@@ -719,16 +933,19 @@ __global__ void mc3_accept_kernel(Mc3Dev d) {
         if (accept) {
             d.lnL[c] = lnL1;
             if (pr.model_changed) d.curmodel[c] ^= 1;
+            if (pr.type == MV_ETBR) d.curtree[c] ^= 1;
             if (pr.type < kMoves) d.acc[c * kMoves + pr.type]++;
         } else {
-            int32_t *parent = d.parent + (size_t)c * NN;
-            int32_t *child = d.child + (size_t)c * NN * 3;
+            // A rejected eTBR move left the current tree buffer as it was.
+            const size_t tc = (size_t)d.curtree[c] * d.nchains + c;
+            int32_t *parent = d.parent + tc * NN;
+            int32_t *child = d.child + tc * NN * 3;
             if (pr.type == MV_BRLEN) {
-                d.len[(size_t)c * NN + pr.node] = pr.oldlen;
+                d.len[tc * NN + pr.node] = pr.oldlen;
             } else if (pr.type == MV_SPR) {
                 // Take p out of (x, xp), put it back between g and b.
                 const int p = pr.p, x = pr.x, b = pr.b, g = pr.g, xp = pr.xp;
-                double *len = d.len + (size_t)c * NN;
+                double *len = d.len + tc * NN;
                 child[xp * 3 + pr.jx] = x;
                 parent[x] = xp;
                 child[p * 3 + pr.jb] = b;
@@ -936,6 +1153,11 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     d.brlen_prior = cfg->brlen_prior;
     d.rate_conc = cfg->rate_conc;
     d.freq_conc = cfg->freq_conc > 0.0 ? cfg->freq_conc : 300.0;
+    if (!(cfg->etbr_pext >= 0.0 && cfg->etbr_pext <= 1.0)) {
+        mc3_free(h);
+        return fail(CXG_EINVAL, "cxgMc3Create: etbr_pext must be in [0, 1]");
+    }
+    d.etbr_pext = cfg->etbr_pext;
     d.alpha_lambda = cfg->alpha_lambda;
     d.alpha_prior = cfg->alpha_prior;
     d.trace_cap = cfg->trace_cap;
@@ -945,10 +1167,10 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
         mc3_free(h);
         return cuda_fail(e, "cudaStreamCreate(mc3)");
     }
-    // Topology, lengths, buffers.
-    std::vector<int32_t> par_all((size_t)C * NN), ch_all((size_t)C * NN * 3);
-    std::vector<double> len_all((size_t)C * NN);
-    for (unsigned c = 0; c < C; ++c) {
+    // Topology, lengths (both tree buffers of every chain), CL buffers.
+    std::vector<int32_t> par_all((size_t)2 * C * NN), ch_all((size_t)2 * C * NN * 3);
+    std::vector<double> len_all((size_t)2 * C * NN);
+    for (unsigned c = 0; c < 2 * C; ++c) {
         memcpy(&par_all[(size_t)c * NN], cfg->parent, NN * 4);
         memcpy(&ch_all[(size_t)c * NN * 3], child.data(), NN * 3 * 4);
         memcpy(&len_all[(size_t)c * NN], cfg->len, NN * 8);
@@ -977,6 +1199,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     if ((rc = mc3_upload(h, &d.parent, par_all.data(), par_all.size())) ||
         (rc = mc3_upload(h, &d.child, ch_all.data(), ch_all.size())) ||
         (rc = mc3_upload(h, &d.len, len_all.data(), len_all.size())) ||
+        (rc = mc3_upload<uint8_t>(h, &d.curtree, nullptr, C)) ||
         (rc = mc3_upload<uint8_t>(h, &d.cur, nullptr, (size_t)C * NN)) ||
         (rc = mc3_upload<uint8_t>(h, &d.dirtyflag, nullptr, (size_t)C * NN)) ||
         (rc = mc3_upload<int32_t>(h, &d.dirty, nullptr, (size_t)C * M)) ||
@@ -1189,7 +1412,10 @@ extern "C" int cxgMc3Run(cxgMc3 *h, unsigned long long ngen, double *seconds) {
     if (seconds) *seconds = ms / 1e3;
     uint32_t st = 0;
     CXG_CUDA(cudaMemcpy(&st, h->d.status, 4, cudaMemcpyDeviceToHost));
-    (void)st;  // undecomposable proposed models are rejected, not errors
+    // Undecomposable proposed models are rejected, not errors (bit 0 is
+    // only set for the initial model); bit 1 is a tree the eTBR re-rooting
+    // could not walk, which a binary tree never gives.
+    if (st & 2u) return fail(CXG_EINVAL, "MC3: an eTBR move met a malformed tree");
     // Any bounded wait that gave up?
     std::vector<char> res((size_t)h->d.nchains * 32);
     CXG_CUDA(cudaMemcpy(res.data(), h->d.results, res.size(), cudaMemcpyDeviceToHost));
@@ -1208,11 +1434,14 @@ extern "C" int cxgMc3Chain(cxgMc3 *h, unsigned chain, double *lnL, double *heat,
     CXG_CUDA(cudaStreamSynchronize(h->stream));
     if (lnL) CXG_CUDA(cudaMemcpy(lnL, d.lnL + chain, 8, cudaMemcpyDeviceToHost));
     if (heat) CXG_CUDA(cudaMemcpy(heat, d.heat + chain, 8, cudaMemcpyDeviceToHost));
+    uint8_t tb = 0;
+    CXG_CUDA(cudaMemcpy(&tb, d.curtree + chain, 1, cudaMemcpyDeviceToHost));
+    const size_t t = (size_t)tb * d.nchains + chain;
     if (parent)
-        CXG_CUDA(cudaMemcpy(parent, d.parent + (size_t)chain * d.nnodes, d.nnodes * 4,
+        CXG_CUDA(cudaMemcpy(parent, d.parent + t * d.nnodes, d.nnodes * 4,
                             cudaMemcpyDeviceToHost));
     if (len)
-        CXG_CUDA(cudaMemcpy(len, d.len + (size_t)chain * d.nnodes, d.nnodes * 8,
+        CXG_CUDA(cudaMemcpy(len, d.len + t * d.nnodes, d.nnodes * 8,
                             cudaMemcpyDeviceToHost));
     uint8_t cm = 0;
     CXG_CUDA(cudaMemcpy(&cm, d.curmodel + chain, 1, cudaMemcpyDeviceToHost));

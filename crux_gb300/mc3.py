@@ -20,7 +20,7 @@ from .alignment import Alignment, TaxaMap
 from .tree import Tree
 
 LAMBDA = 2.0 * math.log(1.6)
-MOVES = ("brlen", "nni", "rates", "alpha", "freqs", "spr")
+MOVES = ("brlen", "nni", "rates", "alpha", "freqs", "spr", "etbr")
 
 
 class Mc3Config(ctypes.Structure):
@@ -40,11 +40,12 @@ class Mc3Config(ctypes.Structure):
         ("heat_delta", ctypes.c_double),
         ("swap_stride", ctypes.c_uint),
         ("seed", ctypes.c_ulonglong),
-        ("move_weight", ctypes.c_double * 6),
+        ("move_weight", ctypes.c_double * 7),
         ("brlen_lambda", ctypes.c_double),
         ("brlen_prior", ctypes.c_double),
         ("rate_conc", ctypes.c_double),
         ("freq_conc", ctypes.c_double),
+        ("etbr_pext", ctypes.c_double),
         ("alpha_lambda", ctypes.c_double),
         ("alpha_prior", ctypes.c_double),
         ("precision", ctypes.c_int),
@@ -143,6 +144,7 @@ class Mc3:
                  nchains=4, heat_delta=0.05, swap_stride=1, seed=1,
                  moves=None, precision="fp32", brlen_lambda=LAMBDA,
                  brlen_prior=10.0, rate_conc=300.0, freq_conc=300.0,
+                 etbr_pext=0.8,
                  alpha_lambda=LAMBDA,
                  alpha_prior=1.0, graph_gens=16, trace_cap=1 << 20, lib=None):
         self.lib = lib or _native.load()
@@ -184,6 +186,7 @@ class Mc3:
         c.brlen_prior = brlen_prior
         c.rate_conc = rate_conc
         c.freq_conc = freq_conc
+        c.etbr_pext = etbr_pext
         c.alpha_lambda = alpha_lambda
         c.alpha_prior = alpha_prior
         c.precision = 1 if precision == "fp32" else 0

@@ -264,11 +264,13 @@ typedef struct {
     double heat_delta;  /* chain i runs at heat 1/(1 + i*heat_delta) */
     unsigned swap_stride;
     unsigned long long seed;
-    double move_weight[6];  /* branch length, NNI, rates, alpha, base
-                               frequencies, SPR */
+    double move_weight[7];  /* branch length, NNI, rates, alpha, base
+                               frequencies, SPR, eTBR */
     double brlen_lambda, brlen_prior;
     double rate_conc;       /* Dirichlet concentration of rate moves */
     double freq_conc;       /* Dirichlet concentration of frequency moves */
+    double etbr_pext;       /* eTBR extension probability (the reference's
+                               etbrPExt, 0.8), in [0, 1] */
     double alpha_lambda, alpha_prior;
     int precision;          /* CXG_FP32 or CXG_FP64 */
     unsigned graph_gens;    /* generations per captured graph (0: 16) */
@@ -284,7 +286,7 @@ int cxgMc3Run(cxgMc3 *mc3, unsigned long long ngen, double *seconds);
 int cxgMc3Chain(cxgMc3 *mc3, unsigned chain, double *lnL, double *heat,
                 int32_t *parent, double *len, double *rates, double *freqs,
                 double *alpha);
-/* Accept/reject counts [chain][move] (6 moves, in move_weight order),
+/* Accept/reject counts [chain][move] (7 moves, in move_weight order),
  * swaps [chain], generation count. */
 int cxgMc3Stats(cxgMc3 *mc3, unsigned *accepts, unsigned *rejects,
                 unsigned *swaps, unsigned long long *gen);

@@ -1,6 +1,6 @@
-"""On-device MC3: after generations of branch-length, NNI, rate and alpha
-moves, every chain's device lnL equals the FP64 oracle's lnL of that
-chain's tree and model (1e-11 relative for the plain FP64 chains, 1e-6 for
+"""On-device MC3: after generations of branch-length, NNI, SPR, eTBR, rate,
+frequency and alpha moves, every chain's device lnL equals the FP64
+oracle's lnL of that chain's tree and model (1e-11 relative for the plain FP64 chains, 1e-6 for
 FP32 chains); moves are accepted and heats are swapped."""
 import numpy as np
 import pytest
@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 
 TOL = {"fp64": 1e-11, "fp32": 1e-6}
 MOVES = {"brlen": 2.0, "nni": 1.0, "spr": 1.0, "rates": 0.5, "alpha": 0.5,
-         "freqs": 0.5}
+         "freqs": 0.5, "etbr": 1.0}
 
 
 def build(precision, nchains=4, seed=9, moves=MOVES, ntaxa=16, nsites=1000):
@@ -44,6 +44,7 @@ def test_mc3_chains_match_oracle(gpu, port, precision):
     assert (acc + rej).min() > 0                # every move was drawn
     assert acc[0] > 0 and acc[1] > 0            # brlen and NNI accepted
     assert acc[5] > 0                           # SPR accepted
+    assert acc[6] > 0                           # eTBR accepted
     assert st["swaps"].sum() > 0
     heats = sorted(m.chain_state(i)["heat"] for i in range(m.nchains))
     assert np.allclose(heats, sorted(1.0 / (1.0 + 0.2 * i) for i in range(4)))
@@ -108,3 +109,75 @@ def test_mc3_samples_the_prior_without_data(gpu):
     assert abs(np.mean(tl) - nedge * 0.1) < 0.08 * nedge * 0.1, np.mean(tl)
     # Exp(10) lengths: the tree length has variance nedge / 100.
     assert abs(np.var(tl) - nedge / 100.0) < 0.3 * nedge / 100.0, np.var(tl)
+
+
+def _empty_alignment(ntaxa, seed):
+    from crux_gb300.alignment import Alignment, TaxaMap
+    case = synth.Case(ntaxa, 50, 0.1, seed)
+    aln0 = case.alignment()
+    rows = np.full((aln0.ntaxa, 4), ord("-"), dtype=np.uint8)
+    aln = Alignment(taxaMap=TaxaMap(aln0.taxaMap.taxa), rows=rows)
+    return case, aln
+
+
+def _is_three_cherries(parent, ntaxa):
+    """A 6-taxon unrooted binary tree is either a caterpillar or three
+    cherries; it is three cherries when every internal edge splits off a
+    pair of leaves."""
+    nn = len(parent)
+    below = [0] * nn
+    for leaf in range(ntaxa):
+        v = leaf
+        while v >= 0:
+            below[v] |= 1 << leaf
+            v = parent[v]
+    for v in range(ntaxa, nn):
+        if parent[v] < 0:
+            continue
+        k = bin(below[v]).count("1")
+        if min(k, ntaxa - k) != 2:
+            return False
+    return True
+
+
+@pytest.mark.parametrize("moves", [{"etbr": 1.0}, {"etbr": 1.0, "brlen": 1.0}])
+def test_mc3_etbr_samples_uniform_topologies(gpu, moves):
+    """Without data the chains sample the prior: every 6-taxon topology is
+    equally likely, so 15 of 105 (1/7) are three cherries, and the Exp(10)
+    branch lengths sum to 0.9 on average.  A wrong eTBR Hastings ratio
+    moves the shape frequency (the extension terms) or the tree length
+    (the multipliers)."""
+    case, aln = _empty_alignment(6, 29)
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=None,
+            nchains=4, heat_delta=0.0, seed=77, precision="fp64",
+            graph_gens=32, moves=moves)
+    m.run(3000)
+    cherries, tl, n = 0, [], 0
+    for _ in range(1000):
+        m.run(64)
+        for i in range(4):
+            st = m.chain_state(i)
+            assert abs(st["lnL"]) < 1e-9
+            cherries += _is_three_cherries(list(st["parent"]), 6)
+            tl.append(st["len"].sum())
+            n += 1
+    acc = m.stats()["accepts"].sum(axis=0)
+    m.close()
+    assert acc[6] > 0
+    frac = cherries / n
+    # 4000 thinned samples: standard error about 0.0055.
+    assert abs(frac - 1.0 / 7.0) < 0.025, frac
+    assert abs(np.mean(tl) - 0.9) < 0.05, np.mean(tl)
+
+
+def test_mc3_etbr_chains_match_oracle(gpu, port):
+    """eTBR alone re-roots the tree buffer on every accepted move; the
+    cached CLs of the nodes it leaves alone must still be right."""
+    m = build("fp64", nchains=3, seed=31, moves={"etbr": 1.0, "brlen": 0.2},
+              ntaxa=24)
+    m.run(200)
+    check_chains(m, port, TOL["fp64"])
+    acc = m.stats()["accepts"].sum(axis=0)
+    assert acc[6] > 0
+    m.close()
