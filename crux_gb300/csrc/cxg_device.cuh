@@ -16,7 +16,12 @@ namespace cxg {
 // P[i][j], in j order (P times the reference's 0/1 row, CxLik.c:357-374
 // with Lik.pyx:1466-1475), in the FP64 table for FP64 plans and in the
 // record, rounded once to FP32, for FP32 plans.
-__device__ inline void pmat_one(const PmatArgs &a, unsigned idx) {
+//
+// Four consecutive lanes (q = lane & 3, all four active) share one idx:
+// lane q computes exp(lambda_q t) and row i = q, so each lane runs a
+// quarter of the serial FP64 work.  Every entry's operations and their
+// order are those of one lane doing it all.
+__device__ inline void pmat_one(const PmatArgs &a, unsigned idx, unsigned q) {
     const unsigned c = idx / a.kact, k = idx % a.kact;
     const int m = a.model[k];
     // Same association as the reference: ((edgeLen*cmult)*rmult)*wNorm.
@@ -25,60 +30,52 @@ __device__ inline void pmat_one(const PmatArgs &a, unsigned idx) {
                                          a.rmult[k]), wn);
     const double *cube = a.cube + (size_t)m * 64;
     const double *ev = a.eig + (size_t)m * 4;
+    const double exq = exp(__dmul_rn(ev[q], t));
+    const unsigned gmask = 0xFu << ((threadIdx.x & 31u) & ~3u);
     double ex[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) ex[q] = exp(__dmul_rn(ev[q], t));
-    double P[16];
+    for (int r = 0; r < 4; ++r) ex[r] = __shfl_sync(gmask, exq, r, 4);
+    const int i = (int)q;
+    double P[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int j = 0; j < 4; ++j) {
+        double s = 0.0;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            double s = 0.0;
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                s = __dadd_rn(s, __dmul_rn(cube[i * 16 + j * 4 + q], ex[q]));
-            P[i * 4 + j] = s < 0.0 ? 0.0 : s;
-        }
+        for (int r = 0; r < 4; ++r) s = __dadd_rn(s, __dmul_rn(cube[i * 16 + j * 4 + r], ex[r]));
+        P[j] = s < 0.0 ? 0.0 : s;
     }
     const int tb = a.tab[c];
     unsigned char *dst = a.rec + a.dst[c];
-    if (tb >= 0 && a.precision == CXG_FP32) {
-        float *o = reinterpret_cast<float *>(dst);
-        for (int mask = 0; mask < 16; ++mask) {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                double acc = 0.0;
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    if (mask & (1 << j)) acc = __dadd_rn(acc, P[i * 4 + j]);
-                o[((size_t)mask * a.kact + k) * 4 + i] = (float)acc;
-            }
-        }
-        return;
-    }
     if (tb >= 0) {
         // Message of a leaf with state mask m: the sum over allowed states j
         // of P[i][j], in j order -- exactly P times the reference's 0/1 row.
-        for (int mask = 0; mask < 16; ++mask) {
-            double *t = a.ltab + (((size_t)tb * 16 + mask) * a.kact + k) * 4;
+        // Built incrementally: entry m is entry (m without its highest
+        // state h) plus P[i][h], which is the same sum in the same order.
+        double T[16];
+        T[0] = 0.0;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                double acc = 0.0;
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    if (mask & (1 << j)) acc = __dadd_rn(acc, P[i * 4 + j]);
-                t[i] = acc;
-            }
+        for (int mk = 1; mk < 16; ++mk) {
+            const int h = mk >= 8 ? 3 : mk >= 4 ? 2 : mk >= 2 ? 1 : 0;
+            T[mk] = __dadd_rn(T[mk ^ (1 << h)], P[h]);
         }
+        if (a.precision == CXG_FP32) {
+            float *o = reinterpret_cast<float *>(dst) + (size_t)k * 4 + i;
+#pragma unroll
+            for (int mk = 0; mk < 16; ++mk) o[(size_t)mk * a.kact * 4] = (float)T[mk];
+            return;
+        }
+        double *tt = a.ltab + ((size_t)tb * 16 * a.kact + k) * 4 + i;
+#pragma unroll
+        for (int mk = 0; mk < 16; ++mk) tt[(size_t)mk * a.kact * 4] = T[mk];
     }
     if (a.precision == CXG_FP32) {
-        float *o = reinterpret_cast<float *>(dst) + (size_t)k * 16;
+        float *o = reinterpret_cast<float *>(dst) + (size_t)k * 16 + i * 4;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) o[q] = (float)P[q];
+        for (int j = 0; j < 4; ++j) o[j] = (float)P[j];
     } else {
-        double *o = reinterpret_cast<double *>(dst) + (size_t)k * 16;
+        double *o = reinterpret_cast<double *>(dst) + (size_t)k * 16 + i * 4;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) o[q] = P[q];
+        for (int j = 0; j < 4; ++j) o[j] = P[j];
     }
 }
 

@@ -33,38 +33,38 @@ namespace cxg {
 // ---------------------------------------------------------------------------
 // P matrices, written into the op records.
 // ---------------------------------------------------------------------------
+// Four lanes per (child edge, component), see pmat_one.
 __global__ void pmat_kernel(PmatArgs a) {
-    const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= a.nchild * a.kact) return;
-    pmat_one(a, idx);
+    const unsigned idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+    if (idx >= a.nchild * a.kact) return;  // the same for all four lanes
+    pmat_one(a, idx, threadIdx.x & 3u);
 }
 
-// P matrices of many jobs in one launch: thread t belongs to the job whose
-// prefix range [prefix[j], prefix[j+1]) holds it.
+// P matrices of many jobs in one launch: (edge, component) t belongs to
+// the job whose prefix range [prefix[j], prefix[j+1]) holds it.
 __global__ void pmat_batch_kernel(const PmatArgs *jobs, const uint32_t *prefix,
                                   uint32_t njobs, uint32_t total) {
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned t = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
     if (t >= total) return;
     unsigned lo = 0, hi = njobs;  // find j with prefix[j] <= t < prefix[j+1]
     while (hi - lo > 1) {
         const unsigned mid = (lo + hi) / 2;
         if (prefix[mid] <= t) lo = mid; else hi = mid;
     }
-    pmat_one(jobs[lo], t - prefix[lo]);
+    pmat_one(jobs[lo], t - prefix[lo], threadIdx.x & 3u);
 }
 
 cudaError_t launch_pmat_batch(const PmatArgs *jobs, const uint32_t *prefix,
                               uint32_t njobs, uint32_t total, cudaStream_t s) {
     if (total == 0) return cudaSuccess;
-    pmat_batch_kernel<<<(total + 127) / 128, 128, 0, s>>>(jobs, prefix, njobs,
-                                                          total);
+    pmat_batch_kernel<<<(total + 31) / 32, 128, 0, s>>>(jobs, prefix, njobs, total);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pmat(const PmatArgs &a, cudaStream_t s) {
     const unsigned n = a.nchild * a.kact;
     if (n == 0) return cudaSuccess;
-    pmat_kernel<<<(n + 127) / 128, 128, 0, s>>>(a);
+    pmat_kernel<<<(n + 31) / 32, 128, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -8,15 +8,16 @@
 // 1/(1 + ind * heatDelta), :51).  Here all chains live in HBM and one
 // generation is four kernels, captured together into a CUDA graph:
 //
-//   mc3_propose  one thread per chain: draw the move (Philox), apply it to
-//                the chain's tree or to the spare model slot, list the dirty
+//   mc3_propose  one block per chain: flip in the CL buffers of the last
+//                accepted move, draw the move (Philox), apply it to the
+//                chain's tree or to the spare model slot, list the dirty
 //                internal nodes bottom-up, and write their op records.
 //                Dirty CLs go to each node's spare CL buffer, so a rejected
 //                move costs no restore.
 //   mc3_pmat     P matrices of every child edge of every chain's ops.
 //   walk_batch   the batched plan walker over (chain, pattern tile) items.
-//   mc3_accept   FP64 Metropolis per chain, then the heat swap; accepted
-//                moves flip the spare buffers in; rejected moves are undone.
+//   mc3_accept   FP64 Metropolis per chain, then the heat swap; rejected
+//                tree moves are undone.
 //
 // Moves (weights set by the caller): branch-length multiplier (as the
 // reference: m = exp(lambda (u - 1/2)), Exp(brlenPrior) prior, Hastings
@@ -71,6 +72,9 @@ struct Mc3Prop {
     int32_t type, node, a, c;
     double oldlen, lnPrior, lnHast;
     int32_t model_changed, ndirty;
+    // Set by the accept kernel; the next proposal flips the dirty nodes'
+    // CL buffers in when it is set.
+    int32_t accepted;
     // SPR undo: subtree s, its parent p, p's old parent g and other child b,
     // target x and its parent xp in the pruned tree; child slots of p in g,
     // of b in p and of x in xp; the old lengths of b, p and x.
@@ -88,7 +92,6 @@ struct Mc3Dev {
     double *len;          // [2][c][nnodes]
     uint8_t *curtree;     // [c]
     uint8_t *cur;         // [c][nnodes]
-    uint8_t *dirtyflag;   // [c][nnodes]
     int32_t *dirty;       // [c][M] dirty internal nodes, bottom-up
     int32_t *stack;       // [c][nnodes] DFS scratch
     void **cl_data;       // [c][M][2]
@@ -349,6 +352,15 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
     for (unsigned i = threadIdx.x; i < NN * 3; i += blockDim.x) child[i] = g_child[i];
     __syncthreads();
     Mc3Prop &pr = d.prop[c];
+    {
+        // The previous generation's accepted move: its dirty nodes' spare
+        // CL buffers become current.
+        const int prev_acc = pr.accepted, prev_nd = pr.ndirty;
+        if (prev_acc)
+            for (int i = threadIdx.x; i < prev_nd; i += blockDim.x)
+                cur[d.dirty[(size_t)c * M + i]] ^= 1;
+        __syncthreads();
+    }
     __shared__ int s_nd, s_lowest;
     __shared__ unsigned s_fin;
     __shared__ bool s_full, s_etbr;
@@ -861,6 +873,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         }
         for (unsigned i = threadIdx.x; i < NN * 3; i += blockDim.x) o_child[i] = child[i];
     }
+    for (unsigned i = threadIdx.x; i < NN; i += blockDim.x) d.cur[(size_t)c * NN + i] = cur[i];
     for (int i = threadIdx.x; i < nd; i += blockDim.x)
         d.dirty[(size_t)c * M + i] = dirty[i];
     if (threadIdx.x == 0) {
@@ -871,9 +884,10 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
     }
 }
 
-// P matrices of every chain's child edges: thread per (chain, kid, comp).
+// P matrices of every chain's child edges.
 __global__ void mc3_pmat_kernel(Mc3Dev d) {
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    // Four lanes per (chain, kid, comp), see pmat_one.
+    const unsigned t = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
     const unsigned per = d.maxkids * d.kact;
     const unsigned c = t / per, r = t % per;
     if (c >= d.nchains || r >= d.nkids[c] * d.kact) return;
@@ -896,7 +910,7 @@ __global__ void mc3_pmat_kernel(Mc3Dev d) {
     a.wnorm_dev = nullptr;
     a.rec = d.rec + (size_t)c * d.M * d.rstride;
     a.ltab = d.ltab + (size_t)c * d.maxkids * 16 * d.kact * 4;
-    pmat_one(a, r);
+    pmat_one(a, r, threadIdx.x & 3u);
 }
 
 // One block; thread c decides chain c, then thread 0 tries the heat swap.
@@ -923,13 +937,8 @@ __global__ void mc3_accept_kernel(Mc3Dev d) {
                 exp(((lnL1 - d.lnL[c]) + pr.lnPrior) * d.heat[c] + pr.lnHast);
             accept = (p >= u) && (p > 0.0) && isfinite(lnL1);
         }
-        uint8_t *cur = d.cur + (size_t)c * NN;
-        uint8_t *dflag = d.dirtyflag + (size_t)c * NN;
-        const int32_t *dirty = d.dirty + (size_t)c * d.M;
-        for (int i = 0; i < pr.ndirty; ++i) {
-            if (accept) cur[dirty[i]] ^= 1;
-            dflag[dirty[i]] = 0;
-        }
+        // The dirty nodes' CL buffers flip in the next proposal kernel.
+        pr.accepted = accept ? 1 : 0;
         if (accept) {
             d.lnL[c] = lnL1;
             if (pr.model_changed) d.curmodel[c] ^= 1;
@@ -1201,7 +1210,6 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
         (rc = mc3_upload(h, &d.len, len_all.data(), len_all.size())) ||
         (rc = mc3_upload<uint8_t>(h, &d.curtree, nullptr, C)) ||
         (rc = mc3_upload<uint8_t>(h, &d.cur, nullptr, (size_t)C * NN)) ||
-        (rc = mc3_upload<uint8_t>(h, &d.dirtyflag, nullptr, (size_t)C * NN)) ||
         (rc = mc3_upload<int32_t>(h, &d.dirty, nullptr, (size_t)C * M)) ||
         (rc = mc3_upload<int32_t>(h, &d.stack, nullptr, (size_t)C * NN)) ||
         (rc = mc3_upload(h, &d.model, models.data(), models.size())) ||
@@ -1331,7 +1339,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
         return fail(CXG_EINVAL, "cxgMc3Create: walker does not fit an SM");
     }
     h->grid = (unsigned)(per * nsm);
-    h->pmat_grid = (C * d.maxkids * K + 127) / 128;
+    h->pmat_grid = (C * d.maxkids * K + 31) / 32;
     h->propose_smem = mc3_propose_smem(NN, M);
     {  // (the default limit counts the kernel's static shared memory too)
         e = cudaFuncSetAttribute(mc3_propose_kernel,
