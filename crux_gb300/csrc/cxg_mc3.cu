@@ -54,12 +54,13 @@ namespace cxg {
 
 enum {
     MV_BRLEN = 0, MV_NNI = 1, MV_RATES = 2, MV_ALPHA = 3, MV_FREQS = 4, MV_SPR = 5,
-    MV_ETBR = 6, MV_INIT = 7
+    MV_ETBR = 6, MV_INVAR = 7, MV_INIT = 8
 };
-constexpr int kMoves = 7;
+constexpr int kMoves = 8;
 
 struct Mc3Model {
     double rates[6], freqs[4], alpha;
+    double wvar, winvar;  // mixture weights of the variable and +I parts
     double pinorm[4], qnorm, cube[64], eig[4];
     double cmult[kMaxComps], rmult[kMaxComps];
     int32_t midx[kMaxComps];
@@ -84,6 +85,7 @@ struct Mc3Prop {
 
 struct Mc3Dev {
     uint32_t nchains, ntaxa, nnodes, root, kact, npat, ppad, prec;
+    uint32_t ncat, invar;  // kact = ncat Gamma categories (+1 with +I)
     uint32_t rstride, M, maxkids, ntiles;
     // Two tree buffers per chain, b = curtree[c] current: buffer b of
     // chain c starts at (b * nchains + c) * nnodes entries.
@@ -115,7 +117,7 @@ struct Mc3Dev {
     unsigned *counter;
     double wcdf[kMoves];
     double brlen_lambda, brlen_prior, rate_conc, alpha_lambda, alpha_prior;
-    double freq_conc, etbr_pext;
+    double freq_conc, etbr_pext, invar_lambda, invar_prior;
     uint32_t swap_stride;
     uint32_t *acc, *rej;  // [c][kMoves]
     uint32_t *nswap;      // [c]
@@ -127,27 +129,39 @@ struct Mc3Dev {
 };
 
 // wNorm and the root weights of a model whose eigensystem and category
-// rates are set (Lik.pyx:1603-1665; every category has weight 1/ncat).
-__device__ void mc3_model_weights(Mc3Model &m, unsigned ncat) {
+// rates are set (Lik.pyx:1603-1665).  Component weights as Lik.setWVar /
+// setWInvar leave them: wVar / ncat for each Gamma category and wInvar for
+// the +I component (cmult 0), each scaled by their sum; the +I component
+// stays out of wNorm.
+__device__ void mc3_model_weights(Mc3Model &m, unsigned ncat, unsigned invar) {
+    const unsigned K = ncat + (invar ? 1u : 0u);
+    double cw[kMaxComps], wsum = 0.0;
+    for (unsigned k = 0; k < ncat; ++k) cw[k] = m.wvar / ncat;
+    if (invar) {
+        cw[ncat] = m.winvar;
+        m.cmult[ncat] = 0.0;
+    }
+    for (unsigned k = 0; k < K; ++k) wsum += cw[k];
     double qmean = 0.0;
-    const double w = 1.0 / ncat;
-    for (unsigned k = 0; k < ncat; ++k) {
+    for (unsigned k = 0; k < K; ++k) {
+        const double ws = cw[k] / wsum;
         m.rmult[k] = 1.0;
         m.midx[k] = 0;
-        if (m.cmult[k] != 0.0) qmean += w * (1.0 / m.qnorm);
+        if (ws != 0.0 && m.cmult[k] != 0.0) qmean += ws * (1.0 / m.qnorm);
+        for (int i = 0; i < 4; ++i) m.pn[k * 4 + i] = m.pinorm[i] * ws;
     }
     m.wnorm = 1.0 / qmean;
-    for (unsigned k = 0; k < ncat; ++k)
-        for (int i = 0; i < 4; ++i) m.pn[k * 4 + i] = m.pinorm[i] * w;
     m.ok = 1;
 }
 
 // Model derived quantities: Q eigensystem (FP64 Jacobi on the device),
 // Gamma category rates, wNorm and the root weights (Lik.pyx:1603-1665).
 // `what` names the parts whose inputs changed (FIN_EIG: rates or
-// frequencies, FIN_GAMMA: alpha); the others are kept.
-enum : unsigned { FIN_EIG = 1, FIN_GAMMA = 2, FIN_ALL = 3 };
-__device__ bool mc3_model_finish(Mc3Model &m, unsigned ncat, unsigned what = FIN_ALL) {
+// frequencies, FIN_GAMMA: alpha, FIN_WEIGHTS: the +I weights only); the
+// others are kept.
+enum : unsigned { FIN_EIG = 1, FIN_GAMMA = 2, FIN_ALL = 3, FIN_WEIGHTS = 4 };
+__device__ bool mc3_model_finish(Mc3Model &m, unsigned ncat, unsigned invar,
+                                 unsigned what = FIN_ALL) {
     if (what & FIN_EIG) {
         double tmp[74];
         qdecomp4(m.rates, m.freqs, tmp);
@@ -164,14 +178,15 @@ __device__ bool mc3_model_finish(Mc3Model &m, unsigned ncat, unsigned what = FIN
             m.cmult[0] = 1.0;
         }
     }
-    mc3_model_weights(m, ncat);
+    mc3_model_weights(m, ncat, invar);
     return true;
 }
 
 // The same with one warp: lanes 0..ncat-2 compute the Gamma category cuts
 // while lane 31 forms the eigensystem; lane 0 finishes.  All 32 lanes of
 // the warp call it; the result (true: decomposed) is lane 0's.
-__device__ bool mc3_model_finish_warp(Mc3Model &m, unsigned ncat, unsigned what) {
+__device__ bool mc3_model_finish_warp(Mc3Model &m, unsigned ncat, unsigned invar,
+                                      unsigned what) {
     __shared__ double s_cut[kMaxComps];
     __shared__ int s_bad;
     const unsigned lane = threadIdx.x & 31u;
@@ -207,7 +222,7 @@ __device__ bool mc3_model_finish_warp(Mc3Model &m, unsigned ncat, unsigned what)
             m.cmult[0] = 1.0;
         }
     }
-    mc3_model_weights(m, ncat);
+    mc3_model_weights(m, ncat, invar);
     return true;
 }
 
@@ -215,7 +230,7 @@ __global__ void mc3_init_kernel(Mc3Dev d) {
     const unsigned c = blockIdx.x;
     if (threadIdx.x != 0 || c >= d.nchains) return;
     Mc3Model &m = d.model[c * 2 + d.curmodel[c]];
-    if (!mc3_model_finish(m, d.kact)) atomicOr(d.status, 1u);
+    if (!mc3_model_finish(m, d.ncat, d.invar)) atomicOr(d.status, 1u);
 }
 
 // log density of Dirichlet(alpha) at x (both length n).
@@ -389,7 +404,8 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             int t = 0;
             while (t < kMoves - 1 && u >= d.wcdf[t]) ++t;
             if ((t == MV_NNI || t == MV_SPR) && N < 4) t = MV_BRLEN;
-            if (t == MV_ALPHA && d.kact < 2) t = MV_BRLEN;
+            if (t == MV_ALPHA && d.ncat < 2) t = MV_BRLEN;
+            if (t == MV_INVAR && !d.invar) t = MV_BRLEN;
             pr.type = t;
             if (t == MV_BRLEN) {
                 // Uniform edge = uniform non-root node (Chain.pyx:442-447).
@@ -589,6 +605,21 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                     pr.lnPrior = -INFINITY;
                     lowest = (int)d.root;
                 }
+            } else if (t == MV_INVAR) {
+                // Multiplier on wVar or wInvar (invarPropose,
+                // Chain.pyx:379-436): Exp(1 - invarPrior) and
+                // Exp(invarPrior) priors, Hastings ln m.
+                const unsigned which = philox_below(rng, 2);
+                const double lnM = d.invar_lambda * (philox_u01(rng) - 0.5);
+                m1 = m0;
+                double &w = which == 0 ? m1.wvar : m1.winvar;
+                const double w0 = w, w1 = w0 * exp(lnM);
+                w = w1;
+                pr.lnPrior = -(which == 0 ? 1.0 - d.invar_prior : d.invar_prior) * (w1 - w0);
+                pr.lnHast = lnM;
+                pr.model_changed = 1;
+                s_fin = FIN_WEIGHTS;
+                full = true;
             } else if (t == MV_FREQS) {
                 // Base frequencies ~ Dirichlet(conc * pi).
                 double f0[4], f1[4], a0[4], a1[4], s0 = 0.0, s1 = 0.0;
@@ -684,7 +715,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
     // 0 lists the dirty nodes and assigns stack slots.
     if (threadIdx.x >= 32 && threadIdx.x < 64 && s_fin) {
         Mc3Model &m1 = d.model[c * 2 + (1 - d.curmodel[c])];
-        const bool ok = mc3_model_finish_warp(m1, d.kact, s_fin);
+        const bool ok = mc3_model_finish_warp(m1, d.ncat, d.invar, s_fin);
         if (threadIdx.x == 32 && !ok) {
             // A model that cannot be decomposed is rejected outright.
             pr.lnPrior = -INFINITY;
@@ -1077,8 +1108,11 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     if (cfg == nullptr || out == nullptr) return fail(CXG_EINVAL, "cxgMc3Create: NULL");
     const unsigned N = cfg->ntaxa;
     if (N < 3 || N > 3000) return fail(CXG_EINVAL, "cxgMc3Create: 3..3000 taxa");
-    if (cfg->ncat < 1 || cfg->ncat > kMaxComps)
-        return fail(CXG_EINVAL, "cxgMc3Create: 1..8 rate categories");
+    if (!(cfg->pinv >= 0.0 && cfg->pinv < 1.0))
+        return fail(CXG_EINVAL, "cxgMc3Create: pinv must be in [0, 1)");
+    const unsigned invar = cfg->pinv > 0.0 ? 1u : 0u;
+    if (cfg->ncat < 1 || cfg->ncat + invar > kMaxComps)
+        return fail(CXG_EINVAL, "cxgMc3Create: 1..8 components (rate categories, +I)");
     if (cfg->nchains < 1 || cfg->nchains > 1024)
         return fail(CXG_EINVAL, "cxgMc3Create: 1..1024 chains");
     if (cfg->precision != CXG_FP32 && cfg->precision != CXG_FP64)
@@ -1108,7 +1142,9 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     h->cfg = *cfg;
     Mc3Dev &d = h->d;
     memset(&d, 0, sizeof(d));
-    const unsigned C = cfg->nchains, K = cfg->ncat;
+    const unsigned C = cfg->nchains, K = cfg->ncat + invar;
+    d.ncat = cfg->ncat;
+    d.invar = invar;
     d.nchains = C;
     d.ntaxa = N;
     d.nnodes = NN;
@@ -1147,15 +1183,19 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     }
     d.seed = cfg->seed;
     d.swap_stride = cfg->swap_stride ? cfg->swap_stride : 1;
-    double wsum = 0.0;
-    for (int i = 0; i < kMoves; ++i) wsum += cfg->move_weight[i];
+    // Without a +I component the +I weight move has nothing to change
+    // (the reference disables PropInvar then, Mc3/__init__.pyx:934-937).
+    double mw[kMoves], wsum = 0.0;
+    for (int i = 0; i < kMoves; ++i) mw[i] = cfg->move_weight[i];
+    if (!invar) mw[MV_INVAR] = 0.0;
+    for (int i = 0; i < kMoves; ++i) wsum += mw[i];
     if (!(wsum > 0.0)) {
         mc3_free(h);
         return fail(CXG_EINVAL, "cxgMc3Create: all move weights are zero");
     }
     double acc = 0.0;
     for (int i = 0; i < kMoves; ++i) {
-        acc += cfg->move_weight[i] / wsum;
+        acc += mw[i] / wsum;
         d.wcdf[i] = (i == kMoves - 1) ? 2.0 : acc;
     }
     d.brlen_lambda = cfg->brlen_lambda;
@@ -1169,6 +1209,12 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     d.etbr_pext = cfg->etbr_pext;
     d.alpha_lambda = cfg->alpha_lambda;
     d.alpha_prior = cfg->alpha_prior;
+    d.invar_lambda = cfg->invar_lambda;
+    d.invar_prior = cfg->invar_prior;
+    if (invar && !(cfg->invar_prior > 0.0 && cfg->invar_prior < 1.0)) {
+        mc3_free(h);
+        return fail(CXG_EINVAL, "cxgMc3Create: invar_prior must be in (0, 1)");
+    }
     d.trace_cap = cfg->trace_cap;
     int rc = 0;
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
@@ -1192,6 +1238,8 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
         for (int i = 0; i < 6; ++i) m.rates[i] = cfg->rates[i];
         for (int i = 0; i < 4; ++i) m.freqs[i] = cfg->freqs[i];
         m.alpha = cfg->alpha;
+        m.wvar = invar ? 1.0 - cfg->pinv : 1.0;
+        m.winvar = invar ? cfg->pinv : 0.0;
     }
     // Leaf masks (0 = any state, as Lik.pyx:1469-1470), pattern weights.
     std::vector<uint8_t> masks((size_t)N * d.ppad, 15);
@@ -1458,6 +1506,21 @@ extern "C" int cxgMc3Chain(cxgMc3 *h, unsigned chain, double *lnL, double *heat,
     if (rates) memcpy(rates, m.rates, 48);
     if (freqs) memcpy(freqs, m.freqs, 32);
     if (alpha) *alpha = m.alpha;
+    return 0;
+}
+
+extern "C" int cxgMc3ChainWeights(cxgMc3 *h, unsigned chain, double *wvar, double *winvar) {
+    if (h == nullptr || chain >= h->d.nchains)
+        return fail(CXG_EINVAL, "cxgMc3ChainWeights: bad chain");
+    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    const Mc3Dev &d = h->d;
+    CXG_CUDA(cudaStreamSynchronize(h->stream));
+    uint8_t cm = 0;
+    CXG_CUDA(cudaMemcpy(&cm, d.curmodel + chain, 1, cudaMemcpyDeviceToHost));
+    Mc3Model m;
+    CXG_CUDA(cudaMemcpy(&m, d.model + chain * 2 + cm, sizeof(m), cudaMemcpyDeviceToHost));
+    if (wvar) *wvar = m.wvar;
+    if (winvar) *winvar = m.winvar;
     return 0;
 }
 

@@ -380,7 +380,7 @@ int upload_dataset(unsigned N, unsigned npat, const uint8_t *masks,
 size_t mc3_bytes(const cxgRequest &r, int prec, unsigned nc) {
     const size_t elt = prec == CXG_FP32 ? 4 : 8;
     const size_t ppad = pad_patterns(r.npat), N = r.ntaxa, M = N - 2;
-    const size_t K = r.ncat;
+    const size_t K = r.ncat + (r.pinv > 0.0 ? 1 : 0);
     const size_t rstride =
         sizeof(RecHead) + 3 * (sizeof(RecChild) + std::max(child_area_bytes(prec, K, true),
                                                            child_area_bytes(prec, K, false))) +
@@ -861,6 +861,9 @@ void mc3_loop(cxgServer *S) {
             c.rate_conc = 300.0;
             c.alpha_lambda = 2.0 * log(1.6);
             c.alpha_prior = 1.0;
+            c.pinv = r.pinv;
+            c.invar_lambda = 2.0 * log(1.6);
+            c.invar_prior = 0.5;
             c.precision = S->cfg.precision;
             c.graph_gens = r.mc3_gens ? r.mc3_gens : 10;
             c.trace_cap = 1;
@@ -953,8 +956,6 @@ extern "C" int cxgServerSubmit(cxgServer *S, const cxgRequest *r,
         return fail(CXG_EINVAL, "cxgServerSubmit: bad request shape");
     if (r->kind != CXG_REQ_LNL && r->kind != CXG_REQ_MC3)
         return fail(CXG_EINVAL, "cxgServerSubmit: unknown request kind");
-    if (r->kind == CXG_REQ_MC3 && r->pinv > 0.0)
-        return fail(CXG_EINVAL, "cxgServerSubmit: MC3 requests take no +I component");
     const unsigned N = r->ntaxa, NN = 2 * N - 2;
     if (r->root < N || r->root >= NN) return fail(CXG_EINVAL, "cxgServerSubmit: bad root");
     std::vector<int> nch(NN, 0);

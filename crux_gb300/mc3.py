@@ -20,7 +20,7 @@ from .alignment import Alignment, TaxaMap
 from .tree import Tree
 
 LAMBDA = 2.0 * math.log(1.6)
-MOVES = ("brlen", "nni", "rates", "alpha", "freqs", "spr", "etbr")
+MOVES = ("brlen", "nni", "rates", "alpha", "freqs", "spr", "etbr", "invar")
 
 
 class Mc3Config(ctypes.Structure):
@@ -40,7 +40,7 @@ class Mc3Config(ctypes.Structure):
         ("heat_delta", ctypes.c_double),
         ("swap_stride", ctypes.c_uint),
         ("seed", ctypes.c_ulonglong),
-        ("move_weight", ctypes.c_double * 7),
+        ("move_weight", ctypes.c_double * 8),
         ("brlen_lambda", ctypes.c_double),
         ("brlen_prior", ctypes.c_double),
         ("rate_conc", ctypes.c_double),
@@ -48,6 +48,9 @@ class Mc3Config(ctypes.Structure):
         ("etbr_pext", ctypes.c_double),
         ("alpha_lambda", ctypes.c_double),
         ("alpha_prior", ctypes.c_double),
+        ("pinv", ctypes.c_double),
+        ("invar_lambda", ctypes.c_double),
+        ("invar_prior", ctypes.c_double),
         ("precision", ctypes.c_int),
         ("graph_gens", ctypes.c_uint),
         ("trace_cap", ctypes.c_ulonglong),
@@ -66,6 +69,9 @@ def declare(lib):
                                 P(ctypes.c_double), P(ctypes.c_double),
                                 P(ctypes.c_double), P(ctypes.c_double)]
     lib.cxgMc3Chain.restype = ctypes.c_int
+    lib.cxgMc3ChainWeights.argtypes = [vp, ctypes.c_uint, P(ctypes.c_double),
+                                       P(ctypes.c_double)]
+    lib.cxgMc3ChainWeights.restype = ctypes.c_int
     lib.cxgMc3Stats.argtypes = [vp, P(ctypes.c_uint), P(ctypes.c_uint),
                                 P(ctypes.c_uint), P(ctypes.c_ulonglong)]
     lib.cxgMc3Stats.restype = ctypes.c_int
@@ -144,7 +150,7 @@ class Mc3:
                  nchains=4, heat_delta=0.05, swap_stride=1, seed=1,
                  moves=None, precision="fp32", brlen_lambda=LAMBDA,
                  brlen_prior=10.0, rate_conc=300.0, freq_conc=300.0,
-                 etbr_pext=0.8,
+                 etbr_pext=0.8, pinv=0.0, invar_lambda=LAMBDA, invar_prior=0.5,
                  alpha_lambda=LAMBDA,
                  alpha_prior=1.0, graph_gens=16, trace_cap=1 << 20, lib=None):
         self.lib = lib or _native.load()
@@ -187,6 +193,9 @@ class Mc3:
         c.rate_conc = rate_conc
         c.freq_conc = freq_conc
         c.etbr_pext = etbr_pext
+        c.pinv = pinv
+        c.invar_lambda = invar_lambda
+        c.invar_prior = invar_prior
         c.alpha_lambda = alpha_lambda
         c.alpha_prior = alpha_prior
         c.precision = 1 if precision == "fp32" else 0
@@ -195,6 +204,7 @@ class Mc3:
         self.cfg = c
         self.nchains = nchains
         self.ncat = c.ncat
+        self.invar = pinv > 0.0
         self.h = ctypes.c_void_p()
         rc = self.lib.cxgMc3Create(ctypes.byref(c), ctypes.byref(self.h))
         if rc != 0:
@@ -225,9 +235,13 @@ class Mc3:
             par.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
             ln.ctypes.data_as(dp), rates.ctypes.data_as(dp),
             freqs.ctypes.data_as(dp), ctypes.byref(alpha)), "cxgMc3Chain")
+        wv, wi = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.cxgMc3ChainWeights(self.h, i, ctypes.byref(wv),
+                                                ctypes.byref(wi)),
+                    "cxgMc3ChainWeights")
         return {"lnL": lnl.value, "heat": heat.value, "parent": par,
                 "len": ln, "rates": rates, "freqs": freqs,
-                "alpha": alpha.value}
+                "alpha": alpha.value, "wvar": wv.value, "winvar": wi.value}
 
     def stats(self):
         n = self.nchains * len(MOVES)
@@ -260,12 +274,16 @@ class Mc3:
         t = Tree(nw)
         t.deroot()
         t.canonize(aln.taxaMap)
-        lik = Lik(t, aln, ncat=self.ncat, lib=lib, precision=precision)
+        lik = Lik(t, aln, ncat=self.ncat, invar=self.invar, lib=lib,
+                  precision=precision)
         lik.setRclass(0, [0, 1, 2, 3, 4, 5], [float(x) for x in st["rates"]])
         for j in range(4):
             lik.setFreq(0, j, float(st["freqs"][j]))
         if self.ncat > 1:
             lik.setAlpha(0, float(st["alpha"]))
+        if self.invar:
+            lik.setWVar(0, st["wvar"])
+            lik.setWInvar(0, st["winvar"])
         return lik, st
 
     def close(self):

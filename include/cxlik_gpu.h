@@ -264,14 +264,20 @@ typedef struct {
     double heat_delta;  /* chain i runs at heat 1/(1 + i*heat_delta) */
     unsigned swap_stride;
     unsigned long long seed;
-    double move_weight[7];  /* branch length, NNI, rates, alpha, base
-                               frequencies, SPR, eTBR */
+    double move_weight[8];  /* branch length, NNI, rates, alpha, base
+                               frequencies, SPR, eTBR, +I weights */
     double brlen_lambda, brlen_prior;
     double rate_conc;       /* Dirichlet concentration of rate moves */
     double freq_conc;       /* Dirichlet concentration of frequency moves */
     double etbr_pext;       /* eTBR extension probability (the reference's
                                etbrPExt, 0.8), in [0, 1] */
     double alpha_lambda, alpha_prior;
+    double pinv;            /* +I weight (0: no +I component); the
+                               variable part starts at 1 - pinv */
+    double invar_lambda;    /* multiplier of +I weight moves */
+    double invar_prior;     /* the reference's invarPrior (0.5): Exp priors
+                               of rate 1 - invarPrior on wVar and
+                               invarPrior on wInvar */
     int precision;          /* CXG_FP32 or CXG_FP64 */
     unsigned graph_gens;    /* generations per captured graph (0: 16) */
     unsigned long long trace_cap;  /* cold-chain lnL trace length */
@@ -286,7 +292,9 @@ int cxgMc3Run(cxgMc3 *mc3, unsigned long long ngen, double *seconds);
 int cxgMc3Chain(cxgMc3 *mc3, unsigned chain, double *lnL, double *heat,
                 int32_t *parent, double *len, double *rates, double *freqs,
                 double *alpha);
-/* Accept/reject counts [chain][move] (7 moves, in move_weight order),
+/* Mixture weights (wVar, wInvar) of one chain's current model. */
+int cxgMc3ChainWeights(cxgMc3 *mc3, unsigned chain, double *wvar, double *winvar);
+/* Accept/reject counts [chain][move] (8 moves, in move_weight order),
  * swaps [chain], generation count. */
 int cxgMc3Stats(cxgMc3 *mc3, unsigned *accepts, unsigned *rejects,
                 unsigned *swaps, unsigned long long *gen);

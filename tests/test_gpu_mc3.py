@@ -41,7 +41,8 @@ def test_mc3_chains_match_oracle(gpu, port, precision):
     assert st["generation"] == 158
     acc = st["accepts"].sum(axis=0)
     rej = st["rejects"].sum(axis=0)
-    assert (acc + rej).min() > 0                # every move was drawn
+    assert (acc + rej)[:7].min() > 0            # every move but +I drawn
+    assert acc[7] + rej[7] == 0                 # no +I component here
     assert acc[0] > 0 and acc[1] > 0            # brlen and NNI accepted
     assert acc[5] > 0                           # SPR accepted
     assert acc[6] > 0                           # eTBR accepted
@@ -181,3 +182,51 @@ def test_mc3_etbr_chains_match_oracle(gpu, port):
     acc = m.stats()["accepts"].sum(axis=0)
     assert acc[6] > 0
     m.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_mc3_invar_chains_match_oracle(gpu, port, precision):
+    """GTR+G4+I chains (five components) with +I weight, alpha, rate,
+    NNI and eTBR moves: each chain's lnL is the oracle's for its tree,
+    model and weights."""
+    case = synth.Case(16, 1000, 0.1, 41, pinv=0.2)
+    aln = case.alignment()
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=0.5,
+            ncat=4, pinv=0.2, nchains=3, heat_delta=0.2, seed=8,
+            moves={"brlen": 1.0, "invar": 2.0, "alpha": 0.5, "rates": 0.5,
+                   "nni": 0.5, "etbr": 0.5},
+            precision=precision, graph_gens=8)
+    check_chains(m, port, TOL[precision])
+    m.run(120)
+    check_chains(m, port, TOL[precision])
+    st = m.stats()
+    acc = st["accepts"].sum(axis=0)
+    assert acc[7] > 0                           # +I weight moves accepted
+    w = [m.chain_state(i) for i in range(3)]
+    assert any(s["winvar"] != 0.2 for s in w)
+    m.close()
+
+
+def test_mc3_invar_weights_sample_their_prior(gpu):
+    """Without data the +I weight moves sample the reference's priors:
+    wVar ~ Exp(1 - invarPrior) and wInvar ~ Exp(invarPrior), both of mean
+    2 at invarPrior 0.5.  A wrong Hastings ratio or prior term moves the
+    means."""
+    case, aln = _empty_alignment(6, 31)
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=None,
+            pinv=0.3, nchains=4, heat_delta=0.0, seed=5, precision="fp64",
+            graph_gens=32, moves={"invar": 1.0})
+    m.run(2000)
+    wv, wi = [], []
+    for _ in range(1000):
+        m.run(32)
+        for i in range(4):
+            st = m.chain_state(i)
+            assert abs(st["lnL"]) < 1e-9
+            wv.append(st["wvar"])
+            wi.append(st["winvar"])
+    m.close()
+    assert abs(np.mean(wv) - 2.0) < 0.25, np.mean(wv)
+    assert abs(np.mean(wi) - 2.0) < 0.25, np.mean(wi)

@@ -135,3 +135,29 @@ def test_raw_dataset_compacted_on_device(gpu):
     srv.close()
     assert va == vb
     assert la == lb
+
+
+def test_mc3_request_with_invariant_sites(gpu):
+    """An MC3-step request of a GTR+G4+I model runs five-component chains:
+    its cold-chain lnL is the one the same chains give through the MC3
+    API (same seed, moves and heats)."""
+    import math
+    from crux_gb300.mc3 import LAMBDA, Mc3
+    case = synth.Case(12, 800, 0.1, 57, pinv=0.25)
+    req = PreparedRequest(case, MC3, mc3_gens=10, mc3_chains=2, seed=9)
+    srv = Server("fp64")
+    got = srv.wait(srv.submit(req))[0]
+    srv.close()
+    aln = req.alignment
+    m = Mc3(case.tree(aln.taxaMap), aln, case.params["rates"],
+            case.params["freqs"], alpha=case.alpha, ncat=case.ncat,
+            pinv=0.25, nchains=2, heat_delta=0.1, seed=9,
+            moves={"brlen": 1.0, "nni": 1.0}, precision="fp64",
+            graph_gens=10, trace_cap=1, brlen_lambda=2.0 * math.log(1.6),
+            alpha_lambda=LAMBDA, etbr_pext=0.0)
+    m.run(10)
+    want = [m.chain_state(i) for i in range(2)]
+    m.close()
+    cold = [s["lnL"] for s in want if s["heat"] == 1.0]
+    assert math.isfinite(got)
+    assert got == cold[0]
