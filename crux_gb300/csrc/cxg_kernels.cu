@@ -866,6 +866,19 @@ __device__ bool walk_tile2(const PlanArgs &a, unsigned tile_idx, const SmemLayou
     return true;
 }
 
+// A batched job's arguments, copied into shared memory when a CTA's next
+// item belongs to another job: read through a pointer into global memory,
+// every field would be reloaded after each store the walker makes.  The
+// previous item ended with a block barrier, so no thread still reads the
+// old copy.
+static_assert(sizeof(PlanArgs) % 8 == 0, "PlanArgs is copied in 8-byte words");
+__device__ __forceinline__ void load_job(PlanArgs &dst, const PlanArgs *src) {
+    const unsigned long long *s = reinterpret_cast<const unsigned long long *>(src);
+    unsigned long long *d = reinterpret_cast<unsigned long long *>(&dst);
+    for (unsigned i = threadIdx.x; i < sizeof(PlanArgs) / 8; i += blockDim.x) d[i] = s[i];
+    __syncthreads();
+}
+
 __device__ __forceinline__ void init_ring(const SmemLayout &Lay, unsigned R) {
     extern __shared__ __align__(128) unsigned char smem[];
     if (threadIdx.x == 0) {
@@ -892,12 +905,14 @@ __global__ void __launch_bounds__(kMaxThreads) walk_kernel(PlanArgs a) {
 template <typename T, int KT, int G, bool STAGED>
 __global__ void __launch_bounds__(kMaxThreads) walk_batch_kernel(BatchArgs b) {
     __shared__ unsigned s_item;
+    __shared__ __align__(16) PlanArgs s_job;
     const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT * G,
                                        blockDim.x / G, b.max_nslot,
                                        b.ring, b.max_rstride, b.max_lmax,
                                        b.max_nleaf);
     init_ring(Lay, b.ring);
     uint32_t phase = 0;
+    unsigned job = ~0u;
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);
         __syncthreads();
@@ -905,7 +920,11 @@ __global__ void __launch_bounds__(kMaxThreads) walk_batch_kernel(BatchArgs b) {
         __syncthreads();
         if (item >= b.nitems) break;
         const WalkItem it = b.items[item];
-        if (!walk_tile<T, KT, G, STAGED>(b.jobs[it.job], it.tile, Lay, b.ring, phase)) break;
+        if (it.job != job) {
+            load_job(s_job, b.jobs + it.job);
+            job = it.job;
+        }
+        if (!walk_tile<T, KT, G, STAGED>(s_job, it.tile, Lay, b.ring, phase)) break;
     }
 }
 
@@ -922,6 +941,8 @@ __global__ void __launch_bounds__(kBlock) walk_kernel2(PlanArgs a) {
 template <int K, bool STAGED>
 __global__ void __launch_bounds__(kBlock) walk_batch_kernel2(BatchArgs b) {
     __shared__ unsigned s_item;
+    __shared__ __align__(16) PlanArgs s_job;
+    unsigned job = ~0u;
     const SmemLayout Lay = smem_layout(CXG_FP32, K, blockDim.x * 2, b.max_nslot, b.ring,
                                        b.max_rstride, b.max_lmax, b.max_nleaf);
     init_ring(Lay, b.ring);
@@ -933,7 +954,11 @@ __global__ void __launch_bounds__(kBlock) walk_batch_kernel2(BatchArgs b) {
         __syncthreads();
         if (item >= b.nitems) break;
         const WalkItem it = b.items[item];
-        if (!walk_tile2<K, STAGED>(b.jobs[it.job], it.tile, Lay, b.ring, phase)) break;
+        if (it.job != job) {
+            load_job(s_job, b.jobs + it.job);
+            job = it.job;
+        }
+        if (!walk_tile2<K, STAGED>(s_job, it.tile, Lay, b.ring, phase)) break;
     }
 }
 
