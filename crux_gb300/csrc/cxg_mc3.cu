@@ -54,13 +54,16 @@ namespace cxg {
 
 enum {
     MV_BRLEN = 0, MV_NNI = 1, MV_RATES = 2, MV_ALPHA = 3, MV_FREQS = 4, MV_SPR = 5,
-    MV_ETBR = 6, MV_INVAR = 7, MV_INIT = 8
+    MV_ETBR = 6, MV_INVAR = 7, MV_GAMMAJ = 8, MV_FREQJ = 9, MV_INIT = 10
 };
-constexpr int kMoves = 8;
+constexpr int kMoves = 10;
 
 struct Mc3Model {
     double rates[6], freqs[4], alpha;
     double wvar, winvar;  // mixture weights of the variable and +I parts
+    // 0: Gamma rates off (the reference's alpha = INFINITY: all variable
+    // weight on the first category, rate 1); 0: equal base frequencies.
+    int32_t gamma_on, freqs_est;
     double pinorm[4], qnorm, cube[64], eig[4];
     double cmult[kMaxComps], rmult[kMaxComps];
     int32_t midx[kMaxComps];
@@ -118,6 +121,7 @@ struct Mc3Dev {
     double wcdf[kMoves];
     double brlen_lambda, brlen_prior, rate_conc, alpha_lambda, alpha_prior;
     double freq_conc, etbr_pext, invar_lambda, invar_prior;
+    double gamma_jump_prior, freq_jump_prior;
     uint32_t swap_stride;
     uint32_t *acc, *rej;  // [c][kMoves]
     uint32_t *nswap;      // [c]
@@ -137,6 +141,16 @@ __device__ void mc3_model_weights(Mc3Model &m, unsigned ncat, unsigned invar) {
     const unsigned K = ncat + (invar ? 1u : 0u);
     double cw[kMaxComps], wsum = 0.0;
     for (unsigned k = 0; k < ncat; ++k) cw[k] = m.wvar / ncat;
+    if (ncat > 1 && !m.gamma_on) {
+        // Lik.setAlpha(INFINITY), Lik.pyx:1264-1273: the first category
+        // takes all the variable weight at rate 1, the others weight 0.
+        cw[0] = m.wvar;
+        m.cmult[0] = 1.0;
+        for (unsigned k = 1; k < ncat; ++k) {
+            cw[k] = 0.0;
+            m.cmult[k] = 0.0;
+        }
+    }
     if (invar) {
         cw[ncat] = m.winvar;
         m.cmult[ncat] = 0.0;
@@ -172,9 +186,9 @@ __device__ bool mc3_model_finish(Mc3Model &m, unsigned ncat, unsigned invar,
         for (int i = 0; i < 4; ++i) m.eig[i] = tmp[69 + i];
     }
     if (what & FIN_GAMMA) {
-        if (ncat > 1) {
+        if (ncat > 1 && m.gamma_on) {
             if (!d_gamma_rates(m.alpha, (int)ncat, m.cmult)) return false;
-        } else {
+        } else if (ncat == 1) {
             m.cmult[0] = 1.0;
         }
     }
@@ -192,7 +206,7 @@ __device__ bool mc3_model_finish_warp(Mc3Model &m, unsigned ncat, unsigned invar
     const unsigned lane = threadIdx.x & 31u;
     if (lane == 0) s_bad = 0;
     __syncwarp();
-    if ((what & FIN_GAMMA) && ncat > 1 && lane < ncat - 1) {
+    if ((what & FIN_GAMMA) && ncat > 1 && m.gamma_on && lane < ncat - 1) {
         const double cut = d_gamma_cut(m.alpha, (int)ncat, (int)lane);
         if (cut == -1.0)
             s_bad = 1;
@@ -215,10 +229,10 @@ __device__ bool mc3_model_finish_warp(Mc3Model &m, unsigned ncat, unsigned invar
     if (lane != 0) return false;
     if (s_bad) return false;
     if (what & FIN_GAMMA) {
-        if (ncat > 1) {
+        if (ncat > 1 && m.gamma_on) {
             for (unsigned i = 0; i + 1 < ncat; ++i) m.cmult[i] = s_cut[i];
             d_gamma_rates_from_cuts((int)ncat, m.cmult);
-        } else {
+        } else if (ncat == 1) {
             m.cmult[0] = 1.0;
         }
     }
@@ -404,8 +418,13 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             int t = 0;
             while (t < kMoves - 1 && u >= d.wcdf[t]) ++t;
             if ((t == MV_NNI || t == MV_SPR) && N < 4) t = MV_BRLEN;
-            if (t == MV_ALPHA && d.ncat < 2) t = MV_BRLEN;
+            // A move with nothing to change in this state is a branch
+            // move instead, so each jump is drawn with the same
+            // probability on both of its sides.
+            if (t == MV_ALPHA && (d.ncat < 2 || !m0.gamma_on)) t = MV_BRLEN;
             if (t == MV_INVAR && !d.invar) t = MV_BRLEN;
+            if (t == MV_GAMMAJ && d.ncat < 2) t = MV_BRLEN;
+            if (t == MV_FREQS && !m0.freqs_est) t = MV_BRLEN;
             pr.type = t;
             if (t == MV_BRLEN) {
                 // Uniform edge = uniform non-root node (Chain.pyx:442-447).
@@ -619,6 +638,57 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 pr.lnHast = lnM;
                 pr.model_changed = 1;
                 s_fin = FIN_WEIGHTS;
+                full = true;
+            } else if (t == MV_GAMMAJ) {
+                // Gamma rates off or on (rateShapeInvJumpPropose,
+                // Chain.pyx:1346-1450).  Adding draws 1/alpha from its
+                // Exp(alpha_prior) prior; the prior and Jacobian terms are
+                // split between lnPrior and lnHast as the reference does.
+                const double sp = d.alpha_prior;
+                m1 = m0;
+                if (m0.gamma_on) {
+                    const double rsi0 = 1.0 / m0.alpha;
+                    m1.gamma_on = 0;
+                    pr.lnPrior = log(d.gamma_jump_prior) - log(sp) + sp * rsi0;
+                    pr.lnHast = log(sp) - sp * rsi0;
+                } else {
+                    const double rsi1 = -log(1.0 - philox_u01(rng)) / sp;
+                    m1.gamma_on = 1;
+                    m1.alpha = 1.0 / rsi1;
+                    pr.lnPrior = -log(d.gamma_jump_prior) + log(sp) - sp * rsi1;
+                    pr.lnHast = -log(sp) + sp * rsi1;
+                }
+                pr.model_changed = 1;
+                s_fin = FIN_GAMMA;
+                full = true;
+            } else if (t == MV_FREQJ) {
+                // Equal or estimated base frequencies (freqJumpPropose,
+                // Chain.pyx:1547-1631).  Estimated frequencies have a flat
+                // Dirichlet prior (density 3! = 6 on the simplex), so
+                // adding draws them from it: the density appears in
+                // lnPrior and lnHast and cancels, as the reference's Exp(1)
+                // terms do.
+                const double ln6 = 1.791759469228055;
+                m1 = m0;
+                if (m0.freqs_est) {
+                    for (int i = 0; i < 4; ++i) m1.freqs[i] = 0.25;
+                    m1.freqs_est = 0;
+                    pr.lnPrior = log(d.freq_jump_prior) - ln6;
+                    pr.lnHast = ln6;
+                } else {
+                    double f[4], s = 0.0;
+                    for (int i = 0; i < 4; ++i) {
+                        f[i] = -log(1.0 - philox_u01(rng));
+                        if (f[i] < 1e-300) f[i] = 1e-300;
+                        s += f[i];
+                    }
+                    for (int i = 0; i < 4; ++i) m1.freqs[i] = f[i] / s;
+                    m1.freqs_est = 1;
+                    pr.lnPrior = -log(d.freq_jump_prior) + ln6;
+                    pr.lnHast = -ln6;
+                }
+                pr.model_changed = 1;
+                s_fin = FIN_EIG;
                 full = true;
             } else if (t == MV_FREQS) {
                 // Base frequencies ~ Dirichlet(conc * pi).
@@ -1211,6 +1281,13 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     d.alpha_prior = cfg->alpha_prior;
     d.invar_lambda = cfg->invar_lambda;
     d.invar_prior = cfg->invar_prior;
+    d.gamma_jump_prior = cfg->gamma_jump_prior;
+    d.freq_jump_prior = cfg->freq_jump_prior;
+    if ((mw[MV_GAMMAJ] > 0.0 && !(cfg->gamma_jump_prior > 0.0)) ||
+        (mw[MV_FREQJ] > 0.0 && !(cfg->freq_jump_prior > 0.0))) {
+        mc3_free(h);
+        return fail(CXG_EINVAL, "cxgMc3Create: jump priors must be positive");
+    }
     if (invar && !(cfg->invar_prior > 0.0 && cfg->invar_prior < 1.0)) {
         mc3_free(h);
         return fail(CXG_EINVAL, "cxgMc3Create: invar_prior must be in (0, 1)");
@@ -1240,6 +1317,10 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
         m.alpha = cfg->alpha;
         m.wvar = invar ? 1.0 - cfg->pinv : 1.0;
         m.winvar = invar ? cfg->pinv : 0.0;
+        m.gamma_on = cfg->ncat > 1 ? 1 : 0;
+        // Equal frequencies start in the equal state (Chain.freqsEqual).
+        m.freqs_est = !(cfg->freqs[0] == cfg->freqs[1] && cfg->freqs[1] == cfg->freqs[2] &&
+                        cfg->freqs[2] == cfg->freqs[3]);
     }
     // Leaf masks (0 = any state, as Lik.pyx:1469-1470), pattern weights.
     std::vector<uint8_t> masks((size_t)N * d.ppad, 15);
@@ -1505,7 +1586,8 @@ extern "C" int cxgMc3Chain(cxgMc3 *h, unsigned chain, double *lnL, double *heat,
     CXG_CUDA(cudaMemcpy(&m, d.model + chain * 2 + cm, sizeof(m), cudaMemcpyDeviceToHost));
     if (rates) memcpy(rates, m.rates, 48);
     if (freqs) memcpy(freqs, m.freqs, 32);
-    if (alpha) *alpha = m.alpha;
+    // Gamma rates switched off read as the reference's alpha = INFINITY.
+    if (alpha) *alpha = (d.ncat > 1 && !m.gamma_on) ? INFINITY : m.alpha;
     return 0;
 }
 

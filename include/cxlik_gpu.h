@@ -264,8 +264,10 @@ typedef struct {
     double heat_delta;  /* chain i runs at heat 1/(1 + i*heat_delta) */
     unsigned swap_stride;
     unsigned long long seed;
-    double move_weight[8];  /* branch length, NNI, rates, alpha, base
-                               frequencies, SPR, eTBR, +I weights */
+    double move_weight[10]; /* branch length, NNI, rates, alpha, base
+                               frequencies, SPR, eTBR, +I weights, Gamma
+                               on/off jump, equal/estimated frequency
+                               jump */
     double brlen_lambda, brlen_prior;
     double rate_conc;       /* Dirichlet concentration of rate moves */
     double freq_conc;       /* Dirichlet concentration of frequency moves */
@@ -278,6 +280,10 @@ typedef struct {
     double invar_prior;     /* the reference's invarPrior (0.5): Exp priors
                                of rate 1 - invarPrior on wVar and
                                invarPrior on wInvar */
+    double gamma_jump_prior; /* the reference's rateShapeInvJumpPrior (1):
+                               prior odds of Gamma off to on */
+    double freq_jump_prior;  /* its freqJumpPrior (1): prior odds of equal
+                               to estimated base frequencies */
     int precision;          /* CXG_FP32 or CXG_FP64 */
     unsigned graph_gens;    /* generations per captured graph (0: 16) */
     unsigned long long trace_cap;  /* cold-chain lnL trace length */
@@ -294,7 +300,7 @@ int cxgMc3Chain(cxgMc3 *mc3, unsigned chain, double *lnL, double *heat,
                 double *alpha);
 /* Mixture weights (wVar, wInvar) of one chain's current model. */
 int cxgMc3ChainWeights(cxgMc3 *mc3, unsigned chain, double *wvar, double *winvar);
-/* Accept/reject counts [chain][move] (8 moves, in move_weight order),
+/* Accept/reject counts [chain][move] (10 moves, in move_weight order),
  * swaps [chain], generation count. */
 int cxgMc3Stats(cxgMc3 *mc3, unsigned *accepts, unsigned *rejects,
                 unsigned *swaps, unsigned long long *gen);

@@ -43,6 +43,7 @@ def test_mc3_chains_match_oracle(gpu, port, precision):
     rej = st["rejects"].sum(axis=0)
     assert (acc + rej)[:7].min() > 0            # every move but +I drawn
     assert acc[7] + rej[7] == 0                 # no +I component here
+    assert (acc + rej)[8:].max() == 0           # no jump moves asked for
     assert acc[0] > 0 and acc[1] > 0            # brlen and NNI accepted
     assert acc[5] > 0                           # SPR accepted
     assert acc[6] > 0                           # eTBR accepted
@@ -230,3 +231,60 @@ def test_mc3_invar_weights_sample_their_prior(gpu):
     m.close()
     assert abs(np.mean(wv) - 2.0) < 0.25, np.mean(wv)
     assert abs(np.mean(wi) - 2.0) < 0.25, np.mean(wi)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_mc3_jump_chains_match_oracle(gpu, port, precision):
+    """Gamma on/off and equal/estimated frequency jumps with the moves
+    inside each state: each chain's lnL is the oracle's for its tree and
+    model, Gamma switched off reading as alpha = INFINITY."""
+    import math
+    # Few sites and hot chains (heats down to 0.1), so that jumps are
+    # accepted now and then.
+    case = synth.Case(16, 100, 0.1, 43, pinv=0.15)
+    aln = case.alignment()
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=0.5,
+            ncat=4, pinv=0.15, nchains=4, heat_delta=3.0, seed=12,
+            moves={"brlen": 1.0, "gammajump": 2.0, "freqjump": 2.0,
+                   "alpha": 0.5, "freqs": 0.5, "invar": 0.5},
+            precision=precision, graph_gens=8)
+    m.run(160)
+    check_chains(m, port, TOL[precision])
+    st = m.stats()
+    acc = st["accepts"].sum(axis=0)
+    rej = st["rejects"].sum(axis=0)
+    assert acc[8] + rej[8] > 0 and acc[9] + rej[9] > 0
+    assert acc[8] + acc[9] > 0
+    m.close()
+
+
+def test_mc3_jumps_sample_their_prior(gpu):
+    """On empty data the jumps sample the model prior: with prior odds 3 of
+    Gamma off (and of equal frequencies), a quarter of the samples have
+    Gamma on (estimated frequencies), and 1/alpha follows its Exp(1) prior
+    while Gamma is on."""
+    import math
+    case, aln = _empty_alignment(6, 33)
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=0.7,
+            ncat=4, nchains=4, heat_delta=0.0, seed=19, precision="fp64",
+            graph_gens=32, gamma_jump_prior=3.0, freq_jump_prior=3.0,
+            moves={"gammajump": 1.0, "freqjump": 1.0, "alpha": 1.0})
+    m.run(2000)
+    on, est, rsi, n = 0, 0, [], 0
+    for _ in range(800):
+        m.run(32)
+        for i in range(4):
+            st = m.chain_state(i)
+            assert abs(st["lnL"]) < 1e-9
+            n += 1
+            if math.isfinite(st["alpha"]):
+                on += 1
+                rsi.append(1.0 / st["alpha"])
+            f = st["freqs"]
+            est += not (f[0] == f[1] == f[2] == f[3])
+    m.close()
+    assert abs(on / n - 0.25) < 0.04, on / n
+    assert abs(est / n - 0.25) < 0.04, est / n
+    assert abs(np.mean(rsi) - 1.0) < 0.15, np.mean(rsi)
