@@ -186,6 +186,8 @@ struct BatchArgs {
     uint32_t max_nslot, max_rstride, max_lmax, max_nleaf;
     uint32_t tpp;         // threads per pattern (all jobs); 0 is read as 1
     uint32_t ppt;         // patterns per thread (all jobs); 0 is read as 1
+    uint32_t direct;      // 1: CTA i walks item i (grid = nitems), no
+                          // counter; launch_batch sets it
 };
 
 size_t plan_smem_bytes(int precision, unsigned kact, unsigned tile, unsigned nslot,

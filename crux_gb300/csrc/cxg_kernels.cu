@@ -913,11 +913,16 @@ __global__ void __launch_bounds__(kMaxThreads) walk_batch_kernel(BatchArgs b) {
     init_ring(Lay, b.ring);
     uint32_t phase = 0;
     unsigned job = ~0u;
-    for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);
-        __syncthreads();
-        const unsigned item = s_item;
-        __syncthreads();
+    for (unsigned n = 0;; ++n) {
+        unsigned item;
+        if (b.direct) {
+            item = n == 0 ? blockIdx.x : b.nitems;
+        } else {
+            if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);
+            __syncthreads();
+            item = s_item;
+            __syncthreads();
+        }
         if (item >= b.nitems) break;
         const WalkItem it = b.items[item];
         if (it.job != job) {
@@ -947,11 +952,16 @@ __global__ void __launch_bounds__(kBlock) walk_batch_kernel2(BatchArgs b) {
                                        b.max_rstride, b.max_lmax, b.max_nleaf);
     init_ring(Lay, b.ring);
     uint32_t phase = 0;
-    for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);
-        __syncthreads();
-        const unsigned item = s_item;
-        __syncthreads();
+    for (unsigned n = 0;; ++n) {
+        unsigned item;
+        if (b.direct) {
+            item = n == 0 ? blockIdx.x : b.nitems;
+        } else {
+            if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);
+            __syncthreads();
+            item = s_item;
+            __syncthreads();
+        }
         if (item >= b.nitems) break;
         const WalkItem it = b.items[item];
         if (it.job != job) {
@@ -1093,8 +1103,16 @@ static cudaError_t launch_batch_t(int precision, const BatchArgs &b,
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch(int precision, const BatchArgs &b, unsigned grid,
+cudaError_t launch_batch(int precision, const BatchArgs &b_in, unsigned grid,
                          cudaStream_t s) {
+    // Items that fit one persistent grid get one CTA each: the hardware
+    // spreads those CTAs over the SMs evenly, where persistent CTAs that
+    // claim items first would crowd onto some SMs.
+    BatchArgs b = b_in;
+    if (b.nitems > 0 && b.nitems <= grid) {
+        b.direct = 1;
+        grid = b.nitems;
+    }
     const unsigned G = b.tpp ? b.tpp : 1, NP = b.ppt ? b.ppt : 1;
     if (b.tile == 0 || b.tile > kBlock || b.tile % 32 || b.tile * G > kMaxThreads ||
         b.tile / NP < 32 || !walker_shape_ok(precision, b.kact, G, NP) || b.ring == 0 ||

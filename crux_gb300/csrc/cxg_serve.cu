@@ -642,7 +642,7 @@ int launch_batch_of(cxgServer *S, SrvBatch &B, cudaStream_t st) {
     CXG_CUDA(launch_pmat_batch((const PmatArgs *)(B.mem + o_pm),
                                (const uint32_t *)(B.mem + o_pre), (uint32_t)n,
                                prefix[n], st));
-    BatchArgs ba;
+    BatchArgs ba{};
     ba.jobs = (const PlanArgs *)(B.mem + o_jobs);
     ba.items = (const WalkItem *)(B.mem + o_items);
     ba.nitems = (uint32_t)items.size();
