@@ -10,14 +10,15 @@
 //      read back); the rank of a character is the position of its
 //      canonical code among those, in byte order, so rank order is byte
 //      order and a rank fits `bits` bits (3 for ACGT, N and gaps).
-//   1. compact_transpose: rows [ntaxa][nsites] -> column-major ranks
-//      [nsites][W] through a shared-memory tile.
-//   2. LSD sort: for each chunk of `cpk` characters, last chunk first, pack
-//      the chunk of every column (in the current order) into a 64-bit key,
-//      first character most significant, and stable-radix-sort (key, column
+//   1. compact_keys: every column's characters, `cpk` to a 64-bit key
+//      (first character most significant, rank order = byte order), as
+//      key[chunk][site], read straight from the row-major input.
+//   2. LSD sort: for each chunk, last first, gather the chunk key of every
+//      column in the current order and stable-radix-sort (key, column
 //      index) pairs (cub::DeviceRadixSort, a CUDA toolkit primitive).
-//   3. compact_flags: a column starts a pattern unless it equals the one
-//      before it (16-byte compares); a scan numbers the patterns.
+//   3. compact_flags: a column starts a pattern unless all its chunk keys
+//      equal those of the column before it (the packing is exact); a scan
+//      numbers the patterns.
 //   4. compact_scatter / compact_emit: the first column of each pattern
 //      represents it, frequencies add (integer atomics: exact), and the
 //      canonical rows and state masks of the patterns are written.
@@ -34,8 +35,6 @@
 namespace cxg {
 namespace {
 
-constexpr unsigned kTT = 32;  // transpose tile (taxa x sites)
-
 // used[c] = 1 for every canonical code c that occurs.
 __global__ void compact_used(const uint8_t *rows, size_t n, const uint8_t *canon,
                              uint32_t *used) {
@@ -50,56 +49,44 @@ __global__ void compact_used(const uint8_t *rows, size_t n, const uint8_t *canon
         if (u[i]) used[i] = 1;
 }
 
-// cols[s][t] = rank[rows[t][s]] for t < ntaxa, 0 (the smallest rank) for
-// the padding taxa up to W.
-__global__ void compact_transpose(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
-                                  unsigned W, const uint8_t *rank, uint8_t *cols) {
-    __shared__ uint8_t t[kTT][kTT + 4];
-    const unsigned s0 = blockIdx.x * kTT, t0 = blockIdx.y * kTT;
-    for (unsigned i = threadIdx.y; i < kTT; i += blockDim.y) {
-        const unsigned tx = t0 + i, sx = s0 + threadIdx.x;
-        t[i][threadIdx.x] =
-            (tx < ntaxa && sx < nsites) ? rank[rows[(size_t)tx * nsites + sx]] : 0;
-    }
-    __syncthreads();
-    for (unsigned i = threadIdx.y; i < kTT; i += blockDim.y) {
-        const unsigned sx = s0 + i, tx = t0 + threadIdx.x;
-        if (sx < nsites && tx < W) cols[(size_t)sx * W + tx] = t[threadIdx.x][i];
-    }
-}
-
-// key[i] = characters [c*cpk, c*cpk + cpk) of column idx[i], `bits` bits
-// each, the first one most significant (beyond W: rank 0).
-__global__ void compact_keys(const uint8_t *cols, unsigned W, const uint32_t *idx,
-                             unsigned n, unsigned c, unsigned bits, unsigned cpk,
-                             unsigned long long *key) {
-    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint8_t *col = cols + (size_t)idx[i] * W;
+// keys[c][s] = ranks of characters [c*cpk, c*cpk + cpk) of column s,
+// `bits` bits each, the first one most significant (rank 0 past ntaxa).
+// Thread per site: each character read is a coalesced row access.
+__global__ void compact_keys(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
+                             const uint8_t *rank, unsigned bits, unsigned cpk,
+                             unsigned long long *keys) {
+    const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned c = blockIdx.y;
+    if (s >= nsites) return;
     unsigned long long k = 0;
     for (unsigned j = 0; j < cpk; ++j) {
         const unsigned t = c * cpk + j;
-        k = (k << bits) | (t < W ? col[t] : 0u);
+        k = (k << bits) | (t < ntaxa ? rank[rows[(size_t)t * nsites + s]] : 0u);
     }
-    key[i] = k;
+    keys[(size_t)c * nsites + s] = k;
 }
 
-// flag[i] = 1 if column idx[i] differs from column idx[i - 1] (or i == 0).
-__global__ void compact_flags(const uint8_t *cols, unsigned W, const uint32_t *idx,
-                              unsigned n, uint32_t *flag) {
+// key[i] = keys[c][idx[i]]: chunk c of the columns in the current order.
+__global__ void compact_gather(const unsigned long long *keys_c, const uint32_t *idx,
+                               unsigned n, unsigned long long *key) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) key[i] = keys_c[idx[i]];
+}
+
+// flag[i] = 1 if column idx[i] differs from column idx[i - 1] (or i == 0):
+// some chunk key differs.
+__global__ void compact_flags(const unsigned long long *keys, unsigned nchunks,
+                              const uint32_t *idx, unsigned n, uint32_t *flag) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (i == 0) {
         flag[0] = 1;
         return;
     }
-    const uint4 *a = reinterpret_cast<const uint4 *>(cols + (size_t)idx[i] * W);
-    const uint4 *b = reinterpret_cast<const uint4 *>(cols + (size_t)idx[i - 1] * W);
+    const size_t a = idx[i], b = idx[i - 1];
     uint32_t diff = 0;
-    for (unsigned q = 0; q < W / 16 && !diff; ++q) {
-        const uint4 x = a[q], y = b[q];
-        diff = (x.x != y.x) | (x.y != y.y) | (x.z != y.z) | (x.w != y.w);
-    }
+    for (unsigned c = 0; c < nchunks && !diff; ++c)
+        diff = keys[(size_t)c * n + a] != keys[(size_t)c * n + b];
     flag[i] = diff;
 }
 
@@ -162,7 +149,8 @@ static void compact_tables(const uint8_t *canon, const uint32_t *used, uint8_t *
 // compact_work_bytes(ntaxa, nsites) bytes.  Waits for the stream once (the
 // codes in use decide the key width).
 size_t compact_work_bytes(unsigned ntaxa, unsigned nsites) {
-    const unsigned W = (ntaxa + 15) / 16 * 16;
+    // Chunk keys for the widest ranks (8 bits: 8 characters a key).
+    const size_t max_chunks = (ntaxa + 7) / 8;
     size_t cub_bytes = 0, scan_bytes = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, (const unsigned long long *)nullptr,
                                     (unsigned long long *)nullptr, (const uint32_t *)nullptr,
@@ -170,7 +158,7 @@ size_t compact_work_bytes(unsigned ntaxa, unsigned nsites) {
     cub::DeviceScan::InclusiveSum(nullptr, scan_bytes, (const uint32_t *)nullptr,
                                   (uint32_t *)nullptr, (int)nsites);
     const size_t n = nsites;
-    return 2048 + al256c(n * W) + 2 * al256c(n * 8) + 4 * al256c(n * 4) +
+    return 2048 + al256c(max_chunks * n * 8) + 2 * al256c(n * 8) + 4 * al256c(n * 4) +
            al256c(cub_bytes > scan_bytes ? cub_bytes : scan_bytes);
 }
 
@@ -179,7 +167,6 @@ int compact_device(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
                    const uint8_t *val, uint8_t any_mask, uint8_t *rows_out, unsigned rstride,
                    uint8_t *masks, unsigned mstride, uint32_t *freq_out, uint32_t *npat_dev,
                    void *work, size_t work_bytes, cudaStream_t s) {
-    const unsigned W = (ntaxa + 15) / 16 * 16;
     const size_t n = nsites;
     if (compact_work_bytes(ntaxa, nsites) > work_bytes)
         return fail(CXG_EINVAL, "compaction: scratch too small");
@@ -202,7 +189,10 @@ int compact_device(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
     unsigned bits = 8;
     compact_tables(canon_host, used_h, rank_h, &bits);
     CXG_CUDA(cudaMemcpyAsync(rank, rank_h, 256, cudaMemcpyHostToDevice, s));
-    uint8_t *cols = (uint8_t *)take(n * W);
+    const unsigned cpk = 64 / bits;
+    const unsigned nchunks = (ntaxa + cpk - 1) / cpk;
+    if (nchunks > 65535) return fail(CXG_EINVAL, "compaction: too many taxa");
+    unsigned long long *keys = (unsigned long long *)take(((size_t)ntaxa + 7) / 8 * n * 8);
     unsigned long long *k0 = (unsigned long long *)take(n * 8);
     unsigned long long *k1 = (unsigned long long *)take(n * 8);
     uint32_t *i0 = (uint32_t *)take(n * 4);
@@ -212,19 +202,16 @@ int compact_device(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
     size_t cub_bytes = work_bytes - (size_t)(p - static_cast<char *>(work));
     void *cub_tmp = p;
 
-    dim3 tb(kTT, 8), tg((nsites + kTT - 1) / kTT, (W + kTT - 1) / kTT);
-    compact_transpose<<<tg, tb, 0, s>>>(rows, ntaxa, nsites, W, rank, cols);
-    CXG_CHECK_LAUNCH("compact_transpose");
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    compact_keys<<<dim3(nb, nchunks), 256, 0, s>>>(rows, ntaxa, nsites, rank, bits, cpk, keys);
+    CXG_CHECK_LAUNCH("compact_keys");
     // Identity order, then one stable sort per key chunk, last chunk first.
     std::vector<uint32_t> iota(n);
     for (size_t i = 0; i < n; ++i) iota[i] = (uint32_t)i;
     CXG_CUDA(cudaMemcpyAsync(i0, iota.data(), n * 4, cudaMemcpyHostToDevice, s));
-    const unsigned cpk = 64 / bits;
-    const unsigned nchunks = (W + cpk - 1) / cpk;
-    const unsigned nb = (unsigned)((n + 255) / 256);
     for (int c = (int)nchunks - 1; c >= 0; --c) {
-        compact_keys<<<nb, 256, 0, s>>>(cols, W, i0, (unsigned)n, (unsigned)c, bits, cpk, k0);
-        CXG_CHECK_LAUNCH("compact_keys");
+        compact_gather<<<nb, 256, 0, s>>>(keys + (size_t)c * n, i0, (unsigned)n, k0);
+        CXG_CHECK_LAUNCH("compact_gather");
         cudaError_t e = cub::DeviceRadixSort::SortPairs(cub_tmp, cub_bytes, k0, k1, i0, i1,
                                                         (int)n, 0, (int)(cpk * bits), s);
         if (e != cudaSuccess) return cuda_fail(e, "compaction radix sort");
@@ -232,7 +219,7 @@ int compact_device(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
         i0 = i1;
         i1 = t;
     }
-    compact_flags<<<nb, 256, 0, s>>>(cols, W, i0, (unsigned)n, flag);
+    compact_flags<<<nb, 256, 0, s>>>(keys, nchunks, i0, (unsigned)n, flag);
     CXG_CHECK_LAUNCH("compact_flags");
     cudaError_t e = cub::DeviceScan::InclusiveSum(cub_tmp, cub_bytes, flag, gid, (int)n, s);
     if (e != cudaSuccess) return cuda_fail(e, "compaction scan");
@@ -255,6 +242,79 @@ int compact_device(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
 using namespace cxg;
 
 static std::mutex g_compact_mu;
+
+// Copies between pageable host arrays and the device go through two pinned
+// chunks (allocated once, kept, guarded by g_compact_mu): the host copies
+// one chunk while the DMA engine moves the other.  Pageable copies run at a
+// small fraction of the DMA rate.
+namespace {
+constexpr size_t kStageChunk = (size_t)32 << 20;
+unsigned char *g_stage[2] = {nullptr, nullptr};
+cudaEvent_t g_stage_ev[2] = {nullptr, nullptr};
+
+int stage_init() {
+    if (g_stage[0]) return 0;
+    unsigned char *p = nullptr;
+    CXG_CUDA(cudaMallocHost((void **)&p, 2 * kStageChunk));
+    cudaError_t e = cudaEventCreateWithFlags(&g_stage_ev[0], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g_stage_ev[1], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        cudaFreeHost(p);
+        return cuda_fail(e, "cxgCompact: staging events");
+    }
+    g_stage[0] = p;
+    g_stage[1] = p + kStageChunk;
+    return 0;
+}
+
+int staged_h2d(void *dst, const void *src, size_t n, cudaStream_t s) {
+    const unsigned char *h = static_cast<const unsigned char *>(src);
+    unsigned char *d = static_cast<unsigned char *>(dst);
+    for (size_t off = 0, i = 0; off < n; off += kStageChunk, ++i) {
+        const int b = (int)(i & 1);
+        const size_t len = n - off < kStageChunk ? n - off : kStageChunk;
+        CXG_CUDA(cudaEventSynchronize(g_stage_ev[b]));  // its last DMA is done
+        memcpy(g_stage[b], h + off, len);
+        CXG_CUDA(cudaMemcpyAsync(d + off, g_stage[b], len, cudaMemcpyHostToDevice, s));
+        CXG_CUDA(cudaEventRecord(g_stage_ev[b], s));
+    }
+    return 0;
+}
+
+// height rows of `width` bytes, device pitch dpitch, into host rows of
+// pitch `width`.
+int staged_d2h_rows(void *dst, const void *src, size_t dpitch, size_t width, size_t height,
+                    cudaStream_t s) {
+    unsigned char *h = static_cast<unsigned char *>(dst);
+    const unsigned char *d = static_cast<const unsigned char *>(src);
+    if (width > kStageChunk) {
+        CXG_CUDA(cudaMemcpy2DAsync(h, width, d, dpitch, width, height, cudaMemcpyDeviceToHost,
+                                   s));
+        CXG_CUDA(cudaStreamSynchronize(s));
+        return 0;
+    }
+    const size_t per = kStageChunk / width;
+    const size_t nblk = (height + per - 1) / per;
+    auto issue = [&](size_t k) -> int {
+        const size_t r0 = k * per, nr = height - r0 < per ? height - r0 : per;
+        const int b = (int)(k & 1);
+        CXG_CUDA(cudaMemcpy2DAsync(g_stage[b], width, d + r0 * dpitch, dpitch, width, nr,
+                                   cudaMemcpyDeviceToHost, s));
+        CXG_CUDA(cudaEventRecord(g_stage_ev[b], s));
+        return 0;
+    };
+    if (int rc = issue(0)) return rc;
+    for (size_t k = 0; k < nblk; ++k) {
+        if (k + 1 < nblk)
+            if (int rc = issue(k + 1)) return rc;
+        const int b = (int)(k & 1);
+        CXG_CUDA(cudaEventSynchronize(g_stage_ev[b]));
+        const size_t r0 = k * per, nr = height - r0 < per ? height - r0 : per;
+        memcpy(h + r0 * width, g_stage[b], nr * width);
+    }
+    return 0;
+}
+}  // namespace
 
 extern "C" int cxgCompact(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
                           const uint32_t *freqs, const uint8_t *canon, const uint8_t *val,
@@ -294,8 +354,8 @@ extern "C" int cxgCompact(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
     memset(tabs, 0, 256);
     memcpy(tabs + 256, canon, 256);
     if (val) memcpy(tabs + 512, val, 256); else memset(tabs + 512, 0, 256);
-    if ((e = cudaMemcpyAsync(d + o_rows, rows, in_bytes, cudaMemcpyHostToDevice, s)) ||
-        (freqs && (e = cudaMemcpyAsync(d + o_freq, freqs, (size_t)nsites * 4,
+    if ((rc = stage_init()) || (rc = staged_h2d(d + o_rows, rows, in_bytes, s))) return fin(rc);
+    if ((freqs && (e = cudaMemcpyAsync(d + o_freq, freqs, (size_t)nsites * 4,
                                        cudaMemcpyHostToDevice, s))) ||
         (e = cudaMemcpyAsync(d + o_tab, tabs, 768, cudaMemcpyHostToDevice, s)))
         return fin(cuda_fail(e, "cxgCompact: upload"));
@@ -311,14 +371,10 @@ extern "C" int cxgCompact(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
         (e = cudaStreamSynchronize(s)))
         return fin(cuda_fail(e, "cxgCompact: pattern count"));
     // Rows and masks come back with row stride npat.
-    if (rows_out && np &&
-        (e = cudaMemcpy2DAsync(rows_out, np, d + o_out, nsites, np, ntaxa,
-                               cudaMemcpyDeviceToHost, s)))
-        return fin(cuda_fail(e, "cxgCompact: rows"));
-    if (masks_out && np &&
-        (e = cudaMemcpy2DAsync(masks_out, np, d + o_mask, nsites, np, ntaxa,
-                               cudaMemcpyDeviceToHost, s)))
-        return fin(cuda_fail(e, "cxgCompact: masks"));
+    if (rows_out && np && (rc = staged_d2h_rows(rows_out, d + o_out, nsites, np, ntaxa, s)))
+        return fin(rc);
+    if (masks_out && np && (rc = staged_d2h_rows(masks_out, d + o_mask, nsites, np, ntaxa, s)))
+        return fin(rc);
     if ((e = cudaMemcpyAsync(freqs_out, d + o_fout, (size_t)np * 4, cudaMemcpyDeviceToHost, s)) ||
         (e = cudaStreamSynchronize(s)))
         return fin(cuda_fail(e, "cxgCompact: frequencies"));
