@@ -163,8 +163,9 @@ def profile_traffic(name):
 
 def autotune(lib, prec, args, lik=None, liks=None):
     """Pick the walker's launch shape (tile, threads per pattern, patterns
-    per thread, stack budget) by timing the candidates on this workload; ``--shape`` fixes it
-    instead.  Returns the shape with how it was chosen."""
+    per thread, stack budget) by timing the candidates on this workload;
+    ``--shape`` fixes it instead.  Returns the shape with how it was
+    chosen."""
     from crux_gb300 import tune
     if args.shape:
         tune.set_shape(lib, *args.shape)
@@ -300,6 +301,15 @@ def run_ours(args, dist):
         lik.lik.invalidate = True
         lik.lnL()
     e2e_s = dist.max((time.perf_counter() - t0) / e2e_runs)
+    # The host planner alone (Lik._plan of a full re-plan), reported apart
+    # from the device work as the reference's planner is.
+    t0 = time.perf_counter()
+    for _ in range(50):
+        lik.lik.invalidate = True
+        lik._prep(None)
+    planner_ms = (time.perf_counter() - t0) / 50 * 1e3
+    lik.lik.invalidate = True
+    lik.lnL()
     h2d, d2h = ctypes.c_size_t(), ctypes.c_size_t()
     gpu.cxgLikLastIo(ctypes.byref(h2d), ctypes.byref(d2h))
     nops = res["fp32"]["info"]["nops"]
@@ -329,6 +339,14 @@ def run_ours(args, dist):
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": "%d full-tree FP64 lnL evaluations (%.1f s)" %
                          (nev, secs)}
+        if kind == "port" and threads > 1:
+            # The same on one core, over a shorter bounded sample.
+            lib.port_set_threads(1)
+            r1, s1, _, n1 = cpu_run(lib, case, aln, 1, 1,
+                                    min_s=args.cpu_seconds / 3)
+            lib.port_set_threads(threads)
+            cpu["single_core"] = {
+                "value": r1, "sample": "%d evaluations (%.1f s)" % (n1, s1)}
 
     if dist.rank == 0:
         fp64 = res["fp64"]
@@ -349,7 +367,8 @@ def run_ours(args, dist):
                                     % (written / 1e9)),
             "e2e": {"value": e2e, "unit": UNIT,
                     "h2d_bytes_per_step": int(h2d.value),
-                    "d2h_bytes_per_step": int(d2h.value)},
+                    "d2h_bytes_per_step": int(d2h.value),
+                    "planner_ms_per_eval": planner_ms},
             "gpu_launches": args.steps * args.batch * info["kernels_per_run"],
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm,

@@ -50,7 +50,8 @@ class CL:
     device holds the data); with a host library they are real arrays.
     """
     __slots__ = ("c", "ptr", "addr", "bufs", "lib", "device", "forget",
-                 "leaf", "valid", "parent", "nSibs", "edgeLen", "__weakref__")
+                 "leaf", "valid", "cvalid", "parent", "nSibs", "edgeLen",
+                 "__weakref__")
 
     def __init__(self, lib, device):
         self.c = (_abi.CxtLikCL(), _abi.CxtLikCL())
@@ -65,7 +66,11 @@ class CL:
         self.forget = hasattr(lib, "cxgLikClForget")
         self.leaf = False
         # Python mirrors of the CxtLikCL cache-key fields, per polarity.
+        # The planner works on the mirrors; the struct's valid field is
+        # brought up to date at the end of each plan (sync_valid), and
+        # cvalid is what the struct holds.
         self.valid = [False, False]
+        self.cvalid = [False, False]
         self.parent = [None, None]
         self.nSibs = [0, 0]
         self.edgeLen = [0.0, 0.0]
@@ -99,11 +104,17 @@ class CL:
         self.c[polarity].valid = False
         self.c[polarity].parent = None
         self.valid[polarity] = False
+        self.cvalid[polarity] = False
         self.parent[polarity] = None
 
     def set_valid(self, polarity, v):
         self.valid[polarity] = v
-        self.c[polarity].valid = v
+
+    def sync_valid(self, polarity):
+        v = self.valid[polarity]
+        if self.cvalid[polarity] != v:
+            self.c[polarity].valid = v
+            self.cvalid[polarity] = v
 
     def release(self):
         for p in (0, 1):
@@ -604,14 +615,19 @@ class Lik:
 
         if inval or cL.parent[pol] is not parent \
                 or cL.nSibs[pol] != nSibs or cL.edgeLen[pol] != edgeLen:
-            parent.set_valid(pol, False)
-            cL.parent[pol] = parent
-            cL.nSibs[pol] = nSibs
-            cL.edgeLen[pol] = edgeLen
+            parent.valid[pol] = False
+            # The struct fields follow the mirrors; a full re-plan of an
+            # unchanged tree writes none of them.
             cLC = cL.c[pol]
-            cLC.parent = parent.ptr[pol]
-            cLC.nSibs = nSibs
-            cLC.edgeLen = edgeLen
+            if cL.parent[pol] is not parent:
+                cL.parent[pol] = parent
+                cLC.parent = parent.ptr[pol]
+            if cL.nSibs[pol] != nSibs:
+                cL.nSibs[pol] = nSibs
+                cLC.nSibs = nSibs
+            if cL.edgeLen[pol] != edgeLen:
+                cL.edgeLen[pol] = edgeLen
+                cLC.edgeLen = edgeLen
 
         if degree != 1:
             if inval or not cL.valid[pol]:
@@ -624,14 +640,16 @@ class Lik:
                     self._planAppend(variant, degree - j - 1, cL, r.other.aux,
                                      r.edge.length)
                     r = r.next
-                cL.set_valid(pol, True)
-                parent.set_valid(pol, False)
+                cL.valid[pol] = True
+                parent.valid[pol] = False
+        self._touched.append(cL)
 
     def _plan(self, root):
         L = self.lik
         pol = L.polarity
         self._pol = pol
         self._pending = []
+        self._touched = [self.rootCL]
         self._inval = bool(L.invalidate)
         self._resize = bool(L.resize)
         self._dims = (L.mschars, L.dim, L.compsLen)
@@ -675,6 +693,9 @@ class Lik:
                                      r.other.aux, r.edge.length)
                 self.rootCL.set_valid(pol, True)
         self._flushSteps()
+        for cl in self._touched:
+            cl.sync_valid(pol)
+        self._touched = []
         L.resize = False
         L.invalidate = False
 
