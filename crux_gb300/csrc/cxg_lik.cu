@@ -88,20 +88,13 @@ struct HostBuf {
 // re-uploaded when the host content's hash changes.  Buffers are never
 // shared between keys, so plans of different Liks never see each other's
 // weights.
+// Device copy of one pattern-weight array, with the host values it was
+// made from: a call whose array (same pointer and length) still holds them
+// reuses it.  The compare is a memcmp, exact and vectorised.
 struct FreqEntry {
     DevBuf dev;
-    uint64_t hash = 0;
+    std::vector<unsigned> host;
 };
-
-static uint64_t hash_u32(const unsigned *p, unsigned n) {
-    uint64_t h = 0x9e3779b97f4a7c15ull ^ n;
-    for (unsigned i = 0; i < n; ++i) {
-        h ^= p[i];
-        h *= 0x100000001b3ull;
-        h ^= h >> 29;
-    }
-    return h;
-}
 
 struct State {
     std::mutex mu;
@@ -503,13 +496,13 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
         char key[64];
         snprintf(key, sizeof(key), "%p:%u", (const void *)fh, npat);
         FreqEntry &fe = S.freqs[key];
-        const uint64_t hv = hash_u32(fh, npat);
-        if (fe.dev.p == nullptr || fe.hash != hv) {
+        if (fe.dev.p == nullptr || fe.host.size() != npat ||
+            memcmp(fe.host.data(), fh, (size_t)npat * 4) != 0) {
             rc = fe.dev.ensure((size_t)npat * 4);
             if (rc) return rc;
             CXG_CUDA(cudaMemcpy(fe.dev.p, fh, (size_t)npat * 4,
                                 cudaMemcpyHostToDevice));
-            fe.hash = hv;
+            fe.host.assign(fh, fh + npat);
         }
         dfreqs = fe.dev.p;
     }
