@@ -6,7 +6,7 @@ exports ``CxLikExecute``: the GPU library, or the CPU oracles used by tests.
 """
 import ctypes
 from ctypes import (POINTER, Structure, c_bool, c_double, c_int, c_uint,
-                    c_void_p)
+                    c_uint32, c_void_p)
 
 import numpy as np
 
@@ -109,6 +109,29 @@ class CxtLik(Structure):
         ("steps", POINTER(CxtLikStep)),
         ("stepsLen", c_uint),
         ("stepsMax", c_uint),
+    ]
+
+
+class CxgPlanSnap(Structure):
+    """cxgPlanSnap (include/cxlik_gpu.h): one rooted traversal, flattened in
+    the planner's post-order, for the native planner cxgPlanSnapRun."""
+    _fields_ = [
+        ("nvis", c_uint32),
+        ("nkid", c_uint32),
+        ("cl", c_void_p),
+        ("up", c_void_p),
+        ("nsibs", c_void_p),
+        ("edge", c_void_p),
+        ("kid0", c_void_p),
+        ("nkids", c_void_p),
+        ("kid_cl", c_void_p),
+        ("kid_int", c_void_p),
+        ("kid_edge", c_void_p),
+        ("valid", c_void_p),
+        ("cvalid", c_void_p),
+        ("m_parent", c_void_p),
+        ("m_nsibs", c_void_p),
+        ("m_elen", c_void_p),
     ]
 
 

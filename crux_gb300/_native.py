@@ -56,6 +56,10 @@ def declare(lib):
     lib.cxgPlanShape.argtypes = [vp, P(c_uint), P(c_uint), P(c_uint), P(c_uint),
                                  P(c_uint)]
     lib.cxgPlanShape.restype = c_int
+    u32p = P(ctypes.c_uint32)
+    lib.cxgPlanSnapRun.argtypes = [P(_abi.CxgPlanSnap), P(c_double), c_int,
+                                   vp, ctypes.c_uint32, u32p, u32p, u32p]
+    lib.cxgPlanSnapRun.restype = c_int
     lib.cxgTune.argtypes = [c_uint, c_uint, c_uint, ctypes.c_size_t]
     lib.cxgTune.restype = c_int
     lib.cxgTuneGet.argtypes = [P(c_uint), P(c_uint), P(c_uint),

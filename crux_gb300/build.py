@@ -1,6 +1,6 @@
 """Build the GB300 library in-tree: crux_gb300/_lib/libcxlik_gpu.so.
 
-nvcc compiles each translation unit for sm_103a only (arch-specific
+nvcc compiles each translation unit (host-only .cpp files too) for sm_103a only (arch-specific
 ``compute_103a``), in parallel, then links one shared library.  Usage:
 ``python -m crux_gb300.build`` (or ``__graft_entry__.build()``).
 """
@@ -15,7 +15,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libcxlik_gpu.so")
 SOURCES = ["cxg_kernels.cu", "cxg_lik.cu", "cxg_noalloc.cu", "cxg_mc3.cu",
-           "cxg_serve.cu", "cxg_compact.cu"]
+           "cxg_serve.cu", "cxg_compact.cu", "cxg_plan.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O3", "-I" + os.path.join(ROOT, "include"),
@@ -45,7 +45,7 @@ def build(verbose=False, extra=()):
 
     def one(src):
         s = os.path.join(SRC, src)
-        o = os.path.join(OUT, src.replace(".cu", ".o"))
+        o = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
         if _stale(o, s):
             cmd = [nvcc(), *ARCH, *FLAGS, *extra, "-c", s, "-o", o]
             if verbose:

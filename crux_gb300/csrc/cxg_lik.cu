@@ -105,6 +105,11 @@ struct State {
     size_t last_h2d = 0, last_d2h = 0;  // bytes copied by the last execute
     DevBuf misc;         // CxLikQDecomp in/out
     HostBuf stage, out;  // program staging, CxLikQDecomp staging
+    // Recorded after each program upload from `stage`: the next translation
+    // waits on it before it rewrites the staging buffer, so no upload has
+    // to be waited for on the launch path.
+    cudaEvent_t stage_ev = nullptr;
+    bool stage_pending = false;
     std::unordered_map<std::string, FreqEntry> freqs;
 };
 
@@ -527,6 +532,10 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     size_t o_lrow = al(o_pn + kact * 4 * 8);
     size_t o_leaf = al(o_lrow + (nrec * (s_lmax ? s_lmax : 1)) * sizeof(void *));
     size_t total = al(o_leaf + (s_nleaf ? s_nleaf : 1) * sizeof(void *));
+    if (S.stage_pending) {
+        CXG_CUDA(cudaEventSynchronize(S.stage_ev));
+        S.stage_pending = false;
+    }
     rc = S.stage.ensure(total);
     if (rc) return rc;
     rc = P.prog.ensure(total);
@@ -593,8 +602,10 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     char *d = static_cast<char *>(P.prog.p);
     CXG_CUDA(cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, S.stream));
     S.last_h2d = total;
-    // The staging buffer is reused by the next translation: finish the copy.
-    CXG_CUDA(cudaStreamSynchronize(S.stream));
+    if (S.stage_ev == nullptr)
+        CXG_CUDA(cudaEventCreateWithFlags(&S.stage_ev, cudaEventDisableTiming));
+    CXG_CUDA(cudaEventRecord(S.stage_ev, S.stream));
+    S.stage_pending = true;
 
     PmatArgs &pa = P.pa;
     pa.nchild = nchild;

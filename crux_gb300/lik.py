@@ -32,6 +32,16 @@ from .cxmath import gamma_rates
 CACHE_LINE = 64
 MQ_MULT = 8  # CxmLikMqMult (CxLik.h:277)
 
+# Counts changes to CL buffers and CL mirrors made outside a planner run
+# (prepare, buffer release, flush).  A flattened traversal kept for the
+# native planner is valid only while this count and the tree's serial
+# number are what they were when it was built.
+_epoch = [0]
+
+
+def _bump():
+    _epoch[0] += 1
+
 
 class Config:
     """Striping policy inputs (pkg/Crux/Config.py; Cx.c:7, 63-66)."""
@@ -77,6 +87,7 @@ class CL:
 
     def prepare(self, polarity, nchars, dim, ncomp):
         if self.bufs[polarity] is None:
+            _bump()
             if self.device:
                 mat, lsc = _tokens(), _tokens()
             else:
@@ -93,6 +104,7 @@ class CL:
     def flush_buffers(self, polarity):
         b = self.bufs[polarity]
         if b is not None:
+            _bump()
             if self.forget:
                 self.lib.cxgLikClForget(_abi.dptr(b[0]))
             self.bufs[polarity] = None
@@ -101,6 +113,9 @@ class CL:
 
     def flush(self, polarity):
         self.flush_buffers(polarity)
+        if self.valid[polarity] or self.cvalid[polarity] or \
+                self.parent[polarity] is not None:
+            _bump()
         self.c[polarity].valid = False
         self.c[polarity].parent = None
         self.valid[polarity] = False
@@ -152,6 +167,26 @@ def default_library():
     return _native.load()
 
 
+_planner = []
+
+
+def planner_library():
+    """The library exporting cxgPlanSnapRun (the GB300 library; loading it
+    makes no CUDA call), or None where it has not been built.  Host-only
+    libraries given as `lib=` (the CPU oracles) plan through it too."""
+    if not _planner:
+        try:
+            from . import _native
+            _planner.append(_native.load())
+        except Exception:
+            _planner.append(None)
+    return _planner[0]
+
+
+class _Snap:
+    """A flattened rooted traversal for cxgPlanSnapRun (see Lik._snapBuild)."""
+
+
 class Lik:
     """Tree likelihood over an alignment and a mixture of models."""
 
@@ -170,6 +205,9 @@ class Lik:
         self.lik = None
         self.mate = None
         self._models = []
+        self._snap = None
+        self._pyKey = None
+        self._compsKey = None
         if alignment is not None:
             self._init0(tree)
             nchars = alignment.nchars
@@ -207,6 +245,9 @@ class Lik:
 
     def _init1(self, tree, nchars, dim, polarity):
         self.mate = None
+        self._snap = None
+        self._pyKey = None
+        self._compsKey = None
         self.tree = tree
         L = self.lik = _abi.CxtLik()
         L.polarity = polarity
@@ -248,7 +289,15 @@ class Lik:
 
     # -- component array maintenance ----------------------------------------
     def _sync_comps(self):
-        """Rebuild the C comps/models arrays from the Python-side lists."""
+        """Rebuild the C comps/models arrays from the Python-side lists, unless
+        they already hold exactly these models and values (the key keeps the
+        model objects themselves, so a replaced model never matches)."""
+        key = (tuple((c["model"], c["weightScaled"], c["cweight"], c["cmult"])
+                     for c in self._comps),
+               tuple((m, m.comp0, m.clen) for m in self._models))
+        if key == self._compsKey:
+            return
+        self._compsKey = key
         n = len(self._comps)
         arr = (_abi.CxtLikComp * max(n, 1))()
         for i, c in enumerate(self._comps):
@@ -644,6 +693,193 @@ class Lik:
                 parent.valid[pol] = False
         self._touched.append(cL)
 
+    # -- native planner (cxgPlanSnapRun) ---------------------------------------
+    # The recursion above runs once per topology, root and set of CL buffers;
+    # _snapBuild then flattens the traversal it took, and later plans of the
+    # same traversal run natively.  Every rule (what is dirty, which steps,
+    # which struct fields change) is the one _planRecurse applies.
+    native_plan = True
+
+    def _snapBuild(self, root, key):
+        pol = self._pol
+        vis = []          # (CL, parent CL, nSibs, edge index, kids or None)
+        opp = []          # CLs an invalidating plan would flush
+        edges, eidx = [], {}
+        ok = [True]
+
+        def eid(e):
+            if e is None:
+                return -1
+            i = eidx.get(id(e))
+            if i is None:
+                i = eidx[id(e)] = len(edges)
+                edges.append(e)
+            return i
+
+        def kid(r, internal=None):
+            c = r.other.aux
+            addr = c.addr[0] if c.bufs[1] is None else c.addr[pol]
+            if internal is None:
+                internal = r.other.node.getDegree() > 1
+            return (addr, internal, eid(r.edge))
+
+        def rec(ring, parent, nSibs, edge):
+            cL = ring.aux
+            degree = ring.node.getDegree()
+            if cL is None or degree == 2 or \
+                    (degree != 1 and cL.bufs[pol] is None):
+                ok[0] = False
+                return
+            r = ring.next
+            while r is not ring:
+                if r.aux is not None:
+                    opp.append(r.aux)
+                rec(r.other, cL, degree, r.edge)
+                if not ok[0]:
+                    return
+                r = r.next
+            kids = None
+            if degree != 1:
+                kids = []
+                r = ring.next
+                for _ in range(1, degree):
+                    kids.append(kid(r))
+                    r = r.next
+            vis.append((cL, parent, nSibs, eid(edge), kids))
+
+        degree = root.getDegree()
+        ring = root.ring
+        if degree == 1:
+            rec(ring.other, self.rootCL, 2, ring.edge)
+            if ok[0]:
+                rec(ring, self.rootCL, 2, None)
+            if ok[0]:
+                c = ring.aux
+                leaf = (c.addr[0] if c.bufs[1] is None else c.addr[pol],
+                        False, -1)
+                rkids = [kid(ring), leaf]
+        else:
+            for r in ring:
+                if r.aux is not None:
+                    opp.append(r.aux)
+                rec(r.other, self.rootCL, degree, r.edge)
+                if not ok[0]:
+                    break
+            if ok[0]:
+                rkids = [kid(r) for r in ring]
+        if not ok[0]:
+            return None
+        vis.append((self.rootCL, None, 0, -1, rkids))
+        index = {id(v[0]): i for i, v in enumerate(vis)}
+        if len(index) != len(vis):
+            return None
+        n = len(vis)
+        sn = _Snap()
+        sn.key = key
+        sn.objs = [v[0] for v in vis]
+        sn.up_obj = [v[1] for v in vis]
+        sn.edges = edges
+        sn.opp_clean = all(
+            f.bufs[pol] is None and not f.valid[pol] and not f.cvalid[pol]
+            and f.parent[pol] is None for f in opp)
+        u32, i32 = np.uint32, np.int32
+        sn.cl = np.array([v[0].addr[pol] for v in vis], dtype=np.uint64)
+        sn.up = np.array([-1 if v[1] is None else index[id(v[1])]
+                          for v in vis], dtype=i32)
+        sn.nsibs = np.array([v[2] for v in vis], dtype=u32)
+        sn.edge = np.array([v[3] for v in vis], dtype=i32)
+        kids = [v[4] or [] for v in vis]
+        sn.nkids = np.array([len(k) for k in kids], dtype=u32)
+        sn.kid0 = np.zeros(n, dtype=u32)
+        if n > 1:
+            sn.kid0[1:] = np.cumsum(sn.nkids[:-1])
+        flat = [k for ks in kids for k in ks]
+        sn.kid_cl = np.array([k[0] for k in flat], dtype=np.uint64)
+        sn.kid_int = np.array([1 if k[1] else 0 for k in flat], dtype=np.uint8)
+        sn.kid_edge = np.array([k[2] for k in flat], dtype=i32)
+        sn.valid = np.array([v[0].valid[pol] for v in vis], dtype=np.uint8)
+        sn.cvalid = np.array([v[0].cvalid[pol] for v in vis], dtype=np.uint8)
+        sn.m_parent = np.array(
+            [0 if v[0].parent[pol] is None else v[0].parent[pol].addr[pol]
+             for v in vis], dtype=np.uint64)
+        sn.m_nsibs = np.array([v[0].nSibs[pol] for v in vis], dtype=u32)
+        sn.m_elen = np.array([v[0].edgeLen[pol] for v in vis],
+                             dtype=np.float64)
+        sn.lens = np.zeros(max(len(edges), 1), dtype=np.float64)
+        sn.changed = np.zeros(n, dtype=u32)
+        c = sn.c = _abi.CxgPlanSnap()
+        c.nvis = n
+        c.nkid = len(flat)
+        for f in ("cl", "up", "nsibs", "edge", "kid0", "nkids", "kid_cl",
+                  "kid_int", "kid_edge", "valid", "cvalid", "m_parent",
+                  "m_nsibs", "m_elen"):
+            setattr(c, f, getattr(sn, f).ctypes.data)
+        sn.cref = ctypes.byref(c)
+        sn.lens_p = _abi.dptr(sn.lens)
+        sn.nsteps = ctypes.c_uint32()
+        sn.nchanged = ctypes.c_uint32()
+        sn.nsteps_p = ctypes.byref(sn.nsteps)
+        sn.nchanged_p = ctypes.byref(sn.nchanged)
+        sn.changed_p = sn.changed.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_uint32))
+        return sn
+
+    def _snapSync(self, sn, idx):
+        """Copy the native mirrors of visits `idx` into the CL objects."""
+        pol = self._pol
+        for v in idx:
+            cl = sn.objs[v]
+            cl.valid[pol] = bool(sn.valid[v])
+            cl.cvalid[pol] = bool(sn.cvalid[v])
+            cl.nSibs[pol] = int(sn.m_nsibs[v])
+            cl.edgeLen[pol] = float(sn.m_elen[v])
+            if sn.up_obj[v] is not None and \
+                    sn.m_parent[v] == sn.up_obj[v].addr[pol]:
+                cl.parent[pol] = sn.up_obj[v]
+
+    def _nativePlan(self, root):
+        """Plan natively if this Lik's traversal is unchanged since the last
+        plan; False when the Python planner must run."""
+        L = self.lik
+        if not self.native_plan or L.resize:
+            return False
+        key = (self.tree.sn, _epoch[0], self._pol, root)
+        sn = self._snap
+        if sn is None or sn.key != key:
+            if self._pyKey != key:
+                return False
+            lib = planner_library()
+            if lib is None:
+                return False
+            sn = self._snapBuild(root, key)
+            self._pyKey = None
+            if sn is None:
+                return False
+            sn.lib = lib
+            self._snap = sn
+        inval = bool(L.invalidate)
+        if inval and not sn.opp_clean:
+            return False
+        sn.lens[:len(sn.edges)] = [e.length for e in sn.edges]
+        rc = sn.lib.cxgPlanSnapRun(sn.cref, sn.lens_p, inval, self._steps,
+                                   L.stepsMax, sn.nsteps_p, sn.changed_p,
+                                   sn.nchanged_p)
+        nc = sn.nchanged.value
+        if nc:
+            self._snapSync(sn, sn.changed[:nc].tolist())
+        if rc != 0:
+            self._snap = None
+            self._snapSync(sn, range(len(sn.objs)))
+            if rc == 1:
+                raise ValueError("Negative branch length")
+            raise RuntimeError("cxgPlanSnapRun: %s"
+                               % sn.lib.cxgLastError().decode())
+        L.stepsLen = sn.nsteps.value
+        self._plan_refs = sn.objs
+        L.resize = False
+        L.invalidate = False
+        return True
+
     def _plan(self, root):
         L = self.lik
         pol = L.polarity
@@ -660,6 +896,15 @@ class Lik:
         L.rootCLC = self.rootCL.ptr[pol]
         if root is None:
             root = self.tree.base
+        if self._nativePlan(root):
+            return
+        self._snap = None
+        self._planPython(root)
+        self._pyKey = (self.tree.sn, _epoch[0], pol, root)
+
+    def _planPython(self, root):
+        L = self.lik
+        pol = self._pol
         degree = root.getDegree()
         ring = root.ring
         if degree == 1:

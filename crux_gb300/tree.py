@@ -209,6 +209,7 @@ class Tree:
 
     def clearAux(self):
         self.aux = None
+        self.sn += 1
         for n in self.nodes:
             n.aux = None
             if n.ring is not None:

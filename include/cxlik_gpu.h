@@ -223,6 +223,50 @@ int cxgPlanDestroy(cxgPlan *plan);
 int cxgPlanShape(const cxgPlan *plan, unsigned *tile, unsigned *threads_per_pattern,
                  unsigned *patterns_per_thread, unsigned *nslot, unsigned *nleaf);
 
+/* The step planner of Lik._planRecurse / Lik._plan (Lik.pyx:1427-1601) run
+ * natively over one rooted traversal of a tree, flattened once by the host
+ * mirror.  Visits are in the planner's post-order and the root CL is the
+ * last.  Visit v's CL is cl[v], its parent is visit up[v] (-1 for the root),
+ * its nSibs and edge length are nsibs[v] and lens[edge[v]] (edge -1 means a
+ * length of 0), and its children are kid0[v] .. kid0[v]+nkids[v]-1 (none for
+ * a leaf).  A child names the CL a step reads (kid_cl), whether it is
+ * internal (kid_int: I or L variants) and its edge (kid_edge).  The five
+ * mirror arrays hold each visit's valid, struct-valid, parent, nSibs and
+ * edgeLen as the caller last saw them; the planner updates them with the
+ * CxtLikCL fields it writes. */
+typedef struct {
+    uint32_t nvis;
+    uint32_t nkid;
+    CxtLikCL *const *cl;
+    const int32_t *up;
+    const uint32_t *nsibs;
+    const int32_t *edge;
+    const uint32_t *kid0;
+    const uint32_t *nkids;
+    CxtLikCL *const *kid_cl;
+    const uint8_t *kid_int;
+    const int32_t *kid_edge;
+    uint8_t *valid;
+    uint8_t *cvalid;
+    CxtLikCL **m_parent;
+    uint32_t *m_nsibs;
+    double *m_elen;
+} cxgPlanSnap;
+
+/* Plan one evaluation (no counterpart entry point: the reference plans in
+ * Cython, Lik.pyx:1427-1601).  Like the Python planner it marks a CL dirty
+ * when its parent, nSibs or edge length changed (or `invalidate` is set),
+ * emits the Compute/Merge steps of every dirty internal CL and of the root,
+ * writes changed CxtLikCL fields and finally each CL's valid flag.  Steps go
+ * to steps[0 .. *nsteps).  The indices of visits whose mirrors changed go to
+ * changed[0 .. *nchanged) (room for nvis).  Returns 0; CXG_EINVAL for a
+ * malformed snapshot or a full step array; 1 when a step would carry a
+ * negative branch length, with the state as far as the planner had come
+ * (the Python planner raises ValueError at the same point). */
+int cxgPlanSnapRun(const cxgPlanSnap *snap, const double *lens, int invalidate,
+                   CxtLikStep *steps, uint32_t cap, uint32_t *nsteps,
+                   uint32_t *changed, uint32_t *nchanged);
+
 /* A batch: the plans of many likelihoods (trees, alignments, models; all
  * with the same number of active components) run by one persistent launch
  * that walks (job, pattern-tile) items, longest jobs first; one run (P

@@ -1,0 +1,185 @@
+"""The native step planner (cxgPlanSnapRun) against the Python restatement of
+Lik._plan / _planRecurse (pkg/Crux/Tree/Lik.pyx:1427-1601).
+
+Two Liks on identical trees take the same random sequence of operations:
+branch rescales, invalidations, other roots, NNI rearrangements, model
+changes, flushes, the other-polarity clone and a negative branch length.
+One plans natively whenever its traversal is unchanged, and the other always
+plans in Python.  After every plan the step arrays, the lnLs (CPU oracle) and
+every CL's mirrors and CxtLikCL fields must be identical.  No GPU is used."""
+import ctypes
+import random
+
+import numpy as np
+import pytest
+
+from crux_gb300 import _abi, lik as likmod, synth
+
+
+def _addr(p):
+    return ctypes.cast(p, ctypes.c_void_p).value
+
+
+def _pairs(a, b):
+    """(CL of a, CL of b) for every ring of the two (same-shaped) trees."""
+    out = [(a.rootCL, b.rootCL)]
+    if a.mate is not None:
+        out.append((a.mate.rootCL, b.mate.rootCL))
+    for ea, eb in zip(a.tree.edges, b.tree.edges):
+        for ra, rb in ((ea.ring, eb.ring), (ea.ring.other, eb.ring.other)):
+            assert (ra.aux is None) == (rb.aux is None)
+            if ra.aux is not None:
+                out.append((ra.aux, rb.aux))
+    return out
+
+
+def _check_same(a, b, la, lb):
+    assert la == lb or (np.isnan(la) and np.isnan(lb))
+    pairs = _pairs(a, b)
+    amap = {None: None}
+    for ca, cb in pairs:
+        for p in (0, 1):
+            amap[ca.addr[p]] = cb.addr[p]
+    objmap = {id(ca): cb for ca, cb in pairs}
+    sa = np.frombuffer(a._steps, dtype=_abi.STEP_DTYPE)[:a.lik.stepsLen]
+    sb = np.frombuffer(b._steps, dtype=_abi.STEP_DTYPE)[:b.lik.stepsLen]
+    assert len(sa) == len(sb)
+    assert (sa["variant"] == sb["variant"]).all()
+    assert (sa["ntrail"] == sb["ntrail"]).all()
+    assert (sa["edgeLen"] == sb["edgeLen"]).all()
+    assert [amap[int(x)] for x in sa["parentCL"]] == sb["parentCL"].tolist()
+    assert [amap[int(x)] for x in sa["childCL"]] == sb["childCL"].tolist()
+    for ca, cb in pairs:
+        for p in (0, 1):
+            assert ca.valid[p] == cb.valid[p]
+            assert ca.cvalid[p] == cb.cvalid[p]
+            assert ca.nSibs[p] == cb.nSibs[p]
+            assert ca.edgeLen[p] == cb.edgeLen[p]
+            assert (ca.bufs[p] is None) == (cb.bufs[p] is None)
+            pa = ca.parent[p]
+            assert (pa is None and cb.parent[p] is None) or \
+                objmap[id(pa)] is cb.parent[p]
+            sa_, sb_ = ca.c[p], cb.c[p]
+            assert bool(sa_.valid) == bool(sb_.valid)
+            assert sa_.nSibs == sb_.nSibs and sa_.edgeLen == sb_.edgeLen
+            assert amap.get(_addr(sa_.parent)) == _addr(sb_.parent)
+
+
+def _nni(tree, k, side):
+    """Swap subtree x (across ring a of u) with subtree y (across ring b of
+    v) over the internal edge u-v.  Each subtree keeps the ring it hangs
+    from, and with it that ring's cached CL, as the sampler's NNI does."""
+    inner = [e for e in tree.edges if e.ring.node.getDegree() > 1
+             and e.ring.other.node.getDegree() > 1]
+    e = inner[k % len(inner)]
+    u, v = e.ring, e.ring.other
+    a = u.next
+    b = v.next if side == 0 else v.next.next
+    ea, eb = a.edge, b.edge
+    x, y = a.other.node, b.other.node
+    un, vn = u.node, v.node
+    xa = ea.ring is a.other      # edge.ring lands on attach's first node
+    yb = eb.ring is b.other
+    ea.detach()
+    eb.detach()
+    if xa:
+        ea.attach(x, vn)
+    else:
+        ea.attach(vn, x)
+    if yb:
+        eb.attach(y, un)
+    else:
+        eb.attach(un, y)
+
+
+def _lnl(lk, root):
+    try:
+        return lk.lnL(root)
+    except ValueError as e:
+        return str(e)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_native_planner_matches_python_planner(port, seed):
+    assert likmod.planner_library() is not None, \
+        "libcxlik_gpu.so (which holds the native planner) is not built"
+    case = synth.Case(10, 300, 0.1, 40 + seed)
+    a = case.lik(lib=port)
+    b = case.lik(lib=port)
+    b.native_plan = False
+    rng = random.Random(seed)
+    root_a = root_b = None
+    native_runs = 0
+    for it in range(400):
+        op = rng.random()
+        ea, eb = a.tree.edges, b.tree.edges
+        if op < 0.45:
+            i = rng.randrange(len(ea))
+            f = rng.uniform(0.5, 2.0)
+            ea[i].length *= f
+            eb[i].length *= f
+        elif op < 0.55:
+            a.lik.invalidate = b.lik.invalidate = True
+        elif op < 0.62:
+            k = rng.randrange(len(a.tree.nodes))
+            root_a, root_b = a.tree.nodes[k], b.tree.nodes[k]
+            if rng.random() < 0.3:
+                root_a = root_b = None
+        elif op < 0.70:
+            k, side = rng.randrange(100), rng.randrange(2)
+            _nni(a.tree, k, side)
+            _nni(b.tree, k, side)
+            root_a = root_b = None
+        elif op < 0.76:
+            alpha = rng.uniform(0.2, 2.0)
+            a.setAlpha(0, alpha)
+            b.setAlpha(0, alpha)
+        elif op < 0.80:
+            a.flush()
+            b.flush()
+        elif op < 0.85:
+            ma, mb = a.clone(), b.clone()
+            mb.native_plan = False
+            for _ in range(rng.randrange(1, 4)):
+                _check_same(ma, mb, _lnl(ma, root_a), _lnl(mb, root_b))
+        elif op < 0.88:
+            i = rng.randrange(len(ea))
+            old = ea[i].length
+            ea[i].length = eb[i].length = -0.25
+            ra, rb = _lnl(a, root_a), _lnl(b, root_b)
+            assert ra == rb
+            ea[i].length = eb[i].length = old
+        had = a._snap is not None
+        _check_same(a, b, _lnl(a, root_a), _lnl(b, root_b))
+        native_runs += had and a._snap is not None
+    # Most plans after the first one on a traversal ran natively.
+    assert native_runs > 100, native_runs
+
+
+def test_native_planner_full_and_dirty_plans(port):
+    """Full re-plans and single-branch dirty paths of a 64-taxon tree plan
+    natively.  A full plan has one step per edge, 2N-3, plus the 0-length
+    merge of a leaf base (Lik.pyx:1560-1575): 2N-2 here."""
+    case = synth.Case(64, 200, 0.05, 11)
+    a = case.lik(lib=port)
+    b = case.lik(lib=port)
+    b.native_plan = False
+    # The first plans create every CL (which any traversal kept for the
+    # native planner notices); from the third plan on `a` plans natively.
+    for _ in range(2):
+        for lk in (a, b):
+            lk.lik.invalidate = True
+        _check_same(a, b, a.lnL(), b.lnL())
+    for lk in (a, b):
+        lk.lik.invalidate = True
+    _check_same(a, b, a.lnL(), b.lnL())
+    assert a.tree.base.getDegree() == 1
+    assert a._snap is not None and a.lik.stepsLen == 2 * 64 - 2
+    rng = random.Random(5)
+    for _ in range(50):
+        i = rng.randrange(len(a.tree.edges))
+        f = rng.uniform(0.5, 2.0)
+        a.tree.edges[i].length *= f
+        b.tree.edges[i].length *= f
+        _check_same(a, b, a.lnL(), b.lnL())
+        assert a._snap is not None
