@@ -161,30 +161,39 @@ def profile_traffic(name):
     return None
 
 
-def autotune(lib, prec, args, lik=None, liks=None):
+def autotune(lib, prec, args, lik=None, liks=None, lanes=True):
     """Pick the walker's launch shape (tile, threads per pattern, patterns
-    per thread, stack budget) by timing the candidates on this workload;
-    ``--shape`` fixes it instead.  Returns the shape with how it was
-    chosen."""
+    per thread, stack budget, op lanes) by timing the candidates on this
+    workload; ``--shape`` fixes it instead.  `lanes` False keeps one op lane
+    (MC3 and the server run the batched walker, which has one).  Returns
+    the shape with how it was chosen."""
     from crux_gb300 import tune
     if args.shape:
         tune.set_shape(lib, *args.shape)
-        t, g, p, b = args.shape
-        return {"tile": t, "tpp": g, "ppt": p, "budget": b, "source": "--shape"}
+        t, g, p, b = args.shape[:4]
+        n = args.shape[4] if len(args.shape) > 4 else 1
+        return {"tile": t, "tpp": g, "ppt": p, "budget": b, "lanes": n,
+                "source": "--shape"}
     if liks is not None:
         r = tune.tune_batch(liks, prec, iters=3,
                             shapes=tune.candidates(
                                 prec, tune.active_components(liks[0]),
-                                budgets=(12 << 10, 24 << 10, 48 << 10)))
+                                budgets=(12 << 10, 24 << 10, 48 << 10),
+                                lanes=(1,)))
     else:
-        r = tune.tune_plan(lik, prec, iters=10)
+        r = tune.tune_plan(lik, prec, iters=10,
+                           shapes=None if lanes else tune.candidates(
+                               prec, tune.active_components(lik), lanes=(1,)))
     best = dict(r["best"])
     top = sorted(r["table"], key=lambda x: x["ms"])
     per_tpp = {}
     for x in top:
-        per_tpp.setdefault(str(x["tpp"]) if x["ppt"] == 1 else
-                           "%d/ppt%d" % (x["tpp"], x["ppt"]),
-                           [x["tile"], x["budget"], x["ms"]])
+        key = str(x["tpp"])
+        if x["ppt"] != 1:
+            key += "/ppt%d" % x["ppt"]
+        if x["lanes"] != 1:
+            key += "/lanes%d" % x["lanes"]
+        per_tpp.setdefault(key, [x["tile"], x["budget"], x["ms"]])
     best.update(source="autotuned", candidates=len(r["table"]),
                 worst_ms=top[-1]["ms"], best_per_tpp=per_tpp)
     return best
@@ -289,7 +298,8 @@ def run_ours(args, dist):
     # End to end through the public API: full re-plan + lnL each run, with
     # the FP32 form's tuned shape.
     sh = res["fp32"]["shape"]
-    tune.set_shape(gpu, sh["tile"], sh["tpp"], sh["ppt"], sh["budget"])
+    tune.set_shape(gpu, sh["tile"], sh["tpp"], sh["ppt"], sh["budget"],
+                   sh["lanes"])
     lik = res["fp32"]["lik"]
     for _ in range(max(args.warmup, 3)):
         lik.lik.invalidate = True
@@ -530,7 +540,7 @@ def run_mc3(args, dist):
     for prec in (("fp32",) if args.profile else ("fp32", "fp64")):
         lk = case.lik(lib=gpu, precision=prec, alignment=aln)
         lk.prepare_plan()
-        shape = autotune(gpu, prec, args, lik=lk)
+        shape = autotune(gpu, prec, args, lik=lk, lanes=False)
         del lk
         m = Mc3(case.tree(aln.taxaMap), aln, case.params["rates"],
                 case.params["freqs"], alpha=0.5, ncat=4,
@@ -800,7 +810,7 @@ def run_serve(args, dist):
     for prec in ("fp32", "fp64"):
         lk = med.case.lik(lib=gpu, precision=prec, alignment=med.alignment)
         lk.prepare_plan()
-        out[prec + "_shape"] = autotune(gpu, prec, args, lik=lk)
+        out[prec + "_shape"] = autotune(gpu, prec, args, lik=lk, lanes=False)
         del lk
         srv = Server(prec)
         for i, r in enumerate(base):
@@ -880,7 +890,7 @@ def main():
     ap.add_argument("--shape", type=lambda v: tuple(int(x) for x in v.split(",")),
                     default=None,
                     help="walker shape tile,threads_per_pattern,"
-                         "patterns_per_thread,stack_bytes "
+                         "patterns_per_thread,stack_bytes[,op_lanes] "
                          "instead of autotuning")
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU baseline and the oracle check")

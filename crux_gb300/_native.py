@@ -65,6 +65,12 @@ def declare(lib):
     lib.cxgTuneGet.argtypes = [P(c_uint), P(c_uint), P(c_uint),
                                P(ctypes.c_size_t)]
     lib.cxgTuneGet.restype = c_int
+    lib.cxgTuneLanes.argtypes = [c_uint]
+    lib.cxgTuneLanes.restype = c_int
+    lib.cxgTuneLanesGet.argtypes = [P(c_uint)]
+    lib.cxgTuneLanesGet.restype = c_int
+    lib.cxgPlanLanes.argtypes = [vp, P(c_uint)]
+    lib.cxgPlanLanes.restype = c_int
     lib.cxgLikExecuteNoAlloc.argtypes = [P(_abi.CxtLik), c_int,
                                          P(ctypes.c_uint32), P(c_double),
                                          vp, P(c_double)]

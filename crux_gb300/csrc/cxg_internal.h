@@ -17,6 +17,8 @@ constexpr unsigned kPatternQuantum = 128;
 constexpr unsigned kBlock = 128;
 // Largest CTA of the plan walkers: tile patterns x threads per pattern.
 constexpr unsigned kMaxThreads = 256;
+// Largest CTA of the op-lane walker: 2 lanes x tile patterns (tile <= 64).
+constexpr unsigned kLaneThreads = 128;
 // Default patterns per tile.
 constexpr unsigned kTile = 64;
 // Most shared-memory stack slots per tile.
@@ -58,7 +60,11 @@ struct RecHead {
     uint32_t nchild;
     int32_t slot;      // stack slot keeping the result for a later op, or -1
     uint32_t flags;    // REC_NO_HBM: the result is not written to HBM
-    uint32_t pad_;
+    // Bytes of the record `ring` positions later, which refills this ring
+    // stage after this op (a multiple of 16); 0: the whole record stride.
+    // Read by the one-lane walker with staged leaves; others copy whole
+    // strides.
+    uint32_t next_bytes;
 };
 
 // RecHead.flags: the parent is consumed from its stack slot (or is the
@@ -136,6 +142,12 @@ struct PlanArgs {
 // `kact` components: one of each for every shape; 2 or 4 threads per
 // pattern for the FP32 form when they divide kact; 2 patterns per thread
 // for the FP32 form with one thread per pattern and at most 5 components.
+// Op lanes (two independent ops per step, walk_tile's L) exist for the
+// FP32 form with one thread and one pattern per thread, kact <= 5.
+inline bool lanes_shape_ok(int precision, unsigned kact, unsigned tpp, unsigned ppt) {
+    return precision == CXG_FP32 && tpp == 1 && ppt == 1 && kact >= 1 && kact <= 5;
+}
+
 inline bool walker_shape_ok(int precision, unsigned kact, unsigned tpp,
                             unsigned ppt = 1) {
     if (ppt == 2)
@@ -257,7 +269,9 @@ int cuda_fail(cudaError_t err, const char *what);
 cudaError_t launch_pmat(const PmatArgs &a, cudaStream_t s);
 cudaError_t launch_pmat_batch(const PmatArgs *jobs, const uint32_t *prefix,
                               uint32_t njobs, uint32_t total, cudaStream_t s);
-cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s);
+// `lanes` 2: the op-lane walker (the plan's records come in steps of two).
+cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s,
+                        unsigned lanes = 1);
 cudaError_t launch_qdecomp(const double *rtri, const double *pi, double *out,
                            cudaStream_t s);
 unsigned plan_blocks(unsigned ppad, unsigned tile);

@@ -340,6 +340,19 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     return false;
 }
 
+// Max of n values as a balanced tree (the same value as a left-to-right
+// chain: fmax is exact and ignores NaN operands either way), so the
+// dependent chain is log2(n) long instead of n.
+template <int N, typename X>
+__device__ __forceinline__ X tree_max(const X *v) {
+    if constexpr (N == 1) {
+        return v[0];
+    } else {
+        constexpr int H = N / 2;
+        return fmax(tree_max<H>(v), tree_max<N - H>(v + H));
+    }
+}
+
 // Max over the G consecutive lanes that share a pattern.
 template <int G, typename X>
 __device__ __forceinline__ X group_max(X x) {
@@ -356,10 +369,21 @@ __device__ __forceinline__ X group_max(X x) {
 // per ring stage, the parity of the next completion to wait for; it
 // persists across the items a CTA processes.  Returns false if a bounded
 // wait gave up.
-template <typename T, int KT, int G, bool STAGED>
+//
+// L > 1 (op lanes; FP32, G = 1, staged leaves): the CTA is L groups of
+// `tile` threads over the same patterns.  The host schedules the plan in
+// steps of L mutually independent ops (a record with no children fills an
+// empty lane) and a ring stage holds one step's L records; lane l runs the
+// step's l-th op.  A result one lane writes is read by another only in a
+// later step, after the block barriers between steps.  The root is the
+// last step's lane-0 op, so lane 0 aggregates it and the other lanes add
+// exact zeros to the tile sum: the bits are those of L = 1.
+template <typename T, int KT, int G, bool STAGED, int L = 1>
 __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
                           const SmemLayout &Lay, unsigned ring_depth,
                           uint32_t &phase) {
+    static_assert(L == 1 || (STAGED && G == 1 && sizeof(T) == 4),
+                  "op lanes: FP32, one thread per pattern, staged leaves");
     typedef typename Prec<T>::S S;
     typedef typename Prec<T>::V V;
     constexpr int U = Prec<T>::U;
@@ -367,10 +391,12 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_ok;
     const unsigned nthr = blockDim.x;
-    const unsigned tile = nthr / G;
+    const unsigned tile = nthr / (G * L);
     const unsigned tid = threadIdx.x;
-    const unsigned pl = tid / G;   // pattern within the tile
-    const unsigned g = tid % G;    // component group of this thread
+    const unsigned lane = L > 1 ? tid / tile : 0u;  // op lane of this thread
+    const unsigned ltid = L > 1 ? tid % tile : tid;
+    const unsigned pl = ltid / G;  // pattern within the tile
+    const unsigned g = ltid % G;   // component group of this thread
     const unsigned k0 = g * KT;    // its first component
     const unsigned p = tile_idx * tile + pl;
     const size_t ppad = a.ppad;
@@ -379,20 +405,21 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
     V *slots = reinterpret_cast<V *>(smem + Lay.slots);
     S *slot_sc = reinterpret_cast<S *>(smem + Lay.slot_sc);
     // STAGED: every leaf's row is staged once per tile and records travel
-    // alone (stage stride a.rstride).  Else each stage carries its op's
+    // alone (stage stride L records).  Else each stage carries its op's
     // leaf rows (stage stride Lay.stage).
-    const size_t sstride = STAGED ? (size_t)a.rstride : Lay.stage;
+    const size_t sstride = STAGED ? (size_t)a.rstride * L : Lay.stage;
     uint8_t *masks = smem + Lay.masks;
     const unsigned R = ring_depth;
+    const unsigned nsteps = a.nops / L;  // the host pads nops to a multiple
 
     if (STAGED) {
-        // Start streaming the job's first R op records.
+        // Start streaming the job's first R steps of op records.
         if (tid == 0) {
             fence_proxy_async();
-            for (unsigned o = 0; o < R && o < a.nops; ++o) {
-                mbar_expect_tx(&bars[o], a.rstride);
-                bulk_g2s(ring + (size_t)o * a.rstride, a.rec + (size_t)o * a.rstride,
-                         a.rstride, &bars[o]);
+            for (unsigned o = 0; o < R && o < nsteps; ++o) {
+                mbar_expect_tx(&bars[o], (uint32_t)sstride);
+                bulk_g2s(ring + (size_t)o * sstride, a.rec + (size_t)o * sstride,
+                         (uint32_t)sstride, &bars[o]);
             }
         }
         // Stage this tile's leaf masks with 16-byte loads.
@@ -416,12 +443,12 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
 
     T acc[KT * 4];
     S lns = S(0);
-    for (unsigned o = 0; o < a.nops; ++o) {
+    for (unsigned o = 0; o < nsteps; ++o) {
         const unsigned stage = o % R;
         // Streaming: thread 0 reads op o + R's leaf-row pointers now; it
         // issues that stage after this op, when the loads have long arrived.
         const uint8_t *pre[kLeafPre] = {nullptr, nullptr, nullptr, nullptr};
-        if (!STAGED && tid == 0 && o + R < a.nops) read_rows(a, o + R, pre);
+        if (!STAGED && tid == 0 && o + R < nsteps) read_rows(a, o + R, pre);
         if (tid == 0) {
             const uint32_t par = (phase >> stage) & 1u;
             s_ok = mbar_wait_bounded(&bars[stage], par);
@@ -432,7 +459,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             if (tid == 0) atomicOr(a.err, 1u);
             return false;  // all threads leave together
         }
-        const unsigned char *rec = ring + (size_t)stage * sstride;
+        const unsigned char *rec = ring + (size_t)stage * sstride + (size_t)lane * a.rstride;
         const uint8_t *lrow = rec + a.rstride;  // this op's leaf rows
         unsigned nlk = 0;  // leaf children of this op seen so far
         const RecHead *hd = reinterpret_cast<const RecHead *>(rec);
@@ -440,23 +467,36 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
         const unsigned nchild = hd->nchild;
         T sc = T(0);  // plain form: max over child messages
         lns = S(0);
-        for (unsigned ci = 0; ci < nchild; ++ci) {
-            const RecChild ch = kids[ci];
-            const T *area = reinterpret_cast<const T *>(rec + ch.off);
-            const V *P = reinterpret_cast<const V *>(area + (size_t)k0 * 16);
-            T msg[KT * 4];
-            const bool leaf = (ch.src == SRC_LEAF);
-            const bool in_slot = (ch.src == SRC_SLOT);
-            unsigned m = 0u;
-            if (STAGED) {
-                if (leaf) m = masks[(size_t)ch.idx * tile + pl];
-            } else {
-                if (leaf) m = lrow[(size_t)(nlk++) * tile + pl];
+        // A child's inputs: its state rows (internal) with its scaler, or
+        // its leaf's state mask.  Loading them is split from computing the
+        // message so that an op with two children issues both children's
+        // loads before it waits on either.
+        struct In {
+            T x[KT * 4];
+            S l;
+            unsigned m;
+        };
+        auto load_in = [&](const RecChild &ch, In &in) {
+            if (ch.src == SRC_LEAF) {
+                in.m = STAGED ? masks[(size_t)ch.idx * tile + pl]
+                              : lrow[(size_t)(nlk++) * tile + pl];
+                return;
             }
+            in.m = 0u;
+            const bool in_slot = (ch.src == SRC_SLOT);
             const V *xs = in_slot ? slots + ((size_t)ch.idx * KA + k0) * U * tile + pl
                                   : static_cast<const V *>(ch.data) + (size_t)k0 * U * ppad + p;
             const size_t stride = in_slot ? tile : ppad;
-            if (sizeof(T) == 4 && leaf) {
+#pragma unroll
+            for (int k = 0; k < KT; ++k) load4<T>(xs + (size_t)k * U * stride, stride, in.x + k * 4);
+            in.l = in_slot ? slot_sc[(size_t)ch.idx * tile + pl]
+                           : static_cast<const S *>(ch.scaler)[p];
+        };
+        auto message = [&](const RecChild &ch, const In &in, T *msg) {
+            const T *area = reinterpret_cast<const T *>(rec + ch.off);
+            const V *P = reinterpret_cast<const V *>(area + (size_t)k0 * 16);
+            const unsigned m = in.m;
+            if (sizeof(T) == 4 && ch.src == SRC_LEAF) {
                 // FP32 leaves: the message of mask m from the record's table.
                 const float4 *t = reinterpret_cast<const float4 *>(area) + (size_t)m * KA + k0;
 #pragma unroll
@@ -467,7 +507,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
                     msg[k * 4 + 2] = (T)v.z;
                     msg[k * 4 + 3] = (T)v.w;
                 }
-            } else if (sizeof(T) == 8 && leaf) {
+            } else if (sizeof(T) == 8 && ch.src == SRC_LEAF) {
                 // FP64 leaves: table lookup (no FP64 arithmetic).
                 const double2 *t = reinterpret_cast<const double2 *>(
                     a.ltab + (((size_t)ch.tab * 16 + m) * KA + k0) * 4);
@@ -479,39 +519,32 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
                 }
             } else {
 #pragma unroll
-            for (int k = 0; k < KT; ++k) {
-                T x[4];
-                if (leaf) {
-                    // Leaf rows are 0/1 state indicators (Lik.pyx:1466-1475):
-                    // P * indicator is exact, as in the reference.
+                for (int k = 0; k < KT; ++k) {
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) x[j] = (T)((m >> j) & 1u);
-                } else {
-                    load4<T>(xs + (size_t)k * U * stride, stride, x);
-                }
+                    for (int i = 0; i < 4; ++i) {
+                        T r[4];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    T r[4];
+                        for (int u = 0; u < U; ++u) {
+                            T tmp[4 / U];
+                            unpack(P[(k * 16 + i * 4) / (4 / U) + u], tmp);
 #pragma unroll
-                    for (int u = 0; u < U; ++u) {
-                        T tmp[4 / U];
-                        unpack(P[(k * 16 + i * 4) / (4 / U) + u], tmp);
-#pragma unroll
-                        for (int q = 0; q < 4 / U; ++q) r[u * (4 / U) + q] = tmp[q];
+                            for (int q = 0; q < 4 / U; ++q) r[u * (4 / U) + q] = tmp[q];
+                        }
+                        const T *x = in.x + k * 4;
+                        T v = r[0] * x[0];
+                        v = fma(r[1], x[1], v);
+                        v = fma(r[2], x[2], v);
+                        v = fma(r[3], x[3], v);
+                        msg[k * 4 + i] = v;
                     }
-                    T v = r[0] * x[0];
-                    v = fma(r[1], x[1], v);
-                    v = fma(r[2], x[2], v);
-                    v = fma(r[3], x[3], v);
-                    msg[k * 4 + i] = v;
                 }
             }
-            }
-            if (!leaf) {
-                const S l = in_slot ? slot_sc[(size_t)ch.idx * tile + pl]
-                                    : static_cast<const S *>(ch.scaler)[p];
-                lns = lns + l;
-            }
+        };
+        // Fold child ci's message into the op: product of messages, sum of
+        // scalers in child order; the plain form's scaler is the max over
+        // every child message (CxLik.c:390-403).
+        auto fold = [&](unsigned ci, const RecChild &ch, const In &in, const T *msg) {
+            if (ch.src != SRC_LEAF) lns = lns + in.l;
             if (ci == 0) {
 #pragma unroll
                 for (int q = 0; q < KT * 4; ++q) acc[q] = msg[q];
@@ -519,28 +552,54 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
 #pragma unroll
                 for (int q = 0; q < KT * 4; ++q) acc[q] *= msg[q];
             }
-            if (sizeof(T) == 8) {
-#pragma unroll
-                for (int q = 0; q < KT * 4; ++q) sc = fmax(sc, msg[q]);
+            if (sizeof(T) == 8) sc = fmax(sc, tree_max<KT * 4>(msg));
+        };
+        // (The FP64 form keeps the loop: both children's rows in registers
+        // at once cost it occupancy, and it is bound by the FP64 pipe.)
+        if (sizeof(T) == 4 && nchild == 2) {
+            const RecChild c0 = kids[0], c1 = kids[1];
+            In in0, in1;
+            load_in(c0, in0);
+            load_in(c1, in1);
+            T msg[KT * 4];
+            message(c0, in0, msg);
+            fold(0, c0, in0, msg);
+            message(c1, in1, msg);
+            fold(1, c1, in1, msg);
+        } else {
+            for (unsigned ci = 0; ci < nchild; ++ci) {
+                const RecChild ch = kids[ci];
+                In in;
+                load_in(ch, in);
+                T msg[KT * 4];
+                message(ch, in, msg);
+                fold(ci, ch, in, msg);
             }
         }
         void *ydata = hd->data;
         void *yscaler = hd->scaler;
         const int yslot = hd->slot;
         const bool yhbm = !(hd->flags & REC_NO_HBM);
+        // Size of the record that refills this stage: only its own bytes
+        // (records of internal children are a third of a leaf table's).
+        const uint32_t nbytes = (L == 1 && hd->next_bytes != 0u &&
+                                 hd->next_bytes <= (uint32_t)sstride)
+                                    ? hd->next_bytes : (uint32_t)sstride;
         // Every thread has read the stage: hand it to op o + R.
         __syncthreads();
-        if (tid == 0 && o + R < a.nops) {
+        if (tid == 0 && o + R < nsteps) {
             if (STAGED) {
                 fence_proxy_async();
-                mbar_expect_tx(&bars[stage], a.rstride);
-                bulk_g2s(ring + (size_t)stage * a.rstride,
-                         a.rec + (size_t)(o + R) * a.rstride, a.rstride, &bars[stage]);
+                mbar_expect_tx(&bars[stage], nbytes);
+                bulk_g2s(ring + (size_t)stage * sstride,
+                         a.rec + (size_t)(o + R) * sstride, nbytes, &bars[stage]);
             } else {
                 issue_stage(a, o + R, ring + (size_t)stage * sstride, &bars[stage], tile_idx,
                             tile, pre);
             }
         }
+        // An empty lane of a step (no children) computes and stores nothing.
+        if (L > 1 && nchild == 0) continue;
         if (sizeof(T) == 8) {
             sc = group_max<G>(sc);
             // Reference rescale: divide by the scaler unless it is 1, add
@@ -553,9 +612,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             }
             lns = lns + (S)log((double)sc);
         } else {
-            T mx = T(0);
-#pragma unroll
-            for (int q = 0; q < KT * 4; ++q) mx = fmax(mx, acc[q]);
+            T mx = fmax(T(0), tree_max<KT * 4>(acc));
             mx = group_max<G>(mx);
             if (mx > T(0) && mx <= (T)3.0e38) {
                 int e;
@@ -600,24 +657,24 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
         for (int k = 0; k < KT; ++k) load4<T>(r + (size_t)k * U * ppad, ppad, acc + k * 4);
         lns = static_cast<const S *>(a.rootsc)[p];
     }
-    // L = sum over components and states in one sequential order; every
+    // Lsum = sum over components and states in one sequential order; every
     // lane of the group gathers the others' entries and sums them all.
-    double L = 0.0;
+    double Lsum = 0.0;
     const unsigned lead = (tid & 31u) - g;
 #pragma unroll
     for (int gg = 0; gg < G; ++gg) {
 #pragma unroll
         for (int q = 0; q < KT * 4; ++q) {
             const T x = G > 1 ? __shfl_sync(0xffffffffu, acc[q], lead + gg) : acc[q];
-            L = fma(__ldg(a.pn + gg * KT * 4 + q), (double)x, L);
+            Lsum = fma(__ldg(a.pn + gg * KT * 4 + q), (double)x, Lsum);
         }
     }
     double v = 0.0;
     bool ninf = false;
-    if (g == 0 && p < a.npat) {
+    if (g == 0 && lane == 0 && p < a.npat) {
         const double lsc = (sizeof(T) == 8) ? (double)lns
                                            : (double)lns * 0.69314718055994530942;
-        v = (log(L) + lsc) * (double)a.freqs[p];
+        v = (log(Lsum) + lsc) * (double)a.freqs[p];
         if (isnan(v)) v = -INFINITY;
         if (a.site) a.site[p] = v;
         if (isinf(v)) {
@@ -900,6 +957,20 @@ __global__ void __launch_bounds__(kMaxThreads) walk_kernel(PlanArgs a) {
     walk_tile<T, KT, G, STAGED>(a, blockIdx.x, Lay, a.ring, phase);
 }
 
+// One plan with L = 2 op lanes (FP32, one thread per pattern, staged
+// leaves): one CTA of NT = 2 x tile threads per tile, tile <= 64.  The
+// bounds keep a 70,000-pattern tree (1,100 tiles of 64, 2,200 of 32) in one
+// wave on 152 SMs: eight 128-thread CTAs per SM (64 registers) or fifteen
+// 64-thread CTAs (68 registers).
+template <int K, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) walk_kernel_lanes(PlanArgs a) {
+    const SmemLayout Lay = smem_layout(CXG_FP32, K, blockDim.x / 2, a.nslot, a.ring,
+                                       a.rstride * 2, 0, a.nleaf);
+    init_ring(Lay, a.ring);
+    uint32_t phase = 0;
+    walk_tile<float, K, 1, true, 2>(a, blockIdx.x, Lay, a.ring, phase);
+}
+
 // Many jobs: a persistent grid claims (job, tile) items in the host's order
 // (longest first).
 template <typename T, int KT, int G, bool STAGED>
@@ -1006,6 +1077,12 @@ static cudaError_t batch_fn(size_t sm, void (**fn)(BatchArgs)) {
     *fn = walk_batch_kernel<T, KT, G, ST>;
     return ensure_smem(walk_batch_kernel<T, KT, G, ST>, sm, optin);
 }
+template <int K, int NT, int MINB>
+static cudaError_t lanes_fn(size_t sm, void (**fn)(PlanArgs)) {
+    static size_t optin = 0;
+    *fn = walk_kernel_lanes<K, NT, MINB>;
+    return ensure_smem(walk_kernel_lanes<K, NT, MINB>, sm, optin);
+}
 template <int K, bool ST>
 static cudaError_t walk2_fn(size_t sm, void (**fn)(PlanArgs)) {
     static size_t optin = 0;
@@ -1061,22 +1138,35 @@ static cudaError_t pick_walker(unsigned kact, unsigned G, bool staged, size_t sm
     return cudaErrorInvalidValue;
 }
 
+// The op-lane walker for kact (FP32), with its dynamic shared memory limit
+// raised to `sm` bytes.
+static cudaError_t pick_walker_lanes(unsigned kact, unsigned tile, size_t sm,
+                                     void (**fn)(PlanArgs)) {
+#define CXG_XL(K) \
+    if (kact == (K))                                                      \
+        return tile == 64 ? lanes_fn<K, 128, 8>(sm, fn) : lanes_fn<K, 64, 15>(sm, fn);
+    CXG_XL(1) CXG_XL(2) CXG_XL(3) CXG_XL(4) CXG_XL(5)
+#undef CXG_XL
+    return cudaErrorInvalidValue;
+}
+
 template <typename T>
-static cudaError_t launch_plan_t(int precision, const PlanArgs &a,
+static cudaError_t launch_plan_t(int precision, const PlanArgs &a, unsigned lanes,
                                  cudaStream_t s) {
     const unsigned G = a.tpp ? a.tpp : 1, NP = a.ppt ? a.ppt : 1;
     const unsigned nb = plan_blocks(a.ppad, a.tile);
     const size_t sm = plan_smem_bytes(precision, a.kact, a.tile, a.nslot,
-                                      a.ring, a.rstride, a.lmax, a.nleaf);
+                                      a.ring, a.rstride * lanes, a.lmax, a.nleaf);
     void (*fn)(PlanArgs) = nullptr;
-    cudaError_t e = NP == 2 ? pick_walker2(a.kact, a.lmax == 0, sm, &fn, false)
-                            : pick_walker<T>(a.kact, G, a.lmax == 0, sm, &fn, false);
+    cudaError_t e = lanes == 2 ? pick_walker_lanes(a.kact, a.tile, sm, &fn)
+                    : NP == 2  ? pick_walker2(a.kact, a.lmax == 0, sm, &fn, false)
+                               : pick_walker<T>(a.kact, G, a.lmax == 0, sm, &fn, false);
     if (e != cudaSuccess) return e;
-    fn<<<nb, a.tile * G / NP, sm, s>>>(a);
+    fn<<<nb, a.tile * G * lanes / NP, sm, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s) {
+cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s, unsigned lanes) {
     const unsigned G = a.tpp ? a.tpp : 1, NP = a.ppt ? a.ppt : 1;
     if (a.tile == 0 || a.tile > kBlock || a.tile % 32 || a.ppad % a.tile ||
         a.tile * G > kMaxThreads || a.tile / NP < 32 ||
@@ -1084,8 +1174,12 @@ cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s) {
         a.ring == 0 || a.ring > 8 || a.rstride % 16 || a.rstride == 0 ||
         a.ntiles != a.ppad / a.tile)
         return cudaErrorInvalidValue;
-    return precision == CXG_FP32 ? launch_plan_t<float>(precision, a, s)
-                                 : launch_plan_t<double>(precision, a, s);
+    if (lanes != 1 && !(lanes == 2 && lanes_shape_ok(precision, a.kact, G, NP) &&
+                        a.lmax == 0 && a.tile * lanes <= kLaneThreads &&
+                        a.nops % lanes == 0))
+        return cudaErrorInvalidValue;
+    return precision == CXG_FP32 ? launch_plan_t<float>(precision, a, lanes, s)
+                                 : launch_plan_t<double>(precision, a, lanes, s);
 }
 
 template <typename T>

@@ -269,6 +269,7 @@ struct Plan {
     double alg_bytes = 0.0;   // algorithmic bytes of one plan-walker launch
     double updates = 0.0;     // pattern-node updates of one run
     unsigned tile = kTile, tpp = 1, ppt = 1, nslot = 0, nleaf = 0;
+    unsigned lanes = 1;       // op lanes of the walker (records per step)
 };
 
 // Launch shape of the plan walker: patterns per CTA, threads per pattern
@@ -276,10 +277,11 @@ struct Plan {
 static unsigned g_tile = kTile;
 static unsigned g_tpp = 1;
 static unsigned g_ppt = 1;
+static unsigned g_lanes = 1;
 static size_t g_smem_budget = 24 * 1024;
 
 static int translate(State &S, CxtLik *lik, int prec, Plan &P,
-                     bool use_slots = true) {
+                     bool use_slots = true, bool allow_lanes = false) {
     int rc;
     if (lik == nullptr) return fail(CXG_EINVAL, "lik is NULL");
     if (lik->dim != 4)
@@ -439,18 +441,69 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     // loses its slot and its consumer reads the HBM copy instead.
     // Record stride: the largest op's header, children and child areas.
     size_t rstride = 16;
-    for (const HostOp &op : ops) {
+    std::vector<size_t> rec_bytes(ops.size());  // each op's record, 16-byte units
+    for (size_t o = 0; o < ops.size(); ++o) {
+        const HostOp &op = ops[o];
         size_t b = sizeof(RecHead) + op.nchild * sizeof(RecChild);
         for (uint32_t c = op.child0; c < op.child0 + op.nchild; ++c)
             b += child_area_bytes(prec, kact, kids[c].src == SRC_LEAF);
         b = (b + 15) & ~(size_t)15;
+        rec_bytes[o] = b;
         if (b > rstride) rstride = b;
     }
-    const unsigned ring = kRing;
+    const bool root_last = !ops.empty() && P.parents.back() == P.root;
+    const unsigned tpp = tuned_tpp(prec, kact, tile);
+    const unsigned ppt = tuned_ppt(prec, kact, tile, tpp);
+    // Op lanes: two mutually independent ops per step (single plans of the
+    // FP32 form with staged leaves, when tuned so).
+    const unsigned lanes =
+        (allow_lanes && g_lanes == 2 && stage_leaves && ops.size() >= 2 &&
+         lanes_shape_ok(prec, kact, tpp, ppt) && tile * 2 <= kLaneThreads)
+            ? 2u : 1u;
+    // order[r]: the op in record position r, or -1 for an empty lane.  With
+    // lanes, each op goes to the earliest step after those of the ops that
+    // produce its children (ops in post-order, steps filled in that order),
+    // and the root takes the last step alone, in lane 0.
+    std::vector<int> order;
+    if (lanes == 1) {
+        order.resize(ops.size());
+        for (size_t o = 0; o < ops.size(); ++o) order[o] = (int)o;
+    } else {
+        std::unordered_map<DevCL *, int> prod;
+        for (size_t o = 0; o < ops.size(); ++o) prod[P.parents[o]] = (int)o;
+        std::vector<int> step_of(ops.size(), 0);
+        std::vector<unsigned> fill;
+        for (size_t o = 0; o < ops.size(); ++o) {
+            size_t lo = 0;
+            for (uint32_t c = ops[o].child0; c < ops[o].child0 + ops[o].nchild; ++c) {
+                if (kids[c].src == SRC_LEAF) continue;
+                auto it = prod.find(kid_cl[c]);
+                if (it != prod.end() && it->second < (int)o)
+                    lo = std::max(lo, (size_t)step_of[it->second] + 1);
+            }
+            const bool alone = root_last && o + 1 == ops.size();
+            if (alone) lo = std::max(lo, fill.size());
+            size_t st = lo;
+            while (st < fill.size() && fill[st] >= lanes) ++st;
+            if (st >= fill.size()) fill.resize(st + 1, 0);
+            step_of[o] = (int)st;
+            fill[st] += alone ? lanes : 1u;
+        }
+        order.assign(fill.size() * lanes, -1);
+        std::vector<unsigned> n_in(fill.size(), 0);
+        for (size_t o = 0; o < ops.size(); ++o) {
+            const size_t st = (size_t)step_of[o];
+            order[st * lanes + n_in[st]++] = (int)o;
+        }
+    }
+    // A stage of the lane walker holds two records: half the stages keep
+    // as many records in flight.
+    const unsigned ring = lanes == 2 ? kRing / 2 : kRing;
+    const unsigned sbytes = (unsigned)rstride * lanes;  // one ring stage
     const size_t base_bytes = plan_smem_bytes(prec, kact, tile, 0, ring,
-                                              (unsigned)rstride, s_lmax, s_nleaf);
+                                              sbytes, s_lmax, s_nleaf);
     const size_t slot_bytes =
-        plan_smem_bytes(prec, kact, tile, 1, ring, (unsigned)rstride, s_lmax, s_nleaf) -
+        plan_smem_bytes(prec, kact, tile, 1, ring, sbytes, s_lmax, s_nleaf) -
         base_bytes;
     unsigned cap = 0;
     if (g_smem_budget > base_bytes)
@@ -459,40 +512,57 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     if (!use_slots) cap = 0;
     unsigned used = 0;
     {
+        // Step by step: every child the step's ops read is taken first, so a
+        // slot they free can hold a result of the same step (results are
+        // stored after the step's release barrier); a slot assigned in this
+        // step is never taken again in it, since both lanes would store it.
         std::vector<int> owner(cap, -1);                 // op holding slot
+        std::vector<size_t> owner_step(cap, 0);
         std::unordered_map<DevCL *, int> made;           // parent -> op
-        for (size_t o = 0; o < ops.size(); ++o) {
-            for (uint32_t c = ops[o].child0; c < ops[o].child0 + ops[o].nchild; ++c) {
-                if (kids[c].src == SRC_LEAF) continue;
-                auto it = made.find(kid_cl[c]);
-                if (it == made.end()) continue;          // from an earlier run
-                const int prod = it->second;
-                const int sl = ops[prod].slot;
-                if (sl >= 0 && owner[sl] == prod) {
-                    kids[c].src = SRC_SLOT;
-                    kids[c].idx = (uint32_t)sl;
-                    owner[sl] = -1;
+        const size_t nsteps = order.size() / lanes;
+        for (size_t st = 0; st < nsteps; ++st) {
+            for (unsigned l = 0; l < lanes; ++l) {
+                const int o = order[st * lanes + l];
+                if (o < 0) continue;
+                for (uint32_t c = ops[o].child0; c < ops[o].child0 + ops[o].nchild; ++c) {
+                    if (kids[c].src == SRC_LEAF) continue;
+                    auto it = made.find(kid_cl[c]);
+                    if (it == made.end()) continue;      // from an earlier run
+                    const int prod = it->second;
+                    const int sl = ops[prod].slot;
+                    if (sl >= 0 && owner[sl] == prod) {
+                        kids[c].src = SRC_SLOT;
+                        kids[c].idx = (uint32_t)sl;
+                        owner[sl] = -1;
+                    }
+                    made.erase(it);
                 }
-                made.erase(it);
             }
-            if (o + 1 == ops.size() || cap == 0) continue;  // root: no slot
-            int sl = -1;
-            for (unsigned k = 0; k < cap && sl < 0; ++k)
-                if (owner[k] < 0) sl = (int)k;
-            if (sl < 0) {
-                int oldest = -1;
-                for (unsigned k = 0; k < cap; ++k)
-                    if (oldest < 0 || owner[k] < owner[oldest]) oldest = (int)k;
-                sl = oldest;
+            for (unsigned l = 0; l < lanes; ++l) {
+                const int o = order[st * lanes + l];
+                if (o < 0) continue;
+                if ((size_t)o + 1 == ops.size() || cap == 0) continue;  // root: no slot
+                int sl = -1;
+                for (unsigned k = 0; k < cap && sl < 0; ++k)
+                    if (owner[k] < 0) sl = (int)k;
+                if (sl < 0) {
+                    int oldest = -1;
+                    for (unsigned k = 0; k < cap; ++k)
+                        if (owner_step[k] != st &&
+                            (oldest < 0 || owner[k] < owner[oldest]))
+                            oldest = (int)k;
+                    sl = oldest;
+                }
+                if (sl < 0) continue;  // every slot taken in this step
+                owner[sl] = o;
+                owner_step[sl] = st;
+                ops[o].slot = sl;
+                made[P.parents[o]] = o;
+                if ((unsigned)sl + 1 > used) used = (unsigned)sl + 1;
             }
-            owner[sl] = (int)o;
-            ops[o].slot = sl;
-            made[P.parents[o]] = (int)o;
-            if ((unsigned)sl + 1 > used) used = (unsigned)sl + 1;
         }
     }
     const unsigned nslot = used;
-    const bool root_last = !ops.empty() && P.parents.back() == P.root;
 
     // Pattern weights, one device copy per (host pointer, length).
     const unsigned *fh = lik->charFreqs + lik->cbase;
@@ -518,7 +588,7 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     const unsigned nchild = (unsigned)kids.size();
     const unsigned nmod = (unsigned)models.size();
     auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
-    const size_t nrec = ops.empty() ? 1 : ops.size();
+    const size_t nrec = order.empty() ? 1 : order.size();
     size_t o_rec = 0;
     size_t o_elen = al(o_rec + nrec * rstride);
     size_t o_cm = al(o_elen + elen.size() * 8);
@@ -543,10 +613,19 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     char *h = static_cast<char *>(S.stage.p);
     memset(h, 0, o_elen);
     uint64_t *dsts = (uint64_t *)(h + o_dst);
-    for (size_t o = 0; o < ops.size(); ++o) {
-        char *r = h + o_rec + o * rstride;
+    for (size_t pos = 0; pos < order.size(); ++pos) {
+        char *r = h + o_rec + pos * rstride;
         RecHead hd;
         memset(&hd, 0, sizeof(hd));
+        if (order[pos] < 0) {  // an empty lane: no children, no result
+            hd.slot = -1;
+            hd.flags = REC_NO_HBM;
+            memcpy(r, &hd, sizeof(hd));
+            continue;
+        }
+        const size_t o = (size_t)order[pos];
+        if (lanes == 1 && pos + ring < order.size())
+            hd.next_bytes = (uint32_t)rec_bytes[order[pos + ring]];
         hd.data = ops[o].data;
         hd.scaler = ops[o].scaler;
         hd.nchild = ops[o].nchild;
@@ -568,7 +647,7 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
             rc_.off = (uint32_t)area;
             memcpy(r + sizeof(RecHead) + ci * sizeof(RecChild), &rc_, sizeof(rc_));
             // Byte offset from the start of the records (pa.rec).
-            dsts[ops[o].child0 + ci] = o * rstride + area;
+            dsts[ops[o].child0 + ci] = pos * rstride + area;
             area += ab;
         }
     }
@@ -645,10 +724,10 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     a.ring = ring;
     a.nslot = nslot;
     a.tile = tile;
-    a.tpp = tuned_tpp(prec, kact, tile);
-    a.ppt = tuned_ppt(prec, kact, tile, a.tpp);
+    a.tpp = tpp;
+    a.ppt = ppt;
     a.root_last = root_last ? 1u : 0u;
-    a.nops = (uint32_t)ops.size();
+    a.nops = (uint32_t)order.size();  // records, empty lanes included
     a.kact = kact;
     a.npat = npat;
     a.ppad = ppad;
@@ -676,6 +755,7 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     P.tile = tile;
     P.tpp = a.tpp;
     P.ppt = a.ppt;
+    P.lanes = lanes;
     P.nslot = nslot;
     P.nleaf = nleaf;
     return 0;
@@ -690,7 +770,7 @@ static int enqueue(State &S, Plan &P, bool want_site,
     CXG_CUDA(cudaMemsetAsync(mp, 0, 32, S.stream));
     CXG_CUDA(launch_pmat(P.pa, S.stream));
     if (e0) CXG_CUDA(cudaEventRecord(e0, S.stream));
-    CXG_CUDA(launch_plan(P.prec, P.a, S.stream));
+    CXG_CUDA(launch_plan(P.prec, P.a, S.stream, P.lanes));
     if (e1) CXG_CUDA(cudaEventRecord(e1, S.stream));
     CXG_CUDA(cudaMemcpyAsync(P.out.p, mp, 32, cudaMemcpyDeviceToHost, S.stream));
     return 0;
@@ -741,7 +821,7 @@ static int execute(CxtLik *lik, int prec, double *lnL, double *site) {
     int rc = ensure_ready(S);
     if (rc) return rc;
     Plan &P = scratch_plan();
-    rc = translate(S, lik, prec, P);
+    rc = translate(S, lik, prec, P, true, true);
     if (rc) return rc;
     rc = enqueue(S, P, site != nullptr);
     if (rc) return rc;
@@ -822,6 +902,20 @@ int cxgTune(unsigned tile, unsigned tpp, unsigned ppt, size_t smem_budget) {
     return 0;
 }
 
+int cxgTuneLanes(unsigned lanes) {
+    if (lanes != 1 && lanes != 2)
+        return fail(CXG_EINVAL, "cxgTuneLanes: op lanes must be 1 or 2");
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    g_lanes = lanes;
+    return 0;
+}
+
+int cxgTuneLanesGet(unsigned *lanes) {
+    if (lanes) *lanes = g_lanes;
+    return 0;
+}
+
 int cxgTuneGet(unsigned *tile, unsigned *tpp, unsigned *ppt, size_t *smem_budget) {
     if (tile) *tile = g_tile;
     if (tpp) *tpp = g_tpp;
@@ -861,7 +955,7 @@ int cxgPlanCreate(CxtLik *lik, int precision, cxgPlan **out) {
     int rc = ensure_ready(S);
     if (rc) return rc;
     cxgPlan *h = new cxgPlan();
-    rc = translate(S, lik, precision, h->p);
+    rc = translate(S, lik, precision, h->p, true, true);
     if (rc) {
         delete h;
         return rc;
@@ -919,6 +1013,12 @@ int cxgPlanShape(const cxgPlan *h, unsigned *tile, unsigned *tpp, unsigned *ppt,
     if (ppt) *ppt = h->p.ppt;
     if (nslot) *nslot = h->p.nslot;
     if (nleaf) *nleaf = h->p.nleaf;
+    return 0;
+}
+
+int cxgPlanLanes(const cxgPlan *h, unsigned *lanes) {
+    if (h == nullptr || lanes == nullptr) return fail(CXG_EINVAL, "cxgPlanLanes: NULL argument");
+    *lanes = h->p.lanes;
     return 0;
 }
 

@@ -921,7 +921,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         hd.nchild = nch;
         hd.slot = op_slot[o];
         hd.flags = 0;
-        hd.pad_ = 0;
+        hd.next_bytes = 0;
         memcpy(r, &hd, sizeof(hd));
         unsigned ci = 0, nkid = kid0[o], nl = 0;
         size_t area = sizeof(RecHead) + nch * sizeof(RecChild);

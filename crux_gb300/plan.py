@@ -54,9 +54,12 @@ class Plan:
                                           ctypes.byref(g), ctypes.byref(p),
                                           ctypes.byref(n), ctypes.byref(l)),
                     "cxgPlanShape")
+        lanes = ctypes.c_uint()
+        self._check(self.lib.cxgPlanLanes(self.h, ctypes.byref(lanes)),
+                    "cxgPlanLanes")
         return {"tile": t.value, "threads_per_pattern": g.value,
                 "patterns_per_thread": p.value, "nslot": n.value,
-                "nleaf": l.value}
+                "nleaf": l.value, "lanes": lanes.value}
 
     def close(self):
         if self.h:

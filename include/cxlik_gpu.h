@@ -222,6 +222,8 @@ int cxgPlanDestroy(cxgPlan *plan);
  * patterns per thread, shared-memory stack slots, distinct leaves. */
 int cxgPlanShape(const cxgPlan *plan, unsigned *tile, unsigned *threads_per_pattern,
                  unsigned *patterns_per_thread, unsigned *nslot, unsigned *nleaf);
+/* Op lanes the plan's walker runs with (cxgTuneLanes). */
+int cxgPlanLanes(const cxgPlan *plan, unsigned *lanes);
 
 /* The step planner of Lik._planRecurse / Lik._plan (Lik.pyx:1427-1601) run
  * natively over one rooted traversal of a tree, flattened once by the host
@@ -442,6 +444,13 @@ int cxgTune(unsigned tile, unsigned threads_per_pattern,
             unsigned patterns_per_thread, size_t smem_budget);
 int cxgTuneGet(unsigned *tile, unsigned *threads_per_pattern,
                unsigned *patterns_per_thread, size_t *smem_budget);
+/* Op lanes of the single-plan walker (cxgLikExecuteLnL, CxLikExecute,
+ * cxgPlanCreate), 1 or 2.  With 2, plans of the FP32 form that stage their
+ * leaves, with one thread and one pattern per thread and <= 5 components,
+ * run two mutually independent node updates per step on two groups of
+ * threads over the same patterns; other plans keep one lane.  Same bits. */
+int cxgTuneLanes(unsigned lanes);
+int cxgTuneLanesGet(unsigned *lanes);
 
 /* No counterpart in the reference.  Evaluate lik's plan without allocating
  * anything, for callers that cannot call cudaMalloc.  Such a caller may

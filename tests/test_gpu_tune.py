@@ -1,7 +1,7 @@
 """Walker shapes and the autotuner: every (tile, threads per pattern,
-patterns per thread, stack budget) gives bit-identical lnLs and site lnLs, in single plans and
-in batches, within the oracle tolerance of each form; the tuner times its
-candidates and sets the fastest."""
+patterns per thread, stack budget, op lanes) gives bit-identical lnLs and
+site lnLs, in single plans and in batches, within the oracle tolerance of
+each form; the tuner times its candidates and sets the fastest."""
 import numpy as np
 import pytest
 
@@ -34,10 +34,12 @@ def test_every_shape_same_bits(gpu, port, restore, precision, shape):
     kact = tune.active_components(lik)
     assert kact == (4 if pinv == 0.0 else 5)
     shapes = tune.candidates(precision, kact)
-    assert any(g > 1 for _, g, _, _ in shapes) == (precision == "fp32" and
-                                                   kact % 2 == 0)
-    assert any(p > 1 for _, _, p, _ in shapes) == (precision == "fp32" and
-                                                   kact <= 5)
+    assert any(g > 1 for _, g, _, _, _ in shapes) == (precision == "fp32" and
+                                                      kact % 2 == 0)
+    assert any(p > 1 for _, _, p, _, _ in shapes) == (precision == "fp32" and
+                                                      kact <= 5)
+    assert any(n > 1 for _, _, _, _, n in shapes) == (precision == "fp32" and
+                                                      kact <= 5)
     first = None
     for shape in shapes:
         tune.set_shape(gpu, *shape)
@@ -59,7 +61,7 @@ def test_batch_every_shape_same_bits(gpu, restore):
                         0.1, 300 + i) for i in range(6)]
     liks = [c.lik(lib=gpu, precision="fp32") for c in cases]
     first = None
-    for shape in tune.candidates("fp32", 4, budgets=(0, 24 << 10)):
+    for shape in tune.candidates("fp32", 4, budgets=(0, 24 << 10), lanes=(1,)):
         tune.set_shape(gpu, *shape)
         for lk in liks:
             lk.prepare_plan()
@@ -76,14 +78,56 @@ def test_tune_plan_sets_fastest(gpu, restore):
     case = synth.Case(32, 20000, 0.1, 91)
     lik = case.lik(lib=gpu, precision="fp32")
     lik.prepare_plan()
-    shapes = [(64, 1, 1, 24 << 10), (64, 4, 1, 24 << 10),
-              (128, 2, 1, 12 << 10), (128, 1, 2, 24 << 10)]
+    shapes = [(64, 1, 1, 24 << 10, 1), (64, 4, 1, 24 << 10, 1),
+              (128, 2, 1, 12 << 10, 1), (128, 1, 2, 24 << 10, 1),
+              (64, 1, 1, 24 << 10, 2)]
     res = tune.tune_plan(lik, "fp32", iters=5, shapes=shapes)
-    assert len(res["table"]) == 4
+    assert len(res["table"]) == 5
     best = res["best"]
     assert best["ms"] == min(r["ms"] for r in res["table"])
     assert tune.get(gpu) == (best["tile"], best["tpp"], best["ppt"],
-                             best["budget"])
+                             best["budget"], best["lanes"])
+
+
+@pytest.mark.parametrize("tile", [32, 64])
+def test_op_lanes_same_bits_on_dirty_paths(gpu, port, restore, tile):
+    """Two op lanes against one on full plans, single-branch dirty paths
+    (chains of dependent ops, so most steps have an empty lane) and other
+    roots, with and without a stack budget: the same bits every time, and
+    the oracle within the FP32 tolerance."""
+    import random
+    from crux_gb300.plan import Plan
+    case = synth.Case(48, 4000, 0.1, 123, pinv=0.2, gap_frac=0.01)
+    one = case.lik(lib=gpu, precision="fp32")
+    two = case.lik(lib=gpu, precision="fp32")
+    ref = case.lik(lib=port)
+    rng = random.Random(9)
+    lanes_seen = set()
+    for it in range(40):
+        if it % 10 == 0:
+            for lk in (one, two, ref):
+                lk.lik.invalidate = True
+        else:
+            i = rng.randrange(len(ref.tree.edges))
+            f = rng.uniform(0.5, 2.0)
+            for lk in (one, two, ref):
+                lk.tree.edges[i].length *= f
+        budget = (0, 12 << 10, 24 << 10)[it % 3]
+        k = rng.randrange(len(ref.tree.nodes)) if it % 7 == 3 else None
+        roots = [None if k is None else lk.tree.nodes[k]
+                 for lk in (one, two, ref)]
+        tune.set_shape(gpu, tile, 1, 1, budget, 1)
+        a = one.lnL(roots[0])
+        tune.set_shape(gpu, tile, 1, 1, budget, 2)
+        two._prep(roots[1])
+        plan = Plan(two, "fp32")
+        lanes_seen.add(plan.shape()["lanes"])
+        b = plan.run()
+        plan.close()
+        want = ref.lnL(roots[2])
+        assert a == b, (it, a, b)
+        assert abs(a - want) <= TOL["fp32"] * abs(want)
+    assert 2 in lanes_seen
 
 
 def test_mc3_and_server_follow_the_shape(gpu, restore):
@@ -95,8 +139,8 @@ def test_mc3_and_server_follow_the_shape(gpu, restore):
     aln = case.alignment()
     req = PreparedRequest(case, LNL)
     traces, served = [], []
-    shapes = [(64, 1, 1, 24 << 10), (64, 4, 1, 24 << 10), (32, 2, 1, 0),
-              (128, 1, 2, 24 << 10)]
+    shapes = [(64, 1, 1, 24 << 10, 1), (64, 4, 1, 24 << 10, 1), (32, 2, 1, 0, 1),
+              (128, 1, 2, 24 << 10, 2)]
     for shape in shapes:
         tune.set_shape(gpu, *shape)
         m = Mc3(case.tree(aln.taxaMap), aln, case.params["rates"],

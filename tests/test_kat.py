@@ -91,17 +91,26 @@ def test_tune_candidates_follow_walker_shapes():
     """The autotuner offers only shapes the library has a walker for."""
     from crux_gb300 import tune
     c4 = tune.candidates("fp32", 4)
-    assert (64, 4, 1, 24 << 10) in c4 and (128, 2, 1, 0) in c4
-    assert all(t * g <= 256 for t, g, _, _ in c4)
-    assert (128, 4, 1, 0) not in c4
+    assert (64, 4, 1, 24 << 10, 1) in c4 and (128, 2, 1, 0, 1) in c4
+    assert all(t * g * n <= 256 for t, g, _, _, n in c4)
+    assert (128, 4, 1, 0, 1) not in c4
     # Two patterns per thread: FP32, one thread per pattern, <= 5
     # components, and a tile that keeps at least one warp.
-    assert (128, 1, 2, 0) in c4 and (64, 1, 2, 0) in c4
-    assert (32, 1, 2, 0) not in c4 and (64, 2, 2, 0) not in c4
-    assert all(g == 1 for _, g, _, _ in tune.candidates("fp32", 5))
-    assert {p for _, _, p, _ in tune.candidates("fp32", 5)} == {1, 2}
-    assert all(g == 1 for _, g, _, _ in tune.candidates("fp64", 4))
-    assert all(p == 1 for _, _, p, _ in tune.candidates("fp64", 4))
-    assert all(p == 1 for _, _, p, _ in tune.candidates("fp32", 6))
-    assert {g for _, g, _, _ in tune.candidates("fp32", 6)} == {1, 2}
-    assert {g for _, g, _, _ in tune.candidates("fp32", 8)} == {1, 2, 4}
+    assert (128, 1, 2, 0, 1) in c4 and (64, 1, 2, 0, 1) in c4
+    assert (32, 1, 2, 0, 1) not in c4 and (64, 2, 2, 0, 1) not in c4
+    # Two op lanes: FP32, one thread and one pattern per thread, <= 5
+    # components, tile <= 64.
+    assert (64, 1, 1, 0, 2) in c4 and (32, 1, 1, 24 << 10, 2) in c4
+    assert (128, 1, 1, 0, 2) not in c4 and (64, 2, 1, 0, 2) not in c4
+    assert (64, 1, 2, 0, 2) not in c4
+    assert all(n == 1 for *_, n in tune.candidates("fp32", 4, lanes=(1,)))
+    assert {n for *_, n in tune.candidates("fp32", 5)} == {1, 2}
+    assert all(n == 1 for *_, n in tune.candidates("fp32", 6))
+    assert all(n == 1 for *_, n in tune.candidates("fp64", 4))
+    assert all(g == 1 for _, g, _, _, _ in tune.candidates("fp32", 5))
+    assert {p for _, _, p, _, _ in tune.candidates("fp32", 5)} == {1, 2}
+    assert all(g == 1 for _, g, _, _, _ in tune.candidates("fp64", 4))
+    assert all(p == 1 for _, _, p, _, _ in tune.candidates("fp64", 4))
+    assert all(p == 1 for _, _, p, _, _ in tune.candidates("fp32", 6))
+    assert {g for _, g, _, _, _ in tune.candidates("fp32", 6)} == {1, 2}
+    assert {g for _, g, _, _, _ in tune.candidates("fp32", 8)} == {1, 2, 4}
