@@ -183,6 +183,12 @@ __device__ inline void qdecomp4(const double *rtri, const double *pi, double *ou
 #pragma unroll
     for (int i = 0; i < 4; ++i) out[i] = pn[i];
     out[4] = 1.0 / qscale;
+    // V = Pi^-1/2 U and V^-1 = U^T Pi^1/2: cube[i][j][k] = V[i][k] V^-1[k][j].
+    // Four reciprocals instead of 64 divisions (FP64 division is a long
+    // instruction sequence on this part); V[i][k] moves by at most an ulp.
+    double isq[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) isq[i] = 1.0 / sq[i];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -190,7 +196,7 @@ __device__ inline void qdecomp4(const double *rtri, const double *pi, double *ou
 #pragma unroll
             for (int k = 0; k < 4; ++k)
                 out[5 + i * 16 + j * 4 + k] =
-                    (u[i * 4 + k] / sq[i]) * (u[j * 4 + k] * sq[j]);
+                    (u[i * 4 + k] * isq[i]) * (u[j * 4 + k] * sq[j]);
 #pragma unroll
     for (int k = 0; k < 4; ++k) out[69 + k] = s[k * 4 + k];
     out[73] = conv ? 0.0 : 2.0;

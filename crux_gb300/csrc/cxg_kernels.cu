@@ -443,6 +443,13 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
 
     T acc[KT * 4];
     S lns = S(0);
+    // The last result this thread computed (its parent buffer and scaler;
+    // the values are acc).  A child of the next op that is that buffer --
+    // in a post-order, the next op is often the parent -- is taken from
+    // registers instead of being read back: the same values, since the
+    // stored FP32 row is acc itself.
+    const void *prev_data = nullptr;
+    S prev_lns = S(0);
     for (unsigned o = 0; o < nsteps; ++o) {
         const unsigned stage = o % R;
         // Streaming: thread 0 reads op o + R's leaf-row pointers now; it
@@ -559,8 +566,26 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
         if (sizeof(T) == 4 && nchild == 2) {
             const RecChild c0 = kids[0], c1 = kids[1];
             In in0, in1;
-            load_in(c0, in0);
-            load_in(c1, in1);
+            const bool f0 = L == 1 && prev_data != nullptr && c0.src != SRC_LEAF &&
+                            c0.data == prev_data;
+            const bool f1 = L == 1 && prev_data != nullptr && c1.src != SRC_LEAF &&
+                            c1.data == prev_data;
+            if (f0) {
+#pragma unroll
+                for (int q = 0; q < KT * 4; ++q) in0.x[q] = acc[q];
+                in0.l = prev_lns;
+                in0.m = 0u;
+            } else {
+                load_in(c0, in0);
+            }
+            if (f1) {
+#pragma unroll
+                for (int q = 0; q < KT * 4; ++q) in1.x[q] = acc[q];
+                in1.l = prev_lns;
+                in1.m = 0u;
+            } else {
+                load_in(c1, in1);
+            }
             T msg[KT * 4];
             message(c0, in0, msg);
             fold(0, c0, in0, msg);
@@ -644,6 +669,8 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             for (int k = 0; k < KT; ++k) store4<T>(ys + (size_t)k * U * tile, tile, acc + k * 4);
             if (g == 0) slot_sc[(size_t)yslot * tile + pl] = lns;
         }
+        prev_data = ydata;
+        prev_lns = lns;
     }
 
     if (a.no_root) {
