@@ -270,8 +270,10 @@ cudaError_t launch_pmat(const PmatArgs &a, cudaStream_t s);
 cudaError_t launch_pmat_batch(const PmatArgs *jobs, const uint32_t *prefix,
                               uint32_t njobs, uint32_t total, cudaStream_t s);
 // `lanes` 2: the op-lane walker (the plan's records come in steps of two).
+// `pdl`: launch as a programmatic dependent of the P kernel launched just
+// before it on `s` (the walker stages its leaves while the P kernel runs).
 cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s,
-                        unsigned lanes = 1);
+                        unsigned lanes = 1, bool pdl = false);
 cudaError_t launch_qdecomp(const double *rtri, const double *pi, double *out,
                            cudaStream_t s);
 unsigned plan_blocks(unsigned ppad, unsigned tile);

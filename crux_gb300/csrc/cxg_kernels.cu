@@ -34,7 +34,20 @@ namespace cxg {
 // P matrices, written into the op records.
 // ---------------------------------------------------------------------------
 // Four lanes per (child edge, component), see pmat_one.
+// Programmatic dependent launch: a walker launched as a dependent of the
+// P kernel may start (be scheduled, set up its shared memory and barriers)
+// once every P block has started; it waits here, before it copies its
+// first records, for the P kernel's matrices and their memory.  Without
+// such a dependency both instructions do nothing.
+__device__ __forceinline__ void pdl_launch_dependents() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 __global__ void pmat_kernel(PmatArgs a) {
+    pdl_launch_dependents();
     const unsigned idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
     if (idx >= a.nchild * a.kact) return;  // the same for all four lanes
     pmat_one(a, idx, threadIdx.x & 3u);
@@ -413,6 +426,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
     const unsigned nsteps = a.nops / L;  // the host pads nops to a multiple
 
     if (STAGED) {
+        pdl_wait();  // the records hold the P kernel's matrices
         // Start streaming the job's first R steps of op records.
         if (tid == 0) {
             fence_proxy_async();
@@ -432,6 +446,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
         }
         __syncthreads();
     } else {
+        pdl_wait();
         // Start streaming the job's first R stages (records and leaf rows).
         if (tid == 0)
             for (unsigned o = 0; o < R && o < a.nops; ++o) {
@@ -753,6 +768,7 @@ __device__ bool walk_tile2(const PlanArgs &a, unsigned tile_idx, const SmemLayou
     const unsigned R = ring_depth;
 
     if (STAGED) {
+        pdl_wait();
         if (tid == 0) {
             fence_proxy_async();
             for (unsigned o = 0; o < R && o < a.nops; ++o) {
@@ -770,6 +786,7 @@ __device__ bool walk_tile2(const PlanArgs &a, unsigned tile_idx, const SmemLayou
         }
         __syncthreads();
     } else {
+        pdl_wait();
         if (tid == 0)
             for (unsigned o = 0; o < R && o < a.nops; ++o) {
                 const uint8_t *rows0[kLeafPre];
@@ -973,9 +990,19 @@ __device__ __forceinline__ void init_ring(const SmemLayout &Lay, unsigned R) {
     __syncthreads();
 }
 
+// Register cap of the FP32 walkers with up to five components a thread:
+// 128.  A 70,000-pattern tree is 1,100 tiles of 64 patterns, and eight
+// 64-thread CTAs per SM (one wave on 152 SMs) need registers <= 128; above,
+// a second wave doubles the tail.  Wider shapes keep the compiler's choice.
+template <typename T, int KT>
+constexpr int walker_min_blocks() {
+    return (sizeof(T) == 4 && KT <= 5) ? 2 : 1;
+}
+
 // One plan: one CTA per tile.
 template <typename T, int KT, int G, bool STAGED>
-__global__ void __launch_bounds__(kMaxThreads) walk_kernel(PlanArgs a) {
+__global__ void __launch_bounds__(kMaxThreads, walker_min_blocks<T, KT>())
+    walk_kernel(PlanArgs a) {
     const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT * G,
                                        blockDim.x / G, a.nslot, a.ring,
                                        a.rstride, a.lmax, a.nleaf);
@@ -1001,7 +1028,8 @@ __global__ void __launch_bounds__(NT, MINB) walk_kernel_lanes(PlanArgs a) {
 // Many jobs: a persistent grid claims (job, tile) items in the host's order
 // (longest first).
 template <typename T, int KT, int G, bool STAGED>
-__global__ void __launch_bounds__(kMaxThreads) walk_batch_kernel(BatchArgs b) {
+__global__ void __launch_bounds__(kMaxThreads, walker_min_blocks<T, KT>())
+    walk_batch_kernel(BatchArgs b) {
     __shared__ unsigned s_item;
     __shared__ __align__(16) PlanArgs s_job;
     const SmemLayout Lay = smem_layout(sizeof(T) == 4 ? CXG_FP32 : CXG_FP64, KT * G,
@@ -1179,7 +1207,7 @@ static cudaError_t pick_walker_lanes(unsigned kact, unsigned tile, size_t sm,
 
 template <typename T>
 static cudaError_t launch_plan_t(int precision, const PlanArgs &a, unsigned lanes,
-                                 cudaStream_t s) {
+                                 bool pdl, cudaStream_t s) {
     const unsigned G = a.tpp ? a.tpp : 1, NP = a.ppt ? a.ppt : 1;
     const unsigned nb = plan_blocks(a.ppad, a.tile);
     const size_t sm = plan_smem_bytes(precision, a.kact, a.tile, a.nslot,
@@ -1189,11 +1217,27 @@ static cudaError_t launch_plan_t(int precision, const PlanArgs &a, unsigned lane
                     : NP == 2  ? pick_walker2(a.kact, a.lmax == 0, sm, &fn, false)
                                : pick_walker<T>(a.kact, G, a.lmax == 0, sm, &fn, false);
     if (e != cudaSuccess) return e;
-    fn<<<nb, a.tile * G * lanes / NP, sm, s>>>(a);
+    const unsigned nt = a.tile * G * lanes / NP;
+    if (pdl) {
+        // A dependent of the P kernel just before it on the stream.
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(nb);
+        cfg.blockDim = dim3(nt);
+        cfg.dynamicSmemBytes = sm;
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, fn, a);
+    }
+    fn<<<nb, nt, sm, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s, unsigned lanes) {
+cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s, unsigned lanes,
+                        bool pdl) {
     const unsigned G = a.tpp ? a.tpp : 1, NP = a.ppt ? a.ppt : 1;
     if (a.tile == 0 || a.tile > kBlock || a.tile % 32 || a.ppad % a.tile ||
         a.tile * G > kMaxThreads || a.tile / NP < 32 ||
@@ -1205,8 +1249,8 @@ cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s, unsign
                         a.lmax == 0 && a.tile * lanes <= kLaneThreads &&
                         a.nops % lanes == 0))
         return cudaErrorInvalidValue;
-    return precision == CXG_FP32 ? launch_plan_t<float>(precision, a, lanes, s)
-                                 : launch_plan_t<double>(precision, a, lanes, s);
+    return precision == CXG_FP32 ? launch_plan_t<float>(precision, a, lanes, pdl, s)
+                                 : launch_plan_t<double>(precision, a, lanes, pdl, s);
 }
 
 template <typename T>

@@ -611,7 +611,9 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     rc = P.prog.ensure(total);
     if (rc) return rc;
     char *h = static_cast<char *>(S.stage.p);
-    memset(h, 0, o_elen);
+    // Record bytes are not zeroed: every header and child descriptor is
+    // written whole below, the child areas by the P kernel, and no kernel
+    // reads a record past its own bytes.
     uint64_t *dsts = (uint64_t *)(h + o_dst);
     for (size_t pos = 0; pos < order.size(); ++pos) {
         char *r = h + o_rec + pos * rstride;
@@ -763,14 +765,18 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
 
 // Enqueue one run (P matrices, plan walk, result copy) on the stream;
 // optional events bracket the plan-walker launch.
+// `pdl`: the walker is a programmatic dependent of the P kernel (not with
+// timing events, whose walker span must be the walker alone).
 static int enqueue(State &S, Plan &P, bool want_site,
-                   cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr) {
+                   cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr,
+                   bool pdl = false) {
     char *mp = static_cast<char *>(P.misc.p);
     P.a.site = want_site ? (double *)(mp + 32) : nullptr;
     CXG_CUDA(cudaMemsetAsync(mp, 0, 32, S.stream));
     CXG_CUDA(launch_pmat(P.pa, S.stream));
     if (e0) CXG_CUDA(cudaEventRecord(e0, S.stream));
-    CXG_CUDA(launch_plan(P.prec, P.a, S.stream, P.lanes));
+    CXG_CUDA(launch_plan(P.prec, P.a, S.stream, P.lanes,
+                         pdl && e0 == nullptr && P.pa.nchild > 0));
     if (e1) CXG_CUDA(cudaEventRecord(e1, S.stream));
     CXG_CUDA(cudaMemcpyAsync(P.out.p, mp, 32, cudaMemcpyDeviceToHost, S.stream));
     return 0;
@@ -823,7 +829,7 @@ static int execute(CxtLik *lik, int prec, double *lnL, double *site) {
     Plan &P = scratch_plan();
     rc = translate(S, lik, prec, P, true, true);
     if (rc) return rc;
-    rc = enqueue(S, P, site != nullptr);
+    rc = enqueue(S, P, site != nullptr, nullptr, nullptr, true);
     if (rc) return rc;
     S.last_d2h = 32 + (site ? (size_t)P.npat * 8 : 0);
     return finish(S, P, lnL, site);
