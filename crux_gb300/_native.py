@@ -33,6 +33,10 @@ def declare(lib):
     lib.cxgLikClForget.restype = c_int
     lib.cxgLikReset.argtypes = []
     lib.cxgLikReset.restype = c_int
+    lib.cxgLikSetPatternWeights.argtypes = [P(c_uint), c_uint]
+    lib.cxgLikSetPatternWeights.restype = c_int
+    lib.cxgLikForgetPatternWeights.argtypes = [P(c_uint), c_uint]
+    lib.cxgLikForgetPatternWeights.restype = c_int
     lib.cxgLikExecuteLnL.argtypes = [P(_abi.CxtLik), c_int, P(c_double),
                                      P(c_double)]
     lib.cxgLikExecuteLnL.restype = c_int

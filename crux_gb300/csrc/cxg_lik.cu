@@ -48,6 +48,9 @@ struct DevCL {
     void *data = nullptr;
     void *scaler = nullptr;
     bool computed = false;
+    // Translation that made this buffer a parent (State::gen); a child of
+    // a later op in the same translation is then "written in this plan".
+    unsigned long long gen = 0;
 };
 
 // Grow-only device buffer.
@@ -94,6 +97,9 @@ struct HostBuf {
 struct FreqEntry {
     DevBuf dev;
     std::vector<unsigned> host;
+    // Registered by cxgLikSetPatternWeights: the caller keeps the host values
+    // unchanged while registered, so calls skip the compare.
+    bool registered = false;
 };
 
 struct State {
@@ -111,6 +117,13 @@ struct State {
     cudaEvent_t stage_ev = nullptr;
     bool stage_pending = false;
     std::unordered_map<std::string, FreqEntry> freqs;
+    unsigned long long gen = 0;  // translations so far
+    // Changes to the CL registry (a buffer allocated, replaced, forgotten or
+    // cleared): a kept translation is valid only for the count it saw.
+    unsigned long long epoch = 0;
+    // The scratch plan's last translation, by the key of plan_key().
+    std::vector<uint64_t> last_key;
+    bool last_valid = false;
 };
 
 static State &state() {
@@ -156,6 +169,7 @@ static int parent_buffer(State &S, const CxtLikCL *cl, unsigned npat,
         }
         free_cl(S, c);
         S.cls.erase(it);
+        ++S.epoch;
     }
     DevCL c;
     c.kind = CL_INTERNAL;
@@ -172,6 +186,7 @@ static int parent_buffer(State &S, const CxtLikCL *cl, unsigned npat,
     }
     S.cl_bytes += (size_t)kact * 4 * ppad * elt + (size_t)ppad * 8;
     auto ins = S.cls.emplace(key, c);
+    ++S.epoch;
     *out = &ins.first->second;
     return 0;
 }
@@ -185,6 +200,7 @@ static int upload_leaf(State &S, const double *key, const uint8_t *masks,
         free_cl(S, it->second);
         S.cls.erase(it);
     }
+    ++S.epoch;
     DevCL c;
     c.kind = CL_LEAF;
     c.npat = n;
@@ -234,16 +250,14 @@ static int leaf_child(State &S, const CxtLik *lik, const CxtLikCL *cl,
 }
 
 // Internal child: computed by an earlier run at this precision, or by an
-// earlier op of the plan being translated (`written`).
+// earlier op of the plan being translated (translation `gen`).
 static int internal_child(State &S, const CxtLik *lik, const CxtLikCL *cl,
-                          unsigned kact, int prec,
-                          const std::vector<DevCL *> &written, DevCL **out) {
+                          unsigned kact, int prec, unsigned long long gen,
+                          DevCL **out) {
     if (cl == nullptr || cl->cLMat == nullptr)
         return fail(CXG_EINVAL, "internal child CL has no cLMat");
     auto it = S.cls.find((uintptr_t)cl->cLMat);
-    bool earlier = false;
-    if (it != S.cls.end())
-        for (DevCL *w : written) earlier |= (w == &it->second);
+    const bool earlier = it != S.cls.end() && it->second.gen == gen;
     if (it == S.cls.end() || it->second.kind != CL_INTERNAL ||
         !(it->second.computed || earlier) || it->second.precision != prec ||
         it->second.npat != lik->mschars || it->second.kcap < kact)
@@ -270,10 +284,64 @@ struct Plan {
     double updates = 0.0;     // pattern-node updates of one run
     unsigned tile = kTile, tpp = 1, ppt = 1, nslot = 0, nleaf = 0;
     unsigned lanes = 1;       // op lanes of the walker (records per step)
+    // Where the per-call values sit in the program (byte offsets): branch
+    // lengths [stepsLen], cmult, rmult, model index [kact], cube and
+    // eigenvalues [models], root weights pn [kact][4]; and what they are
+    // read from (active components, their models).
+    size_t o_elen = 0, o_cm = 0, o_rm = 0, o_mod = 0, o_cube = 0, o_eig = 0,
+           o_dst = 0, o_pn = 0;
+    std::vector<unsigned> act;
+    std::vector<const CxtLikModel *> models;
+    std::vector<int32_t> model_of;
 };
 
 // Launch shape of the plan walker: patterns per CTA, threads per pattern
 // and the shared-memory budget of the CL stack (set by cxgTune).
+// Device copy of lik's pattern weights, one per (host pointer, length),
+// uploaded again whenever the host values differ from the kept copy.
+static int pattern_weights(State &S, const CxtLik *lik, const void **out) {
+    const unsigned npat = lik->mschars;
+    const unsigned *fh = lik->charFreqs + lik->cbase;
+    char key[64];
+    snprintf(key, sizeof(key), "%p:%u", (const void *)fh, npat);
+    FreqEntry &fe = S.freqs[key];
+    if (fe.registered && fe.dev.p != nullptr && fe.host.size() == npat) {
+        *out = fe.dev.p;
+        return 0;
+    }
+    if (fe.dev.p == nullptr || fe.host.size() != npat ||
+        memcmp(fe.host.data(), fh, (size_t)npat * 4) != 0) {
+        int rc = fe.dev.ensure((size_t)npat * 4);
+        if (rc) return rc;
+        CXG_CUDA(cudaMemcpy(fe.dev.p, fh, (size_t)npat * 4, cudaMemcpyHostToDevice));
+        fe.host.assign(fh, fh + npat);
+    }
+    *out = fe.dev.p;
+    return 0;
+}
+
+// The per-call values of a translated plan, into program image h: every
+// step's branch length (each step has one child, so child c is step c),
+// the active components' cmult, rmult, model index and root weights, and
+// each model's eigenvector cube and eigenvalues.
+static void pack_values(const CxtLik *lik, const Plan &P, char *h) {
+    double *el = reinterpret_cast<double *>(h + P.o_elen);
+    for (unsigned s = 0; s < lik->stepsLen; ++s) el[s] = lik->steps[s].edgeLen;
+    for (unsigned k = 0; k < P.kact; ++k) {
+        const CxtLikComp &cp = lik->comps[P.act[k]];
+        reinterpret_cast<double *>(h + P.o_cm)[k] = cp.cmult;
+        reinterpret_cast<double *>(h + P.o_rm)[k] = cp.model->rmult;
+        reinterpret_cast<int32_t *>(h + P.o_mod)[k] = P.model_of[k];
+        for (unsigned i = 0; i < 4; ++i)
+            reinterpret_cast<double *>(h + P.o_pn)[k * 4 + i] =
+                cp.model->piDiagNorm[i] * cp.weightScaled;
+    }
+    for (size_t m = 0; m < P.models.size(); ++m) {
+        memcpy(h + P.o_cube + m * 64 * 8, P.models[m]->qEigVecCube, 64 * 8);
+        memcpy(h + P.o_eig + m * 4 * 8, P.models[m]->qEigVals, 4 * 8);
+    }
+}
+
 static unsigned g_tile = kTile;
 static unsigned g_tpp = 1;
 static unsigned g_ppt = 1;
@@ -331,6 +399,7 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     std::vector<DevCL *> kid_cl;
     int32_t ntab = 0;
     P.parents.clear();
+    const unsigned long long gen = ++S.gen;
     const CxtLikCL *cur_parent = nullptr;
     unsigned expect_trail = 0;
     const double s_el = prec == CXG_FP32 ? 4.0 : 8.0;
@@ -357,6 +426,7 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
             op.slot = -1;
             ops.push_back(op);
             P.parents.push_back(pc);
+            pc->gen = gen;
             cur_parent = st.parentCL;
             bytes += 4.0 * kact * s_el + e_el;  // parent written
         } else {
@@ -366,7 +436,7 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
         }
         DevCL *cc = nullptr;
         rc = leaf ? leaf_child(S, lik, st.childCL, &cc)
-                  : internal_child(S, lik, st.childCL, kact, prec, P.parents,
+                  : internal_child(S, lik, st.childCL, kact, prec, gen,
                                    &cc);
         if (rc) return rc;
         if (cc->data == P.parents.back()->data)
@@ -565,22 +635,9 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
     const unsigned nslot = used;
 
     // Pattern weights, one device copy per (host pointer, length).
-    const unsigned *fh = lik->charFreqs + lik->cbase;
     const void *dfreqs = nullptr;
-    {
-        char key[64];
-        snprintf(key, sizeof(key), "%p:%u", (const void *)fh, npat);
-        FreqEntry &fe = S.freqs[key];
-        if (fe.dev.p == nullptr || fe.host.size() != npat ||
-            memcmp(fe.host.data(), fh, (size_t)npat * 4) != 0) {
-            rc = fe.dev.ensure((size_t)npat * 4);
-            if (rc) return rc;
-            CXG_CUDA(cudaMemcpy(fe.dev.p, fh, (size_t)npat * 4,
-                                cudaMemcpyHostToDevice));
-            fe.host.assign(fh, fh + npat);
-        }
-        dfreqs = fe.dev.p;
-    }
+    rc = pattern_weights(S, lik, &dfreqs);
+    if (rc) return rc;
 
     // Pack the program into pinned staging, one copy:
     //   records [nops][rstride] | elen | cmult | rmult | model | cube | eig |
@@ -653,21 +710,20 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
             area += ab;
         }
     }
-    if (!elen.empty()) memcpy(h + o_elen, elen.data(), elen.size() * 8);
     for (unsigned c = 0; c < nchild; ++c) ((int32_t *)(h + o_tab))[c] = kids[c].tab;
-    for (unsigned k = 0; k < kact; ++k) {
-        const CxtLikComp &cp = lik->comps[act[k]];
-        ((double *)(h + o_cm))[k] = cp.cmult;
-        ((double *)(h + o_rm))[k] = cp.model->rmult;
-        ((int32_t *)(h + o_mod))[k] = model_of[k];
-        for (unsigned i = 0; i < 4; ++i)
-            ((double *)(h + o_pn))[k * 4 + i] =
-                cp.model->piDiagNorm[i] * cp.weightScaled;
-    }
-    for (unsigned m = 0; m < nmod; ++m) {
-        memcpy(h + o_cube + m * 64 * 8, models[m]->qEigVecCube, 64 * 8);
-        memcpy(h + o_eig + m * 4 * 8, models[m]->qEigVals, 4 * 8);
-    }
+    P.kact = kact;
+    P.o_elen = o_elen;
+    P.o_cm = o_cm;
+    P.o_rm = o_rm;
+    P.o_mod = o_mod;
+    P.o_cube = o_cube;
+    P.o_eig = o_eig;
+    P.o_dst = o_dst;
+    P.o_pn = o_pn;
+    P.act = act;
+    P.models = models;
+    P.model_of = model_of;
+    pack_values(lik, P, h);
     {
         // Streamed: leaf rows of each op in child order, null-terminated.
         // Staged: the leaf table.
@@ -820,19 +876,107 @@ static Plan &scratch_plan() {
     return *p;
 }
 
+// Everything a translation depends on apart from the per-call values: the
+// launch shape and precision, the registry state, the Lik's sizes, which
+// components are active with which models, the root, and every step's
+// variant, ntrail and CLs (struct and buffer).  Branch lengths, model
+// parameters, wNorm and the pattern weights are values.
+static void plan_key(const State &S, const CxtLik *lik, int prec,
+                     std::vector<uint64_t> &k) {
+    k.clear();
+    k.reserve(16 + lik->compsLen + 5 * (size_t)lik->stepsLen);
+    k.push_back((uint64_t)prec);
+    k.push_back(g_tile);
+    k.push_back(g_tpp);
+    k.push_back(g_ppt);
+    k.push_back(g_smem_budget);
+    k.push_back(g_lanes);
+    k.push_back(S.epoch);
+    k.push_back((uintptr_t)lik);
+    k.push_back(lik->dim);
+    k.push_back(lik->mschars);
+    k.push_back(lik->cbase);
+    k.push_back((uintptr_t)lik->rootCLC);
+    k.push_back(lik->rootCLC ? (uintptr_t)lik->rootCLC->cLMat : 0);
+    k.push_back(lik->compsLen);
+    for (unsigned c = 0; c < lik->compsLen; ++c)
+        k.push_back(lik->comps[c].weightScaled != 0.0 ? (uintptr_t)lik->comps[c].model : 0);
+    k.push_back(lik->stepsLen);
+    for (unsigned i = 0; i < lik->stepsLen; ++i) {
+        const CxtLikStep &st = lik->steps[i];
+        k.push_back(((uint64_t)(uint32_t)st.variant << 32) | st.ntrail);
+        k.push_back((uintptr_t)st.parentCL);
+        k.push_back(st.parentCL ? (uintptr_t)st.parentCL->cLMat : 0);
+        k.push_back((uintptr_t)st.childCL);
+        k.push_back(st.childCL ? (uintptr_t)st.childCL->cLMat : 0);
+    }
+}
+
+// Reuse the scratch plan's translation for a call with the same key:
+// write the values into the staging image and upload only them (the
+// records, child descriptors and tables on the device are unchanged).
+static int refresh_values(State &S, CxtLik *lik, Plan &P) {
+    const void *dfreqs = nullptr;
+    int rc = pattern_weights(S, lik, &dfreqs);
+    if (rc) return rc;
+    if (S.stage_pending) {
+        CXG_CUDA(cudaEventSynchronize(S.stage_ev));
+        S.stage_pending = false;
+    }
+    const size_t pn_bytes = (size_t)P.kact * 4 * 8;
+    rc = S.stage.ensure(P.o_pn + pn_bytes);
+    if (rc) return rc;
+    char *h = static_cast<char *>(S.stage.p);
+    pack_values(lik, P, h);
+    char *d = static_cast<char *>(P.prog.p);
+    CXG_CUDA(cudaMemcpyAsync(d + P.o_elen, h + P.o_elen, P.o_dst - P.o_elen,
+                             cudaMemcpyHostToDevice, S.stream));
+    CXG_CUDA(cudaMemcpyAsync(d + P.o_pn, h + P.o_pn, pn_bytes, cudaMemcpyHostToDevice,
+                             S.stream));
+    CXG_CUDA(cudaEventRecord(S.stage_ev, S.stream));
+    S.stage_pending = true;
+    S.last_h2d = (P.o_dst - P.o_elen) + pn_bytes;
+    P.pa.wnorm = lik->wNorm;
+    P.a.freqs = static_cast<const uint32_t *>(dfreqs);
+    return 0;
+}
+
 // Translate and run lik's plan.  `site` (host, mschars doubles) optional.
+// A call whose plan has the key of the previous call's (the same steps on
+// the same buffers, as a full re-plan of an unchanged tree gives) reuses
+// that translation and uploads only the new values.
 static int execute(CxtLik *lik, int prec, double *lnL, double *site) {
     State &S = state();
     std::lock_guard<std::mutex> g(S.mu);
     int rc = ensure_ready(S);
     if (rc) return rc;
+    if (lik == nullptr) return fail(CXG_EINVAL, "lik is NULL");
     Plan &P = scratch_plan();
-    rc = translate(S, lik, prec, P, true, true);
-    if (rc) return rc;
+    static std::vector<uint64_t> key;
+    plan_key(S, lik, prec, key);
+    if (S.last_valid && key == S.last_key) {
+        rc = refresh_values(S, lik, P);
+    } else {
+        S.last_valid = false;
+        rc = translate(S, lik, prec, P, true, true);
+        if (rc == 0) {
+            plan_key(S, lik, prec, S.last_key);  // translating may allocate
+            S.last_valid = true;
+        }
+    }
+    if (rc) {
+        S.last_valid = false;
+        return rc;
+    }
     rc = enqueue(S, P, site != nullptr, nullptr, nullptr, true);
-    if (rc) return rc;
+    if (rc) {
+        S.last_valid = false;
+        return rc;
+    }
     S.last_d2h = 32 + (site ? (size_t)P.npat * 8 : 0);
-    return finish(S, P, lnL, site);
+    rc = finish(S, P, lnL, site);
+    if (rc) S.last_valid = false;
+    return rc;
 }
 
 }  // namespace cxg
@@ -870,6 +1014,38 @@ int cxgLikClForget(const double *cLMat) {
     if (it != S.cls.end()) {
         free_cl(S, it->second);
         S.cls.erase(it);
+        ++S.epoch;
+    }
+    return 0;
+}
+
+int cxgLikSetPatternWeights(const unsigned *freqs, unsigned n) {
+    if (freqs == nullptr || n == 0)
+        return fail(CXG_EINVAL, "cxgLikSetPatternWeights: NULL or empty weights");
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    int rc = ensure_ready(S);
+    if (rc) return rc;
+    char key[64];
+    snprintf(key, sizeof(key), "%p:%u", (const void *)freqs, n);
+    FreqEntry &fe = S.freqs[key];
+    rc = fe.dev.ensure((size_t)n * 4);
+    if (rc) return rc;
+    CXG_CUDA(cudaMemcpy(fe.dev.p, freqs, (size_t)n * 4, cudaMemcpyHostToDevice));
+    fe.host.assign(freqs, freqs + n);
+    fe.registered = true;
+    return 0;
+}
+
+int cxgLikForgetPatternWeights(const unsigned *freqs, unsigned n) {
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    char key[64];
+    snprintf(key, sizeof(key), "%p:%u", (const void *)freqs, n);
+    auto it = S.freqs.find(key);
+    if (it != S.freqs.end()) {
+        if (it->second.dev.p) cudaFree(it->second.dev.p);
+        S.freqs.erase(it);
     }
     return 0;
 }
@@ -879,6 +1055,8 @@ int cxgLikReset(void) {
     std::lock_guard<std::mutex> g(S.mu);
     for (auto &kv : S.cls) free_cl(S, kv.second);
     S.cls.clear();
+    ++S.epoch;
+    S.last_valid = false;
     for (auto &kv : S.freqs)
         if (kv.second.dev.p) cudaFree(kv.second.dev.p);
     S.freqs.clear();

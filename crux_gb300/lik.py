@@ -279,6 +279,18 @@ class Lik:
         L.npad = alignment.npad
         self._freqs = np.ascontiguousarray(alignment.freqs, dtype=np.uint32)
         L.charFreqs = _abi.uptr(self._freqs)
+        if self.device and hasattr(self.lib, "cxgLikSetPatternWeights"):
+            # The weights of a compacted alignment do not change: register
+            # them once (the library then skips comparing them per call) and
+            # forget them when this Lik goes away.
+            n = int(L.mschars)
+            rc = self.lib.cxgLikSetPatternWeights(L.charFreqs, n)
+            if rc != 0:
+                raise RuntimeError("cxgLikSetPatternWeights: %s"
+                                   % self.lib.cxgLastError().decode())
+            fin = weakref.finalize(self, self.lib.cxgLikForgetPatternWeights,
+                                   _abi.uptr(self._freqs), n)
+            fin.atexit = False  # the process's exit releases the device copy
         stepsMax = 2 * alignment.ntaxa - 2
         self._steps = (_abi.CxtLikStep * max(stepsMax, 1))()
         L.steps = ctypes.cast(self._steps, ctypes.POINTER(_abi.CxtLikStep))

@@ -186,6 +186,16 @@ int cxgLikClForget(const double *cLMat);
 /* Release every device buffer and cached plan. */
 int cxgLikReset(void);
 
+/* Register a Lik's pattern weights (charFreqs + cbase, n = mschars): they
+ * are uploaded now and the caller promises not to change them while
+ * registered, so plans skip comparing them with the kept copy.  No
+ * counterpart in the reference (Lik.pyx:314 borrows Alignment.freqs, which
+ * does not change after compaction).  Unregistered weights are compared on
+ * every call and uploaded again when they differ.  Forget them before the
+ * host array is freed or changed. */
+int cxgLikSetPatternWeights(const unsigned *freqs, unsigned n);
+int cxgLikForgetPatternWeights(const unsigned *freqs, unsigned n);
+
 /* Execute lik's plan at the given precision; write the compensated FP64
  * sum of site lnLs to *lnL (one 8-byte device-to-host copy).  If siteLnL is
  * non-NULL also fill it (mschars doubles, pad patterns included). */

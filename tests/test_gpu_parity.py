@@ -285,3 +285,57 @@ def test_many_dirty_paths_gtr_gamma_inv(gpu, port, precision):
         eg[i].length = eo[i].length = base[i] * f
         a, b = lg.lnL(), lo.lnL()
         assert rel(a, b) <= TOL[precision], (a, b)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_repeated_full_plans_reuse_translation(gpu, port, precision):
+    """A full re-plan of an unchanged tree has the previous call's steps on
+    the same buffers, so the library reuses that translation and uploads only
+    the new values.  Branch lengths, alpha, rates and frequencies change
+    between calls and every lnL must follow the oracle; the program upload
+    of a reused call is small.  A second Lik interleaved with the first
+    changes the plan on every call (no reuse) and must also follow."""
+    case = synth.Case(24, 2000, 0.1, 611)
+    other = synth.Case(17, 900, 0.1, 612)
+    a = case.lik(lib=gpu, precision=precision)
+    ra = case.lik(lib=port)
+    b = other.lik(lib=gpu, precision=precision)
+    rb = other.lik(lib=port)
+    rng = np.random.default_rng(3)
+    h2d, d2h = ctypes.c_size_t(), ctypes.c_size_t()
+    seen = []
+    for it in range(12):
+        kind = it % 4
+        for lk in (a, ra):
+            lk.lik.invalidate = True
+        if kind == 0:
+            f = rng.uniform(0.5, 2.0, size=len(ra.tree.edges))
+            for lk in (a, ra):
+                for e, x in zip(lk.tree.edges, f):
+                    e.length *= float(x)
+        elif kind == 1:
+            alpha = float(rng.uniform(0.2, 2.0))
+            for lk in (a, ra):
+                lk.setAlpha(0, alpha)
+        elif kind == 2:
+            rates = [float(x) for x in rng.dirichlet(np.ones(6)) * 6]
+            for lk in (a, ra):
+                lk.setRclass(0, [0, 1, 2, 3, 4, 5], rates)
+        else:
+            freqs = rng.dirichlet(np.full(4, 5.0))
+            for lk in (a, ra):
+                for i, x in enumerate(freqs):
+                    lk.setFreq(0, i, float(x))
+        got, want = a.lnL(), ra.lnL()
+        gpu.cxgLikLastIo(ctypes.byref(h2d), ctypes.byref(d2h))
+        assert rel(got, want) <= TOL[precision], (it, got, want)
+        seen.append(got)
+        if it % 2 == 1:
+            # The previous call was a's own (b runs after a on odd calls):
+            # the translation is reused and only the values travel.
+            assert h2d.value < 8192, (it, h2d.value)
+        if it % 2 == 1:
+            for lk in (b, rb):
+                lk.lik.invalidate = True
+            assert rel(b.lnL(), rb.lnL()) <= TOL[precision]
+    assert len(set(seen)) == len(seen)
