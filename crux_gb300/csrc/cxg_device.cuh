@@ -81,14 +81,35 @@ __device__ inline void pmat_one(const PmatArgs &a, unsigned idx, unsigned q) {
 
 
 // ---------------------------------------------------------------------------
-// FP64 eigensystem of Q = R Pi (reversible, 4 states).
+// FP64 eigensystem of Q = R Pi (reversible, 4 states): Q is similar to the
+// symmetric S = Pi^1/2 Q Pi^-1/2, diagonalised by Jacobi rotations
+// (Rutishauser's form), then V = Pi^-1/2 U and V^-1 = U^T Pi^1/2.
 // out: [0..3] piNorm, [4] qNorm, [5..68] cube, [69..72] eigenvalues,
 // [73] status (0 ok, 1 bad input, 2 no convergence).
 // ---------------------------------------------------------------------------
-__device__ inline void qdecomp4(const double *rtri, const double *pi, double *out) {
-    // Every fixed-size loop is unrolled so that the 4 x 4 matrices live in
-    // registers; the arithmetic and its order are those of the loops.
-    double pn[4], sq[4], q[16], s[16], u[16];
+
+// Pick entry r (0..3) without indexing a register array by a run-time value.
+__device__ __forceinline__ double sel4(int r, double a, double b, double c, double d) {
+    return r == 0 ? a : r == 1 ? b : r == 2 ? c : d;
+}
+
+// The eigensystem of qdecomp4 on four lanes of a warp (lanes base .. base+3,
+// all four calling; out in memory those lanes can all reach, as for
+// qdecomp4).  Lane base+r holds row r of S = Pi^1/2 Q Pi^-1/2 and of the
+// rotations U.  Jacobi by rounds: each round applies two disjoint rotations,
+// (0,1)(2,3), then (0,2)(1,3), then (0,3)(1,2).  Disjoint rotations commute
+// and neither changes the entries the other's angle is computed from, so
+// taking both angles from the round's starting matrix is the same as
+// applying them one after the other.  Both lanes of a pair use the lower
+// lane's off-diagonal entry, so they compute the same rotation.  Each FP64
+// instruction of a warp costs the same with one lane active or four, so the
+// four lanes do in one instruction stream what qdecomp4 does in four.
+__device__ inline void qdecomp4_warp(const double *rtri, const double *pi, double *out,
+                                     unsigned base) {
+    const unsigned lane = threadIdx.x & 31u;
+    const int r = (int)(lane - base);
+    const unsigned mask = 0xFu << base;
+    double pn[4];
     double psum = 0.0;
 #pragma unroll
     for (int i = 0; i < 4; ++i) psum += pi[i];
@@ -98,16 +119,17 @@ __device__ inline void qdecomp4(const double *rtri, const double *pi, double *ou
         pn[i] = pi[i] / psum;
         ok = ok && (pn[i] > 0.0);
     }
-    if (!ok) {
-        out[73] = 1.0;
+    if (!ok) {  // the same on the four lanes
+        if (r == 0) out[73] = 1.0;
         return;
     }
-    // Upper-triangle order of rtri: (0,1) (0,2) (0,3) (1,2) (1,3) (2,3).
-    const int tri[4][4] = {{-1, 0, 1, 2}, {0, -1, 3, 4}, {1, 3, -1, 5},
-                           {2, 4, 5, -1}};
     double rt[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) rt[i] = rtri[i];
+    // Upper-triangle order of rtri: (0,1) (0,2) (0,3) (1,2) (1,3) (2,3).
+    const int tri[4][4] = {{-1, 0, 1, 2}, {0, -1, 3, 4}, {1, 3, -1, 5},
+                           {2, 4, 5, -1}};
+    double q[16];
     double qscale = 0.0;
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -125,82 +147,101 @@ __device__ inline void qdecomp4(const double *rtri, const double *pi, double *ou
             if (j != i) d -= q[i * 4 + j];
         q[i * 4 + i] = d;
     }
+    const double sqr = sqrt(sel4(r, pn[0], pn[1], pn[2], pn[3]));
+    double sq[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) sq[i] = sqrt(pn[i]);
+    for (int j = 0; j < 4; ++j) sq[j] = __shfl_sync(mask, sqr, base + j);
+    // Row r of S and of U.
+    double s[4], u[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+        double e[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-            s[i * 4 + j] = (i == j) ? q[i * 4 + i] : rt[tri[i][j]] * sq[i] * sq[j];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) u[i] = (i % 5 == 0) ? 1.0 : 0.0;
+        for (int i = 0; i < 4; ++i)
+            e[i] = (i == j) ? q[i * 4 + i] : rt[tri[i][j]] * sq[i] * sq[j];
+        s[j] = sel4(r, e[0], e[1], e[2], e[3]);
+        u[j] = (j == r) ? 1.0 : 0.0;
+    }
     int conv = 0;
     for (int sweep = 0; sweep < 64 && !conv; ++sweep) {
-        double off = 0.0, dg = 0.0;
+        double offr = 0.0, dgr = 0.0;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            dg += s[i * 4 + i] * s[i * 4 + i];
-#pragma unroll
-            for (int j = i + 1; j < 4; ++j) off += s[i * 4 + j] * s[i * 4 + j];
+        for (int j = 0; j < 4; ++j) {
+            if (j == r) dgr = s[j] * s[j];
+            if (j > r) offr += s[j] * s[j];
         }
-        if (off == 0.0 || off <= 1e-40 * dg) {
+        // Butterfly sums: every lane adds the same pairs, so all agree.
+        offr += __shfl_xor_sync(mask, offr, 1);
+        offr += __shfl_xor_sync(mask, offr, 2);
+        dgr += __shfl_xor_sync(mask, dgr, 1);
+        dgr += __shfl_xor_sync(mask, dgr, 2);
+        if (offr == 0.0 || offr <= 1e-40 * dgr) {
             conv = 1;
             break;
         }
 #pragma unroll
-        for (int pp = 0; pp < 3; ++pp)
+        for (int X = 1; X <= 3; ++X) {  // partner of row r: r ^ X
+            const int pr = r ^ X;
+            const int lo = r < pr ? r : pr;
+            // The pair's entries: the diagonals from their own lanes, the
+            // off-diagonal from the lower lane.
+            const double dr = sel4(r, s[0], s[1], s[2], s[3]);
+            const double dp = __shfl_sync(mask, dr, base + pr);
+            const double opr = sel4(pr, s[0], s[1], s[2], s[3]);
+            const double apq = __shfl_sync(mask, opr, base + lo);
+            const double app = r == lo ? dr : dp, aqq = r == lo ? dp : dr;
+            double c = 1.0, sn = 0.0;
+            if (apq != 0.0) {
+                const double th = (aqq - app) / (2.0 * apq);
+                const double t = (th >= 0.0 ? 1.0 : -1.0) /
+                                 (fabs(th) + sqrt(th * th + 1.0));
+                c = 1.0 / sqrt(t * t + 1.0);
+                sn = t * c;
+            }
+            // The other pair's rotation, from one of its lanes.
+            const int ol = r ^ (X == 1 ? 2 : 1);
+            const double co = __shfl_sync(mask, c, base + ol);
+            const double so = __shfl_sync(mask, sn, base + ol);
+            // Columns: row r of S J and of U J.  Column j pairs with j ^ X.
+            double ns[4], nu[4];
 #pragma unroll
-            for (int qq = pp + 1; qq < 4; ++qq) {
-                const double apq = s[pp * 4 + qq];
-                if (apq != 0.0) {
-                    const double app = s[pp * 4 + pp], aqq = s[qq * 4 + qq];
-                    const double th = (aqq - app) / (2.0 * apq);
-                    const double t = (th >= 0.0 ? 1.0 : -1.0) /
-                                     (fabs(th) + sqrt(th * th + 1.0));
-                    const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const double akp = s[k * 4 + pp], akq = s[k * 4 + qq];
-                        s[k * 4 + pp] = c * akp - sn * akq;
-                        s[k * 4 + qq] = sn * akp + c * akq;
-                    }
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const double apk = s[pp * 4 + k], aqk = s[qq * 4 + k];
-                        s[pp * 4 + k] = c * apk - sn * aqk;
-                        s[qq * 4 + k] = sn * apk + c * aqk;
-                    }
-                    s[pp * 4 + qq] = s[qq * 4 + pp] = 0.0;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const double ukp = u[k * 4 + pp], ukq = u[k * 4 + qq];
-                        u[k * 4 + pp] = c * ukp - sn * ukq;
-                        u[k * 4 + qq] = sn * ukp + c * ukq;
-                    }
+            for (int j = 0; j < 4; ++j) {
+                const int jp = j ^ X;
+                const bool mine = (j == r) || (j == pr);
+                const double cj = mine ? c : co, sj = mine ? sn : so;
+                if (j < jp) {
+                    ns[j] = cj * s[j] - sj * s[jp];
+                    nu[j] = cj * u[j] - sj * u[jp];
+                } else {
+                    ns[j] = sj * s[jp] + cj * s[j];
+                    nu[j] = sj * u[jp] + cj * u[j];
                 }
             }
+            // Rows: row r of J^T (S J) mixes with the partner's row.
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const double o = __shfl_sync(mask, ns[j], base + pr);
+                s[j] = (r == lo) ? c * ns[j] - sn * o : sn * o + c * ns[j];
+                u[j] = nu[j];
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (j == pr) s[j] = 0.0;
+        }
     }
+    out[r] = sel4(r, pn[0], pn[1], pn[2], pn[3]);
+    if (r == 0) out[4] = 1.0 / qscale;
+    // cube[r][j][k] = V[r][k] V^-1[k][j] with V = Pi^-1/2 U, V^-1 = U^T Pi^1/2.
+    const double isq = 1.0 / sel4(r, sq[0], sq[1], sq[2], sq[3]);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) out[i] = pn[i];
-    out[4] = 1.0 / qscale;
-    // V = Pi^-1/2 U and V^-1 = U^T Pi^1/2: cube[i][j][k] = V[i][k] V^-1[k][j].
-    // Four reciprocals instead of 64 divisions (FP64 division is a long
-    // instruction sequence on this part); V[i][k] moves by at most an ulp.
-    double isq[4];
+    for (int j = 0; j < 4; ++j)
 #pragma unroll
-    for (int i = 0; i < 4; ++i) isq[i] = 1.0 / sq[i];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                out[5 + i * 16 + j * 4 + k] =
-                    (u[i * 4 + k] * isq[i]) * (u[j * 4 + k] * sq[j]);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) out[69 + k] = s[k * 4 + k];
-    out[73] = conv ? 0.0 : 2.0;
+        for (int k = 0; k < 4; ++k) {
+            const double ujk = __shfl_sync(mask, u[k], base + j);
+            out[5 + r * 16 + j * 4 + k] = (u[k] * isq) * (ujk * sq[j]);
+        }
+    out[69 + r] = sel4(r, s[0], s[1], s[2], s[3]);
+    if (r == 0) out[73] = conv ? 0.0 : 2.0;
 }
-
 
 }  // namespace cxg

@@ -1310,7 +1310,7 @@ int batch_ctas_per_sm(int precision, unsigned kact, unsigned tile, unsigned tpp,
 
 __global__ void qdecomp_kernel(const double *rtri, const double *pi,
                                double *out) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) qdecomp4(rtri, pi, out);
+    if (blockIdx.x == 0 && threadIdx.x < 4) qdecomp4_warp(rtri, pi, out, 0);
 }
 
 cudaError_t launch_qdecomp(const double *rtri, const double *pi, double *out,

@@ -168,40 +168,20 @@ __device__ void mc3_model_weights(Mc3Model &m, unsigned ncat, unsigned invar) {
     m.ok = 1;
 }
 
-// Model derived quantities: Q eigensystem (FP64 Jacobi on the device),
-// Gamma category rates, wNorm and the root weights (Lik.pyx:1603-1665).
-// `what` names the parts whose inputs changed (FIN_EIG: rates or
-// frequencies, FIN_GAMMA: alpha, FIN_WEIGHTS: the +I weights only); the
-// others are kept.
+// Parts of a model to derive again: FIN_EIG (rates or frequencies changed),
+// FIN_GAMMA (alpha), FIN_WEIGHTS (the +I weights only).
 enum : unsigned { FIN_EIG = 1, FIN_GAMMA = 2, FIN_ALL = 3, FIN_WEIGHTS = 4 };
-__device__ bool mc3_model_finish(Mc3Model &m, unsigned ncat, unsigned invar,
-                                 unsigned what = FIN_ALL) {
-    if (what & FIN_EIG) {
-        double tmp[74];
-        qdecomp4(m.rates, m.freqs, tmp);
-        if (tmp[73] != 0.0) return false;
-        for (int i = 0; i < 4; ++i) m.pinorm[i] = tmp[i];
-        m.qnorm = tmp[4];
-        for (int i = 0; i < 64; ++i) m.cube[i] = tmp[5 + i];
-        for (int i = 0; i < 4; ++i) m.eig[i] = tmp[69 + i];
-    }
-    if (what & FIN_GAMMA) {
-        if (ncat > 1 && m.gamma_on) {
-            if (!d_gamma_rates(m.alpha, (int)ncat, m.cmult)) return false;
-        } else if (ncat == 1) {
-            m.cmult[0] = 1.0;
-        }
-    }
-    mc3_model_weights(m, ncat, invar);
-    return true;
-}
 
-// The same with one warp: lanes 0..ncat-2 compute the Gamma category cuts
-// while lane 31 forms the eigensystem; lane 0 finishes.  All 32 lanes of
-// the warp call it; the result (true: decomposed) is lane 0's.
+// Model derived quantities: Q eigensystem (FP64 Jacobi on the device),
+// Gamma category rates, wNorm and the root weights (Lik.pyx:1603-1665);
+// the parts `what` does not name are kept.  One warp: lanes 0..ncat-2
+// compute the Gamma category cuts while lanes 28..31 form the eigensystem;
+// lane 0 finishes.  All 32 lanes of the warp call it; the result (true:
+// decomposed) is lane 0's.
 __device__ bool mc3_model_finish_warp(Mc3Model &m, unsigned ncat, unsigned invar,
                                       unsigned what) {
     __shared__ double s_cut[kMaxComps];
+    __shared__ double s_eig[74];
     __shared__ int s_bad;
     const unsigned lane = threadIdx.x & 31u;
     if (lane == 0) s_bad = 0;
@@ -213,9 +193,10 @@ __device__ bool mc3_model_finish_warp(Mc3Model &m, unsigned ncat, unsigned invar
         else
             s_cut[lane] = cut;
     }
+    if ((what & FIN_EIG) && lane >= 28) qdecomp4_warp(m.rates, m.freqs, s_eig, 28);
+    __syncwarp();
     if ((what & FIN_EIG) && lane == 31) {
-        double tmp[74];
-        qdecomp4(m.rates, m.freqs, tmp);
+        const double *tmp = s_eig;
         if (tmp[73] != 0.0) {
             s_bad = 1;
         } else {
@@ -242,9 +223,10 @@ __device__ bool mc3_model_finish_warp(Mc3Model &m, unsigned ncat, unsigned invar
 
 __global__ void mc3_init_kernel(Mc3Dev d) {
     const unsigned c = blockIdx.x;
-    if (threadIdx.x != 0 || c >= d.nchains) return;
+    if (c >= d.nchains || threadIdx.x >= 32) return;
     Mc3Model &m = d.model[c * 2 + d.curmodel[c]];
-    if (!mc3_model_finish(m, d.ncat, d.invar)) atomicOr(d.status, 1u);
+    const bool ok = mc3_model_finish_warp(m, d.ncat, d.invar, FIN_ALL);
+    if (threadIdx.x == 0 && !ok) atomicOr(d.status, 1u);
 }
 
 // log density of Dirichlet(alpha) at x (both length n).

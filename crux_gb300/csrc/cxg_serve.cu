@@ -56,9 +56,11 @@ struct SrvModel {
 // (cmult 0) of weight pinv; wNorm and root weights as Lik.prep
 // (Lik.pyx:1603-1665).
 __global__ void srv_model_kernel(SrvModel *m) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double tmp[74];
-    qdecomp4(m->rates, m->freqs, tmp);
+    if (blockIdx.x != 0) return;
+    __shared__ double tmp[74];
+    if (threadIdx.x < 4) qdecomp4_warp(m->rates, m->freqs, tmp, 0);
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     m->ok = 0;
     if (tmp[73] != 0.0) return;
     double pin[4];
