@@ -84,12 +84,14 @@ def test_load_without_gpu_reports_no_device():
 
 
 def test_extension_struct_layouts_match_header():
-    """The ctypes mirrors of the MC3 and server structs (crux_gb300.mc3,
-    crux_gb300.serve) have the header's field offsets and sizes."""
+    """The ctypes mirrors of the MC3, server and native-planner structs
+    (crux_gb300.mc3, crux_gb300.serve, crux_gb300._abi) have the header's
+    field offsets and sizes."""
     from crux_gb300 import mc3, serve
     pairs = [("cxgMc3Config", mc3.Mc3Config), ("cxgRequest", serve.Request),
              ("cxgServerConfig", serve.ServerConfig),
-             ("cxgServerStatsT", serve.ServerStats)]
+             ("cxgServerStatsT", serve.ServerStats),
+             ("cxgPlanSnap", _abi.CxgPlanSnap)]
     lines = []
     want = []
     for cname, py in pairs:
