@@ -183,3 +183,48 @@ def test_native_planner_full_and_dirty_plans(port):
         b.tree.edges[i].length *= f
         _check_same(a, b, a.lnL(), b.lnL())
         assert a._snap is not None
+
+
+def test_native_planner_polytomies(port):
+    """Multifurcating nodes (a degree-5 root, degree-4 and degree-3
+    internal nodes): one Compute step and degree-2 Merge steps per dirty
+    node with ntrail counting down, as the Python planner writes them, at
+    every root and after rescales; and the same lnL as the Python planner
+    on the oracle."""
+    import kat_cases as K
+    from crux_gb300.alignment import Alignment, CTMatrix
+    from crux_gb300.lik import Lik
+    rng = np.random.default_rng(8)
+    names = ["t%d" % i for i in range(9)]
+    fasta = "".join(">%s\n%s\n" % (n, "".join(rng.choice(list("ACGT"), 60)))
+                    for n in names)
+    newick = ("(t0:0.1,t1:0.2,(t2:0.1,t3:0.3,t4:0.05,t5:0.2):0.15,"
+              "(t6:0.1,t7:0.2,t8:0.3):0.1);")
+    aln = Alignment(CTMatrix(fasta))
+    a = Lik(K.tree_for(newick, aln), aln, ncat=4, lib=port)
+    b = Lik(K.tree_for(newick, aln), aln, ncat=4, lib=port)
+    a.setAlpha(0, 0.7)
+    b.setAlpha(0, 0.7)
+    b.native_plan = False
+    degrees = sorted(n.getDegree() for n in a.tree.nodes)
+    assert degrees[-1] >= 4
+    prng = random.Random(2)
+    native = 0
+    for it in range(60):
+        k = prng.randrange(len(a.tree.nodes))
+        if it % 3 == 0:
+            i = prng.randrange(len(a.tree.edges))
+            f = prng.uniform(0.5, 2.0)
+            a.tree.edges[i].length *= f
+            b.tree.edges[i].length *= f
+        ra, rb = (a.tree.nodes[k], b.tree.nodes[k]) if it % 4 == 1 else (None, None)
+        _check_same(a, b, a.lnL(ra), b.lnL(rb))
+        native += a._snap is not None
+    assert native > 20, native
+    # Steps of a node with four children: Compute with ntrail 3, then
+    # Merges with 2, 1, 0.
+    a.lik.invalidate = True
+    a.lnL()
+    steps = a.steps()
+    trails = [t for _, t, _ in steps]
+    assert 3 in trails and trails[trails.index(3) + 1:trails.index(3) + 4] == [2, 1, 0]
