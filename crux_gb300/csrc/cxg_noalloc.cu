@@ -3,9 +3,8 @@
 // Some callers own every byte of device memory themselves. A host
 // application may reserve the GPU heap in its own pool or a framework's
 // caching allocator. A latency-critical loop must not stall the device on
-// cudaMalloc/cudaFree, which can synchronise. Code may be about to be
-// captured into a CUDA graph, where allocation is not allowed. Such callers
-// cannot let the library allocate device buffers on their behalf.
+// cudaMalloc/cudaFree, which can synchronise. Such callers cannot let the
+// library allocate device buffers on their behalf.
 //
 // This entry point evaluates one plan using only memory the caller passes
 // (CL buffers, leaf masks, pattern weights, an optional site-lnL output)

@@ -2,9 +2,9 @@
 
 Some callers own all device memory themselves. It may come from their own
 pool, or from a framework's caching allocator. They may run a
-latency-critical loop that must not stall on cudaMalloc, or be about to
-capture work into a CUDA graph. This entry point takes every buffer from
-the caller, and its scratch is a fixed array inside the library.  The test
+latency-critical loop that must not stall on cudaMalloc. This entry point
+takes every buffer from the caller, and its scratch is a fixed array
+inside the library.  The test
 plays such a caller: it allocates device buffers itself (through the CUDA
 runtime, as the caller would), lays out the CLs and leaf masks, and checks
 that two calls in a row give the same lnL as the allocating entry point
