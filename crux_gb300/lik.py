@@ -21,6 +21,7 @@ Method map to the reference:
 import ctypes
 import math
 import os
+import struct
 import weakref
 
 import numpy as np
@@ -818,6 +819,9 @@ class Lik:
         sn.m_elen = np.array([v[0].edgeLen[pol] for v in vis],
                              dtype=np.float64)
         sn.lens = np.zeros(max(len(edges), 1), dtype=np.float64)
+        # Packs the edges' lengths into sn.lens in one C loop (a numpy slice
+        # assignment from a list converts element by element).
+        sn.lens_pack = struct.Struct("%dd" % len(edges)).pack_into
         sn.changed = np.zeros(n, dtype=u32)
         c = sn.c = _abi.CxgPlanSnap()
         c.nvis = n
@@ -872,7 +876,7 @@ class Lik:
         inval = bool(L.invalidate)
         if inval and not sn.opp_clean:
             return False
-        sn.lens[:len(sn.edges)] = [e.length for e in sn.edges]
+        sn.lens_pack(sn.lens, 0, *[e.length for e in sn.edges])
         rc = sn.lib.cxgPlanSnapRun(sn.cref, sn.lens_p, inval, self._steps,
                                    L.stepsMax, sn.nsteps_p, sn.changed_p,
                                    sn.nchanged_p)
