@@ -228,3 +228,61 @@ def test_native_planner_polytomies(port):
     steps = a.steps()
     trails = [t for _, t, _ in steps]
     assert 3 in trails and trails[trails.index(3) + 1:trails.index(3) + 4] == [2, 1, 0]
+
+
+def test_plan_snap_c_entry_point():
+    """cxgPlanSnapRun through the C ABI (host code: no GPU) on a hand-made
+    snapshot: a root with two leaf children.  It writes the steps and the
+    CxtLikCL fields, reports which visits changed, plans nothing when
+    nothing changed, replans after a length change, returns 1 for a
+    negative length, and rejects a malformed snapshot or a full step
+    array."""
+    from crux_gb300 import _native
+    lib = _native.load()   # loading makes no CUDA call
+    cls = [_abi.CxtLikCL() for _ in range(3)]
+    addr = [ctypes.addressof(c) for c in cls]
+    u32, i32 = np.uint32, np.int32
+    arrs = dict(
+        cl=np.array(addr, dtype=np.uint64), up=np.array([2, 2, -1], dtype=i32),
+        nsibs=np.array([2, 2, 0], dtype=u32), edge=np.array([0, 1, -1], dtype=i32),
+        kid0=np.array([0, 0, 0], dtype=u32), nkids=np.array([0, 0, 2], dtype=u32),
+        kid_cl=np.array(addr[:2], dtype=np.uint64),
+        kid_int=np.array([0, 0], dtype=np.uint8),
+        kid_edge=np.array([0, 1], dtype=i32),
+        valid=np.zeros(3, dtype=np.uint8), cvalid=np.zeros(3, dtype=np.uint8),
+        m_parent=np.zeros(3, dtype=np.uint64), m_nsibs=np.zeros(3, dtype=u32),
+        m_elen=np.zeros(3, dtype=np.float64))
+    snap = _abi.CxgPlanSnap()
+    snap.nvis, snap.nkid = 3, 2
+    for k, v in arrs.items():
+        setattr(snap, k, v.ctypes.data)
+    lens = np.array([0.1, 0.2])
+    steps = (_abi.CxtLikStep * 4)()
+    ns, nc = ctypes.c_uint32(), ctypes.c_uint32()
+    changed = np.zeros(3, dtype=np.uint32)
+
+    def run(inval, cap=4):
+        return lib.cxgPlanSnapRun(
+            ctypes.byref(snap), _abi.dptr(lens), inval, steps, cap,
+            ctypes.byref(ns), changed.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+            ctypes.byref(nc))
+
+    assert run(1) == 0 and ns.value == 2
+    got = [(steps[i].variant, steps[i].ntrail, _addr(steps[i].parentCL),
+            _addr(steps[i].childCL), steps[i].edgeLen) for i in range(2)]
+    assert got == [(_abi.ComputeL, 1, addr[2], addr[0], 0.1),
+                   (_abi.MergeL, 0, addr[2], addr[1], 0.2)]
+    assert sorted(changed[:nc.value].tolist()) == [0, 1, 2]
+    assert _addr(cls[0].parent) == addr[2] and cls[1].nSibs == 2
+    assert cls[1].edgeLen == 0.2 and bool(cls[2].valid)
+    assert run(0) == 0 and ns.value == 0 and nc.value == 0
+    lens[0] = 0.3
+    assert run(0) == 0 and ns.value == 2 and steps[0].edgeLen == 0.3
+    assert changed[:nc.value].tolist() == [0] and cls[0].edgeLen == 0.3
+    lens[1] = -1.0
+    assert run(1) == 1                      # "Negative branch length"
+    lens[1] = 0.2
+    assert run(1, cap=1) == -1              # the step array is too small
+    arrs["up"][2] = 0                       # the last visit must be the root
+    assert run(1) == -1
+    assert b"root" in lib.cxgLastError()
