@@ -785,7 +785,6 @@ def make_serve_pool(n):
 def run_serve(args, dist):
     """Serving loop under Poisson arrivals: p50/p99 latency and throughput
     of the FP32 form and of the plain FP64 form on the same arrivals."""
-    import threading
     import numpy as np
     from crux_gb300.serve import MC3, PreparedRequest, Server
     t0 = time.perf_counter()

@@ -27,7 +27,6 @@ import weakref
 import numpy as np
 
 from . import _abi
-from .alignment import Dna
 from .cxmath import gamma_rates
 
 CACHE_LINE = 64
