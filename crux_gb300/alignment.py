@@ -11,7 +11,9 @@ Host-side restatement of the data model the likelihood consumes:
   ``pad`` (CTMatrix.pyx:610-662), ``canonize`` (856-887) and ``compact``
   (949-1031): columns are canonicalised, sorted bytewise and equal columns
   merged with summed frequencies, which is the order a Python-2 sort of
-  ``[column string, freq]`` pairs produces.
+  ``[column string, freq]`` pairs produces; the Fitch variants
+  (``_fitchCanonize`` :785-854, ``_fitchCompact`` :890-947) and ``render``
+  (:1040-1145), whose text the reference's own compaction tests print.
 """
 import re
 
@@ -245,17 +247,94 @@ class Alignment:
                                      np.ones(npad, dtype=np.uint32)])
         self.npad += npad
 
-    def canonize(self):
-        """Map aliases to primary codes (CTMatrix.pyx:856-887)."""
-        self.rows = self.charType.get().canon_table[self.rows]
+    def canonize(self, fitch=False):
+        """Map aliases to primary codes (CTMatrix.pyx:856-887).
 
-    def compact(self):
+        With ``fitch``, also relabel each column's states in order of first
+        appearance down the column (``_fitchCanonize``, :785-854), so that
+        columns equal up to a renaming of states become equal.
+        """
+        self.rows = self.charType.get().canon_table[self.rows]
+        if fitch:
+            self._fitch_canonize()
+
+    @staticmethod
+    def _bits(v):
+        """State indices of bitmask `v`, lowest first (the ffs order)."""
+        out = []
+        while v:
+            low = v & -v
+            out.append(low.bit_length() - 1)
+            v ^= low
+        return out
+
+    def _fitch_canonize(self):
+        ch = self.charType.get()
+        n = ch.nstates
+        codes = ch.codes()
+        for j in range(self.nchars):
+            col = self.rows[:, j]
+            ftrans = [-1] * n
+            seen = 0
+            for b in col:
+                if seen == n:
+                    break
+                for bit in self._bits(int(ch.val_table[b])):
+                    if ftrans[bit] == -1:
+                        ftrans[bit] = 1 << seen
+                        seen += 1
+                        if seen == n:
+                            break
+            i = 0
+            while seen < n:
+                if ftrans[i] == -1:
+                    ftrans[i] = 1 << seen
+                    seen += 1
+                i += 1
+            trans = np.arange(256, dtype=np.uint8)
+            for code in codes:
+                r = 0
+                for bit in self._bits(ch.code2val(code)):
+                    r |= ftrans[bit]
+                trans[ord(code)] = ord(ch.val2code(r))
+            self.rows[:, j] = trans[col]
+
+    def _fitch_informative(self, col):
+        """(informative, states seen) of one column (CTMatrix.pyx:890-947):
+        more than two states, or two states that each occur twice."""
+        ch = self.charType.get()
+        n = ch.nstates
+        freqs = [0] * n
+        seen = 0
+        for b in col:
+            for bit in self._bits(int(ch.val_table[b])):
+                freqs[bit] += 1
+                if freqs[bit] == 1:
+                    seen += 1
+                    if seen > 2:
+                        return True, seen
+        if seen == 2:
+            mult = 0
+            for i in range(n):
+                if mult >= 2:
+                    break
+                if freqs[i] != 0:
+                    if freqs[i] == 1:
+                        break
+                    mult += 1
+            if mult == 2:
+                return True, seen
+        return False, seen
+
+    def compact(self, fitch=False):
         """Merge identical columns, sorted bytewise (CTMatrix.pyx:949-1031).
 
-        Returns 0 (the Fitch variant, which also drops uninformative sites,
-        is not on the likelihood path).
+        With ``fitch``, the columns are Fitch-canonized first and
+        parsimony-uninformative patterns are dropped afterwards; the return
+        value is then the number of changes dropped (one per unit of
+        frequency of each dropped two-state pattern), else 0.
         """
-        self.canonize()
+        self.canonize(fitch)
         cols = np.ascontiguousarray(self.rows.T)
         key = cols.view(np.dtype((np.void, cols.shape[1]))).ravel()
         order = np.argsort(key, kind="stable")
@@ -265,11 +344,62 @@ class Alignment:
         group = np.cumsum(first) - 1
         freqs = np.zeros(int(first.sum()), dtype=np.uint64)
         np.add.at(freqs, group, self.freqs[order].astype(np.uint64))
-        self.rows = np.ascontiguousarray(cols[order[first]].T)
-        self.freqs = freqs.astype(np.uint32)
-        return 0
+        ucols = cols[order[first]]
+        freqs = freqs.astype(np.uint32)
+        ret = 0
+        if fitch:
+            keep = np.zeros(len(ucols), dtype=bool)
+            for j, col in enumerate(ucols):
+                informative, seen = self._fitch_informative(col)
+                keep[j] = informative
+                if not informative and seen == 2:
+                    ret += int(freqs[j])
+            ucols, freqs = ucols[keep], freqs[keep]
+        self.rows = np.ascontiguousarray(ucols.T).reshape(self.ntaxa,
+                                                          len(ucols))
+        self.freqs = freqs
+        return ret
 
-    def render(self):
-        w = max(len(t) for t in self.taxaMap.taxa)
-        return "\n".join("%-*s %s" % (w, t, self.getSeq(i))
-                         for i, t in enumerate(self.taxaMap.taxa))
+    def render(self, interleave=50, pad=False):
+        """Human-readable alignment with site frequencies, as
+        ``Alignment.render`` prints it (CTMatrix.pyx:1040-1145): blocks of
+        `interleave` columns (rounded up to a multiple of 5; 0 = one
+        block), a frequency line (``(f)`` for f >= 10), ``=`` rules and
+        column offsets.  Padding columns are shown only with ``pad``."""
+        taxa = self.taxaMap.taxa
+        nchars = self.nchars if pad else self.nchars - self.npad
+        lines = []
+        if nchars > 0:
+            w = max(len(t) for t in taxa)
+            if interleave == 0:
+                interleave = nchars
+            elif interleave % 5 != 0:
+                interleave += 5 - interleave % 5
+            seqs = [self.getSeq(k) for k in range(len(taxa))]
+            if not pad and self.npad > 0:
+                seqs = [s[:-self.npad] for s in seqs]
+            for i in range(0, nchars, interleave):
+                lim = min(i + interleave, nchars)
+                if i > 0:
+                    lines.append("\n")
+                head = ["%-*s" % (w, "")]
+                for j in range(i, lim):
+                    if j % 5 == 0:
+                        head.append(" ")
+                    f = int(self.freqs[j])
+                    head.append("%d" % f if f < 10 else "(%d)" % f)
+                lines.append("".join(head) + "\n")
+                rule = "%-*s " % (w, "") + "=" * ((lim - i) + (lim - 1 - i) // 5)
+                lines.append(rule + "\n")
+                for label, seq in zip(taxa, seqs):
+                    lines.append("%-*s" % (w, label) + "".join(
+                        " %s" % seq[j:j + 5] for j in range(i, lim, 5)) + "\n")
+                lines.append(rule + "\n")
+                offs = "%-*s " % (w, "") + "".join(
+                    "%-6d" % j for j in range(i, lim, 5))
+                lines.append(offs.rstrip() + "\n")
+        else:
+            for label in taxa:
+                lines.append("%s\n" % label)
+        text = "".join(lines)
+        return text[:-1] if text.endswith("\n") else text

@@ -73,3 +73,31 @@ def test_compact_alignment_feeds_the_likelihood(gpu, port):
     assert np.array_equal(a_gpu.freqs, a_host.freqs)
     assert case.lik(lib=port, alignment=a_gpu).lnL() == \
         case.lik(lib=port, alignment=a_host).lnL()
+
+
+def _kat():
+    import json
+    import os
+    return json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                       "compaction_kat.json")))
+
+
+def test_compact_matches_reference_kats(gpu):
+    """cxgCompact prints the reference's own compaction answers byte for
+    byte: rinehart.fasta (test/Alignment_a.cx.exp) and the "# Compact"
+    blocks of test/CTMatrix_e.cx.exp, then pads as the reference does."""
+    from crux_gb300.alignment import CTMatrix
+    kat = _kat()
+    aln = Alignment(CTMatrix(kat["rinehart_fasta"]))
+    gc.compact_alignment(aln, gpu)
+    assert aln.render() == kat["alignment_a"]
+    for case in kat["ctmatrix_e"]:
+        aln = Alignment(CTMatrix(case["fasta"]))
+        rows, freqs, masks = gc.compact(aln, gpu)
+        want = host_compact(aln)
+        assert np.array_equal(rows, want.rows)
+        assert np.array_equal(freqs, want.freqs)
+        aln.rows, aln.freqs = np.ascontiguousarray(rows), freqs
+        assert aln.render(pad=True) == case["Compact"]
+        aln.pad("-", 4)
+        assert aln.render() == case["Compact"]
