@@ -233,26 +233,47 @@ def load_cpu_oracle():
     return lib, "port", threads
 
 
+def tree128_config(npat, nops, ws):
+    """The tree128 workload's config; both arms print exactly this."""
+    return dict(WORKLOAD, patterns=npat, node_updates_per_eval=nops,
+                parallelism="replicas" if ws > 1 else "single",
+                l2_flush="inputs>L2 (each evaluation writes all %d internal "
+                         "CLs of %d patterns)" % (nops, npat))
+
+
+REF_EVALS_PER_STEP = 8
+
+
 def run_reference(args, dist):
-    """--impl reference: the reference's CPU path on the host cores."""
+    """--impl reference: the reference's CPU path on the host cores.  Each
+    step is a bounded sample of REF_EVALS_PER_STEP full-tree evaluations of
+    CxLikExecute; planning (the Python restatement of Lik._plan, outside
+    the timed calls) never maps this package's GPU library."""
     if dist.rank != 0:
         dist.close()
         return
+    from crux_gb300 import synth
     lib, kind, threads = load_cpu_oracle()
     case = make_case()
     aln = case.alignment()
-    cpu_run(lib, case, aln, max(args.warmup, 1), threads)
-    rate, secs, ups, _ = cpu_run(lib, case, aln, args.steps, threads)
-    line = {"metric": METRIC, "impl": "reference", "value": rate, "unit": UNIT, "n_gpus": 0,
-            "steps": args.steps, "warmup": args.warmup,
+    cpu_run(lib, case, aln, max(args.warmup, 1) * REF_EVALS_PER_STEP, threads)
+    rate, secs, ups, nev = cpu_run(lib, case, aln,
+                                   args.steps * REF_EVALS_PER_STEP, threads)
+    probe = case.lik(lib=lib, alignment=aln)
+    probe.prepare_plan()
+    nops = synth.nnodes_updates(probe) // int(probe.lik.mschars)
+    line = {"metric": METRIC, "impl": "reference", "value": rate, "unit": UNIT,
+            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
-            "config": dict(WORKLOAD, patterns=aln.nchars, l2_flush="inputs>L2"),
+            "data": "synthetic (seeded Yule tree, GTR+G4 simulation)",
+            "config": tree128_config(aln.nchars, nops, dist.ws),
+            "evals_per_step": REF_EVALS_PER_STEP,
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads,
                              "kind": kind,
-                             "sample": "%d full-tree FP64 lnL evaluations" %
-                                       args.steps},
+                             "sample": "%d steps x %d full-tree FP64 lnL "
+                                       "evaluations (%.1f s)" %
+                                       (args.steps, REF_EVALS_PER_STEP, secs)},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -296,7 +317,8 @@ def run_ours(args, dist):
         return
 
     # End to end through the public API: full re-plan + lnL each run, with
-    # the FP32 form's tuned shape.
+    # the FP32 form's tuned shape.  One step is --batch evaluations, as in
+    # the device-timed leg.
     sh = res["fp32"]["shape"]
     tune.set_shape(gpu, sh["tile"], sh["tpp"], sh["ppt"], sh["budget"],
                    sh["lanes"])
@@ -305,7 +327,7 @@ def run_ours(args, dist):
         lik.lik.invalidate = True
         lik.lnL()
     dist.barrier()
-    e2e_runs = args.steps * max(1, args.batch // 8)
+    e2e_runs = args.steps * args.batch
     t0 = time.perf_counter()
     for _ in range(e2e_runs):
         lik.lik.invalidate = True
@@ -322,9 +344,24 @@ def run_ours(args, dist):
     lik.lnL()
     h2d, d2h = ctypes.c_size_t(), ctypes.c_size_t()
     gpu.cxgLikLastIo(ctypes.byref(h2d), ctypes.byref(d2h))
+    # The drop-in call Crux itself makes (Lik.pyx:1699-1712): CxLikExecute
+    # on host CL structs, every site lnL and stripe sum written back to host
+    # memory, then summed on the host.  It computes in the reference's
+    # precision (the plain FP64 form).
+    ld = case.lik(lib=gpu, alignment=case.alignment(), dropin=True)
+    for _ in range(max(args.warmup, 3)):
+        ld.lik.invalidate = True
+        ld.lnL()
+    dropin_runs = args.steps * 8
+    t0 = time.perf_counter()
+    for _ in range(dropin_runs):
+        ld.lik.invalidate = True
+        dropin_lnl = ld.lnL()
+    dropin_s = dist.max((time.perf_counter() - t0) / dropin_runs)
+    dh2d, dd2h = ctypes.c_size_t(), ctypes.c_size_t()
+    gpu.cxgLikLastIo(ctypes.byref(dh2d), ctypes.byref(dd2h))
     nops = res["fp32"]["info"]["nops"]
     npat = int(res["fp32"]["lik"].lik.mschars)
-    written = nops * npat * (4 * WORKLOAD["ncat"] * 4 + 4)
 
     info = res["fp32"]["info"]
     ws = dist.ws
@@ -346,6 +383,7 @@ def run_ours(args, dist):
                                        threads, min_s=args.cpu_seconds)
         want = case.lik(lib=lib, alignment=case.alignment()).lnL()
         check = {p: abs(res[p]["lnL"] - want) / abs(want) for p in res}
+        check["dropin_fp64"] = abs(dropin_lnl - want) / abs(want)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": "%d full-tree FP64 lnL evaluations (%.1f s)" %
                          (nev, secs)}
@@ -367,22 +405,32 @@ def run_ours(args, dist):
             "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Yule tree, GTR+G4 simulation)",
-            "config": dict(WORKLOAD, patterns=int(fp64["lik"].lik.mschars),
-                           node_updates_per_eval=nops,
-                           evals_per_step=args.batch,
-                           parallelism="replicas" if ws > 1 else "single",
-                           walker_shape=res["fp32"]["shape"],
-                           walker_shape_fp64=fp64["shape"],
-                           l2_flush="inputs>L2 (each step writes %.2f GB of CLs)"
-                                    % (written / 1e9)),
+            "config": tree128_config(npat, nops, ws),
+            "evals_per_step": args.batch,
+            "walker_shape": res["fp32"]["shape"],
+            "walker_shape_fp64": fp64["shape"],
             "e2e": {"value": e2e, "unit": UNIT,
-                    "h2d_bytes_per_step": int(h2d.value),
-                    "d2h_bytes_per_step": int(d2h.value),
-                    "planner_ms_per_eval": planner_ms},
+                    "h2d_bytes_per_step": int(h2d.value) * args.batch,
+                    "d2h_bytes_per_step": int(d2h.value) * args.batch,
+                    "evals_per_step": args.batch,
+                    "ms_per_eval": e2e_s * 1e3,
+                    "planner_ms_per_eval": planner_ms,
+                    "api": "Lik.lnL (cxgLikExecuteLnL), FP32-scaled form"},
+            "e2e_dropin": {"value": info["updates"] * ws / dropin_s,
+                           "unit": UNIT,
+                           "h2d_bytes_per_eval": int(dh2d.value),
+                           "d2h_bytes_per_eval": int(dd2h.value),
+                           "ms_per_eval": dropin_s * 1e3,
+                           "api": "CxLikExecute with host siteLnL/stripeLnL "
+                                  "(plain FP64 form)"},
             "gpu_launches": args.steps * args.batch * info["kernels_per_run"],
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": traffic,
+                         "traffic_source": "committed ncu summary "
+                                           "profiles/walk_kernel_fp32_128taxa_"
+                                           "100ksites.md (not measured in "
+                                           "this run)",
                          "peak_source": "measured" if peaks else "fallback"},
             "cpu_baseline": cpu,
             "clocks": res["fp32"]["clocks"],

@@ -91,8 +91,6 @@ def declare(lib):
     lib.cxgBatchInfo.restype = c_int
     lib.cxgBatchDestroy.argtypes = [vp]
     lib.cxgBatchDestroy.restype = c_int
-    from . import _native_ext
-    _native_ext.declare_ext(lib)
     return lib
 
 

@@ -199,6 +199,10 @@ class Lik:
         buffers with leaf rows of 4 doubles, CxLikExecute, and the stripe
         sum -- instead of the device-resident cxg* path."""
         self.lib = lib if lib is not None else default_library()
+        # A host library that sets plan_natively = False is planned by the
+        # Python restatement alone and never maps the GB300 library.
+        if not getattr(self.lib, "plan_natively", True):
+            self.native_plan = False
         self.dropin = dropin
         self.device = hasattr(self.lib, "cxgLikClForget") and not dropin
         self.precision = precision

@@ -19,17 +19,22 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_SO = os.path.join(HERE, "_ref", "libcxlik_ref.so")
 PORT_SO = os.path.join(HERE, "_build", "libcxlik_port.so")
-REF_TREE = "/root/reference/crux"
+STAGED = os.path.join(HERE, "_ref", "src", "lib", "Crux", "Tree", "CxLik.c")
 
 _cache = {}
 
 
-def build(ref_tree=REF_TREE):
-    """Build the port, and the reference core when its sources exist."""
+def build(ref_tree=None):
+    """Build the port, and the reference core when its sources exist: from
+    `ref_tree` (or $CRUX_REF), a crux source tree, which also stages the
+    files under oracle/_ref/src; else from a staged copy made earlier."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
-    if os.path.isdir(os.path.join(ref_tree, "lib", "Crux", "Tree")):
+    ref_tree = ref_tree or os.environ.get("CRUX_REF")
+    if ref_tree and os.path.isdir(os.path.join(ref_tree, "lib", "Crux", "Tree")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + ref_tree],
                        check=True)
+    elif os.path.exists(STAGED):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF="], check=True)
 
 
 def _capsule_pointer(capsule):
@@ -64,6 +69,7 @@ def load_ref():
         lib.CxThreaded.argtypes = []
         lib.CxThreaded.restype = None
         lib.kind = "reference"
+        lib.plan_natively = False
         _declare(lib)
     _cache["ref"] = lib
     return lib
@@ -89,6 +95,7 @@ def load_port():
     lib.port_get_threads.argtypes = []
     lib.port_get_threads.restype = ctypes.c_int
     lib.kind = "port"
+    lib.plan_natively = False
     _declare(lib)
     _cache["port"] = lib
     return lib

@@ -6,7 +6,11 @@ Each fixture stores its inputs -- rooted Newick, the compressed alignment
 (rows of pattern characters and their frequencies), the GTR/Gamma/+I
 parameters and the host-core count that fixed the stripe padding -- and the
 reference's outputs: lnL, site lnLs, and the lnL after each of a sequence of
-single-branch rescales (dirty-path recomputes).
+single-branch rescales (dirty-path recomputes), each beside the lnL of the
+same tree evaluated from scratch by a second reference Lik (every CL
+recomputed), so that a dirty-path result is pinned independently of the
+planner's cache-validity rule.  The planner here is the Python restatement
+of Lik._plan alone.
 """
 import json
 import os
@@ -32,7 +36,7 @@ NCPUS = 8
 
 
 def main():
-    oracle.build()
+    oracle.build(os.environ.get("CRUX_REF", "/root/reference/crux"))
     ref = oracle.load_ref()
     assert ref is not None, "reference core not built"
     Config.ncpus = NCPUS
@@ -42,6 +46,8 @@ def main():
         rows = [aln.getSeq(i) for i in range(aln.ntaxa)]
         freqs = [int(x) for x in aln.freqs]
         lik = case.lik(lib=ref, alignment=aln)
+        scratch = case.lik(lib=ref, alignment=aln)
+        assert not lik.native_plan and not scratch.native_plan
         lnl = lik.lnL()
         sites = lik.siteLnLs()
         rng = np.random.default_rng(seed)
@@ -51,7 +57,14 @@ def main():
             i = int(rng.integers(len(edges)))
             f = float(rng.uniform(0.5, 2.0))
             edges[i].length *= f
-            dirty.append([i, f, lik.lnL()])
+            se = scratch.tree.edges
+            se[i].length *= f
+            assert se[i].length == edges[i].length
+            scratch.lik.invalidate = True
+            full = scratch.lnL()
+            got = lik.lnL()
+            assert abs(got - full) <= 1e-12 * abs(full), (got, full)
+            dirty.append([i, f, got, full])
         fx = {"name": name, "newick": case.newick, "taxa": aln.taxaMap.taxa,
               "rows": rows, "freqs": freqs, "params": case.params,
               "alpha": case.alpha, "ncat": case.ncat, "pinv": pinv,

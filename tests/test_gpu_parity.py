@@ -25,6 +25,18 @@ def rel(a, b):
     return abs(a - b) / max(abs(b), 1e-300)
 
 
+def from_scratch(case, lo):
+    """lnL of `lo`'s current tree from a fresh oracle Lik that recomputes
+    every CL (invalidate, Python planner): a dirty-path result checked
+    against this does not depend on the planner's cache-validity rule."""
+    fresh = case.lik(lib=lo.lib, alignment=lo.alignment)
+    assert not fresh.native_plan
+    for e, src in zip(fresh.tree.edges, lo.tree.edges):
+        e.length = src.length
+    fresh.lik.invalidate = True
+    return fresh.lnL()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_kat_lik_b(gpu, port, precision):
     g = K.run_lik_b(gpu, precision)
@@ -117,6 +129,9 @@ def test_synthetic_full_then_dirty_paths(gpu, port, shape, precision):
         a, b = lg.lnL(), lo.lnL()
         assert lg.nsteps < 2 * nt - 2 or nt < 8
         assert rel(a, b) <= TOL[precision], (a, b)
+        full = from_scratch(case, lo)
+        assert rel(b, full) <= 1e-12, (b, full)
+        assert rel(a, full) <= TOL[precision], (a, full)
     sg = np.array(lg.siteLnLs())
     so = np.array(lo.siteLnLs())
     tol = TOL[precision] * np.maximum(1.0, np.abs(so)) * 10
@@ -262,9 +277,11 @@ def test_golden_fixtures(gpu, path, precision):
     assert np.all(np.abs(sites - want) <=
                   TOL[precision] * np.maximum(1.0, np.abs(want)) * 10)
     edges = lik.tree.edges
-    for i, f, w in fx["dirty"]:
+    for i, f, w, scratch in fx["dirty"]:
         edges[i].length *= f
-        assert rel(lik.lnL(), w) <= TOL[precision]
+        got = lik.lnL()
+        assert rel(got, w) <= TOL[precision]
+        assert rel(got, scratch) <= TOL[precision]
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
@@ -279,12 +296,16 @@ def test_many_dirty_paths_gtr_gamma_inv(gpu, port, precision):
     base = [e.length for e in eg]
     rng = np.random.default_rng(8)
     assert rel(lg.lnL(), lo.lnL()) <= TOL[precision]
-    for _ in range(300):
+    for k in range(300):
         i = int(rng.integers(len(eg)))
         f = float(rng.uniform(0.5, 2.0))
         eg[i].length = eo[i].length = base[i] * f
         a, b = lg.lnL(), lo.lnL()
         assert rel(a, b) <= TOL[precision], (a, b)
+        if k % 10 == 0:
+            full = from_scratch(case, lo)
+            assert rel(b, full) <= 1e-12, (k, b, full)
+            assert rel(a, full) <= TOL[precision], (k, a, full)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])

@@ -16,9 +16,12 @@ def test_port_matches_reference_fixture(port, path):
     sites = np.array(lik.siteLnLs())
     assert np.allclose(sites, fx["siteLnL"], rtol=1e-12, atol=1e-12)
     edges = lik.tree.edges
-    for i, f, want in fx["dirty"]:
+    for i, f, want, scratch in fx["dirty"]:
         edges[i].length *= f
-        assert math.isclose(lik.lnL(), want, rel_tol=1e-12)
+        got = lik.lnL()
+        assert math.isclose(got, want, rel_tol=1e-12)
+        # The same tree from scratch (every CL recomputed).
+        assert math.isclose(got, scratch, rel_tol=1e-12)
 
 
 def test_fixtures_present():

@@ -106,6 +106,7 @@ def test_native_planner_matches_python_planner(port, seed):
     case = synth.Case(10, 300, 0.1, 40 + seed)
     a = case.lik(lib=port)
     b = case.lik(lib=port)
+    a.native_plan = True
     b.native_plan = False
     rng = random.Random(seed)
     root_a = root_b = None
@@ -139,6 +140,7 @@ def test_native_planner_matches_python_planner(port, seed):
             b.flush()
         elif op < 0.85:
             ma, mb = a.clone(), b.clone()
+            ma.native_plan = True
             mb.native_plan = False
             for _ in range(rng.randrange(1, 4)):
                 _check_same(ma, mb, _lnl(ma, root_a), _lnl(mb, root_b))
@@ -163,6 +165,7 @@ def test_native_planner_full_and_dirty_plans(port):
     case = synth.Case(64, 200, 0.05, 11)
     a = case.lik(lib=port)
     b = case.lik(lib=port)
+    a.native_plan = True
     b.native_plan = False
     # The first plans create every CL (which any traversal kept for the
     # native planner notices); from the third plan on `a` plans natively.
@@ -205,6 +208,7 @@ def test_native_planner_polytomies(port):
     b = Lik(K.tree_for(newick, aln), aln, ncat=4, lib=port)
     a.setAlpha(0, 0.7)
     b.setAlpha(0, 0.7)
+    a.native_plan = True
     b.native_plan = False
     degrees = sorted(n.getDegree() for n in a.tree.nodes)
     assert degrees[-1] >= 4
