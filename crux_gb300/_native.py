@@ -17,6 +17,27 @@ class NativeUnavailable(RuntimeError):
     pass
 
 
+CXG_ENOMEM = -2
+CXG_ETIMEOUT = -4
+
+
+class DeviceTimeout(RuntimeError):
+    """A bounded device wait gave up (CXG_ETIMEOUT)."""
+
+
+def error(lib, rc, what):
+    """The exception for return code `rc` of the library call `what`:
+    MemoryError for CXG_ENOMEM (the reference raises MemoryError when an
+    allocation fails, Lik.pyx:66-84), DeviceTimeout for CXG_ETIMEOUT,
+    RuntimeError otherwise."""
+    msg = "%s: %s" % (what, lib.cxgLastError().decode(errors="replace"))
+    if rc == CXG_ENOMEM:
+        return MemoryError(msg)
+    if rc == CXG_ETIMEOUT:
+        return DeviceTimeout(msg)
+    return RuntimeError(msg)
+
+
 def declare(lib):
     """Declare every entry point of include/cxlik_gpu.h on `lib`."""
     _abi.declare_core(lib)
@@ -91,6 +112,10 @@ def declare(lib):
     lib.cxgBatchInfo.restype = c_int
     lib.cxgBatchDestroy.argtypes = [vp]
     lib.cxgBatchDestroy.restype = c_int
+    lib.cxgDebugSetSpinLimit.argtypes = [c_uint, P(c_uint)]
+    lib.cxgDebugSetSpinLimit.restype = c_int
+    lib.cxgDebugFailAllocs.argtypes = [ctypes.c_longlong]
+    lib.cxgDebugFailAllocs.restype = c_int
     return lib
 
 

@@ -9,7 +9,7 @@ import ctypes
 
 import numpy as np
 
-from . import _abi
+from . import _abi, _native
 
 PER_NODE = 1
 
@@ -27,13 +27,11 @@ class Batch:
                                      PER_NODE if per_node else 0,
                                      ctypes.byref(self.h))
         if rc != 0:
-            raise RuntimeError("cxgBatchCreate: %s"
-                               % self.lib.cxgLastError().decode())
+            raise _native.error(self.lib, rc, "cxgBatchCreate")
 
     def _check(self, rc, what):
         if rc != 0:
-            raise RuntimeError("%s: %s" % (what,
-                                           self.lib.cxgLastError().decode()))
+            raise _native.error(self.lib, rc, what)
 
     def run(self):
         out = np.zeros(len(self.liks))

@@ -48,7 +48,7 @@ def compact(alignment, lib=None, masks=True):
                         out_freqs.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
                         _u8(out_masks) if masks else None, ctypes.byref(npat))
     if rc != 0:
-        raise RuntimeError("cxgCompact: %s" % lib.cxgLastError().decode())
+        raise _native.error(lib, rc, "cxgCompact")
     n = npat.value
     r = out_rows[:ntaxa * n].reshape(ntaxa, n)
     m = out_masks[:ntaxa * n].reshape(ntaxa, n) if masks else None

@@ -255,7 +255,7 @@ cudaEvent_t g_stage_ev[2] = {nullptr, nullptr};
 int stage_init() {
     if (g_stage[0]) return 0;
     unsigned char *p = nullptr;
-    CXG_CUDA(cudaMallocHost((void **)&p, 2 * kStageChunk));
+    CXG_CUDA(host_alloc((void **)&p, 2 * kStageChunk));
     cudaError_t e = cudaEventCreateWithFlags(&g_stage_ev[0], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g_stage_ev[1], cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -338,7 +338,7 @@ extern "C" int cxgCompact(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
     char *d = nullptr;
     cudaStream_t s = nullptr;
     CXG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    cudaError_t e = cudaMallocAsync((void **)&d, o_work + work, s);
+    cudaError_t e = dev_malloc_async((void **)&d, o_work + work, s);
     if (e != cudaSuccess) {
         cudaStreamDestroy(s);
         return cuda_fail(e, "cxgCompact: device memory");

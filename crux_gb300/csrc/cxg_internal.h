@@ -25,7 +25,8 @@ constexpr unsigned kTile = 64;
 constexpr unsigned kMaxSlots = 16;
 // Op records in flight per CTA (bulk-copy ring depth).
 constexpr unsigned kRing = 4;
-// Iteration bound of every spin on an mbarrier.
+// Default iteration bound of every spin on an mbarrier (the record waits
+// take theirs from set_spin_limit).
 constexpr unsigned kSpinLimit = 1u << 26;
 // Largest number of active mixture components held in registers.
 constexpr unsigned kMaxComps = 8;
@@ -248,6 +249,12 @@ struct PmatArgs {
     double *ltab;              // FP64 plans: leaf-message tables
 };
 
+// Allocations of the library (cxg_lik.cu); each fails as an out-of-memory
+// would once the test budget of cxgDebugFailAllocs is spent.
+cudaError_t dev_malloc(void **p, size_t n);
+cudaError_t dev_malloc_async(void **p, size_t n, cudaStream_t s);
+cudaError_t host_alloc(void **p, size_t n);
+
 // Thread-local error message.
 void set_error(const std::string &msg);
 int fail(int code, const std::string &msg);
@@ -277,5 +284,8 @@ cudaError_t launch_plan(int precision, const PlanArgs &a, cudaStream_t s,
 cudaError_t launch_qdecomp(const double *rtri, const double *pi, double *out,
                            cudaStream_t s);
 unsigned plan_blocks(unsigned ppad, unsigned tile);
+// try_wait attempts of the walkers' record waits on the current device
+// (0: give up without waiting).
+cudaError_t set_spin_limit(uint32_t limit);
 
 }  // namespace cxg

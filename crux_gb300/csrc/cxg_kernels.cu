@@ -346,11 +346,33 @@ __device__ __forceinline__ void issue_stage(const PlanArgs &a, unsigned q,
         bulk_g2s(st + a.rstride + (size_t)j * tile, rows[j] + off, tile, bar);
 }
 
+// Attempts of mbarrier.try_wait per record wait (set_spin_limit; the
+// default is kSpinLimit, 0 gives up without waiting).  Read once per tile
+// by the thread that waits.
+__device__ uint32_t g_spin_limit = kSpinLimit;
+
+cudaError_t set_spin_limit(uint32_t limit) {
+    return cudaMemcpyToSymbol(g_spin_limit, &limit, sizeof(limit));
+}
+
 // Spin on a phase with an iteration bound; false if it gave up.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-    for (uint32_t it = 0; it < kSpinLimit; ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                  uint32_t limit = kSpinLimit) {
+    for (uint32_t it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
+}
+
+// After a wait gave up at op (or step) o of n: wait, with the default
+// bound, for the copies still in flight into the ring -- the stages of
+// ops o .. o + R - 1 -- so that none lands after the CTA has left.
+// `phase` is the parity state before op o's stage was flipped.
+__device__ __noinline__ void drain_ring(uint64_t *bars, uint32_t phase, unsigned o,
+                                        unsigned n, unsigned R) {
+    for (unsigned q = o; q < n && q < o + R; ++q) {
+        const unsigned st = q % R;
+        mbar_wait_bounded(&bars[st], (phase >> st) & 1u);
+    }
 }
 
 // Max of n values as a balanced tree (the same value as a left-to-right
@@ -465,6 +487,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
     // stored FP32 row is acc itself.
     const void *prev_data = nullptr;
     S prev_lns = S(0);
+    const uint32_t spin = tid == 0 ? g_spin_limit : 0u;
     for (unsigned o = 0; o < nsteps; ++o) {
         const unsigned stage = o % R;
         // Streaming: thread 0 reads op o + R's leaf-row pointers now; it
@@ -473,7 +496,8 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
         if (!STAGED && tid == 0 && o + R < nsteps) read_rows(a, o + R, pre);
         if (tid == 0) {
             const uint32_t par = (phase >> stage) & 1u;
-            s_ok = mbar_wait_bounded(&bars[stage], par);
+            s_ok = mbar_wait_bounded(&bars[stage], par, spin);
+            if (!s_ok) drain_ring(bars, phase, o, nsteps, R);
             phase ^= 1u << stage;
         }
         __syncthreads();
@@ -797,13 +821,15 @@ __device__ bool walk_tile2(const PlanArgs &a, unsigned tile_idx, const SmemLayou
 
     T acc[2][K * 4];
     int lns[2] = {0, 0};
+    const uint32_t spin = tid == 0 ? g_spin_limit : 0u;
     for (unsigned o = 0; o < a.nops; ++o) {
         const unsigned stage = o % R;
         const uint8_t *pre[kLeafPre] = {nullptr, nullptr, nullptr, nullptr};
         if (!STAGED && tid == 0 && o + R < a.nops) read_rows(a, o + R, pre);
         if (tid == 0) {
             const uint32_t par = (phase >> stage) & 1u;
-            s_ok = mbar_wait_bounded(&bars[stage], par);
+            s_ok = mbar_wait_bounded(&bars[stage], par, spin);
+            if (!s_ok) drain_ring(bars, phase, o, a.nops, R);
             phase ^= 1u << stage;
         }
         __syncthreads();

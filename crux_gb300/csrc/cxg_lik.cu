@@ -15,6 +15,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <unordered_map>
@@ -35,7 +36,37 @@ int fail(int code, const std::string &msg) {
 
 int cuda_fail(cudaError_t err, const char *what) {
     g_err = std::string(what) + ": " + cudaGetErrorString(err);
-    return CXG_ECUDA;
+    return err == cudaErrorMemoryAllocation ? CXG_ENOMEM : CXG_ECUDA;
+}
+
+// Every device and pinned-host allocation of the library goes through
+// these.  For tests (cxgDebugFailAllocs), g_alloc_budget >= 0 is the
+// number of allocations that may still succeed; once it is spent, every
+// allocation fails as an out-of-memory would, without calling CUDA.
+static std::atomic<long long> g_alloc_budget{-1};
+
+static bool alloc_allowed() {
+    long long b = g_alloc_budget.load();
+    while (b >= 0) {
+        if (b == 0) return false;
+        if (g_alloc_budget.compare_exchange_weak(b, b - 1)) return true;
+    }
+    return true;
+}
+
+cudaError_t dev_malloc(void **p, size_t n) {
+    if (!alloc_allowed()) return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, n);
+}
+
+cudaError_t dev_malloc_async(void **p, size_t n, cudaStream_t s) {
+    if (!alloc_allowed()) return cudaErrorMemoryAllocation;
+    return cudaMallocAsync(p, n, s);
+}
+
+cudaError_t host_alloc(void **p, size_t n) {
+    if (!alloc_allowed()) return cudaErrorMemoryAllocation;
+    return cudaHostAlloc(p, n, cudaHostAllocDefault);
 }
 
 
@@ -63,7 +94,7 @@ struct DevBuf {
         p = nullptr;
         cap = 0;
         size_t want = n < 4096 ? 4096 : n + n / 2;
-        cudaError_t e = cudaMalloc(&p, want);
+        cudaError_t e = dev_malloc(&p, want);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(scratch)");
         cap = want;
         return 0;
@@ -80,7 +111,7 @@ struct HostBuf {
         p = nullptr;
         cap = 0;
         size_t want = n < 4096 ? 4096 : n + n / 2;
-        cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+        cudaError_t e = host_alloc(&p, want);
         if (e != cudaSuccess) return cuda_fail(e, "cudaHostAlloc(staging)");
         cap = want;
         return 0;
@@ -178,8 +209,8 @@ static int parent_buffer(State &S, const CxtLikCL *cl, unsigned npat,
     c.ppad = ppad;
     c.kcap = kact;
     const size_t elt = prec == CXG_FP32 ? 4 : 8;
-    CXG_CUDA(cudaMalloc(&c.data, (size_t)kact * 4 * ppad * elt));
-    cudaError_t e = cudaMalloc(&c.scaler, (size_t)ppad * 8);
+    CXG_CUDA(dev_malloc(&c.data, (size_t)kact * 4 * ppad * elt));
+    cudaError_t e = dev_malloc(&c.scaler, (size_t)ppad * 8);
     if (e != cudaSuccess) {
         cudaFree(c.data);
         return cuda_fail(e, "cudaMalloc(scaler)");
@@ -209,8 +240,12 @@ static int upload_leaf(State &S, const double *key, const uint8_t *masks,
     std::vector<uint8_t> h(c.ppad, 15);  // pad patterns: all states allowed
     for (unsigned i = 0; i < n; ++i)
         h[i] = (masks[i] & 15) ? (masks[i] & 15) : (zero_any ? 15 : 0);
-    CXG_CUDA(cudaMalloc(&c.data, c.ppad));
-    CXG_CUDA(cudaMemcpy(c.data, h.data(), c.ppad, cudaMemcpyHostToDevice));
+    CXG_CUDA(dev_malloc(&c.data, c.ppad));
+    cudaError_t e = cudaMemcpy(c.data, h.data(), c.ppad, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(c.data);
+        return cuda_fail(e, "cudaMemcpy(leaf masks)");
+    }
     S.cl_bytes += c.ppad;
     S.cls.emplace((uintptr_t)key, c);
     return 0;
@@ -844,13 +879,15 @@ static int finish(State &S, Plan &P, double *lnL, double *site) {
                                  (size_t)P.npat * 8, cudaMemcpyDeviceToHost,
                                  S.stream));
     CXG_CUDA(cudaStreamSynchronize(S.stream));
-    for (DevCL *p : P.parents) p->computed = true;
     const char *o = static_cast<const char *>(P.out.p);
     uint32_t ninf, err;
     double tot[2];
     memcpy(&ninf, o + 4, 4);
     memcpy(&err, o + 8, 4);
     memcpy(tot, o + 16, 16);
+    // A walk that gave up leaves its parents partly written: a later plan
+    // may not read them as children until they are recomputed.
+    for (DevCL *p : P.parents) p->computed = (err == 0);
     if (err)
         return fail(CXG_ETIMEOUT,
                     "plan walker: an op-record copy did not complete in time");
@@ -1108,6 +1145,25 @@ int cxgTuneGet(unsigned *tile, unsigned *tpp, unsigned *ppt, size_t *smem_budget
     return 0;
 }
 
+int cxgDebugSetSpinLimit(unsigned limit, unsigned *previous) {
+    State &S = state();
+    std::lock_guard<std::mutex> g(S.mu);
+    int rc = ensure_ready(S);
+    if (rc) return rc;
+    static unsigned current = kSpinLimit;
+    // No walker of this library may be running while the bound changes.
+    CXG_CUDA(cudaDeviceSynchronize());
+    CXG_CUDA(set_spin_limit(limit));
+    if (previous) *previous = current;
+    current = limit;
+    return 0;
+}
+
+int cxgDebugFailAllocs(long long after) {
+    g_alloc_budget.store(after < 0 ? -1 : after);
+    return 0;
+}
+
 int cxgLikLastIo(size_t *h2d, size_t *d2h) {
     State &S = state();
     std::lock_guard<std::mutex> g(S.mu);
@@ -1301,11 +1357,11 @@ static int batch_finish(State &S, cxgBatch *b, double *lnLs) {
         memcpy(&ninf, o + j * 32 + 4, 4);
         memcpy(&err, o + j * 32 + 8, 4);
         memcpy(tot, o + j * 32 + 16, 16);
+        for (DevCL *p : b->plans[j]->parents) p->computed = (err == 0);
         if (err)
             return fail(CXG_ETIMEOUT,
                         "batched walker: an op-record copy did not complete");
         if (lnLs) lnLs[j] = ninf ? -INFINITY : tot[0] + tot[1];
-        for (DevCL *p : b->plans[j]->parents) p->computed = true;
     }
     return 0;
 }

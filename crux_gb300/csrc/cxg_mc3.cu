@@ -382,8 +382,10 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         philox_init(rng, d.seed, c, g);
         if (c == 0) *d.counter = 0;
         char *res = d.results + (size_t)c * 32;
+        // A walker tile that gave up on a bounded wait leaves the ticket
+        // counted short; the error word stays set until the run reports it.
+        *(uint32_t *)(res + 0) = 0;  // ticket
         *(uint32_t *)(res + 4) = 0;  // ninf
-        *(uint32_t *)(res + 8) = 0;  // err
 
         const Mc3Model &m0 = d.model[c * 2 + d.curmodel[c]];
         Mc3Model &m1 = d.model[c * 2 + (1 - d.curmodel[c])];
@@ -1114,7 +1116,7 @@ struct cxgMc3 {
 static std::mutex g_mc3_mu;
 
 static int mc3_alloc(cxgMc3 *h, void **p, size_t n) {
-    cudaError_t e = cudaMalloc(p, n ? n : 16);
+    cudaError_t e = dev_malloc((void **)p, n ? n : 16);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(mc3)");
     h->allocs.push_back(*p);
     e = cudaMemset(*p, 0, n ? n : 16);

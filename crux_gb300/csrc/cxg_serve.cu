@@ -355,7 +355,7 @@ int upload_dataset(unsigned N, unsigned npat, const uint8_t *masks,
     ds.ntaxa = N;
     ds.npat = npat;
     ds.stride = ppad;
-    CXG_CUDA(cudaMallocAsync((void **)&ds.mem, ds.bytes, s));
+    CXG_CUDA(dev_malloc_async((void **)&ds.mem, ds.bytes, s));
     ds.masks = (uint8_t *)ds.mem;
     ds.weights = (uint32_t *)(ds.mem + al256((size_t)N * ppad));
     ds.leaves = (const uint8_t **)(ds.mem + al256((size_t)N * ppad) + al256((size_t)npat * 4));
@@ -457,7 +457,7 @@ int prepare_job(cxgServer *S, SrvJob &J) {
     J.kact = K;
     J.ppad = P.ppad;
     J.ntiles = P.ntiles;
-    CXG_CUDA(cudaMallocAsync((void **)&J.mem, P.job_bytes, S->s_prep));
+    CXG_CUDA(dev_malloc_async((void **)&J.mem, P.job_bytes, S->s_prep));
     char *p = J.mem;
     auto take = [&](size_t n) {
         char *q = p;
@@ -613,7 +613,7 @@ int launch_batch_of(cxgServer *S, SrvBatch &B, cudaStream_t st) {
     if (B.slot < 0) return fail(CXG_EBUSY, "server: no free result slot");
     S->slot_busy[B.slot] = true;
     B.host = S->pinned + (size_t)B.slot * S->cfg.max_active * 32;
-    CXG_CUDA(cudaMallocAsync((void **)&B.mem, B.bytes, st));
+    CXG_CUDA(dev_malloc_async((void **)&B.mem, B.bytes, st));
     char *res = B.mem + o_res;
     for (size_t j = 0; j < n; ++j) {
         SrvJob *J = B.jobs[j];
@@ -925,9 +925,8 @@ extern "C" int cxgServerCreate(const cxgServerConfig *cfg, cxgServer **out) {
         return cuda_fail(e, "cudaMemGetInfo");
     }
     S->budget = cfg->hbm_budget ? (size_t)cfg->hbm_budget : (size_t)(fr * 0.8);
-    if ((e = cudaHostAlloc((void **)&S->pinned,
-                           (size_t)kResultSlots * S->cfg.max_active * 32,
-                           cudaHostAllocDefault)) != cudaSuccess) {
+    if ((e = host_alloc((void **)&S->pinned,
+                        (size_t)kResultSlots * S->cfg.max_active * 32)) != cudaSuccess) {
         delete S;
         return cuda_fail(e, "cudaHostAlloc(server results)");
     }
@@ -1090,8 +1089,9 @@ extern "C" int cxgServerAddDatasetRaw(cxgServer *S, unsigned long long id, unsig
     const size_t in_bytes = (size_t)N * nsites;
     char *tmp = nullptr;
     int rc = 0;
-    cudaError_t e = cudaMallocAsync((void **)&ds->mem, ds->bytes, s);
-    if (e == cudaSuccess) e = cudaMallocAsync((void **)&tmp, al256(in_bytes) + 1024 + 256 + work, s);
+    cudaError_t e = dev_malloc_async((void **)&ds->mem, ds->bytes, s);
+    if (e == cudaSuccess)
+        e = dev_malloc_async((void **)&tmp, al256(in_bytes) + 1024 + 256 + work, s);
     if (e != cudaSuccess) {
         if (ds->mem) cudaFreeAsync(ds->mem, s);
         cudaStreamSynchronize(s);

@@ -26,7 +26,7 @@ import weakref
 
 import numpy as np
 
-from . import _abi
+from . import _abi, _native
 from .cxmath import gamma_rates
 
 CACHE_LINE = 64
@@ -290,8 +290,7 @@ class Lik:
             n = int(L.mschars)
             rc = self.lib.cxgLikSetPatternWeights(L.charFreqs, n)
             if rc != 0:
-                raise RuntimeError("cxgLikSetPatternWeights: %s"
-                                   % self.lib.cxgLastError().decode())
+                raise _native.error(self.lib, rc, "cxgLikSetPatternWeights")
             fin = weakref.finalize(self, self.lib.cxgLikForgetPatternWeights,
                                    _abi.uptr(self._freqs), n)
             fin.atexit = False  # the process's exit releases the device copy
@@ -637,8 +636,7 @@ class Lik:
                 masks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
                 L.mschars)
             if rc != 0:
-                raise RuntimeError("cxgLikClSetLeafMasks: %s"
-                                   % self.lib.cxgLastError().decode())
+                raise _native.error(self.lib, rc, "cxgLikClSetLeafMasks")
         else:
             mat = cl.bufs[0][0].reshape(L.mschars, L.dim)
             for j in range(L.dim):
@@ -1025,6 +1023,14 @@ class Lik:
     def _precision_code(self):
         return 1 if self.precision == "fp32" else 0
 
+    def _failed(self, rc):
+        """The exception for a failed evaluation.  The plan marked its CLs
+        valid before the run, which did not complete (an allocation failed,
+        or a bounded device wait gave up), so the next plan recomputes
+        every CL."""
+        self.lik.invalidate = True
+        return _native.error(self.lib, rc, "cxgLikExecuteLnL")
+
     def lnL(self, root=None):
         """Log-likelihood, rooted at `root` (default: the tree's base)."""
         self._prep(root)
@@ -1034,8 +1040,7 @@ class Lik:
                                            self._precision_code(),
                                            ctypes.byref(out), None)
             if rc != 0:
-                raise RuntimeError("cxgLikExecuteLnL: %s"
-                                   % self.lib.cxgLastError().decode())
+                raise self._failed(rc)
             return out.value
         self.lib.CxLikExecute(ctypes.byref(self.lik))
         ret = 0.0
@@ -1053,8 +1058,7 @@ class Lik:
                                            ctypes.byref(out),
                                            _abi.dptr(self.siteLnLBuf))
             if rc != 0:
-                raise RuntimeError("cxgLikExecuteLnL: %s"
-                                   % self.lib.cxgLastError().decode())
+                raise self._failed(rc)
         else:
             self.lib.CxLikExecute(ctypes.byref(self.lik))
         n = self.lik.nchars - self.lik.npad

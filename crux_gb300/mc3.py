@@ -214,13 +214,11 @@ class Mc3:
         self.h = ctypes.c_void_p()
         rc = self.lib.cxgMc3Create(ctypes.byref(c), ctypes.byref(self.h))
         if rc != 0:
-            raise RuntimeError("cxgMc3Create: %s"
-                               % self.lib.cxgLastError().decode())
+            raise _native.error(self.lib, rc, "cxgMc3Create")
 
     def _check(self, rc, what):
         if rc != 0:
-            raise RuntimeError("%s: %s" % (what,
-                                           self.lib.cxgLastError().decode()))
+            raise _native.error(self.lib, rc, what)
 
     def run(self, ngen):
         secs = ctypes.c_double()

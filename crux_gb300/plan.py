@@ -16,13 +16,11 @@ class Plan:
         rc = self.lib.cxgPlanCreate(ctypes.byref(lik.lik), code,
                                     ctypes.byref(self.h))
         if rc != 0:
-            raise RuntimeError("cxgPlanCreate: %s"
-                               % self.lib.cxgLastError().decode())
+            raise _native.error(self.lib, rc, "cxgPlanCreate")
 
     def _check(self, rc, what):
         if rc != 0:
-            raise RuntimeError("%s: %s" % (what,
-                                           self.lib.cxgLastError().decode()))
+            raise _native.error(self.lib, rc, what)
 
     def run(self):
         out = ctypes.c_double()

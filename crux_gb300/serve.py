@@ -139,8 +139,7 @@ class Server:
         self.h = ctypes.c_void_p()
         rc = self.lib.cxgServerCreate(ctypes.byref(c), ctypes.byref(self.h))
         if rc != 0:
-            raise RuntimeError("cxgServerCreate: %s"
-                               % self.lib.cxgLastError().decode())
+            raise _native.error(self.lib, rc, "cxgServerCreate")
         self._keep = {}
 
     def submit(self, prepared):
@@ -148,8 +147,7 @@ class Server:
         rc = self.lib.cxgServerSubmit(self.h, ctypes.byref(prepared.req),
                                       ctypes.byref(t))
         if rc != 0:
-            raise RuntimeError("cxgServerSubmit: %s"
-                               % self.lib.cxgLastError().decode())
+            raise _native.error(self.lib, rc, "cxgServerSubmit")
         return t.value
 
     def add_dataset(self, ident, prepared):
@@ -159,8 +157,7 @@ class Server:
             self.h, ident, prepared.req.ntaxa, prepared.req.npat,
             prepared.req.masks, prepared.req.pattern_freqs)
         if rc != 0:
-            raise RuntimeError("cxgServerAddDataset: %s"
-                               % self.lib.cxgLastError().decode())
+            raise _native.error(self.lib, rc, "cxgServerAddDataset")
 
     def add_dataset_raw(self, ident, alignment):
         """Keep a raw (uncompacted) alignment's patterns on the device under
@@ -178,23 +175,20 @@ class Server:
             rows.ctypes.data_as(u8), canon.ctypes.data_as(u8),
             val.ctypes.data_as(u8), ch.any, ctypes.byref(npat))
         if rc != 0:
-            raise RuntimeError("cxgServerAddDatasetRaw: %s"
-                               % self.lib.cxgLastError().decode())
+            raise _native.error(self.lib, rc, "cxgServerAddDatasetRaw")
         return npat.value
 
     def drop_dataset(self, ident):
         rc = self.lib.cxgServerDropDataset(self.h, ident)
         if rc != 0:
-            raise RuntimeError("cxgServerDropDataset: %s"
-                               % self.lib.cxgLastError().decode())
+            raise _native.error(self.lib, rc, "cxgServerDropDataset")
 
     def wait(self, ticket, timeout=120.0):
         v, lat = ctypes.c_double(), ctypes.c_double()
         rc = self.lib.cxgServerWait(self.h, ticket, timeout, ctypes.byref(v),
                                     ctypes.byref(lat))
         if rc != 0:
-            raise RuntimeError("cxgServerWait: %s"
-                               % self.lib.cxgLastError().decode())
+            raise _native.error(self.lib, rc, "cxgServerWait")
         return v.value, lat.value
 
     def stats(self):

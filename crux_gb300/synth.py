@@ -164,13 +164,14 @@ class Case:
         t.canonize(taxaMap)
         return t
 
-    def lik(self, lib=None, precision="fp64", alignment=None):
+    def lik(self, lib=None, precision="fp64", alignment=None, dropin=False):
         from .lik import Lik
         aln = alignment if alignment is not None else self.alignment()
         t = self.tree(aln.taxaMap)
         invar = self.pinv > 0.0
         ncat = self.ncat if self.alpha is not None else 1
-        lik = Lik(t, aln, ncat=ncat, invar=invar, lib=lib, precision=precision)
+        lik = Lik(t, aln, ncat=ncat, invar=invar, lib=lib, precision=precision,
+                  dropin=dropin)
         apply_params(lik, 0, self.params, self.alpha, self.pinv)
         return lik
 

@@ -462,6 +462,19 @@ int cxgTuneGet(unsigned *tile, unsigned *threads_per_pattern,
 int cxgTuneLanes(unsigned lanes);
 int cxgTuneLanesGet(unsigned *lanes);
 
+/* Failure paths, for tests (no counterpart in the reference).
+ * cxgDebugSetSpinLimit: mbarrier.try_wait attempts the plan walkers make
+ * per op-record wait before giving up (the default is 2^26; 0 gives up at
+ * once).  A walk that gives up drains its copies in flight, sets the run's
+ * error word and the call returns CXG_ETIMEOUT; the CLs it was computing
+ * count as not computed.  Waits for the device to be idle first; *previous
+ * (optional) receives the bound it replaces.
+ * cxgDebugFailAllocs: let `after` more device or pinned-host allocations
+ * of the library succeed, then fail every one as an out-of-memory
+ * (CXG_ENOMEM) without calling CUDA; negative: off. */
+int cxgDebugSetSpinLimit(unsigned limit, unsigned *previous);
+int cxgDebugFailAllocs(long long after);
+
 /* No counterpart in the reference.  Evaluate lik's plan without allocating
  * anything, for callers that cannot call cudaMalloc.  Such a caller may
  * own the device heap through its own pool or allocator, may be on a
