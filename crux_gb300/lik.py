@@ -183,6 +183,23 @@ def planner_library():
     return _planner[0]
 
 
+def _lik_unpickled(precision, dropin):
+    """An empty Lik for pickle to fill (Lik.__setstate__); its library is
+    set by Lik.unpickle."""
+    ret = Lik.__new__(Lik)
+    ret.lib = None
+    ret.dropin = dropin
+    ret.device = False
+    ret.precision = precision
+    ret.lik = None
+    ret.mate = None
+    ret._models = []
+    ret._snap = None
+    ret._pyKey = None
+    ret._compsKey = None
+    return ret
+
+
 class _Snap:
     """A flattened rooted traversal for cxgPlanSnapRun (see Lik._snapBuild)."""
 
@@ -198,13 +215,8 @@ class Lik:
         `dropin`: drive the library exactly as Lik.pyx does -- host CL
         buffers with leaf rows of 4 doubles, CxLikExecute, and the stripe
         sum -- instead of the device-resident cxg* path."""
-        self.lib = lib if lib is not None else default_library()
-        # A host library that sets plan_natively = False is planned by the
-        # Python restatement alone and never maps the GB300 library.
-        if not getattr(self.lib, "plan_natively", True):
-            self.native_plan = False
         self.dropin = dropin
-        self.device = hasattr(self.lib, "cxgLikClForget") and not dropin
+        self._set_lib(lib if lib is not None else default_library())
         self.precision = precision
         self.lik = None
         self.mate = None
@@ -224,6 +236,14 @@ class Lik:
             self._init2(alignment, char_)
             for _ in range(nmodels):
                 self.addModel(1.0, ncat, catMedian, invar)
+
+    def _set_lib(self, lib):
+        self.lib = lib
+        # A host library that sets plan_natively = False is planned by the
+        # Python restatement alone and never maps the GB300 library.
+        if not getattr(lib, "plan_natively", True):
+            self.native_plan = False
+        self.device = hasattr(lib, "cxgLikClForget") and not self.dropin
 
     # -- construction (Lik.pyx:221-324) ------------------------------------
     @staticmethod
@@ -531,6 +551,160 @@ class Lik:
         self._comps[mod.comp0 + mod.clen - 1]["cweight"] = wInvar
         self._sync_comps()
         self.lik.reweight = True
+
+    # -- pickling (Lik.pyx:326-386, 573-585) ---------------------------------
+    def __reduce__(self):
+        return (_lik_unpickled, (self.precision, self.dropin), self.__getstate__())
+
+    def __getstate__(self):
+        """(tree, nchars, dim) and one tuple per model: weight, rmult,
+        rclass, rates, freqs, alpha, ncat, catMedian, invar, wVar, wInvar.
+        The alignment is not part of the state: ``unpickle`` takes it from
+        the Lik it is called on."""
+        init_args = (self.tree, self.lik.nchars, self.lik.dim)
+        models = []
+        for i in range(len(self._models)):
+            models.append((self.getWeight(i), self.getRmult(i), self.getRclass(i),
+                           [self.getRate(i, j) for j in range(self.getNrates(i))],
+                           [self.getFreq(i, j) for j in range(self.lik.dim)],
+                           self.getAlpha(i), self.getNcat(i), self.getCatMedian(i),
+                           self.getInvar(i), self.getWVar(i), self.getWInvar(i)))
+        return (init_args, models)
+
+    def __setstate__(self, data):
+        init_args, models = data
+        tree, nchars, dim = init_args
+        self._init0(tree)
+        self._init1(tree, nchars, dim, 0)
+        for i, (weight, rmult, rclass, rates, freqs, alpha, ncat, catMedian,
+                invar, wVar, wInvar) in enumerate(models):
+            self.addModel(weight, ncat, catMedian, invar)
+            self.setRmult(i, rmult)
+            self.setRclass(i, rclass, rates)
+            assert len(freqs) == self.lik.dim
+            for j in range(self.lik.dim):
+                self.setFreq(i, j, freqs[j])
+            if alpha != math.inf:
+                self.setAlpha(i, alpha)
+            if invar:
+                self.setWVar(i, wVar)
+                self.setWInvar(i, wInvar)
+
+    def unpickle(self, data):
+        """The partial Lik pickled in `data` (bytes), completed with this
+        Lik's alignment, library, precision and drop-in mode."""
+        import pickle
+        ret = pickle.loads(data)
+        ret.dropin = self.dropin
+        ret._set_lib(self.lib)
+        ret._init2(self.alignment, self.char_)
+        return ret
+
+    # -- simulation (Lik.pyx:662-833) ---------------------------------------
+    def simulate(self, nchars=0, rng=None):
+        """A duplicate of this Lik (see dup) whose alignment holds sequences
+        simulated under the current models, tree and branch lengths: nchars
+        sites (default: as many as this alignment's unpadded sites), padded
+        to the stripe width as a new Lik would be, uncompacted.  Draws come
+        from `rng` (a random.Random; default: the random module), in the
+        reference's order: the root sequence component by component, then
+        each child edge depth-first in ring order."""
+        import random
+        from .alignment import Alignment
+        rng = rng if rng is not None else random
+        ret = Lik(lib=self.lib, precision=self.precision, dropin=self.dropin)
+        tree = self.tree.dup()
+        if nchars == 0:
+            nchars = self.alignment.nchars - self.alignment.npad
+        aln = Alignment(taxaMap=self.alignment.taxaMap, nchars=nchars,
+                        charType=self.alignment.charType)
+        npad = self._computeNpad(nchars, self._computeStripeWidth(nchars))
+        if npad != 0:
+            aln.pad(self.char_.val2code(self.char_.any), npad)
+            nchars += npad
+        ret._init0(tree)
+        ret._init1(tree, nchars, self.lik.dim, 0)
+        ret._init2(aln, self.char_)
+        self._dup(ret)
+        ret._simulate(rng)
+        return ret
+
+    def _simulate(self, rng):
+        L = self.lik
+        dim = L.dim
+        i2c = "".join(self.char_.pcodes())
+        self.prep()
+        # Breaks between the sites simulated under each component, by
+        # weightScaled (Lik.pyx:760-776).
+        nsim = self.alignment.nchars - self.alignment.npad
+        brks = []
+        wsum = 0.0
+        for i in range(L.compsLen - 1):
+            wsum += L.comps[i].weightScaled
+            if wsum > 1.0:
+                wsum = 1.0
+            brks.append(int(math.ceil(wsum * float(nsim))))
+        brks.append(nsim)
+
+        def cdf_of(row):
+            cdf, cum = [], 0.0
+            for j in range(dim - 1):
+                cum += row[j]
+                if cum > 1.0:
+                    cum = 1.0
+                cdf.append(cum)
+            cdf.append(1.0)
+            return cdf
+
+        def draw(cdf):
+            u = rng.random()
+            for j in range(dim):
+                if cdf[j] >= u:
+                    return j
+            raise AssertionError("CDF does not reach 1")
+
+        def root_seq():
+            seq, c = [], 0
+            for comp in range(L.compsLen):
+                m = L.comps[comp].model.contents
+                cdf = cdf_of([m.piDiagNorm[j] for j in range(dim)])
+                while c < brks[comp]:
+                    seq.append(draw(cdf))
+                    c += 1
+            return seq
+
+        P = np.zeros(dim * dim, dtype=np.float64)
+
+        def child_seq(par, brlen):
+            seq, c = [], 0
+            for comp in range(L.compsLen):
+                m = L.comps[comp].model.contents
+                self.lib.CxLikPt(dim, _abi.dptr(P), m.qEigVecCube, m.qEigVals,
+                                 brlen)
+                cdfs = [cdf_of(P[i * dim:(i + 1) * dim]) for i in range(dim)]
+                while c < brks[comp]:
+                    seq.append(draw(cdfs[par[c]]))
+                    c += 1
+            return seq
+
+        def put(node, seq):
+            if node.getTaxon() is not None:
+                self.alignment.setSeq(
+                    self.alignment.taxaMap.indGet(node.getTaxon()), 0,
+                    "".join(i2c[x] for x in seq))
+
+        base = self.tree.getBase()
+        seq = root_seq()
+        put(base, seq)
+        if base.ring is None:
+            return
+        stack = [(r.other, seq) for r in reversed(list(base.ring))]
+        while stack:
+            ring, par = stack.pop()
+            s = child_seq(par, ring.edge.length)
+            put(ring.node, s)
+            for r in reversed(list(ring.siblings())):
+                stack.append((r.other, s))
 
     # -- copies (Lik.pyx:587-660, 835-883) ------------------------------------
     def _dup(self, other):

@@ -292,6 +292,28 @@ class Tree:
             new.base = rec(self.base, None)
         return new
 
+    # -- pickling (__init__.pyx:53-63, 626-647, 801-809) ---------------------
+    def __reduce__(self):
+        """Pickled as flat tables, not as the linked ring structure (whose
+        recursion a deep tree would overflow): every node's taxon and its
+        rings in ring order from its head ring, every edge's length, the
+        base.  Unpickling rebuilds the same ring order, which fixes the
+        post-order step plan; aux data (CL caches) is dropped, as the
+        reference's __setstate__ drops it."""
+        nodes, edges = self._walk()
+        nid = {id(n): i for i, n in enumerate(nodes)}
+        eid = {id(e): i for i, e in enumerate(edges)}
+        rings = []
+        for n in nodes:
+            rs = []
+            if n.ring is not None:
+                for r in n.ring:
+                    rs.append((eid[id(r.edge)], 0 if r is r.edge.ring else 1))
+            rings.append(rs)
+        state = (self.rooted, nid[id(self.base)] if self.base is not None else -1,
+                 [n.taxon for n in nodes], rings, [e.length for e in edges])
+        return (_tree_from_state, (state,))
+
     def render(self, lengths=True, fmt="%.7e"):
         """Newick text of an unrooted tree (for diagnostics)."""
         out = []
@@ -332,6 +354,32 @@ _TOKEN = re.compile(r"""
   | (?P<qlabel>'(?:[^']|'')*')
   | (?P<word>[^\s()\[\]':;,]+)
 """, re.X)
+
+
+def _tree_from_state(state):
+    """Rebuild a Tree pickled by Tree.__reduce__."""
+    rooted, base, taxa, rings, lengths = state
+    t = Tree()
+    t.rooted = rooted
+    nodes = []
+    for taxon in taxa:
+        n = Node(t)
+        n.taxon = taxon
+        nodes.append(n)
+    edges = []
+    for length in lengths:
+        e = Edge(t)
+        e.length = length
+        edges.append(e)
+    for n, rs in zip(nodes, rings):
+        objs = [edges[e].ring if end == 0 else edges[e].ring.other for e, end in rs]
+        for i, r in enumerate(objs):
+            r.node = n
+            r.next = objs[(i + 1) % len(objs)]
+            r.prev = objs[i - 1]
+        n.ring = objs[0] if objs else None
+    t.base = nodes[base] if base >= 0 else None
+    return t
 
 
 class NewickParser:

@@ -360,3 +360,24 @@ def test_repeated_full_plans_reuse_translation(gpu, port, precision):
                 lk.lik.invalidate = True
             assert rel(b.lnL(), rb.lnL()) <= TOL[precision]
     assert len(set(seen)) == len(seen)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_pickle_round_trip_and_simulate(gpu, port, precision):
+    """A pickled Lik completed by unpickle gives the same lnL bit for bit
+    on the GPU (Lik.pyx:326-386, 573-585); a simulated Lik (Lik.pyx:
+    662-833, P(t) from the GPU library's CxLikPt) evaluates on the GPU as
+    the oracle evaluates the same simulated alignment."""
+    import pickle
+    import random
+    case = synth.Case(20, 1500, 0.1, 95, pinv=0.2)
+    lik = case.lik(lib=gpu, precision=precision)
+    want = lik.lnL()
+    ret = lik.unpickle(pickle.dumps(lik))
+    assert ret.lnL() == want
+    sim = lik.simulate(3000, rng=random.Random(7))
+    got = sim.lnL()
+    ref = Lik(sim.tree.dup(), sim.alignment, ncat=case.ncat, invar=True,
+              lib=port)
+    synth.apply_params(ref, 0, case.params, case.alpha, case.pinv)
+    assert rel(got, ref.lnL()) <= TOL[precision], (got, ref.lnL())
