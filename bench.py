@@ -288,7 +288,7 @@ def run_ours(args, dist):
 
     from crux_gb300 import tune
     res = {}
-    for prec in (("fp32",) if args.profile else ("fp32", "fp64")):
+    for prec in ((args.precision,) if args.profile else ("fp32", "fp64")):
         lik = case.lik(lib=gpu, precision=prec)
         lnl_first = lik.lnL()
         lik.lik.invalidate = True
@@ -312,8 +312,8 @@ def run_ours(args, dist):
     if args.profile:
         for p in res.values():
             p["plan"].close()
-        print(json.dumps({"profile_run": True,
-                          "ms_per_run": res["fp32"]["ms"]}))
+        print(json.dumps({"profile_run": True, "precision": args.precision,
+                          "ms_per_run": res[args.precision]["ms"]}))
         return
 
     # End to end through the public API: full re-plan + lnL each run, with
@@ -443,9 +443,23 @@ def run_ours(args, dist):
             "kernel_ms": kern_ms,
             "rel_err_vs_fp64_oracle": check,
         }
+        for p in res.values():
+            p["plan"].close()
+        if not args.no_sub:
+            # Bounded MC3 and serving records on the same run (each under
+            # its own clock sampler), with the tree's tuned walker shapes.
+            shapes = {"fp32": res["fp32"]["shape"], "fp64": res["fp64"]["shape"]}
+            line["mc3"] = mc3_measure(
+                MC3["mc3"], args.sub_mc3_gens, args.sub_mc3_gens64,
+                shapes=shapes, oracle=None if args.no_cpu else lib,
+                check_every=1000, seq_gens=args.sub_mc3_gens64)
+            line["serve"] = serve_measure(args.sub_serve_datasets,
+                                          args.sub_serve_rates, 2.0,
+                                          shapes=shapes)
         print(json.dumps(line), flush=True)
-    for p in res.values():
-        p["plan"].close()
+    else:
+        for p in res.values():
+            p["plan"].close()
     dist.close()
 
 
@@ -566,85 +580,138 @@ MC3 = {"mc3": {"workload": "mc3_128taxa_100ksites_gtr_gamma4_8chains",
                     "check_every": 250}}
 
 
-def run_mc3(args, dist):
-    """On-device MC3: generations/s of the FP32-scaled chains and of the
-    plain FP64 chains from the same seed, with the cold chain's lnL checked
-    against the FP64 oracle every `check_every` generations."""
-    from crux_gb300 import _native, synth
+MC3_WARM = 48
+
+
+def mc3_measure(w, gens, gens64, shapes=None, args=None, oracle=None,
+                check_every=None, seq_gens=None):
+    """On-device MC3 on workload `w`: `gens` generations of the FP32 chains
+    and `gens64` of the plain FP64 chains from the same seed, each under its
+    own clock sampler.  Every `check_every` FP32 generations each chain's
+    lnL is checked against the FP64 oracle (`oracle`, a CPU library; None:
+    no check).  Over the first `seq_gens` generations both runs must take
+    the same accept/reject sequence: their per-chain, per-move accept and
+    reject counts are equal and their cold-chain traces agree to 1e-6.
+    `shapes`: walker shape per precision (else autotuned with `args`)."""
+    import numpy as np
+    from crux_gb300 import _native, synth, tune
     from crux_gb300.mc3 import Mc3
-    w = dict(MC3[args.workload])
-    if args.chains:
-        w["nchains"] = args.chains
-    gens = args.gens or w["gens"]
     gpu = _native.load()
     case = synth.Case(w["ntaxa"], w["nsites"], w["mean_brlen"], w["seed"])
     aln = case.alignment()
-    port = None
-    if not args.no_cpu:
-        from oracle import oracle
-        port = oracle.load_port()
-        port.port_set_threads(os.cpu_count() or 1)
+    check_every = check_every or w["check_every"]
+    seq_gens = min(seq_gens or gens64, gens, gens64)
     out = {}
-    for prec in (("fp32",) if args.profile else ("fp32", "fp64")):
-        lk = case.lik(lib=gpu, precision=prec, alignment=aln)
-        lk.prepare_plan()
-        shape = autotune(gpu, prec, args, lik=lk, lanes=False)
-        del lk
+    for prec, ngen in (("fp32", gens), ("fp64", gens64)):
+        if ngen <= 0:
+            continue
+        if shapes and prec in shapes:
+            sh = shapes[prec]
+            tune.set_shape(gpu, sh["tile"], sh["tpp"], sh["ppt"], sh["budget"])
+            shape = dict(sh, lanes=1, source=sh.get("source", "given"))
+        else:
+            lk = case.lik(lib=gpu, precision=prec, alignment=aln)
+            lk.prepare_plan()
+            shape = autotune(gpu, prec, args, lik=lk, lanes=False)
+            del lk
         m = Mc3(case.tree(aln.taxaMap), aln, case.params["rates"],
                 case.params["freqs"], alpha=0.5, ncat=4,
                 nchains=w["nchains"], heat_delta=w["heat_delta"],
                 seed=w["seed"], moves=w["moves"], precision=prec,
                 graph_gens=16)
-        m.run(max(args.warmup, 3) * 16)
-        secs = 0.0
-        drift = []
-        done = 0
+        # The same untimed warm-up in both precisions, so that their
+        # generations stay aligned for the accept/reject comparison.
+        m.run(MC3_WARM)
+        secs, drift, done = 0.0, [], 0
+        seq = None
         clocks = Clocks()
-        if prec == "fp32":
-            clocks.start()
-        while done < gens:
-            step = min(w["check_every"], gens - done)
+        clocks.start()
+        while done < ngen:
+            step = min(check_every - done % check_every, ngen - done)
+            if done < seq_gens < done + step:
+                step = seq_gens - done
             secs += m.run(step)
             done += step
-            if port is not None and prec == "fp32":
-                cold = max(range(m.nchains),
-                           key=lambda i: m.chain_state(i)["heat"])
-                lik, st = m.chain_lik(cold, port)
-                want = lik.lnL()
-                drift.append(abs(st["lnL"] - want) / abs(want))
-        ck = clocks.stop() if prec == "fp32" else None
+            if done == seq_gens:
+                st = m.stats()
+                seq = {"accepts": st["accepts"], "rejects": st["rejects"],
+                       "trace": m.trace(MC3_WARM + seq_gens)[MC3_WARM:]}
+            if oracle is not None and prec == "fp32" and \
+                    (done % check_every == 0 or done == ngen):
+                worst = 0.0
+                for i in range(m.nchains):
+                    lik, st = m.chain_lik(i, oracle)
+                    want = lik.lnL()
+                    worst = max(worst, abs(st["lnL"] - want) / abs(want))
+                drift.append({"generation": done, "max_rel_err": worst})
+        ck = clocks.stop()
         st = m.stats()
-        out[prec] = {"gens_per_s": gens / secs, "secs": secs,
-                     "accept_rate": (st["accepts"].sum() /
-                                     max(1, st["accepts"].sum() +
-                                         st["rejects"].sum())),
+        acc, rej = int(st["accepts"].sum()), int(st["rejects"].sum())
+        out[prec] = {"gens_per_s": ngen / secs, "gens": ngen, "secs": secs,
+                     "accept_rate": acc / max(1, acc + rej),
                      "swaps": int(st["swaps"].sum()) // 2,
-                     "drift": drift, "clocks": ck, "shape": shape,
-                     "trace_head": [float(x) for x in m.trace(8)]}
+                     "drift_vs_fp64_oracle": drift, "clocks": ck,
+                     "walker_shape": shape, "seq": seq}
         m.close()
+    res = {"workload": w["workload"], "config": dict(w, gens=gens,
+                                                     patterns=aln.nchars)}
+    for prec in out:
+        r = dict(out[prec])
+        r.pop("seq")
+        res[prec] = r
+    if "fp32" in out and "fp64" in out and out["fp32"]["seq"] is not None \
+            and out["fp64"]["seq"] is not None:
+        a, b = out["fp32"]["seq"], out["fp64"]["seq"]
+        rel = np.abs(a["trace"] - b["trace"]) / np.abs(b["trace"])
+        same = bool(np.array_equal(a["accepts"], b["accepts"]) and
+                    np.array_equal(a["rejects"], b["rejects"]) and
+                    (rel <= 1e-6).all())
+        res["accept_sequence"] = {
+            "generations": seq_gens, "same_fp32_fp64": same,
+            "max_trace_rel_diff": float(rel.max()),
+            "first_trace_divergence": (int(np.argmax(rel > 1e-6))
+                                       if (rel > 1e-6).any() else None)}
+        res["fp32_over_fp64"] = (out["fp32"]["gens_per_s"] /
+                                 out["fp64"]["gens_per_s"])
+    return res
+
+
+def run_mc3(args, dist):
+    """On-device MC3: generations/s of the FP32-scaled chains and of the
+    plain FP64 chains from the same seed, with every chain's lnL checked
+    against the FP64 oracle every `check_every` generations."""
+    w = dict(MC3[args.workload])
+    if args.chains:
+        w["nchains"] = args.chains
+    gens = args.gens or w["gens"]
+    oracle = None
+    if not args.no_cpu:
+        oracle, _, _ = load_cpu_oracle()
     if args.profile:
+        r = mc3_measure(w, gens, 0, args=args)
         print(json.dumps({"profile_run": True, "workload": w["workload"],
                           "nchains": w["nchains"],
-                          "gens_per_s": out["fp32"]["gens_per_s"]}))
+                          "gens_per_s": r["fp32"]["gens_per_s"]}))
         dist.close()
         return
-    f32, f64 = out["fp32"], out["fp64"]
+    r = mc3_measure(w, gens, gens, args=args, oracle=oracle)
+    f32, f64 = r["fp32"], r["fp64"]
     line = {
         "metric": "MC3 generations/s (FP32-scaled chains, on device)",
         "value": f32["gens_per_s"], "unit": "generations/s", "n_gpus": 1,
-        "steps": gens, "warmup": max(args.warmup, 3) * 16,
+        "steps": gens, "warmup": MC3_WARM,
         "ms_per_step": 1e3 * f32["secs"] / gens, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": dict(w, gens=gens, patterns=aln.nchars,
-                       walker_shape=f32["shape"], walker_shape_fp64=f64["shape"]),
+        "config": r["config"],
         "fp64_plain_gens_per_s": f64["gens_per_s"],
-        "fp32_over_fp64": f32["gens_per_s"] / f64["gens_per_s"],
+        "fp32_over_fp64": r["fp32_over_fp64"],
         "accept_rate": f32["accept_rate"], "swaps": f32["swaps"],
-        "drift_vs_fp64_oracle": f32["drift"],
-        "trace_head_fp32": f32["trace_head"],
-        "trace_head_fp64": f64["trace_head"],
-        "clocks": f32["clocks"],
+        "drift_vs_fp64_oracle": f32["drift_vs_fp64_oracle"],
+        "accept_sequence": r["accept_sequence"],
+        "walker_shape": f32["walker_shape"],
+        "walker_shape_fp64": f64["walker_shape"],
+        "clocks": f32["clocks"], "clocks_fp64": f64["clocks"],
     }
     print(json.dumps(line), flush=True)
     dist.close()
@@ -830,14 +897,18 @@ def make_serve_pool(n):
     return pool
 
 
-def run_serve(args, dist):
-    """Serving loop under Poisson arrivals: p50/p99 latency and throughput
-    of the FP32 form and of the plain FP64 form on the same arrivals."""
+def serve_measure(ndatasets, rates, seconds, args=None, shapes=None):
+    """The serving loop under Poisson arrivals at each of `rates` for
+    `seconds` each, on `ndatasets` resident datasets of the serve
+    workload's distribution, in the FP32 form and the plain FP64 form on
+    the same arrivals.  Returns the per-rate p50/p99 and throughput of
+    each precision, each precision's clocks, and the largest relative
+    difference between the FP32 and FP64 lnLs of the same requests."""
     import numpy as np
-    from crux_gb300.serve import MC3, PreparedRequest, Server
+    from crux_gb300 import _native, tune
+    from crux_gb300.serve import LNL, MC3, PreparedRequest, Server
     t0 = time.perf_counter()
-    from crux_gb300.serve import LNL
-    base = make_serve_pool(args.jobs or SERVE["datasets"])
+    base = make_serve_pool(ndatasets)
     # Each alignment is registered once as a resident dataset; requests
     # name it and carry only their tree and model.
     pool = [PreparedRequest(r.case, LNL, alignment=r.alignment,
@@ -848,17 +919,20 @@ def run_serve(args, dist):
                 for i, r in enumerate(base) if r.alignment.ntaxa >= 4
                 and r.case.pinv == 0.0]
     setup_s = time.perf_counter() - t0
-    rates = args.rates or SERVE["rates"]
-    out = {}
-    from crux_gb300 import _native
     gpu = _native.load()
     # Tune the walker on the median-sized dataset of the pool.
     med = sorted(base, key=lambda r: r.req.ntaxa * r.req.npat)[len(base) // 2]
+    out = {}
     for prec in ("fp32", "fp64"):
-        lk = med.case.lik(lib=gpu, precision=prec, alignment=med.alignment)
-        lk.prepare_plan()
-        out[prec + "_shape"] = autotune(gpu, prec, args, lik=lk, lanes=False)
-        del lk
+        if shapes and prec in shapes:
+            sh = shapes[prec]
+            tune.set_shape(gpu, sh["tile"], sh["tpp"], sh["ppt"], sh["budget"])
+            out[prec + "_shape"] = dict(sh, lanes=1)
+        else:
+            lk = med.case.lik(lib=gpu, precision=prec, alignment=med.alignment)
+            lk.prepare_plan()
+            out[prec + "_shape"] = autotune(gpu, prec, args, lik=lk, lanes=False)
+            del lk
         srv = Server(prec)
         for i, r in enumerate(base):
             srv.add_dataset(i + 1, r)
@@ -868,10 +942,11 @@ def run_serve(args, dist):
         for m in mc3_pool:
             srv.wait(srv.submit(m), timeout=600)
         per = []
+        clocks = Clocks()
+        clocks.start()
         for lam in rates:
             rng = np.random.default_rng(SERVE["seed"] + int(lam))
-            dur = SERVE["seconds_per_rate"]
-            n = max(10, int(lam * dur))
+            n = max(10, int(lam * seconds))
             gaps = rng.exponential(1.0 / lam, n)
             kinds = rng.random(n) < SERVE["mc3_prob"]
             picks = rng.integers(len(pool), size=n)
@@ -904,6 +979,7 @@ def run_serve(args, dist):
                         "max_batch": st["max_batch"], "batches": st["batches"],
                         "bytes_peak": st["bytes_peak"]})
             out.setdefault(prec + "_vals", {}).update(dict(vals))
+        out[prec + "_clocks"] = clocks.stop()
         srv.close()
         out[prec] = per
     errs = []
@@ -911,18 +987,34 @@ def run_serve(args, dist):
         w = out["fp64_vals"].get(k)
         if w is not None:
             errs.append(abs(v - w) / abs(w))
-    best = max(out["fp32"], key=lambda r: r["throughput_rps"])
+    return {"workload": SERVE["workload"],
+            "config": dict(SERVE, datasets=len(pool), rates=rates,
+                           seconds_per_rate=seconds, setup_s=round(setup_s, 1)),
+            "walker_shape": out["fp32_shape"],
+            "walker_shape_fp64": out["fp64_shape"],
+            "sweep_fp32": out["fp32"], "sweep_fp64": out["fp64"],
+            "clocks": out["fp32_clocks"], "clocks_fp64": out["fp64_clocks"],
+            "max_rel_err_fp32_vs_fp64": max(errs) if errs else None}
+
+
+def run_serve(args, dist):
+    """Serving loop under Poisson arrivals: p50/p99 latency and throughput
+    of the FP32 form and of the plain FP64 form on the same arrivals."""
+    rates = args.rates or SERVE["rates"]
+    r = serve_measure(args.jobs or SERVE["datasets"], rates,
+                      SERVE["seconds_per_rate"], args=args)
+    best = max(r["sweep_fp32"], key=lambda x: x["throughput_rps"])
     line = {
         "metric": "serving: p50/p99 latency and throughput (FP32-scaled form)",
         "value": best["throughput_rps"], "unit": "requests/s",
         "n_gpus": 1, "steps": len(rates), "warmup": 1,
         "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": dict(SERVE, datasets=len(pool), setup_s=round(setup_s, 1),
-                       rates=rates, walker_shape=out["fp32_shape"],
-                       walker_shape_fp64=out["fp64_shape"]),
-        "sweep_fp32": out["fp32"], "sweep_fp64": out["fp64"],
-        "max_rel_err_fp32_vs_fp64": max(errs) if errs else None,
+        "config": r["config"], "walker_shape": r["walker_shape"],
+        "walker_shape_fp64": r["walker_shape_fp64"],
+        "sweep_fp32": r["sweep_fp32"], "sweep_fp64": r["sweep_fp64"],
+        "clocks": r["clocks"], "clocks_fp64": r["clocks_fp64"],
+        "max_rel_err_fp32_vs_fp64": r["max_rel_err_fp32_vs_fp64"],
     }
     print(json.dumps(line), flush=True)
     dist.close()
@@ -947,7 +1039,9 @@ def main():
     ap.add_argument("--batch", type=int, default=256,
                     help="full-tree evaluations per step")
     ap.add_argument("--profile", action="store_true",
-                    help="FP32 plan only, no e2e/CPU legs (for ncu)")
+                    help="one plan (--precision) only, no e2e/CPU legs (for ncu)")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"],
+                    help="--profile: the plan's precision")
     ap.add_argument("--workload", default="tree128",
                     choices=["tree128", "batch256", "mc3", "mc3small", "dirty64", "compact",
                              "serve"])
@@ -959,6 +1053,17 @@ def main():
                     help="MC3 workloads: number of chains")
     ap.add_argument("--jobs", type=int, default=None,
                     help="batch256: number of jobs (default 256)")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="tree128: skip the MC3 and serving sub-records")
+    ap.add_argument("--sub-mc3-gens", type=int, default=2000,
+                    help="tree128: FP32 generations of the MC3 sub-record")
+    ap.add_argument("--sub-mc3-gens64", type=int, default=500,
+                    help="tree128: plain FP64 generations of the MC3 sub-record")
+    ap.add_argument("--sub-serve-datasets", type=int, default=8,
+                    help="tree128: resident datasets of the serving sub-record")
+    ap.add_argument("--sub-serve-rates", type=float, nargs="*",
+                    default=[100.0, 1000.0],
+                    help="tree128: arrival rates of the serving sub-record")
     args = ap.parse_args()
     dist = Dist()
     if args.impl == "reference":

@@ -14,8 +14,9 @@ namespace cxg {
 // the op record as the plan's precision.  A leaf child (tab >= 0) gets its
 // message table instead: row mask = sum over the allowed states j of
 // P[i][j], in j order (P times the reference's 0/1 row, CxLik.c:357-374
-// with Lik.pyx:1466-1475), in the FP64 table for FP64 plans and in the
-// record, rounded once to FP32, for FP32 plans.
+// with Lik.pyx:1466-1475), in the FP64 table for FP64 plans ([16 masks]
+// [kact][4]) and in the record, rounded once to FP32, for FP32 plans
+// ([kact][16 masks][4]).
 //
 // Four consecutive lanes (q = lane & 3, all four active) share one idx:
 // lane q computes exp(lambda_q t) and row i = q, so each lane runs a
@@ -59,9 +60,12 @@ __device__ inline void pmat_one(const PmatArgs &a, unsigned idx, unsigned q) {
             T[mk] = __dadd_rn(T[mk ^ (1 << h)], P[h]);
         }
         if (a.precision == CXG_FP32) {
-            float *o = reinterpret_cast<float *>(dst) + (size_t)k * 4 + i;
+            // Component-major, [kact][16 masks][4 states]: the walker's
+            // threads read one component's rows at once, so rows of
+            // different masks sit in different shared-memory banks.
+            float *o = reinterpret_cast<float *>(dst) + (size_t)k * 64 + i;
 #pragma unroll
-            for (int mk = 0; mk < 16; ++mk) o[(size_t)mk * a.kact * 4] = (float)T[mk];
+            for (int mk = 0; mk < 16; ++mk) o[(size_t)mk * 4] = (float)T[mk];
             return;
         }
         double *tt = a.ltab + ((size_t)tb * 16 * a.kact + k) * 4 + i;

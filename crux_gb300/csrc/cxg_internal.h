@@ -53,7 +53,7 @@ enum : uint32_t {
 //
 // A child's area is filled in place by the P-matrix kernel of each run:
 // the P matrices T P[kact][16], or for a leaf child of an FP32 plan its
-// message table float[16 masks][kact][4] (the message P x indicator(mask)
+// message table float[kact][16 masks][4] (the message P x indicator(mask)
 // of every state mask, summed in FP64 and rounded once).
 struct RecHead {
     void *data;        // parent CL in HBM, [K][U][ppad] 16-byte units

@@ -424,7 +424,6 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
     constexpr int U = Prec<T>::U;
     constexpr int KA = KT * G;  // active components of the job
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ int s_ok;
     const unsigned nthr = blockDim.x;
     const unsigned tile = nthr / (G * L);
     const unsigned tid = threadIdx.x;
@@ -487,31 +486,33 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
     // stored FP32 row is acc itself.
     const void *prev_data = nullptr;
     S prev_lns = S(0);
-    const uint32_t spin = tid == 0 ? g_spin_limit : 0u;
-    for (unsigned o = 0; o < nsteps; ++o) {
-        const unsigned stage = o % R;
+    const uint32_t spin = g_spin_limit;
+    for (unsigned o = 0, stage = 0; o < nsteps;
+         ++o, stage = (stage + 1 == R) ? 0u : stage + 1) {
         // Streaming: thread 0 reads op o + R's leaf-row pointers now; it
         // issues that stage after this op, when the loads have long arrived.
         const uint8_t *pre[kLeafPre] = {nullptr, nullptr, nullptr, nullptr};
         if (!STAGED && tid == 0 && o + R < nsteps) read_rows(a, o + R, pre);
-        if (tid == 0) {
-            const uint32_t par = (phase >> stage) & 1u;
-            s_ok = mbar_wait_bounded(&bars[stage], par, spin);
-            if (!s_ok) drain_ring(bars, phase, o, nsteps, R);
-            phase ^= 1u << stage;
-        }
-        __syncthreads();
-        if (!s_ok) {
-            if (tid == 0) atomicOr(a.err, 1u);
-            return false;  // all threads leave together
-        }
+        // Every thread waits for the op's record itself (one block barrier
+        // per op, the hand-off below); a warp computes only if all its
+        // threads saw the record arrive.
+        const bool ok =
+            __all_sync(0xffffffffu, mbar_wait_bounded(&bars[stage], (phase >> stage) & 1u,
+                                                      spin));
+        phase ^= 1u << stage;
+        void *ydata = nullptr, *yscaler = nullptr;
+        int yslot = -1;
+        bool yhbm = false;
+        uint32_t nbytes = (uint32_t)sstride;
+        unsigned nchild = 0;
+        T sc = T(0);  // plain form: max over child messages
+        if (ok) {
         const unsigned char *rec = ring + (size_t)stage * sstride + (size_t)lane * a.rstride;
         const uint8_t *lrow = rec + a.rstride;  // this op's leaf rows
         unsigned nlk = 0;  // leaf children of this op seen so far
         const RecHead *hd = reinterpret_cast<const RecHead *>(rec);
         const RecChild *kids = reinterpret_cast<const RecChild *>(rec + sizeof(RecHead));
-        const unsigned nchild = hd->nchild;
-        T sc = T(0);  // plain form: max over child messages
+        nchild = hd->nchild;
         lns = S(0);
         // A child's inputs: its state rows (internal) with its scaler, or
         // its leaf's state mask.  Loading them is split from computing the
@@ -544,10 +545,10 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             const unsigned m = in.m;
             if (sizeof(T) == 4 && ch.src == SRC_LEAF) {
                 // FP32 leaves: the message of mask m from the record's table.
-                const float4 *t = reinterpret_cast<const float4 *>(area) + (size_t)m * KA + k0;
+                const float4 *t = reinterpret_cast<const float4 *>(area) + (size_t)k0 * 16 + m;
 #pragma unroll
                 for (int k = 0; k < KT; ++k) {
-                    const float4 v = t[k];
+                    const float4 v = t[k * 16];
                     msg[k * 4 + 0] = (T)v.x;
                     msg[k * 4 + 1] = (T)v.y;
                     msg[k * 4 + 2] = (T)v.z;
@@ -640,17 +641,25 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
                 fold(ci, ch, in, msg);
             }
         }
-        void *ydata = hd->data;
-        void *yscaler = hd->scaler;
-        const int yslot = hd->slot;
-        const bool yhbm = !(hd->flags & REC_NO_HBM);
+        ydata = hd->data;
+        yscaler = hd->scaler;
+        yslot = hd->slot;
+        yhbm = !(hd->flags & REC_NO_HBM);
         // Size of the record that refills this stage: only its own bytes
         // (records of internal children are a third of a leaf table's).
-        const uint32_t nbytes = (L == 1 && hd->next_bytes != 0u &&
-                                 hd->next_bytes <= (uint32_t)sstride)
-                                    ? hd->next_bytes : (uint32_t)sstride;
-        // Every thread has read the stage: hand it to op o + R.
-        __syncthreads();
+        nbytes = (L == 1 && hd->next_bytes != 0u && hd->next_bytes <= (uint32_t)sstride)
+                     ? hd->next_bytes : (uint32_t)sstride;
+        }  // ok
+        // Every thread has read the stage: hand it to op o + R.  A record
+        // wait that gave up in any warp ends the tile for all: thread 0
+        // waits for the copies still in flight into the ring.
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) {
+                atomicOr(a.err, 1u);
+                drain_ring(bars, phase ^ (1u << stage), o, nsteps, R);
+            }
+            return false;
+        }
         if (tid == 0 && o + R < nsteps) {
             if (STAGED) {
                 fence_proxy_async();
@@ -678,7 +687,12 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
         } else {
             T mx = fmax(T(0), tree_max<KT * 4>(acc));
             mx = group_max<G>(mx);
-            if (mx > T(0) && mx <= (T)3.0e38) {
+            // Rescale only when the largest entry fell below 2^-16 (or the
+            // op has more than two children): every entry is at most 1, a
+            // binary op's result then keeps its largest entry far above the
+            // FP32 normal range's floor, and scaling by a power of two is
+            // exact, so each rescale that is skipped changes no mantissa.
+            if (mx > T(0) && mx <= (T)3.0e38 && (nchild > 2 || mx < (T)1.52587890625e-05f)) {
                 int e;
                 frexpf((float)mx, &e);
                 const int n = -e;
@@ -822,8 +836,8 @@ __device__ bool walk_tile2(const PlanArgs &a, unsigned tile_idx, const SmemLayou
     T acc[2][K * 4];
     int lns[2] = {0, 0};
     const uint32_t spin = tid == 0 ? g_spin_limit : 0u;
-    for (unsigned o = 0; o < a.nops; ++o) {
-        const unsigned stage = o % R;
+    for (unsigned o = 0, stage = 0; o < a.nops;
+         ++o, stage = (stage + 1 == R) ? 0u : stage + 1) {
         const uint8_t *pre[kLeafPre] = {nullptr, nullptr, nullptr, nullptr};
         if (!STAGED && tid == 0 && o + R < a.nops) read_rows(a, o + R, pre);
         if (tid == 0) {
@@ -857,10 +871,10 @@ __device__ bool walk_tile2(const PlanArgs &a, unsigned tile_idx, const SmemLayou
                 if (!STAGED) ++nlk;
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    const float4 *t = reinterpret_cast<const float4 *>(area) + (size_t)m[h] * K;
+                    const float4 *t = reinterpret_cast<const float4 *>(area) + m[h];
 #pragma unroll
                     for (int k = 0; k < K; ++k) {
-                        const float4 v = t[k];
+                        const float4 v = t[k * 16];
                         msg[h][k * 4 + 0] = v.x;
                         msg[h][k * 4 + 1] = v.y;
                         msg[h][k * 4 + 2] = v.z;
@@ -931,7 +945,8 @@ __device__ bool walk_tile2(const PlanArgs &a, unsigned tile_idx, const SmemLayou
             T mx = T(0);
 #pragma unroll
             for (int q = 0; q < K * 4; ++q) mx = fmax(mx, acc[h][q]);
-            if (mx > T(0) && mx <= (T)3.0e38) {
+            // The rescale rule of walk_tile (same bits).
+            if (mx > T(0) && mx <= (T)3.0e38 && (nchild > 2 || mx < 1.52587890625e-05f)) {
                 int e;
                 frexpf(mx, &e);
                 const int n = -e;

@@ -57,6 +57,7 @@ static std::mutex g_na_mu;
 
 // Device address of the scratch array on the current device; the first call
 // per device looks it up (do that first call before any stream capture).
+// The address stays valid for the life of the device's primary context.
 static int na_setup(unsigned char **out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
@@ -124,21 +125,30 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
         model_of[k] = idx;
     }
 
-    // Pass 1: count ops and children, check the step grammar.
+    // Pass 1: count ops and children, check the step grammar, and size the
+    // records: each op's exact bytes (header, children, each child's area
+    // by kind) and its number of leaf children, as the allocating path
+    // sizes them.
     unsigned nops = 0, nkids = 0, maxdeg = 0, deg = 0;
     const CxtLikCL *cur = nullptr;
     unsigned expect = 0;
+    size_t op_bytes = 0, max_bytes = 0;
+    unsigned op_leaves = 0, lmax = 0;
     for (unsigned s = 0; s < lik->stepsLen; ++s) {
         const CxtLikStep &stp = lik->steps[s];
         if ((unsigned)stp.variant > 3) return fail(CXG_EINVAL, "bad step variant");
         const bool compute = stp.variant == CxeLikStepComputeL ||
                              stp.variant == CxeLikStepComputeI;
+        const bool leaf = stp.variant == CxeLikStepComputeL ||
+                          stp.variant == CxeLikStepMergeL;
         if (compute) {
             if (cur != nullptr)
                 return fail(CXG_EINVAL, "Compute step before ntrail reached 0");
             cur = stp.parentCL;
             ++nops;
             deg = 0;
+            op_bytes = sizeof(RecHead);
+            op_leaves = 0;
         } else if (cur == nullptr || stp.parentCL != cur ||
                    stp.ntrail + 1 != expect) {
             return fail(CXG_EINVAL, "Merge step does not continue its node");
@@ -147,10 +157,19 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
             stp.parentCL->lnScale == nullptr || stp.childCL == nullptr ||
             stp.childCL->cLMat == nullptr)
             return fail(CXG_EINVAL, "step CL without device buffers");
+        // CL rows move in 16-byte units.
+        if (((uintptr_t)stp.parentCL->cLMat | (uintptr_t)stp.childCL->cLMat) % 16)
+            return fail(CXG_EINVAL, "CL buffer not 16-byte aligned");
         ++nkids;
         if (++deg > maxdeg) maxdeg = deg;
+        op_bytes += sizeof(RecChild) + child_area_bytes(prec, kact, leaf);
+        if (leaf) ++op_leaves;
         expect = stp.ntrail;
-        if (stp.ntrail == 0) cur = nullptr;
+        if (stp.ntrail == 0) {
+            cur = nullptr;
+            max_bytes = std::max(max_bytes, al16(op_bytes));
+            lmax = std::max(lmax, op_leaves);
+        }
     }
     if (cur != nullptr) return fail(CXG_EINVAL, "plan ends mid-node");
     if (nops > kNaMaxOps || nkids > kNaMaxKids)
@@ -160,17 +179,11 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
     if (lik->rootCLC == nullptr || lik->rootCLC->cLMat == nullptr ||
         lik->rootCLC->lnScale == nullptr)
         return fail(CXG_EINVAL, "rootCLC without device buffers");
+    if ((uintptr_t)lik->rootCLC->cLMat % 16)
+        return fail(CXG_EINVAL, "CL buffer not 16-byte aligned");
 
-    // Record stride: the largest op, every child taking the larger area
-    // (an FP32 leaf's message table or a P matrix).
-    size_t rstride = 16;
-    {
-        const size_t area = std::max(child_area_bytes(prec, kact, true),
-                                     child_area_bytes(prec, kact, false));
-        size_t b = sizeof(RecHead) + maxdeg * (sizeof(RecChild) + area);
-        b = al16(b);
-        if (b > rstride) rstride = b;
-    }
+    // Record stride: the largest op's own bytes.
+    const size_t rstride = std::max<size_t>(16, max_bytes);
     if ((size_t)(nops ? nops : 1) * rstride > kNaRecBudget)
         return fail(CXG_EINVAL, "cxgLikExecuteNoAlloc: op records above 1.5 MiB");
 
@@ -188,8 +201,8 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
     const size_t o_dst = al16(o_eig + nmod * 4 * 8);
     const size_t o_tab = al16(o_dst + (size_t)nkids * 8);
     const size_t o_pn = al16(o_tab + (size_t)nkids * 4);
-    // Leaf rows: up to maxdeg leaf children per op (lmax), null-terminated.
-    const unsigned lmax = maxdeg;
+    // Leaf rows: up to lmax leaf children per op, null-terminated when
+    // fewer.
     const size_t o_lrow = al16(o_pn + kact * 4 * 8);
     const size_t o_ltab =
         al16(o_lrow + (size_t)(nops ? nops : 1) * (lmax ? lmax : 1) * sizeof(void *));

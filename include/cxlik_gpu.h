@@ -477,17 +477,16 @@ int cxgDebugFailAllocs(long long after);
 
 /* No counterpart in the reference.  Evaluate lik's plan without allocating
  * anything, for callers that cannot call cudaMalloc.  Such a caller may
- * own the device heap through its own pool or allocator, may be on a
+ * own the device heap through its own pool or allocator, or may be on a
  * latency-critical path where cudaMalloc/cudaFree could synchronise the
- * device, or may be about to capture the work into a CUDA graph.  Every
- * memory the computation touches is the caller's:
+ * device.  Every memory the computation touches is the caller's:
  *   - each CxtLikCL in lik->steps and lik->rootCLC holds DEVICE pointers:
  *     internal CL: cLMat -> kact*4*ceil128(mschars) elements of the
  *     precision (double or float) laid out [kact][U][ppad] in 16-byte
  *     units, lnScale -> ppad scalers (double for CXG_FP64, int32 for
  *     CXG_FP32; size the buffer for 8 bytes per pattern); leaf CL: cLMat
- *     -> ppad uint8 state masks (pad patterns set to 15; 16-byte aligned, as
- *     cudaMalloc returns), lnScale unused;
+ *     -> ppad uint8 state masks (pad patterns set to 15), lnScale unused;
+ *     every cLMat 16-byte aligned, as cudaMalloc returns;
  *   - dFreqs: mschars uint32 pattern weights on the device;
  *   - dSiteLnL: optional device output of mschars site lnLs (NULL: none);
  *   - stream: the caller's cudaStream_t (NULL: the default stream).
@@ -495,8 +494,12 @@ int cxgDebugFailAllocs(long long after);
  * loads the library holds it until exit); limits: <= 1024 node updates,
  * <= 2048 children, <= 2^20 patterns, <= 8 active components.  The first
  * call on a device looks up that array's address: make it before any
- * stream capture.  Calls share the array; calls that overlap on the GPU
- * race.  Returns after the lnL has been copied back. */
+ * stream capture.  With CUDA's lazy module loading, the first call of each
+ * precision on a device also loads the library's kernels, which the driver
+ * may allocate for: make one call of each precision as a warm-up outside
+ * the region where nothing may allocate.  Calls share the array; calls
+ * that overlap on the GPU race.  Returns after the lnL has been copied
+ * back. */
 int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
                          const uint32_t *dFreqs, double *dSiteLnL,
                          void *stream, double *lnL);
