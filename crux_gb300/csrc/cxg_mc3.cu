@@ -54,9 +54,9 @@ namespace cxg {
 
 enum {
     MV_BRLEN = 0, MV_NNI = 1, MV_RATES = 2, MV_ALPHA = 3, MV_FREQS = 4, MV_SPR = 5,
-    MV_ETBR = 6, MV_INVAR = 7, MV_GAMMAJ = 8, MV_FREQJ = 9, MV_INIT = 10
+    MV_ETBR = 6, MV_INVAR = 7, MV_GAMMAJ = 8, MV_FREQJ = 9, MV_INVARJ = 10, MV_INIT = 11
 };
-constexpr int kMoves = 10;
+constexpr int kMoves = 11;
 
 struct Mc3Model {
     double rates[6], freqs[4], alpha;
@@ -121,7 +121,7 @@ struct Mc3Dev {
     double wcdf[kMoves];
     double brlen_lambda, brlen_prior, rate_conc, alpha_lambda, alpha_prior;
     double freq_conc, etbr_pext, invar_lambda, invar_prior;
-    double gamma_jump_prior, freq_jump_prior;
+    double gamma_jump_prior, freq_jump_prior, invar_jump_prior;
     uint32_t swap_stride;
     uint32_t *acc, *rej;  // [c][kMoves]
     uint32_t *nswap;      // [c]
@@ -406,7 +406,9 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             // move instead, so each jump is drawn with the same
             // probability on both of its sides.
             if (t == MV_ALPHA && (d.ncat < 2 || !m0.gamma_on)) t = MV_BRLEN;
-            if (t == MV_INVAR && !d.invar) t = MV_BRLEN;
+            if ((t == MV_INVAR && (!d.invar || m0.winvar == 0.0)) ||
+                (t == MV_INVARJ && !d.invar))
+                t = MV_BRLEN;
             if (t == MV_GAMMAJ && d.ncat < 2) t = MV_BRLEN;
             if (t == MV_FREQS && !m0.freqs_est) t = MV_BRLEN;
             pr.type = t;
@@ -620,6 +622,41 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 w = w1;
                 pr.lnPrior = -(which == 0 ? 1.0 - d.invar_prior : d.invar_prior) * (w1 - w0);
                 pr.lnHast = lnM;
+                pr.model_changed = 1;
+                s_fin = FIN_WEIGHTS;
+                full = true;
+            } else if (t == MV_INVARJ) {
+                // +I off or on (invarJumpPropose, Chain.pyx:1449-1546).  Off
+                // is wInvar = 0 with wVar = 1, as the reference's removal
+                // leaves it; the +I component stays in the layout with
+                // weight 0.  On, (wVar, wInvar) have the priors of the +I
+                // weight move, Exp of rates 1 - invarPrior and invarPrior
+                // (Chain.pyx:418-421), and adding draws them from those
+                // priors, so the prior and proposal densities cancel in the
+                // unheated chain; they are split between lnPrior and lnHast
+                // as the reference splits its terms.  (The reference draws
+                // added weights with means 1 - invarPrior and invarPrior,
+                // which is not the density its weight move and prior use.)
+                const double ip = d.invar_prior;
+                m1 = m0;
+                auto lnw = [&](double wv, double wi) {
+                    return log(1.0 - ip) - (1.0 - ip) * wv + log(ip) - ip * wi;
+                };
+                if (m0.winvar != 0.0) {
+                    const double dens = lnw(m0.wvar, m0.winvar);
+                    m1.wvar = 1.0;
+                    m1.winvar = 0.0;
+                    pr.lnPrior = log(d.invar_jump_prior) - dens;
+                    pr.lnHast = dens;
+                } else {
+                    const double wv = -log(1.0 - philox_u01(rng)) / (1.0 - ip);
+                    const double wi = -log(1.0 - philox_u01(rng)) / ip;
+                    const double dens = lnw(wv, wi);
+                    m1.wvar = wv;
+                    m1.winvar = wi > 0.0 ? wi : 1e-300;
+                    pr.lnPrior = -log(d.invar_jump_prior) + dens;
+                    pr.lnHast = -dens;
+                }
                 pr.model_changed = 1;
                 s_fin = FIN_WEIGHTS;
                 full = true;
@@ -1241,7 +1278,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     // (the reference disables PropInvar then, Mc3/__init__.pyx:934-937).
     double mw[kMoves], wsum = 0.0;
     for (int i = 0; i < kMoves; ++i) mw[i] = cfg->move_weight[i];
-    if (!invar) mw[MV_INVAR] = 0.0;
+    if (!invar) mw[MV_INVAR] = mw[MV_INVARJ] = 0.0;
     for (int i = 0; i < kMoves; ++i) wsum += mw[i];
     if (!(wsum > 0.0)) {
         mc3_free(h);
@@ -1267,8 +1304,10 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     d.invar_prior = cfg->invar_prior;
     d.gamma_jump_prior = cfg->gamma_jump_prior;
     d.freq_jump_prior = cfg->freq_jump_prior;
+    d.invar_jump_prior = cfg->invar_jump_prior;
     if ((mw[MV_GAMMAJ] > 0.0 && !(cfg->gamma_jump_prior > 0.0)) ||
-        (mw[MV_FREQJ] > 0.0 && !(cfg->freq_jump_prior > 0.0))) {
+        (mw[MV_FREQJ] > 0.0 && !(cfg->freq_jump_prior > 0.0)) ||
+        (mw[MV_INVARJ] > 0.0 && !(cfg->invar_jump_prior > 0.0))) {
         mc3_free(h);
         return fail(CXG_EINVAL, "cxgMc3Create: jump priors must be positive");
     }

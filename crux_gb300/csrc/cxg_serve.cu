@@ -868,6 +868,7 @@ void mc3_loop(cxgServer *S) {
             c.invar_prior = 0.5;
             c.gamma_jump_prior = 1.0;
             c.freq_jump_prior = 1.0;
+            c.invar_jump_prior = 1.0;
             c.precision = S->cfg.precision;
             c.graph_gens = r.mc3_gens ? r.mc3_gens : 10;
             c.trace_cap = 1;

@@ -21,7 +21,7 @@ from .tree import Tree
 
 LAMBDA = 2.0 * math.log(1.6)
 MOVES = ("brlen", "nni", "rates", "alpha", "freqs", "spr", "etbr", "invar",
-         "gammajump", "freqjump")
+         "gammajump", "freqjump", "invarjump")
 
 
 class Mc3Config(ctypes.Structure):
@@ -41,7 +41,7 @@ class Mc3Config(ctypes.Structure):
         ("heat_delta", ctypes.c_double),
         ("swap_stride", ctypes.c_uint),
         ("seed", ctypes.c_ulonglong),
-        ("move_weight", ctypes.c_double * 10),
+        ("move_weight", ctypes.c_double * 11),
         ("brlen_lambda", ctypes.c_double),
         ("brlen_prior", ctypes.c_double),
         ("rate_conc", ctypes.c_double),
@@ -57,6 +57,7 @@ class Mc3Config(ctypes.Structure):
         ("precision", ctypes.c_int),
         ("graph_gens", ctypes.c_uint),
         ("trace_cap", ctypes.c_ulonglong),
+        ("invar_jump_prior", ctypes.c_double),
     ]
 
 
@@ -154,7 +155,7 @@ class Mc3:
                  moves=None, precision="fp32", brlen_lambda=LAMBDA,
                  brlen_prior=10.0, rate_conc=300.0, freq_conc=300.0,
                  etbr_pext=0.8, pinv=0.0, invar_lambda=LAMBDA, invar_prior=0.5,
-                 gamma_jump_prior=1.0, freq_jump_prior=1.0,
+                 gamma_jump_prior=1.0, freq_jump_prior=1.0, invar_jump_prior=1.0,
                  alpha_lambda=LAMBDA,
                  alpha_prior=1.0, graph_gens=16, trace_cap=1 << 20, lib=None):
         self.lib = lib or _native.load()
@@ -202,6 +203,7 @@ class Mc3:
         c.invar_prior = invar_prior
         c.gamma_jump_prior = gamma_jump_prior
         c.freq_jump_prior = freq_jump_prior
+        c.invar_jump_prior = invar_jump_prior
         c.alpha_lambda = alpha_lambda
         c.alpha_prior = alpha_prior
         c.precision = 1 if precision == "fp32" else 0

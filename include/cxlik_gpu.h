@@ -320,10 +320,10 @@ typedef struct {
     double heat_delta;  /* chain i runs at heat 1/(1 + i*heat_delta) */
     unsigned swap_stride;
     unsigned long long seed;
-    double move_weight[10]; /* branch length, NNI, rates, alpha, base
+    double move_weight[11]; /* branch length, NNI, rates, alpha, base
                                frequencies, SPR, eTBR, +I weights, Gamma
                                on/off jump, equal/estimated frequency
-                               jump */
+                               jump, +I off/on jump */
     double brlen_lambda, brlen_prior;
     double rate_conc;       /* Dirichlet concentration of rate moves */
     double freq_conc;       /* Dirichlet concentration of frequency moves */
@@ -343,6 +343,8 @@ typedef struct {
     int precision;          /* CXG_FP32 or CXG_FP64 */
     unsigned graph_gens;    /* generations per captured graph (0: 16) */
     unsigned long long trace_cap;  /* cold-chain lnL trace length */
+    double invar_jump_prior; /* the reference's invarJumpPrior (1): prior
+                               odds of +I off to on */
 } cxgMc3Config;
 typedef struct cxgMc3 cxgMc3;
 /* Build the chains and run generation 0 (a full evaluation). */
@@ -356,7 +358,7 @@ int cxgMc3Chain(cxgMc3 *mc3, unsigned chain, double *lnL, double *heat,
                 double *alpha);
 /* Mixture weights (wVar, wInvar) of one chain's current model. */
 int cxgMc3ChainWeights(cxgMc3 *mc3, unsigned chain, double *wvar, double *winvar);
-/* Accept/reject counts [chain][move] (10 moves, in move_weight order),
+/* Accept/reject counts [chain][move] (11 moves, in move_weight order),
  * swaps [chain], generation count. */
 int cxgMc3Stats(cxgMc3 *mc3, unsigned *accepts, unsigned *rejects,
                 unsigned *swaps, unsigned long long *gen);

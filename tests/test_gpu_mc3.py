@@ -288,3 +288,61 @@ def test_mc3_jumps_sample_their_prior(gpu):
     assert abs(on / n - 0.25) < 0.04, on / n
     assert abs(est / n - 0.25) < 0.04, est / n
     assert abs(np.mean(rsi) - 1.0) < 0.15, np.mean(rsi)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_mc3_invar_jump_chains_match_oracle(gpu, port, precision):
+    """The +I off/on jump (invarJumpPropose, Chain.pyx:1449-1546) beside
+    the +I weight, alpha and branch moves: every chain's lnL is the
+    oracle's for its tree, model and weights, +I off reading as wInvar = 0
+    with wVar = 1; hot chains switch +I both ways."""
+    case = synth.Case(16, 100, 0.1, 47, pinv=0.2)
+    aln = case.alignment()
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=0.5,
+            ncat=4, pinv=0.2, nchains=4, heat_delta=3.0, seed=14,
+            moves={"brlen": 1.0, "invar": 1.0, "invarjump": 2.0, "alpha": 0.5},
+            precision=precision, graph_gens=8)
+    seen_off = seen_on_again = False
+    for _ in range(10):
+        m.run(24)
+        check_chains(m, port, TOL[precision])
+        for i in range(4):
+            st = m.chain_state(i)
+            if st["winvar"] == 0.0:
+                assert st["wvar"] == 1.0
+                seen_off = True
+            elif seen_off:
+                seen_on_again = True
+    st = m.stats()
+    assert st["accepts"].sum(axis=0)[10] > 0
+    assert seen_off and seen_on_again
+    m.close()
+
+
+def test_mc3_invar_jump_samples_its_prior(gpu):
+    """Without data the +I jump and weight moves sample the prior: +I on
+    and off equally often (invarJumpPrior 1), and when on, wVar and wInvar
+    of the weight move's priors, Exp of rates 1 - invarPrior and
+    invarPrior (means 2 at invarPrior 0.5).  A wrong Hastings ratio or
+    prior term moves the fraction or the means."""
+    case, aln = _empty_alignment(6, 33)
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=None,
+            pinv=0.3, nchains=4, heat_delta=0.0, seed=6, precision="fp64",
+            graph_gens=32, moves={"invar": 1.0, "invarjump": 1.0})
+    m.run(2000)
+    on, wv, wi = [], [], []
+    for _ in range(1200):
+        m.run(32)
+        for i in range(4):
+            st = m.chain_state(i)
+            assert abs(st["lnL"]) < 1e-9
+            on.append(st["winvar"] != 0.0)
+            if st["winvar"] != 0.0:
+                wv.append(st["wvar"])
+                wi.append(st["winvar"])
+    m.close()
+    assert abs(np.mean(on) - 0.5) < 0.06, np.mean(on)
+    assert abs(np.mean(wv) - 2.0) < 0.3, np.mean(wv)
+    assert abs(np.mean(wi) - 2.0) < 0.3, np.mean(wi)

@@ -29,3 +29,50 @@ def test_tree_arrays_round_trip(port):
     synth.apply_params(lik, 0, case.params, case.alpha)
     b = lik.lnL()
     assert math.isclose(a, b, rel_tol=1e-12)
+
+
+def test_invar_jump_terms_keep_the_prior():
+    """The +I jump's prior and Hastings terms, as the device proposal
+    computes them (cxg_mc3.cu, MV_INVARJ), with the +I weight move's terms,
+    run as a Markov chain without data: +I is on half the time
+    (invarJumpPrior 1) and, when on, wVar and wInvar have the weight
+    move's Exp priors of rates 1 - invarPrior and invarPrior (means 2)."""
+    rng = np.random.default_rng(1)
+    ip, lam = 0.5, 2.0 * math.log(1.6)
+
+    def lnw(a, b):
+        return math.log(1 - ip) - (1 - ip) * a + math.log(ip) - ip * b
+
+    on, wv, wi = True, 0.7, 0.3
+    n = 400_000
+    U = rng.random((n, 4))
+    non = swv = swi = 0.0
+    for u in U:
+        if u[0] < 0.5:                      # weight move (off: nothing)
+            if on:
+                lnm = lam * (u[2] - 0.5)
+                if u[1] < 0.5:
+                    w1 = wv * math.exp(lnm)
+                    if math.exp(-(1 - ip) * (w1 - wv) + lnm) >= u[3]:
+                        wv = w1
+                else:
+                    w1 = wi * math.exp(lnm)
+                    if math.exp(-ip * (w1 - wi) + lnm) >= u[3]:
+                        wi = w1
+        elif on:                            # jump: remove
+            d = lnw(wv, wi)
+            if math.exp((math.log(1.0) - d) + d) >= u[3]:
+                on, wv, wi = False, 1.0, 0.0
+        else:                               # jump: add
+            a = -math.log(1 - u[1]) / (1 - ip)
+            b = -math.log(1 - u[2]) / ip
+            d = lnw(a, b)
+            if math.exp((-math.log(1.0) + d) - d) >= u[3]:
+                on, wv, wi = True, a, b
+        if on:
+            non += 1
+            swv += wv
+            swi += wi
+    assert abs(non / n - 0.5) < 0.02, non / n
+    assert abs(swv / non - 2.0) < 0.1, swv / non
+    assert abs(swi / non - 2.0) < 0.1, swi / non
