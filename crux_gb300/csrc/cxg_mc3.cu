@@ -54,12 +54,16 @@ namespace cxg {
 
 enum {
     MV_BRLEN = 0, MV_NNI = 1, MV_RATES = 2, MV_ALPHA = 3, MV_FREQS = 4, MV_SPR = 5,
-    MV_ETBR = 6, MV_INVAR = 7, MV_GAMMAJ = 8, MV_FREQJ = 9, MV_INVARJ = 10, MV_INIT = 11
+    MV_ETBR = 6, MV_INVAR = 7, MV_GAMMAJ = 8, MV_FREQJ = 9, MV_INVARJ = 10,
+    MV_RATEJ = 11, MV_RATE1 = 12, MV_INIT = 13
 };
-constexpr int kMoves = 11;
+constexpr int kMoves = 13;
 
 struct Mc3Model {
+    // rates: the six exchangeabilities; those of one rate class (rclass, a
+    // restricted growth string with nrates classes) are equal.
     double rates[6], freqs[4], alpha;
+    int32_t rclass[6], nrates;
     double wvar, winvar;  // mixture weights of the variable and +I parts
     // 0: Gamma rates off (the reference's alpha = INFINITY: all variable
     // weight on the first category, rate 1); 0: equal base frequencies.
@@ -122,6 +126,7 @@ struct Mc3Dev {
     double brlen_lambda, brlen_prior, rate_conc, alpha_lambda, alpha_prior;
     double freq_conc, etbr_pext, invar_lambda, invar_prior;
     double gamma_jump_prior, freq_jump_prior, invar_jump_prior;
+    double rate_jump_prior, rate_lambda;
     uint32_t swap_stride;
     uint32_t *acc, *rej;  // [c][kMoves]
     uint32_t *nswap;      // [c]
@@ -230,6 +235,19 @@ __global__ void mc3_init_kernel(Mc3Dev d) {
 }
 
 // log density of Dirichlet(alpha) at x (both length n).
+// Partitions of the six exchangeabilities into k classes, k = 1..6
+// (Stirling numbers of the second kind S(6, k)).
+__constant__ double kStirling6[7] = {0.0, 1.0, 31.0, 90.0, 65.0, 15.0, 1.0};
+
+// Relabel rate classes in order of first appearance.
+__device__ void rgs_normalize(int32_t *rc) {
+    int32_t map[6] = {-1, -1, -1, -1, -1, -1}, next = 0;
+    for (int i = 0; i < 6; ++i) {
+        if (map[rc[i]] < 0) map[rc[i]] = next++;
+        rc[i] = map[rc[i]];
+    }
+}
+
 __device__ double ln_dirichlet(const double *alpha, const double *x, int n) {
     double s = 0.0, r = 0.0;
     for (int i = 0; i < n; ++i) {
@@ -409,6 +427,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             if ((t == MV_INVAR && (!d.invar || m0.winvar == 0.0)) ||
                 (t == MV_INVARJ && !d.invar))
                 t = MV_BRLEN;
+            if ((t == MV_RATES || t == MV_RATE1) && m0.nrates < 2) t = MV_BRLEN;
             if (t == MV_GAMMAJ && d.ncat < 2) t = MV_BRLEN;
             if (t == MV_FREQS && !m0.freqs_est) t = MV_BRLEN;
             pr.type = t;
@@ -660,6 +679,112 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 pr.model_changed = 1;
                 s_fin = FIN_WEIGHTS;
                 full = true;
+            } else if (t == MV_RATE1) {
+                // One class rate times m = exp(lambda (u - 1/2)), Exp(1)
+                // prior (ratePropose, Chain.pyx:267-319).
+                const int r = (int)philox_below(rng, (uint32_t)m0.nrates);
+                const double lnM = d.rate_lambda * (philox_u01(rng) - 0.5);
+                double c0 = 0.0;
+                for (int i = 0; i < 6; ++i)
+                    if (m0.rclass[i] == r) c0 = m0.rates[i];
+                const double c1 = c0 * exp(lnM);
+                m1 = m0;
+                for (int i = 0; i < 6; ++i)
+                    if (m0.rclass[i] == r) m1.rates[i] = c1;
+                pr.lnPrior = -(c1 - c0);
+                pr.lnHast = lnM;
+                pr.model_changed = 1;
+                s_fin = FIN_EIG;
+                full = true;
+            } else if (t == MV_RATEJ) {
+                // Rate classes merged or split (rateJumpPropose,
+                // rateMergePropose, rateSplitPropose, Chain.pyx:821-1075).
+                // Prior (as the reference's randomLik draws it): k classes
+                // with probability proportional to rateJumpPrior^-(k-1), a
+                // uniform partition among the S(6, k), class rates iid
+                // Exp(1).  Split: a uniform splittable class, a uniform
+                // bipartition of its n0 members into non-empty parts A and
+                // B, u uniform, rA = r0 n0 u / nA and rB = r0 n0 (1-u) / nB
+                // (the member-weighted mean stays r0; Jacobian
+                // n0^2 r0 / (nA nB)).  Merge: a uniform pair of classes to
+                // their member-weighted mean.  Split or merge is chosen
+                // with probability 1/2 where both exist.  The Hastings
+                // terms are this scheme's own: the reference pre-assigns
+                // two members to the parts and flips a coin for the rest,
+                // which is not the uniform bipartition its proposal
+                // ratio assumes.
+                const int k = m0.nrates;
+                int cnt[6] = {0, 0, 0, 0, 0, 0};
+                double cr[6];
+                for (int i = 0; i < 6; ++i) {
+                    cnt[m0.rclass[i]]++;
+                    cr[m0.rclass[i]] = m0.rates[i];
+                }
+                const bool merge =
+                    k == 6 ? true : (k == 1 ? false : philox_below(rng, 2) == 0);
+                const double lrjp = log(d.rate_jump_prior);
+                m1 = m0;
+                if (!merge) {
+                    int sp[6], ns = 0;
+                    for (int r = 0; r < k; ++r)
+                        if (cnt[r] > 1) sp[ns++] = r;
+                    const int c = sp[philox_below(rng, (uint32_t)ns)];
+                    const int n0 = cnt[c];
+                    const uint32_t z = 1u + philox_below(rng, (1u << n0) - 2u);
+                    const double u = philox_u01(rng), r0 = cr[c];
+                    int nA = 0, j = 0;
+                    for (int i = 0; i < 6; ++i)
+                        if (m0.rclass[i] == c) nA += (z >> j++) & 1u;
+                    const int nB = n0 - nA;
+                    const double rA = r0 * n0 * u / nA, rB = r0 * n0 * (1.0 - u) / nB;
+                    j = 0;
+                    for (int i = 0; i < 6; ++i)
+                        if (m0.rclass[i] == c) {
+                            if ((z >> j++) & 1u) {
+                                m1.rates[i] = rA;
+                            } else {
+                                m1.rclass[i] = k;
+                                m1.rates[i] = rB;
+                            }
+                        }
+                    rgs_normalize(m1.rclass);
+                    m1.nrates = k + 1;
+                    const double pS = k == 1 ? 1.0 : 0.5, pM = k + 1 == 6 ? 1.0 : 0.5;
+                    pr.lnPrior = -lrjp + log(kStirling6[k]) - log(kStirling6[k + 1]) +
+                                 (r0 - rA - rB);
+                    pr.lnHast = (log(pM) - log(0.5 * (k + 1) * k)) -
+                                (log(pS) - log((double)ns) - log((double)((1 << (n0 - 1)) - 1))) +
+                                log((double)n0 * n0 * r0 / ((double)nA * nB));
+                } else {
+                    const int x = (int)philox_below(rng, (uint32_t)k);
+                    int y = (int)philox_below(rng, (uint32_t)(k - 1));
+                    if (y >= x) ++y;
+                    const int a = x < y ? x : y, b = x < y ? y : x;
+                    const int nA = cnt[a], nB = cnt[b], n0 = nA + nB;
+                    const double rA = cr[a], rB = cr[b];
+                    const double r0 = (nA * rA + nB * rB) / n0;
+                    for (int i = 0; i < 6; ++i) {
+                        int r = m0.rclass[i];
+                        if (r == b) r = a;
+                        else if (r > b) --r;
+                        m1.rclass[i] = r;
+                        if (r == a) m1.rates[i] = r0;
+                    }
+                    m1.nrates = k - 1;
+                    int cnt1[6] = {0, 0, 0, 0, 0, 0}, ns1 = 0;
+                    for (int i = 0; i < 6; ++i) cnt1[m1.rclass[i]]++;
+                    for (int r = 0; r < k - 1; ++r) ns1 += cnt1[r] > 1;
+                    const double pS = k - 1 == 1 ? 1.0 : 0.5, pM = k == 6 ? 1.0 : 0.5;
+                    pr.lnPrior = lrjp + log(kStirling6[k]) - log(kStirling6[k - 1]) -
+                                 (r0 - rA - rB);
+                    pr.lnHast = (log(pS) - log((double)ns1) -
+                                 log((double)((1 << (n0 - 1)) - 1))) -
+                                (log(pM) - log(0.5 * k * (k - 1))) -
+                                log((double)n0 * n0 * r0 / ((double)nA * nB));
+                }
+                pr.model_changed = 1;
+                s_fin = FIN_EIG;
+                full = true;
             } else if (t == MV_GAMMAJ) {
                 // Gamma rates off or on (rateShapeInvJumpPropose,
                 // Chain.pyx:1346-1450).  Adding draws 1/alpha from its
@@ -733,23 +858,28 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 s_fin = FIN_EIG;
                 full = true;
             } else if (t == MV_RATES) {
-                // Exchangeabilities ~ Dirichlet(conc * r / sum r).
+                // Class rates ~ Dirichlet(conc * r / sum r) over the k rate
+                // classes, their sum kept (the rates' prior, iid Exp(1),
+                // is flat Dirichlet in r / sum r and independent of the
+                // sum).
+                const int k = m0.nrates;
                 double r0[6], r1[6], a0[6], a1[6], s0 = 0.0, s1 = 0.0;
-                for (int i = 0; i < 6; ++i) s0 += m0.rates[i];
-                for (int i = 0; i < 6; ++i) {
-                    r0[i] = m0.rates[i] / s0;
-                    a0[i] = d.rate_conc * r0[i];
-                    r1[i] = philox_gamma(rng, a0[i]);
-                    if (r1[i] < 1e-300) r1[i] = 1e-300;
-                    s1 += r1[i];
+                for (int i = 0; i < 6; ++i) r0[m0.rclass[i]] = m0.rates[i];
+                for (int r = 0; r < k; ++r) s0 += r0[r];
+                for (int r = 0; r < k; ++r) {
+                    r0[r] /= s0;
+                    a0[r] = d.rate_conc * r0[r];
+                    r1[r] = philox_gamma(rng, a0[r]);
+                    if (r1[r] < 1e-300) r1[r] = 1e-300;
+                    s1 += r1[r];
                 }
-                for (int i = 0; i < 6; ++i) {
-                    r1[i] /= s1;
-                    a1[i] = d.rate_conc * r1[i];
+                for (int r = 0; r < k; ++r) {
+                    r1[r] /= s1;
+                    a1[r] = d.rate_conc * r1[r];
                 }
                 m1 = m0;
-                for (int i = 0; i < 6; ++i) m1.rates[i] = r1[i] * 6.0;
-                pr.lnHast = ln_dirichlet(a1, r0, 6) - ln_dirichlet(a0, r1, 6);
+                for (int i = 0; i < 6; ++i) m1.rates[i] = r1[m0.rclass[i]] * s0;
+                pr.lnHast = ln_dirichlet(a1, r0, k) - ln_dirichlet(a0, r1, k);
                 pr.model_changed = 1;
                 s_fin = FIN_EIG;
                 full = true;
@@ -1305,6 +1435,28 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     d.gamma_jump_prior = cfg->gamma_jump_prior;
     d.freq_jump_prior = cfg->freq_jump_prior;
     d.invar_jump_prior = cfg->invar_jump_prior;
+    d.rate_jump_prior = cfg->rate_jump_prior;
+    d.rate_lambda = cfg->rate_lambda;
+    // Rate classes: a restricted growth string, equal rates within a class.
+    int nrates = 0;
+    for (int i = 0; i < 6; ++i) {
+        const int r = cfg->rclass[i];
+        if (r < 0 || r > nrates) {
+            mc3_free(h);
+            return fail(CXG_EINVAL, "cxgMc3Create: rclass is not a restricted growth string");
+        }
+        if (r == nrates) ++nrates;
+        for (int j = 0; j < i; ++j)
+            if (cfg->rclass[j] == r && cfg->rates[j] != cfg->rates[i]) {
+                mc3_free(h);
+                return fail(CXG_EINVAL,
+                            "cxgMc3Create: rates of one rate class differ");
+            }
+    }
+    if (mw[MV_RATEJ] > 0.0 && !(cfg->rate_jump_prior > 0.0)) {
+        mc3_free(h);
+        return fail(CXG_EINVAL, "cxgMc3Create: rate_jump_prior must be positive");
+    }
     if ((mw[MV_GAMMAJ] > 0.0 && !(cfg->gamma_jump_prior > 0.0)) ||
         (mw[MV_FREQJ] > 0.0 && !(cfg->freq_jump_prior > 0.0)) ||
         (mw[MV_INVARJ] > 0.0 && !(cfg->invar_jump_prior > 0.0))) {
@@ -1336,6 +1488,8 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     for (auto &m : models) {
         memset(&m, 0, sizeof(m));
         for (int i = 0; i < 6; ++i) m.rates[i] = cfg->rates[i];
+        for (int i = 0; i < 6; ++i) m.rclass[i] = cfg->rclass[i];
+        m.nrates = nrates;
         for (int i = 0; i < 4; ++i) m.freqs[i] = cfg->freqs[i];
         m.alpha = cfg->alpha;
         m.wvar = invar ? 1.0 - cfg->pinv : 1.0;

@@ -869,6 +869,9 @@ void mc3_loop(cxgServer *S) {
             c.gamma_jump_prior = 1.0;
             c.freq_jump_prior = 1.0;
             c.invar_jump_prior = 1.0;
+            for (int i = 0; i < 6; ++i) c.rclass[i] = i;
+            c.rate_jump_prior = 1.0;
+            c.rate_lambda = 2.0 * log(1.6);
             c.precision = S->cfg.precision;
             c.graph_gens = r.mc3_gens ? r.mc3_gens : 10;
             c.trace_cap = 1;

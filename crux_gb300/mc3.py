@@ -21,7 +21,7 @@ from .tree import Tree
 
 LAMBDA = 2.0 * math.log(1.6)
 MOVES = ("brlen", "nni", "rates", "alpha", "freqs", "spr", "etbr", "invar",
-         "gammajump", "freqjump", "invarjump")
+         "gammajump", "freqjump", "invarjump", "ratejump", "rate")
 
 
 class Mc3Config(ctypes.Structure):
@@ -41,7 +41,7 @@ class Mc3Config(ctypes.Structure):
         ("heat_delta", ctypes.c_double),
         ("swap_stride", ctypes.c_uint),
         ("seed", ctypes.c_ulonglong),
-        ("move_weight", ctypes.c_double * 11),
+        ("move_weight", ctypes.c_double * 13),
         ("brlen_lambda", ctypes.c_double),
         ("brlen_prior", ctypes.c_double),
         ("rate_conc", ctypes.c_double),
@@ -58,6 +58,9 @@ class Mc3Config(ctypes.Structure):
         ("graph_gens", ctypes.c_uint),
         ("trace_cap", ctypes.c_ulonglong),
         ("invar_jump_prior", ctypes.c_double),
+        ("rclass", ctypes.c_int * 6),
+        ("rate_jump_prior", ctypes.c_double),
+        ("rate_lambda", ctypes.c_double),
     ]
 
 
@@ -156,6 +159,7 @@ class Mc3:
                  brlen_prior=10.0, rate_conc=300.0, freq_conc=300.0,
                  etbr_pext=0.8, pinv=0.0, invar_lambda=LAMBDA, invar_prior=0.5,
                  gamma_jump_prior=1.0, freq_jump_prior=1.0, invar_jump_prior=1.0,
+                 rclass=(0, 1, 2, 3, 4, 5), rate_jump_prior=1.0, rate_lambda=LAMBDA,
                  alpha_lambda=LAMBDA,
                  alpha_prior=1.0, graph_gens=16, trace_cap=1 << 20, lib=None):
         self.lib = lib or _native.load()
@@ -204,6 +208,10 @@ class Mc3:
         c.gamma_jump_prior = gamma_jump_prior
         c.freq_jump_prior = freq_jump_prior
         c.invar_jump_prior = invar_jump_prior
+        for i in range(6):
+            c.rclass[i] = int(rclass[i])
+        c.rate_jump_prior = rate_jump_prior
+        c.rate_lambda = rate_lambda
         c.alpha_lambda = alpha_lambda
         c.alpha_prior = alpha_prior
         c.precision = 1 if precision == "fp32" else 0
@@ -245,8 +253,11 @@ class Mc3:
         self._check(self.lib.cxgMc3ChainWeights(self.h, i, ctypes.byref(wv),
                                                 ctypes.byref(wi)),
                     "cxgMc3ChainWeights")
+        # Rate classes: exchangeabilities of one class hold one value.
+        seen = {}
+        rclass = [seen.setdefault(float(x), len(seen)) for x in rates]
         return {"lnL": lnl.value, "heat": heat.value, "parent": par,
-                "len": ln, "rates": rates, "freqs": freqs,
+                "len": ln, "rates": rates, "rclass": rclass, "freqs": freqs,
                 "alpha": alpha.value, "wvar": wv.value, "winvar": wi.value}
 
     def stats(self):

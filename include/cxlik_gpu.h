@@ -320,10 +320,12 @@ typedef struct {
     double heat_delta;  /* chain i runs at heat 1/(1 + i*heat_delta) */
     unsigned swap_stride;
     unsigned long long seed;
-    double move_weight[11]; /* branch length, NNI, rates, alpha, base
-                               frequencies, SPR, eTBR, +I weights, Gamma
-                               on/off jump, equal/estimated frequency
-                               jump, +I off/on jump */
+    double move_weight[13]; /* branch length, NNI, rates (Dirichlet over
+                               the class rates), alpha, base frequencies,
+                               SPR, eTBR, +I weights, Gamma on/off jump,
+                               equal/estimated frequency jump, +I off/on
+                               jump, rate-class merge/split jump, one
+                               class rate's multiplier */
     double brlen_lambda, brlen_prior;
     double rate_conc;       /* Dirichlet concentration of rate moves */
     double freq_conc;       /* Dirichlet concentration of frequency moves */
@@ -345,6 +347,12 @@ typedef struct {
     unsigned long long trace_cap;  /* cold-chain lnL trace length */
     double invar_jump_prior; /* the reference's invarJumpPrior (1): prior
                                odds of +I off to on */
+    int rclass[6];          /* rate classes of the exchangeabilities, a
+                               restricted growth string ({0,1,2,3,4,5}:
+                               GTR); rates of one class must be equal */
+    double rate_jump_prior; /* the reference's rateJumpPrior (1): prior
+                               odds of k-1 to k rate classes */
+    double rate_lambda;     /* class-rate multiplier (2 ln 1.6) */
 } cxgMc3Config;
 typedef struct cxgMc3 cxgMc3;
 /* Build the chains and run generation 0 (a full evaluation). */
@@ -358,7 +366,7 @@ int cxgMc3Chain(cxgMc3 *mc3, unsigned chain, double *lnL, double *heat,
                 double *alpha);
 /* Mixture weights (wVar, wInvar) of one chain's current model. */
 int cxgMc3ChainWeights(cxgMc3 *mc3, unsigned chain, double *wvar, double *winvar);
-/* Accept/reject counts [chain][move] (11 moves, in move_weight order),
+/* Accept/reject counts [chain][move] (13 moves, in move_weight order),
  * swaps [chain], generation count. */
 int cxgMc3Stats(cxgMc3 *mc3, unsigned *accepts, unsigned *rejects,
                 unsigned *swaps, unsigned long long *gen);

@@ -346,3 +346,59 @@ def test_mc3_invar_jump_samples_its_prior(gpu):
     assert abs(np.mean(on) - 0.5) < 0.06, np.mean(on)
     assert abs(np.mean(wv) - 2.0) < 0.3, np.mean(wv)
     assert abs(np.mean(wi) - 2.0) < 0.3, np.mean(wi)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_mc3_rate_jump_chains_match_oracle(gpu, port, precision):
+    """Rate classes merged and split (rateJumpPropose, Chain.pyx:821-1075)
+    beside the class-rate multiplier (ratePropose, :267-319) and the
+    Dirichlet move over class rates: every chain's lnL is the oracle's for
+    its tree and exchangeabilities, and hot chains visit fewer classes."""
+    case = synth.Case(16, 100, 0.1, 48)
+    aln = case.alignment()
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=0.5,
+            ncat=4, nchains=4, heat_delta=3.0, seed=15,
+            moves={"brlen": 1.0, "ratejump": 2.0, "rate": 1.0, "rates": 0.5},
+            precision=precision, graph_gens=8)
+    ks = set()
+    for _ in range(10):
+        m.run(24)
+        check_chains(m, port, TOL[precision])
+        for i in range(4):
+            ks.add(max(m.chain_state(i)["rclass"]) + 1)
+    st = m.stats()
+    acc = st["accepts"].sum(axis=0)
+    assert acc[11] > 0 and acc[12] > 0
+    assert min(ks) < 6
+    m.close()
+
+
+def test_mc3_rate_jump_samples_its_prior(gpu):
+    """Without data the rate moves sample the prior the reference's
+    randomLik draws from (rateJumpPrior 1): every number of rate classes
+    1..6 equally often, every partition with two classes seen, and class
+    rates of mean 1 (Exp(1)).  A wrong Hastings ratio or prior term moves
+    the class counts."""
+    case, aln = _empty_alignment(6, 34)
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=None,
+            nchains=8, heat_delta=0.0, seed=7, precision="fp64", graph_gens=32,
+            moves={"ratejump": 1.0, "rate": 1.0, "rates": 1.0})
+    m.run(2000)
+    ks, parts, r0 = [], set(), []
+    for _ in range(1500):
+        m.run(32)
+        for i in range(8):
+            st = m.chain_state(i)
+            assert abs(st["lnL"]) < 1e-9
+            k = max(st["rclass"]) + 1
+            ks.append(k)
+            if k == 2:
+                parts.add(tuple(st["rclass"]))
+            r0.append(st["rates"][0])
+    m.close()
+    frac = np.bincount(ks, minlength=7)[1:] / len(ks)
+    assert np.all(np.abs(frac - 1.0 / 6.0) < 0.05), frac
+    assert len(parts) == 31
+    assert abs(np.mean(r0) - 1.0) < 0.15, np.mean(r0)
