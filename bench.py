@@ -843,7 +843,8 @@ def run_compact(args, dist):
     from crux_gb300.alignment import Alignment, CTMatrix
     gpu = _native.load()
     out = []
-    for ntaxa, nsites in COMPACT["shapes"]:
+    shapes = [args.compact_shape] if args.compact_shape else COMPACT["shapes"]
+    for ntaxa, nsites in shapes:
         case = synth.Case(ntaxa, nsites, COMPACT["mean_brlen"], COMPACT["seed"],
                           gap_frac=COMPACT["gap_frac"])
         raw = Alignment(CTMatrix(case.fasta))
@@ -869,7 +870,7 @@ def run_compact(args, dist):
         "steps": max(1, args.steps // 4), "warmup": max(args.warmup, 1),
         "ms_per_step": 1e3 * out[-1]["gpu_s"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-        "data": "synthetic (seeded)", "config": dict(COMPACT), "shapes": out,
+        "data": "synthetic (seeded)", "config": dict(COMPACT, shapes=shapes), "shapes": out,
     }
     print(json.dumps(line), flush=True)
     dist.close()
@@ -1053,6 +1054,8 @@ def main():
                     help="MC3 workloads: number of chains")
     ap.add_argument("--jobs", type=int, default=None,
                     help="batch256: number of jobs (default 256)")
+    ap.add_argument("--compact-shape", type=lambda v: [int(x) for x in v.split(",")],
+                    default=None, help="compact: one ntaxa,nsites shape only")
     ap.add_argument("--no-sub", action="store_true",
                     help="tree128: skip the MC3 and serving sub-records")
     ap.add_argument("--sub-mc3-gens", type=int, default=2000,

@@ -15,15 +15,15 @@
 //      key[chunk][site], read straight from the row-major input.
 //   2. LSD sort: for each chunk, last first, gather the chunk key of every
 //      column in the current order and stable-radix-sort (key, column
-//      index) pairs (cub::DeviceRadixSort, a CUDA toolkit primitive).
+//      index) pairs: 8-bit digits, each a histogram per tile, one scan of
+//      the (digit, tile) counts and a stable scatter (radix_hist,
+//      radix_scan, radix_scatter below).
 //   3. compact_flags: a column starts a pattern unless all its chunk keys
 //      equal those of the column before it (the packing is exact); a scan
 //      numbers the patterns.
 //   4. compact_scatter / compact_emit: the first column of each pattern
 //      represents it, frequencies add (integer atomics: exact), and the
 //      canonical rows and state masks of the patterns are written.
-#include <cub/device/device_radix_sort.cuh>
-#include <cub/device/device_scan.cuh>
 #include <cuda_runtime.h>
 #include <string.h>
 
@@ -35,15 +35,31 @@
 namespace cxg {
 namespace {
 
-// used[c] = 1 for every canonical code c that occurs.
+// used[c] = 1 for every canonical code c that occurs.  Rows are read 16
+// bytes a thread (the input is a device allocation, 16-byte aligned).
 __global__ void compact_used(const uint8_t *rows, size_t n, const uint8_t *canon,
                              uint32_t *used) {
     __shared__ uint32_t u[256];
-    for (unsigned i = threadIdx.x; i < 256; i += blockDim.x) u[i] = 0;
+    __shared__ uint8_t cs[256];
+    for (unsigned i = threadIdx.x; i < 256; i += blockDim.x) {
+        u[i] = 0;
+        cs[i] = canon[i];
+    }
     __syncthreads();
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+    const size_t n16 = n / 16;
+    const uint4 *r16 = reinterpret_cast<const uint4 *>(rows);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const uint4 v = __ldg(r16 + i);
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) u[cs[(w[q] >> (8 * b)) & 255u]] = 1;
+    }
+    for (size_t i = n16 * 16 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x)
-        u[canon[rows[i]]] = 1;
+        u[cs[rows[i]]] = 1;
     __syncthreads();
     for (unsigned i = threadIdx.x; i < 256; i += blockDim.x)
         if (u[i]) used[i] = 1;
@@ -127,6 +143,164 @@ __global__ void compact_emit(const uint8_t *rows, unsigned ntaxa, unsigned nsite
 
 size_t al256c(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// --- stable LSD radix sort of (64-bit key, 32-bit value) pairs ------------
+// One pass orders the pairs by the 8-bit digit (key >> shift) & 255, keeping
+// the order of equal digits.  The input is cut into tiles of kSortTile
+// pairs, one CTA each.
+constexpr unsigned kSortThreads = 256;
+constexpr unsigned kSortTile = 1024;
+
+// hist[d * ntiles + b] = pairs of tile b with digit d.
+__global__ void __launch_bounds__(kSortThreads)
+    radix_hist(const unsigned long long *key, unsigned n, unsigned shift, uint32_t *hist) {
+    __shared__ uint32_t h[256];
+    const unsigned t = threadIdx.x;
+    h[t] = 0;
+    __syncthreads();
+    const unsigned base = blockIdx.x * kSortTile;
+    const unsigned end = min(base + kSortTile, n);
+    for (unsigned i = base + t; i < end; i += kSortThreads)
+        atomicAdd(&h[(unsigned)(key[i] >> shift) & 255u], 1u);
+    __syncthreads();
+    hist[t * gridDim.x + blockIdx.x] = h[t];
+}
+
+// Exclusive scan of the NT values v[0..n) in place, one CTA of NT
+// threads: each thread sums a contiguous segment, the segment sums are
+// scanned in shared memory, then each thread writes its segment's
+// prefixes.  Returns the total (every thread).
+template <unsigned NT>
+__device__ uint32_t block_exclusive_scan(uint32_t *v, unsigned n) {
+    __shared__ uint32_t part[NT];
+    const unsigned t = threadIdx.x;
+    const unsigned seg = (n + NT - 1) / NT;
+    const unsigned a = min(t * seg, n), b = min(a + seg, n);
+    uint32_t sum = 0;
+    for (unsigned i = a; i < b; ++i) sum += v[i];
+    part[t] = sum;
+    __syncthreads();
+    for (unsigned off = 1; off < NT; off <<= 1) {
+        const uint32_t x = t >= off ? part[t - off] : 0u;
+        __syncthreads();
+        part[t] += x;
+        __syncthreads();
+    }
+    uint32_t run = part[t] - sum;  // exclusive prefix of this segment
+    for (unsigned i = a; i < b; ++i) {
+        const uint32_t x = v[i];
+        v[i] = run;
+        run += x;
+    }
+    const uint32_t total = part[NT - 1];
+    __syncthreads();  // part is reused by the next call
+    return total;
+}
+
+// Exclusive scan of v[0..n) in place, one CTA of 1024 threads.
+__global__ void __launch_bounds__(1024) radix_scan(uint32_t *v, unsigned n) {
+    block_exclusive_scan<1024>(v, n);
+}
+
+// Digit d's row of tile counts, hist[d * ntiles ..], scanned in place by
+// CTA d; tot[d] = the digit's count.
+__global__ void __launch_bounds__(kSortThreads)
+    radix_rowscan(uint32_t *hist, unsigned ntiles, uint32_t *tot) {
+    const uint32_t t = block_exclusive_scan<kSortThreads>(hist + (size_t)blockIdx.x * ntiles,
+                                                          ntiles);
+    if (threadIdx.x == 0) tot[blockIdx.x] = t;
+}
+
+// Stable scatter of one pass.  A tile is read in rounds of kSortThreads
+// pairs, pair r + t to thread t, so lower threads hold earlier pairs.  A
+// pair's place is its digit's next free slot for this tile (offs: the
+// digit's base, an exclusive scan of the digit counts tot, plus its
+// row-scanned tile count), plus the pairs with its digit in lower warps of
+// the round (wcnt) and in lower lanes of its warp (__match_any_sync).
+__global__ void __launch_bounds__(kSortThreads)
+    radix_scatter(const unsigned long long *kin, const uint32_t *vin, unsigned n,
+                  unsigned shift, const uint32_t *hist, const uint32_t *tot,
+                  unsigned long long *kout, uint32_t *vout) {
+    constexpr unsigned W = kSortThreads / 32;
+    __shared__ uint32_t offs[256];
+    __shared__ uint32_t wcnt[W][256];
+    const unsigned t = threadIdx.x, w = t / 32, lane = t % 32;
+    offs[t] = tot[t];
+    __syncthreads();
+    block_exclusive_scan<kSortThreads>(offs, 256);
+    offs[t] += hist[t * gridDim.x + blockIdx.x];
+    for (unsigned j = 0; j < W; ++j) wcnt[j][t] = 0;
+    __syncthreads();
+    const unsigned base = blockIdx.x * kSortTile;
+    const unsigned end = min(base + kSortTile, n);
+    for (unsigned r = base; r < end; r += kSortThreads) {
+        const unsigned i = r + t;
+        const bool active = i < end;
+        const unsigned long long k = active ? kin[i] : 0ull;
+        const uint32_t v = active ? vin[i] : 0u;
+        // Inactive lanes get a digit no other lane has.
+        const unsigned d = active ? ((unsigned)(k >> shift) & 255u) : 256u + lane;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const unsigned below = __popc(peers & ((1u << lane) - 1u));
+        const bool leader = below == 0;
+        if (active && leader) wcnt[w][d] = __popc(peers);
+        __syncthreads();
+        if (active) {
+            unsigned pos = offs[d] + below;
+            for (unsigned j = 0; j < w; ++j) pos += wcnt[j][d];
+            kout[pos] = k;
+            vout[pos] = v;
+        }
+        __syncthreads();
+        if (active && leader) {
+            atomicAdd(&offs[d], __popc(peers));
+            wcnt[w][d] = 0;
+        }
+        __syncthreads();
+    }
+}
+
+// Inclusive scan of n values (in and out may not alias), by tiles of 1024:
+// tile sums, an exclusive scan of those (radix_scan), then each tile's
+// inclusive scan plus its offset.
+__global__ void __launch_bounds__(1024)
+    tile_sums(const uint32_t *in, unsigned n, uint32_t *sums) {
+    __shared__ uint32_t ws[32];
+    const unsigned i = blockIdx.x * 1024 + threadIdx.x;
+    uint32_t x = i < n ? in[i] : 0u;
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x / 32] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        x = ws[threadIdx.x];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (threadIdx.x == 0) sums[blockIdx.x] = x;
+    }
+}
+
+__global__ void __launch_bounds__(1024)
+    tile_scan(const uint32_t *in, unsigned n, const uint32_t *offs, uint32_t *out) {
+    __shared__ uint32_t ws[32];
+    const unsigned lane = threadIdx.x & 31, w = threadIdx.x / 32;
+    const unsigned i = blockIdx.x * 1024 + threadIdx.x;
+    uint32_t x = i < n ? in[i] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (unsigned)o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t y = ws[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t z = __shfl_up_sync(0xffffffffu, y, o);
+            if (lane >= (unsigned)o) y += z;
+        }
+        ws[lane] = y;
+    }
+    __syncthreads();
+    if (i < n) out[i] = x + (w ? ws[w - 1] : 0u) + offs[blockIdx.x];
+}
+
 }  // namespace
 
 // Rank table over the canonical codes that occur (used[code] != 0), in
@@ -151,15 +325,11 @@ static void compact_tables(const uint8_t *canon, const uint32_t *used, uint8_t *
 size_t compact_work_bytes(unsigned ntaxa, unsigned nsites) {
     // Chunk keys for the widest ranks (8 bits: 8 characters a key).
     const size_t max_chunks = (ntaxa + 7) / 8;
-    size_t cub_bytes = 0, scan_bytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, (const unsigned long long *)nullptr,
-                                    (unsigned long long *)nullptr, (const uint32_t *)nullptr,
-                                    (uint32_t *)nullptr, (int)nsites);
-    cub::DeviceScan::InclusiveSum(nullptr, scan_bytes, (const uint32_t *)nullptr,
-                                  (uint32_t *)nullptr, (int)nsites);
     const size_t n = nsites;
+    const size_t ntiles = (n + kSortTile - 1) / kSortTile;
+    const size_t hist = ntiles * 256 * 4 + 1024, scan = ((n + 1023) / 1024) * 4;
     return 2048 + al256c(max_chunks * n * 8) + 2 * al256c(n * 8) + 4 * al256c(n * 4) +
-           al256c(cub_bytes > scan_bytes ? cub_bytes : scan_bytes);
+           al256c(hist > scan ? hist : scan);
 }
 
 int compact_device(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
@@ -199,8 +369,9 @@ int compact_device(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
     uint32_t *i1 = (uint32_t *)take(n * 4);
     uint32_t *flag = (uint32_t *)take(n * 4);
     uint32_t *gid = (uint32_t *)take(n * 4);
-    size_t cub_bytes = work_bytes - (size_t)(p - static_cast<char *>(work));
-    void *cub_tmp = p;
+    const unsigned ntiles = (unsigned)((n + kSortTile - 1) / kSortTile);
+    uint32_t *hist = (uint32_t *)p;  // [256][ntiles] digit counts, or tile sums
+    uint32_t *dtot = hist + (size_t)ntiles * 256;  // [256] counts of each digit
 
     const unsigned nb = (unsigned)((n + 255) / 256);
     compact_keys<<<dim3(nb, nchunks), 256, 0, s>>>(rows, ntaxa, nsites, rank, bits, cpk, keys);
@@ -209,20 +380,33 @@ int compact_device(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
     std::vector<uint32_t> iota(n);
     for (size_t i = 0; i < n; ++i) iota[i] = (uint32_t)i;
     CXG_CUDA(cudaMemcpyAsync(i0, iota.data(), n * 4, cudaMemcpyHostToDevice, s));
+    const unsigned kbits = cpk * bits;
     for (int c = (int)nchunks - 1; c >= 0; --c) {
         compact_gather<<<nb, 256, 0, s>>>(keys + (size_t)c * n, i0, (unsigned)n, k0);
         CXG_CHECK_LAUNCH("compact_gather");
-        cudaError_t e = cub::DeviceRadixSort::SortPairs(cub_tmp, cub_bytes, k0, k1, i0, i1,
-                                                        (int)n, 0, (int)(cpk * bits), s);
-        if (e != cudaSuccess) return cuda_fail(e, "compaction radix sort");
-        uint32_t *t = i0;
-        i0 = i1;
-        i1 = t;
+        // Stable passes over the key's 8-bit digits, least significant first.
+        for (unsigned shift = 0; shift < kbits; shift += 8) {
+            radix_hist<<<ntiles, kSortThreads, 0, s>>>(k0, (unsigned)n, shift, hist);
+            radix_rowscan<<<256, kSortThreads, 0, s>>>(hist, ntiles, dtot);
+            radix_scatter<<<ntiles, kSortThreads, 0, s>>>(k0, i0, (unsigned)n, shift, hist,
+                                                          dtot, k1, i1);
+            CXG_CHECK_LAUNCH("compaction radix sort");
+            unsigned long long *tk = k0;
+            k0 = k1;
+            k1 = tk;
+            uint32_t *ti = i0;
+            i0 = i1;
+            i1 = ti;
+        }
     }
     compact_flags<<<nb, 256, 0, s>>>(keys, nchunks, i0, (unsigned)n, flag);
     CXG_CHECK_LAUNCH("compact_flags");
-    cudaError_t e = cub::DeviceScan::InclusiveSum(cub_tmp, cub_bytes, flag, gid, (int)n, s);
-    if (e != cudaSuccess) return cuda_fail(e, "compaction scan");
+    // gid = inclusive scan of the flags.
+    const unsigned nt = (unsigned)((n + 1023) / 1024);
+    tile_sums<<<nt, 1024, 0, s>>>(flag, (unsigned)n, hist);
+    radix_scan<<<1, 1024, 0, s>>>(hist, nt);
+    tile_scan<<<nt, 1024, 0, s>>>(flag, (unsigned)n, hist, gid);
+    CXG_CHECK_LAUNCH("compaction scan");
     CXG_CUDA(cudaMemcpyAsync(npat_dev, gid + n - 1, 4, cudaMemcpyDeviceToDevice, s));
     // rep reuses the key buffer (n words); frequencies start at zero.
     uint32_t *rep = reinterpret_cast<uint32_t *>(k0);

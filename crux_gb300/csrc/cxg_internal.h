@@ -207,7 +207,7 @@ size_t plan_smem_bytes(int precision, unsigned kact, unsigned tile, unsigned nsl
                        unsigned ring, unsigned rstride, unsigned lmax,
                        unsigned nleaf);
 // Pattern compression on the device (cxg_compact.cu): scratch bytes, and
-// the compaction of rows [ntaxa][nsites] (device) into rows_out / masks
+// the compaction of rows [ntaxa][nsites] (device, 16-byte aligned) into rows_out / masks
 // (row strides rstride / mstride; mask pad patterns up to mstride get
 // any_mask), freq_out and *npat_dev (device).  canon_host is the host copy
 // of the device table canon.  Waits for the stream once.
