@@ -447,11 +447,12 @@ def run_ours(args, dist):
             p["plan"].close()
         if not args.no_sub:
             # Bounded MC3 and serving records on the same run (each under
-            # its own clock sampler), with the tree's tuned walker shapes.
+            # its own clock sampler).  MC3 tunes its walker shape on its own
+            # generations; the server takes the tree's tuned shapes.
             shapes = {"fp32": res["fp32"]["shape"], "fp64": res["fp64"]["shape"]}
             line["mc3"] = mc3_measure(
                 MC3["mc3"], args.sub_mc3_gens, args.sub_mc3_gens64,
-                shapes=shapes, oracle=None if args.no_cpu else lib,
+                args=args, oracle=None if args.no_cpu else lib,
                 check_every=1000, seq_gens=args.sub_mc3_gens64)
             line["serve"] = serve_measure(args.sub_serve_datasets,
                                           args.sub_serve_rates, 2.0,
@@ -592,7 +593,8 @@ def mc3_measure(w, gens, gens64, shapes=None, args=None, oracle=None,
     no check).  Over the first `seq_gens` generations both runs must take
     the same accept/reject sequence: their per-chain, per-move accept and
     reject counts are equal and their cold-chain traces agree to 1e-6.
-    `shapes`: walker shape per precision (else autotuned with `args`)."""
+    `shapes`: walker shape per precision (else ``args.shape``, else tuned
+    on a few generations of each candidate)."""
     import numpy as np
     from crux_gb300 import _native, synth, tune
     from crux_gb300.mc3 import Mc3
@@ -605,20 +607,28 @@ def mc3_measure(w, gens, gens64, shapes=None, args=None, oracle=None,
     for prec, ngen in (("fp32", gens), ("fp64", gens64)):
         if ngen <= 0:
             continue
+        def make():
+            return Mc3(case.tree(aln.taxaMap), aln, case.params["rates"],
+                       case.params["freqs"], alpha=0.5, ncat=4,
+                       nchains=w["nchains"], heat_delta=w["heat_delta"],
+                       seed=w["seed"], moves=w["moves"], precision=prec,
+                       graph_gens=16)
+
         if shapes and prec in shapes:
             sh = shapes[prec]
             tune.set_shape(gpu, sh["tile"], sh["tpp"], sh["ppt"], sh["budget"])
             shape = dict(sh, lanes=1, source=sh.get("source", "given"))
+        elif args is not None and args.shape:
+            shape = autotune(gpu, prec, args)
         else:
-            lk = case.lik(lib=gpu, precision=prec, alignment=aln)
-            lk.prepare_plan()
-            shape = autotune(gpu, prec, args, lik=lk, lanes=False)
-            del lk
-        m = Mc3(case.tree(aln.taxaMap), aln, case.params["rates"],
-                case.params["freqs"], alpha=0.5, ncat=4,
-                nchains=w["nchains"], heat_delta=w["heat_delta"],
-                seed=w["seed"], moves=w["moves"], precision=prec,
-                graph_gens=16)
+            # Tuned on the MC3 run itself (dirty-path walks, not a full
+            # plan): a few generations per candidate.
+            r = tune.tune_mc3(gpu, make, prec, gens=32 if prec == "fp32" else 8,
+                              warm=8 if prec == "fp32" else 2)
+            top = sorted(r["table"], key=lambda x: x["ms"])
+            shape = dict(r["best"], source="autotuned on MC3 generations",
+                         candidates=len(r["table"]), worst_ms=top[-1]["ms"])
+        m = make()
         # The same untimed warm-up in both precisions, so that their
         # generations stay aligned for the accept/reject comparison.
         m.run(MC3_WARM)

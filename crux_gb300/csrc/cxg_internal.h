@@ -72,6 +72,52 @@ struct RecHead {
 // root) and is not kept as a cache, so the walker skips its HBM write.
 enum : uint32_t { REC_NO_HBM = 1 };
 
+// RecHead.flags bits 8-10: the kind of a two-child op of an FP32 plan run
+// one op at a time, one thread per pattern, named by where its children
+// come from (F: the previous op's result, still in registers; L: a leaf;
+// I: an internal CL in HBM or a stack slot).  The walker then runs
+// straight-line code for that kind.  Bit 12 gives the record index of
+// child A (the first letter); child B is the other.  A product of two
+// messages and a sum of two integer exponents are the same in either
+// order, so the kind's A/B order gives the bits of the record order.
+// OPK_GENERIC (0) runs the general per-child loop.
+enum : uint32_t {
+    OPK_GENERIC = 0,
+    OPK_FL = 1,
+    OPK_FI = 2,
+    OPK_LL = 3,
+    OPK_IL = 4,
+    OPK_II = 5
+};
+constexpr uint32_t kOpKindShift = 8;
+constexpr uint32_t kOpKindA = 1u << 12;
+
+// RecHead.flags bits of a two-child op whose children are of classes a and
+// b (0: L, 1: I, 2: F).  A is the child of the higher class.
+__host__ __device__ inline uint32_t op_kind_of_classes(int a, int b) {
+    if (a == 2 && b == 2) return 0;  // not a plan
+    const int hi = a > b ? a : b, lo = a > b ? b : a;
+    const uint32_t ia = (a >= b) ? 0u : kOpKindA;
+    uint32_t kind = OPK_GENERIC;
+    if (hi == 2) kind = lo == 0 ? OPK_FL : OPK_FI;
+    else if (hi == 1) kind = lo == 0 ? OPK_IL : OPK_II;
+    else kind = OPK_LL;
+    return (kind << kOpKindShift) | ia;
+}
+
+// The same for children with sources src0 / src1 and HBM rows data0 /
+// data1, in an op run right after the op whose result is `prev` (null for
+// the first op): a child is F when it is that result, which the walker
+// still holds in registers.
+__host__ __device__ inline uint32_t op_kind_flags(uint32_t src0, const void *data0,
+                                                  uint32_t src1, const void *data1,
+                                                  const void *prev) {
+    auto cls = [&](uint32_t src, const void *d) {
+        return src == SRC_LEAF ? 0 : (prev != nullptr && d == prev ? 2 : 1);
+    };
+    return op_kind_of_classes(cls(src0, data0), cls(src1, data1));
+}
+
 // One child of an op.  `data`/`scaler` address the HBM copy (SRC_GLOBAL);
 // for SRC_LEAF `data` is the leaf's mask array [ppad] (one uint8 state
 // mask per pattern) and `idx` its staged row when the job stages leaves;

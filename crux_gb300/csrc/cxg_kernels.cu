@@ -396,6 +396,125 @@ __device__ __forceinline__ X group_max(X x) {
     return x;
 }
 
+// --- FP32 two-child ops by kind (one thread per pattern) --------------------
+// Row r of a P matrix against the four states x of one component, in the
+// order of the general path (a product, then three fused adds).
+__device__ __forceinline__ float pdot(const float4 r, const float *x) {
+    float v = r.x * x[0];
+    v = fmaf(r.y, x[1], v);
+    v = fmaf(r.z, x[2], v);
+    v = fmaf(r.w, x[3], v);
+    return v;
+}
+
+// An internal child's rows and exponent: from its stack slot, or from HBM
+// through L2 (the rows were written by this same thread earlier in the
+// walk, or by an earlier launch).
+template <int KT>
+__device__ __forceinline__ int load_internal(const RecChild &c, const float4 *slots,
+                                             const int *slot_sc, unsigned tile,
+                                             unsigned pl, unsigned p, size_t ppad,
+                                             float *x) {
+    if (c.src == SRC_SLOT) {
+        const float4 *s = slots + (size_t)c.idx * KT * tile + pl;
+#pragma unroll
+        for (int k = 0; k < KT; ++k) unpack(s[(size_t)k * tile], x + 4 * k);
+        return slot_sc[(size_t)c.idx * tile + pl];
+    }
+    const float4 *g = static_cast<const float4 *>(c.data) + p;
+#pragma unroll
+    for (int k = 0; k < KT; ++k) unpack(__ldcg(g + (size_t)k * ppad), x + 4 * k);
+    return __ldcg(static_cast<const int *>(c.scaler) + p);
+}
+
+// One two-child op of kind `kind` (OPK_*): acc becomes the product of the
+// two children's messages and the return value the sum of their
+// exponents.  acc holds the previous op's result on entry (child A of the
+// F kinds) and prev_lns its exponent.  `ia` is child A's record index; a
+// streamed leaf's row is its rank among the op's leaf children.
+template <int KT, bool STAGED>
+__device__ __forceinline__ int op2_kind(uint32_t kind, const unsigned char *rec,
+                                        const RecChild *kids, unsigned ia, float *acc,
+                                        int prev_lns, const uint8_t *masks,
+                                        const uint8_t *lrow, const float4 *slots,
+                                        const int *slot_sc, unsigned tile, unsigned pl,
+                                        unsigned p, size_t ppad) {
+    const RecChild &cA = kids[ia];
+    const RecChild &cB = kids[ia ^ 1u];
+    const float4 *PA = reinterpret_cast<const float4 *>(rec + cA.off);
+    const float4 *PB = reinterpret_cast<const float4 *>(rec + cB.off);
+    auto mask = [&](const RecChild &c, unsigned rank) -> unsigned {
+        return STAGED ? masks[(size_t)c.idx * tile + pl] : lrow[(size_t)rank * tile + pl];
+    };
+    // acc[k] = a * b, one component (states 0..3) at a time.
+    auto mul4 = [](float *y, const float *a, const float4 b) {
+        y[0] = a[0] * b.x;
+        y[1] = a[1] * b.y;
+        y[2] = a[2] * b.z;
+        y[3] = a[3] * b.w;
+    };
+    switch (kind) {
+    case OPK_LL: {
+        const unsigned mA = mask(cA, ia), mB = mask(cB, ia ^ 1u);
+#pragma unroll
+        for (int k = 0; k < KT; ++k) {
+            const float4 a = PA[k * 16 + mA];
+            const float ax[4] = {a.x, a.y, a.z, a.w};
+            mul4(acc + 4 * k, ax, PB[k * 16 + mB]);
+        }
+        return 0;
+    }
+    case OPK_FL: {
+        const unsigned mB = mask(cB, 0);
+#pragma unroll
+        for (int k = 0; k < KT; ++k) {
+            float m[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) m[i] = pdot(PA[k * 4 + i], acc + 4 * k);
+            mul4(acc + 4 * k, m, PB[k * 16 + mB]);
+        }
+        return prev_lns;
+    }
+    case OPK_IL: {
+        float xA[KT * 4];
+        const int lA = load_internal<KT>(cA, slots, slot_sc, tile, pl, p, ppad, xA);
+        const unsigned mB = mask(cB, 0);
+#pragma unroll
+        for (int k = 0; k < KT; ++k) {
+            float m[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) m[i] = pdot(PA[k * 4 + i], xA + 4 * k);
+            mul4(acc + 4 * k, m, PB[k * 16 + mB]);
+        }
+        return lA;
+    }
+    case OPK_FI: {
+        float xB[KT * 4];
+        const int lB = load_internal<KT>(cB, slots, slot_sc, tile, pl, p, ppad, xB);
+#pragma unroll
+        for (int k = 0; k < KT; ++k) {
+            float m[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) m[i] = pdot(PA[k * 4 + i], acc + 4 * k);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[4 * k + i] = m[i] * pdot(PB[k * 4 + i], xB + 4 * k);
+        }
+        return prev_lns + lB;
+    }
+    default: {  // OPK_II
+        float xA[KT * 4], xB[KT * 4];
+        const int lA = load_internal<KT>(cA, slots, slot_sc, tile, pl, p, ppad, xA);
+        const int lB = load_internal<KT>(cB, slots, slot_sc, tile, pl, p, ppad, xB);
+#pragma unroll
+        for (int k = 0; k < KT; ++k)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                acc[4 * k + i] = pdot(PA[k * 4 + i], xA + 4 * k) * pdot(PB[k * 4 + i], xB + 4 * k);
+        return lA + lB;
+    }
+    }
+}
+
 // Walk every op of job `a` for tile `tile_idx`, aggregate the root and
 // reduce.  G consecutive threads share a pattern, each holding KT of its
 // KT*G components; with G = 1 one thread owns a pattern.  Every G gives the
@@ -601,9 +720,25 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             }
             if (sizeof(T) == 8) sc = fmax(sc, tree_max<KT * 4>(msg));
         };
+        // A two-child FP32 op whose kind the host set runs straight-line
+        // code for its kind (the general path below gives the same bits).
+        uint32_t kind = OPK_GENERIC;
+        if constexpr (sizeof(T) == 4 && G == 1 && L == 1) {
+            const uint32_t fl = hd->flags;
+            kind = (fl >> kOpKindShift) & 7u;
+            // A walk that starts inside a plan (one launch per node) holds
+            // no previous result: its first op runs the general path, which
+            // reads that child from where its record says.
+            if ((kind == OPK_FL || kind == OPK_FI) && o == 0) kind = OPK_GENERIC;
+            if (kind != OPK_GENERIC)
+                lns = op2_kind<KT, STAGED>(kind, rec, kids, (fl & kOpKindA) ? 1u : 0u, acc,
+                                           prev_lns, masks, lrow, slots, slot_sc, tile, pl,
+                                           p, ppad);
+        }
         // (The FP64 form keeps the loop: both children's rows in registers
         // at once cost it occupancy, and it is bound by the FP64 pipe.)
-        if (sizeof(T) == 4 && nchild == 2) {
+        if (kind != OPK_GENERIC) {
+        } else if (sizeof(T) == 4 && !(G == 1 && L == 1) && nchild == 2) {
             const RecChild c0 = kids[0], c1 = kids[1];
             In in0, in1;
             const bool f0 = L == 1 && prev_data != nullptr && c0.src != SRC_LEAF &&

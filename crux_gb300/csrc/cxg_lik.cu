@@ -724,6 +724,11 @@ static int translate(State &S, CxtLik *lik, int prec, Plan &P,
         hd.scaler = ops[o].scaler;
         hd.nchild = ops[o].nchild;
         hd.slot = ops[o].slot;
+        if (prec == CXG_FP32 && lanes == 1 && ops[o].nchild == 2) {
+            const HostChild &k0 = kids[ops[o].child0], &k1 = kids[ops[o].child0 + 1];
+            hd.flags |= op_kind_flags(k0.src, k0.data, k1.src, k1.data,
+                                      pos > 0 ? ops[order[pos - 1]].data : nullptr);
+        }
         memcpy(r, &hd, sizeof(hd));
         size_t area = sizeof(RecHead) + ops[o].nchild * sizeof(RecChild);
         for (uint32_t ci = 0; ci < ops[o].nchild; ++ci) {

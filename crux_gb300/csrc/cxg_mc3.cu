@@ -1073,7 +1073,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         hd.slot = op_slot[o];
         hd.flags = 0;
         hd.next_bytes = 0;
-        memcpy(r, &hd, sizeof(hd));
+        int kcls[3] = {1, 1, 1};
         unsigned ci = 0, nkid = kid0[o], nl = 0;
         size_t area = sizeof(RecHead) + nch * sizeof(RecChild);
         const uint8_t **lr = lrows + (size_t)o * 3;
@@ -1104,6 +1104,9 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             }
             ch.off = (uint32_t)area;
             memcpy(r + sizeof(RecHead) + ci * sizeof(RecChild), &ch, sizeof(ch));
+            // Class for the op kind: dirty node o - 1 is F (its result is
+            // still in the walker's registers).
+            kcls[ci] = u < (int)N ? 0 : (o > 0 && u == dirty[o - 1] ? 2 : 1);
             klen[nkid] = len[u];
             kdst[nkid] = (size_t)o * d.rstride + area;
             area += child_area_bytes((int)d.prec, d.kact, u < (int)N);
@@ -1111,6 +1114,8 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             ++ci;
         }
         for (unsigned j = nl; j < 3; ++j) lr[j] = nullptr;
+        if (d.prec == CXG_FP32 && nch == 2) hd.flags |= op_kind_of_classes(kcls[0], kcls[1]);
+        memcpy(r, &hd, sizeof(hd));
     }
     // The tree (moved) and the dirty list back to HBM; an eTBR result goes
     // to the spare tree buffer, which the accept kernel makes current.

@@ -334,6 +334,13 @@ extern "C" int cxgLikExecuteNoAlloc(const CxtLik *lik, int precision,
             hd.slot = sl;
             if ((unsigned)sl + 1 > used) used = (unsigned)sl + 1;
         }
+        if (prec == CXG_FP32 && n == 2) {
+            RecChild k0, k1;
+            memcpy(&k0, r + sizeof(RecHead), sizeof(k0));
+            memcpy(&k1, r + sizeof(RecHead) + sizeof(RecChild), sizeof(k1));
+            hd.flags |= op_kind_flags(k0.src, k0.data, k1.src, k1.data,
+                                      o > 0 ? op_parent[o - 1]->cLMat : nullptr);
+        }
         memcpy(r, &hd, sizeof(hd));
         ++o;
         s += n;

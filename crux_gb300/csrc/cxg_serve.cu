@@ -499,6 +499,7 @@ int prepare_job(cxgServer *S, SrvJob &J) {
         }
         memcpy(rr, &hd, sizeof(hd));
         size_t area = sizeof(RecHead) + nch * sizeof(RecChild);
+        int kcls[3] = {1, 1, 1};
         for (unsigned ci = 0; ci < nch; ++ci) {
             const HostKid &k = P.kids[o][ci];
             RecChild ch;
@@ -521,10 +522,17 @@ int prepare_job(cxgServer *S, SrvJob &J) {
                 ch.scaler = sc_of(k.idx);
             }
             memcpy(rr + sizeof(RecHead) + ci * sizeof(RecChild), &ch, sizeof(ch));
+            // Class for the op kind: the previous op's node is F (its result
+            // is still in the walker's registers).
+            kcls[ci] = k.src == SRC_LEAF ? 0 : (o > 0 && k.node == P.order[o - 1] ? 2 : 1);
             hlen[nk] = J.rq->len[k.node];
             hdst[nk] = (size_t)o * rstride + area;
             area += child_area_bytes(prec, K, k.src == SRC_LEAF);
             ++nk;
+        }
+        if (prec == CXG_FP32 && nch == 2) {
+            hd.flags |= op_kind_of_classes(kcls[0], kcls[1]);
+            memcpy(rr, &hd, sizeof(hd));
         }
     }
     SrvModel hmod;

@@ -134,6 +134,27 @@ def tune_plan(lik, precision="fp32", iters=20, shapes=None):
     return _sweep(lik.lib, shapes, measure)
 
 
+def tune_mc3(lib, make, precision="fp32", kact=4, gens=32, warm=16, shapes=None):
+    """Tune on an MC3 run.  ``make()`` builds an ``Mc3`` with the shape
+    that is set; each candidate runs `warm` generations, then `gens` more,
+    and its time is their device time (``cxgMc3Run``) per generation.  MC3
+    walks short dirty paths over many (chain, tile) items, so per-tile
+    costs weigh more there than on a full plan, and the two can prefer
+    different tiles."""
+    shapes = shapes or candidates(precision, kact, tpps=(1,), ppts=(1,),
+                                  budgets=(0, 24 << 10), lanes=(1,))
+
+    def measure():
+        m = make()
+        try:
+            m.run(warm)
+            return 1e3 * m.run(gens) / gens
+        finally:
+            m.close()
+
+    return _sweep(lib, shapes, measure)
+
+
 def tune_batch(liks, precision="fp32", iters=5, shapes=None):
     """Tune on a batch of planned Liks (one persistent launch); the time is
     the walker's mean over `iters` graph replays."""
