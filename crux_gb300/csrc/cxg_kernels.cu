@@ -427,26 +427,29 @@ __device__ __forceinline__ int load_internal(const RecChild &c, const float4 *sl
     return __ldcg(static_cast<const int *>(c.scaler) + p);
 }
 
-// One two-child op of kind `kind` (OPK_*): acc becomes the product of the
-// two children's messages and the return value the sum of their
+// One two-child op of kind `kind` (OPK_*) for the NP patterns pl[h] (in
+// the tile) / p[h] (in the CL buffers) a thread owns: acc[h] becomes the
+// product of the two children's messages and lns[h] the sum of their
 // exponents.  acc holds the previous op's result on entry (child A of the
-// F kinds) and prev_lns its exponent.  `ia` is child A's record index; a
-// streamed leaf's row is its rank among the op's leaf children.
-template <int KT, bool STAGED>
-__device__ __forceinline__ int op2_kind(uint32_t kind, const unsigned char *rec,
-                                        const RecChild *kids, unsigned ia, float *acc,
-                                        int prev_lns, const uint8_t *masks,
-                                        const uint8_t *lrow, const float4 *slots,
-                                        const int *slot_sc, unsigned tile, unsigned pl,
-                                        unsigned p, size_t ppad) {
+// F kinds), with its exponents in lns.  `ia` is child A's record index; a
+// streamed leaf's row is its rank among the op's leaf children.  Each P
+// row is read from shared memory once for all NP patterns.
+template <int KT, bool STAGED, int NP>
+__device__ __forceinline__ void op2_kind(uint32_t kind, const unsigned char *rec,
+                                         const RecChild *kids, unsigned ia,
+                                         float (&acc)[NP][KT * 4], int (&lns)[NP],
+                                         const uint8_t *masks, const uint8_t *lrow,
+                                         const float4 *slots, const int *slot_sc,
+                                         unsigned tile, const unsigned (&pl)[NP],
+                                         const unsigned (&p)[NP], size_t ppad) {
     const RecChild &cA = kids[ia];
     const RecChild &cB = kids[ia ^ 1u];
     const float4 *PA = reinterpret_cast<const float4 *>(rec + cA.off);
     const float4 *PB = reinterpret_cast<const float4 *>(rec + cB.off);
-    auto mask = [&](const RecChild &c, unsigned rank) -> unsigned {
-        return STAGED ? masks[(size_t)c.idx * tile + pl] : lrow[(size_t)rank * tile + pl];
+    auto mask = [&](const RecChild &c, unsigned rank, unsigned q) -> unsigned {
+        return STAGED ? masks[(size_t)c.idx * tile + q] : lrow[(size_t)rank * tile + q];
     };
-    // acc[k] = a * b, one component (states 0..3) at a time.
+    // y = a * b, one component (states 0..3) at a time.
     auto mul4 = [](float *y, const float *a, const float4 b) {
         y[0] = a[0] * b.x;
         y[1] = a[1] * b.y;
@@ -455,62 +458,104 @@ __device__ __forceinline__ int op2_kind(uint32_t kind, const unsigned char *rec,
     };
     switch (kind) {
     case OPK_LL: {
-        const unsigned mA = mask(cA, ia), mB = mask(cB, ia ^ 1u);
+        unsigned mA[NP], mB[NP];
 #pragma unroll
-        for (int k = 0; k < KT; ++k) {
-            const float4 a = PA[k * 16 + mA];
-            const float ax[4] = {a.x, a.y, a.z, a.w};
-            mul4(acc + 4 * k, ax, PB[k * 16 + mB]);
+        for (int h = 0; h < NP; ++h) {
+            mA[h] = mask(cA, ia, pl[h]);
+            mB[h] = mask(cB, ia ^ 1u, pl[h]);
         }
-        return 0;
-    }
-    case OPK_FL: {
-        const unsigned mB = mask(cB, 0);
-#pragma unroll
-        for (int k = 0; k < KT; ++k) {
-            float m[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) m[i] = pdot(PA[k * 4 + i], acc + 4 * k);
-            mul4(acc + 4 * k, m, PB[k * 16 + mB]);
-        }
-        return prev_lns;
-    }
-    case OPK_IL: {
-        float xA[KT * 4];
-        const int lA = load_internal<KT>(cA, slots, slot_sc, tile, pl, p, ppad, xA);
-        const unsigned mB = mask(cB, 0);
-#pragma unroll
-        for (int k = 0; k < KT; ++k) {
-            float m[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) m[i] = pdot(PA[k * 4 + i], xA + 4 * k);
-            mul4(acc + 4 * k, m, PB[k * 16 + mB]);
-        }
-        return lA;
-    }
-    case OPK_FI: {
-        float xB[KT * 4];
-        const int lB = load_internal<KT>(cB, slots, slot_sc, tile, pl, p, ppad, xB);
-#pragma unroll
-        for (int k = 0; k < KT; ++k) {
-            float m[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) m[i] = pdot(PA[k * 4 + i], acc + 4 * k);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) acc[4 * k + i] = m[i] * pdot(PB[k * 4 + i], xB + 4 * k);
-        }
-        return prev_lns + lB;
-    }
-    default: {  // OPK_II
-        float xA[KT * 4], xB[KT * 4];
-        const int lA = load_internal<KT>(cA, slots, slot_sc, tile, pl, p, ppad, xA);
-        const int lB = load_internal<KT>(cB, slots, slot_sc, tile, pl, p, ppad, xB);
 #pragma unroll
         for (int k = 0; k < KT; ++k)
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-                acc[4 * k + i] = pdot(PA[k * 4 + i], xA + 4 * k) * pdot(PB[k * 4 + i], xB + 4 * k);
-        return lA + lB;
+            for (int h = 0; h < NP; ++h) {
+                const float4 a = PA[k * 16 + mA[h]];
+                const float ax[4] = {a.x, a.y, a.z, a.w};
+                mul4(acc[h] + 4 * k, ax, PB[k * 16 + mB[h]]);
+            }
+#pragma unroll
+        for (int h = 0; h < NP; ++h) lns[h] = 0;
+        return;
+    }
+    case OPK_FL:
+    case OPK_IL: {
+        // A's rows: the previous result (FL) or loaded (IL); B a leaf.
+        float xA[NP][KT * 4];
+        int lA[NP];
+#pragma unroll
+        for (int h = 0; h < NP; ++h) {
+            if (kind == OPK_IL) {
+                lA[h] = load_internal<KT>(cA, slots, slot_sc, tile, pl[h], p[h], ppad, xA[h]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < KT * 4; ++q) xA[h][q] = acc[h][q];
+                lA[h] = lns[h];
+            }
+        }
+        unsigned mB[NP];
+#pragma unroll
+        for (int h = 0; h < NP; ++h) mB[h] = mask(cB, 0, pl[h]);
+#pragma unroll
+        for (int k = 0; k < KT; ++k) {
+            float m[NP][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float4 r = PA[k * 4 + i];
+#pragma unroll
+                for (int h = 0; h < NP; ++h) m[h][i] = pdot(r, xA[h] + 4 * k);
+            }
+#pragma unroll
+            for (int h = 0; h < NP; ++h) mul4(acc[h] + 4 * k, m[h], PB[k * 16 + mB[h]]);
+        }
+#pragma unroll
+        for (int h = 0; h < NP; ++h) lns[h] = lA[h];
+        return;
+    }
+    case OPK_FI: {
+        float xB[NP][KT * 4];
+        int lB[NP];
+#pragma unroll
+        for (int h = 0; h < NP; ++h)
+            lB[h] = load_internal<KT>(cB, slots, slot_sc, tile, pl[h], p[h], ppad, xB[h]);
+#pragma unroll
+        for (int k = 0; k < KT; ++k) {
+            float m[NP][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float4 r = PA[k * 4 + i];
+#pragma unroll
+                for (int h = 0; h < NP; ++h) m[h][i] = pdot(r, acc[h] + 4 * k);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float4 r = PB[k * 4 + i];
+#pragma unroll
+                for (int h = 0; h < NP; ++h) acc[h][4 * k + i] = m[h][i] * pdot(r, xB[h] + 4 * k);
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < NP; ++h) lns[h] = lns[h] + lB[h];
+        return;
+    }
+    default: {  // OPK_II
+        float xA[NP][KT * 4], xB[NP][KT * 4];
+        int lA[NP], lB[NP];
+#pragma unroll
+        for (int h = 0; h < NP; ++h) {
+            lA[h] = load_internal<KT>(cA, slots, slot_sc, tile, pl[h], p[h], ppad, xA[h]);
+            lB[h] = load_internal<KT>(cB, slots, slot_sc, tile, pl[h], p[h], ppad, xB[h]);
+        }
+#pragma unroll
+        for (int k = 0; k < KT; ++k)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float4 ra = PA[k * 4 + i], rb = PB[k * 4 + i];
+#pragma unroll
+                for (int h = 0; h < NP; ++h)
+                    acc[h][4 * k + i] = pdot(ra, xA[h] + 4 * k) * pdot(rb, xB[h] + 4 * k);
+            }
+#pragma unroll
+        for (int h = 0; h < NP; ++h) lns[h] = lA[h] + lB[h];
+        return;
     }
     }
 }
@@ -730,10 +775,14 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
             // no previous result: its first op runs the general path, which
             // reads that child from where its record says.
             if ((kind == OPK_FL || kind == OPK_FI) && o == 0) kind = OPK_GENERIC;
-            if (kind != OPK_GENERIC)
-                lns = op2_kind<KT, STAGED>(kind, rec, kids, (fl & kOpKindA) ? 1u : 0u, acc,
-                                           prev_lns, masks, lrow, slots, slot_sc, tile, pl,
-                                           p, ppad);
+            if (kind != OPK_GENERIC) {
+                float(&acc1)[1][KT * 4] = reinterpret_cast<float(&)[1][KT * 4]>(acc);
+                int l1[1] = {prev_lns};
+                const unsigned pl1[1] = {pl}, p1[1] = {p};
+                op2_kind<KT, STAGED, 1>(kind, rec, kids, (fl & kOpKindA) ? 1u : 0u, acc1, l1,
+                                        masks, lrow, slots, slot_sc, tile, pl1, p1, ppad);
+                lns = l1[0];
+            }
         }
         // (The FP64 form keeps the loop: both children's rows in registers
         // at once cost it occupancy, and it is bound by the FP64 pipe.)
@@ -925,7 +974,6 @@ __device__ bool walk_tile2(const PlanArgs &a, unsigned tile_idx, const SmemLayou
                            unsigned ring_depth, uint32_t &phase) {
     typedef float T;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ int s_ok;
     const unsigned nthr = blockDim.x;
     const unsigned tile = 2 * nthr;
     const unsigned tid = threadIdx.x;
@@ -970,28 +1018,35 @@ __device__ bool walk_tile2(const PlanArgs &a, unsigned tile_idx, const SmemLayou
 
     T acc[2][K * 4];
     int lns[2] = {0, 0};
-    const uint32_t spin = tid == 0 ? g_spin_limit : 0u;
+    const uint32_t spin = g_spin_limit;
     for (unsigned o = 0, stage = 0; o < a.nops;
          ++o, stage = (stage + 1 == R) ? 0u : stage + 1) {
         const uint8_t *pre[kLeafPre] = {nullptr, nullptr, nullptr, nullptr};
         if (!STAGED && tid == 0 && o + R < a.nops) read_rows(a, o + R, pre);
-        if (tid == 0) {
-            const uint32_t par = (phase >> stage) & 1u;
-            s_ok = mbar_wait_bounded(&bars[stage], par, spin);
-            if (!s_ok) drain_ring(bars, phase, o, a.nops, R);
-            phase ^= 1u << stage;
-        }
-        __syncthreads();
-        if (!s_ok) {
-            if (tid == 0) atomicOr(a.err, 1u);
-            return false;  // all threads leave together
-        }
+        // Every thread waits for the record (walk_tile's hand-off).
+        const bool ok =
+            __all_sync(0xffffffffu, mbar_wait_bounded(&bars[stage], (phase >> stage) & 1u,
+                                                      spin));
+        phase ^= 1u << stage;
+        void *ydata = nullptr, *yscaler = nullptr;
+        int yslot = -1;
+        bool yhbm = false;
+        unsigned nchild = 0;
+        uint32_t nbytes = (uint32_t)sstride;
+        if (ok) {
         const unsigned char *rec = ring + (size_t)stage * sstride;
         const uint8_t *lrow = rec + a.rstride;
         unsigned nlk = 0;
         const RecHead *hd = reinterpret_cast<const RecHead *>(rec);
         const RecChild *kids = reinterpret_cast<const RecChild *>(rec + sizeof(RecHead));
-        const unsigned nchild = hd->nchild;
+        nchild = hd->nchild;
+        const uint32_t fl = hd->flags;
+        uint32_t kind = (fl >> kOpKindShift) & 7u;
+        if ((kind == OPK_FL || kind == OPK_FI) && o == 0) kind = OPK_GENERIC;
+        if (kind != OPK_GENERIC) {
+            op2_kind<K, STAGED, 2>(kind, rec, kids, (fl & kOpKindA) ? 1u : 0u, acc, lns, masks,
+                                   lrow, slots, slot_sc, tile, pl, p, ppad);
+        } else {
         lns[0] = lns[1] = 0;
         for (unsigned ci = 0; ci < nchild; ++ci) {
             const RecChild ch = kids[ci];
@@ -1059,17 +1114,27 @@ __device__ bool walk_tile2(const PlanArgs &a, unsigned tile_idx, const SmemLayou
                 }
             }
         }
-        void *ydata = hd->data;
-        void *yscaler = hd->scaler;
-        const int yslot = hd->slot;
-        const bool yhbm = !(hd->flags & REC_NO_HBM);
-        __syncthreads();
+        }  // generic
+        ydata = hd->data;
+        yscaler = hd->scaler;
+        yslot = hd->slot;
+        yhbm = !(fl & REC_NO_HBM);
+        nbytes = (hd->next_bytes != 0u && hd->next_bytes <= (uint32_t)sstride)
+                     ? hd->next_bytes : (uint32_t)sstride;
+        }  // ok
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) {
+                atomicOr(a.err, 1u);
+                drain_ring(bars, phase ^ (1u << stage), o, a.nops, R);
+            }
+            return false;
+        }
         if (tid == 0 && o + R < a.nops) {
             if (STAGED) {
                 fence_proxy_async();
-                mbar_expect_tx(&bars[stage], a.rstride);
+                mbar_expect_tx(&bars[stage], nbytes);
                 bulk_g2s(ring + (size_t)stage * a.rstride,
-                         a.rec + (size_t)(o + R) * a.rstride, a.rstride, &bars[stage]);
+                         a.rec + (size_t)(o + R) * a.rstride, nbytes, &bars[stage]);
             } else {
                 issue_stage(a, o + R, ring + (size_t)stage * sstride, &bars[stage], tile_idx,
                             tile, pre);
