@@ -375,6 +375,16 @@ __device__ __noinline__ void drain_ring(uint64_t *bars, uint32_t phase, unsigned
     }
 }
 
+// The per-op hand-off barrier of the walkers: true when every thread's
+// record wait succeeded.  `ok` is uniform within each warp.
+__device__ __forceinline__ bool cta_hand_off(bool ok, unsigned nthr) {
+    if (nthr == 32) {
+        __syncwarp();
+        return ok;
+    }
+    return __syncthreads_and(ok) != 0;
+}
+
 // Max of n values as a balanced tree (the same value as a left-to-right
 // chain: fmax is exact and ignores NaN operands either way), so the
 // dependent chain is log2(n) long instead of n.
@@ -836,8 +846,10 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
         }  // ok
         // Every thread has read the stage: hand it to op o + R.  A record
         // wait that gave up in any warp ends the tile for all: thread 0
-        // waits for the copies still in flight into the ring.
-        if (!__syncthreads_and(ok)) {
+        // waits for the copies still in flight into the ring.  A one-warp
+        // CTA needs only a warp barrier: every other shared row a thread
+        // touches (stack slots, leaf masks) is its own pattern's.
+        if (!cta_hand_off(ok, nthr)) {
             if (tid == 0) {
                 atomicOr(a.err, 1u);
                 drain_ring(bars, phase ^ (1u << stage), o, nsteps, R);
@@ -1122,7 +1134,7 @@ __device__ bool walk_tile2(const PlanArgs &a, unsigned tile_idx, const SmemLayou
         nbytes = (hd->next_bytes != 0u && hd->next_bytes <= (uint32_t)sstride)
                      ? hd->next_bytes : (uint32_t)sstride;
         }  // ok
-        if (!__syncthreads_and(ok)) {
+        if (!cta_hand_off(ok, nthr)) {
             if (tid == 0) {
                 atomicOr(a.err, 1u);
                 drain_ring(bars, phase ^ (1u << stage), o, a.nops, R);
