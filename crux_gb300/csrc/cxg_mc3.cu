@@ -55,20 +55,36 @@ namespace cxg {
 enum {
     MV_BRLEN = 0, MV_NNI = 1, MV_RATES = 2, MV_ALPHA = 3, MV_FREQS = 4, MV_SPR = 5,
     MV_ETBR = 6, MV_INVAR = 7, MV_GAMMAJ = 8, MV_FREQJ = 9, MV_INVARJ = 10,
-    MV_RATEJ = 11, MV_RATE1 = 12, MV_INIT = 13
+    MV_RATEJ = 11, MV_RATE1 = 12, MV_WEIGHT = 13, MV_RMULT = 14, MV_MIXJ = 15,
+    MV_INIT = 16
 };
-constexpr int kMoves = 13;
+constexpr int kMoves = 16;
+// Most models in a chain's mixture.
+constexpr int kMaxModels = 4;
 
-struct Mc3Model {
+// One model of a chain's mixture (a CxtLikModel with its parameters).
+struct Mc3Sub {
     // rates: the six exchangeabilities; those of one rate class (rclass, a
     // restricted growth string with nrates classes) are equal.
     double rates[6], freqs[4], alpha;
     int32_t rclass[6], nrates;
-    double wvar, winvar;  // mixture weights of the variable and +I parts
+    double wvar, winvar;  // weights of the variable and +I parts
     // 0: Gamma rates off (the reference's alpha = INFINITY: all variable
     // weight on the first category, rate 1); 0: equal base frequencies.
     int32_t gamma_on, freqs_est;
-    double pinorm[4], qnorm, cube[64], eig[4];
+    double weight, rmult;       // mixture weight and rate multiplier
+    double gcat[kMaxComps];     // Gamma category rates (Gamma on)
+};
+
+// A chain's model: nmodels mixture members in slots 0..nmodels-1.  The
+// walker's components are model-major, kper = ncat (+1 with +I) per slot
+// for mmax slots; the components of unused slots carry weight 0 and model
+// 0's matrices, so their rows stay finite.
+struct Mc3Model {
+    Mc3Sub q[kMaxModels];
+    int32_t nmodels;
+    double pinorm[kMaxModels * 4], qnorm[kMaxModels];
+    double cube[kMaxModels * 64], eig[kMaxModels * 4];
     double cmult[kMaxComps], rmult[kMaxComps];
     int32_t midx[kMaxComps];
     double wnorm;
@@ -92,7 +108,8 @@ struct Mc3Prop {
 
 struct Mc3Dev {
     uint32_t nchains, ntaxa, nnodes, root, kact, npat, ppad, prec;
-    uint32_t ncat, invar;  // kact = ncat Gamma categories (+1 with +I)
+    uint32_t ncat, invar;  // kper = ncat Gamma categories (+1 with +I)
+    uint32_t kper, mmax;   // components per model; kact = mmax * kper
     uint32_t rstride, M, maxkids, ntiles;
     // Two tree buffers per chain, b = curtree[c] current: buffer b of
     // chain c starts at (b * nchains + c) * nnodes entries.
@@ -127,6 +144,11 @@ struct Mc3Dev {
     double freq_conc, etbr_pext, invar_lambda, invar_prior;
     double gamma_jump_prior, freq_jump_prior, invar_jump_prior;
     double rate_jump_prior, rate_lambda;
+    double mix_jump_prior, weight_lambda, rmult_lambda;
+    // Moves with a non-zero weight (bit per MV_*): a new mixture member's
+    // parameters are drawn from the prior where a move can change them,
+    // else copied from slot 0.
+    uint32_t moves_on;
     uint32_t swap_stride;
     uint32_t *acc, *rej;  // [c][kMoves]
     uint32_t *nswap;      // [c]
@@ -137,92 +159,105 @@ struct Mc3Dev {
     uint32_t staged;      // leaves staged per tile (else streamed)
 };
 
-// wNorm and the root weights of a model whose eigensystem and category
-// rates are set (Lik.pyx:1603-1665).  Component weights as Lik.setWVar /
-// setWInvar leave them: wVar / ncat for each Gamma category and wInvar for
-// the +I component (cmult 0), each scaled by their sum; the +I component
-// stays out of wNorm.
-__device__ void mc3_model_weights(Mc3Model &m, unsigned ncat, unsigned invar) {
-    const unsigned K = ncat + (invar ? 1u : 0u);
-    double cw[kMaxComps], wsum = 0.0;
-    for (unsigned k = 0; k < ncat; ++k) cw[k] = m.wvar / ncat;
-    if (ncat > 1 && !m.gamma_on) {
-        // Lik.setAlpha(INFINITY), Lik.pyx:1264-1273: the first category
-        // takes all the variable weight at rate 1, the others weight 0.
-        cw[0] = m.wvar;
-        m.cmult[0] = 1.0;
-        for (unsigned k = 1; k < ncat; ++k) {
-            cw[k] = 0.0;
-            m.cmult[k] = 0.0;
-        }
-    }
-    if (invar) {
-        cw[ncat] = m.winvar;
-        m.cmult[ncat] = 0.0;
-    }
-    for (unsigned k = 0; k < K; ++k) wsum += cw[k];
+// wNorm and the root weights of a mixture whose members' eigensystems and
+// category rates are set (Lik.pyx:1603-1665).  Component weights as
+// Lik.setWVar / setWInvar leave them within a member: wVar / ncat for each
+// Gamma category and wInvar for the +I component (cmult 0), scaled by
+// their sum; across members, by weight / (sum of the members' weights).
+// wNorm = 1 / sum of weightScaled * rmult / qNorm over components with
+// non-zero weight and rate; the +I components stay out of it.
+__device__ void mc3_model_weights(Mc3Model &m, unsigned ncat, unsigned invar,
+                                  unsigned mmax) {
+    const unsigned kper = ncat + (invar ? 1u : 0u);
+    double wsum = 0.0;
+    for (int mi = 0; mi < m.nmodels; ++mi) wsum += m.q[mi].weight;
     double qmean = 0.0;
-    for (unsigned k = 0; k < K; ++k) {
-        const double ws = cw[k] / wsum;
-        m.rmult[k] = 1.0;
-        m.midx[k] = 0;
-        if (ws != 0.0 && m.cmult[k] != 0.0) qmean += ws * (1.0 / m.qnorm);
-        for (int i = 0; i < 4; ++i) m.pn[k * 4 + i] = m.pinorm[i] * ws;
+    for (unsigned mi = 0; mi < mmax; ++mi) {
+        const bool on = (int)mi < m.nmodels;
+        const unsigned src = on ? mi : 0u;
+        const Mc3Sub &s = m.q[src];
+        double cw[kMaxComps], cm[kMaxComps], cwsum = 0.0;
+        for (unsigned k = 0; k < ncat; ++k) {
+            cw[k] = s.wvar / ncat;
+            cm[k] = ncat == 1 ? 1.0 : s.gcat[k];
+        }
+        if (ncat > 1 && !s.gamma_on) {
+            // Lik.setAlpha(INFINITY), Lik.pyx:1264-1273: the first category
+            // takes all the variable weight at rate 1, the others weight 0.
+            cw[0] = s.wvar;
+            cm[0] = 1.0;
+            for (unsigned k = 1; k < ncat; ++k) {
+                cw[k] = 0.0;
+                cm[k] = 0.0;
+            }
+        }
+        if (invar) {
+            cw[ncat] = s.winvar;
+            cm[ncat] = 0.0;
+        }
+        for (unsigned k = 0; k < kper; ++k) cwsum += cw[k];
+        for (unsigned k = 0; k < kper; ++k) {
+            const unsigned c = mi * kper + k;
+            const double ws = on ? (s.weight / wsum) * (cw[k] / cwsum) : 0.0;
+            m.cmult[c] = cm[k];
+            m.rmult[c] = s.rmult;
+            m.midx[c] = (int32_t)src;
+            if (ws != 0.0 && cm[k] != 0.0) qmean += ws * (s.rmult / m.qnorm[src]);
+            for (int i = 0; i < 4; ++i) m.pn[c * 4 + i] = m.pinorm[src * 4 + i] * ws;
+        }
     }
     m.wnorm = 1.0 / qmean;
     m.ok = 1;
 }
 
 // Parts of a model to derive again: FIN_EIG (rates or frequencies changed),
-// FIN_GAMMA (alpha), FIN_WEIGHTS (the +I weights only).
+// FIN_GAMMA (alpha), FIN_WEIGHTS (weights only: +I weights, mixture
+// weights and rate multipliers, members added or removed).
 enum : unsigned { FIN_EIG = 1, FIN_GAMMA = 2, FIN_ALL = 3, FIN_WEIGHTS = 4 };
 
-// Model derived quantities: Q eigensystem (FP64 Jacobi on the device),
-// Gamma category rates, wNorm and the root weights (Lik.pyx:1603-1665);
-// the parts `what` does not name are kept.  One warp: lanes 0..ncat-2
-// compute the Gamma category cuts while lanes 28..31 form the eigensystem;
-// lane 0 finishes.  All 32 lanes of the warp call it; the result (true:
-// decomposed) is lane 0's.
+// Derived quantities of mixture member `mi`: its Q eigensystem (FP64
+// Jacobi on the device) and Gamma category rates, then wNorm and the root
+// weights of the whole mixture (Lik.pyx:1603-1665); the parts `what` does
+// not name are kept.  One warp: lanes 0..ncat-2 compute the Gamma category
+// cuts while lanes 28..31 form the eigensystem; lane 0 finishes.  All 32
+// lanes of the warp call it; the result (true: decomposed) is lane 0's.
 __device__ bool mc3_model_finish_warp(Mc3Model &m, unsigned ncat, unsigned invar,
-                                      unsigned what) {
+                                      unsigned mmax, unsigned what, unsigned mi) {
     __shared__ double s_cut[kMaxComps];
     __shared__ double s_eig[74];
     __shared__ int s_bad;
+    Mc3Sub &q = m.q[mi];
     const unsigned lane = threadIdx.x & 31u;
     if (lane == 0) s_bad = 0;
     __syncwarp();
-    if ((what & FIN_GAMMA) && ncat > 1 && m.gamma_on && lane < ncat - 1) {
-        const double cut = d_gamma_cut(m.alpha, (int)ncat, (int)lane);
+    if ((what & FIN_GAMMA) && ncat > 1 && q.gamma_on && lane < ncat - 1) {
+        const double cut = d_gamma_cut(q.alpha, (int)ncat, (int)lane);
         if (cut == -1.0)
             s_bad = 1;
         else
             s_cut[lane] = cut;
     }
-    if ((what & FIN_EIG) && lane >= 28) qdecomp4_warp(m.rates, m.freqs, s_eig, 28);
+    if ((what & FIN_EIG) && lane >= 28) qdecomp4_warp(q.rates, q.freqs, s_eig, 28);
     __syncwarp();
     if ((what & FIN_EIG) && lane == 31) {
         const double *tmp = s_eig;
         if (tmp[73] != 0.0) {
             s_bad = 1;
         } else {
-            for (int i = 0; i < 4; ++i) m.pinorm[i] = tmp[i];
-            m.qnorm = tmp[4];
-            for (int i = 0; i < 64; ++i) m.cube[i] = tmp[5 + i];
-            for (int i = 0; i < 4; ++i) m.eig[i] = tmp[69 + i];
+            for (int i = 0; i < 4; ++i) m.pinorm[mi * 4 + i] = tmp[i];
+            m.qnorm[mi] = tmp[4];
+            for (int i = 0; i < 64; ++i) m.cube[mi * 64 + i] = tmp[5 + i];
+            for (int i = 0; i < 4; ++i) m.eig[mi * 4 + i] = tmp[69 + i];
         }
     }
     __syncwarp();
     if (lane != 0) return false;
     if (s_bad) return false;
-    if (what & FIN_GAMMA) {
-        if (ncat > 1 && m.gamma_on) {
-            for (unsigned i = 0; i + 1 < ncat; ++i) m.cmult[i] = s_cut[i];
-            d_gamma_rates_from_cuts((int)ncat, m.cmult);
-        } else if (ncat == 1) {
-            m.cmult[0] = 1.0;
-        }
+    if ((what & FIN_GAMMA) && ncat > 1 && q.gamma_on) {
+        for (unsigned i = 0; i + 1 < ncat; ++i) q.gcat[i] = s_cut[i];
+        d_gamma_rates_from_cuts((int)ncat, q.gcat);
     }
-    mc3_model_weights(m, ncat, invar);
+    mc3_model_weights(m, ncat, invar, mmax);
     return true;
 }
 
@@ -230,7 +265,9 @@ __global__ void mc3_init_kernel(Mc3Dev d) {
     const unsigned c = blockIdx.x;
     if (c >= d.nchains || threadIdx.x >= 32) return;
     Mc3Model &m = d.model[c * 2 + d.curmodel[c]];
-    const bool ok = mc3_model_finish_warp(m, d.ncat, d.invar, FIN_ALL);
+    bool ok = true;
+    for (int mi = 0; mi < m.nmodels; ++mi)
+        ok &= mc3_model_finish_warp(m, d.ncat, d.invar, d.mmax, FIN_ALL, (unsigned)mi);
     if (threadIdx.x == 0 && !ok) atomicOr(d.status, 1u);
 }
 
@@ -255,6 +292,150 @@ __device__ double ln_dirichlet(const double *alpha, const double *x, int n) {
         r += (alpha[i] - 1.0) * log(x[i]) - lgamma(alpha[i]);
     }
     return r + lgamma(s);
+}
+
+// Mixture members.  A member's prior density (in log) is the product of
+// the parts its moves sample, as those moves' Hastings terms assume:
+// weight and rate multiplier iid Exp(1); base frequencies equal (odds
+// freqJumpPrior to estimated) or estimated with a flat Dirichlet prior
+// (density 3! = 6); k rate classes with probability proportional to
+// rateJumpPrior^-(k-1), a uniform partition among the S(6, k), class
+// rates iid Exp(1); Gamma off (odds rateShapeInvJumpPrior to on) or 1/alpha
+// ~ Exp(alpha_prior); +I off (odds invarJumpPrior to on) or wVar, wInvar ~
+// Exp(1 - invarPrior), Exp(invarPrior).  A part no enabled move changes is
+// the same in every member (slot 0's, copied) and adds nothing; a
+// structural choice whose jump is disabled is slot 0's too.
+__device__ inline bool mv_on(const Mc3Dev &d, int mv) { return (d.moves_on >> mv) & 1u; }
+
+__device__ double mc3_member_lnprior(const Mc3Sub &q, const Mc3Dev &d) {
+    double lp = -q.weight - q.rmult;
+    if (mv_on(d, MV_FREQS) || mv_on(d, MV_FREQJ)) {
+        if (mv_on(d, MV_FREQJ)) {
+            const double f = d.freq_jump_prior;
+            lp += q.freqs_est ? -log1p(f) : log(f) - log1p(f);
+        }
+        if (q.freqs_est) lp += 1.791759469228055;  // ln 3!
+    }
+    if (mv_on(d, MV_RATES) || mv_on(d, MV_RATE1) || mv_on(d, MV_RATEJ)) {
+        double r[6];
+        for (int i = 0; i < 6; ++i) r[q.rclass[i]] = q.rates[i];
+        for (int c = 0; c < q.nrates; ++c) lp -= r[c];
+        if (mv_on(d, MV_RATEJ)) {
+            // P(k) = rjp^-(k-1) / sum_j rjp^-(j-1), then 1 / S(6, k).
+            const double lr = log(d.rate_jump_prior);
+            double z = 0.0;
+            for (int j = 1; j <= 6; ++j) z += exp(-lr * (j - 1));
+            lp += -lr * (q.nrates - 1) - log(z) - log(kStirling6[q.nrates]);
+        }
+    }
+    if (d.ncat > 1 && (mv_on(d, MV_ALPHA) || mv_on(d, MV_GAMMAJ))) {
+        if (mv_on(d, MV_GAMMAJ)) {
+            const double g = d.gamma_jump_prior;
+            lp += q.gamma_on ? -log1p(g) : log(g) - log1p(g);
+        }
+        if (q.gamma_on) lp += log(d.alpha_prior) - d.alpha_prior / q.alpha;
+    }
+    if (d.invar && (mv_on(d, MV_INVAR) || mv_on(d, MV_INVARJ))) {
+        const bool on = q.winvar != 0.0;
+        if (mv_on(d, MV_INVARJ)) {
+            const double j = d.invar_jump_prior;
+            lp += on ? -log1p(j) : log(j) - log1p(j);
+        }
+        if (on) {
+            const double ip = d.invar_prior;
+            lp += log(1.0 - ip) - (1.0 - ip) * q.wvar + log(ip) - ip * q.winvar;
+        }
+    }
+    return lp;
+}
+
+// A new member drawn from that density (slot 0's member `ref` gives the
+// fixed parts); returns its log density.
+__device__ double mc3_draw_member(Mc3Sub &q, const Mc3Sub &ref, const Mc3Dev &d,
+                                  Philox &rng) {
+    auto expo = [&]() {
+        const double x = -log(1.0 - philox_u01(rng));
+        return x > 1e-300 ? x : 1e-300;
+    };
+    q = ref;
+    q.weight = expo();
+    q.rmult = expo();
+    if (mv_on(d, MV_FREQS) || mv_on(d, MV_FREQJ)) {
+        if (mv_on(d, MV_FREQJ))
+            q.freqs_est = philox_u01(rng) < 1.0 / (1.0 + d.freq_jump_prior) ? 1 : 0;
+        if (q.freqs_est) {
+            double f[4], sum = 0.0;
+            for (int i = 0; i < 4; ++i) sum += (f[i] = expo());
+            for (int i = 0; i < 4; ++i) q.freqs[i] = f[i] / sum;
+        } else {
+            for (int i = 0; i < 4; ++i) q.freqs[i] = 0.25;
+        }
+    }
+    if (mv_on(d, MV_RATES) || mv_on(d, MV_RATE1) || mv_on(d, MV_RATEJ)) {
+        if (mv_on(d, MV_RATEJ)) {
+            // k, then the r-th restricted growth string with k classes in
+            // lexicographic order (203 strings in all).
+            const double lr = log(d.rate_jump_prior);
+            double z = 0.0, w[7];
+            for (int j = 1; j <= 6; ++j) z += (w[j] = exp(-lr * (j - 1)));
+            const double u = philox_u01(rng) * z;
+            int k = 1;
+            double acc = w[1];
+            while (k < 6 && u >= acc) acc += w[++k];
+            uint32_t r = philox_below(rng, (uint32_t)kStirling6[k]);
+            int a[6] = {0, 0, 0, 0, 0, 0};
+            for (int guard = 0; guard < 203; ++guard) {
+                int mx = 0;
+                for (int i = 0; i < 6; ++i) mx = a[i] > mx ? a[i] : mx;
+                if (mx + 1 == k) {
+                    if (r == 0) break;
+                    --r;
+                }
+                // Next string: the rightmost a[i] below 1 + max(a[0..i-1])
+                // goes up by one, the rest of the string to 0.
+                int i = 5;
+                for (; i >= 1; --i) {
+                    int pm = 0;
+                    for (int h = 0; h < i; ++h) pm = a[h] > pm ? a[h] : pm;
+                    if (a[i] <= pm) break;
+                }
+                if (i < 1) break;
+                ++a[i];
+                for (int h = i + 1; h < 6; ++h) a[h] = 0;
+            }
+            for (int i = 0; i < 6; ++i) q.rclass[i] = a[i];
+            q.nrates = k;
+        }
+        double cr[6];
+        for (int c = 0; c < q.nrates; ++c) cr[c] = expo();
+        for (int i = 0; i < 6; ++i) q.rates[i] = cr[q.rclass[i]];
+    }
+    if (d.ncat > 1 && (mv_on(d, MV_ALPHA) || mv_on(d, MV_GAMMAJ))) {
+        if (mv_on(d, MV_GAMMAJ))
+            q.gamma_on = philox_u01(rng) < 1.0 / (1.0 + d.gamma_jump_prior) ? 1 : 0;
+        if (q.gamma_on) q.alpha = d.alpha_prior / expo();
+    }
+    if (d.invar && (mv_on(d, MV_INVAR) || mv_on(d, MV_INVARJ))) {
+        bool on = q.winvar != 0.0;
+        if (mv_on(d, MV_INVARJ)) on = philox_u01(rng) < 1.0 / (1.0 + d.invar_jump_prior);
+        if (on) {
+            q.wvar = expo() / (1.0 - d.invar_prior);
+            q.winvar = expo() / d.invar_prior;
+        } else {
+            q.wvar = 1.0;
+            q.winvar = 0.0;
+        }
+    }
+    return mc3_member_lnprior(q, d);
+}
+
+// Member `from` (parameters and derived matrices) into slot `to`.
+__device__ void mc3_move_member(Mc3Model &m, unsigned from, unsigned to) {
+    m.q[to] = m.q[from];
+    for (int i = 0; i < 4; ++i) m.pinorm[to * 4 + i] = m.pinorm[from * 4 + i];
+    m.qnorm[to] = m.qnorm[from];
+    for (int i = 0; i < 64; ++i) m.cube[to * 64 + i] = m.cube[from * 64 + i];
+    for (int i = 0; i < 4; ++i) m.eig[to * 4 + i] = m.eig[from * 4 + i];
 }
 
 // One end of an eTBR move (Chain.pyx:517-597 for the X end, the same for
@@ -391,7 +572,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         __syncthreads();
     }
     __shared__ int s_nd, s_lowest;
-    __shared__ unsigned s_fin;
+    __shared__ unsigned s_fin, s_fin_mi;
     __shared__ bool s_full, s_etbr;
     if (threadIdx.x == 0) {
         s_fin = 0;
@@ -410,6 +591,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         pr.model_changed = 0;
         pr.lnPrior = 0.0;
         pr.lnHast = 0.0;
+        unsigned mi = 0;  // the mixture member a model move changes
         bool full = false;
         int lowest = -1;  // lowest dirty node of a path move
         if (g == 0) {
@@ -420,16 +602,23 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             int t = 0;
             while (t < kMoves - 1 && u >= d.wcdf[t]) ++t;
             if ((t == MV_NNI || t == MV_SPR) && N < 4) t = MV_BRLEN;
+            // A model move acts on one uniform member of the mixture
+            // (drawn only when there are several).
+            const int nm = m0.nmodels;
+            mi = nm > 1 ? philox_below(rng, (uint32_t)nm) : 0u;
+            const Mc3Sub &q0 = m0.q[mi];
             // A move with nothing to change in this state is a branch
             // move instead, so each jump is drawn with the same
             // probability on both of its sides.
-            if (t == MV_ALPHA && (d.ncat < 2 || !m0.gamma_on)) t = MV_BRLEN;
-            if ((t == MV_INVAR && (!d.invar || m0.winvar == 0.0)) ||
+            if (t == MV_ALPHA && (d.ncat < 2 || !q0.gamma_on)) t = MV_BRLEN;
+            if ((t == MV_INVAR && (!d.invar || q0.winvar == 0.0)) ||
                 (t == MV_INVARJ && !d.invar))
                 t = MV_BRLEN;
-            if ((t == MV_RATES || t == MV_RATE1) && m0.nrates < 2) t = MV_BRLEN;
+            if ((t == MV_RATES || t == MV_RATE1) && q0.nrates < 2) t = MV_BRLEN;
             if (t == MV_GAMMAJ && d.ncat < 2) t = MV_BRLEN;
-            if (t == MV_FREQS && !m0.freqs_est) t = MV_BRLEN;
+            if (t == MV_FREQS && !q0.freqs_est) t = MV_BRLEN;
+            if ((t == MV_WEIGHT || t == MV_RMULT) && nm < 2) t = MV_BRLEN;
+            if (t == MV_MIXJ && d.mmax < 2) t = MV_BRLEN;
             pr.type = t;
             if (t == MV_BRLEN) {
                 // Uniform edge = uniform non-root node (Chain.pyx:442-447).
@@ -636,7 +825,8 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 const unsigned which = philox_below(rng, 2);
                 const double lnM = d.invar_lambda * (philox_u01(rng) - 0.5);
                 m1 = m0;
-                double &w = which == 0 ? m1.wvar : m1.winvar;
+                Mc3Sub &q1 = m1.q[mi];
+                double &w = which == 0 ? q1.wvar : q1.winvar;
                 const double w0 = w, w1 = w0 * exp(lnM);
                 w = w1;
                 pr.lnPrior = -(which == 0 ? 1.0 - d.invar_prior : d.invar_prior) * (w1 - w0);
@@ -658,21 +848,22 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 // which is not the density its weight move and prior use.)
                 const double ip = d.invar_prior;
                 m1 = m0;
+                Mc3Sub &q1 = m1.q[mi];
                 auto lnw = [&](double wv, double wi) {
                     return log(1.0 - ip) - (1.0 - ip) * wv + log(ip) - ip * wi;
                 };
-                if (m0.winvar != 0.0) {
-                    const double dens = lnw(m0.wvar, m0.winvar);
-                    m1.wvar = 1.0;
-                    m1.winvar = 0.0;
+                if (q0.winvar != 0.0) {
+                    const double dens = lnw(q0.wvar, q0.winvar);
+                    q1.wvar = 1.0;
+                    q1.winvar = 0.0;
                     pr.lnPrior = log(d.invar_jump_prior) - dens;
                     pr.lnHast = dens;
                 } else {
                     const double wv = -log(1.0 - philox_u01(rng)) / (1.0 - ip);
                     const double wi = -log(1.0 - philox_u01(rng)) / ip;
                     const double dens = lnw(wv, wi);
-                    m1.wvar = wv;
-                    m1.winvar = wi > 0.0 ? wi : 1e-300;
+                    q1.wvar = wv;
+                    q1.winvar = wi > 0.0 ? wi : 1e-300;
                     pr.lnPrior = -log(d.invar_jump_prior) + dens;
                     pr.lnHast = -dens;
                 }
@@ -682,15 +873,16 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             } else if (t == MV_RATE1) {
                 // One class rate times m = exp(lambda (u - 1/2)), Exp(1)
                 // prior (ratePropose, Chain.pyx:267-319).
-                const int r = (int)philox_below(rng, (uint32_t)m0.nrates);
+                const int r = (int)philox_below(rng, (uint32_t)q0.nrates);
                 const double lnM = d.rate_lambda * (philox_u01(rng) - 0.5);
                 double c0 = 0.0;
                 for (int i = 0; i < 6; ++i)
-                    if (m0.rclass[i] == r) c0 = m0.rates[i];
+                    if (q0.rclass[i] == r) c0 = q0.rates[i];
                 const double c1 = c0 * exp(lnM);
                 m1 = m0;
+                Mc3Sub &q1 = m1.q[mi];
                 for (int i = 0; i < 6; ++i)
-                    if (m0.rclass[i] == r) m1.rates[i] = c1;
+                    if (q0.rclass[i] == r) q1.rates[i] = c1;
                 pr.lnPrior = -(c1 - c0);
                 pr.lnHast = lnM;
                 pr.model_changed = 1;
@@ -713,17 +905,18 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 // two members to the parts and flips a coin for the rest,
                 // which is not the uniform bipartition its proposal
                 // ratio assumes.
-                const int k = m0.nrates;
+                const int k = q0.nrates;
                 int cnt[6] = {0, 0, 0, 0, 0, 0};
                 double cr[6];
                 for (int i = 0; i < 6; ++i) {
-                    cnt[m0.rclass[i]]++;
-                    cr[m0.rclass[i]] = m0.rates[i];
+                    cnt[q0.rclass[i]]++;
+                    cr[q0.rclass[i]] = q0.rates[i];
                 }
                 const bool merge =
                     k == 6 ? true : (k == 1 ? false : philox_below(rng, 2) == 0);
                 const double lrjp = log(d.rate_jump_prior);
                 m1 = m0;
+                Mc3Sub &q1 = m1.q[mi];
                 if (!merge) {
                     int sp[6], ns = 0;
                     for (int r = 0; r < k; ++r)
@@ -734,21 +927,21 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                     const double u = philox_u01(rng), r0 = cr[c];
                     int nA = 0, j = 0;
                     for (int i = 0; i < 6; ++i)
-                        if (m0.rclass[i] == c) nA += (z >> j++) & 1u;
+                        if (q0.rclass[i] == c) nA += (z >> j++) & 1u;
                     const int nB = n0 - nA;
                     const double rA = r0 * n0 * u / nA, rB = r0 * n0 * (1.0 - u) / nB;
                     j = 0;
                     for (int i = 0; i < 6; ++i)
-                        if (m0.rclass[i] == c) {
+                        if (q0.rclass[i] == c) {
                             if ((z >> j++) & 1u) {
-                                m1.rates[i] = rA;
+                                q1.rates[i] = rA;
                             } else {
-                                m1.rclass[i] = k;
-                                m1.rates[i] = rB;
+                                q1.rclass[i] = k;
+                                q1.rates[i] = rB;
                             }
                         }
-                    rgs_normalize(m1.rclass);
-                    m1.nrates = k + 1;
+                    rgs_normalize(q1.rclass);
+                    q1.nrates = k + 1;
                     const double pS = k == 1 ? 1.0 : 0.5, pM = k + 1 == 6 ? 1.0 : 0.5;
                     pr.lnPrior = -lrjp + log(kStirling6[k]) - log(kStirling6[k + 1]) +
                                  (r0 - rA - rB);
@@ -764,15 +957,15 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                     const double rA = cr[a], rB = cr[b];
                     const double r0 = (nA * rA + nB * rB) / n0;
                     for (int i = 0; i < 6; ++i) {
-                        int r = m0.rclass[i];
+                        int r = q0.rclass[i];
                         if (r == b) r = a;
                         else if (r > b) --r;
-                        m1.rclass[i] = r;
-                        if (r == a) m1.rates[i] = r0;
+                        q1.rclass[i] = r;
+                        if (r == a) q1.rates[i] = r0;
                     }
-                    m1.nrates = k - 1;
+                    q1.nrates = k - 1;
                     int cnt1[6] = {0, 0, 0, 0, 0, 0}, ns1 = 0;
-                    for (int i = 0; i < 6; ++i) cnt1[m1.rclass[i]]++;
+                    for (int i = 0; i < 6; ++i) cnt1[q1.rclass[i]]++;
                     for (int r = 0; r < k - 1; ++r) ns1 += cnt1[r] > 1;
                     const double pS = k - 1 == 1 ? 1.0 : 0.5, pM = k == 6 ? 1.0 : 0.5;
                     pr.lnPrior = lrjp + log(kStirling6[k]) - log(kStirling6[k - 1]) -
@@ -792,15 +985,16 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 // split between lnPrior and lnHast as the reference does.
                 const double sp = d.alpha_prior;
                 m1 = m0;
-                if (m0.gamma_on) {
-                    const double rsi0 = 1.0 / m0.alpha;
-                    m1.gamma_on = 0;
+                Mc3Sub &q1 = m1.q[mi];
+                if (q0.gamma_on) {
+                    const double rsi0 = 1.0 / q0.alpha;
+                    q1.gamma_on = 0;
                     pr.lnPrior = log(d.gamma_jump_prior) - log(sp) + sp * rsi0;
                     pr.lnHast = log(sp) - sp * rsi0;
                 } else {
                     const double rsi1 = -log(1.0 - philox_u01(rng)) / sp;
-                    m1.gamma_on = 1;
-                    m1.alpha = 1.0 / rsi1;
+                    q1.gamma_on = 1;
+                    q1.alpha = 1.0 / rsi1;
                     pr.lnPrior = -log(d.gamma_jump_prior) + log(sp) - sp * rsi1;
                     pr.lnHast = -log(sp) + sp * rsi1;
                 }
@@ -816,9 +1010,10 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 // terms do.
                 const double ln6 = 1.791759469228055;
                 m1 = m0;
-                if (m0.freqs_est) {
-                    for (int i = 0; i < 4; ++i) m1.freqs[i] = 0.25;
-                    m1.freqs_est = 0;
+                Mc3Sub &q1 = m1.q[mi];
+                if (q0.freqs_est) {
+                    for (int i = 0; i < 4; ++i) q1.freqs[i] = 0.25;
+                    q1.freqs_est = 0;
                     pr.lnPrior = log(d.freq_jump_prior) - ln6;
                     pr.lnHast = ln6;
                 } else {
@@ -828,8 +1023,8 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                         if (f[i] < 1e-300) f[i] = 1e-300;
                         s += f[i];
                     }
-                    for (int i = 0; i < 4; ++i) m1.freqs[i] = f[i] / s;
-                    m1.freqs_est = 1;
+                    for (int i = 0; i < 4; ++i) q1.freqs[i] = f[i] / s;
+                    q1.freqs_est = 1;
                     pr.lnPrior = -log(d.freq_jump_prior) + ln6;
                     pr.lnHast = -ln6;
                 }
@@ -839,9 +1034,9 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             } else if (t == MV_FREQS) {
                 // Base frequencies ~ Dirichlet(conc * pi).
                 double f0[4], f1[4], a0[4], a1[4], s0 = 0.0, s1 = 0.0;
-                for (int i = 0; i < 4; ++i) s0 += m0.freqs[i];
+                for (int i = 0; i < 4; ++i) s0 += q0.freqs[i];
                 for (int i = 0; i < 4; ++i) {
-                    f0[i] = m0.freqs[i] / s0;
+                    f0[i] = q0.freqs[i] / s0;
                     a0[i] = d.freq_conc * f0[i];
                     f1[i] = philox_gamma(rng, a0[i]);
                     if (f1[i] < 1e-300) f1[i] = 1e-300;
@@ -852,7 +1047,8 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                     a1[i] = d.freq_conc * f1[i];
                 }
                 m1 = m0;
-                for (int i = 0; i < 4; ++i) m1.freqs[i] = f1[i];
+                Mc3Sub &q1 = m1.q[mi];
+                for (int i = 0; i < 4; ++i) q1.freqs[i] = f1[i];
                 pr.lnHast = ln_dirichlet(a1, f0, 4) - ln_dirichlet(a0, f1, 4);
                 pr.model_changed = 1;
                 s_fin = FIN_EIG;
@@ -862,9 +1058,9 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 // classes, their sum kept (the rates' prior, iid Exp(1),
                 // is flat Dirichlet in r / sum r and independent of the
                 // sum).
-                const int k = m0.nrates;
+                const int k = q0.nrates;
                 double r0[6], r1[6], a0[6], a1[6], s0 = 0.0, s1 = 0.0;
-                for (int i = 0; i < 6; ++i) r0[m0.rclass[i]] = m0.rates[i];
+                for (int i = 0; i < 6; ++i) r0[q0.rclass[i]] = q0.rates[i];
                 for (int r = 0; r < k; ++r) s0 += r0[r];
                 for (int r = 0; r < k; ++r) {
                     r0[r] /= s0;
@@ -878,17 +1074,77 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                     a1[r] = d.rate_conc * r1[r];
                 }
                 m1 = m0;
-                for (int i = 0; i < 6; ++i) m1.rates[i] = r1[m0.rclass[i]] * s0;
+                Mc3Sub &q1 = m1.q[mi];
+                for (int i = 0; i < 6; ++i) q1.rates[i] = r1[q0.rclass[i]] * s0;
                 pr.lnHast = ln_dirichlet(a1, r0, k) - ln_dirichlet(a0, r1, k);
                 pr.model_changed = 1;
                 s_fin = FIN_EIG;
                 full = true;
+            } else if (t == MV_WEIGHT || t == MV_RMULT) {
+                // A member's mixture weight or rate multiplier times
+                // exp(lambda (u - 1/2)), Exp(1) prior, Hastings ln m
+                // (weightPropose, rmultPropose, Chain.pyx:72-141, 200-266).
+                const bool wt = t == MV_WEIGHT;
+                const double lnM =
+                    (wt ? d.weight_lambda : d.rmult_lambda) * (philox_u01(rng) - 0.5);
+                m1 = m0;
+                double &x = wt ? m1.q[mi].weight : m1.q[mi].rmult;
+                const double x0 = x, x1 = x0 * exp(lnM);
+                x = x1;
+                pr.lnPrior = -(x1 - x0);
+                pr.lnHast = lnM;
+                pr.model_changed = 1;
+                s_fin = FIN_WEIGHTS;
+                full = true;
+            } else if (t == MV_MIXJ) {
+                // A member added or removed (mixtureJumpPropose,
+                // mixtureAddPropose, mixtureRemovePropose,
+                // Chain.pyx:1633-1814).  Prior: k members with probability
+                // proportional to (1 - mixJumpPrior)^(k-1), k <= mmax, each
+                // drawn from mc3_member_lnprior's density.  Add draws the
+                // new member from that density, appends it and swaps it
+                // with a uniform slot j <= k; remove takes a uniform slot j,
+                // moves the last member there and drops the last: the two
+                // are each other's reverse with the same 1/(k+1) choice.
+                // Add or remove is chosen with probability 1/2 where both
+                // exist.  The member's density is in lnPrior and lnHast and
+                // cancels in the unheated chain.
+                const int k = m0.nmodels;
+                auto p_add = [&](int n) { return n < (int)d.mmax ? (n > 1 ? 0.5 : 1.0) : 0.0; };
+                auto p_rm = [&](int n) { return n > 1 ? (n < (int)d.mmax ? 0.5 : 1.0) : 0.0; };
+                const bool add = k < (int)d.mmax && (k == 1 || philox_below(rng, 2) == 0);
+                const double l1m = log1p(-d.mix_jump_prior);
+                m1 = m0;
+                if (add) {
+                    const unsigned j = philox_below(rng, (uint32_t)(k + 1));
+                    Mc3Sub nq;
+                    const double lnp = mc3_draw_member(nq, m0.q[0], d, rng);
+                    if ((int)j < k) mc3_move_member(m1, j, (unsigned)k);
+                    m1.q[j] = nq;
+                    m1.nmodels = k + 1;
+                    pr.lnPrior = l1m + lnp;
+                    pr.lnHast = log(p_rm(k + 1)) - log(p_add(k)) - lnp;
+                    s_fin = FIN_ALL;
+                    s_fin_mi = j;
+                } else {
+                    const unsigned j = philox_below(rng, (uint32_t)k);
+                    const double lnp = mc3_member_lnprior(m0.q[j], d);
+                    if ((int)j + 1 < k) mc3_move_member(m1, (unsigned)(k - 1), j);
+                    m1.nmodels = k - 1;
+                    pr.lnPrior = -l1m - lnp;
+                    pr.lnHast = log(p_add(k - 1)) - log(p_rm(k)) + lnp;
+                    s_fin = FIN_WEIGHTS;
+                    s_fin_mi = 0;
+                }
+                pr.model_changed = 1;
+                full = true;
             } else {
                 // Inverse Gamma shape multiplier (Chain.pyx:320-377).
                 const double lnM = d.alpha_lambda * (philox_u01(rng) - 0.5);
-                const double a0i = 1.0 / m0.alpha, a1i = a0i * exp(lnM);
+                const double a0i = 1.0 / q0.alpha, a1i = a0i * exp(lnM);
                 m1 = m0;
-                m1.alpha = 1.0 / a1i;
+                Mc3Sub &q1 = m1.q[mi];
+                q1.alpha = 1.0 / a1i;
                 pr.lnPrior = -d.alpha_prior * (a1i - a0i);
                 pr.lnHast = lnM;
                 pr.model_changed = 1;
@@ -896,6 +1152,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 full = true;
             }
         }
+        if (pr.type != MV_MIXJ) s_fin_mi = mi;
         s_full = full;
         s_lowest = lowest;
     }
@@ -936,7 +1193,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
     // 0 lists the dirty nodes and assigns stack slots.
     if (threadIdx.x >= 32 && threadIdx.x < 64 && s_fin) {
         Mc3Model &m1 = d.model[c * 2 + (1 - d.curmodel[c])];
-        const bool ok = mc3_model_finish_warp(m1, d.ncat, d.invar, s_fin);
+        const bool ok = mc3_model_finish_warp(m1, d.ncat, d.invar, d.mmax, s_fin, s_fin_mi);
         if (threadIdx.x == 32 && !ok) {
             // A model that cannot be decomposed is rejected outright.
             pr.lnPrior = -INFINITY;
@@ -1337,8 +1594,12 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     if (!(cfg->pinv >= 0.0 && cfg->pinv < 1.0))
         return fail(CXG_EINVAL, "cxgMc3Create: pinv must be in [0, 1)");
     const unsigned invar = cfg->pinv > 0.0 ? 1u : 0u;
-    if (cfg->ncat < 1 || cfg->ncat + invar > kMaxComps)
-        return fail(CXG_EINVAL, "cxgMc3Create: 1..8 components (rate categories, +I)");
+    const unsigned mmax = cfg->max_models ? cfg->max_models : 1u;
+    if (mmax > (unsigned)kMaxModels)
+        return fail(CXG_EINVAL, "cxgMc3Create: max_models must be 1..4");
+    if (cfg->ncat < 1 || mmax * (cfg->ncat + invar) > kMaxComps)
+        return fail(CXG_EINVAL,
+                    "cxgMc3Create: 1..8 components (max_models x (rate categories, +I))");
     if (cfg->nchains < 1 || cfg->nchains > 1024)
         return fail(CXG_EINVAL, "cxgMc3Create: 1..1024 chains");
     if (cfg->precision != CXG_FP32 && cfg->precision != CXG_FP64)
@@ -1368,9 +1629,11 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     h->cfg = *cfg;
     Mc3Dev &d = h->d;
     memset(&d, 0, sizeof(d));
-    const unsigned C = cfg->nchains, K = cfg->ncat + invar;
+    const unsigned C = cfg->nchains, K = mmax * (cfg->ncat + invar);
     d.ncat = cfg->ncat;
     d.invar = invar;
+    d.kper = cfg->ncat + invar;
+    d.mmax = mmax;
     d.nchains = C;
     d.ntaxa = N;
     d.nnodes = NN;
@@ -1423,6 +1686,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     for (int i = 0; i < kMoves; ++i) {
         acc += mw[i] / wsum;
         d.wcdf[i] = (i == kMoves - 1) ? 2.0 : acc;
+        if (mw[i] > 0.0) d.moves_on |= 1u << i;
     }
     d.brlen_lambda = cfg->brlen_lambda;
     d.brlen_prior = cfg->brlen_prior;
@@ -1442,6 +1706,14 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     d.invar_jump_prior = cfg->invar_jump_prior;
     d.rate_jump_prior = cfg->rate_jump_prior;
     d.rate_lambda = cfg->rate_lambda;
+    d.mix_jump_prior = cfg->mixture_jump_prior;
+    d.weight_lambda = cfg->weight_lambda;
+    d.rmult_lambda = cfg->rmult_lambda;
+    if (mw[MV_MIXJ] > 0.0 && mmax > 1 &&
+        !(cfg->mixture_jump_prior >= 0.0 && cfg->mixture_jump_prior < 1.0)) {
+        mc3_free(h);
+        return fail(CXG_EINVAL, "cxgMc3Create: mixture_jump_prior must be in [0, 1)");
+    }
     // Rate classes: a restricted growth string, equal rates within a class.
     int nrates = 0;
     for (int i = 0; i < 6; ++i) {
@@ -1492,17 +1764,21 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     std::vector<Mc3Model> models((size_t)C * 2);
     for (auto &m : models) {
         memset(&m, 0, sizeof(m));
-        for (int i = 0; i < 6; ++i) m.rates[i] = cfg->rates[i];
-        for (int i = 0; i < 6; ++i) m.rclass[i] = cfg->rclass[i];
-        m.nrates = nrates;
-        for (int i = 0; i < 4; ++i) m.freqs[i] = cfg->freqs[i];
-        m.alpha = cfg->alpha;
-        m.wvar = invar ? 1.0 - cfg->pinv : 1.0;
-        m.winvar = invar ? cfg->pinv : 0.0;
-        m.gamma_on = cfg->ncat > 1 ? 1 : 0;
+        m.nmodels = 1;
+        Mc3Sub &q = m.q[0];
+        for (int i = 0; i < 6; ++i) q.rates[i] = cfg->rates[i];
+        for (int i = 0; i < 6; ++i) q.rclass[i] = cfg->rclass[i];
+        q.nrates = nrates;
+        for (int i = 0; i < 4; ++i) q.freqs[i] = cfg->freqs[i];
+        q.alpha = cfg->alpha;
+        q.wvar = invar ? 1.0 - cfg->pinv : 1.0;
+        q.winvar = invar ? cfg->pinv : 0.0;
+        q.gamma_on = cfg->ncat > 1 ? 1 : 0;
         // Equal frequencies start in the equal state (Chain.freqsEqual).
-        m.freqs_est = !(cfg->freqs[0] == cfg->freqs[1] && cfg->freqs[1] == cfg->freqs[2] &&
+        q.freqs_est = !(cfg->freqs[0] == cfg->freqs[1] && cfg->freqs[1] == cfg->freqs[2] &&
                         cfg->freqs[2] == cfg->freqs[3]);
+        q.weight = 1.0;
+        q.rmult = 1.0;
     }
     // Leaf masks (0 = any state, as Lik.pyx:1469-1470), pattern weights.
     std::vector<uint8_t> masks((size_t)N * d.ppad, 15);
@@ -1766,10 +2042,39 @@ extern "C" int cxgMc3Chain(cxgMc3 *h, unsigned chain, double *lnL, double *heat,
     CXG_CUDA(cudaMemcpy(&cm, d.curmodel + chain, 1, cudaMemcpyDeviceToHost));
     Mc3Model m;
     CXG_CUDA(cudaMemcpy(&m, d.model + chain * 2 + cm, sizeof(m), cudaMemcpyDeviceToHost));
-    if (rates) memcpy(rates, m.rates, 48);
-    if (freqs) memcpy(freqs, m.freqs, 32);
+    const Mc3Sub &q = m.q[0];
+    if (rates) memcpy(rates, q.rates, 48);
+    if (freqs) memcpy(freqs, q.freqs, 32);
     // Gamma rates switched off read as the reference's alpha = INFINITY.
-    if (alpha) *alpha = (d.ncat > 1 && !m.gamma_on) ? INFINITY : m.alpha;
+    if (alpha) *alpha = (d.ncat > 1 && !q.gamma_on) ? INFINITY : q.alpha;
+    return 0;
+}
+
+extern "C" int cxgMc3ChainModel(cxgMc3 *h, unsigned chain, unsigned model,
+                                unsigned *nmodels, cxgMc3ModelState *out) {
+    if (h == nullptr || chain >= h->d.nchains || model >= (unsigned)kMaxModels)
+        return fail(CXG_EINVAL, "cxgMc3ChainModel: bad chain or model");
+    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    const Mc3Dev &d = h->d;
+    CXG_CUDA(cudaStreamSynchronize(h->stream));
+    uint8_t cm = 0;
+    CXG_CUDA(cudaMemcpy(&cm, d.curmodel + chain, 1, cudaMemcpyDeviceToHost));
+    Mc3Model m;
+    CXG_CUDA(cudaMemcpy(&m, d.model + chain * 2 + cm, sizeof(m), cudaMemcpyDeviceToHost));
+    if (nmodels) *nmodels = (unsigned)m.nmodels;
+    if (out == nullptr) return 0;
+    if ((int)model >= m.nmodels) return fail(CXG_EINVAL, "cxgMc3ChainModel: no such model");
+    const Mc3Sub &q = m.q[model];
+    memcpy(out->rates, q.rates, 48);
+    memcpy(out->freqs, q.freqs, 32);
+    out->alpha = (d.ncat > 1 && !q.gamma_on) ? INFINITY : q.alpha;
+    out->wvar = q.wvar;
+    out->winvar = q.winvar;
+    out->weight = q.weight;
+    out->rmult = q.rmult;
+    for (int i = 0; i < 6; ++i) out->rclass[i] = q.rclass[i];
+    out->nrates = q.nrates;
+    out->freqs_est = q.freqs_est;
     return 0;
 }
 
@@ -1783,8 +2088,8 @@ extern "C" int cxgMc3ChainWeights(cxgMc3 *h, unsigned chain, double *wvar, doubl
     CXG_CUDA(cudaMemcpy(&cm, d.curmodel + chain, 1, cudaMemcpyDeviceToHost));
     Mc3Model m;
     CXG_CUDA(cudaMemcpy(&m, d.model + chain * 2 + cm, sizeof(m), cudaMemcpyDeviceToHost));
-    if (wvar) *wvar = m.wvar;
-    if (winvar) *winvar = m.winvar;
+    if (wvar) *wvar = m.q[0].wvar;
+    if (winvar) *winvar = m.q[0].winvar;
     return 0;
 }
 

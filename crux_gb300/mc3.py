@@ -21,7 +21,9 @@ from .tree import Tree
 
 LAMBDA = 2.0 * math.log(1.6)
 MOVES = ("brlen", "nni", "rates", "alpha", "freqs", "spr", "etbr", "invar",
-         "gammajump", "freqjump", "invarjump", "ratejump", "rate")
+         "gammajump", "freqjump", "invarjump", "ratejump", "rate", "weight",
+         "rmult", "mixturejump")
+MAX_MODELS = 4
 
 
 class Mc3Config(ctypes.Structure):
@@ -41,7 +43,7 @@ class Mc3Config(ctypes.Structure):
         ("heat_delta", ctypes.c_double),
         ("swap_stride", ctypes.c_uint),
         ("seed", ctypes.c_ulonglong),
-        ("move_weight", ctypes.c_double * 13),
+        ("move_weight", ctypes.c_double * 16),
         ("brlen_lambda", ctypes.c_double),
         ("brlen_prior", ctypes.c_double),
         ("rate_conc", ctypes.c_double),
@@ -61,6 +63,25 @@ class Mc3Config(ctypes.Structure):
         ("rclass", ctypes.c_int * 6),
         ("rate_jump_prior", ctypes.c_double),
         ("rate_lambda", ctypes.c_double),
+        ("max_models", ctypes.c_uint),
+        ("mixture_jump_prior", ctypes.c_double),
+        ("weight_lambda", ctypes.c_double),
+        ("rmult_lambda", ctypes.c_double),
+    ]
+
+
+class Mc3ModelState(ctypes.Structure):
+    _fields_ = [
+        ("rates", ctypes.c_double * 6),
+        ("freqs", ctypes.c_double * 4),
+        ("alpha", ctypes.c_double),
+        ("wvar", ctypes.c_double),
+        ("winvar", ctypes.c_double),
+        ("weight", ctypes.c_double),
+        ("rmult", ctypes.c_double),
+        ("rclass", ctypes.c_int * 6),
+        ("nrates", ctypes.c_int),
+        ("freqs_est", ctypes.c_int),
     ]
 
 
@@ -79,6 +100,9 @@ def declare(lib):
     lib.cxgMc3ChainWeights.argtypes = [vp, ctypes.c_uint, P(ctypes.c_double),
                                        P(ctypes.c_double)]
     lib.cxgMc3ChainWeights.restype = ctypes.c_int
+    lib.cxgMc3ChainModel.argtypes = [vp, ctypes.c_uint, ctypes.c_uint,
+                                     P(ctypes.c_uint), P(Mc3ModelState)]
+    lib.cxgMc3ChainModel.restype = ctypes.c_int
     lib.cxgMc3Stats.argtypes = [vp, P(ctypes.c_uint), P(ctypes.c_uint),
                                 P(ctypes.c_uint), P(ctypes.c_ulonglong)]
     lib.cxgMc3Stats.restype = ctypes.c_int
@@ -160,6 +184,8 @@ class Mc3:
                  etbr_pext=0.8, pinv=0.0, invar_lambda=LAMBDA, invar_prior=0.5,
                  gamma_jump_prior=1.0, freq_jump_prior=1.0, invar_jump_prior=1.0,
                  rclass=(0, 1, 2, 3, 4, 5), rate_jump_prior=1.0, rate_lambda=LAMBDA,
+                 max_models=1, mixture_jump_prior=1.0 / 3.0,
+                 weight_lambda=LAMBDA, rmult_lambda=LAMBDA,
                  alpha_lambda=LAMBDA,
                  alpha_prior=1.0, graph_gens=16, trace_cap=1 << 20, lib=None):
         self.lib = lib or _native.load()
@@ -212,6 +238,10 @@ class Mc3:
             c.rclass[i] = int(rclass[i])
         c.rate_jump_prior = rate_jump_prior
         c.rate_lambda = rate_lambda
+        c.max_models = max_models
+        c.mixture_jump_prior = mixture_jump_prior
+        c.weight_lambda = weight_lambda
+        c.rmult_lambda = rmult_lambda
         c.alpha_lambda = alpha_lambda
         c.alpha_prior = alpha_prior
         c.precision = 1 if precision == "fp32" else 0
@@ -258,7 +288,29 @@ class Mc3:
         rclass = [seen.setdefault(float(x), len(seen)) for x in rates]
         return {"lnL": lnl.value, "heat": heat.value, "parent": par,
                 "len": ln, "rates": rates, "rclass": rclass, "freqs": freqs,
-                "alpha": alpha.value, "wvar": wv.value, "winvar": wi.value}
+                "alpha": alpha.value, "wvar": wv.value, "winvar": wi.value,
+                "models": self.chain_models(i)}
+
+    def chain_models(self, i):
+        """Chain i's mixture members: one dict of parameters each."""
+        n = ctypes.c_uint()
+        self._check(self.lib.cxgMc3ChainModel(self.h, i, 0, ctypes.byref(n),
+                                              None), "cxgMc3ChainModel")
+        out = []
+        for m in range(n.value):
+            st = Mc3ModelState()
+            self._check(self.lib.cxgMc3ChainModel(self.h, i, m, None,
+                                                  ctypes.byref(st)),
+                        "cxgMc3ChainModel")
+            out.append({"rates": [st.rates[j] for j in range(6)],
+                        "rclass": [st.rclass[j] for j in range(6)],
+                        "nrates": st.nrates,
+                        "freqs": [st.freqs[j] for j in range(4)],
+                        "freqs_est": bool(st.freqs_est),
+                        "alpha": st.alpha, "wvar": st.wvar,
+                        "winvar": st.winvar, "weight": st.weight,
+                        "rmult": st.rmult})
+        return out
 
     def stats(self):
         n = self.nchains * len(MOVES)
@@ -291,16 +343,22 @@ class Mc3:
         t = Tree(nw)
         t.deroot()
         t.canonize(aln.taxaMap)
-        lik = Lik(t, aln, ncat=self.ncat, invar=self.invar, lib=lib,
-                  precision=precision)
-        lik.setRclass(0, [0, 1, 2, 3, 4, 5], [float(x) for x in st["rates"]])
-        for j in range(4):
-            lik.setFreq(0, j, float(st["freqs"][j]))
-        if self.ncat > 1:
-            lik.setAlpha(0, float(st["alpha"]))
-        if self.invar:
-            lik.setWVar(0, st["wvar"])
-            lik.setWInvar(0, st["winvar"])
+        models = st["models"]
+        lik = Lik(t, aln, nmodels=len(models), ncat=self.ncat,
+                  invar=self.invar, lib=lib, precision=precision)
+        for m, q in enumerate(models):
+            lik.setRclass(m, [0, 1, 2, 3, 4, 5],
+                          [float(x) for x in q["rates"]])
+            for j in range(4):
+                lik.setFreq(m, j, float(q["freqs"][j]))
+            if self.ncat > 1:
+                lik.setAlpha(m, float(q["alpha"]))
+            if self.invar:
+                lik.setWVar(m, q["wvar"])
+                lik.setWInvar(m, q["winvar"])
+            if len(models) > 1:
+                lik.setWeight(m, q["weight"])
+                lik.setRmult(m, q["rmult"])
         return lik, st
 
     def close(self):

@@ -320,12 +320,14 @@ typedef struct {
     double heat_delta;  /* chain i runs at heat 1/(1 + i*heat_delta) */
     unsigned swap_stride;
     unsigned long long seed;
-    double move_weight[13]; /* branch length, NNI, rates (Dirichlet over
+    double move_weight[16]; /* branch length, NNI, rates (Dirichlet over
                                the class rates), alpha, base frequencies,
                                SPR, eTBR, +I weights, Gamma on/off jump,
                                equal/estimated frequency jump, +I off/on
                                jump, rate-class merge/split jump, one
-                               class rate's multiplier */
+                               class rate's multiplier, mixture weight,
+                               mixture rate multiplier, mixture member
+                               add/remove jump */
     double brlen_lambda, brlen_prior;
     double rate_conc;       /* Dirichlet concentration of rate moves */
     double freq_conc;       /* Dirichlet concentration of frequency moves */
@@ -353,20 +355,37 @@ typedef struct {
     double rate_jump_prior; /* the reference's rateJumpPrior (1): prior
                                odds of k-1 to k rate classes */
     double rate_lambda;     /* class-rate multiplier (2 ln 1.6) */
+    unsigned max_models;    /* mixture members a chain may hold, 1..4 (0:
+                               1); the walker carries max_models x (ncat
+                               + +I) components, at most 8 */
+    double mixture_jump_prior; /* the reference's mixtureJumpPrior (1/3):
+                               k + 1 members have prior odds
+                               1 - mixture_jump_prior to k */
+    double weight_lambda, rmult_lambda; /* mixture weight and rate
+                               multiplier moves (2 ln 1.6) */
 } cxgMc3Config;
+/* One mixture member of a chain (alpha is INFINITY with Gamma off). */
+typedef struct {
+    double rates[6], freqs[4], alpha, wvar, winvar, weight, rmult;
+    int rclass[6], nrates, freqs_est;
+} cxgMc3ModelState;
 typedef struct cxgMc3 cxgMc3;
 /* Build the chains and run generation 0 (a full evaluation). */
 int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **mc3);
 /* Advance every chain `ngen` generations (one move each, then a heat-swap
  * attempt every swap_stride); *seconds = device time. */
 int cxgMc3Run(cxgMc3 *mc3, unsigned long long ngen, double *seconds);
-/* Current state of one chain (tree in the same node numbering). */
+/* Current state of one chain (tree in the same node numbering; the model
+ * parameters are its first mixture member's). */
 int cxgMc3Chain(cxgMc3 *mc3, unsigned chain, double *lnL, double *heat,
                 int32_t *parent, double *len, double *rates, double *freqs,
                 double *alpha);
-/* Mixture weights (wVar, wInvar) of one chain's current model. */
+/* Weights (wVar, wInvar) of one chain's first mixture member. */
 int cxgMc3ChainWeights(cxgMc3 *mc3, unsigned chain, double *wvar, double *winvar);
-/* Accept/reject counts [chain][move] (13 moves, in move_weight order),
+/* Member `model` of one chain's mixture, and the member count. */
+int cxgMc3ChainModel(cxgMc3 *mc3, unsigned chain, unsigned model,
+                     unsigned *nmodels, cxgMc3ModelState *out);
+/* Accept/reject counts [chain][move] (16 moves, in move_weight order),
  * swaps [chain], generation count. */
 int cxgMc3Stats(cxgMc3 *mc3, unsigned *accepts, unsigned *rejects,
                 unsigned *swaps, unsigned long long *gen);

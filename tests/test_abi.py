@@ -88,7 +88,9 @@ def test_extension_struct_layouts_match_header():
     (crux_gb300.mc3, crux_gb300.serve, crux_gb300._abi) have the header's
     field offsets and sizes."""
     from crux_gb300 import mc3, serve
-    pairs = [("cxgMc3Config", mc3.Mc3Config), ("cxgRequest", serve.Request),
+    pairs = [("cxgMc3Config", mc3.Mc3Config),
+             ("cxgMc3ModelState", mc3.Mc3ModelState),
+             ("cxgRequest", serve.Request),
              ("cxgServerConfig", serve.ServerConfig),
              ("cxgServerStatsT", serve.ServerStats),
              ("cxgPlanSnap", _abi.CxgPlanSnap)]

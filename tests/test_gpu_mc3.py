@@ -402,3 +402,73 @@ def test_mc3_rate_jump_samples_its_prior(gpu):
     assert np.all(np.abs(frac - 1.0 / 6.0) < 0.05), frac
     assert len(parts) == 31
     assert abs(np.mean(r0) - 1.0) < 0.15, np.mean(r0)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_mc3_mixture_chains_match_oracle(gpu, port, precision):
+    """Mixture members added and removed (mixtureJumpPropose,
+    Chain.pyx:1633-1814), their weights and rate multipliers moved
+    (weightPropose, rmultPropose, :72-141, 200-266) beside per-member
+    model moves: every chain's lnL is the oracle's for a Lik holding the
+    chain's members (nmodels, setWeight, setRmult and each member's
+    parameters)."""
+    case = synth.Case(14, 150, 0.1, 61)
+    aln = case.alignment()
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=0.5,
+            ncat=4, nchains=4, heat_delta=0.5, seed=21,
+            moves={"brlen": 1.0, "mixturejump": 2.0, "weight": 1.0,
+                   "rmult": 1.0, "alpha": 0.5, "rates": 0.5, "freqs": 0.5,
+                   "freqjump": 0.5, "gammajump": 0.5},
+            max_models=2, mixture_jump_prior=0.2, precision=precision,
+            graph_gens=8)
+    seen = set()
+    for _ in range(12):
+        m.run(24)
+        check_chains(m, port, TOL[precision])
+        for i in range(4):
+            seen.add(len(m.chain_models(i)))
+    st = m.stats()
+    acc = st["accepts"].sum(axis=0)
+    assert acc[15] > 0, acc
+    assert acc[13] > 0 and acc[14] > 0, acc
+    assert seen == {1, 2}, seen
+    m.close()
+
+
+def test_mc3_mixture_jump_samples_its_prior(gpu):
+    """Without data the mixture moves sample their prior: k members with
+    probability proportional to (1 - mixtureJumpPrior)^(k-1) for k <= 4,
+    member weights and rate multipliers of mean 1 (Exp(1)), estimated base
+    frequencies in half the members (freqJumpPrior 1) and class rates of
+    mean 1.  A wrong Hastings ratio or member density moves the counts."""
+    case, aln = _empty_alignment(6, 35)
+    t = case.tree(aln.taxaMap)
+    mjp = 1.0 / 3.0
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=None,
+            nchains=8, heat_delta=0.0, seed=8, precision="fp64", graph_gens=32,
+            moves={"mixturejump": 2.0, "weight": 1.0, "rmult": 1.0,
+                   "rates": 0.5, "freqs": 0.5, "freqjump": 1.0},
+            max_models=4, mixture_jump_prior=mjp)
+    m.run(2000)
+    ks, w, rm, est, r0 = [], [], [], [], []
+    for _ in range(1200):
+        m.run(32)
+        for i in range(8):
+            ms = m.chain_models(i)
+            ks.append(len(ms))
+            for q in ms:
+                w.append(q["weight"])
+                rm.append(q["rmult"])
+                est.append(q["freqs_est"])
+                r0.append(q["rates"][0])
+        assert abs(m.chain_state(0)["lnL"]) < 1e-9
+    m.close()
+    want = np.array([(1.0 - mjp) ** (k - 1) for k in range(1, 5)])
+    want /= want.sum()
+    frac = np.bincount(ks, minlength=5)[1:] / len(ks)
+    assert np.all(np.abs(frac - want) < 0.04), (frac, want)
+    assert abs(np.mean(w) - 1.0) < 0.12, np.mean(w)
+    assert abs(np.mean(rm) - 1.0) < 0.12, np.mean(rm)
+    assert abs(np.mean(est) - 0.5) < 0.06, np.mean(est)
+    assert abs(np.mean(r0) - 1.0) < 0.15, np.mean(r0)
