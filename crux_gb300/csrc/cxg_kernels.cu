@@ -406,6 +406,33 @@ __device__ __forceinline__ X group_max(X x) {
     return x;
 }
 
+// The plain form's scaler: the max over child messages of doubles that are
+// >= 0 (P entries are clamped at 0, CL rows are their products), taken on
+// the bit patterns with integer compares, which order non-negative doubles
+// as their values.  The value is fmax's, and the FP64 pipe, which bounds
+// the plain form, does no max work.  (A NaN entry would win here where
+// fmax skips it; a pattern with a NaN entry ends with a NaN site lnL
+// either way, since the entry is in the parent's rows.)
+__device__ __forceinline__ double max_nonneg(double a, double b) {
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return __longlong_as_double(x > y ? x : y);
+}
+template <int N>
+__device__ __forceinline__ double tree_max_nonneg(const double *v) {
+    if constexpr (N == 1) {
+        return v[0];
+    } else {
+        constexpr int H = N / 2;
+        return max_nonneg(tree_max_nonneg<H>(v), tree_max_nonneg<N - H>(v + H));
+    }
+}
+template <int G>
+__device__ __forceinline__ double group_max_nonneg(double x) {
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1) x = max_nonneg(x, __shfl_xor_sync(0xffffffffu, x, o));
+    return x;
+}
+
 // --- FP32 two-child ops by kind (one thread per pattern) --------------------
 // Row r of a P matrix against the four states x of one component, in the
 // order of the general path (a product, then three fused adds).
@@ -773,7 +800,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
 #pragma unroll
                 for (int q = 0; q < KT * 4; ++q) acc[q] *= msg[q];
             }
-            if (sizeof(T) == 8) sc = fmax(sc, tree_max<KT * 4>(msg));
+            if constexpr (sizeof(T) == 8) sc = max_nonneg(sc, tree_max_nonneg<KT * 4>(msg));
         };
         // A two-child FP32 op whose kind the host set runs straight-line
         // code for its kind (the general path below gives the same bits).
@@ -870,7 +897,7 @@ __device__ bool walk_tile(const PlanArgs &a, unsigned tile_idx,
         // An empty lane of a step (no children) computes and stores nothing.
         if (L > 1 && nchild == 0) continue;
         if (sizeof(T) == 8) {
-            sc = group_max<G>(sc);
+            if constexpr (sizeof(T) == 8) sc = group_max_nonneg<G>(sc);
             // Reference rescale: divide by the scaler unless it is 1, add
             // its log (a zero scaler gives NaN rows and a -inf site, as in
             // the reference).
