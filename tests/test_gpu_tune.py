@@ -155,3 +155,47 @@ def test_mc3_and_server_follow_the_shape(gpu, restore):
         srv.close()
     assert all(np.array_equal(traces[0], t) for t in traces[1:])
     assert all(s == served[0] for s in served[1:])
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_streamed_leaves_every_shape(gpu, port, restore, precision):
+    """A 300-taxon tree: at tile 64 and 128 its leaf masks exceed the
+    staging budget (16 KiB a tile), so each op's leaf rows travel with its
+    record (streamed leaves) and the FP32 op kinds read a leaf's row by its
+    rank among the op's leaf children.  Every shape gives the same bits as
+    the staged tile-32 shape, within the oracle tolerance, full and after a
+    dirty path; so does a batch holding the tree."""
+    case = synth.Case(300, 400, 0.1, 303, gap_frac=0.01)
+    lo = case.lik(lib=port)
+    want = lo.lnL()
+    lik = case.lik(lib=gpu, precision=precision)
+    lik.lnL()
+    first = None
+    for shape in tune.candidates(precision, 4, budgets=(0, 24 << 10), lanes=(1,)):
+        tune.set_shape(gpu, *shape)
+        lik.lik.invalidate = True
+        v = lik.lnL()
+        if first is None:
+            first = v
+            assert abs(v - want) <= TOL[precision] * abs(want), (v, want)
+        else:
+            assert v == first, shape
+    e_lo, e_g = lo.tree.edges[7], lik.tree.edges[7]
+    old = e_g.length
+    e_lo.length = old * 1.4
+    want2 = lo.lnL()
+    for shape in [(128, 1, 1, 0), (64, 1, 1, 24 << 10), (32, 1, 1, 0)]:
+        tune.set_shape(gpu, *shape)
+        e_g.length = old
+        lik.lik.invalidate = True
+        lik.lnL()
+        e_g.length = old * 1.4
+        v2 = lik.lnL()  # a dirty path
+        assert abs(v2 - want2) <= TOL[precision] * abs(want2), (shape, v2, want2)
+    if precision == "fp32":
+        tune.set_shape(gpu, 128, 1, 1, 0)
+        lik.prepare_plan()
+        b = Batch([lik], "fp32")
+        got = b.run()
+        b.close()
+        assert abs(got[0] - want2) <= TOL["fp32"] * abs(want2)
