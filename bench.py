@@ -786,8 +786,12 @@ def run_dirty(args, dist):
         clocks = Clocks()
         if prec == "fp32":
             clocks.start()
-        vals, secs, nodes = replay(lik, count_updates=True)
+        vals, secs, _ = replay(lik)
         ck = clocks.stop() if prec == "fp32" else None
+        # Node updates per recompute, counted on an untimed replay of the
+        # same rescales (the same dirty paths).
+        _, _, nodes = replay(case.lik(lib=gpu, precision=prec, alignment=aln),
+                             count_updates=True)
         # Device time of one dirty path: the next rescale's plan, rerun.
         lik.tree.edges[0].length *= 1.25
         lik.prepare_plan(full=False)
