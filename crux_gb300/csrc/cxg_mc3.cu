@@ -2054,6 +2054,143 @@ extern "C" int cxgMc3Chain(cxgMc3 *h, unsigned chain, double *lnL, double *heat,
     return 0;
 }
 
+// Checkpoint and resume.  A chain's state is its tree, heat and mixture
+// members (cxgMc3Chain, cxgMc3ChainModel); with the generation count and
+// the move counts it is all that a run carries from one generation to the
+// next, since every draw comes from Philox keyed by (seed, chain,
+// generation).  CLs are not saved: cxgMc3Resume recomputes them.
+
+// Chain `chain` takes this tree (rooted at the run's root), heat and
+// mixture.  Call cxgMc3Resume before running.
+extern "C" int cxgMc3SetChain(cxgMc3 *h, unsigned chain, const int32_t *parent,
+                              const double *len, double heat, unsigned nmodels,
+                              const cxgMc3ModelState *models) {
+    if (h == nullptr || chain >= h->d.nchains || parent == nullptr || len == nullptr ||
+        models == nullptr)
+        return fail(CXG_EINVAL, "cxgMc3SetChain: bad arguments");
+    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    Mc3Dev &d = h->d;
+    const unsigned N = d.ntaxa, NN = d.nnodes;
+    if (nmodels < 1 || nmodels > d.mmax)
+        return fail(CXG_EINVAL, "cxgMc3SetChain: 1..max_models members");
+    if (!(heat > 0.0 && heat <= 1.0)) return fail(CXG_EINVAL, "cxgMc3SetChain: heat in (0, 1]");
+    std::vector<int32_t> child(NN * 3, -1);
+    std::vector<int> nch(NN, 0);
+    for (unsigned v = 0; v < NN; ++v) {
+        const int p = parent[v];
+        if (v == d.root) {
+            if (p != -1) return fail(CXG_EINVAL, "cxgMc3SetChain: root has a parent");
+            continue;
+        }
+        if (p < (int)N || p >= (int)NN || nch[p] >= 3)
+            return fail(CXG_EINVAL, "cxgMc3SetChain: not a binary tree at the run's root");
+        if (!(len[v] >= 0.0)) return fail(CXG_EINVAL, "cxgMc3SetChain: negative length");
+        child[p * 3 + nch[p]++] = (int)v;
+    }
+    for (unsigned v = N; v < NN; ++v)
+        if (nch[v] != (v == d.root ? 3 : 2))
+            return fail(CXG_EINVAL, "cxgMc3SetChain: tree is not binary (root degree 3)");
+    Mc3Model m;
+    memset(&m, 0, sizeof(m));
+    m.nmodels = (int32_t)nmodels;
+    for (unsigned k = 0; k < nmodels; ++k) {
+        const cxgMc3ModelState &s = models[k];
+        Mc3Sub &q = m.q[k];
+        int nr = 0;
+        for (int i = 0; i < 6; ++i) {
+            const int r = s.rclass[i];
+            if (r < 0 || r > nr) return fail(CXG_EINVAL, "cxgMc3SetChain: rclass is not an RGS");
+            if (r == nr) ++nr;
+            for (int j = 0; j < i; ++j)
+                if (s.rclass[j] == r && s.rates[j] != s.rates[i])
+                    return fail(CXG_EINVAL, "cxgMc3SetChain: rates of one class differ");
+            if (!(s.rates[i] > 0.0)) return fail(CXG_EINVAL, "cxgMc3SetChain: rates must be > 0");
+            q.rates[i] = s.rates[i];
+            q.rclass[i] = r;
+        }
+        q.nrates = nr;
+        for (int i = 0; i < 4; ++i) {
+            if (!(s.freqs[i] > 0.0)) return fail(CXG_EINVAL, "cxgMc3SetChain: freqs must be > 0");
+            q.freqs[i] = s.freqs[i];
+        }
+        q.freqs_est = s.freqs_est ? 1 : 0;
+        q.gamma_on = (d.ncat > 1 && !isinf(s.alpha)) ? 1 : 0;
+        q.alpha = isinf(s.alpha) ? 1.0 : s.alpha;
+        if (q.gamma_on && !(q.alpha > 0.0)) return fail(CXG_EINVAL, "cxgMc3SetChain: alpha");
+        q.wvar = d.invar ? s.wvar : 1.0;
+        q.winvar = d.invar ? s.winvar : 0.0;
+        q.weight = s.weight;
+        q.rmult = s.rmult;
+        if (!(q.wvar > 0.0 && q.winvar >= 0.0 && q.weight > 0.0 && q.rmult > 0.0))
+            return fail(CXG_EINVAL, "cxgMc3SetChain: weights must be positive");
+    }
+    CXG_CUDA(cudaStreamSynchronize(h->stream));
+    const size_t t0 = (size_t)0 * d.nchains + chain, t1 = (size_t)1 * d.nchains + chain;
+    for (size_t t : {t0, t1}) {
+        CXG_CUDA(cudaMemcpy(d.parent + t * NN, parent, NN * 4, cudaMemcpyHostToDevice));
+        CXG_CUDA(cudaMemcpy(d.child + t * NN * 3, child.data(), NN * 12, cudaMemcpyHostToDevice));
+        CXG_CUDA(cudaMemcpy(d.len + t * NN, len, NN * 8, cudaMemcpyHostToDevice));
+    }
+    const uint8_t zero = 0;
+    CXG_CUDA(cudaMemcpy(d.curtree + chain, &zero, 1, cudaMemcpyHostToDevice));
+    CXG_CUDA(cudaMemcpy(d.curmodel + chain, &zero, 1, cudaMemcpyHostToDevice));
+    CXG_CUDA(cudaMemcpy(d.model + (size_t)chain * 2, &m, sizeof(m), cudaMemcpyHostToDevice));
+    CXG_CUDA(cudaMemcpy(d.heat + chain, &heat, 8, cudaMemcpyHostToDevice));
+    return 0;
+}
+
+// Per-chain accept and reject counts ([chain][move], kMoves moves) and
+// swap counts, as cxgMc3Stats gives them.
+extern "C" int cxgMc3SetCounts(cxgMc3 *h, const unsigned *accepts, const unsigned *rejects,
+                               const unsigned *swaps) {
+    if (h == nullptr) return fail(CXG_EINVAL, "cxgMc3SetCounts: NULL");
+    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    const Mc3Dev &d = h->d;
+    CXG_CUDA(cudaStreamSynchronize(h->stream));
+    if (accepts)
+        CXG_CUDA(cudaMemcpy(d.acc, accepts, (size_t)d.nchains * kMoves * 4,
+                            cudaMemcpyHostToDevice));
+    if (rejects)
+        CXG_CUDA(cudaMemcpy(d.rej, rejects, (size_t)d.nchains * kMoves * 4,
+                            cudaMemcpyHostToDevice));
+    if (swaps) CXG_CUDA(cudaMemcpy(d.nswap, swaps, d.nchains * 4, cudaMemcpyHostToDevice));
+    return 0;
+}
+
+// Recompute every chain's CLs and lnL from its tree and mixture (a full
+// evaluation, as generation 0 does), then continue at `generation`: the
+// next generation draws what an uninterrupted run draws there.
+extern "C" int cxgMc3Resume(cxgMc3 *h, unsigned long long generation) {
+    if (h == nullptr) return fail(CXG_EINVAL, "cxgMc3Resume: NULL");
+    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    Mc3Dev &d = h->d;
+    CXG_CUDA(cudaStreamSynchronize(h->stream));
+    // No previous move to flip in; generation 0 is the full evaluation.
+    std::vector<Mc3Prop> props(d.nchains);
+    memset(props.data(), 0, props.size() * sizeof(Mc3Prop));
+    CXG_CUDA(cudaMemcpy(d.prop, props.data(), props.size() * sizeof(Mc3Prop),
+                        cudaMemcpyHostToDevice));
+    const unsigned long long g0 = 0;
+    CXG_CUDA(cudaMemcpy(d.gen, &g0, 8, cudaMemcpyHostToDevice));
+    const uint32_t st0 = 0;
+    CXG_CUDA(cudaMemcpy(d.status, &st0, 4, cudaMemcpyHostToDevice));
+    mc3_init_kernel<<<d.nchains, 32, 0, h->stream>>>(d);
+    CXG_CHECK_LAUNCH("mc3_init_kernel");
+    int rc = mc3_enqueue_gen(h);
+    if (rc) return rc;
+    uint32_t st = 0;
+    CXG_CUDA(cudaMemcpyAsync(&st, d.status, 4, cudaMemcpyDeviceToHost, h->stream));
+    CXG_CUDA(cudaStreamSynchronize(h->stream));
+    if (st & 1u) return fail(CXG_EINVAL, "cxgMc3Resume: a model cannot be decomposed");
+    std::vector<char> res((size_t)d.nchains * 32);
+    CXG_CUDA(cudaMemcpy(res.data(), d.results, res.size(), cudaMemcpyDeviceToHost));
+    for (unsigned c = 0; c < d.nchains; ++c)
+        if (*(const uint32_t *)(res.data() + (size_t)c * 32 + 8))
+            return fail(CXG_ETIMEOUT, "MC3 walker: a record copy timed out");
+    CXG_CUDA(cudaMemcpy(d.gen, &generation, 8, cudaMemcpyHostToDevice));
+    return 0;
+}
+
 extern "C" int cxgMc3ChainModel(cxgMc3 *h, unsigned chain, unsigned model,
                                 unsigned *nmodels, cxgMc3ModelState *out) {
     if (h == nullptr || chain >= h->d.nchains || model >= (unsigned)kMaxModels)

@@ -103,6 +103,15 @@ def declare(lib):
     lib.cxgMc3ChainModel.argtypes = [vp, ctypes.c_uint, ctypes.c_uint,
                                      P(ctypes.c_uint), P(Mc3ModelState)]
     lib.cxgMc3ChainModel.restype = ctypes.c_int
+    lib.cxgMc3SetChain.argtypes = [vp, ctypes.c_uint, P(ctypes.c_int32),
+                                   P(ctypes.c_double), ctypes.c_double,
+                                   ctypes.c_uint, P(Mc3ModelState)]
+    lib.cxgMc3SetChain.restype = ctypes.c_int
+    lib.cxgMc3SetCounts.argtypes = [vp, P(ctypes.c_uint), P(ctypes.c_uint),
+                                    P(ctypes.c_uint)]
+    lib.cxgMc3SetCounts.restype = ctypes.c_int
+    lib.cxgMc3Resume.argtypes = [vp, ctypes.c_ulonglong]
+    lib.cxgMc3Resume.restype = ctypes.c_int
     lib.cxgMc3Stats.argtypes = [vp, P(ctypes.c_uint), P(ctypes.c_uint),
                                 P(ctypes.c_uint), P(ctypes.c_ulonglong)]
     lib.cxgMc3Stats.restype = ctypes.c_int
@@ -311,6 +320,60 @@ class Mc3:
                         "winvar": st.winvar, "weight": st.weight,
                         "rmult": st.rmult})
         return out
+
+    def checkpoint(self):
+        """The run's state as plain data: the generation count, each
+        chain's tree, heat and mixture members, and the move and swap
+        counts.  CLs are not saved; ``restore`` recomputes them."""
+        st = self.stats()
+        chains = []
+        for i in range(self.nchains):
+            cs = self.chain_state(i)
+            chains.append({"parent": cs["parent"].tolist(),
+                           "len": cs["len"].tolist(), "heat": cs["heat"],
+                           "lnL": cs["lnL"], "models": cs["models"]})
+        return {"generation": int(st["generation"]), "chains": chains,
+                "accepts": st["accepts"].tolist(),
+                "rejects": st["rejects"].tolist(),
+                "swaps": st["swaps"].tolist()}
+
+    def restore(self, ckpt):
+        """Continue a checkpointed run in this one (built with the same
+        configuration and seed): every chain takes its saved state, the
+        CLs are recomputed, and the next generation draws what the
+        uninterrupted run draws there."""
+        if len(ckpt["chains"]) != self.nchains:
+            raise ValueError("checkpoint has %d chains, this run %d"
+                             % (len(ckpt["chains"]), self.nchains))
+        for i, ch in enumerate(ckpt["chains"]):
+            par = np.ascontiguousarray(ch["parent"], dtype=np.int32)
+            ln = np.ascontiguousarray(ch["len"], dtype=np.float64)
+            ms = (Mc3ModelState * len(ch["models"]))()
+            for k, q in enumerate(ch["models"]):
+                for j in range(6):
+                    ms[k].rates[j] = q["rates"][j]
+                    ms[k].rclass[j] = q["rclass"][j]
+                for j in range(4):
+                    ms[k].freqs[j] = q["freqs"][j]
+                ms[k].alpha = q["alpha"]
+                ms[k].wvar = q["wvar"]
+                ms[k].winvar = q["winvar"]
+                ms[k].weight = q["weight"]
+                ms[k].rmult = q["rmult"]
+                ms[k].nrates = q["nrates"]
+                ms[k].freqs_est = int(q["freqs_est"])
+            self._check(self.lib.cxgMc3SetChain(
+                self.h, i, par.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                ln.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                float(ch["heat"]), len(ch["models"]), ms), "cxgMc3SetChain")
+        n = self.nchains * len(MOVES)
+        acc = (ctypes.c_uint * n)(*np.ravel(ckpt["accepts"]).tolist())
+        rej = (ctypes.c_uint * n)(*np.ravel(ckpt["rejects"]).tolist())
+        sw = (ctypes.c_uint * self.nchains)(*ckpt["swaps"])
+        self._check(self.lib.cxgMc3SetCounts(self.h, acc, rej, sw),
+                    "cxgMc3SetCounts")
+        self._check(self.lib.cxgMc3Resume(self.h, int(ckpt["generation"])),
+                    "cxgMc3Resume")
 
     def stats(self):
         n = self.nchains * len(MOVES)

@@ -385,6 +385,17 @@ int cxgMc3ChainWeights(cxgMc3 *mc3, unsigned chain, double *wvar, double *winvar
 /* Member `model` of one chain's mixture, and the member count. */
 int cxgMc3ChainModel(cxgMc3 *mc3, unsigned chain, unsigned model,
                      unsigned *nmodels, cxgMc3ModelState *out);
+/* Checkpoint and resume: a chain's tree (rooted at the run's root), heat
+ * and mixture members as cxgMc3Chain / cxgMc3ChainModel read them, and the
+ * counts of cxgMc3Stats, go into a run built with the same configuration;
+ * cxgMc3Resume then recomputes every chain's CLs and lnL and continues at
+ * `generation`, drawing what an uninterrupted run draws there. */
+int cxgMc3SetChain(cxgMc3 *mc3, unsigned chain, const int32_t *parent,
+                   const double *len, double heat, unsigned nmodels,
+                   const cxgMc3ModelState *models);
+int cxgMc3SetCounts(cxgMc3 *mc3, const unsigned *accepts, const unsigned *rejects,
+                    const unsigned *swaps);
+int cxgMc3Resume(cxgMc3 *mc3, unsigned long long generation);
 /* Accept/reject counts [chain][move] (16 moves, in move_weight order),
  * swaps [chain], generation count. */
 int cxgMc3Stats(cxgMc3 *mc3, unsigned *accepts, unsigned *rejects,
