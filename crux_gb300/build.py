@@ -57,8 +57,10 @@ def build(verbose=False, extra=()):
         objs = list(ex.map(one, SOURCES))
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB)
                                       for o in objs):
+        # -ldl: the header-only NVTX ranges open a profiler's injection
+        # library on demand.
         cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart",
-               "-lpthread"]
+               "-lpthread", "-ldl"]
         if verbose:
             print(" ".join(cmd))
         subprocess.run(cmd, check=True)

@@ -504,6 +504,7 @@ extern "C" int cxgCompact(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
                           const uint32_t *freqs, const uint8_t *canon, const uint8_t *val,
                           uint8_t any_mask, uint8_t *rows_out, uint32_t *freqs_out,
                           uint8_t *masks_out, unsigned *npat) {
+    NvtxRange nr("cxgCompact");
     if (rows == nullptr || canon == nullptr || npat == nullptr || freqs_out == nullptr)
         return fail(CXG_EINVAL, "cxgCompact: NULL");
     if (masks_out && val == nullptr) return fail(CXG_EINVAL, "cxgCompact: masks need val");

@@ -7,8 +7,19 @@
 #include <string>
 
 #include "cxlik_gpu.h"
+#include <nvtx3/nvToolsExt.h>
 
 namespace cxg {
+
+// An NVTX range over one library call (header-only NVTX: a no-op unless a
+// profiler is attached), so that a trace or an `ncu --nvtx` filter can
+// tell the calls apart.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Patterns are padded to a multiple of this on the device, so that every
 // plane of a CL buffer starts on a 512-byte boundary.

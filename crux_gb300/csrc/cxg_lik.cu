@@ -1186,6 +1186,7 @@ int cxgLikDeviceBytes(size_t *bytes) {
 
 int cxgLikExecuteLnL(CxtLik *lik, int precision, double *lnL,
                      double *siteLnL) {
+    NvtxRange r("cxgLikExecuteLnL");
     return execute(lik, precision, lnL, siteLnL);
 }
 
@@ -1374,6 +1375,7 @@ static int batch_finish(State &S, cxgBatch *b, double *lnLs) {
 void CxLikExecute(CxtLik *lik) {
     // CxLik.c:914-968: nothing to do for an empty plan.
     if (lik == nullptr || lik->stepsLen == 0) return;
+    NvtxRange r("CxLikExecute");
     double tot = 0.0;
     if (execute(lik, CXG_FP64, &tot, lik->siteLnL + lik->cbase) != 0) {
         // No error channel in the reference signature: poison the outputs
@@ -1549,6 +1551,7 @@ int cxgBatchCreate(CxtLik *const *liks, unsigned n, int precision,
 
 int cxgBatchRun(cxgBatch *b, double *lnLs) {
     if (b == nullptr) return fail(CXG_EINVAL, "cxgBatchRun: NULL batch");
+    NvtxRange r("cxgBatchRun");
     State &S = state();
     std::lock_guard<std::mutex> g(S.mu);
     if (b->exec)

@@ -1989,6 +1989,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
 extern "C" int cxgMc3Run(cxgMc3 *h, unsigned long long ngen, double *seconds) {
     if (h == nullptr) return fail(CXG_EINVAL, "cxgMc3Run: NULL");
     std::lock_guard<std::mutex> lk(g_mc3_mu);
+    NvtxRange nr("cxgMc3Run");
     cudaEvent_t t0, t1;
     CXG_CUDA(cudaEventCreate(&t0));
     CXG_CUDA(cudaEventCreate(&t1));

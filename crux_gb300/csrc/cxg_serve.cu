@@ -602,6 +602,7 @@ int prepare_job(cxgServer *S, SrvJob &J) {
 
 // Launch one batch of prepared jobs (all of one walker shape).
 int launch_batch_of(cxgServer *S, SrvBatch &B, cudaStream_t st) {
+    NvtxRange nr("cxgServer batch launch");
     const size_t n = B.jobs.size();
     std::vector<PlanArgs> jobs(n);
     std::vector<PmatArgs> pm(n);
