@@ -116,6 +116,13 @@ def declare(lib):
     lib.cxgDebugSetSpinLimit.restype = c_int
     lib.cxgDebugFailAllocs.argtypes = [ctypes.c_longlong]
     lib.cxgDebugFailAllocs.restype = c_int
+    lib.cxgDebugCanaries.argtypes = [c_int]
+    lib.cxgDebugCanaries.restype = c_int
+    lib.cxgDebugCheckCanaries.argtypes = [P(ctypes.c_ulonglong),
+                                          P(ctypes.c_ulonglong)]
+    lib.cxgDebugCheckCanaries.restype = c_int
+    lib.cxgDebugCanarySelfTest.argtypes = [P(c_int)]
+    lib.cxgDebugCanarySelfTest.restype = c_int
     return lib
 
 

@@ -530,7 +530,7 @@ extern "C" int cxgCompact(const uint8_t *rows, unsigned ntaxa, unsigned nsites,
     }
     int rc = 0;
     auto fin = [&](int r) {
-        cudaFreeAsync(d, s);
+        dev_free_async(d, s);
         cudaStreamSynchronize(s);
         cudaStreamDestroy(s);
         return r;

@@ -310,6 +310,8 @@ struct PmatArgs {
 // would once the test budget of cxgDebugFailAllocs is spent.
 cudaError_t dev_malloc(void **p, size_t n);
 cudaError_t dev_malloc_async(void **p, size_t n, cudaStream_t s);
+cudaError_t dev_free(void *p);
+cudaError_t dev_free_async(void *p, cudaStream_t s);
 cudaError_t host_alloc(void **p, size_t n);
 
 // Thread-local error message.

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -54,14 +55,96 @@ static bool alloc_allowed() {
     return true;
 }
 
+// Debug canaries (cxgDebugCanaries, or CXG_DEBUG_CANARY set in the
+// environment): every device allocation gets kCanaryBytes more, filled
+// with kCanaryByte, and is tracked until it is freed.  A write past the end
+// of a buffer changes its canary; cxgDebugCheckCanaries and every
+// synchronous free read the canaries back.  This stands in for a memory
+// checker on GPUs where none may run.
+constexpr size_t kCanaryBytes = 256;
+constexpr unsigned char kCanaryByte = 0xA5;
+static std::mutex g_canary_mu;
+static std::unordered_map<void *, size_t> g_canary;  // live allocation -> size
+static std::atomic<int> g_canary_on{-1};               // -1: not yet read
+static std::atomic<unsigned long long> g_canary_bad{0};
+
+static bool canary_on() {
+    int v = g_canary_on.load();
+    if (v < 0) {
+        v = getenv("CXG_DEBUG_CANARY") != nullptr ? 1 : 0;
+        int expect = -1;
+        g_canary_on.compare_exchange_strong(expect, v);
+        v = g_canary_on.load();
+    }
+    return v > 0;
+}
+
+static void canary_track(void *p, size_t n) {
+    std::lock_guard<std::mutex> g(g_canary_mu);
+    g_canary[p] = n;
+}
+
+// Read one allocation's canary back (the device is idle); true if intact.
+static bool canary_intact(void *p, size_t n) {
+    unsigned char buf[kCanaryBytes];
+    if (cudaMemcpy(buf, static_cast<char *>(p) + n, kCanaryBytes, cudaMemcpyDeviceToHost) !=
+        cudaSuccess)
+        return false;
+    for (size_t i = 0; i < kCanaryBytes; ++i)
+        if (buf[i] != kCanaryByte) return false;
+    return true;
+}
+
 cudaError_t dev_malloc(void **p, size_t n) {
     if (!alloc_allowed()) return cudaErrorMemoryAllocation;
-    return cudaMalloc(p, n);
+    if (!canary_on()) return cudaMalloc(p, n);
+    cudaError_t e = cudaMalloc(p, n + kCanaryBytes);
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(static_cast<char *>(*p) + n, kCanaryByte, kCanaryBytes);
+    if (e == cudaSuccess) canary_track(*p, n);
+    return e;
 }
 
 cudaError_t dev_malloc_async(void **p, size_t n, cudaStream_t s) {
     if (!alloc_allowed()) return cudaErrorMemoryAllocation;
-    return cudaMallocAsync(p, n, s);
+    if (!canary_on()) return cudaMallocAsync(p, n, s);
+    cudaError_t e = cudaMallocAsync(p, n + kCanaryBytes, s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(static_cast<char *>(*p) + n, kCanaryByte, kCanaryBytes, s);
+    if (e == cudaSuccess) canary_track(*p, n);
+    return e;
+}
+
+// Frees of the library's device allocations.  A synchronous free checks
+// the canary first (after the device is idle); a stream-ordered one only
+// stops tracking the buffer.
+cudaError_t dev_free(void *p) {
+    if (p == nullptr) return cudaSuccess;
+    if (canary_on()) {
+        size_t n = 0;
+        bool tracked = false;
+        {
+            std::lock_guard<std::mutex> g(g_canary_mu);
+            auto it = g_canary.find(p);
+            if (it != g_canary.end()) {
+                n = it->second;
+                tracked = true;
+                g_canary.erase(it);
+            }
+        }
+        if (tracked && cudaDeviceSynchronize() == cudaSuccess && !canary_intact(p, n))
+            g_canary_bad.fetch_add(1);
+    }
+    return cudaFree(p);
+}
+
+cudaError_t dev_free_async(void *p, cudaStream_t s) {
+    if (p == nullptr) return cudaSuccess;
+    if (canary_on()) {
+        std::lock_guard<std::mutex> g(g_canary_mu);
+        g_canary.erase(p);
+    }
+    return cudaFreeAsync(p, s);
 }
 
 cudaError_t host_alloc(void **p, size_t n) {
@@ -90,7 +173,7 @@ struct DevBuf {
     size_t cap = 0;
     int ensure(size_t n) {
         if (n <= cap) return 0;
-        if (p) cudaFree(p);
+        if (p) dev_free(p);
         p = nullptr;
         cap = 0;
         size_t want = n < 4096 ? 4096 : n + n / 2;
@@ -173,8 +256,8 @@ static int ensure_ready(State &S) {
 }
 
 static void free_cl(State &S, DevCL &c) {
-    if (c.data) cudaFree(c.data);
-    if (c.scaler) cudaFree(c.scaler);
+    if (c.data) dev_free(c.data);
+    if (c.scaler) dev_free(c.scaler);
     size_t elt = (c.kind == CL_LEAF) ? 1 : (c.precision == CXG_FP32 ? 4 : 8);
     if (c.kind == CL_LEAF)
         S.cl_bytes -= c.ppad;
@@ -212,7 +295,7 @@ static int parent_buffer(State &S, const CxtLikCL *cl, unsigned npat,
     CXG_CUDA(dev_malloc(&c.data, (size_t)kact * 4 * ppad * elt));
     cudaError_t e = dev_malloc(&c.scaler, (size_t)ppad * 8);
     if (e != cudaSuccess) {
-        cudaFree(c.data);
+        dev_free(c.data);
         return cuda_fail(e, "cudaMalloc(scaler)");
     }
     S.cl_bytes += (size_t)kact * 4 * ppad * elt + (size_t)ppad * 8;
@@ -243,7 +326,7 @@ static int upload_leaf(State &S, const double *key, const uint8_t *masks,
     CXG_CUDA(dev_malloc(&c.data, c.ppad));
     cudaError_t e = cudaMemcpy(c.data, h.data(), c.ppad, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
-        cudaFree(c.data);
+        dev_free(c.data);
         return cuda_fail(e, "cudaMemcpy(leaf masks)");
     }
     S.cl_bytes += c.ppad;
@@ -901,10 +984,10 @@ static int finish(State &S, Plan &P, double *lnL, double *site) {
 }
 
 static void free_plan(Plan &P) {
-    if (P.prog.p) cudaFree(P.prog.p);
-    if (P.ltab.p) cudaFree(P.ltab.p);
-    if (P.partial.p) cudaFree(P.partial.p);
-    if (P.misc.p) cudaFree(P.misc.p);
+    if (P.prog.p) dev_free(P.prog.p);
+    if (P.ltab.p) dev_free(P.ltab.p);
+    if (P.partial.p) dev_free(P.partial.p);
+    if (P.misc.p) dev_free(P.misc.p);
     if (P.out.p) cudaFreeHost(P.out.p);
     P.prog = DevBuf();
     P.ltab = DevBuf();
@@ -1086,7 +1169,7 @@ int cxgLikForgetPatternWeights(const unsigned *freqs, unsigned n) {
     snprintf(key, sizeof(key), "%p:%u", (const void *)freqs, n);
     auto it = S.freqs.find(key);
     if (it != S.freqs.end()) {
-        if (it->second.dev.p) cudaFree(it->second.dev.p);
+        if (it->second.dev.p) dev_free(it->second.dev.p);
         S.freqs.erase(it);
     }
     return 0;
@@ -1100,7 +1183,7 @@ int cxgLikReset(void) {
     ++S.epoch;
     S.last_valid = false;
     for (auto &kv : S.freqs)
-        if (kv.second.dev.p) cudaFree(kv.second.dev.p);
+        if (kv.second.dev.p) dev_free(kv.second.dev.p);
     S.freqs.clear();
     return 0;
 }
@@ -1166,6 +1249,49 @@ int cxgDebugSetSpinLimit(unsigned limit, unsigned *previous) {
 
 int cxgDebugFailAllocs(long long after) {
     g_alloc_budget.store(after < 0 ? -1 : after);
+    return 0;
+}
+
+int cxgDebugCanaries(int on) {
+    g_canary_on.store(on ? 1 : 0);
+    return 0;
+}
+
+int cxgDebugCanarySelfTest(int *detected) {
+    if (detected == nullptr) return fail(CXG_EINVAL, "cxgDebugCanarySelfTest: NULL");
+    if (!canary_on()) return fail(CXG_EINVAL, "cxgDebugCanarySelfTest: canaries are off");
+    // A 1000-byte allocation whose canary a host-side memset then changes:
+    // the byte written lies inside what cudaMalloc gave, past the 1000.
+    void *p = nullptr;
+    CXG_CUDA(dev_malloc(&p, 1000));
+    CXG_CUDA(cudaMemset(static_cast<char *>(p) + 1000 + 17, 0, 1));
+    CXG_CUDA(cudaDeviceSynchronize());
+    size_t n = 0;
+    {
+        std::lock_guard<std::mutex> g(g_canary_mu);
+        n = g_canary.count(p) ? g_canary[p] : 0;
+    }
+    *detected = (n == 1000 && !canary_intact(p, n)) ? 1 : 0;
+    {
+        std::lock_guard<std::mutex> g(g_canary_mu);
+        g_canary.erase(p);
+    }
+    CXG_CUDA(cudaFree(p));
+    return 0;
+}
+
+int cxgDebugCheckCanaries(unsigned long long *checked, unsigned long long *bad) {
+    CXG_CUDA(cudaDeviceSynchronize());
+    std::vector<std::pair<void *, size_t>> live;
+    {
+        std::lock_guard<std::mutex> g(g_canary_mu);
+        live.assign(g_canary.begin(), g_canary.end());
+    }
+    unsigned long long nbad = g_canary_bad.exchange(0);
+    for (auto &kv : live)
+        if (!canary_intact(kv.first, kv.second)) ++nbad;
+    if (checked) *checked = live.size();
+    if (bad) *bad = nbad;
     return 0;
 }
 
@@ -1316,7 +1442,7 @@ static void free_batch(cxgBatch *b) {
         delete p;
     }
     for (DevBuf *d : {&b->jobs, &b->items, &b->pmats, &b->prefix, &b->results})
-        if (d->p) cudaFree(d->p);
+        if (d->p) dev_free(d->p);
     if (b->out.p) cudaFreeHost(b->out.p);
     delete b;
 }

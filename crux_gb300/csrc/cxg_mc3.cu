@@ -1571,7 +1571,7 @@ static int mc3_upload(cxgMc3 *h, T **dst, const T *src, size_t count) {
 static void mc3_free(cxgMc3 *h) {
     if (h->exec) cudaGraphExecDestroy(h->exec);
     if (h->graph) cudaGraphDestroy(h->graph);
-    for (void *p : h->allocs) cudaFree(p);
+    for (void *p : h->allocs) dev_free(p);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }

@@ -421,7 +421,7 @@ SrvDataset *unref_dataset(cxgServer *S, SrvDataset *ds) {
 // Give back what an lnL job holds: its memory and its dataset (its own
 // copy, or its reference to a registered one).
 void release_job(cxgServer *S, SrvJob *J, cudaStream_t st) {
-    if (J->mem) cudaFreeAsync(J->mem, st);
+    if (J->mem) dev_free_async(J->mem, st);
     SrvDataset *gone = nullptr;
     {
         std::lock_guard<std::mutex> g(S->mu);
@@ -429,7 +429,7 @@ void release_job(cxgServer *S, SrvJob *J, cudaStream_t st) {
         gone = J->own_ds ? J->ds : unref_dataset(S, J->ds);
     }
     if (gone) {
-        if (gone->mem) cudaFreeAsync(gone->mem, st);
+        if (gone->mem) dev_free_async(gone->mem, st);
         delete gone;
     }
     delete J;
@@ -703,7 +703,7 @@ void retire(cxgServer *S, SrvBatch &B) {
         }
         release_job(S, J, B.stream);
     }
-    cudaFreeAsync(B.mem, B.stream);
+    dev_free_async(B.mem, B.stream);
     cudaEventDestroy(B.done);
     S->slot_busy[B.slot] = false;
 }
@@ -916,7 +916,7 @@ void mc3_loop(cxgServer *S) {
             gone = unref_dataset(S, rq->ds);
         }
         if (gone) {
-            cudaFree(gone->mem);
+            dev_free(gone->mem);
             delete gone;
         }
     }
@@ -1064,7 +1064,7 @@ extern "C" int cxgServerAddDataset(cxgServer *S, unsigned long long id, unsigned
         if (e != cudaSuccess) rc = cuda_fail(e, "cxgServerAddDataset");
     }
     if (rc) {
-        if (ds->mem) cudaFree(ds->mem);
+        if (ds->mem) dev_free(ds->mem);
         return rc;
     }
     std::lock_guard<std::mutex> g(S->mu);
@@ -1106,7 +1106,7 @@ extern "C" int cxgServerAddDatasetRaw(cxgServer *S, unsigned long long id, unsig
     if (e == cudaSuccess)
         e = dev_malloc_async((void **)&tmp, al256(in_bytes) + 1024 + 256 + work, s);
     if (e != cudaSuccess) {
-        if (ds->mem) cudaFreeAsync(ds->mem, s);
+        if (ds->mem) dev_free_async(ds->mem, s);
         cudaStreamSynchronize(s);
         return cuda_fail(e, "cxgServerAddDatasetRaw: device memory");
     }
@@ -1148,9 +1148,9 @@ extern "C" int cxgServerAddDatasetRaw(cxgServer *S, unsigned long long id, unsig
             (e = cudaStreamSynchronize(s)))
             rc = cuda_fail(e, "cxgServerAddDatasetRaw: host copy");
     }
-    cudaFreeAsync(tmp, s);
+    dev_free_async(tmp, s);
     if (rc) {
-        cudaFreeAsync(ds->mem, s);
+        dev_free_async(ds->mem, s);
         cudaStreamSynchronize(s);
         return rc;
     }
@@ -1179,7 +1179,7 @@ extern "C" int cxgServerDropDataset(cxgServer *S, unsigned long long id) {
         }
     }
     if (gone) {
-        cudaFree(gone->mem);
+        dev_free(gone->mem);
         delete gone;
     }
     return 0;
@@ -1233,7 +1233,7 @@ extern "C" int cxgServerDestroy(cxgServer *S) {
     for (auto &kv : S->sessions) cxgMc3Destroy(kv.second.mc3);
     cudaStreamSynchronize(S->s_prep);
     for (auto &kv : S->datasets) {
-        cudaFree(kv.second->mem);
+        dev_free(kv.second->mem);
         delete kv.second;
     }
     for (auto &st : S->s_walk) {

@@ -514,6 +514,16 @@ int cxgTuneLanesGet(unsigned *lanes);
  * (CXG_ENOMEM) without calling CUDA; negative: off. */
 int cxgDebugSetSpinLimit(unsigned limit, unsigned *previous);
 int cxgDebugFailAllocs(long long after);
+/* cxgDebugCanaries: give every later device allocation of the library a
+ * 256-byte canary after its end (also on when CXG_DEBUG_CANARY is set in
+ * the environment).  cxgDebugCheckCanaries: wait for the device, read every
+ * live allocation's canary back, and count those changed since (with any a
+ * synchronous free found changed). */
+int cxgDebugCanaries(int on);
+int cxgDebugCheckCanaries(unsigned long long *checked, unsigned long long *bad);
+/* The check itself: a 1000-byte allocation whose canary a host memset
+ * changes must read as changed (*detected = 1).  Canaries must be on. */
+int cxgDebugCanarySelfTest(int *detected);
 
 /* No counterpart in the reference.  Evaluate lik's plan without allocating
  * anything, for callers that cannot call cudaMalloc.  Such a caller may

@@ -42,11 +42,32 @@ def oracle_lib(request):
 
 @pytest.fixture(scope="session")
 def gpu():
-    """The GB300 library; fails (does not skip) when it cannot load."""
+    """The GB300 library; fails (does not skip) when it cannot load.  Every
+    device allocation it makes in the tests carries a canary (see
+    canaries_intact)."""
     from crux_gb300 import _native
     lib = _native.load()
     import ctypes
     buf = ctypes.create_string_buffer(256)
     lib.cxgInfo(buf, 256)
     assert b"no device" not in buf.value, buf.value
+    assert lib.cxgDebugCanaries(1) == 0
     return lib
+
+
+@pytest.fixture(autouse=True)
+def canaries_intact(request):
+    """After every GPU test: no kernel wrote past the end of a library
+    allocation (each carries a 256-byte canary, read back here and at every
+    synchronous free).  A memory checker may not run on the GPUs."""
+    yield
+    if request.node.get_closest_marker("gpu") is None or \
+            "gpu" not in request.fixturenames:
+        return
+    import ctypes
+    lib = request.getfixturevalue("gpu")
+    checked, bad = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+    assert lib.cxgDebugCheckCanaries(ctypes.byref(checked),
+                                     ctypes.byref(bad)) == 0
+    assert bad.value == 0, "%d of %d canaries overwritten" % (bad.value,
+                                                              checked.value)

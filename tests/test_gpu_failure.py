@@ -244,3 +244,15 @@ def test_server_admission_allocation_failure(gpu, port):
     for g, w in zip(got, want + [want[1]]):
         assert rel(g, w) <= TOL["fp32"]
     assert st["completed"] >= 6
+
+
+def test_allocation_canaries_detect_an_overrun(gpu):
+    """The canary check every GPU test ends with sees a byte changed past
+    the end of an allocation (written by a host-side memset inside the
+    allocation's canary, not by a kernel)."""
+    det = ctypes.c_int()
+    assert gpu.cxgDebugCanarySelfTest(ctypes.byref(det)) == 0
+    assert det.value == 1
+    checked, bad = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+    assert gpu.cxgDebugCheckCanaries(ctypes.byref(checked), ctypes.byref(bad)) == 0
+    assert bad.value == 0

@@ -315,7 +315,20 @@ def test_repeated_full_plans_reuse_translation(gpu, port, precision):
     the new values.  Branch lengths, alpha, rates and frequencies change
     between calls and every lnL must follow the oracle; the program upload
     of a reused call is small.  A second Lik interleaved with the first
-    changes the plan on every call (no reuse) and must also follow."""
+    changes the plan on every call (no reuse) and must also follow.  The
+    garbage collector stays off during the calls: a Lik of an earlier test
+    collected between two calls would release its CL buffers, and a
+    registry change rightly ends the reuse."""
+    import gc
+    gc.collect()
+    gc.disable()
+    try:
+        _repeated_full_plans(gpu, port, precision)
+    finally:
+        gc.enable()
+
+
+def _repeated_full_plans(gpu, port, precision):
     case = synth.Case(24, 2000, 0.1, 611)
     other = synth.Case(17, 900, 0.1, 612)
     a = case.lik(lib=gpu, precision=precision)
