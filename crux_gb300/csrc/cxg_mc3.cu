@@ -60,9 +60,9 @@ enum {
     MV_BRLEN = 0, MV_NNI = 1, MV_RATES = 2, MV_ALPHA = 3, MV_FREQS = 4, MV_SPR = 5,
     MV_ETBR = 6, MV_INVAR = 7, MV_GAMMAJ = 8, MV_FREQJ = 9, MV_INVARJ = 10,
     MV_RATEJ = 11, MV_RATE1 = 12, MV_WEIGHT = 13, MV_RMULT = 14, MV_MIXJ = 15,
-    MV_INIT = 16
+    MV_POLYJ = 16, MV_INIT = 17
 };
-constexpr int kMoves = 16;
+constexpr int kMoves = 17;
 // Most models in a chain's mixture.
 constexpr int kMaxModels = 4;
 
@@ -120,6 +120,9 @@ struct Mc3Dev {
     int32_t *parent;      // [2][c][nnodes]
     int32_t *child;       // [2][c][nnodes][3]
     double *len;          // [2][c][nnodes]
+    // [2][c][nnodes]: the edge above node v is contracted (length 0): its
+    // two ends are one node of a multifurcating tree (polytomy jumps).
+    uint8_t *coll;
     uint8_t *curtree;     // [c]
     uint8_t *cur;         // [c][nnodes]
     int32_t *dirty;       // [c][M] dirty internal nodes, bottom-up
@@ -149,6 +152,8 @@ struct Mc3Dev {
     double gamma_jump_prior, freq_jump_prior, invar_jump_prior;
     double rate_jump_prior, rate_lambda;
     double mix_jump_prior, weight_lambda, rmult_lambda;
+    double polytomy_jump_prior;
+    uint32_t poly;  // polytomy jumps on (trees may hold contracted edges)
     // Moves with a non-zero weight (bit per MV_*): a new mixture member's
     // parameters are drawn from the prior where a move can change them,
     // else copied from slot 0.
@@ -442,6 +447,42 @@ __device__ void mc3_move_member(Mc3Model &m, unsigned from, unsigned to) {
     for (int i = 0; i < 4; ++i) m.eig[to * 4 + i] = m.eig[from * 4 + i];
 }
 
+// Polytomies.  The chain's tree stays binary; an internal edge may be
+// contracted (coll, length 0), and the multifurcating tree it stands for
+// merges the edge's two ends.  The state is the multifurcating tree T'
+// with a binary resolution R of each polytomy, and the target puts R
+// uniform given T': the reference's prior on T' (polytomyJumpPrior per
+// contracted edge, Exp(brlenPrior) lengths of the others) divided by
+// NR(T'), the number of resolutions, prod over polytomies of (2d - 5)!!
+// for degree d.  Every topology move adds ln NR(before) - ln NR(after) to
+// its prior term.  A T' node merging c binary nodes has degree c + 2, so
+// ln NR = sum over those sets of ln (2c - 1)!!.  uf and cnt are scratch
+// ([nnodes] and [nnodes - ntaxa]).
+__device__ double log_nresolutions(const int32_t *parent, const uint8_t *coll, int32_t *uf,
+                                   int32_t *cnt, unsigned N, unsigned NN) {
+    for (unsigned v = N; v < NN; ++v) {
+        uf[v] = (int32_t)v;
+        cnt[v - N] = 0;
+    }
+    auto find = [&](int v) {
+        while (uf[v] != v) {
+            uf[v] = uf[uf[v]];
+            v = uf[v];
+        }
+        return v;
+    };
+    for (unsigned v = N; v < NN; ++v)
+        if (coll[v] && parent[v] >= 0) {
+            const int a = find((int)v), b = find(parent[v]);
+            if (a != b) uf[a] = b;
+        }
+    for (unsigned v = N; v < NN; ++v) cnt[find((int)v) - (int)N]++;
+    double s = 0.0;
+    for (unsigned i = 0; i < NN - N; ++i)
+        for (int k = 2; k <= cnt[i]; ++k) s += log(2.0 * k - 1.0);
+    return s;
+}
+
 // One end of an eTBR move (Chain.pyx:517-597 for the X end, the same for
 // Y) on a binary tree held as incidence lists: inc[v][0..2] are the edges
 // at node v (-1: none) and ex[e] is the XOR of edge e's two end nodes, so
@@ -526,7 +567,7 @@ __device__ EtbrEnd etbr_end(int n0, int eA, int32_t *inc, int32_t *ex, Philox &r
 // cur), dirty flags, DFS stack, dirty list, the per-op prefix of
 // children, and the stack slot of each op and of each op's children.
 __host__ __device__ inline size_t mc3_propose_smem(unsigned NN, unsigned M) {
-    return (size_t)NN * (8 + 4 + 12 + 4 + 1 + 1) + (size_t)M * 4 + (size_t)(M + 1) * 4 +
+    return (size_t)NN * (8 + 4 + 12 + 4 + 1 + 1 + 1) + (size_t)M * 4 + (size_t)(M + 1) * 4 +
            (size_t)M * 4 + 64;
 }
 
@@ -550,6 +591,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
     uint8_t *dflag = cur + NN;
     int8_t *op_slot = reinterpret_cast<int8_t *>(dflag + NN);   // [M]
     int8_t *kid_slot = op_slot + M;                             // [M][3]
+    uint8_t *coll = reinterpret_cast<uint8_t *>(kid_slot + (size_t)M * 3);  // [NN]
     const unsigned tb = d.curtree[c];
     const size_t t_cur = (size_t)tb * d.nchains + c, t_alt = (size_t)(1 - tb) * d.nchains + c;
     int32_t *g_parent = d.parent + t_cur * NN;
@@ -557,11 +599,13 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
     double *g_len = d.len + t_cur * NN;
     int32_t *a_child = d.child + t_alt * NN * 3;
     double *a_len = d.len + t_alt * NN;
+    uint8_t *a_coll = d.coll + t_alt * NN;
     for (unsigned i = threadIdx.x; i < NN; i += blockDim.x) {
         len[i] = g_len[i];
         parent[i] = g_parent[i];
         cur[i] = d.cur[(size_t)c * NN + i];
         dflag[i] = 0;
+        coll[i] = d.coll[t_cur * NN + i];
     }
     for (unsigned i = threadIdx.x; i < NN * 3; i += blockDim.x) child[i] = g_child[i];
     __syncthreads();
@@ -597,6 +641,8 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         pr.lnHast = 0.0;
         unsigned mi = 0;  // the mixture member a model move changes
         bool full = false;
+        bool topo = false;  // a topology move under polytomy jumps
+        double lnr0 = 0.0;  // ln NR of the current tree (topo)
         int lowest = -1;  // lowest dirty node of a path move
         if (g == 0) {
             pr.type = MV_INIT;
@@ -623,11 +669,24 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             if (t == MV_FREQS && !q0.freqs_est) t = MV_BRLEN;
             if ((t == MV_WEIGHT || t == MV_RMULT) && nm < 2) t = MV_BRLEN;
             if (t == MV_MIXJ && d.mmax < 2) t = MV_BRLEN;
+            if (t == MV_POLYJ && N < 4) t = MV_BRLEN;
             pr.type = t;
+            topo = d.poly && (t == MV_NNI || t == MV_SPR || t == MV_ETBR || t == MV_POLYJ);
+            if (topo) lnr0 = log_nresolutions(parent, coll, stack, dirty, N, NN);
             if (t == MV_BRLEN) {
-                // Uniform edge = uniform non-root node (Chain.pyx:442-447).
-                unsigned k = philox_below(rng, NN - 1);
-                const unsigned e = (k >= d.root) ? k + 1 : k;
+                // Uniform edge = uniform non-root node (Chain.pyx:442-447)
+                // that is not contracted.
+                unsigned ncol = 0;
+                if (d.poly)
+                    for (unsigned v = N; v < NN; ++v) ncol += coll[v];
+                unsigned k = philox_below(rng, NN - 1 - ncol);
+                unsigned e = (k >= d.root) ? k + 1 : k;
+                if (ncol) {
+                    for (e = 0; e < NN; ++e) {
+                        if (e == d.root || coll[e]) continue;
+                        if (k-- == 0) break;
+                    }
+                }
                 const double lnM = d.brlen_lambda * (philox_u01(rng) - 0.5);
                 const double v0 = len[e], v1 = v0 * exp(lnM);
                 len[e] = v1;
@@ -746,6 +805,10 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 pr.jx = jx;
                 pr.lnHast = (lx > 0.0) ? log(lx) - log(pr.lb + pr.lp) : 0.0;
                 pr.lnPrior = (lx > 0.0) ? 0.0 : -INFINITY;
+                // The edges whose lengths SPR merges and splits must be
+                // real ones (it never changes contraction flags, so its
+                // reverse meets the same edges).
+                if (coll[p] || coll[b] || coll[x]) pr.lnPrior = -INFINITY;
                 // Dirty: both paths to the root (p's new place, g's old child).
                 for (int v = p; v >= 0; v = parent[v]) dflag[v] = 1;
                 for (int v = g; v >= 0; v = parent[v]) dflag[v] = 1;
@@ -769,7 +832,8 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 double lnH = X.lnq + Y.lnq, lnP = 0.0;
                 const int em[3] = {eA, X.eX, Y.eX};
                 for (int q = 0; q < 3; ++q) {
-                    if (em[q] < 0) continue;
+                    // A contracted edge keeps length 0 (no multiplier).
+                    if (em[q] < 0 || coll[em[q]]) continue;
                     const double lnM = d.brlen_lambda * (philox_u01(rng) - 0.5);
                     const double v0 = len[em[q]], v1 = v0 * exp(lnM);
                     len[em[q]] = v1;
@@ -784,6 +848,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 // and lengths; dflag[v] is v's next incidence slot.
                 parent[d.root] = -1;
                 a_len[d.root] = len[d.root];
+                a_coll[d.root] = 0;
                 int v = (int)d.root;
                 // The walk takes 3 NN slot steps and NN - 1 steps back up;
                 // the bound only guards against a malformed tree.
@@ -801,6 +866,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                         a_child[v * 3 + j] = u;
                         parent[u] = v;
                         a_len[u] = len[e];
+                        a_coll[u] = coll[e];
                         v = u;
                     } else {
                         if (v == (int)d.root) break;
@@ -1084,6 +1150,55 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 pr.model_changed = 1;
                 s_fin = FIN_EIG;
                 full = true;
+            } else if (t == MV_POLYJ) {
+                // An internal edge contracted or restored (polytomyJumpPropose,
+                // polytomyMergePropose, polytomySplitPropose,
+                // Chain.pyx:1076-1345).  Contract: a uniform internal edge
+                // that is not contracted gets length 0.  Restore: a uniform
+                // contracted edge gets a length drawn from its Exp(brlenPrior)
+                // prior.  Each is the other's reverse; the choice between
+                // them is 1/2 where both exist.  The prior ratio is the
+                // reference's (polytomyJumpPrior and the edge's length
+                // density); the resolution count NR follows below.
+                unsigned nnc = 0, ncc = 0;
+                for (unsigned w = N; w < NN; ++w) {
+                    if (w == d.root) continue;
+                    if (coll[w])
+                        ++ncc;
+                    else
+                        ++nnc;
+                }
+                auto pcol = [](unsigned a, unsigned b) {
+                    return a > 0 ? (b > 0 ? 0.5 : 1.0) : 0.0;
+                };
+                const bool col = nnc > 0 && (ncc == 0 || philox_below(rng, 2) == 0);
+                unsigned k = philox_below(rng, col ? nnc : ncc);
+                int v = -1;
+                for (unsigned w = N; w < NN && v < 0; ++w) {
+                    if (w == d.root || (coll[w] != 0) == col) continue;
+                    if (k-- == 0) v = (int)w;
+                }
+                const double bp = d.brlen_prior, lpj = log(d.polytomy_jump_prior);
+                pr.node = v;
+                pr.oldlen = len[v];
+                pr.a = coll[v];
+                if (col) {
+                    const double ld = log(bp) - bp * len[v];
+                    coll[v] = 1;
+                    len[v] = 0.0;
+                    pr.lnPrior = lpj - ld;
+                    pr.lnHast = log(pcol(ncc + 1, nnc - 1)) - log((double)(ncc + 1)) + ld -
+                                (log(pcol(nnc, ncc)) - log((double)nnc));
+                } else {
+                    const double l = -log(1.0 - philox_u01(rng)) / bp;
+                    const double ld = log(bp) - bp * l;
+                    coll[v] = 0;
+                    len[v] = l;
+                    pr.lnPrior = -lpj + ld;
+                    pr.lnHast = log(pcol(nnc + 1, ncc - 1)) - log((double)(nnc + 1)) - ld -
+                                (log(pcol(ncc, nnc)) - log((double)ncc));
+                }
+                lowest = parent[v];
             } else if (t == MV_WEIGHT || t == MV_RMULT) {
                 // A member's mixture weight or rate multiplier times
                 // exp(lambda (u - 1/2)), Exp(1) prior, Hastings ln m
@@ -1156,6 +1271,12 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 full = true;
             }
         }
+        if (topo && pr.lnPrior > -INFINITY) {
+            // eTBR left the new tree's flags in the spare buffer.
+            const double lnr1 = log_nresolutions(parent, pr.type == MV_ETBR ? a_coll : coll,
+                                                 stack, dirty, N, NN);
+            pr.lnPrior += lnr0 - lnr1;
+        }
         if (pr.type != MV_MIXJ) s_fin_mi = mi;
         s_full = full;
         s_lowest = lowest;
@@ -1167,6 +1288,7 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         // the set or a child's edge length changed.
         for (unsigned v = threadIdx.x; v < NN; v += blockDim.x) {
             len[v] = a_len[v];
+            coll[v] = a_coll[v];
             int nw[3] = {-1, -1, -1}, n = 0;
             for (int j = 0; j < 3; ++j) {
                 const int x = a_child[v * 3 + j];
@@ -1385,9 +1507,11 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         int32_t *o_parent = d.parent + to * NN;
         int32_t *o_child = d.child + to * NN * 3;
         double *o_len = d.len + to * NN;
+        uint8_t *o_coll = d.coll + to * NN;
         for (unsigned i = threadIdx.x; i < NN; i += blockDim.x) {
             o_len[i] = len[i];
             o_parent[i] = parent[i];
+            o_coll[i] = coll[i];
         }
         for (unsigned i = threadIdx.x; i < NN * 3; i += blockDim.x) o_child[i] = child[i];
     }
@@ -1469,6 +1593,9 @@ __global__ void mc3_accept_kernel(Mc3Dev d) {
             int32_t *child = d.child + tc * NN * 3;
             if (pr.type == MV_BRLEN) {
                 d.len[tc * NN + pr.node] = pr.oldlen;
+            } else if (pr.type == MV_POLYJ) {
+                d.len[tc * NN + pr.node] = pr.oldlen;
+                d.coll[tc * NN + pr.node] = (uint8_t)pr.a;
             } else if (pr.type == MV_SPR) {
                 // Take p out of (x, xp), put it back between g and b.
                 const int p = pr.p, x = pr.x, b = pr.b, g = pr.g, xp = pr.xp;
@@ -1711,6 +1838,12 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     d.rate_jump_prior = cfg->rate_jump_prior;
     d.rate_lambda = cfg->rate_lambda;
     d.mix_jump_prior = cfg->mixture_jump_prior;
+    d.polytomy_jump_prior = cfg->polytomy_jump_prior;
+    d.poly = mw[MV_POLYJ] > 0.0 ? 1u : 0u;
+    if (d.poly && !(cfg->polytomy_jump_prior > 0.0)) {
+        mc3_free(h);
+        return fail(CXG_EINVAL, "cxgMc3Create: polytomy_jump_prior must be positive");
+    }
     d.weight_lambda = cfg->weight_lambda;
     d.rmult_lambda = cfg->rmult_lambda;
     if (mw[MV_MIXJ] > 0.0 && mmax > 1 &&
@@ -1799,6 +1932,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     if ((rc = mc3_upload(h, &d.parent, par_all.data(), par_all.size())) ||
         (rc = mc3_upload(h, &d.child, ch_all.data(), ch_all.size())) ||
         (rc = mc3_upload(h, &d.len, len_all.data(), len_all.size())) ||
+        (rc = mc3_upload<uint8_t>(h, &d.coll, nullptr, (size_t)2 * C * NN)) ||
         (rc = mc3_upload<uint8_t>(h, &d.curtree, nullptr, C)) ||
         (rc = mc3_upload<uint8_t>(h, &d.cur, nullptr, (size_t)C * NN)) ||
         (rc = mc3_upload<int32_t>(h, &d.dirty, nullptr, (size_t)C * M)) ||
@@ -2064,8 +2198,8 @@ extern "C" int cxgMc3Chain(cxgMc3 *h, unsigned chain, double *lnL, double *heat,
 // Chain `chain` takes this tree (rooted at the run's root), heat and
 // mixture.  Call cxgMc3Resume before running.
 extern "C" int cxgMc3SetChain(cxgMc3 *h, unsigned chain, const int32_t *parent,
-                              const double *len, double heat, unsigned nmodels,
-                              const cxgMc3ModelState *models) {
+                              const double *len, const uint8_t *collapsed, double heat,
+                              unsigned nmodels, const cxgMc3ModelState *models) {
     if (h == nullptr || chain >= h->d.nchains || parent == nullptr || len == nullptr ||
         models == nullptr)
         return fail(CXG_EINVAL, "cxgMc3SetChain: bad arguments");
@@ -2091,6 +2225,18 @@ extern "C" int cxgMc3SetChain(cxgMc3 *h, unsigned chain, const int32_t *parent,
     for (unsigned v = N; v < NN; ++v)
         if (nch[v] != (v == d.root ? 3 : 2))
             return fail(CXG_EINVAL, "cxgMc3SetChain: tree is not binary (root degree 3)");
+    std::vector<uint8_t> coll(NN, 0);
+    if (collapsed)
+        for (unsigned v = 0; v < NN; ++v) {
+            if (!collapsed[v]) continue;
+            if (v < N || v == d.root || len[v] != 0.0)
+                return fail(CXG_EINVAL,
+                            "cxgMc3SetChain: only internal edges of length 0 can be contracted");
+            // (Only a run with polytomy jumps keeps its moves off them.)
+            if (!d.poly)
+                return fail(CXG_EINVAL, "cxgMc3SetChain: contracted edges need polytomy jumps");
+            coll[v] = 1;
+        }
     Mc3Model m;
     memset(&m, 0, sizeof(m));
     m.nmodels = (int32_t)nmodels;
@@ -2131,7 +2277,9 @@ extern "C" int cxgMc3SetChain(cxgMc3 *h, unsigned chain, const int32_t *parent,
         CXG_CUDA(cudaMemcpy(d.parent + t * NN, parent, NN * 4, cudaMemcpyHostToDevice));
         CXG_CUDA(cudaMemcpy(d.child + t * NN * 3, child.data(), NN * 12, cudaMemcpyHostToDevice));
         CXG_CUDA(cudaMemcpy(d.len + t * NN, len, NN * 8, cudaMemcpyHostToDevice));
+        CXG_CUDA(cudaMemcpy(d.coll + t * NN, coll.data(), NN, cudaMemcpyHostToDevice));
     }
+
     const uint8_t zero = 0;
     CXG_CUDA(cudaMemcpy(d.curtree + chain, &zero, 1, cudaMemcpyHostToDevice));
     CXG_CUDA(cudaMemcpy(d.curmodel + chain, &zero, 1, cudaMemcpyHostToDevice));
@@ -2189,6 +2337,19 @@ extern "C" int cxgMc3Resume(cxgMc3 *h, unsigned long long generation) {
         if (*(const uint32_t *)(res.data() + (size_t)c * 32 + 8))
             return fail(CXG_ETIMEOUT, "MC3 walker: a record copy timed out");
     CXG_CUDA(cudaMemcpy(d.gen, &generation, 8, cudaMemcpyHostToDevice));
+    return 0;
+}
+
+extern "C" int cxgMc3ChainCollapsed(cxgMc3 *h, unsigned chain, uint8_t *out) {
+    if (h == nullptr || chain >= h->d.nchains || out == nullptr)
+        return fail(CXG_EINVAL, "cxgMc3ChainCollapsed: bad arguments");
+    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    const Mc3Dev &d = h->d;
+    CXG_CUDA(cudaStreamSynchronize(h->stream));
+    uint8_t tb = 0;
+    CXG_CUDA(cudaMemcpy(&tb, d.curtree + chain, 1, cudaMemcpyDeviceToHost));
+    const size_t t = (size_t)tb * d.nchains + chain;
+    CXG_CUDA(cudaMemcpy(out, d.coll + t * d.nnodes, d.nnodes, cudaMemcpyDeviceToHost));
     return 0;
 }
 

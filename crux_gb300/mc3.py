@@ -22,7 +22,7 @@ from .tree import Tree
 LAMBDA = 2.0 * math.log(1.6)
 MOVES = ("brlen", "nni", "rates", "alpha", "freqs", "spr", "etbr", "invar",
          "gammajump", "freqjump", "invarjump", "ratejump", "rate", "weight",
-         "rmult", "mixturejump")
+         "rmult", "mixturejump", "polytomyjump")
 MAX_MODELS = 4
 
 
@@ -43,7 +43,7 @@ class Mc3Config(ctypes.Structure):
         ("heat_delta", ctypes.c_double),
         ("swap_stride", ctypes.c_uint),
         ("seed", ctypes.c_ulonglong),
-        ("move_weight", ctypes.c_double * 16),
+        ("move_weight", ctypes.c_double * 17),
         ("brlen_lambda", ctypes.c_double),
         ("brlen_prior", ctypes.c_double),
         ("rate_conc", ctypes.c_double),
@@ -67,6 +67,7 @@ class Mc3Config(ctypes.Structure):
         ("mixture_jump_prior", ctypes.c_double),
         ("weight_lambda", ctypes.c_double),
         ("rmult_lambda", ctypes.c_double),
+        ("polytomy_jump_prior", ctypes.c_double),
     ]
 
 
@@ -104,8 +105,11 @@ def declare(lib):
                                      P(ctypes.c_uint), P(Mc3ModelState)]
     lib.cxgMc3ChainModel.restype = ctypes.c_int
     lib.cxgMc3SetChain.argtypes = [vp, ctypes.c_uint, P(ctypes.c_int32),
-                                   P(ctypes.c_double), ctypes.c_double,
-                                   ctypes.c_uint, P(Mc3ModelState)]
+                                   P(ctypes.c_double), P(ctypes.c_uint8),
+                                   ctypes.c_double, ctypes.c_uint,
+                                   P(Mc3ModelState)]
+    lib.cxgMc3ChainCollapsed.argtypes = [vp, ctypes.c_uint, P(ctypes.c_uint8)]
+    lib.cxgMc3ChainCollapsed.restype = ctypes.c_int
     lib.cxgMc3SetChain.restype = ctypes.c_int
     lib.cxgMc3SetCounts.argtypes = [vp, P(ctypes.c_uint), P(ctypes.c_uint),
                                     P(ctypes.c_uint)]
@@ -195,6 +199,7 @@ class Mc3:
                  rclass=(0, 1, 2, 3, 4, 5), rate_jump_prior=1.0, rate_lambda=LAMBDA,
                  max_models=1, mixture_jump_prior=1.0 / 3.0,
                  weight_lambda=LAMBDA, rmult_lambda=LAMBDA,
+                 polytomy_jump_prior=1.0,
                  alpha_lambda=LAMBDA,
                  alpha_prior=1.0, graph_gens=16, trace_cap=1 << 20, lib=None):
         self.lib = lib or _native.load()
@@ -251,6 +256,7 @@ class Mc3:
         c.mixture_jump_prior = mixture_jump_prior
         c.weight_lambda = weight_lambda
         c.rmult_lambda = rmult_lambda
+        c.polytomy_jump_prior = polytomy_jump_prior
         c.alpha_lambda = alpha_lambda
         c.alpha_prior = alpha_prior
         c.precision = 1 if precision == "fp32" else 0
@@ -295,10 +301,14 @@ class Mc3:
         # Rate classes: exchangeabilities of one class hold one value.
         seen = {}
         rclass = [seen.setdefault(float(x), len(seen)) for x in rates]
+        coll = np.zeros(nn, dtype=np.uint8)
+        self._check(self.lib.cxgMc3ChainCollapsed(
+            self.h, i, coll.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))),
+            "cxgMc3ChainCollapsed")
         return {"lnL": lnl.value, "heat": heat.value, "parent": par,
                 "len": ln, "rates": rates, "rclass": rclass, "freqs": freqs,
                 "alpha": alpha.value, "wvar": wv.value, "winvar": wi.value,
-                "models": self.chain_models(i)}
+                "models": self.chain_models(i), "collapsed": coll}
 
     def chain_models(self, i):
         """Chain i's mixture members: one dict of parameters each."""
@@ -331,6 +341,7 @@ class Mc3:
             cs = self.chain_state(i)
             chains.append({"parent": cs["parent"].tolist(),
                            "len": cs["len"].tolist(), "heat": cs["heat"],
+                           "collapsed": cs["collapsed"].tolist(),
                            "lnL": cs["lnL"], "models": cs["models"]})
         return {"generation": int(st["generation"]), "chains": chains,
                 "accepts": st["accepts"].tolist(),
@@ -348,6 +359,8 @@ class Mc3:
         for i, ch in enumerate(ckpt["chains"]):
             par = np.ascontiguousarray(ch["parent"], dtype=np.int32)
             ln = np.ascontiguousarray(ch["len"], dtype=np.float64)
+            co = np.ascontiguousarray(ch.get("collapsed", np.zeros(len(par))),
+                                      dtype=np.uint8)
             ms = (Mc3ModelState * len(ch["models"]))()
             for k, q in enumerate(ch["models"]):
                 for j in range(6):
@@ -365,6 +378,7 @@ class Mc3:
             self._check(self.lib.cxgMc3SetChain(
                 self.h, i, par.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                 ln.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                co.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
                 float(ch["heat"]), len(ch["models"]), ms), "cxgMc3SetChain")
         n = self.nchains * len(MOVES)
         acc = (ctypes.c_uint * n)(*np.ravel(ckpt["accepts"]).tolist())

@@ -320,14 +320,15 @@ typedef struct {
     double heat_delta;  /* chain i runs at heat 1/(1 + i*heat_delta) */
     unsigned swap_stride;
     unsigned long long seed;
-    double move_weight[16]; /* branch length, NNI, rates (Dirichlet over
+    double move_weight[17]; /* branch length, NNI, rates (Dirichlet over
                                the class rates), alpha, base frequencies,
                                SPR, eTBR, +I weights, Gamma on/off jump,
                                equal/estimated frequency jump, +I off/on
                                jump, rate-class merge/split jump, one
                                class rate's multiplier, mixture weight,
                                mixture rate multiplier, mixture member
-                               add/remove jump */
+                               add/remove jump, polytomy jump (an
+                               internal edge contracted or restored) */
     double brlen_lambda, brlen_prior;
     double rate_conc;       /* Dirichlet concentration of rate moves */
     double freq_conc;       /* Dirichlet concentration of frequency moves */
@@ -363,6 +364,8 @@ typedef struct {
                                1 - mixture_jump_prior to k */
     double weight_lambda, rmult_lambda; /* mixture weight and rate
                                multiplier moves (2 ln 1.6) */
+    double polytomy_jump_prior; /* the reference's polytomyJumpPrior (1):
+                               prior odds of one more contracted edge */
 } cxgMc3Config;
 /* One mixture member of a chain (alpha is INFINITY with Gamma off). */
 typedef struct {
@@ -382,6 +385,9 @@ int cxgMc3Chain(cxgMc3 *mc3, unsigned chain, double *lnL, double *heat,
                 double *alpha);
 /* Weights (wVar, wInvar) of one chain's first mixture member. */
 int cxgMc3ChainWeights(cxgMc3 *mc3, unsigned chain, double *wvar, double *winvar);
+/* Contracted edges of one chain's tree: out[v] = 1 where the edge above
+ * node v has length 0 and stands for a polytomy (polytomy jumps). */
+int cxgMc3ChainCollapsed(cxgMc3 *mc3, unsigned chain, uint8_t *out);
 /* Member `model` of one chain's mixture, and the member count. */
 int cxgMc3ChainModel(cxgMc3 *mc3, unsigned chain, unsigned model,
                      unsigned *nmodels, cxgMc3ModelState *out);
@@ -391,12 +397,12 @@ int cxgMc3ChainModel(cxgMc3 *mc3, unsigned chain, unsigned model,
  * cxgMc3Resume then recomputes every chain's CLs and lnL and continues at
  * `generation`, drawing what an uninterrupted run draws there. */
 int cxgMc3SetChain(cxgMc3 *mc3, unsigned chain, const int32_t *parent,
-                   const double *len, double heat, unsigned nmodels,
-                   const cxgMc3ModelState *models);
+                   const double *len, const uint8_t *collapsed, double heat,
+                   unsigned nmodels, const cxgMc3ModelState *models);
 int cxgMc3SetCounts(cxgMc3 *mc3, const unsigned *accepts, const unsigned *rejects,
                     const unsigned *swaps);
 int cxgMc3Resume(cxgMc3 *mc3, unsigned long long generation);
-/* Accept/reject counts [chain][move] (16 moves, in move_weight order),
+/* Accept/reject counts [chain][move] (17 moves, in move_weight order),
  * swaps [chain], generation count. */
 int cxgMc3Stats(cxgMc3 *mc3, unsigned *accepts, unsigned *rejects,
                 unsigned *swaps, unsigned long long *gen);

@@ -484,7 +484,8 @@ def test_mc3_checkpoint_resume_continues_bit_exact(gpu, precision):
     import json
     moves = {"brlen": 1.0, "nni": 0.5, "spr": 0.5, "etbr": 0.5, "rates": 0.5,
              "alpha": 0.5, "freqs": 0.5, "gammajump": 0.3, "ratejump": 0.3,
-             "mixturejump": 0.5, "weight": 0.3, "rmult": 0.3}
+             "mixturejump": 0.5, "weight": 0.3, "rmult": 0.3,
+             "polytomyjump": 0.5}
 
     def make():
         case = synth.Case(12, 300, 0.1, 71)
@@ -519,3 +520,86 @@ def test_mc3_checkpoint_resume_continues_bit_exact(gpu, precision):
     assert ta["generation"] == tb["generation"] == 161
     a.close()
     b.close()
+
+
+def _splits(parent, collapsed, ntaxa):
+    """The multifurcating tree a chain stands for: the leaf sets below its
+    internal edges that are not contracted, each as the side without leaf
+    0."""
+    nn = len(parent)
+    below = [0] * nn
+    for leaf in range(ntaxa):
+        v = leaf
+        while v >= 0:
+            below[v] |= 1 << leaf
+            v = parent[v]
+    full = (1 << ntaxa) - 1
+    out = set()
+    for v in range(ntaxa, nn):
+        if parent[v] < 0 or collapsed[v]:
+            continue
+        s = below[v]
+        out.add(s if not (s & 1) else full ^ s)
+    return frozenset(out)
+
+
+def test_mc3_polytomy_jumps_sample_their_prior(gpu):
+    """Without data, polytomy jumps with NNI, SPR, eTBR and branch moves
+    sample the reference's prior over multifurcating trees (polytomyJumpPrior
+    1: every one of the 26 five-taxon trees equally often: 15 resolved, 10
+    with one polytomy, the star) with Exp(10) lengths on the edges that are
+    not contracted.  A missing resolution-count term in the topology moves,
+    or a wrong Hastings ratio in the jump, moves these frequencies."""
+    case, aln = _empty_alignment(5, 36)
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=None,
+            nchains=8, heat_delta=0.0, seed=10, precision="fp64", graph_gens=32,
+            moves={"polytomyjump": 2.0, "nni": 1.0, "spr": 0.5, "etbr": 0.5,
+                   "brlen": 1.0})
+    m.run(2000)
+    seen, lens = {}, []
+    for _ in range(1500):
+        m.run(16)
+        for i in range(8):
+            st = m.chain_state(i)
+            assert abs(st["lnL"]) < 1e-9
+            sp = _splits(st["parent"], st["collapsed"], 5)
+            seen[sp] = seen.get(sp, 0) + 1
+            for v in range(5, len(st["parent"])):
+                if st["parent"][v] >= 0:
+                    if st["collapsed"][v]:
+                        assert st["len"][v] == 0.0
+                    else:
+                        lens.append(st["len"][v])
+    m.close()
+    total = sum(seen.values())
+    assert len(seen) == 26, len(seen)
+    by_edges = {0: 0, 1: 0, 2: 0}
+    for sp, n in seen.items():
+        by_edges[len(sp)] += n
+        assert abs(n / total - 1.0 / 26.0) < 0.012, (sorted(sp), n / total)
+    assert abs(by_edges[2] / total - 15.0 / 26.0) < 0.03, by_edges
+    assert abs(np.mean(lens) - 0.1) < 0.01, np.mean(lens)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_mc3_polytomy_chains_match_oracle(gpu, port, precision):
+    """Chains whose trees gain and lose polytomies (contracted edges of
+    length 0): every chain's lnL is the oracle's for its tree."""
+    case = synth.Case(14, 200, 0.1, 62)
+    aln = case.alignment()
+    t = case.tree(aln.taxaMap)
+    m = Mc3(t, aln, case.params["rates"], case.params["freqs"], alpha=0.5,
+            ncat=4, nchains=4, heat_delta=0.5, seed=23,
+            moves={"brlen": 1.0, "polytomyjump": 2.0, "nni": 0.5, "etbr": 0.5,
+                   "spr": 0.5}, precision=precision, graph_gens=8)
+    ncoll = set()
+    for _ in range(10):
+        m.run(24)
+        check_chains(m, port, TOL[precision])
+        for i in range(4):
+            ncoll.add(int(m.chain_state(i)["collapsed"].sum()))
+    acc = m.stats()["accepts"].sum(axis=0)
+    assert acc[16] > 0, acc
+    assert max(ncoll) > 0, ncoll
+    m.close()
