@@ -38,10 +38,11 @@
 // the first edge of each path get multipliers.  A chain's tree has two
 // buffers: an eTBR move writes the re-rooted result into the spare one,
 // which an accepted move makes current.  Reversible jumps: Gamma on/off,
-// equal/estimated frequencies, +I off/on, rate classes merged/split, and
+// equal/estimated frequencies, +I off/on, rate classes merged/split,
 // mixture members added/removed, with the mixture weight and rate
-// multiplier moves (Chain.pyx:72-141, 200-266, 821-1075, 1346-1814); each
-// model move changes one uniform member of a chain's mixture.
+// multiplier moves, and polytomies (an internal edge contracted or
+// restored) (Chain.pyx:72-141, 200-266, 821-1814); each model move
+// changes one uniform member of a chain's mixture.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
