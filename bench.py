@@ -574,6 +574,18 @@ MC3 = {"mc3": {"workload": "mc3_128taxa_100ksites_gtr_gamma4_8chains",
                "nchains": 8, "heat_delta": 0.1, "seed": 20261205,
                "moves": {"brlen": 2.0, "nni": 1.0, "spr": 1.0, "rates": 1.0,
                          "alpha": 1.0}, "gens": 2000, "check_every": 1000},
+       # The reference sampler's default proposal mix (Mc3/__init__.pyx:
+       # 255-289): one rate category, no +I, mixtures (here of at most four
+       # members), eTBR and polytomy jumps as the topology moves.
+       "mc3ref": {"workload": "mc3_128taxa_100ksites_reference_default_moves_8chains",
+                  "ntaxa": 128, "nsites": 100000, "mean_brlen": 0.05,
+                  "nchains": 8, "heat_delta": 0.1, "seed": 20261208,
+                  "ncat": 1, "max_models": 4,
+                  "moves": {"weight": 30.0, "freqs": 10.0, "rmult": 10.0,
+                            "rate": 30.0, "brlen": 20.0, "etbr": 80.0,
+                            "ratejump": 10.0, "polytomyjump": 40.0,
+                            "freqjump": 10.0, "mixturejump": 5.0},
+                  "gens": 2000, "check_every": 1000},
        "mc3small": {"workload": "mc3_16taxa_1000sites_gtr_gamma4_4chains",
                     "ntaxa": 16, "nsites": 1000, "mean_brlen": 0.1,
                     "nchains": 4, "heat_delta": 0.2, "seed": 20261206,
@@ -607,12 +619,15 @@ def mc3_measure(w, gens, gens64, shapes=None, args=None, oracle=None,
     for prec, ngen in (("fp32", gens), ("fp64", gens64)):
         if ngen <= 0:
             continue
+        ncat = w.get("ncat", 4)
+
         def make():
             return Mc3(case.tree(aln.taxaMap), aln, case.params["rates"],
-                       case.params["freqs"], alpha=0.5, ncat=4,
-                       nchains=w["nchains"], heat_delta=w["heat_delta"],
-                       seed=w["seed"], moves=w["moves"], precision=prec,
-                       graph_gens=16)
+                       case.params["freqs"], alpha=0.5 if ncat > 1 else None,
+                       ncat=ncat, nchains=w["nchains"],
+                       heat_delta=w["heat_delta"], seed=w["seed"],
+                       moves=w["moves"], precision=prec, graph_gens=16,
+                       max_models=w.get("max_models", 1))
 
         if shapes and prec in shapes:
             sh = shapes[prec]
@@ -657,8 +672,12 @@ def mc3_measure(w, gens, gens64, shapes=None, args=None, oracle=None,
         ck = clocks.stop()
         st = m.stats()
         acc, rej = int(st["accepts"].sum()), int(st["rejects"].sum())
+        from crux_gb300.mc3 import MOVES
+        a_m, r_m = st["accepts"].sum(axis=0), st["rejects"].sum(axis=0)
+        by_move = {MOVES[j]: {"accepts": int(a_m[j]), "rejects": int(r_m[j])}
+                   for j in range(len(MOVES)) if a_m[j] + r_m[j] > 0}
         out[prec] = {"gens_per_s": ngen / secs, "gens": ngen, "secs": secs,
-                     "accept_rate": acc / max(1, acc + rej),
+                     "accept_rate": acc / max(1, acc + rej), "by_move": by_move,
                      "swaps": int(st["swaps"].sum()) // 2,
                      "drift_vs_fp64_oracle": drift, "clocks": ck,
                      "walker_shape": shape, "seq": seq}
@@ -717,6 +736,7 @@ def run_mc3(args, dist):
         "fp64_plain_gens_per_s": f64["gens_per_s"],
         "fp32_over_fp64": r["fp32_over_fp64"],
         "accept_rate": f32["accept_rate"], "swaps": f32["swaps"],
+        "moves": f32["by_move"],
         "drift_vs_fp64_oracle": f32["drift_vs_fp64_oracle"],
         "accept_sequence": r["accept_sequence"],
         "walker_shape": f32["walker_shape"],
@@ -1058,7 +1078,8 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"],
                     help="--profile: the plan's precision")
     ap.add_argument("--workload", default="tree128",
-                    choices=["tree128", "batch256", "mc3", "mc3small", "dirty64", "compact",
+                    choices=["tree128", "batch256", "mc3", "mc3ref", "mc3small", "dirty64",
+                             "compact",
                              "serve"])
     ap.add_argument("--rates", type=float, nargs="*", default=None,
                     help="serve: arrival rates (requests/s) to sweep")
