@@ -64,6 +64,11 @@ enum {
     MV_POLYJ = 16, MV_INIT = 17
 };
 constexpr int kMoves = 17;
+// Moves that change the model (the spare model slot).
+constexpr uint32_t kModelMoves =
+    (1u << MV_RATES) | (1u << MV_ALPHA) | (1u << MV_FREQS) | (1u << MV_INVAR) |
+    (1u << MV_GAMMAJ) | (1u << MV_FREQJ) | (1u << MV_INVARJ) | (1u << MV_RATEJ) |
+    (1u << MV_RATE1) | (1u << MV_WEIGHT) | (1u << MV_RMULT) | (1u << MV_MIXJ);
 // Most models in a chain's mixture.
 constexpr int kMaxModels = 4;
 
@@ -127,6 +132,12 @@ struct Mc3Dev {
     uint8_t *curtree;     // [c]
     uint8_t *cur;         // [c][nnodes]
     int32_t *dirty;       // [c][M] dirty internal nodes, bottom-up
+    // A full walk's op order, children and stack slots, kept per chain
+    // while its topology stays: fl_nd[c] ops (0: not kept), the order
+    // [c][M], the children prefix [c][M + 1], op and child slots [c][4M].
+    int32_t *fl_nd, *fl_dirty;
+    uint32_t *fl_kid0;
+    int8_t *fl_slot;
     int32_t *stack;       // [c][nnodes] DFS scratch
     void **cl_data;       // [c][M][2]
     void **cl_sc;         // [c][M][2]
@@ -618,9 +629,21 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
         if (prev_acc)
             for (int i = threadIdx.x; i < prev_nd; i += blockDim.x)
                 cur[d.dirty[(size_t)c * M + i]] ^= 1;
+        // A model move edits the spare model slot, which starts as a copy
+        // of the current one: copied here by the whole block (a struct
+        // copy by the deciding thread alone took tens of microseconds).
+        if (g > 0 && (d.moves_on & kModelMoves)) {
+            static_assert(sizeof(Mc3Model) % 8 == 0, "model slots copy in 8-byte words");
+            const unsigned long long *src =
+                reinterpret_cast<const unsigned long long *>(&d.model[c * 2 + d.curmodel[c]]);
+            unsigned long long *dst =
+                reinterpret_cast<unsigned long long *>(&d.model[c * 2 + (1 - d.curmodel[c])]);
+            for (unsigned i = threadIdx.x; i < sizeof(Mc3Model) / 8; i += blockDim.x)
+                dst[i] = src[i];
+        }
         __syncthreads();
     }
-    __shared__ int s_nd, s_lowest;
+    __shared__ int s_nd, s_lowest, s_fl;
     __shared__ unsigned s_fin, s_fin_mi;
     __shared__ bool s_full, s_etbr;
     if (threadIdx.x == 0) {
@@ -895,7 +918,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 // Exp(invarPrior) priors, Hastings ln m.
                 const unsigned which = philox_below(rng, 2);
                 const double lnM = d.invar_lambda * (philox_u01(rng) - 0.5);
-                m1 = m0;
                 Mc3Sub &q1 = m1.q[mi];
                 double &w = which == 0 ? q1.wvar : q1.winvar;
                 const double w0 = w, w1 = w0 * exp(lnM);
@@ -918,7 +940,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 // added weights with means 1 - invarPrior and invarPrior,
                 // which is not the density its weight move and prior use.)
                 const double ip = d.invar_prior;
-                m1 = m0;
                 Mc3Sub &q1 = m1.q[mi];
                 auto lnw = [&](double wv, double wi) {
                     return log(1.0 - ip) - (1.0 - ip) * wv + log(ip) - ip * wi;
@@ -950,7 +971,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 for (int i = 0; i < 6; ++i)
                     if (q0.rclass[i] == r) c0 = q0.rates[i];
                 const double c1 = c0 * exp(lnM);
-                m1 = m0;
                 Mc3Sub &q1 = m1.q[mi];
                 for (int i = 0; i < 6; ++i)
                     if (q0.rclass[i] == r) q1.rates[i] = c1;
@@ -986,7 +1006,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 const bool merge =
                     k == 6 ? true : (k == 1 ? false : philox_below(rng, 2) == 0);
                 const double lrjp = log(d.rate_jump_prior);
-                m1 = m0;
                 Mc3Sub &q1 = m1.q[mi];
                 if (!merge) {
                     int sp[6], ns = 0;
@@ -1055,7 +1074,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 // Exp(alpha_prior) prior; the prior and Jacobian terms are
                 // split between lnPrior and lnHast as the reference does.
                 const double sp = d.alpha_prior;
-                m1 = m0;
                 Mc3Sub &q1 = m1.q[mi];
                 if (q0.gamma_on) {
                     const double rsi0 = 1.0 / q0.alpha;
@@ -1080,7 +1098,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 // lnPrior and lnHast and cancels, as the reference's Exp(1)
                 // terms do.
                 const double ln6 = 1.791759469228055;
-                m1 = m0;
                 Mc3Sub &q1 = m1.q[mi];
                 if (q0.freqs_est) {
                     for (int i = 0; i < 4; ++i) q1.freqs[i] = 0.25;
@@ -1117,7 +1134,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                     f1[i] /= s1;
                     a1[i] = d.freq_conc * f1[i];
                 }
-                m1 = m0;
                 Mc3Sub &q1 = m1.q[mi];
                 for (int i = 0; i < 4; ++i) q1.freqs[i] = f1[i];
                 pr.lnHast = ln_dirichlet(a1, f0, 4) - ln_dirichlet(a0, f1, 4);
@@ -1144,7 +1160,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                     r1[r] /= s1;
                     a1[r] = d.rate_conc * r1[r];
                 }
-                m1 = m0;
                 Mc3Sub &q1 = m1.q[mi];
                 for (int i = 0; i < 6; ++i) q1.rates[i] = r1[q0.rclass[i]] * s0;
                 pr.lnHast = ln_dirichlet(a1, r0, k) - ln_dirichlet(a0, r1, k);
@@ -1207,7 +1222,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 const bool wt = t == MV_WEIGHT;
                 const double lnM =
                     (wt ? d.weight_lambda : d.rmult_lambda) * (philox_u01(rng) - 0.5);
-                m1 = m0;
                 double &x = wt ? m1.q[mi].weight : m1.q[mi].rmult;
                 const double x0 = x, x1 = x0 * exp(lnM);
                 x = x1;
@@ -1234,7 +1248,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 auto p_rm = [&](int n) { return n > 1 ? (n < (int)d.mmax ? 0.5 : 1.0) : 0.0; };
                 const bool add = k < (int)d.mmax && (k == 1 || philox_below(rng, 2) == 0);
                 const double l1m = log1p(-d.mix_jump_prior);
-                m1 = m0;
                 if (add) {
                     const unsigned j = philox_below(rng, (uint32_t)(k + 1));
                     Mc3Sub nq;
@@ -1262,7 +1275,6 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 // Inverse Gamma shape multiplier (Chain.pyx:320-377).
                 const double lnM = d.alpha_lambda * (philox_u01(rng) - 0.5);
                 const double a0i = 1.0 / q0.alpha, a1i = a0i * exp(lnM);
-                m1 = m0;
                 Mc3Sub &q1 = m1.q[mi];
                 q1.alpha = 1.0 / a1i;
                 pr.lnPrior = -d.alpha_prior * (a1i - a0i);
@@ -1357,6 +1369,9 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
                 dirty[i] = dirty[j];
                 dirty[j] = t;
             }
+        } else if (full && d.fl_nd[c] > 0) {
+            // The kept full walk: the block copies it in below.
+            nd = d.fl_nd[c];
         } else if (full) {
             // Iterative post-order from the root.
             int sp = 0, top = 0;
@@ -1380,6 +1395,10 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             for (int v = lowest; v >= 0; v = parent[v]) dirty[nd++] = v;
         }
         pr.ndirty = nd;
+        s_fl = full ? (d.fl_nd[c] > 0 ? 1 : 2) : 0;  // 1: copy in, 2: keep
+        if (s_fl == 1) {
+            s_nd = nd;
+        } else {
         for (int i = 0; i < nd; ++i) dflag[dirty[i]] = 1;
 
         // Children before each op (record layout).
@@ -1432,9 +1451,36 @@ __global__ void mc3_propose_kernel(Mc3Dev d) {
             op_slot[o] = (int8_t)sl;
         }
         s_nd = nd;
+        }  // listed here
     }
     __syncthreads();
     const int nd = s_nd;
+    if (s_fl != 0) {
+        // A full walk of a topology seen before: order, children and slots
+        // come from the chain's kept copy; a new one is kept for later.
+        int32_t *fd = d.fl_dirty + (size_t)c * M;
+        uint32_t *fk = d.fl_kid0 + (size_t)c * (M + 1);
+        int8_t *fs = d.fl_slot + (size_t)c * 4 * M;
+        if (s_fl == 1) {
+            for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+                dirty[i] = fd[i];
+                op_slot[i] = fs[i];
+            }
+            for (int i = threadIdx.x; i <= nd; i += blockDim.x) kid0[i] = fk[i];
+            for (int i = threadIdx.x; i < 3 * nd; i += blockDim.x) kid_slot[i] = fs[M + i];
+            for (unsigned v = N + threadIdx.x; v < NN; v += blockDim.x) dflag[v] = 1;
+        } else {
+            for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+                fd[i] = dirty[i];
+                fs[i] = op_slot[i];
+            }
+            for (int i = threadIdx.x; i <= nd; i += blockDim.x) fk[i] = kid0[i];
+            for (int i = threadIdx.x; i < 3 * nd; i += blockDim.x) fs[M + i] = kid_slot[i];
+            __syncthreads();
+            if (threadIdx.x == 0) d.fl_nd[c] = nd;
+        }
+        __syncthreads();
+    }
     // Op records, one op per thread: parent -> its spare buffer; children
     // -> spare buffer if dirty (computed earlier in this walk), else
     // current.  A leaf child points at the leaf's mask array.
@@ -1584,6 +1630,7 @@ __global__ void mc3_accept_kernel(Mc3Dev d) {
         pr.accepted = accept ? 1 : 0;
         if (accept) {
             d.lnL[c] = lnL1;
+            if (pr.type == MV_NNI || pr.type == MV_SPR || pr.type == MV_ETBR) d.fl_nd[c] = 0;
             if (pr.model_changed) d.curmodel[c] ^= 1;
             if (pr.type == MV_ETBR) d.curtree[c] ^= 1;
             if (pr.type < kMoves) d.acc[c * kMoves + pr.type]++;
@@ -1937,6 +1984,10 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
         (rc = mc3_upload<uint8_t>(h, &d.curtree, nullptr, C)) ||
         (rc = mc3_upload<uint8_t>(h, &d.cur, nullptr, (size_t)C * NN)) ||
         (rc = mc3_upload<int32_t>(h, &d.dirty, nullptr, (size_t)C * M)) ||
+        (rc = mc3_upload<int32_t>(h, &d.fl_nd, nullptr, C)) ||
+        (rc = mc3_upload<int32_t>(h, &d.fl_dirty, nullptr, (size_t)C * M)) ||
+        (rc = mc3_upload<uint32_t>(h, &d.fl_kid0, nullptr, (size_t)C * (M + 1))) ||
+        (rc = mc3_upload<int8_t>(h, &d.fl_slot, nullptr, (size_t)C * 4 * M)) ||
         (rc = mc3_upload<int32_t>(h, &d.stack, nullptr, (size_t)C * NN)) ||
         (rc = mc3_upload(h, &d.model, models.data(), models.size())) ||
         (rc = mc3_upload<uint8_t>(h, &d.curmodel, nullptr, C)) ||
@@ -2282,6 +2333,8 @@ extern "C" int cxgMc3SetChain(cxgMc3 *h, unsigned chain, const int32_t *parent,
     }
 
     const uint8_t zero = 0;
+    const int32_t none = 0;
+    CXG_CUDA(cudaMemcpy(d.fl_nd + chain, &none, 4, cudaMemcpyHostToDevice));
     CXG_CUDA(cudaMemcpy(d.curtree + chain, &zero, 1, cudaMemcpyHostToDevice));
     CXG_CUDA(cudaMemcpy(d.curmodel + chain, &zero, 1, cudaMemcpyHostToDevice));
     CXG_CUDA(cudaMemcpy(d.model + (size_t)chain * 2, &m, sizeof(m), cudaMemcpyHostToDevice));
