@@ -199,6 +199,56 @@ def autotune(lib, prec, args, lik=None, liks=None, lanes=True):
     return best
 
 
+def batched_measure(gpu, case, nevals, oracle=None):
+    """The bench tree under `nevals` different GTR exchangeabilities (the
+    work of as many chains' proposals) in one persistent batched launch
+    (crux_gb300.batch.Batch): pattern-node updates/s of the walk, its
+    roofline by algorithmic bytes, and two of the lnLs against the FP64
+    oracle.  The shape is tuned on this batch."""
+    import numpy as np
+    from crux_gb300 import tune
+    from crux_gb300.batch import Batch
+    aln = case.alignment()
+    rng = np.random.default_rng(WORKLOAD["seed"] + 1)
+    rates = [[float(x) for x in rng.dirichlet(np.ones(6)) * 6] for _ in range(nevals)]
+    liks = []
+    for r in rates:
+        lk = case.lik(lib=gpu, precision="fp32", alignment=aln)
+        lk.setRclass(0, [0, 1, 2, 3, 4, 5], r)
+        lk.prepare_plan()
+        liks.append(lk)
+    tr = tune.tune_batch(liks, "fp32", iters=3,
+                         shapes=tune.candidates("fp32", 4,
+                                                budgets=(0, 12 << 10, 24 << 10),
+                                                lanes=(1,)))
+    b = Batch(liks, "fp32")
+    got = b.run()
+    b.time(3)
+    t = b.time(20)
+    info = b.info()
+    b.close()
+    peaks = measured_peaks()
+    hbm = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = info["alg_bytes"] / (t["walk_ms"] / 1e3) / 1e9
+    out = {"evals_per_launch": nevals,
+           "value": info["updates"] / (t["walk_ms"] / 1e3), "unit": UNIT,
+           "walk_ms": t["walk_ms"], "ms_per_run": t["ms_per_run"],
+           "ms_per_eval": t["walk_ms"] / nevals,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
+                        "unit": "GB/s", "frac": achieved / hbm},
+           "shape": dict(tr["best"])}
+    if oracle is not None:
+        err = 0.0
+        for i in (0, nevals - 1):
+            lo = case.lik(lib=oracle, alignment=case.alignment())
+            lo.setRclass(0, [0, 1, 2, 3, 4, 5], rates[i])
+            want = lo.lnL()
+            err = max(err, abs(got[i] - want) / abs(want))
+        out["rel_err_vs_fp64_oracle"] = err
+    del liks
+    return out
+
+
 def cpu_run(lib, case, aln, steps, threads, min_s=0.0):
     """Time full-plan FP64 evaluations of the oracle: at least `steps`, and
     more until `min_s` seconds of CxLikExecute have run.  Returns
@@ -445,6 +495,9 @@ def run_ours(args, dist):
         }
         for p in res.values():
             p["plan"].close()
+        if args.batched_evals > 0:
+            line["batched"] = batched_measure(
+                gpu, case, args.batched_evals, None if args.no_cpu else lib)
         if not args.no_sub:
             # Bounded MC3 and serving records on the same run (each under
             # its own clock sampler).  MC3 tunes its walker shape on its own
@@ -1091,6 +1144,9 @@ def main():
                     help="batch256: number of jobs (default 256)")
     ap.add_argument("--compact-shape", type=lambda v: [int(x) for x in v.split(",")],
                     default=None, help="compact: one ntaxa,nsites shape only")
+    ap.add_argument("--batched-evals", type=int, default=32,
+                    help="tree128: evaluations of the tree (each under its own "
+                         "exchangeabilities) in the batched record (0: none)")
     ap.add_argument("--no-sub", action="store_true",
                     help="tree128: skip the MC3 and serving sub-records")
     ap.add_argument("--sub-mc3-gens", type=int, default=2000,
