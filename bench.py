@@ -19,6 +19,8 @@ walker; the plain FP64 path is measured beside it on the same plan.
              against MEASURED_PEAKS.json hbm_gbs
   cpu_baseline  the FP64 oracle CxLikExecute on the host cores (reference
              build when present, else this repository's port)
+  batched    the same tree under 32 sets of exchangeabilities in one
+             persistent batched launch (the work of 32 chains' proposals)
 
 ``--impl reference`` times the reference's CPU implementation on the same
 workload instead and prints its own line.
