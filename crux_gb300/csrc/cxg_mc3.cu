@@ -2313,6 +2313,9 @@ extern "C" int cxgMc3SetChain(cxgMc3 *h, unsigned chain, const int32_t *parent,
             q.freqs[i] = s.freqs[i];
         }
         q.freqs_est = s.freqs_est ? 1 : 0;
+        if (!q.freqs_est && !(q.freqs[0] == q.freqs[1] && q.freqs[1] == q.freqs[2] &&
+                              q.freqs[2] == q.freqs[3]))
+            return fail(CXG_EINVAL, "cxgMc3SetChain: equal-frequency member with unequal freqs");
         q.gamma_on = (d.ncat > 1 && !isinf(s.alpha)) ? 1 : 0;
         q.alpha = isinf(s.alpha) ? 1.0 : s.alpha;
         if (q.gamma_on && !(q.alpha > 0.0)) return fail(CXG_EINVAL, "cxgMc3SetChain: alpha");
