@@ -1067,7 +1067,8 @@ def serve_measure(ndatasets, rates, seconds, args=None, shapes=None):
                         "throughput_rps": n / wall,
                         "updates_per_s": st["updates"] / wall,
                         "max_batch": st["max_batch"], "batches": st["batches"],
-                        "bytes_peak": st["bytes_peak"]})
+                        "bytes_peak": st["bytes_peak"],
+                        "deferrals": st["deferrals"]})
             out.setdefault(prec + "_vals", {}).update(dict(vals))
         out[prec + "_clocks"] = clocks.stop()
         srv.close()

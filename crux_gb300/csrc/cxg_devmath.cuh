@@ -270,10 +270,10 @@ __device__ inline double d_chi2_quantile(double p, double v, double lg) {
 }
 
 // Category means (median = false) of ncat equal-probability Gamma(alpha)
-// categories, mean 1 (Lik.pyx:1222-1242).  Returns false on failure.
-// Cumulative share of the mean below the i-th category boundary (i <
+// categories, mean 1 (Lik.pyx:1222-1242), in two steps.  d_gamma_cut: the
+// cumulative share of the mean below the i-th category boundary (i <
 // ncat - 1); -1 if the quantile fails.  Categories are independent, so a
-// warp may compute them in parallel.
+// warp computes them in parallel.
 __device__ inline double d_gamma_cut(double alpha, int ncat, int i) {
     const double lga = d_ln_gamma(alpha), lga1 = d_ln_gamma(alpha + 1.0);
     const double pt = d_chi2_quantile((i + 1.0) / ncat, alpha * 2.0, lga);
@@ -289,16 +289,6 @@ __device__ inline void d_gamma_rates_from_cuts(int ncat, double *rates) {
         rates[i] *= ncat;
     }
     rates[0] *= ncat;
-}
-
-__device__ inline bool d_gamma_rates(double alpha, int ncat, double *rates) {
-    for (int i = 0; i < ncat - 1; ++i) {
-        const double cut = d_gamma_cut(alpha, ncat, i);
-        if (cut == -1.0) return false;
-        rates[i] = cut;
-    }
-    d_gamma_rates_from_cuts(ncat, rates);
-    return true;
 }
 
 }  // namespace cxg

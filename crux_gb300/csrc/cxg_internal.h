@@ -319,6 +319,10 @@ void set_error(const std::string &msg);
 int fail(int code, const std::string &msg);
 int cuda_fail(cudaError_t err, const char *what);
 
+// lnL of the chain at heat 1 after the work queued on an MC3 handle (one
+// synchronisation of its stream, two copies); -inf if no chain is cold.
+int mc3_cold_lnl(cxgMc3 *h, double *out);
+
 #define CXG_CUDA(call)                                         \
     do {                                                       \
         cudaError_t e_ = (call);                               \

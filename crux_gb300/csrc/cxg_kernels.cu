@@ -25,6 +25,8 @@
 //                   rotations of the symmetrised matrix (CxLik.c:59-250).
 #include <math.h>
 
+#include <mutex>
+
 #include "cxg_internal.h"
 #include "cxg_device.cuh"
 
@@ -1385,6 +1387,10 @@ static cudaError_t ensure_smem(Kern k, size_t sm, size_t &optin) {
     // Raised on every new maximum, not only above 48 KiB: the default limit
     // counts static and dynamic shared memory together, so a dynamic size
     // just under 48 KiB plus the walker's static arrays would not launch.
+    // Several host threads launch walkers (the server's workers): the
+    // attribute only grows, under one lock.
+    static std::mutex mu;
+    std::lock_guard<std::mutex> g(mu);
     if (sm > optin) {
         cudaError_t e = cudaFuncSetAttribute(
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

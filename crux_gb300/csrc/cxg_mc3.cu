@@ -1708,6 +1708,9 @@ using namespace cxg;
 // Host side.
 // ---------------------------------------------------------------------------
 struct cxgMc3 {
+    // Calls on one handle are serialised; separate handles (their own
+    // streams, graphs and buffers) run concurrently.
+    std::mutex mu;
     Mc3Dev d;
     cxgMc3Config cfg;
     cudaStream_t stream = nullptr;
@@ -1720,8 +1723,6 @@ struct cxgMc3 {
     unsigned graph_gens = 0;
     double last_walk_ms = 0.0;
 };
-
-static std::mutex g_mc3_mu;
 
 static int mc3_alloc(cxgMc3 *h, void **p, size_t n) {
     cudaError_t e = dev_malloc((void **)p, n ? n : 16);
@@ -1766,7 +1767,6 @@ static int mc3_enqueue_gen(cxgMc3 *h) {
 }
 
 extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
-    std::lock_guard<std::mutex> lk(g_mc3_mu);
     if (cfg == nullptr || out == nullptr) return fail(CXG_EINVAL, "cxgMc3Create: NULL");
     const unsigned N = cfg->ntaxa;
     if (N < 3 || N > 3000) return fail(CXG_EINVAL, "cxgMc3Create: 3..3000 taxa");
@@ -2174,7 +2174,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
 
 extern "C" int cxgMc3Run(cxgMc3 *h, unsigned long long ngen, double *seconds) {
     if (h == nullptr) return fail(CXG_EINVAL, "cxgMc3Run: NULL");
-    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    std::lock_guard<std::mutex> lk(h->mu);
     NvtxRange nr("cxgMc3Run");
     cudaEvent_t t0, t1;
     CXG_CUDA(cudaEventCreate(&t0));
@@ -2197,17 +2197,35 @@ extern "C" int cxgMc3Run(cxgMc3 *h, unsigned long long ngen, double *seconds) {
     cudaEventDestroy(t1);
     if (seconds) *seconds = ms / 1e3;
     uint32_t st = 0;
-    CXG_CUDA(cudaMemcpy(&st, h->d.status, 4, cudaMemcpyDeviceToHost));
+    std::vector<char> res((size_t)h->d.nchains * 32);
+    CXG_CUDA(cudaMemcpyAsync(&st, h->d.status, 4, cudaMemcpyDeviceToHost, h->stream));
+    CXG_CUDA(cudaMemcpyAsync(res.data(), h->d.results, res.size(), cudaMemcpyDeviceToHost,
+                             h->stream));
+    CXG_CUDA(cudaStreamSynchronize(h->stream));
     // Undecomposable proposed models are rejected, not errors (bit 0 is
     // only set for the initial model); bit 1 is a tree the eTBR re-rooting
     // could not walk, which a binary tree never gives.
     if (st & 2u) return fail(CXG_EINVAL, "MC3: an eTBR move met a malformed tree");
     // Any bounded wait that gave up?
-    std::vector<char> res((size_t)h->d.nchains * 32);
-    CXG_CUDA(cudaMemcpy(res.data(), h->d.results, res.size(), cudaMemcpyDeviceToHost));
     for (unsigned c = 0; c < h->d.nchains; ++c)
         if (*(const uint32_t *)(res.data() + (size_t)c * 32 + 8))
             return fail(CXG_ETIMEOUT, "MC3 walker: a record copy timed out");
+    return 0;
+}
+
+int cxg::mc3_cold_lnl(cxgMc3 *h, double *out) {
+    if (h == nullptr || out == nullptr) return fail(CXG_EINVAL, "mc3_cold_lnl: NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    const unsigned C = h->d.nchains;
+    std::vector<double> v(2 * (size_t)C);
+    CXG_CUDA(cudaMemcpyAsync(v.data(), h->d.lnL, C * 8, cudaMemcpyDeviceToHost, h->stream));
+    CXG_CUDA(cudaMemcpyAsync(v.data() + C, h->d.heat, C * 8, cudaMemcpyDeviceToHost,
+                             h->stream));
+    CXG_CUDA(cudaStreamSynchronize(h->stream));
+    double best = -INFINITY;
+    for (unsigned c = 0; c < C; ++c)
+        if (v[C + c] == 1.0) best = v[c];
+    *out = best;
     return 0;
 }
 
@@ -2215,7 +2233,7 @@ extern "C" int cxgMc3Chain(cxgMc3 *h, unsigned chain, double *lnL, double *heat,
                            int32_t *parent, double *len, double *rates,
                            double *freqs, double *alpha) {
     if (h == nullptr || chain >= h->d.nchains) return fail(CXG_EINVAL, "cxgMc3Chain: bad chain");
-    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    std::lock_guard<std::mutex> lk(h->mu);
     const Mc3Dev &d = h->d;
     CXG_CUDA(cudaStreamSynchronize(h->stream));
     if (lnL) CXG_CUDA(cudaMemcpy(lnL, d.lnL + chain, 8, cudaMemcpyDeviceToHost));
@@ -2255,7 +2273,7 @@ extern "C" int cxgMc3SetChain(cxgMc3 *h, unsigned chain, const int32_t *parent,
     if (h == nullptr || chain >= h->d.nchains || parent == nullptr || len == nullptr ||
         models == nullptr)
         return fail(CXG_EINVAL, "cxgMc3SetChain: bad arguments");
-    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    std::lock_guard<std::mutex> lk(h->mu);
     Mc3Dev &d = h->d;
     const unsigned N = d.ntaxa, NN = d.nnodes;
     if (nmodels < 1 || nmodels > d.mmax)
@@ -2350,7 +2368,7 @@ extern "C" int cxgMc3SetChain(cxgMc3 *h, unsigned chain, const int32_t *parent,
 extern "C" int cxgMc3SetCounts(cxgMc3 *h, const unsigned *accepts, const unsigned *rejects,
                                const unsigned *swaps) {
     if (h == nullptr) return fail(CXG_EINVAL, "cxgMc3SetCounts: NULL");
-    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    std::lock_guard<std::mutex> lk(h->mu);
     const Mc3Dev &d = h->d;
     CXG_CUDA(cudaStreamSynchronize(h->stream));
     if (accepts)
@@ -2368,7 +2386,7 @@ extern "C" int cxgMc3SetCounts(cxgMc3 *h, const unsigned *accepts, const unsigne
 // next generation draws what an uninterrupted run draws there.
 extern "C" int cxgMc3Resume(cxgMc3 *h, unsigned long long generation) {
     if (h == nullptr) return fail(CXG_EINVAL, "cxgMc3Resume: NULL");
-    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    std::lock_guard<std::mutex> lk(h->mu);
     Mc3Dev &d = h->d;
     CXG_CUDA(cudaStreamSynchronize(h->stream));
     // No previous move to flip in; generation 0 is the full evaluation.
@@ -2400,7 +2418,7 @@ extern "C" int cxgMc3Resume(cxgMc3 *h, unsigned long long generation) {
 extern "C" int cxgMc3ChainCollapsed(cxgMc3 *h, unsigned chain, uint8_t *out) {
     if (h == nullptr || chain >= h->d.nchains || out == nullptr)
         return fail(CXG_EINVAL, "cxgMc3ChainCollapsed: bad arguments");
-    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    std::lock_guard<std::mutex> lk(h->mu);
     const Mc3Dev &d = h->d;
     CXG_CUDA(cudaStreamSynchronize(h->stream));
     uint8_t tb = 0;
@@ -2414,7 +2432,7 @@ extern "C" int cxgMc3ChainModel(cxgMc3 *h, unsigned chain, unsigned model,
                                 unsigned *nmodels, cxgMc3ModelState *out) {
     if (h == nullptr || chain >= h->d.nchains || model >= (unsigned)kMaxModels)
         return fail(CXG_EINVAL, "cxgMc3ChainModel: bad chain or model");
-    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    std::lock_guard<std::mutex> lk(h->mu);
     const Mc3Dev &d = h->d;
     CXG_CUDA(cudaStreamSynchronize(h->stream));
     uint8_t cm = 0;
@@ -2441,7 +2459,7 @@ extern "C" int cxgMc3ChainModel(cxgMc3 *h, unsigned chain, unsigned model,
 extern "C" int cxgMc3ChainWeights(cxgMc3 *h, unsigned chain, double *wvar, double *winvar) {
     if (h == nullptr || chain >= h->d.nchains)
         return fail(CXG_EINVAL, "cxgMc3ChainWeights: bad chain");
-    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    std::lock_guard<std::mutex> lk(h->mu);
     const Mc3Dev &d = h->d;
     CXG_CUDA(cudaStreamSynchronize(h->stream));
     uint8_t cm = 0;
@@ -2456,7 +2474,7 @@ extern "C" int cxgMc3ChainWeights(cxgMc3 *h, unsigned chain, double *wvar, doubl
 extern "C" int cxgMc3Stats(cxgMc3 *h, unsigned *accepts, unsigned *rejects,
                            unsigned *swaps, unsigned long long *gen) {
     if (h == nullptr) return fail(CXG_EINVAL, "cxgMc3Stats: NULL");
-    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    std::lock_guard<std::mutex> lk(h->mu);
     const Mc3Dev &d = h->d;
     CXG_CUDA(cudaStreamSynchronize(h->stream));
     if (accepts)
@@ -2472,7 +2490,7 @@ extern "C" int cxgMc3Stats(cxgMc3 *h, unsigned *accepts, unsigned *rejects,
 
 extern "C" int cxgMc3Trace(cxgMc3 *h, double *out, unsigned long long n) {
     if (h == nullptr) return fail(CXG_EINVAL, "cxgMc3Trace: NULL");
-    std::lock_guard<std::mutex> lk(g_mc3_mu);
+    std::lock_guard<std::mutex> lk(h->mu);
     if (n > h->d.trace_cap) n = h->d.trace_cap;
     CXG_CUDA(cudaStreamSynchronize(h->stream));
     CXG_CUDA(cudaMemcpy(out, h->d.trace, n * 8, cudaMemcpyDeviceToHost));
@@ -2481,8 +2499,10 @@ extern "C" int cxgMc3Trace(cxgMc3 *h, double *out, unsigned long long n) {
 
 extern "C" int cxgMc3Destroy(cxgMc3 *h) {
     if (h == nullptr) return 0;
-    std::lock_guard<std::mutex> lk(g_mc3_mu);
-    cudaStreamSynchronize(h->stream);
+    {
+        std::lock_guard<std::mutex> lk(h->mu);  // waits for a call in progress
+        cudaStreamSynchronize(h->stream);
+    }
     mc3_free(h);
     return 0;
 }

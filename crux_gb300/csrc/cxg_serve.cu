@@ -33,6 +33,7 @@
 #include <mutex>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "cxg_devmath.cuh"
@@ -54,23 +55,44 @@ struct SrvModel {
 // Model of one request, FP64 on the GPU: mixture of ncat Gamma categories
 // with weight (1 - pinv)/ncat each and, if pinv > 0, an invariant component
 // (cmult 0) of weight pinv; wNorm and root weights as Lik.prep
-// (Lik.pyx:1603-1665).
-__global__ void srv_model_kernel(SrvModel *m) {
-    if (blockIdx.x != 0) return;
+// (Lik.pyx:1603-1665).  One warp per request (block b builds m[b]): lanes
+// 0..ncat-2 compute the Gamma category cuts while lanes 28..31 form the
+// eigensystem; lane 0 finishes.
+constexpr unsigned kModelsPerLaunch = 128;
+struct SrvModelList {
+    SrvModel *m[kModelsPerLaunch];
+};
+
+__global__ void srv_model_kernel(SrvModelList list, unsigned n) {
+    if (blockIdx.x >= n) return;
+    SrvModel *m = list.m[blockIdx.x];
     __shared__ double tmp[74];
-    if (threadIdx.x < 4) qdecomp4_warp(m->rates, m->freqs, tmp, 0);
-    __syncthreads();
-    if (threadIdx.x != 0) return;
+    __shared__ double cut[kMaxComps];
+    __shared__ int bad;
+    const unsigned lane = threadIdx.x;
+    const int ncat = m->ncat;
+    if (lane == 0) bad = 0;
+    __syncwarp();
+    if (ncat > 1 && (int)lane < ncat - 1) {
+        const double c = d_gamma_cut(m->alpha, ncat, (int)lane);
+        if (c == -1.0)
+            bad = 1;
+        else
+            cut[lane] = c;
+    }
+    if (lane >= 28) qdecomp4_warp(m->rates, m->freqs, tmp, 28);
+    __syncwarp();
+    if (lane != 0) return;
     m->ok = 0;
-    if (tmp[73] != 0.0) return;
+    if (tmp[73] != 0.0 || bad) return;
     double pin[4];
     for (int i = 0; i < 4; ++i) pin[i] = tmp[i];
     const double qnorm = tmp[4];
     for (int i = 0; i < 64; ++i) m->cube[i] = tmp[5 + i];
     for (int i = 0; i < 4; ++i) m->eig[i] = tmp[69 + i];
-    const int ncat = m->ncat;
     if (ncat > 1) {
-        if (!d_gamma_rates(m->alpha, ncat, m->cmult)) return;
+        for (int i = 0; i + 1 < ncat; ++i) m->cmult[i] = cut[i];
+        d_gamma_rates_from_cuts(ncat, m->cmult);
     } else {
         m->cmult[0] = 1.0;
     }
@@ -108,6 +130,7 @@ struct HostPlan {
     unsigned tile = kTile, tpp = 1, ppt = 1, lmax = 0;
     bool staged = false;  // leaves staged per tile (else streamed)
     size_t rstride = 0, job_bytes = 0, data_bytes = 0;
+    size_t up_bytes = 0;  // records .. model: the job's one upload
     std::vector<int> order, slot, hbm;
     std::vector<std::vector<HostKid>> kids;
 };
@@ -163,6 +186,7 @@ struct SrvJob {
     unsigned kact = 0, ppad = 0, ntiles = 0, nops = 0, nchild = 0;
     size_t bytes = 0;
     char *mem = nullptr;        // one stream-ordered allocation
+    SrvModel *model = nullptr;  // in mem; built by srv_model_kernel
     PlanArgs a;
     PmatArgs pa;
     double updates = 0.0;
@@ -182,6 +206,73 @@ struct SrvBatch {
 // (which may synchronise) on the request path.
 constexpr int kResultSlots = 8;
 
+// Pinned upload staging.  The host writes a group's records, kid tables
+// and models straight into pinned memory and sends each job with one copy;
+// a copy from pageable memory may instead hold the calling thread until
+// the stream drains.  A buffer is reused once the event recorded after its
+// copies has completed; buffers grow (rarely: a pinned allocation may
+// synchronise) to the largest group seen.  Used by the likelihood worker
+// thread only.
+constexpr unsigned kStageBufs = 16;
+struct StageBuf {
+    char *p = nullptr;
+    size_t cap = 0;
+    cudaEvent_t ev = nullptr;
+    bool pending = false;
+};
+struct StagePool {
+    std::vector<StageBuf> bufs;
+    // A buffer of at least n bytes whose earlier copies are done, or null
+    // on an allocation failure.
+    StageBuf *get(size_t n) {
+        if (bufs.capacity() < kStageBufs) bufs.reserve(kStageBufs);
+        n = std::max<size_t>(n, 1);
+        StageBuf *best = nullptr, *free_small = nullptr;
+        for (auto &b : bufs) {
+            if (b.pending && cudaEventQuery(b.ev) == cudaSuccess) b.pending = false;
+            if (b.pending) continue;
+            if (b.cap >= n && (!best || b.cap < best->cap)) best = &b;
+            if (b.cap < n) free_small = &b;
+        }
+        if (best) return best;
+        StageBuf *b = free_small;
+        if (!b && bufs.size() < kStageBufs) {
+            bufs.emplace_back();
+            b = &bufs.back();
+            if (cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) != cudaSuccess) {
+                bufs.pop_back();
+                return nullptr;
+            }
+        }
+        if (!b) {  // all in flight: wait for the first
+            b = &bufs.front();
+            cudaEventSynchronize(b->ev);
+            b->pending = false;
+            if (b->cap >= n) return b;
+        }
+        if (b->p) cudaFreeHost(b->p);
+        b->p = nullptr;
+        b->cap = 0;
+        const size_t cap = std::max<size_t>(n, (size_t)1 << 20);
+        if (host_alloc((void **)&b->p, cap) != cudaSuccess) return nullptr;
+        b->cap = cap;
+        return b;
+    }
+    // Mark b busy until the work now queued on s is done.
+    void hand_off(StageBuf *b, cudaStream_t s) {
+        cudaEventRecord(b->ev, s);
+        b->pending = true;
+    }
+    void release() {
+        for (auto &b : bufs) {
+            if (b.pending) cudaEventSynchronize(b.ev);
+            if (b.p) cudaFreeHost(b.p);
+            if (b.ev) cudaEventDestroy(b.ev);
+        }
+        bufs.clear();
+    }
+};
+
 }  // namespace cxg
 
 using namespace cxg;
@@ -195,11 +286,14 @@ struct cxgServer {
     std::condition_variable done_cv;
     uint64_t next_ticket = 1;
     bool stop = false;
-    std::thread worker, mc3_worker;
+    std::thread worker;
+    std::vector<std::thread> mc3_workers;
+    std::unordered_set<uint64_t> mc3_busy;  // sessions a worker runs (under mu)
+    std::mutex sess_mu;                     // sessions, use_clock (before mu)
     cudaStream_t s_prep = nullptr, s_walk[2] = {nullptr, nullptr};
     size_t bytes_in_use = 0, bytes_peak = 0, budget = 0;
     std::vector<double> latencies;
-    unsigned long long completed = 0, batches = 0, max_batch = 0;
+    unsigned long long completed = 0, batches = 0, max_batch = 0, deferrals = 0;
     double updates_done = 0.0;
     std::chrono::steady_clock::time_point t_first, t_last;
     bool any_done = false;
@@ -208,6 +302,7 @@ struct cxgServer {
     std::unordered_map<uint64_t, SrvDataset *> datasets;
     char *pinned = nullptr;  // [kResultSlots][max_active * 32]
     bool slot_busy[kResultSlots] = {};
+    StagePool stage;  // likelihood worker's upload staging
 };
 
 namespace {
@@ -341,6 +436,9 @@ void plan_request(SrvRequest &rq, int prec) {
     b += al256(kids * (8 + 8 + 4));                      // lens, dsts, tabs
     b += al256((size_t)P.ntiles * 16);                   // partial sums
     b += al256(sizeof(SrvModel));
+    P.up_bytes = al256((size_t)nops * P.rstride) +
+                 al256((size_t)nops * (P.lmax ? P.lmax : 1) * 8) + al256(kids * (8 + 8 + 4)) +
+                 al256((size_t)P.ntiles * 16) + sizeof(SrvModel);
     if (prec == CXG_FP64) b += al256(kids * 16 * K * 4 * 8);
     P.job_bytes = b;
     P.data_bytes = dataset_bytes(N, r.npat);
@@ -435,9 +533,30 @@ void release_job(cxgServer *S, SrvJob *J, cudaStream_t st) {
     delete J;
 }
 
+// Returned by prepare_job when the job's memory cannot be had now: the
+// request goes back to the head of the queue until batches in flight give
+// their memory back.
+constexpr int kDeferJob = 1;
+
+// The device's stream-ordered pool keeps freed blocks, and a block freed
+// on a batch stream may still be pending when the preparation stream asks
+// for memory.  Wait for the streams and hand the pool's unused memory back
+// so the next allocation can map it afresh.
+void reclaim_pool(cxgServer *S) {
+    for (auto &st : S->s_walk) cudaStreamSynchronize(st);
+    cudaStreamSynchronize(S->s_prep);
+    int dev = 0;
+    cudaMemPool_t pool = nullptr;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetMemPool(&pool, dev) == cudaSuccess)
+        cudaMemPoolTrimTo(pool, 0);
+}
+
 // Prepare an admitted lnL request: upload its patterns unless they are a
-// registered dataset, allocate its job memory, write its records and model.
-int prepare_job(cxgServer *S, SrvJob &J) {
+// registered dataset, allocate its job memory, write its records, kid
+// tables and model parameters into `stage` (pinned, plan.up_bytes, laid
+// out as the job memory from the records to the model) and send them with
+// one copy.  The model itself is built by srv_model_kernel afterwards.
+int prepare_job(cxgServer *S, SrvJob &J, char *stage) {
     const cxgRequest &r = J.rq->req;
     const HostPlan &P = J.rq->plan;
     const int prec = S->cfg.precision;
@@ -457,7 +576,18 @@ int prepare_job(cxgServer *S, SrvJob &J) {
     J.kact = K;
     J.ppad = P.ppad;
     J.ntiles = P.ntiles;
-    CXG_CUDA(dev_malloc_async((void **)&J.mem, P.job_bytes, S->s_prep));
+    cudaError_t ae = dev_malloc_async((void **)&J.mem, P.job_bytes, S->s_prep);
+    if (ae == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        reclaim_pool(S);
+        ae = dev_malloc_async((void **)&J.mem, P.job_bytes, S->s_prep);
+    }
+    if (ae == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        J.mem = nullptr;
+        return kDeferJob;
+    }
+    if (ae != cudaSuccess) return cuda_fail(ae, "dev_malloc_async(server job)");
     char *p = J.mem;
     auto take = [&](size_t n) {
         char *q = p;
@@ -478,14 +608,21 @@ int prepare_job(cxgServer *S, SrvJob &J) {
     int32_t *ktab = (int32_t *)(kidarr + (size_t)P.nk * 16);
     auto cl_of = [&](int h) { return cls + (size_t)h * K * 4 * ppad * elt; };
     auto sc_of = [&](int h) { return scs + (size_t)h * ppad * 8; };
-    std::vector<unsigned char> hrec((size_t)P.nops * rstride, 0);
-    std::vector<const uint8_t *> hlr((size_t)P.nops * (P.lmax ? P.lmax : 1), nullptr);
-    std::vector<double> hlen(P.nk);
-    std::vector<uint64_t> hdst(P.nk);
-    std::vector<int32_t> htab(P.nk, -1);
+    // Host images at the same offsets from `stage` as on the device from rec.
+    auto host_of = [&](const void *d) {
+        return stage + ((const char *)d - (const char *)rec);
+    };
+    unsigned char *hrec = (unsigned char *)stage;
+    const uint8_t **hlr = (const uint8_t **)host_of(lrows);
+    double *hlen = (double *)host_of(klen);
+    uint64_t *hdst = (uint64_t *)host_of(kdst);
+    int32_t *htab = (int32_t *)host_of(ktab);
+    memset(hrec, 0, (size_t)P.nops * rstride);
+    memset(hlr, 0, (size_t)P.nops * (P.lmax ? P.lmax : 1) * sizeof(void *));
+    for (unsigned i = 0; i < P.nk; ++i) htab[i] = -1;
     unsigned nk = 0;
     for (unsigned o = 0; o < P.nops; ++o) {
-        unsigned char *rr = hrec.data() + (size_t)o * rstride;
+        unsigned char *rr = hrec + (size_t)o * rstride;
         const unsigned nch = (unsigned)P.kids[o].size();
         RecHead hd;
         memset(&hd, 0, sizeof(hd));
@@ -509,7 +646,7 @@ int prepare_job(cxgServer *S, SrvJob &J) {
             if (k.src == SRC_LEAF) {
                 ch.data = J.ds->masks + (size_t)k.idx * J.ds->stride;  // taxon's masks
                 ch.idx = (uint32_t)k.idx;                       // its staged row
-                const uint8_t **lr = hlr.data() + (size_t)o * P.lmax;
+                const uint8_t **lr = hlr + (size_t)o * P.lmax;
                 unsigned j = 0;
                 while (lr[j] != nullptr) ++j;
                 lr[j] = static_cast<const uint8_t *>(ch.data);
@@ -535,25 +672,17 @@ int prepare_job(cxgServer *S, SrvJob &J) {
             memcpy(rr, &hd, sizeof(hd));
         }
     }
-    SrvModel hmod;
+    SrvModel &hmod = *(SrvModel *)host_of(model);
     memset(&hmod, 0, sizeof(hmod));
     memcpy(hmod.rates, r.rates, 48);
     memcpy(hmod.freqs, r.freqs, 32);
     hmod.alpha = r.alpha;
     hmod.pinv = r.pinv;
     hmod.ncat = (int32_t)r.ncat;
-    // Uploads from pageable memory are staged before the calls return, so
-    // the host vectors may go out of scope afterwards.
-    cudaStream_t s = S->s_prep;
-    CXG_CUDA(cudaMemcpyAsync(rec, hrec.data(), hrec.size(), cudaMemcpyHostToDevice, s));
-    CXG_CUDA(cudaMemcpyAsync(lrows, hlr.data(), hlr.size() * sizeof(void *),
-                             cudaMemcpyHostToDevice, s));
-    CXG_CUDA(cudaMemcpyAsync(klen, hlen.data(), nk * 8, cudaMemcpyHostToDevice, s));
-    CXG_CUDA(cudaMemcpyAsync(kdst, hdst.data(), nk * 8, cudaMemcpyHostToDevice, s));
-    CXG_CUDA(cudaMemcpyAsync(ktab, htab.data(), nk * 4, cudaMemcpyHostToDevice, s));
-    CXG_CUDA(cudaMemcpyAsync(model, &hmod, sizeof(hmod), cudaMemcpyHostToDevice, s));
-    srv_model_kernel<<<1, 32, 0, s>>>(model);
-    CXG_CHECK_LAUNCH("srv_model_kernel");
+    // The partial sums between the kid tables and the model go up too
+    // (unset; the walker writes them before it reads them).
+    CXG_CUDA(cudaMemcpyAsync(rec, stage, P.up_bytes, cudaMemcpyHostToDevice, S->s_prep));
+    J.model = model;
 
     PlanArgs &a = J.a;
     memset(&a, 0, sizeof(a));
@@ -643,12 +772,16 @@ int launch_batch_of(cxgServer *S, SrvBatch &B, cudaStream_t st) {
     std::stable_sort(items.begin(), items.end(), [&](const WalkItem &x, const WalkItem &y) {
         return jobs[x.job].nops > jobs[y.job].nops;
     });
-    std::vector<char> host(o_res);
-    memcpy(host.data() + o_jobs, jobs.data(), n * sizeof(PlanArgs));
-    memcpy(host.data() + o_items, items.data(), items.size() * sizeof(WalkItem));
-    memcpy(host.data() + o_pm, pm.data(), n * sizeof(PmatArgs));
-    memcpy(host.data() + o_pre, prefix.data(), (n + 1) * 4);
-    CXG_CUDA(cudaMemcpyAsync(B.mem, host.data(), o_res, cudaMemcpyHostToDevice, st));
+    StageBuf *sb = S->stage.get(o_res);
+    if (!sb) return fail(CXG_ENOMEM, "server: pinned staging");
+    char *host = sb->p;
+    memcpy(host + o_jobs, jobs.data(), n * sizeof(PlanArgs));
+    memcpy(host + o_items, items.data(), items.size() * sizeof(WalkItem));
+    memcpy(host + o_pm, pm.data(), n * sizeof(PmatArgs));
+    memcpy(host + o_pre, prefix.data(), (n + 1) * 4);
+    const cudaError_t ce = cudaMemcpyAsync(B.mem, host, o_res, cudaMemcpyHostToDevice, st);
+    S->stage.hand_off(sb, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(server batch)");
     CXG_CUDA(cudaMemsetAsync(res, 0, n * 32 + 16, st));
     CXG_CUDA(launch_pmat_batch((const PmatArgs *)(B.mem + o_pm),
                                (const uint32_t *)(B.mem + o_pre), (uint32_t)n,
@@ -742,16 +875,70 @@ void lnl_loop(cxgServer *S) {
                 admitted.push_back(J);
             }
         }
-        for (SrvJob *J : admitted) {
-            const int rc = prepare_job(S, *J);
-            if (rc) {
-                complete(S, J->rq->ticket, rc, NAN, J->rq->t_submit);
-                release_job(S, J, S->s_prep);
-                continue;
-            }
-            ready.push_back(J);
-        }
         if (!admitted.empty()) {
+            NvtxRange nr("cxgServer prepare");
+            size_t up = 0;
+            for (SrvJob *J : admitted) up += al256(J->rq->plan.up_bytes);
+            StageBuf *sb = S->stage.get(up);
+            char *hp = sb ? sb->p : nullptr;
+            std::vector<SrvJob *> prepared;
+            std::vector<std::unique_ptr<SrvRequest>> deferred;
+            for (SrvJob *J : admitted) {
+                int rc = !deferred.empty() ? kDeferJob
+                         : sb             ? prepare_job(S, *J, hp)
+                                          : fail(CXG_ENOMEM, "server: pinned staging");
+                if (hp) hp += al256(J->rq->plan.up_bytes);
+                // Out of memory with nothing else holding any: a failure.
+                if (rc == kDeferJob && deferred.empty() && prepared.empty() &&
+                    ready.empty() && inflight.empty())
+                    rc = fail(CXG_ENOMEM, "server: job memory (cudaMallocAsync)");
+                if (rc == kDeferJob) {
+                    if (J->mem) dev_free_async(J->mem, S->s_prep);
+                    if (J->own_ds && J->ds) {
+                        if (J->ds->mem) dev_free_async(J->ds->mem, S->s_prep);
+                        delete J->ds;
+                    }
+                    {
+                        std::lock_guard<std::mutex> g(S->mu);
+                        S->bytes_in_use -= J->bytes;
+                    }
+                    deferred.push_back(std::move(J->rq));
+                    delete J;
+                    continue;
+                }
+                if (rc) {
+                    complete(S, J->rq->ticket, rc, NAN, J->rq->t_submit);
+                    release_job(S, J, S->s_prep);
+                    continue;
+                }
+                prepared.push_back(J);
+            }
+            // One model launch per kModelsPerLaunch jobs, a warp per job.
+            for (size_t i = 0; i < prepared.size(); i += kModelsPerLaunch) {
+                const unsigned nm =
+                    (unsigned)std::min<size_t>(kModelsPerLaunch, prepared.size() - i);
+                SrvModelList ml;
+                for (unsigned j = 0; j < nm; ++j) ml.m[j] = prepared[i + j]->model;
+                srv_model_kernel<<<nm, 32, 0, S->s_prep>>>(ml, nm);
+                const cudaError_t e = cudaGetLastError();
+                for (unsigned j = 0; j < nm; ++j) {
+                    SrvJob *J = prepared[i + j];
+                    if (e == cudaSuccess) {
+                        ready.push_back(J);
+                        continue;
+                    }
+                    complete(S, J->rq->ticket, cuda_fail(e, "srv_model_kernel"), NAN,
+                             J->rq->t_submit);
+                    release_job(S, J, S->s_prep);
+                }
+            }
+            if (sb) S->stage.hand_off(sb, S->s_prep);
+            if (!deferred.empty()) {
+                std::lock_guard<std::mutex> g(S->mu);
+                for (size_t i = deferred.size(); i-- > 0;)
+                    S->lnl_q.push_front(std::move(deferred[i]));
+                S->deferrals += deferred.size();
+            }
             cudaEventRecord(prep_done, S->s_prep);
             // Batch streams wait for the preparation of these jobs.
             for (auto &st : S->s_walk) cudaStreamWaitEvent(st, prep_done, 0);
@@ -803,51 +990,77 @@ void lnl_loop(cxgServer *S) {
     cudaEventDestroy(prep_done);
 }
 
+// MC3 requests run on kMc3Workers threads, each session's handle (own
+// stream and generation graph) on one of them at a time: small sessions
+// overlap on the device, and the requests of a session keep their order.
+constexpr unsigned kMc3Workers = 4;
+
 void mc3_loop(cxgServer *S) {
     for (;;) {
         std::unique_ptr<SrvRequest> rq;
         {
             std::unique_lock<std::mutex> g(S->mu);
-            S->cv.wait_for(g, std::chrono::milliseconds(2),
-                           [&] { return S->stop || !S->mc3_q.empty(); });
-            if (S->mc3_q.empty()) {
-                if (S->stop) break;
+            // The first queued request whose session no other worker runs.
+            auto runnable = [&] {
+                for (auto q = S->mc3_q.begin(); q != S->mc3_q.end(); ++q)
+                    if ((*q)->req.session == 0 || !S->mc3_busy.count((*q)->req.session))
+                        return q;
+                return S->mc3_q.end();
+            };
+            S->cv.wait_for(g, std::chrono::milliseconds(2), [&] {
+                return runnable() != S->mc3_q.end() || (S->stop && S->mc3_q.empty());
+            });
+            auto q = runnable();
+            if (q == S->mc3_q.end()) {
+                if (S->stop && S->mc3_q.empty()) break;
                 continue;
             }
-            rq = std::move(S->mc3_q.front());
-            S->mc3_q.pop_front();
+            rq = std::move(*q);
+            S->mc3_q.erase(q);
+            if (rq->req.session) S->mc3_busy.insert(rq->req.session);
         }
         const cxgRequest &r = rq->req;
         cxgMc3 *m = nullptr;
         int rc = 0;
         const unsigned nc = r.mc3_chains ? r.mc3_chains : 4;
         const size_t need = mc3_bytes(r, S->cfg.precision, nc);
-        auto it = r.session ? S->sessions.find(r.session) : S->sessions.end();
-        if (it != S->sessions.end()) {
-            m = it->second.mc3;
-            it->second.last_use = ++S->use_clock;
-        } else {
-            // Admission by free HBM: evict idle sessions, least recently
-            // used first, until the new chains fit the budget.
-            for (;;) {
-                {
-                    std::lock_guard<std::mutex> g(S->mu);
-                    if (S->bytes_in_use + need <= S->budget || S->sessions.empty()) {
-                        S->bytes_in_use += need;
-                        S->bytes_peak = std::max(S->bytes_peak, S->bytes_in_use);
-                        break;
+        {
+            std::lock_guard<std::mutex> sg(S->sess_mu);
+            auto it = r.session ? S->sessions.find(r.session) : S->sessions.end();
+            if (it != S->sessions.end()) {
+                m = it->second.mc3;
+                it->second.last_use = ++S->use_clock;
+            } else {
+                // Admission by free HBM: evict idle sessions (none that a
+                // worker runs), least recently used first, until the new
+                // chains fit the budget.
+                for (;;) {
+                    auto lru = S->sessions.end();
+                    {
+                        std::lock_guard<std::mutex> g(S->mu);
+                        if (S->bytes_in_use + need <= S->budget) {
+                            S->bytes_in_use += need;
+                            S->bytes_peak = std::max(S->bytes_peak, S->bytes_in_use);
+                            break;
+                        }
+                        for (auto q = S->sessions.begin(); q != S->sessions.end(); ++q)
+                            if (!S->mc3_busy.count(q->first) &&
+                                (lru == S->sessions.end() ||
+                                 q->second.last_use < lru->second.last_use))
+                                lru = q;
+                        if (lru == S->sessions.end()) {  // nothing to evict
+                            S->bytes_in_use += need;
+                            S->bytes_peak = std::max(S->bytes_peak, S->bytes_in_use);
+                            break;
+                        }
+                        S->bytes_in_use -= lru->second.bytes;
                     }
+                    cxgMc3Destroy(lru->second.mc3);
+                    S->sessions.erase(lru);
                 }
-                auto lru = S->sessions.begin();
-                for (auto q = S->sessions.begin(); q != S->sessions.end(); ++q)
-                    if (q->second.last_use < lru->second.last_use) lru = q;
-                cxgMc3Destroy(lru->second.mc3);
-                {
-                    std::lock_guard<std::mutex> g(S->mu);
-                    S->bytes_in_use -= lru->second.bytes;
-                }
-                S->sessions.erase(lru);
             }
+        }
+        if (m == nullptr) {
             cxgMc3Config c;
             memset(&c, 0, sizeof(c));
             c.ntaxa = r.ntaxa;
@@ -886,6 +1099,7 @@ void mc3_loop(cxgServer *S) {
             c.trace_cap = 1;
             rc = cxgMc3Create(&c, &m);
             if (rc == 0 && r.session) {
+                std::lock_guard<std::mutex> sg(S->sess_mu);
                 SrvSession ss;
                 ss.mc3 = m;
                 ss.bytes = need;
@@ -898,23 +1112,16 @@ void mc3_loop(cxgServer *S) {
         }
         double lnl = NAN;
         if (rc == 0) rc = cxgMc3Run(m, r.mc3_gens ? r.mc3_gens : 10, nullptr);
-        if (rc == 0) {
-            // Report the cold chain.
-            double best = -INFINITY;
-            for (unsigned c = 0; c < nc && rc == 0; ++c) {
-                double l = 0.0, h = 0.0;
-                rc = cxgMc3Chain(m, c, &l, &h, nullptr, nullptr, nullptr, nullptr, nullptr);
-                if (h == 1.0) best = l;
-            }
-            lnl = best;
-        }
+        if (rc == 0) rc = mc3_cold_lnl(m, &lnl);  // the cold chain's
         if (m && !r.session) cxgMc3Destroy(m);
         complete(S, rq->ticket, rc, lnl, rq->t_submit);
         SrvDataset *gone = nullptr;
         {
             std::lock_guard<std::mutex> g(S->mu);
             gone = unref_dataset(S, rq->ds);
+            if (r.session) S->mc3_busy.erase(r.session);
         }
+        S->cv.notify_all();  // a worker may wait for this session
         if (gone) {
             dev_free(gone->mem);
             delete gone;
@@ -955,10 +1162,11 @@ extern "C" int cxgServerCreate(const cxgServerConfig *cfg, cxgServer **out) {
         cudaSetDevice(dev);
         lnl_loop(S);
     });
-    S->mc3_worker = std::thread([S, dev] {
-        cudaSetDevice(dev);
-        mc3_loop(S);
-    });
+    for (unsigned w = 0; w < kMc3Workers; ++w)
+        S->mc3_workers.emplace_back([S, dev] {
+            cudaSetDevice(dev);
+            mc3_loop(S);
+        });
     *out = S;
     return 0;
 }
@@ -1192,6 +1400,7 @@ extern "C" int cxgServerStats(cxgServer *S, cxgServerStatsT *st) {
     st->completed = S->completed;
     st->batches = S->batches;
     st->max_batch = S->max_batch;
+    st->deferrals = S->deferrals;
     st->bytes_peak = S->bytes_peak;
     st->bytes_budget = S->budget;
     st->updates = S->updates_done;
@@ -1215,7 +1424,7 @@ extern "C" int cxgServerResetStats(cxgServer *S) {
     if (S == nullptr) return fail(CXG_EINVAL, "cxgServerResetStats: NULL");
     std::lock_guard<std::mutex> g(S->mu);
     S->latencies.clear();
-    S->completed = S->batches = S->max_batch = 0;
+    S->completed = S->batches = S->max_batch = S->deferrals = 0;
     S->updates_done = 0.0;
     S->any_done = false;
     return 0;
@@ -1229,7 +1438,8 @@ extern "C" int cxgServerDestroy(cxgServer *S) {
     }
     S->cv.notify_all();
     if (S->worker.joinable()) S->worker.join();
-    if (S->mc3_worker.joinable()) S->mc3_worker.join();
+    for (auto &w : S->mc3_workers)
+        if (w.joinable()) w.join();
     for (auto &kv : S->sessions) cxgMc3Destroy(kv.second.mc3);
     cudaStreamSynchronize(S->s_prep);
     for (auto &kv : S->datasets) {
@@ -1240,6 +1450,7 @@ extern "C" int cxgServerDestroy(cxgServer *S) {
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);
     }
+    S->stage.release();
     cudaStreamDestroy(S->s_prep);
     cudaFreeHost(S->pinned);
     delete S;

@@ -55,7 +55,8 @@ class ServerStats(ctypes.Structure):
                 ("p99_ms", ctypes.c_double),
                 ("max_ms", ctypes.c_double),
                 ("wall_s", ctypes.c_double),
-                ("updates", ctypes.c_double)]
+                ("updates", ctypes.c_double),
+                ("deferrals", ctypes.c_ulonglong)]
 
 
 def declare(lib):

@@ -447,6 +447,9 @@ typedef struct {
     unsigned long long completed, batches, max_batch;
     unsigned long long bytes_peak, bytes_budget;
     double p50_ms, p99_ms, max_ms, wall_s, updates;
+    unsigned long long deferrals;   /* lnL requests put back in the queue
+                                       because their memory could not be had
+                                       until batches in flight finished */
 } cxgServerStatsT;
 int cxgServerCreate(const cxgServerConfig *cfg, cxgServer **server);
 /* Copies the request; returns at once with a ticket.  Thread-safe. */
