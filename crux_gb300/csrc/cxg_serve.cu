@@ -5,10 +5,12 @@
 //
 //   admit    while the request's device bytes fit the HBM budget and the
 //            active-job limit: stream-ordered allocation (cudaMallocAsync,
-//            so admission never synchronises the device), upload of its
-//            leaf masks and weights, its model built on the GPU in FP64
-//            (Q eigensystem, Gamma categories, +I), its op records packed
-//            on the host;
+//            so admission never synchronises the device; under memory
+//            pressure the request waits in the queue), its op records
+//            packed on the host into pinned staging and sent with one
+//            copy, then the models of all admitted requests built on the
+//            GPU in FP64 (Q eigensystem, Gamma categories, +I) by one
+//            launch, a warp per request;
 //   batch    every prepared lnL job joins the next persistent walker launch
 //            (P matrices for all jobs, then (job, tile) items longest
 //            first), one launch per number of mixture components; up to two
@@ -17,9 +19,10 @@
 //   retire   when a batch's event fires: read the lnLs, complete the
 //            tickets (latency = submit to completion), free the memory.
 //
-// MC3-step requests run n generations of on-device MC3 (cxgMc3*) on a
-// second worker; a session id keeps a chain resident across requests.
-// Their kernels run on their own streams and overlap the lnL batches.
+// MC3-step requests run n generations of on-device MC3 (cxgMc3*) on four
+// more workers; a session id keeps a chain resident across requests, and
+// a session's requests run one at a time in submission order.  Their
+// kernels run on their own streams and overlap the lnL batches.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>

@@ -372,6 +372,8 @@ typedef struct {
     double rates[6], freqs[4], alpha, wvar, winvar, weight, rmult;
     int rclass[6], nrates, freqs_est;
 } cxgMc3ModelState;
+/* Calls on one handle are serialised; separate handles (each with its own
+ * stream, graph and buffers) may be driven from separate threads at once. */
 typedef struct cxgMc3 cxgMc3;
 /* Build the chains and run generation 0 (a full evaluation). */
 int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **mc3);
