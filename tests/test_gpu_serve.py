@@ -161,3 +161,40 @@ def test_mc3_request_with_invariant_sites(gpu):
     cold = [s["lnL"] for s in want if s["heat"] == 1.0]
     assert math.isfinite(got)
     assert got == cold[0]
+
+
+def test_mc3_sessions_keep_order_across_workers(gpu):
+    """Requests of two sessions, submitted interleaved and all at once, run
+    on the server's MC3 workers concurrently: each session's k-th request
+    reports the cold-chain lnL the same chains reach after k steps through
+    the MC3 API, so no two requests of a session ran out of order or at
+    the same time."""
+    import math
+    from crux_gb300.mc3 import LAMBDA, Mc3
+    cases = [synth.Case(10, 600, 0.1, 61), synth.Case(14, 900, 0.1, 62)]
+    gens, steps = 5, 3
+    reqs = [PreparedRequest(c, MC3, mc3_gens=gens, mc3_chains=2, seed=21 + i,
+                            session=100 + i) for i, c in enumerate(cases)]
+    lone = PreparedRequest(cases[0], MC3, mc3_gens=gens, mc3_chains=2, seed=33)
+    srv = Server("fp64")
+    tickets = []
+    for _ in range(steps):
+        tickets.append([srv.submit(r) for r in reqs] + [srv.submit(lone)])
+    got = [[srv.wait(t)[0] for t in row] for row in tickets]
+    srv.close()
+    for i, (case, req) in enumerate(zip(cases, reqs)):
+        aln = req.alignment
+        m = Mc3(case.tree(aln.taxaMap), aln, case.params["rates"],
+                case.params["freqs"], alpha=case.alpha, ncat=case.ncat,
+                nchains=2, heat_delta=0.1, seed=21 + i,
+                moves={"brlen": 1.0, "nni": 1.0}, precision="fp64",
+                graph_gens=gens, trace_cap=1, brlen_lambda=2.0 * math.log(1.6),
+                alpha_lambda=LAMBDA, etbr_pext=0.0)
+        for k in range(steps):
+            m.run(gens)
+            cold = [m.chain_state(c)["lnL"] for c in range(2)
+                    if m.chain_state(c)["heat"] == 1.0]
+            assert got[k][i] == cold[0], (i, k)
+        m.close()
+    # The session-less request starts afresh each time.
+    assert got[0][2] == got[1][2] == got[2][2]
