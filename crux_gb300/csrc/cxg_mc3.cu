@@ -1724,6 +1724,21 @@ struct cxgMc3 {
     double last_walk_ms = 0.0;
 };
 
+// The proposal kernel's dynamic shared-memory limit is one setting for
+// every handle: it only grows, under one lock, so a smaller handle made
+// later (or on another thread) never lowers it below what a larger one
+// launches with.
+static cudaError_t raise_propose_smem(size_t n) {
+    static std::mutex mu;
+    static size_t cur = 0;
+    std::lock_guard<std::mutex> g(mu);
+    if (n <= cur) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(
+        mc3_propose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)n);
+    if (e == cudaSuccess) cur = n;
+    return e;
+}
+
 static int mc3_alloc(cxgMc3 *h, void **p, size_t n) {
     cudaError_t e = dev_malloc((void **)p, n ? n : 16);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(mc3)");
@@ -2119,9 +2134,7 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     h->pmat_grid = (C * d.maxkids * K + 31) / 32;
     h->propose_smem = mc3_propose_smem(NN, M);
     {  // (the default limit counts the kernel's static shared memory too)
-        e = cudaFuncSetAttribute(mc3_propose_kernel,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)h->propose_smem);
+        e = raise_propose_smem(h->propose_smem);
         if (e != cudaSuccess) {
             mc3_free(h);
             return cuda_fail(e, "cxgMc3Create: proposal shared memory");
