@@ -443,7 +443,7 @@ int stage_init() {
     cudaError_t e = cudaEventCreateWithFlags(&g_stage_ev[0], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g_stage_ev[1], cudaEventDisableTiming);
     if (e != cudaSuccess) {
-        cudaFreeHost(p);
+        host_free(p);
         return cuda_fail(e, "cxgCompact: staging events");
     }
     g_stage[0] = p;

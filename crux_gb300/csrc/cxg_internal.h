@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <string>
 
 #include "cxlik_gpu.h"
@@ -318,6 +319,16 @@ cudaError_t host_alloc(void **p, size_t n);
 void set_error(const std::string &msg);
 int fail(int code, const std::string &msg);
 int cuda_fail(cudaError_t err, const char *what);
+
+// Stream capture and device-wide synchronisation exclude each other: a
+// call that synchronises the device (cudaFree, cudaFreeHost,
+// cudaDeviceSynchronize) on one thread while another thread captures a
+// stream invalidates that capture.  Captures hold this lock from begin to
+// end; the library's frees and device synchronisations go through
+// dev_free, host_free and device_sync, which take it.
+std::mutex &capture_gate();
+cudaError_t host_free(void *p);
+cudaError_t device_sync();
 
 // lnL of the chain at heat 1 after the work queued on an MC3 handle (one
 // synchronisation of its stream, two copies); -inf if no chain is cold.

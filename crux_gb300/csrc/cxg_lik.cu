@@ -118,8 +118,25 @@ cudaError_t dev_malloc_async(void **p, size_t n, cudaStream_t s) {
 // Frees of the library's device allocations.  A synchronous free checks
 // the canary first (after the device is idle); a stream-ordered one only
 // stops tracking the buffer.
+std::mutex &capture_gate() {
+    static std::mutex m;
+    return m;
+}
+
+cudaError_t host_free(void *p) {
+    if (p == nullptr) return cudaSuccess;
+    std::lock_guard<std::mutex> g(capture_gate());
+    return cudaFreeHost(p);
+}
+
+cudaError_t device_sync() {
+    std::lock_guard<std::mutex> g(capture_gate());
+    return cudaDeviceSynchronize();
+}
+
 cudaError_t dev_free(void *p) {
     if (p == nullptr) return cudaSuccess;
+    std::lock_guard<std::mutex> gate(capture_gate());
     if (canary_on()) {
         size_t n = 0;
         bool tracked = false;
@@ -190,7 +207,7 @@ struct HostBuf {
     size_t cap = 0;
     int ensure(size_t n) {
         if (n <= cap) return 0;
-        if (p) cudaFreeHost(p);
+        if (p) host_free(p);
         p = nullptr;
         cap = 0;
         size_t want = n < 4096 ? 4096 : n + n / 2;
@@ -988,7 +1005,7 @@ static void free_plan(Plan &P) {
     if (P.ltab.p) dev_free(P.ltab.p);
     if (P.partial.p) dev_free(P.partial.p);
     if (P.misc.p) dev_free(P.misc.p);
-    if (P.out.p) cudaFreeHost(P.out.p);
+    if (P.out.p) host_free(P.out.p);
     P.prog = DevBuf();
     P.ltab = DevBuf();
     P.partial = DevBuf();
@@ -1240,7 +1257,7 @@ int cxgDebugSetSpinLimit(unsigned limit, unsigned *previous) {
     if (rc) return rc;
     static unsigned current = kSpinLimit;
     // No walker of this library may be running while the bound changes.
-    CXG_CUDA(cudaDeviceSynchronize());
+    CXG_CUDA(device_sync());
     CXG_CUDA(set_spin_limit(limit));
     if (previous) *previous = current;
     current = limit;
@@ -1265,7 +1282,7 @@ int cxgDebugCanarySelfTest(int *detected) {
     void *p = nullptr;
     CXG_CUDA(dev_malloc(&p, 1000));
     CXG_CUDA(cudaMemset(static_cast<char *>(p) + 1000 + 17, 0, 1));
-    CXG_CUDA(cudaDeviceSynchronize());
+    CXG_CUDA(device_sync());
     size_t n = 0;
     {
         std::lock_guard<std::mutex> g(g_canary_mu);
@@ -1276,12 +1293,15 @@ int cxgDebugCanarySelfTest(int *detected) {
         std::lock_guard<std::mutex> g(g_canary_mu);
         g_canary.erase(p);
     }
-    CXG_CUDA(cudaFree(p));
+    {
+        std::lock_guard<std::mutex> gate(capture_gate());
+        CXG_CUDA(cudaFree(p));
+    }
     return 0;
 }
 
 int cxgDebugCheckCanaries(unsigned long long *checked, unsigned long long *bad) {
-    CXG_CUDA(cudaDeviceSynchronize());
+    CXG_CUDA(device_sync());
     std::vector<std::pair<void *, size_t>> live;
     {
         std::lock_guard<std::mutex> g(g_canary_mu);
@@ -1443,7 +1463,7 @@ static void free_batch(cxgBatch *b) {
     }
     for (DevBuf *d : {&b->jobs, &b->items, &b->pmats, &b->prefix, &b->results})
         if (d->p) dev_free(d->p);
-    if (b->out.p) cudaFreeHost(b->out.p);
+    if (b->out.p) host_free(b->out.p);
     delete b;
 }
 
@@ -1650,14 +1670,21 @@ int cxgBatchCreate(CxtLik *const *liks, unsigned n, int precision,
             b->launches += 1;
         }
         // Capture one run as a CUDA graph.
-        if ((e = cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal)) !=
-            cudaSuccess) {
+        cudaGraph_t graph = nullptr;
+        bool began = false;
+        {
+            std::lock_guard<std::mutex> gate(capture_gate());
+            e = cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                began = true;
+                rc = batch_enqueue(S, b);
+                e = cudaStreamEndCapture(S.stream, &graph);
+            }
+        }
+        if (!began) {
             free_batch(b);
             return cuda_fail(e, "cudaStreamBeginCapture");
         }
-        rc = batch_enqueue(S, b);
-        cudaGraph_t graph = nullptr;
-        e = cudaStreamEndCapture(S.stream, &graph);
         if (rc || e != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);
             free_batch(b);

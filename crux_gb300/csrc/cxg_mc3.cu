@@ -2163,14 +2163,15 @@ extern "C" int cxgMc3Create(const cxgMc3Config *cfg, cxgMc3 **out) {
     }
     // Capture a block of generations as one graph.
     h->graph_gens = cfg->graph_gens ? cfg->graph_gens : 16;
-    e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) {
-        mc3_free(h);
-        return cuda_fail(e, "cudaStreamBeginCapture(mc3)");
-    }
-    for (unsigned i = 0; i < h->graph_gens && rc == 0; ++i) rc = mc3_enqueue_gen(h);
     cudaGraph_t graph = nullptr;
-    e = cudaStreamEndCapture(h->stream, &graph);
+    {
+        std::lock_guard<std::mutex> gate(capture_gate());
+        e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            for (unsigned i = 0; i < h->graph_gens && rc == 0; ++i) rc = mc3_enqueue_gen(h);
+            e = cudaStreamEndCapture(h->stream, &graph);
+        }
+    }
     if (rc || e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
         mc3_free(h);

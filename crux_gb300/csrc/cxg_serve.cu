@@ -253,7 +253,7 @@ struct StagePool {
             b->pending = false;
             if (b->cap >= n) return b;
         }
-        if (b->p) cudaFreeHost(b->p);
+        if (b->p) host_free(b->p);
         b->p = nullptr;
         b->cap = 0;
         const size_t cap = std::max<size_t>(n, (size_t)1 << 20);
@@ -269,7 +269,7 @@ struct StagePool {
     void release() {
         for (auto &b : bufs) {
             if (b.pending) cudaEventSynchronize(b.ev);
-            if (b.p) cudaFreeHost(b.p);
+            if (b.p) host_free(b.p);
             if (b.ev) cudaEventDestroy(b.ev);
         }
         bufs.clear();
@@ -844,6 +844,24 @@ void retire(cxgServer *S, SrvBatch &B) {
     S->slot_busy[B.slot] = false;
 }
 
+// Evict the least recently used MC3 session that no worker runs; the
+// caller holds sess_mu.  False if every session is in use (or none).
+bool evict_lru_session(cxgServer *S) {
+    auto lru = S->sessions.end();
+    {
+        std::lock_guard<std::mutex> g(S->mu);
+        for (auto q = S->sessions.begin(); q != S->sessions.end(); ++q)
+            if (!S->mc3_busy.count(q->first) &&
+                (lru == S->sessions.end() || q->second.last_use < lru->second.last_use))
+                lru = q;
+        if (lru == S->sessions.end()) return false;
+        S->bytes_in_use -= lru->second.bytes;
+    }
+    cxgMc3Destroy(lru->second.mc3);
+    S->sessions.erase(lru);
+    return true;
+}
+
 void lnl_loop(cxgServer *S) {
     std::vector<SrvJob *> ready;        // prepared, waiting for a batch
     std::deque<SrvBatch> inflight;
@@ -853,6 +871,7 @@ void lnl_loop(cxgServer *S) {
     for (;;) {
         // 1. Admit.
         std::vector<SrvJob *> admitted;
+        bool blocked = false;  // the head does not fit and no lnL job holds memory
         {
             std::unique_lock<std::mutex> g(S->mu);
             if (S->lnl_q.empty() && ready.empty() && inflight.empty()) {
@@ -868,7 +887,10 @@ void lnl_loop(cxgServer *S) {
             while (!S->lnl_q.empty() && active + admitted.size() < S->cfg.max_active) {
                 SrvRequest &rq = *S->lnl_q.front();
                 const size_t need = rq.plan.job_bytes + (rq.ds ? 0 : rq.plan.data_bytes);
-                if (S->bytes_in_use + need > S->budget && S->bytes_in_use > 0) break;
+                if (S->bytes_in_use + need > S->budget && S->bytes_in_use > 0) {
+                    blocked = active == 0 && admitted.empty();
+                    break;
+                }
                 SrvJob *J = new SrvJob();
                 J->bytes = need;
                 J->rq = std::move(S->lnl_q.front());
@@ -877,6 +899,17 @@ void lnl_loop(cxgServer *S) {
                 S->bytes_peak = std::max(S->bytes_peak, S->bytes_in_use);
                 admitted.push_back(J);
             }
+        }
+        // Only idle MC3 sessions (and resident datasets) hold the budget:
+        // give the head request the memory of the least recently used one.
+        if (blocked) {
+            bool freed;
+            {
+                std::lock_guard<std::mutex> sg(S->sess_mu);
+                freed = evict_lru_session(S);
+            }
+            // Sessions in use give their memory back when they finish.
+            if (!freed) std::this_thread::sleep_for(std::chrono::microseconds(200));
         }
         if (!admitted.empty()) {
             NvtxRange nr("cxgServer prepare");
@@ -1038,28 +1071,17 @@ void mc3_loop(cxgServer *S) {
                 // worker runs), least recently used first, until the new
                 // chains fit the budget.
                 for (;;) {
-                    auto lru = S->sessions.end();
+                    bool fits;
                     {
                         std::lock_guard<std::mutex> g(S->mu);
-                        if (S->bytes_in_use + need <= S->budget) {
-                            S->bytes_in_use += need;
-                            S->bytes_peak = std::max(S->bytes_peak, S->bytes_in_use);
-                            break;
-                        }
-                        for (auto q = S->sessions.begin(); q != S->sessions.end(); ++q)
-                            if (!S->mc3_busy.count(q->first) &&
-                                (lru == S->sessions.end() ||
-                                 q->second.last_use < lru->second.last_use))
-                                lru = q;
-                        if (lru == S->sessions.end()) {  // nothing to evict
-                            S->bytes_in_use += need;
-                            S->bytes_peak = std::max(S->bytes_peak, S->bytes_in_use);
-                            break;
-                        }
-                        S->bytes_in_use -= lru->second.bytes;
+                        fits = S->bytes_in_use + need <= S->budget;
                     }
-                    cxgMc3Destroy(lru->second.mc3);
-                    S->sessions.erase(lru);
+                    if (fits || !evict_lru_session(S)) {  // (or nothing to evict)
+                        std::lock_guard<std::mutex> g(S->mu);
+                        S->bytes_in_use += need;
+                        S->bytes_peak = std::max(S->bytes_peak, S->bytes_in_use);
+                        break;
+                    }
                 }
             }
         }
@@ -1455,7 +1477,7 @@ extern "C" int cxgServerDestroy(cxgServer *S) {
     }
     S->stage.release();
     cudaStreamDestroy(S->s_prep);
-    cudaFreeHost(S->pinned);
+    host_free(S->pinned);
     delete S;
     return 0;
 }

@@ -198,3 +198,27 @@ def test_mc3_sessions_keep_order_across_workers(gpu):
         m.close()
     # The session-less request starts afresh each time.
     assert got[0][2] == got[1][2] == got[2][2]
+
+
+def test_lnl_request_evicts_idle_mc3_session(gpu, port):
+    """An lnL request that fits the HBM budget only without an idle MC3
+    session's chains evicts that session instead of waiting for ever; the
+    session's next request starts its chains afresh."""
+    mreq = PreparedRequest(synth.Case(12, 800, 0.1, 71), MC3, mc3_gens=5,
+                           mc3_chains=2, seed=3, session=7)
+    lreq = PreparedRequest(synth.Case(40, 4000, 0.1, 72), LNL)
+    sizes = []
+    for r in (mreq, lreq):
+        srv = Server("fp32")
+        srv.wait(srv.submit(r))
+        sizes.append(srv.stats()["bytes_peak"])
+        srv.close()
+    budget = max(sizes) + min(sizes) // 2
+    srv = Server("fp32", hbm_budget=budget)
+    first = srv.wait(srv.submit(mreq))[0]
+    got = srv.wait(srv.submit(lreq), timeout=60)[0]
+    again = srv.wait(srv.submit(mreq))[0]
+    srv.close()
+    want = lreq.oracle_lik(port).lnL()
+    assert abs(got - want) <= 1e-6 * abs(want)
+    assert again == first
