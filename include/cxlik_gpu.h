@@ -556,7 +556,7 @@ int cxgDebugCanarySelfTest(int *detected);
  * <= 2048 children, <= 2^20 patterns, <= 8 active components.  The first
  * call on a device looks up that array's address: make it before any
  * stream capture.  With CUDA's lazy module loading, the first call of each
- * precision on a device also loads the library's kernels, which the driver
+ * precision on a device also loads the library's kernels, which the CUDA driver
  * may allocate for: make one call of each precision as a warm-up outside
  * the region where nothing may allocate.  Calls share the array; calls
  * that overlap on the GPU race.  Returns after the lnL has been copied
