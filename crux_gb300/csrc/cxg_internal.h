@@ -305,6 +305,8 @@ struct PmatArgs {
     const double *wnorm_dev;   // if set, wNorm is read here (model built on the GPU)
     unsigned char *rec;
     double *ltab;              // FP64 plans: leaf-message tables
+    uint64_t *zero = nullptr;  // pmat_kernel: four words cleared before the
+                               // walker that follows it runs (its result)
 };
 
 // Allocations of the library (cxg_lik.cu); each fails as an out-of-memory

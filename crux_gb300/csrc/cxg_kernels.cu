@@ -50,6 +50,9 @@ __device__ __forceinline__ void pdl_wait() {
 
 __global__ void pmat_kernel(PmatArgs a) {
     pdl_launch_dependents();
+    // The walker's result words (ticket, counts, sum): it reads them only
+    // after this grid has completed (stream order, or griddepcontrol.wait).
+    if (a.zero != nullptr && blockIdx.x == 0 && threadIdx.x < 4) a.zero[threadIdx.x] = 0;
     const unsigned idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
     if (idx >= a.nchild * a.kact) return;  // the same for all four lanes
     pmat_one(a, idx, threadIdx.x & 3u);

@@ -968,7 +968,11 @@ static int enqueue(State &S, Plan &P, bool want_site,
                    bool pdl = false) {
     char *mp = static_cast<char *>(P.misc.p);
     P.a.site = want_site ? (double *)(mp + 32) : nullptr;
-    CXG_CUDA(cudaMemsetAsync(mp, 0, 32, S.stream));
+    // The P kernel clears the walker's 32 result bytes; a plan with no P
+    // matrices clears them with a memset.
+    const bool pmat = P.pa.nchild * P.pa.kact > 0;
+    P.pa.zero = pmat ? reinterpret_cast<uint64_t *>(mp) : nullptr;
+    if (!pmat) CXG_CUDA(cudaMemsetAsync(mp, 0, 32, S.stream));
     CXG_CUDA(launch_pmat(P.pa, S.stream));
     if (e0) CXG_CUDA(cudaEventRecord(e0, S.stream));
     CXG_CUDA(launch_plan(P.prec, P.a, S.stream, P.lanes,
