@@ -292,6 +292,7 @@ struct cxgServer {
     std::thread worker;
     std::vector<std::thread> mc3_workers;
     std::unordered_set<uint64_t> mc3_busy;  // sessions a worker runs (under mu)
+    unsigned mc3_running = 0;               // MC3 requests a worker runs (under mu)
     std::mutex sess_mu;                     // sessions, use_clock (before mu)
     cudaStream_t s_prep = nullptr, s_walk[2] = {nullptr, nullptr};
     size_t bytes_in_use = 0, bytes_peak = 0, budget = 0;
@@ -908,8 +909,33 @@ void lnl_loop(cxgServer *S) {
                 std::lock_guard<std::mutex> sg(S->sess_mu);
                 freed = evict_lru_session(S);
             }
-            // Sessions in use give their memory back when they finish.
-            if (!freed) std::this_thread::sleep_for(std::chrono::microseconds(200));
+            if (!freed) {
+                // Closing with no MC3 request left to give memory back:
+                // the request fails rather than hold the close up.
+                std::unique_ptr<SrvRequest> gone;
+                SrvDataset *gds = nullptr;
+                {
+                    std::lock_guard<std::mutex> g(S->mu);
+                    if (S->stop && S->mc3_running == 0 && !S->lnl_q.empty()) {
+                        gone = std::move(S->lnl_q.front());
+                        S->lnl_q.pop_front();
+                        gds = unref_dataset(S, gone->ds);
+                    }
+                }
+                if (gone) {
+                    complete(S, gone->ticket,
+                             fail(CXG_ENOMEM, "server closed before the request's memory "
+                                              "was free"),
+                             NAN, gone->t_submit);
+                    if (gds) {
+                        dev_free(gds->mem);
+                        delete gds;
+                    }
+                } else {
+                    // Sessions in use give their memory back when they finish.
+                    std::this_thread::sleep_for(std::chrono::microseconds(200));
+                }
+            }
         }
         if (!admitted.empty()) {
             NvtxRange nr("cxgServer prepare");
@@ -1054,6 +1080,7 @@ void mc3_loop(cxgServer *S) {
             rq = std::move(*q);
             S->mc3_q.erase(q);
             if (rq->req.session) S->mc3_busy.insert(rq->req.session);
+            ++S->mc3_running;
         }
         const cxgRequest &r = rq->req;
         cxgMc3 *m = nullptr;
@@ -1145,6 +1172,7 @@ void mc3_loop(cxgServer *S) {
             std::lock_guard<std::mutex> g(S->mu);
             gone = unref_dataset(S, rq->ds);
             if (r.session) S->mc3_busy.erase(r.session);
+            --S->mc3_running;
         }
         S->cv.notify_all();  // a worker may wait for this session
         if (gone) {

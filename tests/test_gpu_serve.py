@@ -222,3 +222,18 @@ def test_lnl_request_evicts_idle_mc3_session(gpu, port):
     want = lreq.oracle_lik(port).lnL()
     assert abs(got - want) <= 1e-6 * abs(want)
     assert again == first
+
+
+def test_close_fails_requests_waiting_for_memory(gpu):
+    """A request that waits for memory that only a resident dataset holds
+    (a budget of one byte) is still waiting after a while, and does not
+    hold the server's close up: close fails it and returns."""
+    from crux_gb300._native import DeviceTimeout
+    req = requests(1, seed=950)[0]
+    srv = Server("fp32", hbm_budget=1)
+    srv.add_dataset(1, req)
+    r = PreparedRequest(req.case, LNL, alignment=req.alignment, dataset=1)
+    t = srv.submit(r)
+    with pytest.raises(DeviceTimeout):
+        srv.wait(t, timeout=0.5)
+    srv.close()
