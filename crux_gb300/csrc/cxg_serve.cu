@@ -1028,6 +1028,8 @@ void lnl_loop(cxgServer *S) {
                 const int rc = launch_batch_of(S, B, st);
                 if (rc && B.slot >= 0) S->slot_busy[B.slot] = false;
                 if (rc) {
+                    if (B.mem) dev_free_async(B.mem, st);
+                    if (B.done) cudaEventDestroy(B.done);
                     for (SrvJob *J : B.jobs) {
                         complete(S, J->rq->ticket, rc, NAN, J->rq->t_submit);
                         release_job(S, J, st);
