@@ -755,7 +755,10 @@ int launch_batch_of(cxgServer *S, SrvBatch &B, cudaStream_t st) {
     if (B.slot < 0) return fail(CXG_EBUSY, "server: no free result slot");
     S->slot_busy[B.slot] = true;
     B.host = S->pinned + (size_t)B.slot * S->cfg.max_active * 32;
-    CXG_CUDA(dev_malloc_async((void **)&B.mem, B.bytes, st));
+    if (const cudaError_t e = dev_malloc_async((void **)&B.mem, B.bytes, st)) {
+        B.mem = nullptr;
+        return cuda_fail(e, "dev_malloc_async(server batch)");
+    }
     char *res = B.mem + o_res;
     for (size_t j = 0; j < n; ++j) {
         SrvJob *J = B.jobs[j];
