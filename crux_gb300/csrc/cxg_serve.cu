@@ -457,7 +457,10 @@ int upload_dataset(unsigned N, unsigned npat, const uint8_t *masks,
     ds.ntaxa = N;
     ds.npat = npat;
     ds.stride = ppad;
-    CXG_CUDA(dev_malloc_async((void **)&ds.mem, ds.bytes, s));
+    if (const cudaError_t e = dev_malloc_async((void **)&ds.mem, ds.bytes, s)) {
+        ds.mem = nullptr;  // nothing for the caller to free
+        return cuda_fail(e, "dev_malloc_async(server dataset)");
+    }
     ds.masks = (uint8_t *)ds.mem;
     ds.weights = (uint32_t *)(ds.mem + al256((size_t)N * ppad));
     ds.leaves = (const uint8_t **)(ds.mem + al256((size_t)N * ppad) + al256((size_t)npat * 4));
@@ -591,7 +594,10 @@ int prepare_job(cxgServer *S, SrvJob &J, char *stage) {
         J.mem = nullptr;
         return kDeferJob;
     }
-    if (ae != cudaSuccess) return cuda_fail(ae, "dev_malloc_async(server job)");
+    if (ae != cudaSuccess) {
+        J.mem = nullptr;
+        return cuda_fail(ae, "dev_malloc_async(server job)");
+    }
     char *p = J.mem;
     auto take = [&](size_t n) {
         char *q = p;
