@@ -718,7 +718,7 @@ int prepare_job(cxgServer *S, SrvJob &J, char *stage) {
     a.ltab = ltab;
     a.ntiles = J.ntiles;
     PmatArgs &pa = J.pa;
-    memset(&pa, 0, sizeof(pa));
+    pa = PmatArgs{};
     pa.nchild = nk;
     pa.kact = K;
     pa.precision = prec;
