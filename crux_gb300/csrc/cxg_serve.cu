@@ -554,8 +554,10 @@ void reclaim_pool(cxgServer *S) {
     cudaStreamSynchronize(S->s_prep);
     int dev = 0;
     cudaMemPool_t pool = nullptr;
-    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetMemPool(&pool, dev) == cudaSuccess)
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetMemPool(&pool, dev) == cudaSuccess) {
+        std::lock_guard<std::mutex> gate(capture_gate());  // unmaps device memory
         cudaMemPoolTrimTo(pool, 0);
+    }
 }
 
 // Prepare an admitted lnL request: upload its patterns unless they are a
