@@ -45,10 +45,16 @@ def test_barrier_and_max_over_two_ranks():
                                       stdout=subprocess.PIPE, stderr=subprocess.PIPE,
                                       text=True))
     outs = []
-    for p in procs:
-        out, err = p.communicate(timeout=120)
-        assert p.returncode == 0, err
-        outs.append(json.loads(out.strip().splitlines()[-1]))
+    try:
+        for p in procs:
+            out, err = p.communicate(timeout=120)
+            assert p.returncode == 0, err
+            outs.append(json.loads(out.strip().splitlines()[-1]))
+    finally:
+        for p in procs:  # a rank that failed must not leave its peer waiting
+            if p.poll() is None:
+                p.kill()
+                p.wait()
     assert sorted(o["rank"] for o in outs) == [0, 1]
     for o in outs:
         assert o["ws"] == 2
